@@ -1,0 +1,128 @@
+"""GB300-native Schwarzschild ray tracer: the per-pixel march of DeepjotG/BlackHoleRender.
+
+Python face of the C ABI in include/bhr.h (libbhr.so, built in-tree for sm_103a). Device
+buffers and streams come from PyTorch; the work runs in the library's CUDA kernels. There is
+no CPU fallback: on a machine without the library or a GB300 the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import (  # noqa: F401
+    DISK_NONE, DISK_THIN, DISK_VOLUMETRIC, FLAG_FALLBACK, FLAG_FP64, FLAG_NONFINITE, FLAG_SURROGATE,
+    HIT_DTYPE, METHOD_PLAIN, METHOD_SURROGATE, PREC_FP32, PREC_MIXED, SQRT27, STATUS_BUDGET,
+    STATUS_CAPTURED, STATUS_ESCAPED, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, Options, Stats, View,
+)
+
+HIT_BYTES = 64
+
+
+def make_view(term_mode: int = TERM_SHADER, *, width: int | None = None, height: int | None = None,
+              fov_deg: float | None = None, preset: int | None = None, pose=None, look_at=None,
+              **fields) -> View:
+    """A view with the reference defaults (bhr_view_init), then the given overrides.
+
+    pose=(r, inclination_rad, azimuth_rad) places the camera on a sphere looking at the hole;
+    look_at=(pos, target) uses Camera::lookAt semantics. Other keyword arguments set fields.
+    """
+    L = _abi.lib()
+    v = View()
+    _abi.check(L.bhr_view_init(ctypes.byref(v), term_mode))
+    if preset is not None:
+        _abi.check(L.bhr_view_apply_preset(ctypes.byref(v), preset))
+    if width is not None:
+        v.width = width
+    if height is not None:
+        v.height = height
+    if fov_deg is not None:
+        _abi.check(L.bhr_view_set_fov(ctypes.byref(v), ctypes.c_float(fov_deg)))
+    if pose is not None:
+        r, inc, az = pose
+        _abi.check(L.bhr_view_orbit_pose(ctypes.byref(v), float(r), float(inc), float(az)))
+    if look_at is not None:
+        pos, tgt = look_at
+        P = (ctypes.c_double * 3)(*map(float, pos))
+        T = (ctypes.c_double * 3)(*map(float, tgt))
+        _abi.check(L.bhr_view_look_at(ctypes.byref(v), P, T))
+    for k, val in fields.items():
+        if not hasattr(v, k):
+            raise AttributeError(f"bhr_view has no field {k!r}")
+        setattr(v, k, val)
+    return v
+
+
+def hits_numpy(buf) -> np.ndarray:
+    """Structured numpy view (HIT_DTYPE) of a host uint8 buffer or CPU tensor of records."""
+    arr = buf.numpy() if hasattr(buf, "numpy") else np.asarray(buf)
+    return arr.view(np.uint8).reshape(-1).view(HIT_DTYPE)
+
+
+class Tracer:
+    """A bhr context on one CUDA device (bhr_create / bhr_trace / bhr_destroy)."""
+
+    def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, chunk: int = 0,
+                 refill: int = 0):
+        L = _abi.lib()
+        self._ctx = ctypes.c_void_p()
+        opts = Options(device, block_size, blocks_per_sm, chunk, refill)
+        _abi.check(L.bhr_create(ctypes.byref(self._ctx), ctypes.byref(opts)))
+        self.device = device
+
+    def close(self) -> None:
+        if self._ctx:
+            _abi.lib().bhr_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def trace_ptrs(self, views: Sequence[View], out_ptrs: Sequence[int], precision: int = PREC_FP32,
+                   method: int = METHOD_PLAIN, stream: int = 0) -> None:
+        """bhr_trace on raw device pointers (one per view) and a raw cudaStream_t."""
+        n = len(views)
+        arr = (View * n)(*views)
+        ptrs = (ctypes.c_void_p * n)(*out_ptrs)
+        _abi.check(_abi.lib().bhr_trace(self._ctx, arr, n, ptrs, precision, method, ctypes.c_void_p(stream)),
+                   self._ctx)
+
+    def trace(self, views: Sequence[View] | View, outs=None, precision: int = PREC_FP32,
+              method: int = METHOD_PLAIN, stream=None):
+        """Traces views into device tensors (uint8, rays*64 bytes each; allocated if None).
+
+        Runs on `stream` (a torch.cuda.Stream; default: the current stream) and returns the
+        list of output tensors without synchronising.
+        """
+        import torch
+
+        if isinstance(views, View):
+            views = [views]
+        dev = torch.device("cuda", self.device)
+        if outs is None:
+            outs = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        self.trace_ptrs(views, [o.data_ptr() for o in outs], precision, method, stream.cuda_stream)
+        return outs
+
+    def stats(self) -> Stats:
+        s = Stats()
+        _abi.check(_abi.lib().bhr_trace_stats(self._ctx, ctypes.byref(s)), self._ctx)
+        return s
+
+    def view_times_ms(self, nviews: int) -> np.ndarray:
+        out = (ctypes.c_double * nviews)()
+        _abi.check(_abi.lib().bhr_trace_view_times(self._ctx, out, nviews), self._ctx)
+        return np.array(out[:], dtype=np.float64)

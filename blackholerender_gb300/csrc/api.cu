@@ -1,0 +1,483 @@
+// Host side of the C ABI (include/bhr.h): context, argument checks, the Settings / Camera /
+// setTraceUniforms mirror, and the launch sequence of a trace.
+//
+// Host float arithmetic here is built with -ffp-contract=off so the per-view constants match
+// the reference's own float computation on both x86-64 and aarch64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bhr.h"
+#include "kernels.cuh"
+
+struct bhr_ctx {
+    int device = 0;
+    int sms = 0;
+    bhr::LaunchCfg cfg_one{256, 0, 256, 4};
+    bhr::LaunchCfg cfg_multi{256, 0, 256, 4};
+    bhr::WorkQueue* q = nullptr;  // one per batch slot
+    int nq = 0;
+    int2* band = nullptr;
+    bhr::PromoEntry* promo = nullptr;
+    int64_t scratch_rays = 0;  // capacity of band / promo in rays
+    cudaStream_t last_stream = nullptr;
+    int last_batches = 0;
+    int last_nviews = 0;
+    bool have_last = false;
+    std::string err;
+};
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_err;  // last error without a context
+
+int fail(bhr_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(bhr_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, BHR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool finite3f(const float* a) { return std::isfinite(a[0]) && std::isfinite(a[1]) && std::isfinite(a[2]); }
+
+// blackhole.frag:89: rEscMin = max(uDiskOuter * 1.25, 12.0)
+float shader_r_esc_min(float disk_outer) { return std::max(disk_outer * 1.25f, 12.0f); }
+
+int check_view(bhr_ctx* c, const bhr_view& v, int k) {
+    char buf[160];
+    auto bad = [&](const char* what) {
+        std::snprintf(buf, sizeof buf, "view %d: %s", k, what);
+        return fail(c, BHR_ERR_INVALID_ARG, buf);
+    };
+    if (v.width <= 0 || v.height <= 0) return bad("width and height must be positive");
+    if (int64_t(v.width) * v.height > int64_t(INT32_MAX)) return bad("width * height exceeds 2^31 - 1 rays");
+    if (v.max_steps < 0) return bad("max_steps must be >= 0");
+    if (v.disk_mode == BHR_DISK_VOLUMETRIC)
+        return fail(c, BHR_ERR_UNSUPPORTED, "view " + std::to_string(k) + ": volumetric disk is not supported");
+    if (v.disk_mode != BHR_DISK_NONE && v.disk_mode != BHR_DISK_THIN) return bad("unknown disk_mode");
+    if (v.term_mode < BHR_TERM_SHADER || v.term_mode > BHR_TERM_CPU) return bad("unknown term_mode");
+    if (!finite3f(v.cam_pos)) return bad("camera position is not finite");
+    for (float e : v.cam_basis)
+        if (!std::isfinite(e)) return bad("camera basis is not finite");
+    if (!(v.tan_half_fov > 0.0f) || !std::isfinite(v.tan_half_fov)) return bad("tan_half_fov must be positive");
+    if (!(v.step_scale > 0.0f) || !(v.ds_floor >= 0.0f)) return bad("step_scale must be > 0 and ds_floor >= 0");
+    const float rc = std::sqrt(v.cam_pos[0] * v.cam_pos[0] + v.cam_pos[1] * v.cam_pos[1] + v.cam_pos[2] * v.cam_pos[2]);
+    if (!(rc > 0.0f)) return bad("camera at the origin");
+    return BHR_OK;
+}
+
+// setTraceUniforms (Renderer.cpp:242-356) + the per-ray constants of blackhole.frag:77-89 that
+// depend only on the view, in float with the reference's operation order.
+bhr::DevView make_dev_view(const bhr_view& v, bhr_hit* out) {
+    bhr::DevView d{};
+    for (int k = 0; k < 3; ++k) d.cam[k] = v.cam_pos[k];
+    for (int k = 0; k < 9; ++k) d.basis[k] = v.cam_basis[k];
+    d.tan_half = v.tan_half_fov;
+    d.jitter[0] = v.jitter[0];
+    d.jitter[1] = v.jitter[1];
+    d.width = v.width;
+    d.height = v.height;
+    d.max_steps = v.max_steps;
+    d.aspect = float(v.width) / float(v.height);
+    const float* p = v.cam_pos;
+    d.rcam = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    for (int k = 0; k < 3; ++k) d.rhat[k] = p[k] / d.rcam;
+    d.lapse = std::sqrt(std::max(1.0f - 2.0f / d.rcam, 0.0f));
+    d.baxis_scale = 1.0f / std::sqrt(std::max(1.0f - 2.0f / d.rcam, 1e-6f));
+    d.step_scale = v.step_scale;
+    d.disk_step = v.disk_step;
+    d.disk_inner = v.disk_inner;
+    d.disk_outer = v.disk_outer;
+    d.slab = 2.5f * v.disk_thickness;
+    const float lo = v.disk_inner - 1.0f, hi = v.disk_outer + 1.0f;
+    d.rcyl_lo2 = lo > 0.0f ? lo * lo : -1.0f;
+    d.rcyl_hi2 = hi > 0.0f ? hi * hi : -1.0f;
+    d.capture_r = v.capture_r;
+    d.escape_r = v.escape_r;
+    d.esc_tol = v.esc_tol;
+    d.r_esc_min = v.term_mode == BHR_TERM_SHADER ? shader_r_esc_min(v.disk_outer) : v.r_esc_min;
+    d.ds_floor = v.ds_floor;
+    d.promote_band = v.promote_band;
+    d.promote_r = v.promote_r;
+    d.disk_mode = v.disk_mode;
+    d.lensing = (v.lensing != 0 && v.far_mode == 0) ? 1 : 0;
+    d.far_mode = v.far_mode != 0 ? 1 : 0;
+    d.term_mode = v.term_mode;
+    for (int k = 0; k < 3; ++k) d.cam_d[k] = double(v.cam_pos[k]);
+    d.chunk_start = 0;
+    d.nrays = int64_t(v.width) * v.height;
+    d.out = out;
+    return d;
+}
+
+int ensure_scratch(bhr_ctx* c, int nbatches, int64_t rays, bool mixed) {
+    if (nbatches > c->nq) {
+        if (c->q) cudaFree(c->q);
+        c->q = nullptr;
+        c->nq = 0;
+        cudaError_t e = cudaMalloc(&c->q, sizeof(bhr::WorkQueue) * size_t(nbatches));
+        if (e != cudaSuccess) return fail(c, BHR_ERR_OOM, std::string("work queue: ") + cudaGetErrorString(e));
+        c->nq = nbatches;
+    }
+    if (mixed && rays > c->scratch_rays) {
+        if (c->band) cudaFree(c->band);
+        if (c->promo) cudaFree(c->promo);
+        c->band = nullptr;
+        c->promo = nullptr;
+        c->scratch_rays = 0;
+        cudaError_t e = cudaMalloc(&c->band, sizeof(int2) * size_t(rays));
+        if (e == cudaSuccess) e = cudaMalloc(&c->promo, sizeof(bhr::PromoEntry) * size_t(rays));
+        if (e != cudaSuccess) return fail(c, BHR_ERR_OOM, std::string("FP64 queue: ") + cudaGetErrorString(e));
+        c->scratch_rays = rays;
+    }
+    return BHR_OK;
+}
+
+bhr::LaunchCfg finish_cfg(const bhr_ctx* c, bhr::LaunchCfg cfg, bool multi, bool mixed, int bps_override) {
+    int bps = bps_override > 0 ? bps_override : bhr::march_blocks_per_sm(cfg.block, multi, mixed);
+    bps = std::max(1, std::min(bps, bhr::march_blocks_per_sm(cfg.block, multi, mixed)));
+    cfg.grid = c->sms * bps;
+    cfg.refill = std::max(1, std::min(cfg.refill, 32));
+    cfg.chunk = std::max(32, cfg.chunk);
+    return cfg;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bhr_abi_version(void) { return BHR_ABI_VERSION; }
+
+const char* bhr_last_error(const bhr_ctx* ctx) {
+    if (ctx) return ctx->err.c_str();
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    return g_err.c_str();
+}
+
+int bhr_create(bhr_ctx** out, const bhr_options* opts) {
+    if (!out) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_create: ctx pointer is NULL");
+    *out = nullptr;
+    bhr_ctx* c = new (std::nothrow) bhr_ctx();
+    if (!c) return fail(nullptr, BHR_ERR_OOM, "bhr_create: out of host memory");
+    c->device = opts ? opts->device : 0;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        delete c;
+        return fail(nullptr, BHR_ERR_CUDA, std::string("bhr_create: no CUDA device: ") + cudaGetErrorString(e));
+    }
+    if (c->device < 0 || c->device >= ndev) {
+        delete c;
+        return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_create: device ordinal out of range");
+    }
+    cudaDeviceProp prop{};
+    e = cudaGetDeviceProperties(&prop, c->device);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(nullptr, e, "bhr_create: cudaGetDeviceProperties");
+    }
+    if (prop.major * 10 + prop.minor != 103) {
+        delete c;
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "bhr_create: device %d is sm_%d%d; this library is built for sm_103a only",
+                      c->device, prop.major, prop.minor);
+        return fail(nullptr, BHR_ERR_UNSUPPORTED, buf);
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    c->sms = prop.multiProcessorCount;
+    int bps_one = 0, bps_multi = 0;
+    if (opts) {
+        if (opts->block_size == 128 || opts->block_size == 256 || opts->block_size == 512) {
+            c->cfg_one.block = opts->block_size;
+            c->cfg_multi.block = opts->block_size;
+        } else if (opts->block_size != 0) {
+            cudaSetDevice(prev);
+            delete c;
+            return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_create: block_size must be 0, 128, 256 or 512");
+        }
+        if (opts->chunk > 0) c->cfg_one.chunk = c->cfg_multi.chunk = opts->chunk;
+        if (opts->refill > 0) c->cfg_one.refill = c->cfg_multi.refill = opts->refill;
+        bps_one = bps_multi = opts->blocks_per_sm;
+    }
+    c->cfg_one = finish_cfg(c, c->cfg_one, false, false, bps_one);
+    c->cfg_multi = finish_cfg(c, c->cfg_multi, true, false, bps_multi);
+    const int rc = ensure_scratch(c, 1, 0, false);
+    cudaSetDevice(prev);
+    if (rc != BHR_OK) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return BHR_OK;
+}
+
+int bhr_destroy(bhr_ctx* c) {
+    if (!c) return BHR_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    if (c->q) cudaFree(c->q);
+    if (c->band) cudaFree(c->band);
+    if (c->promo) cudaFree(c->promo);
+    cudaSetDevice(prev);
+    delete c;
+    return BHR_OK;
+}
+
+int bhr_view_init(bhr_view* v, int term_mode) {
+    if (!v) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_init: view is NULL");
+    if (term_mode < BHR_TERM_SHADER || term_mode > BHR_TERM_CPU)
+        return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_init: unknown term_mode");
+    std::memset(v, 0, sizeof *v);
+    // Settings defaults (Settings.h:19-37,82); the disk mode is thin (volumetric is out of scope)
+    v->width = 1920;
+    v->height = 1080;
+    v->max_steps = 450;
+    v->step_scale = 0.05f;
+    v->disk_step = 0.18f;
+    v->disk_inner = 6.0f;
+    v->disk_outer = 20.0f;
+    v->disk_thickness = 0.035f;
+    v->disk_mode = BHR_DISK_THIN;
+    v->lensing = 1;
+    v->far_mode = 0;
+    v->term_mode = term_mode;
+    bhr_view_set_fov(v, 60.0f);
+    // default pose: the "Interstellar shot" bookmark (Camera.cpp:54-55)
+    const double pos[3] = {0.0, 2.6, 24.9}, tgt[3] = {0.0, 0.0, 0.0};
+    bhr_view_look_at(v, pos, tgt);
+    v->escape_r = 1000.0f;
+    v->promote_band = 1e-2f;
+    v->promote_r = 2.5f;
+    switch (term_mode) {
+        case BHR_TERM_SHADER:  // R_HORIZON + 0.02 (blackhole.frag:144), ESC_TOL (geodesic.glsl:8)
+            v->capture_r = 2.0f + 0.02f;
+            v->esc_tol = 0.01f;
+            v->r_esc_min = shader_r_esc_min(v->disk_outer);
+            v->ds_floor = 0.02f;
+            break;
+        case BHR_TERM_CONFIG:
+            v->capture_r = 2.0001f;
+            v->esc_tol = 0.01f;
+            v->r_esc_min = shader_r_esc_min(v->disk_outer);
+            v->ds_floor = 0.02f;
+            break;
+        case BHR_TERM_CPU:  // trace() defaults (Geodesic.h:107-108,119)
+            v->max_steps = 200000;
+            v->step_scale = 0.005f;
+            v->capture_r = 2.01f;
+            v->esc_tol = 1e-4f;
+            v->r_esc_min = 30.0f;
+            v->ds_floor = 1e-4f;
+            v->disk_mode = BHR_DISK_NONE;
+            break;
+    }
+    return BHR_OK;
+}
+
+int bhr_view_apply_preset(bhr_view* v, int preset) {
+    if (!v) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_apply_preset: view is NULL");
+    switch (preset) {  // Settings::applyPreset (Settings.cpp:12-35)
+        case 0: v->max_steps = 200; v->step_scale = 0.10f; v->disk_step = 0.35f; break;
+        case 1: v->max_steps = 300; v->step_scale = 0.07f; v->disk_step = 0.30f; break;
+        case 2: v->max_steps = 450; v->step_scale = 0.05f; v->disk_step = 0.18f; break;
+        case 3: v->max_steps = 700; v->step_scale = 0.035f; v->disk_step = 0.10f; break;
+        default: return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_apply_preset: preset must be 0..3");
+    }
+    return BHR_OK;
+}
+
+int bhr_view_set_fov(bhr_view* v, float fov_deg) {
+    if (!v || !(fov_deg > 0.0f) || !(fov_deg < 180.0f))
+        return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_set_fov: fov must be in (0, 180) degrees");
+    // Renderer.cpp:246: std::tan(glm::radians(s.fovDeg) * 0.5f)
+    const float rad = fov_deg * 0.01745329251994329576923690768489f;
+    v->tan_half_fov = std::tan(rad * 0.5f);
+    return BHR_OK;
+}
+
+int bhr_view_look_at(bhr_view* v, const double pos[3], const double target[3]) {
+    if (!v || !pos || !target) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_look_at: NULL argument");
+    // Camera.cpp:12-23 lookRotation(from, target, up = (0,1,0)), then basis() = mat3_cast(quat)
+    const double fd[3] = {target[0] - pos[0], target[1] - pos[1], target[2] - pos[2]};
+    const double len = std::sqrt(fd[0] * fd[0] + fd[1] * fd[1] + fd[2] * fd[2]);
+    float f[3] = {0.0f, 0.0f, -1.0f};
+    if (len > 0.0)
+        for (int k = 0; k < 3; ++k) f[k] = float(fd[k] / len);
+    float u[3] = {0.0f, 1.0f, 0.0f};
+    if (std::fabs(f[0] * u[0] + f[1] * u[1] + f[2] * u[2]) > 0.999f) {
+        u[0] = 0.0f; u[1] = 0.0f; u[2] = -1.0f;
+    }
+    float r[3] = {f[1] * u[2] - u[1] * f[2], f[2] * u[0] - u[2] * f[0], f[0] * u[1] - u[0] * f[1]};
+    const float rl = 1.0f / std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    for (float& e : r) e *= rl;
+    const float uu[3] = {r[1] * f[2] - f[1] * r[2], r[2] * f[0] - f[2] * r[0], r[0] * f[1] - f[0] * r[1]};
+    // m = mat3(r, uu, -f): column-major m[col][row]
+    const float m[3][3] = {{r[0], r[1], r[2]}, {uu[0], uu[1], uu[2]}, {-f[0], -f[1], -f[2]}};
+    // rotation matrix -> unit quaternion by the largest-component method (Shepperd 1978)
+    const float t[4] = {m[0][0] + m[1][1] + m[2][2], m[0][0] - m[1][1] - m[2][2], m[1][1] - m[0][0] - m[2][2],
+                        m[2][2] - m[0][0] - m[1][1]};
+    int big = 0;
+    for (int k = 1; k < 4; ++k)
+        if (t[k] > t[big]) big = k;
+    const float bv = std::sqrt(t[big] + 1.0f) * 0.5f;
+    const float mult = 0.25f / bv;
+    float qw, qx, qy, qz;
+    switch (big) {
+        case 0: qw = bv; qx = (m[1][2] - m[2][1]) * mult; qy = (m[2][0] - m[0][2]) * mult; qz = (m[0][1] - m[1][0]) * mult; break;
+        case 1: qw = (m[1][2] - m[2][1]) * mult; qx = bv; qy = (m[0][1] + m[1][0]) * mult; qz = (m[2][0] + m[0][2]) * mult; break;
+        case 2: qw = (m[2][0] - m[0][2]) * mult; qx = (m[0][1] + m[1][0]) * mult; qy = bv; qz = (m[1][2] + m[2][1]) * mult; break;
+        default: qw = (m[0][1] - m[1][0]) * mult; qx = (m[2][0] + m[0][2]) * mult; qy = (m[1][2] + m[2][1]) * mult; qz = bv; break;
+    }
+    const float qn = 1.0f / std::sqrt(qw * qw + qx * qx + qy * qy + qz * qz);
+    qw *= qn; qx *= qn; qy *= qn; qz *= qn;
+    // quaternion -> rotation matrix (columns right, up, back)
+    const float xx = qx * qx, yy = qy * qy, zz = qz * qz, xz = qx * qz, xy = qx * qy, yz = qy * qz;
+    const float wx = qw * qx, wy = qw * qy, wz = qw * qz;
+    float* B = v->cam_basis;
+    B[0] = 1.0f - 2.0f * (yy + zz); B[1] = 2.0f * (xy + wz);        B[2] = 2.0f * (xz - wy);
+    B[3] = 2.0f * (xy - wz);        B[4] = 1.0f - 2.0f * (xx + zz); B[5] = 2.0f * (yz + wx);
+    B[6] = 2.0f * (xz + wy);        B[7] = 2.0f * (yz - wx);        B[8] = 1.0f - 2.0f * (xx + yy);
+    // uCamPos = vec3(Camera::position())
+    for (int k = 0; k < 3; ++k) v->cam_pos[k] = float(pos[k]);
+    return BHR_OK;
+}
+
+int bhr_view_orbit_pose(bhr_view* v, double r, double incl, double azim) {
+    if (!v || !(r > 0.0)) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_orbit_pose: bad argument");
+    const double pos[3] = {r * std::sin(incl) * std::sin(azim), r * std::cos(incl), r * std::sin(incl) * std::cos(azim)};
+    const double tgt[3] = {0.0, 0.0, 0.0};
+    return bhr_view_look_at(v, pos, tgt);
+}
+
+int64_t bhr_view_rays(const bhr_view* v) {
+    if (!v || v->width <= 0 || v->height <= 0) return 0;
+    return int64_t(v->width) * v->height;
+}
+
+int bhr_trace(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out_dev, int precision, int method,
+              void* cuda_stream) {
+    if (!c) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_trace: ctx is NULL");
+    if (!views || nviews <= 0 || !out_dev) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: no views or outputs");
+    if (precision != BHR_PREC_FP32 && precision != BHR_PREC_MIXED)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: unknown precision");
+    if (method != BHR_METHOD_PLAIN && method != BHR_METHOD_SURROGATE)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: unknown method");
+    if (method == BHR_METHOD_SURROGATE)
+        return fail(c, BHR_ERR_NOT_READY, "bhr_trace: the surrogate runs through bhr_surrogate_trace");
+    int64_t rays = 0;
+    for (int k = 0; k < nviews; ++k) {
+        const int rc = check_view(c, views[k], k);
+        if (rc != BHR_OK) return rc;
+        if (!out_dev[k]) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: output buffer " + std::to_string(k) + " is NULL");
+        if (reinterpret_cast<uintptr_t>(out_dev[k]) % 16 != 0)
+            return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: output buffers must be 16-byte aligned");
+        rays += int64_t(views[k].width) * views[k].height;
+    }
+    const bool mixed = precision == BHR_PREC_MIXED;
+    const int nb = nviews == 1 ? 1 : (nviews + bhr::kMaxViews - 1) / bhr::kMaxViews;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    int rc = ensure_scratch(c, nb, rays, mixed);
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    const int fp64_grid = c->sms * 8;
+    for (int bi = 0; rc == BHR_OK && bi < nb; ++bi) {
+        bhr::Scratch sc{c->q + bi, c->band, c->promo};
+        cudaError_t e = cudaMemsetAsync(sc.q, 0, sizeof(bhr::WorkQueue), st);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(c, e, "bhr_trace: cudaMemsetAsync");
+            break;
+        }
+        if (nviews == 1) {
+            const bhr::DevView dv = make_dev_view(views[0], out_dev[0]);
+            bhr::LaunchCfg cfg = c->cfg_one;
+            if (mixed) cfg = finish_cfg(c, cfg, false, true, cfg.grid / c->sms);
+            e = bhr::launch_march_one(dv, sc, mixed, cfg, st);
+            if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_one(dv, sc, fp64_grid, st);
+        } else {
+            static thread_local bhr::ViewBatch b;  // 14 KB; passed by value as a kernel parameter
+            const int v0 = bi * bhr::kMaxViews;
+            b.nviews = std::min(bhr::kMaxViews, nviews - v0);
+            int64_t chunk_acc = 0;
+            bhr::LaunchCfg cfg = c->cfg_multi;
+            if (mixed) cfg = finish_cfg(c, cfg, true, true, cfg.grid / c->sms);
+            for (int k = 0; k < b.nviews; ++k) {
+                b.views[k] = make_dev_view(views[v0 + k], out_dev[v0 + k]);
+                b.views[k].chunk_start = chunk_acc;
+                chunk_acc += (b.views[k].nrays + cfg.chunk - 1) / cfg.chunk;
+            }
+            b.total_chunks = chunk_acc;
+            e = bhr::launch_march_multi(b, sc, mixed, cfg, st);
+            if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_multi(b, sc, fp64_grid, st);
+        }
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace: kernel launch");
+    }
+    if (rc == BHR_OK) {
+        c->last_stream = st;
+        c->last_batches = nb;
+        c->last_nviews = nviews;
+        c->have_last = true;
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int bhr_trace_stats(bhr_ctx* c, bhr_stats* s) {
+    if (!c || !s) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_stats: NULL argument");
+    std::memset(s, 0, sizeof *s);
+    if (!c->have_last) return fail(c, BHR_ERR_NOT_READY, "bhr_trace_stats: no trace on this context yet");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->last_stream);
+    std::vector<bhr::WorkQueue> qs(size_t(c->last_batches));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(qs.data(), c->q, sizeof(bhr::WorkQueue) * qs.size(), cudaMemcpyDeviceToHost);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bhr_trace_stats");
+    for (const auto& q : qs) {
+        s->steps += q.steps;
+        s->fp64_rays += q.fp64_rays;
+        s->fp64_steps += q.fp64_steps;
+        s->nonfinite += q.nonfinite;
+    }
+    return BHR_OK;
+}
+
+int bhr_trace_view_times(bhr_ctx* c, double* ms, int nviews) {
+    if (!c || !ms || nviews <= 0) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_view_times: bad argument");
+    if (!c->have_last || c->last_nviews != nviews || nviews == 1)
+        return fail(c, BHR_ERR_NOT_READY, "bhr_trace_view_times: needs the last trace to be a multi-view trace");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->last_stream);
+    std::vector<bhr::WorkQueue> qs(size_t(c->last_batches));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(qs.data(), c->q, sizeof(bhr::WorkQueue) * qs.size(), cudaMemcpyDeviceToHost);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bhr_trace_view_times");
+    for (int k = 0; k < nviews; ++k) {
+        const bhr::WorkQueue& q = qs[size_t(k / bhr::kMaxViews)];
+        const int s = k % bhr::kMaxViews;
+        ms[k] = q.view_t_end[s] >= q.t_start ? double(q.view_t_end[s] - q.t_start) * 1e-6 : -1.0;
+    }
+    return BHR_OK;
+}
+
+}  // extern "C"

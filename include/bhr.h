@@ -1,0 +1,190 @@
+/*
+ * bhr.h - C ABI of the GB300 Schwarzschild ray tracer.
+ *
+ * This is the drop-in boundary for the per-pixel march of the reference renderer
+ * (DeepjotG/BlackHoleRender). The reference drives that march as a GLSL program:
+ *   Renderer::tracePass        src/Renderer.cpp:369-387   (one full-screen draw)
+ *   Renderer::setTraceUniforms src/Renderer.cpp:242-356   (the uniforms below)
+ *   blackhole.frag main()      shaders/blackhole.frag:67-253 (ray gen + march loop)
+ * The reference has no FFI of its own; this header splits blackhole.frag at the end of
+ * its march loop and returns, per pixel, the state the shading after the loop reads
+ * (status, escape direction, disk-plane crossings, bAxis).
+ *
+ * Conventions (all entry points):
+ *   - return BHR_OK (0) or a negative BHR_ERR_* code; no C++ exception crosses the ABI;
+ *     bhr_last_error() gives the message of the last failure on a context.
+ *   - GPU calls are stream-ordered and asynchronous on the caller's cudaStream_t
+ *     (passed as void*, NULL = legacy default stream); the caller synchronises.
+ *   - a context is not thread-safe: one context per host thread.
+ *   - output buffers are owned by the caller (device memory for bhr_trace*).
+ *   - frame: black hole at the origin, +Y = disk normal (src/Units.h:5-7), units G=c=M=1.
+ *   - hit records are row-major, row 0 = bottom row (gl_FragCoord convention).
+ */
+#ifndef BHR_H
+#define BHR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BHR_ABI_VERSION 1
+
+/* ---- return codes ---------------------------------------------------------------- */
+#define BHR_OK 0
+#define BHR_ERR_INVALID_ARG (-1)
+#define BHR_ERR_OOM (-2)
+#define BHR_ERR_CUDA (-3)
+#define BHR_ERR_TIMEOUT (-4)      /* a bounded device-side wait ran out */
+#define BHR_ERR_UNSUPPORTED (-5)  /* e.g. DISK_VOLUMETRIC, no sm_103 device */
+#define BHR_ERR_NOT_READY (-6)    /* surrogate used before it was trained or loaded */
+#define BHR_ERR_IO (-7)
+
+/* ---- hit status (low bits of bhr_hit.status) -------------------------------------- */
+#define BHR_STATUS_ESCAPED 1   /* blackhole.frag status 1 */
+#define BHR_STATUS_CAPTURED 2  /* blackhole.frag status 2 (horizon test) */
+#define BHR_STATUS_BUDGET 3    /* step budget ran out; blackhole.frag:252 shades it as captured */
+
+/* ---- bhr_hit.flags ----------------------------------------------------------------- */
+#define BHR_FLAG_FP64 0x01       /* some or all of the march ran in FP64 (mixed precision) */
+#define BHR_FLAG_SURROGATE 0x02  /* record produced by the learned orbit surrogate */
+#define BHR_FLAG_FALLBACK 0x04   /* surrogate declined the ray; the integrator produced it */
+#define BHR_FLAG_NONFINITE 0x08  /* a non-finite state was met (blackhole.frag:367 NaN view) */
+
+/* ---- disk modes (src/Settings.h:7, shaders/common.glsl:12-14) ---------------------- */
+#define BHR_DISK_NONE 0
+#define BHR_DISK_THIN 1
+#define BHR_DISK_VOLUMETRIC 2 /* rejected with BHR_ERR_UNSUPPORTED */
+
+/* ---- termination rules ------------------------------------------------------------- */
+/* SHADER: blackhole.frag:144,151-155 - capture r < 2.02, tolerance escape
+ *         0.75 b^3/r^4 < esc_tol once outgoing beyond r_esc_min = max(1.25 r_out, 12),
+ *         steps ds = max(step_scale * r * farMul, 0.02) plus the disk-slab clamp.
+ * CONFIG: same step rule; capture r < capture_r (2.0001), escape once outgoing with
+ *         r > escape_r (1000); farFieldDirection is still applied at the exit.
+ * CPU:    src/physics/Geodesic.h:107-140 trace() - capture r < 2.01, tolerance escape with
+ *         esc_tol / r_esc_min, ds = max(step_scale * r, 1e-4), no farMul, no slab clamp. */
+#define BHR_TERM_SHADER 0
+#define BHR_TERM_CONFIG 1
+#define BHR_TERM_CPU 2
+
+/* ---- precision / method selectors for bhr_trace ------------------------------------- */
+#define BHR_PREC_FP32 0   /* plain FP32 march */
+#define BHR_PREC_MIXED 1  /* FP32 bulk, FP64 for the photon-sphere band and r < promote_r */
+#define BHR_METHOD_PLAIN 0
+#define BHR_METHOD_SURROGATE 1
+
+/* One camera view: the tracer uniforms of blackhole.frag:27-37 and disk.glsl:8-10, plus the
+ * termination rule. bhr_view_init() fills the reference defaults. 160 bytes. */
+typedef struct bhr_view {
+    float cam_pos[3];      /* uCamPos = vec3(Camera::position())             Renderer.cpp:249 */
+    float cam_basis[9];    /* uCamBasis, column-major, columns right, up, back Renderer.cpp:250 */
+    float tan_half_fov;    /* uTanHalfFov = tan(radians(fovDeg) * 0.5f)       Renderer.cpp:246 */
+    float jitter[2];       /* uJitter (pixels), 0 for parity                   Renderer.cpp:248 */
+    int32_t width;         /* uResolution.x */
+    int32_t height;        /* uResolution.y */
+    int32_t max_steps;     /* uMaxSteps                                         Renderer.cpp:314 */
+    float step_scale;      /* uStepScale */
+    float disk_step;       /* uDiskStep */
+    float disk_inner;      /* uDiskInner */
+    float disk_outer;      /* uDiskOuter */
+    float disk_thickness;  /* uDiskThickness (H/r) */
+    int32_t disk_mode;     /* uDiskMode: BHR_DISK_* */
+    int32_t lensing;       /* uLensing */
+    int32_t far_mode;      /* uFarMode (camera radius > 1e7, App.cpp:506) */
+    int32_t term_mode;     /* BHR_TERM_* */
+    float capture_r;       /* horizon test radius */
+    float escape_r;        /* CONFIG escape radius */
+    float esc_tol;         /* tolerance escape (ESC_TOL, geodesic.glsl:8) */
+    float r_esc_min;       /* CPU rule's rEscMin; SHADER derives max(1.25 disk_outer, 12) (frag:89) */
+    float ds_floor;        /* smallest step (0.02 shader, 1e-4 CPU mirror) */
+    float promote_band;    /* MIXED: |b - sqrt(27)| below this runs in FP64 (1e-2) */
+    float promote_r;       /* MIXED: march continues in FP64 once r < promote_r (2.5) */
+    int32_t reserved[6];
+} bhr_view;
+
+/* Per-pixel hit record: the march state blackhole.frag's shading reads after the loop
+ * (status/escDir :97-98, the crossing points handed to thinDiskSample :209-216, bAxis :88)
+ * plus the fields of the CPU mirror's TraceResult (Geodesic.h:97-103). 64 bytes, written
+ * as four 16-byte stores. */
+typedef struct bhr_hit {
+    uint8_t status;        /* BHR_STATUS_* */
+    uint8_t ncross;        /* crossings recorded below (r in [disk_inner, disk_outer]), 0..3 */
+    uint8_t flags;         /* BHR_FLAG_* */
+    uint8_t nplane;        /* all y = 0 plane crossings (TraceResult::equatorCrossings), saturating */
+    uint32_t steps;        /* march steps executed */
+    float dir[3];          /* escDir (unit) when status is ESCAPED, else zero (as TraceResult::dir) */
+    float b_axis;          /* impactParameterAboutAxis(camPos, dir, +Y) */
+    float b;               /* impact parameter h / |v| at the camera */
+    float min_r;           /* smallest r seen at the loop head (TraceResult::minR) */
+    float cross_r[3];      /* |hit.xz| of recorded crossings, march order (disk.glsl:114) */
+    float cross_phi[3];    /* atan(hit.z, hit.x) of recorded crossings (disk.glsl:116) */
+    float reserved[2];
+} bhr_hit;
+
+typedef struct bhr_ctx bhr_ctx;
+
+typedef struct bhr_options {
+    int32_t device;        /* CUDA device ordinal */
+    int32_t block_size;    /* 0 = autotuned / default */
+    int32_t blocks_per_sm; /* 0 = autotuned / default */
+    int32_t chunk;         /* rays a warp takes from the work queue at once, 0 = default */
+    int32_t refill;        /* idle lanes before a warp refills, 0 = default */
+    int32_t reserved[3];
+} bhr_options;
+
+/* Per-call statistics, filled by bhr_trace_stats after the stream work completed. */
+typedef struct bhr_stats {
+    uint64_t rays;           /* rays traced */
+    uint64_t steps;          /* sum of executed march steps */
+    uint64_t fp64_rays;      /* rays that ran (partly) in FP64 */
+    uint64_t fp64_steps;     /* steps taken in FP64 */
+    uint64_t surrogate_rays; /* rays answered by the surrogate */
+    uint64_t fallback_rays;  /* rays the surrogate sent to the integrator */
+    uint64_t nonfinite;      /* rays with a non-finite state */
+    uint64_t reserved;
+} bhr_stats;
+
+/* ---- context ----------------------------------------------------------------------- */
+int bhr_abi_version(void);
+int bhr_create(bhr_ctx** ctx, const bhr_options* opts); /* opts may be NULL */
+int bhr_destroy(bhr_ctx* ctx);
+const char* bhr_last_error(const bhr_ctx* ctx); /* ctx may be NULL: last global error */
+
+/* ---- host helpers mirroring Settings / Camera / setTraceUniforms --------------------- */
+/* Fills v with the reference defaults (Settings.h:19-37,82: High preset, thin disk [6,20],
+ * H/r 0.035, FOV 60) and the given termination rule's constants. */
+int bhr_view_init(bhr_view* v, int term_mode);
+/* Applies Settings::applyPreset's trace fields (Settings.cpp:12-35): preset 0..3 = Low..Ultra
+ * (max_steps, step_scale, disk_step; disk mode is left as it is). */
+int bhr_view_apply_preset(bhr_view* v, int preset);
+/* Camera pose from a position and a target, as Camera::lookAt / lookRotation
+ * (Camera.cpp:12-23,67): float basis through a unit quaternion, up (0,1,0) with the
+ * (0,0,-1) fallback when |dot(f, up)| > 0.999. Sets cam_pos and cam_basis. */
+int bhr_view_look_at(bhr_view* v, const double pos[3], const double target[3]);
+/* tan_half_fov from a vertical FOV in degrees, as Renderer.cpp:246 (float arithmetic). */
+int bhr_view_set_fov(bhr_view* v, float fov_deg);
+/* Pose on a sphere: pos = r (sin i sin a, cos i, sin i cos a), looking at the hole. */
+int bhr_view_orbit_pose(bhr_view* v, double r, double incl_rad, double azim_rad);
+/* Rays of a view (width * height). */
+int64_t bhr_view_rays(const bhr_view* v);
+
+/* ---- tracing ------------------------------------------------------------------------- */
+/* Traces nviews views. out_dev[k] is a caller-owned device buffer of width*height records
+ * for view k. precision: BHR_PREC_*; method: BHR_METHOD_*. One view runs the plain kernel
+ * with the view in constant memory; several views run one persistent launch over a
+ * shared work queue. Work memory (queue counters, FP64 hand-off queue) is owned by ctx. */
+int bhr_trace(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
+              int precision, int method, void* cuda_stream);
+/* Statistics of the last bhr_trace on ctx (synchronises that call's stream). */
+int bhr_trace_stats(bhr_ctx* ctx, bhr_stats* stats);
+/* Per-view latency of the last multi-view bhr_trace: milliseconds from the start of the
+ * launch to the moment the view's last ray finished (synchronises that call's stream). */
+int bhr_trace_view_times(bhr_ctx* ctx, double* ms, int nviews);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BHR_H */

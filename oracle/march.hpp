@@ -1,0 +1,286 @@
+// CPU restatement of the reference's per-pixel march -- TEST INFRASTRUCTURE ONLY.
+//
+// This is the oracle the CUDA kernels are checked against. It is never linked into the
+// product library (blackholerender_gb300/libbhr.so); only tests/, __graft_entry__.smoke()
+// and bench.py's CPU-baseline leg load it.
+//
+// It restates, line by line and templated on the arithmetic type T (double = the FP64 oracle,
+// float = the FP32 behaviour check):
+//   shaders/geodesic.glsl:10-53       geoAccel, rk4Step, initialVelocity,
+//                                     impactParameterAboutAxis, farFieldDirection
+//   shaders/common.glsl:7-14          R_HORIZON, B_CRIT, disk modes
+//   shaders/disk.glsl:24,113-116      slab half-height, crossing radius/azimuth + range test
+//   shaders/blackhole.frag:67-93      ray generation and per-ray constants
+//   shaders/blackhole.frag:138-216,252  march loop (variant BHS_BODIES 0, BHS_GAS 0, thin disk)
+//   src/physics/Geodesic.h:107-140    trace(), the CPU mirror's loop (BHR_TERM_CPU)
+// Vector formulas follow GLM/GLSL definitions (dot = (x+y)+z, normalize = v * (1/sqrt(dot)),
+// mix(a,b,t) = a*(1-t) + b*t) so the double path reproduces the reference's CPU code bit for
+// bit when built with -ffp-contract=off.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <limits>
+
+#include "bhr.h"
+
+namespace oracle {
+
+template <class T>
+struct V3 {
+    T x, y, z;
+};
+template <class T> inline V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> inline V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> inline V3<T> operator-(V3<T> a) { return {-a.x, -a.y, -a.z}; }
+template <class T> inline V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class T> inline V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class T> inline V3<T> operator/(V3<T> a, T s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class T> inline T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> inline T length(V3<T> a) { return std::sqrt(dot(a, a)); }
+template <class T> inline V3<T> normalize(V3<T> a) { return a * (T(1) / std::sqrt(dot(a, a))); }
+template <class T> inline V3<T> cross(V3<T> a, V3<T> b) {
+    return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+
+// geodesic.glsl:10-14 / Geodesic.h:21-25
+template <class T> inline V3<T> geoAccel(V3<T> x, T h2) {
+    const T r2 = dot(x, x);
+    const T r = std::sqrt(r2);
+    return x * (T(-3) * h2 / (r2 * r2 * r));
+}
+
+// geodesic.glsl:16-23 / Geodesic.h:27-34
+template <class T> inline void rk4Step(V3<T>& x, V3<T>& v, T h2, T dt) {
+    const T hdt = T(0.5) * dt;
+    const V3<T> k1v = geoAccel(x, h2), k1x = v;
+    const V3<T> k2v = geoAccel(x + hdt * k1x, h2), k2x = v + hdt * k1v;
+    const V3<T> k3v = geoAccel(x + hdt * k2x, h2), k3x = v + hdt * k2v;
+    const V3<T> k4v = geoAccel(x + dt * k3x, h2), k4x = v + dt * k3v;
+    const T s = dt / T(6);
+    x = x + s * (k1x + T(2) * k2x + T(2) * k3x + k4x);
+    v = v + s * (k1v + T(2) * k2v + T(2) * k3v + k4v);
+}
+
+// geodesic.glsl:27-34 / Geodesic.h:40-47
+template <class T> inline V3<T> initialVelocity(V3<T> camPos, V3<T> dir) {
+    const T r = length(camPos);
+    const V3<T> rhat = camPos / r;
+    const T nr = dot(dir, rhat);
+    const V3<T> nperp = dir - nr * rhat;
+    const T f = std::sqrt(std::max(T(1) - T(2) / r, T(0)));
+    return normalize(nr * f * rhat + nperp);
+}
+
+// geodesic.glsl:37-40 (shader form: inversesqrt(max(1 - 2/r, 1e-6)), axis = +Y)
+template <class T> inline T impactParameterAboutY(V3<T> camPos, V3<T> dir) {
+    const T r = length(camPos);
+    const V3<T> c = cross(camPos, dir);
+    return -c.y * (T(1) / std::sqrt(std::max(T(1) - T(2) / r, T(1e-6))));
+}
+
+// geodesic.glsl:43-53 / Geodesic.h:65-75
+template <class T> inline V3<T> farFieldDirection(V3<T> x, V3<T> v, T h2) {
+    const T vlen = length(v);
+    const V3<T> vh = v / vlen;
+    const T r = length(x);
+    const T p = dot(x, vh);
+    const V3<T> bvec = x - p * vh;
+    const T s = std::clamp(p / r, T(0), T(1));
+    const T r3 = r * r * r;
+    const V3<T> dv = -(h2 / vlen) * (vh / r3 + bvec * ((T(2) + s) / (r3 * r * (T(1) + s) * (T(1) + s))));
+    return normalize(v + dv);
+}
+
+// Termination and step rule constants of one view, in the arithmetic type T.
+template <class T>
+struct Rule {
+    int term_mode = BHR_TERM_SHADER;
+    int max_steps = 450;
+    int disk_mode = BHR_DISK_THIN;
+    bool lensing = true;
+    bool far_mode = false;
+    T step_scale = T(0.05), disk_step = T(0.18);
+    T disk_inner = T(6), disk_outer = T(20), disk_thickness = T(0.035);
+    T capture_r = T(2.02f), escape_r = T(1000), esc_tol = T(0.01f), r_esc_min = T(25), ds_floor = T(0.02f);
+
+    static Rule from_view(const bhr_view& w) {
+        Rule r;
+        r.term_mode = w.term_mode;
+        r.max_steps = w.max_steps;
+        r.disk_mode = w.disk_mode;
+        r.lensing = w.lensing != 0;
+        r.far_mode = w.far_mode != 0;
+        r.step_scale = T(w.step_scale);
+        r.disk_step = T(w.disk_step);
+        r.disk_inner = T(w.disk_inner);
+        r.disk_outer = T(w.disk_outer);
+        r.disk_thickness = T(w.disk_thickness);
+        r.capture_r = T(w.capture_r);
+        r.escape_r = T(w.escape_r);
+        r.esc_tol = T(w.esc_tol);
+        // blackhole.frag:89 derives rEscMin from uDiskOuter; the CPU mirror takes it as an argument
+        r.r_esc_min = w.term_mode == BHR_TERM_SHADER ? T(std::max(w.disk_outer * 1.25f, 12.0f)) : T(w.r_esc_min);
+        r.ds_floor = T(w.ds_floor);
+        return r;
+    }
+};
+
+template <class T>
+struct Result {
+    int status = 0;
+    int steps = 0;
+    int ncross = 0;
+    int nplane = 0;
+    bool nonfinite = false;
+    V3<T> dir{0, 0, 0};
+    T b = 0, b_axis = 0;
+    T min_r = std::numeric_limits<T>::infinity();
+    T cross_r[3] = {0, 0, 0};
+    T cross_phi[3] = {0, 0, 0};
+    V3<T> x{0, 0, 0}, v{0, 0, 0};  // final state (for tests)
+};
+
+// blackhole.frag:68-72: primary ray of pixel (i, j), row 0 at the bottom.
+template <class T> inline V3<T> primaryRay(const bhr_view& w, int i, int j) {
+    const T pxx = T(i) + T(0.5) + T(w.jitter[0]);
+    const T pxy = T(j) + T(0.5) + T(w.jitter[1]);
+    const T ndcx = pxx / T(w.width) * T(2) - T(1);
+    const T ndcy = pxy / T(w.height) * T(2) - T(1);
+    const T aspect = T(w.width) / T(w.height);
+    const T th = T(w.tan_half_fov);
+    const V3<T> dc = normalize(V3<T>{ndcx * th * aspect, ndcy * th, T(-1)});
+    const float* B = w.cam_basis;  // column-major
+    const V3<T> d{T(B[0]) * dc.x + T(B[3]) * dc.y + T(B[6]) * dc.z,
+                  T(B[1]) * dc.x + T(B[4]) * dc.y + T(B[7]) * dc.z,
+                  T(B[2]) * dc.x + T(B[5]) * dc.y + T(B[8]) * dc.z};
+    return normalize(d);
+}
+
+template <class T> inline bool finite3(V3<T> a) {
+    return std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(a.z);
+}
+
+// blackhole.frag:77-93 (setup) + :138-253 (march), or Geodesic.h:107-140 for BHR_TERM_CPU.
+template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {
+    Result<T> res;
+    const bool lensing = R.lensing && !R.far_mode;
+    V3<T> x = camPos;
+    V3<T> v = dir;
+    T h2 = 0, h = 0;
+    if (lensing) {
+        v = initialVelocity(camPos, dir);
+        const V3<T> hv = cross(x, v);
+        h2 = dot(hv, hv);
+        h = std::sqrt(h2);
+    }
+    res.b_axis = impactParameterAboutY(camPos, dir);
+    res.b = lensing ? h / length(v) : T(0);
+    const bool shader_rule = R.term_mode != BHR_TERM_CPU;
+    const T farMul = shader_rule ? std::clamp((h - T(6)) / T(3), T(1), T(3)) : T(1);
+    const T slab = T(2.5) * R.disk_thickness;  // diskSlabHalfHeight(r) = slab * r (disk.glsl:24)
+    int status = 0;
+    V3<T> escDir = dir;
+    int steps = 0;
+    if (R.far_mode) {
+        status = BHR_STATUS_ESCAPED;
+        escDir = dir;
+    } else {
+        for (int i = 0; i < R.max_steps; ++i) {
+            const T r = length(x);
+            res.min_r = std::min(res.min_r, r);
+            if (r < R.capture_r) {
+                status = BHR_STATUS_CAPTURED;
+                break;
+            }
+            const T vlen = length(v);
+            if (dot(x, v) > T(0)) {
+                bool esc = false;
+                if (R.term_mode == BHR_TERM_CONFIG) {
+                    esc = r > R.escape_r;
+                } else if (r > R.r_esc_min) {
+                    const T b = h / vlen;
+                    esc = !lensing || T(0.75) * b * b * b / (r * r * r * r) < R.esc_tol;
+                }
+                if (esc) {
+                    escDir = lensing ? farFieldDirection(x, v, h2) : normalize(v);
+                    status = BHR_STATUS_ESCAPED;
+                    break;
+                }
+            }
+            T ds;
+            if (shader_rule) {
+                ds = std::max(R.step_scale * r * farMul, R.ds_floor);
+                if (R.disk_mode != BHR_DISK_NONE) {
+                    const T rcyl = std::sqrt(x.x * x.x + x.z * x.z);
+                    if (rcyl > R.disk_inner - T(1) && rcyl < R.disk_outer + T(1)) {
+                        const T outside = std::fabs(x.y) - slab * rcyl;
+                        if (outside > T(0))
+                            ds = std::min(ds, std::max(R.disk_step, outside / (std::fabs(v.y) / vlen + slab)));
+                    }
+                }
+            } else {
+                ds = std::max(R.step_scale * r, R.ds_floor);
+            }
+            const T dt = ds / vlen;
+            const V3<T> x0 = x;
+            if (lensing)
+                rk4Step(x, v, h2, dt);
+            else
+                x = x + v * dt;
+            steps = i + 1;
+            if ((x.y > T(0)) != (x0.y > T(0))) {
+                if (res.nplane < 255) ++res.nplane;
+                if (R.disk_mode == BHR_DISK_THIN) {
+                    const T f = x0.y / (x0.y - x.y);
+                    const V3<T> hit = x0 * (T(1) - f) + x * f;
+                    const T rh = std::sqrt(hit.x * hit.x + hit.z * hit.z);
+                    if (rh >= R.disk_inner && rh <= R.disk_outer && res.ncross < 3) {
+                        res.cross_r[res.ncross] = rh;
+                        res.cross_phi[res.ncross] = std::atan2(hit.z, hit.x);
+                        ++res.ncross;
+                    }
+                }
+            }
+            if (!finite3(x) || !finite3(v)) {
+                res.nonfinite = true;
+                break;
+            }
+        }
+        if (status == 0) status = BHR_STATUS_BUDGET;
+    }
+    res.status = status;
+    res.steps = steps;
+    res.dir = escDir;
+    res.x = x;
+    res.v = v;
+    return res;
+}
+
+template <class T> inline void toHit(const Result<T>& r, bhr_hit* o) {
+    *o = bhr_hit{};
+    o->status = static_cast<uint8_t>(r.status);
+    o->ncross = static_cast<uint8_t>(r.ncross);
+    o->flags = r.nonfinite ? BHR_FLAG_NONFINITE : 0;
+    o->nplane = static_cast<uint8_t>(r.nplane);
+    o->steps = static_cast<uint32_t>(r.steps);
+    if (r.status == BHR_STATUS_ESCAPED) {  // dir is zero unless the ray escaped
+        o->dir[0] = static_cast<float>(r.dir.x);
+        o->dir[1] = static_cast<float>(r.dir.y);
+        o->dir[2] = static_cast<float>(r.dir.z);
+    }
+    o->b_axis = static_cast<float>(r.b_axis);
+    o->b = static_cast<float>(r.b);
+    o->min_r = std::isfinite(r.min_r) ? static_cast<float>(r.min_r) : 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        o->cross_r[k] = static_cast<float>(r.cross_r[k]);
+        o->cross_phi[k] = static_cast<float>(r.cross_phi[k]);
+    }
+}
+
+template <class T> inline Result<T> marchPixel(const bhr_view& w, const Rule<T>& R, int i, int j) {
+    const V3<T> cam{T(w.cam_pos[0]), T(w.cam_pos[1]), T(w.cam_pos[2])};
+    return march(R, cam, primaryRay<T>(w, i, j));
+}
+
+}  // namespace oracle

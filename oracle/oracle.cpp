@@ -1,0 +1,158 @@
+// C entry points of the CPU oracle (liboracle.so) -- TEST INFRASTRUCTURE ONLY.
+// Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg through ctypes;
+// never by the product library. The march itself is oracle/march.hpp.
+#include <algorithm>
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "march.hpp"
+
+using namespace oracle;
+
+namespace {
+
+template <class F>
+void parallel_for(int64_t n, int nthreads, int64_t grain, F&& fn) {
+    if (nthreads <= 1 || n <= grain) {
+        for (int64_t k = 0; k < n; ++k) fn(k);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> pool;
+    pool.reserve(nthreads);
+    for (int t = 0; t < nthreads; ++t) {
+        pool.emplace_back([&] {
+            for (;;) {
+                const int64_t b = next.fetch_add(grain);
+                if (b >= n) break;
+                const int64_t e = std::min(n, b + grain);
+                for (int64_t k = b; k < e; ++k) fn(k);
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+}
+
+bool view_ok(const bhr_view* v) {
+    return v && v->width > 0 && v->height > 0 && v->max_steps >= 0 && v->disk_mode != BHR_DISK_VOLUMETRIC;
+}
+
+template <class T>
+void trace_one(const bhr_view& w, const Rule<T>& R, int64_t idx, bhr_hit* out) {
+    const int i = static_cast<int>(idx % w.width);
+    const int j = static_cast<int>(idx / w.width);
+    toHit(marchPixel<T>(w, R, i, j), out);
+}
+
+}  // namespace
+
+extern "C" {
+
+// Traces every pixel of a view (row-major, row 0 at the bottom) into host memory.
+int oracle_trace_view(const bhr_view* v, bhr_hit* out, int nthreads, int fp64) {
+    if (!view_ok(v) || !out) return BHR_ERR_INVALID_ARG;
+    const int64_t n = static_cast<int64_t>(v->width) * v->height;
+    if (fp64) {
+        const Rule<double> R = Rule<double>::from_view(*v);
+        parallel_for(n, nthreads, 256, [&](int64_t k) { trace_one<double>(*v, R, k, out + k); });
+    } else {
+        const Rule<float> R = Rule<float>::from_view(*v);
+        parallel_for(n, nthreads, 256, [&](int64_t k) { trace_one<float>(*v, R, k, out + k); });
+    }
+    return BHR_OK;
+}
+
+// Traces the listed pixel indices (idx = j * width + i); out[k] belongs to idx[k].
+int oracle_trace_pixels(const bhr_view* v, const int64_t* idx, int64_t n, bhr_hit* out, int nthreads, int fp64) {
+    if (!view_ok(v) || !idx || !out || n < 0) return BHR_ERR_INVALID_ARG;
+    const int64_t npix = static_cast<int64_t>(v->width) * v->height;
+    for (int64_t k = 0; k < n; ++k)
+        if (idx[k] < 0 || idx[k] >= npix) return BHR_ERR_INVALID_ARG;
+    if (fp64) {
+        const Rule<double> R = Rule<double>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { trace_one<double>(*v, R, idx[k], out + k); });
+    } else {
+        const Rule<float> R = Rule<float>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { trace_one<float>(*v, R, idx[k], out + k); });
+    }
+    return BHR_OK;
+}
+
+// Primary ray directions of the listed pixels in double (blackhole.frag:68-72 in FP64).
+int oracle_primary_rays(const bhr_view* v, const int64_t* idx, int64_t n, double* dirs) {
+    if (!view_ok(v) || !idx || !dirs) return BHR_ERR_INVALID_ARG;
+    for (int64_t k = 0; k < n; ++k) {
+        const V3<double> d = primaryRay<double>(*v, static_cast<int>(idx[k] % v->width),
+                                                static_cast<int>(idx[k] / v->width));
+        dirs[3 * k] = d.x;
+        dirs[3 * k + 1] = d.y;
+        dirs[3 * k + 2] = d.z;
+    }
+    return BHR_OK;
+}
+
+// One ray from a double camera position and direction under the rule of `rule` (its pose,
+// size and pixel fields are ignored). state_out (may be NULL) gets the final x, v and dir
+// in double: x[3], v[3], dir[3].
+int oracle_march_ray(const bhr_view* rule, const double cam[3], const double dir[3], int fp64, bhr_hit* out,
+                     double* state_out) {
+    if (!rule || !cam || !dir || !out) return BHR_ERR_INVALID_ARG;
+    if (fp64) {
+        const Rule<double> R = Rule<double>::from_view(*rule);
+        const Result<double> r = march(R, V3<double>{cam[0], cam[1], cam[2]}, V3<double>{dir[0], dir[1], dir[2]});
+        toHit(r, out);
+        if (state_out) {
+            const double s[9] = {r.x.x, r.x.y, r.x.z, r.v.x, r.v.y, r.v.z, r.dir.x, r.dir.y, r.dir.z};
+            std::memcpy(state_out, s, sizeof s);
+        }
+    } else {
+        const Rule<float> R = Rule<float>::from_view(*rule);
+        const Result<float> r = march(R, V3<float>{float(cam[0]), float(cam[1]), float(cam[2])},
+                                      V3<float>{float(dir[0]), float(dir[1]), float(dir[2])});
+        toHit(r, out);
+        if (state_out) {
+            const double s[9] = {r.x.x, r.x.y, r.x.z, r.v.x, r.v.y, r.v.z, r.dir.x, r.dir.y, r.dir.z};
+            std::memcpy(state_out, s, sizeof s);
+        }
+    }
+    return BHR_OK;
+}
+
+// Geodesic.h:107-140 trace(camPos, dir, maxSteps, stepScale, escTol, rEscMin) with the
+// reference's double constants (capture below 2 + 0.01, ds floor 1e-4, no disk).
+// out9: final x[3], v[3], dir[3]; out_int: status, steps, equatorCrossings; out_minr: minR.
+int oracle_cpu_trace(const double cam[3], const double dir[3], int max_steps, double step_scale, double esc_tol,
+                     double r_esc_min, double* out9, int* out_int, double* out_minr) {
+    if (!cam || !dir || !out9 || !out_int || !out_minr) return BHR_ERR_INVALID_ARG;
+    Rule<double> R;
+    R.term_mode = BHR_TERM_CPU;
+    R.max_steps = max_steps;
+    R.disk_mode = BHR_DISK_NONE;
+    R.lensing = true;
+    R.far_mode = false;
+    R.step_scale = step_scale;
+    R.capture_r = 2.0 + 0.01;
+    R.esc_tol = esc_tol;
+    R.r_esc_min = r_esc_min;
+    R.ds_floor = 1e-4;
+    const Result<double> r = march(R, V3<double>{cam[0], cam[1], cam[2]}, V3<double>{dir[0], dir[1], dir[2]});
+    // TraceResult::dir is zero unless the ray escaped (Geodesic.h:99)
+    const bool esc = r.status == BHR_STATUS_ESCAPED;
+    const double s[9] = {r.x.x, r.x.y, r.x.z, r.v.x, r.v.y, r.v.z,
+                         esc ? r.dir.x : 0.0, esc ? r.dir.y : 0.0, esc ? r.dir.z : 0.0};
+    std::memcpy(out9, s, sizeof s);
+    // TraceResult::Status: Escaped 0, Captured 1, MaxSteps 2
+    out_int[0] = r.status == BHR_STATUS_ESCAPED ? 0 : (r.status == BHR_STATUS_CAPTURED ? 1 : 2);
+    out_int[1] = r.steps;
+    out_int[2] = r.nplane;
+    *out_minr = r.min_r;
+    return BHR_OK;
+}
+
+int oracle_hit_size(void) { return static_cast<int>(sizeof(bhr_hit)); }
+int oracle_view_size(void) { return static_cast<int>(sizeof(bhr_view)); }
+
+}  // extern "C"

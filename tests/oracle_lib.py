@@ -1,0 +1,118 @@
+"""ctypes loader of the CPU oracle (oracle/_build/liboracle.so) for the tests.
+
+The oracle is test infrastructure: it checks the CUDA path and is never imported by the
+product package. It is built from oracle/Makefile on first use.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from blackholerender_gb300 import HIT_DTYPE, View
+
+ROOT = Path(__file__).resolve().parent.parent
+ORACLE_DIR = ROOT / "oracle"
+LIB = ORACLE_DIR / "_build" / "liboracle.so"
+REF_LIB = ORACLE_DIR / "_ref" / "libbhs_ref.so"
+
+_lib = None
+_ref = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "all"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = ctypes.CDLL(str(LIB))
+        VP = ctypes.POINTER(View)
+        D = ctypes.POINTER(ctypes.c_double)
+        L.oracle_trace_view.argtypes = [VP, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.oracle_trace_pixels.argtypes = [VP, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_int]
+        L.oracle_primary_rays.argtypes = [VP, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+        L.oracle_march_ray.argtypes = [VP, D, D, ctypes.c_int, ctypes.c_void_p, D]
+        L.oracle_cpu_trace.argtypes = [D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, D,
+                                       ctypes.POINTER(ctypes.c_int), D]
+        assert L.oracle_hit_size() == 64 and L.oracle_view_size() == ctypes.sizeof(View)
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own Geodesic.h compiled by oracle/Makefile (only where its sources are)."""
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            return None
+        L = ctypes.CDLL(str(REF_LIB))
+        D = ctypes.POINTER(ctypes.c_double)
+        L.ref_trace.argtypes = [D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, D,
+                                ctypes.POINTER(ctypes.c_int), D]
+        _ref = L
+    return _ref
+
+
+def nthreads() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+def trace_view(view: View, fp64: bool = True, threads: int | None = None) -> np.ndarray:
+    out = np.zeros(view.rays, dtype=HIT_DTYPE)
+    rc = lib().oracle_trace_view(ctypes.byref(view), out.ctypes.data, threads or nthreads(), int(fp64))
+    assert rc == 0, rc
+    return out
+
+
+def trace_pixels(view: View, idx: np.ndarray, fp64: bool = True, threads: int | None = None) -> np.ndarray:
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    out = np.zeros(len(idx), dtype=HIT_DTYPE)
+    rc = lib().oracle_trace_pixels(ctypes.byref(view), idx.ctypes.data, len(idx), out.ctypes.data,
+                                   threads or nthreads(), int(fp64))
+    assert rc == 0, rc
+    return out
+
+
+def primary_rays(view: View, idx: np.ndarray) -> np.ndarray:
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    out = np.zeros((len(idx), 3), dtype=np.float64)
+    assert lib().oracle_primary_rays(ctypes.byref(view), idx.ctypes.data, len(idx), out.ctypes.data) == 0
+    return out
+
+
+def cpu_trace(cam, d, max_steps=200000, step_scale=0.005, esc_tol=1e-4, r_esc_min=30.0):
+    """oracle restatement of Geodesic.h trace(): (status, steps, crossings, dir[3], minR)."""
+    D3 = ctypes.c_double * 3
+    o9 = (ctypes.c_double * 9)()
+    oi = (ctypes.c_int * 3)()
+    om = ctypes.c_double()
+    lib().oracle_cpu_trace(D3(*cam), D3(*d), max_steps, step_scale, esc_tol, r_esc_min, o9, oi, ctypes.byref(om))
+    return oi[0], oi[1], oi[2], np.array(o9[6:9]), om.value
+
+
+def ref_trace(cam, d, max_steps=200000, step_scale=0.005, esc_tol=1e-4, r_esc_min=30.0):
+    """The reference's own trace() through oracle/_ref (same return layout as cpu_trace)."""
+    L = ref_lib()
+    D3 = ctypes.c_double * 3
+    o9 = (ctypes.c_double * 9)()
+    oi = (ctypes.c_int * 3)()
+    om = ctypes.c_double()
+    L.ref_trace(D3(*cam), D3(*d), max_steps, step_scale, esc_tol, r_esc_min, o9, oi, ctypes.byref(om))
+    return oi[0], oi[1], oi[2], np.array(o9[0:3]), om.value
+
+
+def angle(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Angle (rad) between direction rows, robust near zero: atan2(|a x b|, a . b) in float64."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    c = np.linalg.norm(np.cross(a, b), axis=-1)
+    d = np.sum(a * b, axis=-1)
+    return np.arctan2(c, d)
