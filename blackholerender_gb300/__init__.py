@@ -117,6 +117,17 @@ class Tracer:
         self.trace_ptrs(views, [o.data_ptr() for o in outs], precision, method, stream.cuda_stream)
         return outs
 
+    def trace_host(self, views: Sequence[View], outs: Sequence[np.ndarray], precision: int = PREC_FP32,
+                   method: int = METHOD_PLAIN) -> None:
+        """bhr_trace_host: records land in host arrays (HIT_DTYPE or uint8, one per view)."""
+        n = len(views)
+        for v, o in zip(views, outs):
+            if o.nbytes < v.rays * HIT_BYTES:
+                raise ValueError("host output buffer too small")
+        arr = (View * n)(*views)
+        ptrs = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
+        _abi.check(_abi.lib().bhr_trace_host(self._ctx, arr, n, ptrs, precision, method), self._ctx)
+
     def stats(self) -> Stats:
         s = Stats()
         _abi.check(_abi.lib().bhr_trace_stats(self._ctx, ctypes.byref(s)), self._ctx)

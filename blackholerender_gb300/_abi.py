@@ -117,12 +117,12 @@ HIT_DTYPE = np.dtype(
         ("nplane", np.uint8),
         ("steps", np.uint32),
         ("dir", np.float32, (3,)),
+        ("min_r", np.float32),
+        ("reserved", np.float32, (2,)),
         ("b_axis", np.float32),
         ("b", np.float32),
-        ("min_r", np.float32),
         ("cross_r", np.float32, (3,)),
         ("cross_phi", np.float32, (3,)),
-        ("reserved", np.float32, (2,)),
     ]
 )
 assert HIT_DTYPE.itemsize == 64
@@ -143,6 +143,7 @@ SIGNATURES = {
     "bhr_view_orbit_pose": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "bhr_view_rays": (ctypes.c_int64, [_VP]),
     "bhr_trace": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, _P]),
+    "bhr_trace_host": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int]),
     "bhr_trace_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
     "bhr_trace_view_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
 }

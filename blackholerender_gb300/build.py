@@ -28,6 +28,11 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libbhr.so")
 
 
+# Device float code flushes denormals (as GLSL does): rsqrt and the fast divide then map to
+# single SFU instructions without subnormal fix-up sequences. FP64 code is unaffected.
+DEVICE_FLAGS = {"kernels.cu": ["-ftz=true"], "surrogate.cu": ["-ftz=true"]}
+
+
 def _flags() -> list[str]:
     return ARCH + [
         "-O3", "-lineinfo", "-std=c++17",
@@ -52,7 +57,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     for src in srcs:
         obj = BUILD / (src.stem + ".o")
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc, *_flags(), "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *_flags(), *DEVICE_FLAGS.get(src.name, []), "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

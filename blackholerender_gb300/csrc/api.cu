@@ -20,15 +20,22 @@
 struct bhr_ctx {
     int device = 0;
     int sms = 0;
-    bhr::LaunchCfg cfg_one{256, 0, 256, 4};
-    bhr::LaunchCfg cfg_multi{256, 0, 256, 4};
+    int block = 512;        // threads per block of the FP32 march
+    int blocks_per_sm = 0;  // 0: as many as fit
+    int chunk = 64;         // rays per work chunk
+    int refill = 8;         // idle lanes that trigger a refill
     bhr::WorkQueue* q = nullptr;  // one per batch slot
     int nq = 0;
     int2* band = nullptr;
     bhr::PromoEntry* promo = nullptr;
     int64_t scratch_rays = 0;  // capacity of band / promo in rays
+    // bhr_trace_host: device staging (two halves) and two streams, created on first use
+    bhr_hit* staging = nullptr;
+    int64_t staging_rays = 0;  // rays per half
+    cudaStream_t hstream[2] = {nullptr, nullptr};
     cudaStream_t last_stream = nullptr;
     int last_batches = 0;
+    std::vector<std::pair<int, int>> last_slots;  // (work queue, view slot) per view of the last trace
     int last_nviews = 0;
     bool have_last = false;
     std::string err;
@@ -98,29 +105,37 @@ bhr::DevView make_dev_view(const bhr_view& v, bhr_hit* out) {
     d.baxis_scale = 1.0f / std::sqrt(std::max(1.0f - 2.0f / d.rcam, 1e-6f));
     d.step_scale = v.step_scale;
     d.disk_step = v.disk_step;
-    d.disk_inner = v.disk_inner;
-    d.disk_outer = v.disk_outer;
-    d.slab = 2.5f * v.disk_thickness;
-    const float lo = v.disk_inner - 1.0f, hi = v.disk_outer + 1.0f;
-    d.rcyl_lo2 = lo > 0.0f ? lo * lo : -1.0f;
-    d.rcyl_hi2 = hi > 0.0f ? hi * hi : -1.0f;
-    d.capture_r = v.capture_r;
-    d.escape_r = v.escape_r;
-    d.esc_tol = v.esc_tol;
-    d.r_esc_min = v.term_mode == BHR_TERM_SHADER ? shader_r_esc_min(v.disk_outer) : v.r_esc_min;
-    d.ds_floor = v.ds_floor;
-    d.promote_band = v.promote_band;
-    d.promote_r = v.promote_r;
-    d.disk_mode = v.disk_mode;
-    d.lensing = (v.lensing != 0 && v.far_mode == 0) ? 1 : 0;
-    d.far_mode = v.far_mode != 0 ? 1 : 0;
-    d.term_mode = v.term_mode;
     for (int k = 0; k < 3; ++k) d.cam_d[k] = double(v.cam_pos[k]);
     d.chunk_start = 0;
     d.nrays = int64_t(v.width) * v.height;
     d.out = out;
     return d;
 }
+
+// The launch-wide constants of a view: termination rule and disk geometry.
+bhr::Rule make_rule(const bhr_view& v) {
+    bhr::Rule r{};
+    r.capture_r = v.capture_r;
+    r.escape_r = v.escape_r;
+    r.esc_tol = v.esc_tol;
+    r.r_esc_min = v.term_mode == BHR_TERM_SHADER ? shader_r_esc_min(v.disk_outer) : v.r_esc_min;
+    r.ds_floor = v.ds_floor;
+    r.slab = 2.5f * v.disk_thickness;
+    const float lo = v.disk_inner - 1.0f, hi = v.disk_outer + 1.0f;
+    r.rcyl_lo2 = lo > 0.0f ? lo * lo : -1.0f;
+    r.rcyl_hi2 = hi > 0.0f ? hi * hi : -1.0f;
+    r.disk_inner = v.disk_inner;
+    r.disk_outer = v.disk_outer;
+    r.promote_r = v.promote_r;
+    r.promote_band = v.promote_band;
+    r.term_mode = v.term_mode;
+    r.disk_mode = v.disk_mode;
+    r.lensing = (v.lensing != 0 && v.far_mode == 0) ? 1 : 0;
+    r.far_mode = v.far_mode != 0 ? 1 : 0;
+    return r;
+}
+
+bool same_rule(const bhr::Rule& a, const bhr::Rule& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
 
 int ensure_scratch(bhr_ctx* c, int nbatches, int64_t rays, bool mixed) {
     if (nbatches > c->nq) {
@@ -145,12 +160,15 @@ int ensure_scratch(bhr_ctx* c, int nbatches, int64_t rays, bool mixed) {
     return BHR_OK;
 }
 
-bhr::LaunchCfg finish_cfg(const bhr_ctx* c, bhr::LaunchCfg cfg, bool multi, bool mixed, int bps_override) {
-    int bps = bps_override > 0 ? bps_override : bhr::march_blocks_per_sm(cfg.block, multi, mixed);
-    bps = std::max(1, std::min(bps, bhr::march_blocks_per_sm(cfg.block, multi, mixed)));
+bhr::LaunchCfg make_cfg(const bhr_ctx* c, int variant, bool multi, bool mixed) {
+    bhr::LaunchCfg cfg{};
+    cfg.block = c->block;
+    cfg.variant = variant;
+    const int fit = std::max(1, bhr::march_blocks_per_sm(cfg.block, variant, multi, mixed));
+    const int bps = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, fit) : fit;
     cfg.grid = c->sms * bps;
-    cfg.refill = std::max(1, std::min(cfg.refill, 32));
-    cfg.chunk = std::max(32, cfg.chunk);
+    cfg.refill = std::max(1, std::min(c->refill, 32));
+    cfg.chunk = std::max(32, c->chunk);
     return cfg;
 }
 
@@ -199,22 +217,18 @@ int bhr_create(bhr_ctx** out, const bhr_options* opts) {
     cudaGetDevice(&prev);
     cudaSetDevice(c->device);
     c->sms = prop.multiProcessorCount;
-    int bps_one = 0, bps_multi = 0;
     if (opts) {
-        if (opts->block_size == 128 || opts->block_size == 256 || opts->block_size == 512) {
-            c->cfg_one.block = opts->block_size;
-            c->cfg_multi.block = opts->block_size;
+        if (opts->block_size == 256 || opts->block_size == 512) {
+            c->block = opts->block_size;
         } else if (opts->block_size != 0) {
             cudaSetDevice(prev);
             delete c;
-            return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_create: block_size must be 0, 128, 256 or 512");
+            return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_create: block_size must be 0, 256 or 512");
         }
-        if (opts->chunk > 0) c->cfg_one.chunk = c->cfg_multi.chunk = opts->chunk;
-        if (opts->refill > 0) c->cfg_one.refill = c->cfg_multi.refill = opts->refill;
-        bps_one = bps_multi = opts->blocks_per_sm;
+        if (opts->chunk > 0) c->chunk = opts->chunk;
+        if (opts->refill > 0) c->refill = opts->refill;
+        if (opts->blocks_per_sm > 0) c->blocks_per_sm = opts->blocks_per_sm;
     }
-    c->cfg_one = finish_cfg(c, c->cfg_one, false, false, bps_one);
-    c->cfg_multi = finish_cfg(c, c->cfg_multi, true, false, bps_multi);
     const int rc = ensure_scratch(c, 1, 0, false);
     cudaSetDevice(prev);
     if (rc != BHR_OK) {
@@ -233,6 +247,9 @@ int bhr_destroy(bhr_ctx* c) {
     if (c->q) cudaFree(c->q);
     if (c->band) cudaFree(c->band);
     if (c->promo) cudaFree(c->promo);
+    if (c->staging) cudaFree(c->staging);
+    for (cudaStream_t& st : c->hstream)
+        if (st) cudaStreamDestroy(st);
     cudaSetDevice(prev);
     delete c;
     return BHR_OK;
@@ -389,49 +406,140 @@ int bhr_trace(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out
         rays += int64_t(views[k].width) * views[k].height;
     }
     const bool mixed = precision == BHR_PREC_MIXED;
-    const int nb = nviews == 1 ? 1 : (nviews + bhr::kMaxViews - 1) / bhr::kMaxViews;
+    // group views by rule (one launch per group and per kMaxViews views)
+    std::vector<bhr::Rule> rules;
+    std::vector<std::vector<int>> groups;
+    for (int k = 0; k < nviews; ++k) {
+        const bhr::Rule r = make_rule(views[k]);
+        size_t g = 0;
+        while (g < rules.size() && !same_rule(rules[g], r)) ++g;
+        if (g == rules.size()) {
+            rules.push_back(r);
+            groups.emplace_back();
+        }
+        groups[g].push_back(k);
+    }
+    int nb = 0;
+    for (const auto& g : groups) nb += int((g.size() + bhr::kMaxViews - 1) / bhr::kMaxViews);
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(c->device);
     int rc = ensure_scratch(c, nb, rays, mixed);
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     const int fp64_grid = c->sms * 8;
-    for (int bi = 0; rc == BHR_OK && bi < nb; ++bi) {
-        bhr::Scratch sc{c->q + bi, c->band, c->promo};
-        cudaError_t e = cudaMemsetAsync(sc.q, 0, sizeof(bhr::WorkQueue), st);
-        if (e != cudaSuccess) {
-            rc = cuda_fail(c, e, "bhr_trace: cudaMemsetAsync");
-            break;
-        }
-        if (nviews == 1) {
-            const bhr::DevView dv = make_dev_view(views[0], out_dev[0]);
-            bhr::LaunchCfg cfg = c->cfg_one;
-            if (mixed) cfg = finish_cfg(c, cfg, false, true, cfg.grid / c->sms);
-            e = bhr::launch_march_one(dv, sc, mixed, cfg, st);
-            if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_one(dv, sc, fp64_grid, st);
-        } else {
-            static thread_local bhr::ViewBatch b;  // 14 KB; passed by value as a kernel parameter
-            const int v0 = bi * bhr::kMaxViews;
-            b.nviews = std::min(bhr::kMaxViews, nviews - v0);
-            int64_t chunk_acc = 0;
-            bhr::LaunchCfg cfg = c->cfg_multi;
-            if (mixed) cfg = finish_cfg(c, cfg, true, true, cfg.grid / c->sms);
-            for (int k = 0; k < b.nviews; ++k) {
-                b.views[k] = make_dev_view(views[v0 + k], out_dev[v0 + k]);
-                b.views[k].chunk_start = chunk_acc;
-                chunk_acc += (b.views[k].nrays + cfg.chunk - 1) / cfg.chunk;
+    int bi = 0;
+    std::vector<std::pair<int, int>> slots(size_t(nviews), {0, 0});
+    for (size_t g = 0; rc == BHR_OK && g < groups.size(); ++g) {
+        const bhr::Rule& rule = rules[g];
+        const int variant = bhr::rule_variant(rule);
+        const std::vector<int>& members = groups[g];
+        for (size_t m0 = 0; rc == BHR_OK && m0 < members.size(); m0 += bhr::kMaxViews, ++bi) {
+            bhr::Scratch sc{c->q + bi, c->band, c->promo};
+            cudaError_t e = cudaMemsetAsync(sc.q, 0, sizeof(bhr::WorkQueue), st);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(c, e, "bhr_trace: cudaMemsetAsync");
+                break;
             }
-            b.total_chunks = chunk_acc;
-            e = bhr::launch_march_multi(b, sc, mixed, cfg, st);
-            if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_multi(b, sc, fp64_grid, st);
+            const size_t nv = std::min<size_t>(bhr::kMaxViews, members.size() - m0);
+            if (nviews == 1) {
+                const bhr::DevView dv = make_dev_view(views[0], out_dev[0]);
+                e = bhr::launch_march_one(dv, rule, sc, mixed, make_cfg(c, variant, false, mixed), st);
+                if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_one(dv, rule, sc, fp64_grid, st);
+            } else {
+                static thread_local bhr::ViewBatch b;  // ~12 KB, passed by value as a kernel parameter
+                const bhr::LaunchCfg cfg = make_cfg(c, variant, true, mixed);
+                b.nviews = int(nv);
+                b.rule = rule;
+                int64_t chunk_acc = 0;
+                for (size_t k = 0; k < nv; ++k) {
+                    const int vi = members[m0 + k];
+                    slots[size_t(vi)] = {bi, int(k)};
+                    b.views[k] = make_dev_view(views[vi], out_dev[vi]);
+                    b.views[k].chunk_start = chunk_acc;
+                    chunk_acc += (b.views[k].nrays + cfg.chunk - 1) / cfg.chunk;
+                }
+                b.total_chunks = chunk_acc;
+                e = bhr::launch_march_multi(b, sc, mixed, cfg, st);
+                if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_multi(b, sc, fp64_grid, st);
+            }
+            if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace: kernel launch");
         }
-        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace: kernel launch");
     }
     if (rc == BHR_OK) {
         c->last_stream = st;
         c->last_batches = nb;
         c->last_nviews = nviews;
+        c->last_slots = std::move(slots);
         c->have_last = true;
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int bhr_trace_host(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out_host, int precision,
+                   int method) {
+    if (!c) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_trace_host: ctx is NULL");
+    if (!views || nviews <= 0 || !out_host) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_host: no views or outputs");
+    int64_t biggest = 0;
+    for (int k = 0; k < nviews; ++k) {
+        const int rc = check_view(c, views[k], k);
+        if (rc != BHR_OK) return rc;
+        if (!out_host[k]) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_host: output buffer is NULL");
+        biggest = std::max(biggest, int64_t(views[k].width) * views[k].height);
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    int rc = BHR_OK;
+    // groups of views, each traced in one launch into one staging half while the other half's
+    // records travel to the host on the other stream
+    const int64_t half = std::max<int64_t>(biggest, int64_t(1) << 22);
+    if (half > c->staging_rays) {
+        if (c->staging) cudaFree(c->staging);
+        c->staging = nullptr;
+        c->staging_rays = 0;
+        cudaError_t e = cudaMalloc(&c->staging, sizeof(bhr_hit) * size_t(2 * half));
+        if (e != cudaSuccess) rc = fail(c, BHR_ERR_OOM, std::string("bhr_trace_host staging: ") + cudaGetErrorString(e));
+        else c->staging_rays = half;
+    }
+    for (int k = 0; rc == BHR_OK && k < 2; ++k)
+        if (!c->hstream[k] && cudaStreamCreateWithFlags(&c->hstream[k], cudaStreamNonBlocking) != cudaSuccess)
+            rc = fail(c, BHR_ERR_CUDA, "bhr_trace_host: cannot create streams");
+    std::vector<bhr_hit*> dst;
+    int g = 0;
+    for (int k0 = 0; rc == BHR_OK && k0 < nviews; ++g) {
+        // views that fit one staging half, at most kMaxViews
+        int k1 = k0;
+        int64_t acc = 0;
+        while (k1 < nviews && k1 - k0 < bhr::kMaxViews) {
+            const int64_t n = int64_t(views[k1].width) * views[k1].height;
+            if (acc + n > c->staging_rays && k1 > k0) break;
+            acc += n;
+            ++k1;
+        }
+        cudaStream_t st = c->hstream[g & 1];
+        bhr_hit* base = c->staging + (g & 1) * c->staging_rays;
+        dst.clear();
+        int64_t off = 0;
+        for (int k = k0; k < k1; ++k) {
+            dst.push_back(base + off);
+            off += int64_t(views[k].width) * views[k].height;
+        }
+        rc = bhr_trace(c, views + k0, k1 - k0, dst.data(), precision, method, st);
+        off = 0;
+        for (int k = k0; rc == BHR_OK && k < k1; ++k) {
+            const int64_t n = int64_t(views[k].width) * views[k].height;
+            cudaError_t e = cudaMemcpyAsync(out_host[k], base + off, sizeof(bhr_hit) * size_t(n),
+                                            cudaMemcpyDeviceToHost, st);
+            if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace_host: copy to host");
+            off += n;
+        }
+        k0 = k1;
+    }
+    for (cudaStream_t st : c->hstream) {
+        if (!st) continue;
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess && rc == BHR_OK) rc = cuda_fail(c, e, "bhr_trace_host: synchronize");
     }
     cudaSetDevice(prev);
     return rc;
@@ -473,8 +581,8 @@ int bhr_trace_view_times(bhr_ctx* c, double* ms, int nviews) {
     cudaSetDevice(prev);
     if (e != cudaSuccess) return cuda_fail(c, e, "bhr_trace_view_times");
     for (int k = 0; k < nviews; ++k) {
-        const bhr::WorkQueue& q = qs[size_t(k / bhr::kMaxViews)];
-        const int s = k % bhr::kMaxViews;
+        const bhr::WorkQueue& q = qs[size_t(c->last_slots[size_t(k)].first)];
+        const int s = c->last_slots[size_t(k)].second;
         ms[k] = q.view_t_end[s] >= q.t_start ? double(q.view_t_end[s] - q.t_start) * 1e-6 : -1.0;
     }
     return BHR_OK;

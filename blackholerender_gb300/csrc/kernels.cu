@@ -1,15 +1,15 @@
 // March kernels for sm_103a.
 //
-// k_march_one / k_march_multi: persistent FP32 march, one ray per lane, 32 rays in flight
-//   per warp. Retired lanes are refilled from a per-warp ring of rays that were set up 32
-//   at a time (convergent) into shared memory, so ray setup never runs one lane at a time
-//   and the step loop stays full. Work comes from a global chunk counter (scratch), `chunk`
-//   consecutive pixels at a time. Finished rays are written as 16-byte stores into the
-//   caller's hit buffer; a record is 64 B, two whole 32 B sectors, so lane-scattered stores
-//   move no extra DRAM bytes.
-//     k_march_one:   one view, passed as a __grid_constant__ parameter (constant bank).
-//     k_march_multi: up to kMaxViews views in one launch, copied to shared memory; work
-//                    chunks never straddle views; per-view completion times are recorded.
+// k_march_one / k_march_multi: persistent FP32 march, one ray per lane, 32 rays in flight per
+//   warp. Retired lanes are refilled from a per-warp ring of rays that were set up 32 at a time
+//   (convergent) into shared memory, so ray setup never runs one lane at a time and the step
+//   loop stays full. Work comes from a global chunk counter (context scratch), `chunk`
+//   consecutive pixels at a time. A record is 64 B: a lane writes its two start words when the
+//   ray starts and its two end words when it retires, each a whole 32 B sector, so lane-
+//   scattered stores move no extra DRAM bytes.
+//     k_march_one:   one view; view and rule are __grid_constant__ parameters (constant bank).
+//     k_march_multi: up to kMaxViews views sharing one rule; views are copied to shared memory;
+//                    work chunks never straddle views; per-view completion times are recorded.
 //   With kMixed, rays with |b - sqrt(27)| < promote_band are queued for FP64 from the start,
 //   and rays that reach r < promote_r hand their state to the FP64 queue.
 // k_march_fp64_*: drains the FP64 queue in double precision.
@@ -32,15 +32,28 @@ __device__ __forceinline__ unsigned long long globaltimer() {
     return t;
 }
 
-// First two 16-byte words of a finished record (the crossing words are written during the march).
-__device__ __forceinline__ void write_hit(bhr_hit* rec, uint32_t info, uint32_t steps, float min_r, float3 d,
-                                          float b_axis, float b, uint32_t flags) {
+// End words of a finished record (words 0-7).
+__device__ __forceinline__ void write_end(bhr_hit* rec, uint32_t info, uint32_t steps, float min_r, float3 d,
+                                          uint32_t flags) {
     const uint32_t status = (info >> kStatusShift) & 0xfu;
-    if ((info >> 16) & 1u) flags |= BHR_FLAG_NONFINITE;
     const uint32_t w0 = status | (((info >> kNcrossShift) & 3u) << 8) | (flags << 16) | ((info & 0xffu) << 24);
     float4* p = reinterpret_cast<float4*>(rec);
     p[0] = make_float4(__uint_as_float(w0), __uint_as_float(steps), d.x, d.y);
-    p[1] = make_float4(d.z, b_axis, b, min_r);
+    p[1] = make_float4(d.z, min_r, 0.f, 0.f);
+}
+
+// Start words of a record (words 8-15): b_axis, b, crossing slots cleared.
+__device__ __forceinline__ void write_start(bhr_hit* rec, float b_axis, float b) {
+    float4* p = reinterpret_cast<float4*>(rec);
+    p[2] = make_float4(b_axis, b, 0.f, 0.f);
+    p[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// A state that went non-finite marches on (comparisons with NaN fail) until the budget; it is
+// flagged when the ray retires.
+template <class T>
+__device__ __forceinline__ bool nonfinite_state(const RayState<T>& s) {
+    return !isfinite(dot3(s.x, s.x) + dot3(s.v, s.v));
 }
 
 template <class T>
@@ -57,10 +70,11 @@ __device__ __forceinline__ float3 exit_dir(const RayState<T>& s, bool lensing) {
 
 // Per-warp ring of set-up rays in shared memory, structure of arrays.
 struct Pool {
-    float* f;         // [8][kPool]: v.x v.y v.z h2 ssf b_axis b ray
-    uint8_t* view;    // [kPool] view slot (multi-view launches)
+    float* f;       // [6][kPool]: v.x v.y v.z h2 ssf ray
+    uint8_t* view;  // [kPool] view slot (multi-view launches)
     __device__ __forceinline__ float& at(int k, int slot) const { return f[k * kPool + slot]; }
 };
+constexpr int kPoolFields = 6;
 
 // Warp-aggregated append of one entry per calling lane; returns this lane's slot.
 __device__ __forceinline__ unsigned long long warp_append(unsigned long long* ctr) {
@@ -73,8 +87,8 @@ __device__ __forceinline__ unsigned long long warp_append(unsigned long long* ct
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
-template <bool kMulti, bool kMixed>
-__device__ __forceinline__ void march_warp(const DevView* views, int nviews, int64_t total_chunks,
+template <bool kMulti, int kTerm, int kDisk, bool kMixed>
+__device__ __forceinline__ void march_warp(const DevView* views, int nviews, int64_t total_chunks, const Rule& R,
                                            const Scratch sc, int chunk, int refill_min, Pool pool) {
     WorkQueue* q = sc.q;
     const int lane = threadIdx.x & 31;
@@ -83,7 +97,7 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
     int cview = 0;
     int phead = 0, pcount = 0;   // pool ring
     bool dry = false;
-    bool active = false, pending = false;
+    bool active = false, pending = false, stamp = false;
     RayState<float> s;
     s.x = {0.f, 0.f, 0.f};
     s.v = {0.f, 0.f, 0.f};
@@ -92,9 +106,11 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
     s.min_r = 0.f;
     s.steps = 0;
     s.info = 0;
-    float b_axis = 0.f, b = 0.f;
-    int ridx = 0;   // ray index within its view
-    int vslot = 0;  // view slot of the lane's ray
+    bhr_hit* rec = nullptr;
+    int ridx = 0;      // ray index within its view
+    int vslot = 0;     // view slot of the lane's ray
+    int lane_budget = kMulti ? 0 : views[0].max_steps;
+    float lane_dstep = kMulti ? 0.f : views[0].disk_step;
     unsigned long long steps_sum = 0, promoted = 0, nonfinite = 0;
 
     for (;;) {
@@ -103,7 +119,6 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
         if (nidle != 0 && (nidle >= refill_min || dry)) {
             // ---- retire the finished rays of this warp
             if (pending) {
-                const DevView& w = views[vslot];
                 const uint32_t st = (s.info >> kStatusShift) & 0xfu;
                 bool counted = true;
                 if (kMixed && st == kPromote) {
@@ -115,27 +130,29 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                     e.x[0] = s.x.x; e.x[1] = s.x.y; e.x[2] = s.x.z;
                     e.v[0] = s.v.x; e.v[1] = s.v.y; e.v[2] = s.v.z;
                     e.min_r = s.min_r;
-                    e.b_axis = b_axis;
-                    e.b = b;
                     ++promoted;
                     counted = false;  // the FP64 pass finishes it
-                    steps_sum += s.steps;
                 } else {
-                    write_hit(w.out + ridx, s.info, s.steps, s.min_r, exit_dir(s, w.lensing != 0), b_axis, b, 0u);
-                    steps_sum += s.steps;
-                    nonfinite += (s.info >> 16) & 1u;
+                    const bool bad = nonfinite_state(s);
+                    write_end(rec, s.info, s.steps, s.min_r, exit_dir(s, R.lensing != 0),
+                              bad ? BHR_FLAG_NONFINITE : 0u);
+                    nonfinite += bad ? 1 : 0;
                 }
-                if constexpr (kMulti) {
-                    if (counted) {
-                        const unsigned m = __match_any_sync(__activemask(), vslot);
-                        if (lane == __ffs(m) - 1) {
-                            const unsigned long long c = __popc(m);
-                            const unsigned long long old = atomicAdd(&q->view_done[vslot], c);
-                            if (old + c == (unsigned long long)w.nrays) q->view_t_end[vslot] = globaltimer();
-                        }
-                    }
-                }
+                steps_sum += s.steps;
+                stamp = counted;
                 pending = false;
+            }
+            if constexpr (kMulti) {
+                // a view's completion time = the latest retire time of its rays: one atomicMax
+                // per distinct view among the rays retired now (usually one)
+                unsigned sm = __ballot_sync(0xffffffffu, stamp);
+                while (sm) {
+                    const int leader = __ffs(sm) - 1;
+                    const int v0 = __shfl_sync(0xffffffffu, vslot, leader);
+                    sm &= ~__ballot_sync(0xffffffffu, stamp && vslot == v0);
+                    if (lane == leader) atomicMax(&q->view_t_end[v0], globaltimer());
+                }
+                stamp = false;
             }
             // ---- top up the pool with convergent setup batches of up to 32 rays
             while (pcount < nidle && !dry) {
@@ -149,7 +166,7 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                     }
                     int v = 0;
                     if constexpr (kMulti) {
-                        // chunks never straddle views: find v with chunk_start[v] <= base
+                        // chunks never straddle views: the last v with chunk_start[v] <= base
                         for (int g = 0; g < nviews; g += 32) {
                             const int k = g + lane;
                             const bool ge = k < nviews && (int64_t)base >= views[k].chunk_start;
@@ -169,11 +186,11 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                 if (lane < n) {
                     const int j = my / w.width;
                     const int i = my - j * w.width;
-                    V3<float> dir;
-                    ri = setup_ray<float>(w, i, j, &dir);
+                    ri = setup_ray<float>(w, R, i, j);
+                    write_start(w.out + my, ri.b_axis, ri.b);
                     keep = true;
                     if constexpr (kMixed) {
-                        if (w.lensing && fabsf(ri.b - kSqrt27f) < w.promote_band) {
+                        if (R.lensing && fabsf(ri.b - kSqrt27f) < R.promote_band) {
                             keep = false;  // the whole ray runs in FP64
                             sc.band[warp_append(&q->band_count)] = make_int2(my, cview);
                         }
@@ -187,9 +204,7 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                     pool.at(2, slot) = ri.v.z;
                     pool.at(3, slot) = ri.h2;
                     pool.at(4, slot) = ri.ssf;
-                    pool.at(5, slot) = ri.b_axis;
-                    pool.at(6, slot) = ri.b;
-                    pool.at(7, slot) = __int_as_float(my);
+                    pool.at(5, slot) = __int_as_float(my);
                     if constexpr (kMulti) pool.view[slot] = (uint8_t)cview;
                 }
                 pcount += __popc(km);
@@ -205,17 +220,16 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                 s.v = {pool.at(0, slot), pool.at(1, slot), pool.at(2, slot)};
                 s.h2 = pool.at(3, slot);
                 s.ssf = pool.at(4, slot);
-                b_axis = pool.at(5, slot);
-                b = pool.at(6, slot);
-                ridx = __float_as_int(pool.at(7, slot));
+                ridx = __float_as_int(pool.at(5, slot));
+                rec = w.out + ridx;
                 s.x = {w.cam[0], w.cam[1], w.cam[2]};
                 s.min_r = __int_as_float(0x7f800000);  // +inf
                 s.steps = 0;
                 s.info = 0;
-                // crossing words start at zero; march_step fills them as crossings happen
-                float4* p = reinterpret_cast<float4*>(w.out + ridx);
-                p[2] = make_float4(0.f, 0.f, 0.f, 0.f);
-                p[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if constexpr (kMulti) {
+                    lane_budget = w.max_steps;
+                    lane_dstep = w.disk_step;
+                }
                 active = true;
             }
             const int taken = min(nidle, pcount);
@@ -228,8 +242,7 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
 #pragma unroll
         for (int u = 0; u < kStepsPerCheck; ++u) {
             if (active) {
-                const DevView& w = views[vslot];
-                if (march_step<float, kMixed>(w, s, w.out + ridx)) {
+                if (march_step<float, kTerm, kDisk, kMixed>(R, lane_budget, lane_dstep, s, rec)) {
                     active = false;
                     pending = true;
                 }
@@ -255,7 +268,7 @@ __device__ __forceinline__ void note_start(WorkQueue* q) {
 // FP64 continuation: band rays from scratch, then promoted FP32 states. One ray per thread
 // with dynamic fetch; FP64 runs at a small fraction of the FP32 rate, so the queues are short.
 template <bool kMulti>
-__device__ __forceinline__ void march_fp64(const DevView* views, const Scratch sc) {
+__device__ __forceinline__ void march_fp64(const DevView* views, const Rule& R, const Scratch sc) {
     WorkQueue* q = sc.q;
     const unsigned long long nband = q->band_count;
     const unsigned long long nprom = q->promo_count;
@@ -264,7 +277,6 @@ __device__ __forceinline__ void march_fp64(const DevView* views, const Scratch s
         const unsigned long long k = atomicAdd(&q->fp64_next, 1ull);
         if (k >= nband + nprom) break;
         RayState<double> s;
-        float b_axis, b;
         int ray, vs;
         uint32_t base_steps = 0;
         if (k < nband) {
@@ -274,8 +286,7 @@ __device__ __forceinline__ void march_fp64(const DevView* views, const Scratch s
             const DevView& w = views[vs];
             const int j = ray / w.width;
             const int i = ray - j * w.width;
-            V3<double> dir;
-            const RayInit<double> ri = setup_ray<double>(w, i, j, &dir);
+            const RayInit<double> ri = setup_ray<double>(w, R, i, j);
             s.x = {w.cam_d[0], w.cam_d[1], w.cam_d[2]};
             s.v = ri.v;
             s.h2 = ri.h2;
@@ -283,11 +294,7 @@ __device__ __forceinline__ void march_fp64(const DevView* views, const Scratch s
             s.min_r = __longlong_as_double(0x7ff0000000000000ll);
             s.steps = 0;
             s.info = 0;
-            b_axis = (float)ri.b_axis;
-            b = (float)ri.b;
-            float4* p = reinterpret_cast<float4*>(w.out + ray);
-            p[2] = make_float4(0.f, 0.f, 0.f, 0.f);
-            p[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+            write_start(w.out + ray, (float)ri.b_axis, (float)ri.b);
             ++nrays;
         } else {
             const PromoEntry& e = sc.promo[k - nband];
@@ -297,8 +304,7 @@ __device__ __forceinline__ void march_fp64(const DevView* views, const Scratch s
             // continue from the FP32 state; h2 and the step factor are recomputed in FP64
             const int j = ray / w.width;
             const int i = ray - j * w.width;
-            V3<double> dir;
-            const RayInit<double> ri = setup_ray<double>(w, i, j, &dir);
+            const RayInit<double> ri = setup_ray<double>(w, R, i, j);
             s.x = {e.x[0], e.x[1], e.x[2]};
             s.v = {e.v[0], e.v[1], e.v[2]};
             s.h2 = ri.h2;
@@ -307,20 +313,17 @@ __device__ __forceinline__ void march_fp64(const DevView* views, const Scratch s
             s.steps = e.steps;
             s.info = e.info;
             base_steps = e.steps;
-            b_axis = e.b_axis;
-            b = e.b;
         }
         const DevView& w = views[vs];
         bhr_hit* rec = w.out + ray;
-        while (!march_step<double, false>(w, s, rec)) {
+        while (!march_step<double, -1, -1, false>(R, w.max_steps, (double)w.disk_step, s, rec)) {
         }
         steps_sum += s.steps - base_steps;
-        nonfinite += (s.info >> 16) & 1u;
-        write_hit(rec, s.info, s.steps, (float)s.min_r, exit_dir(s, w.lensing != 0), b_axis, b, BHR_FLAG_FP64);
-        if constexpr (kMulti) {
-            const unsigned long long old = atomicAdd(&q->view_done[vs], 1ull);
-            if (old + 1 == (unsigned long long)w.nrays) q->view_t_end[vs] = globaltimer();
-        }
+        const bool bad = nonfinite_state(s);
+        nonfinite += bad ? 1 : 0;
+        write_end(rec, s.info, s.steps, (float)s.min_r, exit_dir(s, R.lensing != 0),
+                  BHR_FLAG_FP64 | (bad ? BHR_FLAG_NONFINITE : 0u));
+        if constexpr (kMulti) atomicMax(&q->view_t_end[vs], globaltimer());
     }
     if (steps_sum | nrays | nonfinite) {
         atomicAdd(&q->fp64_steps, steps_sum);
@@ -332,20 +335,21 @@ __device__ __forceinline__ void march_fp64(const DevView* views, const Scratch s
 
 }  // namespace
 
-template <int BS, bool kMixed>
-__global__ void __launch_bounds__(BS) k_march_one(const __grid_constant__ DevView view, const Scratch sc,
-                                                  int chunk, int refill_min) {
-    __shared__ float s_pool[BS / 32][8 * kPool];
+template <int BS, int kTerm, int kDisk, bool kMixed>
+__global__ void __launch_bounds__(BS) k_march_one(const __grid_constant__ DevView view, const __grid_constant__ Rule rule,
+                                                  const Scratch sc, int chunk, int refill_min) {
+    __shared__ float s_pool[BS / 32][kPoolFields * kPool];
     note_start(sc.q);
     const int wid = threadIdx.x >> 5;
     const int64_t total_chunks = (view.nrays + chunk - 1) / chunk;
-    march_warp<false, kMixed>(&view, 1, total_chunks, sc, chunk, refill_min, Pool{s_pool[wid], nullptr});
+    march_warp<false, kTerm, kDisk, kMixed>(&view, 1, total_chunks, rule, sc, chunk, refill_min,
+                                            Pool{s_pool[wid], nullptr});
 }
 
-template <int BS, bool kMixed>
+template <int BS, int kTerm, int kDisk, bool kMixed>
 __global__ void __launch_bounds__(BS) k_march_multi(const __grid_constant__ ViewBatch batch, const Scratch sc,
                                                     int chunk, int refill_min) {
-    __shared__ float s_pool[BS / 32][8 * kPool];
+    __shared__ float s_pool[BS / 32][kPoolFields * kPool];
     __shared__ uint8_t s_pool_view[BS / 32][kPool];
     __shared__ DevView s_views[kMaxViews];
     note_start(sc.q);
@@ -354,62 +358,85 @@ __global__ void __launch_bounds__(BS) k_march_multi(const __grid_constant__ View
         reinterpret_cast<uint32_t*>(s_views)[k] = reinterpret_cast<const uint32_t*>(batch.views)[k];
     __syncthreads();
     const int wid = threadIdx.x >> 5;
-    march_warp<true, kMixed>(s_views, batch.nviews, batch.total_chunks, sc, chunk, refill_min,
-                             Pool{s_pool[wid], s_pool_view[wid]});
+    march_warp<true, kTerm, kDisk, kMixed>(s_views, batch.nviews, batch.total_chunks, batch.rule, sc, chunk,
+                                           refill_min, Pool{s_pool[wid], s_pool_view[wid]});
 }
 
-__global__ void __launch_bounds__(128) k_march_fp64_one(const __grid_constant__ DevView view, const Scratch sc) {
-    march_fp64<false>(&view, sc);
+__global__ void __launch_bounds__(128) k_march_fp64_one(const __grid_constant__ DevView view,
+                                                        const __grid_constant__ Rule rule, const Scratch sc) {
+    march_fp64<false>(&view, rule, sc);
 }
 
 __global__ void __launch_bounds__(128) k_march_fp64_multi(const __grid_constant__ ViewBatch batch,
                                                           const Scratch sc) {
-    march_fp64<true>(batch.views, sc);
+    march_fp64<true>(batch.views, batch.rule, sc);
 }
 
 // ---------------------------------------------------------------------------------------
-// launchers
-template <int BS>
-static cudaError_t launch_one_bs(const DevView& v, const Scratch& s, bool mixed, const LaunchCfg& c,
-                                 cudaStream_t st) {
-    if (mixed)
-        k_march_one<BS, true><<<c.grid, BS, 0, st>>>(v, s, c.chunk, c.refill);
-    else
-        k_march_one<BS, false><<<c.grid, BS, 0, st>>>(v, s, c.chunk, c.refill);
-    return cudaGetLastError();
-}
+// dispatch: (term, disk) -> compiled variant; anything else runs the generic variant
+namespace {
 
-template <int BS>
-static cudaError_t launch_multi_bs(const ViewBatch& b, const Scratch& s, bool mixed, const LaunchCfg& c,
-                                   cudaStream_t st) {
-    if (mixed)
-        k_march_multi<BS, true><<<c.grid, BS, 0, st>>>(b, s, c.chunk, c.refill);
-    else
-        k_march_multi<BS, false><<<c.grid, BS, 0, st>>>(b, s, c.chunk, c.refill);
-    return cudaGetLastError();
-}
+template <int BS, int kTerm, int kDisk, bool kMixed>
+struct Kern {
+    static const void* one() { return (const void*)k_march_one<BS, kTerm, kDisk, kMixed>; }
+    static const void* multi() { return (const void*)k_march_multi<BS, kTerm, kDisk, kMixed>; }
+};
 
-cudaError_t launch_march_one(const DevView& v, const Scratch& s, bool mixed, const LaunchCfg& c, cudaStream_t st) {
-    switch (c.block) {
-        case 128: return launch_one_bs<128>(v, s, mixed, c, st);
-        case 256: return launch_one_bs<256>(v, s, mixed, c, st);
-        case 512: return launch_one_bs<512>(v, s, mixed, c, st);
-        default: return cudaErrorInvalidValue;
+template <int BS, bool kMixed>
+const void* pick(int variant, bool multi) {
+    switch (variant) {
+        case kVariantConfigThin:
+            return multi ? Kern<BS, BHR_TERM_CONFIG, BHR_DISK_THIN, kMixed>::multi()
+                         : Kern<BS, BHR_TERM_CONFIG, BHR_DISK_THIN, kMixed>::one();
+        case kVariantShaderThin:
+            return multi ? Kern<BS, BHR_TERM_SHADER, BHR_DISK_THIN, kMixed>::multi()
+                         : Kern<BS, BHR_TERM_SHADER, BHR_DISK_THIN, kMixed>::one();
+        case kVariantCpuNone:
+            return multi ? Kern<BS, BHR_TERM_CPU, BHR_DISK_NONE, kMixed>::multi()
+                         : Kern<BS, BHR_TERM_CPU, BHR_DISK_NONE, kMixed>::one();
+        default:
+            return multi ? Kern<BS, -1, -1, kMixed>::multi() : Kern<BS, -1, -1, kMixed>::one();
     }
+}
+
+const void* pick_kernel(int block, int variant, bool multi, bool mixed) {
+    switch (block) {
+        case 256: return mixed ? pick<256, true>(variant, multi) : pick<256, false>(variant, multi);
+        case 512: return mixed ? pick<512, true>(variant, multi) : pick<512, false>(variant, multi);
+        default: return nullptr;
+    }
+}
+
+}  // namespace
+
+int rule_variant(const Rule& r) {
+    if (!r.lensing || r.far_mode) return kVariantGeneric;
+    if (r.term_mode == BHR_TERM_CONFIG && r.disk_mode == BHR_DISK_THIN) return kVariantConfigThin;
+    if (r.term_mode == BHR_TERM_SHADER && r.disk_mode == BHR_DISK_THIN) return kVariantShaderThin;
+    if (r.term_mode == BHR_TERM_CPU && r.disk_mode == BHR_DISK_NONE) return kVariantCpuNone;
+    return kVariantGeneric;
+}
+
+cudaError_t launch_march_one(const DevView& v, const Rule& r, const Scratch& s, bool mixed, const LaunchCfg& c,
+                             cudaStream_t st) {
+    const void* fn = pick_kernel(c.block, c.variant, false, mixed);
+    if (!fn) return cudaErrorInvalidValue;
+    int chunk = c.chunk, refill = c.refill;
+    void* args[] = {(void*)&v, (void*)&r, (void*)&s, &chunk, &refill};
+    return cudaLaunchKernel(fn, dim3(c.grid), dim3(c.block), args, 0, st);
 }
 
 cudaError_t launch_march_multi(const ViewBatch& b, const Scratch& s, bool mixed, const LaunchCfg& c,
                                cudaStream_t st) {
-    switch (c.block) {
-        case 128: return launch_multi_bs<128>(b, s, mixed, c, st);
-        case 256: return launch_multi_bs<256>(b, s, mixed, c, st);
-        case 512: return launch_multi_bs<512>(b, s, mixed, c, st);
-        default: return cudaErrorInvalidValue;
-    }
+    const void* fn = pick_kernel(c.block, c.variant, true, mixed);
+    if (!fn) return cudaErrorInvalidValue;
+    int chunk = c.chunk, refill = c.refill;
+    void* args[] = {(void*)&b, (void*)&s, &chunk, &refill};
+    return cudaLaunchKernel(fn, dim3(c.grid), dim3(c.block), args, 0, st);
 }
 
-cudaError_t launch_march_fp64_one(const DevView& v, const Scratch& s, int grid, cudaStream_t st) {
-    k_march_fp64_one<<<grid, 128, 0, st>>>(v, s);
+cudaError_t launch_march_fp64_one(const DevView& v, const Rule& r, const Scratch& s, int grid, cudaStream_t st) {
+    k_march_fp64_one<<<grid, 128, 0, st>>>(v, r, s);
     return cudaGetLastError();
 }
 
@@ -418,25 +445,12 @@ cudaError_t launch_march_fp64_multi(const ViewBatch& b, const Scratch& s, int gr
     return cudaGetLastError();
 }
 
-template <int BS>
-static int bps(bool multi, bool mixed) {
+int march_blocks_per_sm(int block, int variant, bool multi, bool mixed) {
+    const void* fn = pick_kernel(block, variant, multi, mixed);
+    if (!fn) return 0;
     int n = 0;
-    if (multi)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, mixed ? (const void*)k_march_multi<BS, true> : (const void*)k_march_multi<BS, false>, BS, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, mixed ? (const void*)k_march_one<BS, true> : (const void*)k_march_one<BS, false>, BS, 0);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, 0) != cudaSuccess) return 0;
     return n;
-}
-
-int march_blocks_per_sm(int block, bool multi, bool mixed) {
-    switch (block) {
-        case 128: return bps<128>(multi, mixed);
-        case 256: return bps<256>(multi, mixed);
-        case 512: return bps<512>(multi, mixed);
-        default: return 0;
-    }
 }
 
 }  // namespace bhr

@@ -21,26 +21,26 @@ struct WorkQueue {
     unsigned long long fp64_steps;   // steps taken in FP64
     unsigned long long nonfinite;    // rays that met a non-finite state
     unsigned long long t_start;      // globaltimer when the first block started
-    unsigned long long view_done[kMaxViews];   // finished rays per view
     unsigned long long view_t_end[kMaxViews];  // globaltimer when a view's last ray finished
 };
 
-// An FP32 ray state handed to the FP64 pass (mixed precision). 64 bytes.
+// An FP32 ray state handed to the FP64 pass (mixed precision). 48 bytes.
 struct PromoEntry {
-    int64_t ray;       // ray index within its view
+    int32_t ray;       // ray index within its view
     int32_t view;      // view slot in the launch
     uint32_t steps;    // steps already taken
     uint32_t info;     // nplane / ncross bits (status cleared)
     float x[3], v[3];
-    float min_r, b_axis, b;
-    uint32_t pad[2];
+    float min_r;
+    uint32_t pad;
 };
 
-// Several views for one persistent launch, passed as a __grid_constant__ parameter.
+// Several views sharing one rule, for one persistent launch (a __grid_constant__ parameter).
 struct ViewBatch {
     int32_t nviews;
     int32_t pad;
     int64_t total_chunks;
+    Rule rule;
     DevView views[kMaxViews];
 };
 
@@ -50,19 +50,25 @@ struct Scratch {
     PromoEntry* promo;  // promoted FP32 states
 };
 
+// Compiled specialisations of the loop body (lensing on, no far mode).
+enum : int { kVariantGeneric = 0, kVariantConfigThin = 1, kVariantShaderThin = 2, kVariantCpuNone = 3 };
+
 struct LaunchCfg {
-    int block;   // 128, 256 or 512
-    int grid;    // persistent blocks
-    int chunk;   // rays per work chunk
-    int refill;  // idle lanes that trigger a refill (1..32)
+    int block;    // 256 or 512
+    int grid;     // persistent blocks
+    int chunk;    // rays per work chunk
+    int refill;   // idle lanes that trigger a refill (1..32)
+    int variant;  // kVariant*
 };
 
-cudaError_t launch_march_one(const DevView& v, const Scratch& s, bool mixed, const LaunchCfg& c, cudaStream_t st);
+int rule_variant(const Rule& r);
+cudaError_t launch_march_one(const DevView& v, const Rule& r, const Scratch& s, bool mixed, const LaunchCfg& c,
+                             cudaStream_t st);
 cudaError_t launch_march_multi(const ViewBatch& b, const Scratch& s, bool mixed, const LaunchCfg& c,
                                cudaStream_t st);
-cudaError_t launch_march_fp64_one(const DevView& v, const Scratch& s, int grid, cudaStream_t st);
+cudaError_t launch_march_fp64_one(const DevView& v, const Rule& r, const Scratch& s, int grid, cudaStream_t st);
 cudaError_t launch_march_fp64_multi(const ViewBatch& b, const Scratch& s, int grid, cudaStream_t st);
-// Max resident blocks per SM of the FP32 march kernel for a block size (occupancy API).
-int march_blocks_per_sm(int block, bool multi, bool mixed);
+// Max resident blocks per SM of an FP32 march kernel (occupancy API).
+int march_blocks_per_sm(int block, int variant, bool multi, bool mixed);
 
 }  // namespace bhr

@@ -107,8 +107,9 @@ typedef struct bhr_view {
 
 /* Per-pixel hit record: the march state blackhole.frag's shading reads after the loop
  * (status/escDir :97-98, the crossing points handed to thinDiskSample :209-216, bAxis :88)
- * plus the fields of the CPU mirror's TraceResult (Geodesic.h:97-103). 64 bytes, written
- * as four 16-byte stores. */
+ * plus the fields of the CPU mirror's TraceResult (Geodesic.h:97-103). 64 bytes = four
+ * 16-byte words: the first two are written when the ray ends, the last two when it starts
+ * (b_axis, b) and at each recorded crossing. */
 typedef struct bhr_hit {
     uint8_t status;        /* BHR_STATUS_* */
     uint8_t ncross;        /* crossings recorded below (r in [disk_inner, disk_outer]), 0..3 */
@@ -116,12 +117,12 @@ typedef struct bhr_hit {
     uint8_t nplane;        /* all y = 0 plane crossings (TraceResult::equatorCrossings), saturating */
     uint32_t steps;        /* march steps executed */
     float dir[3];          /* escDir (unit) when status is ESCAPED, else zero (as TraceResult::dir) */
+    float min_r;           /* smallest r seen at the loop head (TraceResult::minR) */
+    float reserved[2];
     float b_axis;          /* impactParameterAboutAxis(camPos, dir, +Y) */
     float b;               /* impact parameter h / |v| at the camera */
-    float min_r;           /* smallest r seen at the loop head (TraceResult::minR) */
     float cross_r[3];      /* |hit.xz| of recorded crossings, march order (disk.glsl:114) */
     float cross_phi[3];    /* atan(hit.z, hit.x) of recorded crossings (disk.glsl:116) */
-    float reserved[2];
 } bhr_hit;
 
 typedef struct bhr_ctx bhr_ctx;
@@ -178,6 +179,13 @@ int64_t bhr_view_rays(const bhr_view* v);
  * shared work queue. Work memory (queue counters, FP64 hand-off queue) is owned by ctx. */
 int bhr_trace(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
               int precision, int method, void* cuda_stream);
+/* Host-memory variant for callers without device buffers (the CPU mirror's trace() callers):
+ * traces into context-owned device staging and copies every view's records to out_host[k]
+ * (width*height records each), overlapping the copies of one group of views with the trace
+ * of the next. Synchronous: returns after all records are on the host. Pinned host buffers
+ * (cudaHostAlloc) let the copies run asynchronously. */
+int bhr_trace_host(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* out_host,
+                   int precision, int method);
 /* Statistics of the last bhr_trace on ctx (synchronises that call's stream). */
 int bhr_trace_stats(bhr_ctx* ctx, bhr_stats* stats);
 /* Per-view latency of the last multi-view bhr_trace: milliseconds from the start of the
