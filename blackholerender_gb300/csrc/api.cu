@@ -103,6 +103,7 @@ bhr::DevView make_dev_view(const bhr_view& v, bhr_hit* out) {
     for (int k = 0; k < 3; ++k) d.rhat[k] = p[k] / d.rcam;
     d.lapse = std::sqrt(std::max(1.0f - 2.0f / d.rcam, 0.0f));
     d.baxis_scale = 1.0f / std::sqrt(std::max(1.0f - 2.0f / d.rcam, 1e-6f));
+    d.two_over_r3 = 2.0f / (d.rcam * d.rcam * d.rcam);
     d.step_scale = v.step_scale;
     d.disk_step = v.disk_step;
     for (int k = 0; k < 3; ++k) d.cam_d[k] = double(v.cam_pos[k]);

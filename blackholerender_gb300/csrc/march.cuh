@@ -46,7 +46,7 @@ struct DevView {
     float lapse;         // sqrt(max(1 - 2/rcam, 0))          initialVelocity
     float baxis_scale;   // inversesqrt(max(1 - 2/rcam, 1e-6))  impactParameterAboutAxis
     float step_scale, disk_step;
-    int32_t pad;
+    float two_over_r3;   // 2 / rcam^3 (impact parameter from h)
     double cam_d[3];     // the same float uniforms promoted, for the FP64 path
     int64_t chunk_start; // first work chunk of this view (multi-view launches)
     int64_t nrays;       // width * height
@@ -85,7 +85,7 @@ template <class T> struct RayInit {
     T h2;        // |x × v|^2
     T ssf;       // step_scale * farMul (shader rule) or step_scale (CPU rule)
     T b_axis;    // impactParameterAboutAxis(camPos, dir, +Y)
-    T b;         // h / |v|
+    T b;         // impact parameter h / |v_inf|
 };
 
 // blackhole.frag:68-93 for pixel (i, j) of view w, in arithmetic type T.
@@ -96,7 +96,10 @@ __device__ __forceinline__ RayInit<T> setup_ray(const DevView& w, const Rule& R,
     const T ndcx = pxx / T(w.width) * T(2) - T(1);
     const T ndcy = pxy / T(w.height) * T(2) - T(1);
     const T th = T(w.tan_half);
-    V3<T> dc{ndcx * th * T(w.aspect), ndcy * th, T(-1)};
+    // uResolution.x / uResolution.y: float in the shader, double on the FP64 path (near the
+    // photon sphere a 1e-8 change of direction moves the exit direction by ~1e-3 rad)
+    const T aspect = sizeof(T) == 8 ? T(w.width) / T(w.height) : T(w.aspect);
+    V3<T> dc{ndcx * th * aspect, ndcy * th, T(-1)};
     T inv = M<T>::rsqrt(dot3(dc, dc));
     dc = {dc.x * inv, dc.y * inv, dc.z * inv};
     V3<T> d{T(w.basis[0]) * dc.x + T(w.basis[3]) * dc.y + T(w.basis[6]) * dc.z,
@@ -133,7 +136,15 @@ __device__ __forceinline__ RayInit<T> setup_ray(const DevView& w, const Rule& R,
         o.v = v;
         o.h2 = dot3(hv, hv);
         const T h = M<T>::sqrt(o.h2);
-        o.b = h * M<T>::rsqrt(dot3(v, v));
+        // b = h / |v_inf| with |v_inf|^2 = |v|^2 - 2 h2 / r^3 (Geodesic.h:50-54 impactParameter)
+        T two_over_r3;
+        if constexpr (sizeof(T) == 8) {
+            const double r = ::sqrt(dot3(cam, cam));
+            two_over_r3 = 2.0 / (r * r * r);
+        } else {
+            two_over_r3 = w.two_over_r3;
+        }
+        o.b = h * M<T>::rsqrt(dot3(v, v) - o.h2 * two_over_r3);
         T far_mul = T(1);
         if (R.term_mode != BHR_TERM_CPU) far_mul = M<T>::fmin(M<T>::fmax((h - T(6)) / T(3), T(1)), T(3));
         o.ssf = T(w.step_scale) * far_mul;

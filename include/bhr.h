@@ -120,7 +120,7 @@ typedef struct bhr_hit {
     float min_r;           /* smallest r seen at the loop head (TraceResult::minR) */
     float reserved[2];
     float b_axis;          /* impactParameterAboutAxis(camPos, dir, +Y) */
-    float b;               /* impact parameter h / |v| at the camera */
+    float b;               /* impact parameter h / |v_inf| (Geodesic.h:50-54 impactParameter) */
     float cross_r[3];      /* |hit.xz| of recorded crossings, march order (disk.glsl:114) */
     float cross_phi[3];    /* atan(hit.z, hit.x) of recorded crossings (disk.glsl:116) */
 } bhr_hit;

@@ -175,7 +175,12 @@ template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {
         h = std::sqrt(h2);
     }
     res.b_axis = impactParameterAboutY(camPos, dir);
-    res.b = lensing ? h / length(v) : T(0);
+    // impact parameter b = h / |v_inf|, |v_inf|^2 = |v|^2 - 2 h^2 / r^3 (energy integral of
+    // x'' = -3 h^2 x / r^5); equals Geodesic.h:50-54 impactParameter = r sin(alpha) / sqrt(1 - 2/r)
+    if (lensing) {
+        const T rc = length(camPos);
+        res.b = h / std::sqrt(dot(v, v) - T(2) * h2 / (rc * rc * rc));
+    }
     const bool shader_rule = R.term_mode != BHR_TERM_CPU;
     const T farMul = shader_rule ? std::clamp((h - T(6)) / T(3), T(1), T(3)) : T(1);
     const T slab = T(2.5) * R.disk_thickness;  // diskSlabHalfHeight(r) = slab * r (disk.glsl:24)

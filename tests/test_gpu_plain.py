@@ -30,17 +30,14 @@ def _run(tr, view):
 def test_c1_full_image(tracer, term):
     v = workloads.c1_view(term)
     gpu = _run(tracer, v)
-    ref = O.trace_view(v, fp64=True)
-    rep = parity.compare(gpu, ref, max_steps=v.max_steps)
-    parity.assert_fp32_parity(rep, f"C1 term={term}")
+    rep = parity.check_fp32(gpu, v, where=f"C1 term={term}")
     assert rep.n_compared > 0.95 * rep.n
 
 
 def test_c2_pose0_reduced(tracer):
     v = workloads.c2_views(TERM_CONFIG, width=480, height=270)[0]
     gpu = _run(tracer, v)
-    ref = O.trace_view(v, fp64=True)
-    parity.assert_fp32_parity(parity.compare(gpu, ref, max_steps=v.max_steps), "C2 pose0 480x270")
+    parity.check_fp32(gpu, v, where="C2 pose0 480x270")
 
 
 def test_c2_full_res_sampled(tracer):
@@ -49,13 +46,11 @@ def test_c2_full_res_sampled(tracer):
     for v in views[:4]:
         gpu = _run(tracer, v)
         idx = rng.choice(v.rays, 4000, replace=False)
-        ref = O.trace_pixels(v, idx, fp64=True)
-        parity.assert_fp32_parity(parity.compare(gpu[idx], ref, max_steps=v.max_steps), "C2 1080p sample")
+        parity.check_fp32(gpu, v, idx, where="C2 1080p sample")
 
 
 def test_cpu_rule(tracer):
     v = make_view(TERM_CPU, width=96, height=54, fov_deg=60.0, pose=(25.0, 1.4, 0.3), max_steps=20000,
                   step_scale=0.02)
     gpu = _run(tracer, v)
-    ref = O.trace_view(v, fp64=True)
-    parity.assert_fp32_parity(parity.compare(gpu, ref, max_steps=v.max_steps), "CPU rule")
+    parity.check_fp32(gpu, v, where="CPU rule")
