@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "bhr.h"
+#include "host_views.h"
 #include "kernels.cuh"
 
 struct bhr_ctx {
@@ -57,84 +58,15 @@ int cuda_fail(bhr_ctx* c, cudaError_t e, const char* what) {
     return fail(c, BHR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-bool finite3f(const float* a) { return std::isfinite(a[0]) && std::isfinite(a[1]) && std::isfinite(a[2]); }
-
-// blackhole.frag:89: rEscMin = max(uDiskOuter * 1.25, 12.0)
-float shader_r_esc_min(float disk_outer) { return std::max(disk_outer * 1.25f, 12.0f); }
-
 int check_view(bhr_ctx* c, const bhr_view& v, int k) {
-    char buf[160];
-    auto bad = [&](const char* what) {
-        std::snprintf(buf, sizeof buf, "view %d: %s", k, what);
-        return fail(c, BHR_ERR_INVALID_ARG, buf);
-    };
-    if (v.width <= 0 || v.height <= 0) return bad("width and height must be positive");
-    if (int64_t(v.width) * v.height > int64_t(INT32_MAX)) return bad("width * height exceeds 2^31 - 1 rays");
-    if (v.max_steps < 0) return bad("max_steps must be >= 0");
-    if (v.disk_mode == BHR_DISK_VOLUMETRIC)
-        return fail(c, BHR_ERR_UNSUPPORTED, "view " + std::to_string(k) + ": volumetric disk is not supported");
-    if (v.disk_mode != BHR_DISK_NONE && v.disk_mode != BHR_DISK_THIN) return bad("unknown disk_mode");
-    if (v.term_mode < BHR_TERM_SHADER || v.term_mode > BHR_TERM_CPU) return bad("unknown term_mode");
-    if (!finite3f(v.cam_pos)) return bad("camera position is not finite");
-    for (float e : v.cam_basis)
-        if (!std::isfinite(e)) return bad("camera basis is not finite");
-    if (!(v.tan_half_fov > 0.0f) || !std::isfinite(v.tan_half_fov)) return bad("tan_half_fov must be positive");
-    if (!(v.step_scale > 0.0f) || !(v.ds_floor >= 0.0f)) return bad("step_scale must be > 0 and ds_floor >= 0");
-    const float rc = std::sqrt(v.cam_pos[0] * v.cam_pos[0] + v.cam_pos[1] * v.cam_pos[1] + v.cam_pos[2] * v.cam_pos[2]);
-    if (!(rc > 0.0f)) return bad("camera at the origin");
-    return BHR_OK;
+    std::string msg;
+    const int rc = bhr::host::check_view(v, k, &msg);
+    return rc == BHR_OK ? BHR_OK : fail(c, rc, msg);
 }
 
-// setTraceUniforms (Renderer.cpp:242-356) + the per-ray constants of blackhole.frag:77-89 that
-// depend only on the view, in float with the reference's operation order.
-bhr::DevView make_dev_view(const bhr_view& v, bhr_hit* out) {
-    bhr::DevView d{};
-    for (int k = 0; k < 3; ++k) d.cam[k] = v.cam_pos[k];
-    for (int k = 0; k < 9; ++k) d.basis[k] = v.cam_basis[k];
-    d.tan_half = v.tan_half_fov;
-    d.jitter[0] = v.jitter[0];
-    d.jitter[1] = v.jitter[1];
-    d.width = v.width;
-    d.height = v.height;
-    d.max_steps = v.max_steps;
-    d.aspect = float(v.width) / float(v.height);
-    const float* p = v.cam_pos;
-    d.rcam = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-    for (int k = 0; k < 3; ++k) d.rhat[k] = p[k] / d.rcam;
-    d.lapse = std::sqrt(std::max(1.0f - 2.0f / d.rcam, 0.0f));
-    d.baxis_scale = 1.0f / std::sqrt(std::max(1.0f - 2.0f / d.rcam, 1e-6f));
-    d.two_over_r3 = 2.0f / (d.rcam * d.rcam * d.rcam);
-    d.step_scale = v.step_scale;
-    d.disk_step = v.disk_step;
-    for (int k = 0; k < 3; ++k) d.cam_d[k] = double(v.cam_pos[k]);
-    d.chunk_start = 0;
-    d.nrays = int64_t(v.width) * v.height;
-    d.out = out;
-    return d;
-}
-
-// The launch-wide constants of a view: termination rule and disk geometry.
-bhr::Rule make_rule(const bhr_view& v) {
-    bhr::Rule r{};
-    r.capture_r = v.capture_r;
-    r.escape_r = v.escape_r;
-    r.esc_tol = v.esc_tol;
-    r.r_esc_min = v.term_mode == BHR_TERM_SHADER ? shader_r_esc_min(v.disk_outer) : v.r_esc_min;
-    r.ds_floor = v.ds_floor;
-    r.slab = 2.5f * v.disk_thickness;
-    const float lo = v.disk_inner - 1.0f, hi = v.disk_outer + 1.0f;
-    r.rcyl_lo2 = lo > 0.0f ? lo * lo : -1.0f;
-    r.rcyl_hi2 = hi > 0.0f ? hi * hi : -1.0f;
-    r.disk_inner = v.disk_inner;
-    r.disk_outer = v.disk_outer;
-    r.promote_r = v.promote_r;
-    r.promote_band = v.promote_band;
-    r.term_mode = v.term_mode;
-    r.disk_mode = v.disk_mode;
-    r.lensing = (v.lensing != 0 && v.far_mode == 0) ? 1 : 0;
-    r.far_mode = v.far_mode != 0 ? 1 : 0;
-    return r;
-}
+using bhr::host::make_dev_view;
+using bhr::host::make_rule;
+using bhr::host::shader_r_esc_min;
 
 bool same_rule(const bhr::Rule& a, const bhr::Rule& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
 
@@ -174,6 +106,8 @@ bhr::LaunchCfg make_cfg(const bhr_ctx* c, int variant, bool multi, bool mixed) {
 }
 
 }  // namespace
+
+void bhr::set_last_error(const std::string& msg) { fail(nullptr, BHR_ERR_INVALID_ARG, msg); }
 
 extern "C" {
 
