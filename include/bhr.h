@@ -186,6 +186,19 @@ int bhr_trace(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* o
  * (cudaHostAlloc) let the copies run asynchronously. */
 int bhr_trace_host(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* out_host,
                    int precision, int method);
+/* Mixed-precision trace of one view (as bhr_trace with BHR_PREC_MIXED, BHR_METHOD_PLAIN) for
+ * callers that cannot allocate device memory: a render loop that must not stall on cudaMalloc
+ * and cudaFree (they synchronise the device), a host whose memory pool owns all device memory,
+ * or code recording a CUDA graph. This entry point has no counterpart in the reference. It needs
+ * no context and allocates nothing: its work memory is one static device array of about 15 MB,
+ * held by every GPU that loads the library until the process exits, and sized for at most
+ * 262144 rays (e.g. 512x512 or 640x360) per call; larger views are rejected with
+ * BHR_ERR_INVALID_ARG. Runs on the current device and on cuda_stream; errors are reported by
+ * bhr_last_error(NULL). Every call shares that array: calls that overlap on the GPU (other
+ * streams or host threads) race, calls on one stream are ordered. The first call on a device
+ * resolves the array's device address (cudaGetSymbolAddress, which may load the module): make
+ * it before any stream capture. */
+int bhr_trace_noalloc(const bhr_view* view, bhr_hit* out_dev, void* cuda_stream);
 /* Statistics of the last bhr_trace on ctx (synchronises that call's stream). */
 int bhr_trace_stats(bhr_ctx* ctx, bhr_stats* stats);
 /* Per-view latency of the last multi-view bhr_trace: milliseconds from the start of the
