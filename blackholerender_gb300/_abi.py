@@ -149,6 +149,37 @@ SIGNATURES = {
     "bhr_trace_view_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
 }
 
+class SurrogateConfig(ctypes.Structure):
+    _fields_ = [
+        ("rc_lo", ctypes.c_float), ("rc_hi", ctypes.c_float), ("b_max", ctypes.c_float), ("band", ctypes.c_float),
+        ("t_eps", ctypes.c_float), ("t_scale", ctypes.c_float), ("y_scale", ctypes.c_float),
+        ("escape_r", ctypes.c_float), ("reserved", ctypes.c_int32 * 8),
+    ]
+
+
+_F = ctypes.POINTER(ctypes.c_float)
+SIGNATURES.update({
+    "bhr_surrogate_default_config": (ctypes.c_int, [ctypes.POINTER(SurrogateConfig)]),
+    "bhr_surrogate_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(SurrogateConfig),
+                                            ctypes.c_uint64]),
+    "bhr_surrogate_destroy": (ctypes.c_int, [_P]),
+    "bhr_surrogate_generate": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64, _P,
+                                              ctypes.POINTER(ctypes.c_uint64)]),
+    "bhr_surrogate_train": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_float, ctypes.c_uint64, _P, _F]),
+    "bhr_surrogate_samples": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _F, ctypes.POINTER(ctypes.c_int8)]),
+    "bhr_surrogate_param_count": (ctypes.c_int, []),
+    "bhr_surrogate_params": (ctypes.c_int, [_P, _F, ctypes.c_int]),
+    "bhr_surrogate_set_params": (ctypes.c_int, [_P, _F, ctypes.c_int]),
+    "bhr_surrogate_gradients": (ctypes.c_int, [_P, _F, ctypes.POINTER(ctypes.c_int8), ctypes.c_int, ctypes.c_float,
+                                               _F, _F]),
+    "bhr_surrogate_eval": (ctypes.c_int, [_P, _F, ctypes.c_int, _F]),
+    "bhr_surrogate_save": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "bhr_surrogate_load": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "bhr_surrogate_trace": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), _P]),
+    "bhr_surrogate_trace_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+})
+
 _lib = None
 
 

@@ -17,7 +17,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libbhr.so"
-SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu"]
+SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu", "surrogate_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

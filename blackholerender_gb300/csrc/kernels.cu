@@ -87,9 +87,12 @@ __device__ __forceinline__ unsigned long long warp_append(unsigned long long* ct
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
-template <bool kMulti, int kTerm, int kDisk, bool kMixed>
+// kList: the rays of view 0 are the `list_len` pixel indices in `list` (the surrogate's
+// fallback rays), written with BHR_FLAG_FALLBACK.
+template <bool kMulti, int kTerm, int kDisk, bool kMixed, bool kList = false>
 __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int64_t total_chunks, const Rule& R,
-                                           const Scratch sc, int chunk, int refill_min, Pool pool) {
+                                           const Scratch sc, int chunk, int refill_min, Pool pool,
+                                           const int* list = nullptr, int64_t list_len = 0) {
     WorkQueue* q = sc.q;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -135,7 +138,7 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                 } else {
                     const bool bad = nonfinite_state(s);
                     write_end(rec, s.info, s.steps, s.min_r, exit_dir(s, R.lensing != 0),
-                              bad ? BHR_FLAG_NONFINITE : 0u);
+                              (bad ? BHR_FLAG_NONFINITE : 0u) | (kList ? BHR_FLAG_FALLBACK : 0u));
                     nonfinite += bad ? 1 : 0;
                 }
                 steps_sum += s.steps;
@@ -176,13 +179,13 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                     }
                     cview = v;
                     cbeg = ((int64_t)base - views[v].chunk_start) * chunk;
-                    cend = min(cbeg + (int64_t)chunk, views[v].nrays);
+                    cend = min(cbeg + (int64_t)chunk, kList ? list_len : views[v].nrays);
                 }
                 const int n = (int)min((int64_t)32, cend - cbeg);
                 const DevView& w = views[cview];
                 bool keep = false;
                 RayInit<float> ri;
-                const int my = (int)(cbeg + lane);
+                const int my = kList ? (lane < n ? list[cbeg + lane] : 0) : (int)(cbeg + lane);
                 if (lane < n) {
                     const int j = my / w.width;
                     const int i = my - j * w.width;
@@ -362,6 +365,19 @@ __global__ void __launch_bounds__(BS) k_march_multi(const __grid_constant__ View
                                            refill_min, Pool{s_pool[wid], s_pool_view[wid]});
 }
 
+template <int kTerm, int kDisk>
+__global__ void __launch_bounds__(512) k_march_list(const __grid_constant__ DevView view,
+                                                    const __grid_constant__ Rule rule, const Scratch sc,
+                                                    const int* list, const unsigned long long* list_len, int chunk,
+                                                    int refill_min) {
+    __shared__ float s_pool[512 / 32][kPoolFields * kPool];
+    const int wid = threadIdx.x >> 5;
+    const int64_t n = (int64_t)*list_len;
+    const int64_t total_chunks = (n + chunk - 1) / chunk;
+    march_warp<false, kTerm, kDisk, false, true>(&view, 1, total_chunks, rule, sc, chunk, refill_min,
+                                                 Pool{s_pool[wid], nullptr}, list, n);
+}
+
 __global__ void __launch_bounds__(128) k_march_fp64_one(const __grid_constant__ DevView view,
                                                         const __grid_constant__ Rule rule, const Scratch sc) {
     march_fp64<false>(&view, rule, sc);
@@ -443,6 +459,21 @@ cudaError_t launch_march_fp64_one(const DevView& v, const Rule& r, const Scratch
 cudaError_t launch_march_fp64_multi(const ViewBatch& b, const Scratch& s, int grid, cudaStream_t st) {
     k_march_fp64_multi<<<grid, 128, 0, st>>>(b, s);
     return cudaGetLastError();
+}
+
+cudaError_t launch_march_list(const DevView& v, const Rule& r, const Scratch& s, const int* list,
+                              const unsigned long long* list_len, const LaunchCfg& c, cudaStream_t st) {
+    int chunk = c.chunk, refill = c.refill;
+    const void* fn;
+    switch (c.variant) {
+        case kVariantConfigThin: fn = (const void*)k_march_list<BHR_TERM_CONFIG, BHR_DISK_THIN>; break;
+        case kVariantShaderThin: fn = (const void*)k_march_list<BHR_TERM_SHADER, BHR_DISK_THIN>; break;
+        case kVariantCpuNone: fn = (const void*)k_march_list<BHR_TERM_CPU, BHR_DISK_NONE>; break;
+        default: fn = (const void*)k_march_list<-1, -1>; break;
+    }
+    const int grid = c.grid > 0 ? c.grid : 1;
+    void* args[] = {(void*)&v, (void*)&r, (void*)&s, (void*)&list, (void*)&list_len, &chunk, &refill};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(512), args, 0, st);
 }
 
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed) {

@@ -21,6 +21,9 @@ struct WorkQueue {
     unsigned long long fp64_steps;   // steps taken in FP64
     unsigned long long nonfinite;    // rays that met a non-finite state
     unsigned long long t_start;      // globaltimer when the first block started
+    unsigned long long surr_rays;    // rays answered by the surrogate
+    unsigned long long fb_count;     // rays the surrogate sent to the integrator
+    unsigned long long capture_disagree;  // surrogate capture flag disagreed with b vs sqrt(27)
     unsigned long long view_t_end[kMaxViews];  // globaltimer when a view's last ray finished
 };
 
@@ -68,6 +71,9 @@ cudaError_t launch_march_multi(const ViewBatch& b, const Scratch& s, bool mixed,
                                cudaStream_t st);
 cudaError_t launch_march_fp64_one(const DevView& v, const Rule& r, const Scratch& s, int grid, cudaStream_t st);
 cudaError_t launch_march_fp64_multi(const ViewBatch& b, const Scratch& s, int grid, cudaStream_t st);
+// The FP32 march over a list of pixel indices of one view (512 threads per block, c.grid blocks).
+cudaError_t launch_march_list(const DevView& v, const Rule& r, const Scratch& s, const int* list,
+                              const unsigned long long* list_len, const LaunchCfg& c, cudaStream_t st);
 // Max resident blocks per SM of an FP32 march kernel (occupancy API).
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed);
 

@@ -1,0 +1,906 @@
+// Learned orbit surrogate for sm_103a: training data from the FP64 integrator, a fused BF16
+// tensor-core MLP (mma.sync m16n8k16, FP32 accumulation) for training and inference, Adam, and
+// the surrogate trace with its fallback list.
+//
+// Network (3 -> 64 -> 64 -> 64 -> 2, SiLU): inputs x1 = scaled log r_cam, x2 = scaled
+// sign(beta) ln(1 + |beta|/eps) with beta = b / sqrt(27) - 1, x3 = orbit coordinate sigma
+// (surrogate_math.cuh); outputs y = (polar angle of the integrated orbit - closed-form baseline)
+// / y_scale at sigma, and a capture logit. The first and last layers run in FP32 on the CUDA
+// cores, the two 64x64 layers in BF16 on the tensor cores, activations rounded to BF16 between
+// them, exactly as in training. SiLU uses the SFU tanh: silu(z) = z/2 (1 + tanh(z/2)).
+//
+// Fragment layout (PTX ISA, mma.m16n8k16 .bf16): with g = lane / 4, t = lane % 4, a thread holds
+// A rows g and g+8, columns 2t, 2t+1, 2t+8, 2t+9; B column g, rows 2t, 2t+1, 2t+8, 2t+9; C rows
+// g and g+8, columns 2t, 2t+1. A layer's C tiles (n = 8j..8j+7) therefore become the next layer's
+// A tiles (k = 16i..16i+15) from tiles 2i and 2i+1 without leaving registers.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "surrogate.cuh"
+#include "surrogate_math.cuh"
+
+namespace bhr {
+namespace surr {
+
+namespace {
+
+constexpr float kSqrt27f = 5.19615242270663f;
+constexpr double kSqrt27d = 5.196152422706632;
+
+// ---------------------------------------------------------------------------------------
+// small helpers
+__device__ __forceinline__ float tanh_sfu(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float silu(float z) {
+    const float h = 0.5f * z;
+    return fmaf(h, tanh_sfu(h), h);
+}
+// d silu / dz = s + z s (1 - s), s = 1/2 + tanh(z/2)/2
+__device__ __forceinline__ float silu_grad(float z) {
+    const float s = fmaf(0.5f, tanh_sfu(0.5f * z), 0.5f);
+    return fmaf(z * s, 1.0f - s, s);
+}
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return uint32_t(__bfloat16_as_ushort(lo)) | (uint32_t(__bfloat16_as_ushort(hi)) << 16);
+}
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Network weights in shared memory.
+struct SmemNet {
+    __nv_bfloat16 w2[kH * kLd];  // [out][in]
+    __nv_bfloat16 w3[kH * kLd];
+    float4 w1[kH];               // {w[f][0], w[f][1], w[f][2], b[f]}
+    float b2[kH], b3[kH];
+    float w4[kOut * kH];
+    float b4[kOut];
+};
+// Transposed hidden weights for the backward pass: wT[in][out].
+struct SmemNetT {
+    __nv_bfloat16 w2t[kH * kLd];
+    __nv_bfloat16 w3t[kH * kLd];
+};
+
+__device__ void load_net(SmemNet& N, SmemNetT* T, const float* __restrict__ P) {
+    for (int k = threadIdx.x; k < kH * kH; k += blockDim.x) {
+        const int o = k / kH, i = k % kH;
+        const __nv_bfloat16 a = __float2bfloat16_rn(P[kW2 + k]);
+        const __nv_bfloat16 c = __float2bfloat16_rn(P[kW3 + k]);
+        N.w2[o * kLd + i] = a;
+        N.w3[o * kLd + i] = c;
+        if (T) {
+            T->w2t[i * kLd + o] = a;
+            T->w3t[i * kLd + o] = c;
+        }
+    }
+    for (int f = threadIdx.x; f < kH; f += blockDim.x) {
+        N.w1[f] = make_float4(P[kW1 + 3 * f], P[kW1 + 3 * f + 1], P[kW1 + 3 * f + 2], P[kB1 + f]);
+        N.b2[f] = P[kB2 + f];
+        N.b3[f] = P[kB3 + f];
+        N.w4[f] = P[kW4 + f];
+        N.w4[kH + f] = P[kW4 + kH + f];
+    }
+    if (threadIdx.x < kOut) N.b4[threadIdx.x] = P[kB4 + threadIdx.x];
+}
+
+// Layer 1 (FP32) for rows ra, rb of a 16-row tile: pre-activations z and BF16 A fragments of
+// silu(z) for the 16 features f = 16i + 2t + {0, 1, 8, 9} this thread owns.
+template <bool kStore>
+__device__ __forceinline__ void layer1(const SmemNet& N, const float4& xa, const float4& xb, uint32_t (&A)[4][4],
+                                       int t, __nv_bfloat16* zs, __nv_bfloat16* hs, int ra, int rb) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float ha[4], hb[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int f = 16 * i + 2 * t + (q & 1) + ((q & 2) ? 8 : 0);
+            const float4 w = N.w1[f];
+            const float za = fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w)));
+            const float zb = fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w)));
+            ha[q] = silu(za);
+            hb[q] = silu(zb);
+            if (kStore) {
+                zs[ra * kLd + f] = __float2bfloat16_rn(za);
+                zs[rb * kLd + f] = __float2bfloat16_rn(zb);
+                hs[ra * kLd + f] = __float2bfloat16_rn(ha[q]);
+                hs[rb * kLd + f] = __float2bfloat16_rn(hb[q]);
+            }
+        }
+        A[i][0] = pack_bf16(ha[0], ha[1]);
+        A[i][1] = pack_bf16(hb[0], hb[1]);
+        A[i][2] = pack_bf16(ha[2], ha[3]);
+        A[i][3] = pack_bf16(hb[2], hb[3]);
+    }
+}
+
+// C = A W^T + bias for a 64x64 BF16 layer (W in shared memory, [n][k] with row stride kLd).
+__device__ __forceinline__ void mma_layer(const __nv_bfloat16* W, const float* bias, const uint32_t (&A)[4][4],
+                                          float (&C)[8][4], int g, int t) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float c0 = bias ? bias[8 * j + 2 * t] : 0.f;
+        const float c1 = bias ? bias[8 * j + 2 * t + 1] : 0.f;
+        C[j][0] = c0;
+        C[j][1] = c1;
+        C[j][2] = c0;
+        C[j][3] = c1;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const __nv_bfloat16* wp = W + (8 * j + g) * kLd + 16 * i + 2 * t;
+            mma_bf16(C[j], A[i], lds32(wp), lds32(wp + 8));
+        }
+    }
+}
+
+// C tiles (FP32) -> silu -> next layer's A fragments (BF16).
+__device__ __forceinline__ void act_pack(const float (&C)[8][4], uint32_t (&A)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        A[i][0] = pack_bf16(silu(C[2 * i][0]), silu(C[2 * i][1]));
+        A[i][1] = pack_bf16(silu(C[2 * i][2]), silu(C[2 * i][3]));
+        A[i][2] = pack_bf16(silu(C[2 * i + 1][0]), silu(C[2 * i + 1][1]));
+        A[i][3] = pack_bf16(silu(C[2 * i + 1][2]), silu(C[2 * i + 1][3]));
+    }
+}
+
+// C tiles (FP32, no activation) -> BF16 A fragments (used for gradients dz).
+__device__ __forceinline__ void pack_only(const float (&C)[8][4], uint32_t (&A)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        A[i][0] = pack_bf16(C[2 * i][0], C[2 * i][1]);
+        A[i][1] = pack_bf16(C[2 * i][2], C[2 * i][3]);
+        A[i][2] = pack_bf16(C[2 * i + 1][0], C[2 * i + 1][1]);
+        A[i][3] = pack_bf16(C[2 * i + 1][2], C[2 * i + 1][3]);
+    }
+}
+
+// Output layer (FP32) on z3 tiles: o[row][out] for rows g and g+8, reduced over the quad.
+__device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][4], float (&o)[2][2], int t) {
+    float pa0 = 0.f, pa1 = 0.f, pb0 = 0.f, pb1 = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int f = 8 * j + 2 * t;
+        const float h00 = silu(Z[j][0]), h01 = silu(Z[j][1]), h10 = silu(Z[j][2]), h11 = silu(Z[j][3]);
+        const float w0a = N.w4[f], w0b = N.w4[f + 1], w1a = N.w4[kH + f], w1b = N.w4[kH + f + 1];
+        pa0 = fmaf(w0a, h00, fmaf(w0b, h01, pa0));
+        pa1 = fmaf(w1a, h00, fmaf(w1b, h01, pa1));
+        pb0 = fmaf(w0a, h10, fmaf(w0b, h11, pb0));
+        pb1 = fmaf(w1a, h10, fmaf(w1b, h11, pb1));
+    }
+#pragma unroll
+    for (int m = 1; m <= 2; m <<= 1) {
+        pa0 += __shfl_xor_sync(0xffffffffu, pa0, m);
+        pa1 += __shfl_xor_sync(0xffffffffu, pa1, m);
+        pb0 += __shfl_xor_sync(0xffffffffu, pb0, m);
+        pb1 += __shfl_xor_sync(0xffffffffu, pb1, m);
+    }
+    o[0][0] = pa0 + N.b4[0];
+    o[0][1] = pa1 + N.b4[1];
+    o[1][0] = pb0 + N.b4[0];
+    o[1][1] = pb1 + N.b4[1];
+}
+
+// Forward pass of 32 queries held in shared memory (q[r] = {x1, x2, sigma, -}); all 32 lanes.
+__device__ void mlp_eval32(const SmemNet& N, const float4* q, float2* out) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll 1
+    for (int mt = 0; mt < 2; ++mt) {
+        const int ra = 16 * mt + g, rb = ra + 8;
+        uint32_t A[4][4];
+        float C[8][4];
+        layer1<false>(N, q[ra], q[rb], A, t, nullptr, nullptr, ra, rb);
+        mma_layer(N.w2, N.b2, A, C, g, t);
+        act_pack(C, A);
+        mma_layer(N.w3, N.b3, A, C, g, t);
+        float o[2][2];
+        out_layer(N, C, o, t);
+        if (t == 0) {
+            out[ra] = make_float2(o[0][0], o[0][1]);
+            out[rb] = make_float2(o[1][0], o[1][1]);
+        }
+    }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------------------------------
+// training data: FP64 RK4 in the orbital plane (x'' = -3 h^2 x / r^5, the reference's equation)
+
+__device__ __forceinline__ uint64_t splitmix(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+__device__ __forceinline__ double unif(uint64_t& s) {
+    s = splitmix(s);
+    return double(s >> 11) * (1.0 / 9007199254740992.0);
+}
+
+struct P2 {
+    double x, y;
+};
+__device__ __forceinline__ P2 acc2(P2 p, double m3h2) {
+    const double r2 = p.x * p.x + p.y * p.y;
+    const double ri = rsqrt(r2);
+    const double k = m3h2 * ri * ri * ri * ri * ri;
+    return {k * p.x, k * p.y};
+}
+
+// Polar angle at which the cubic Hermite arc between (x0, m0) and (x1, m1) reaches radius R,
+// relative to x0 (m = v dt). Newton on |p(tau)|^2 = R^2 from linear interpolation of r.
+__device__ double hermite_angle(P2 x0, P2 m0, P2 x1, P2 m1, double r0, double r1, double R) {
+    double tau = (R - r0) / (r1 - r0);
+    tau = tau < 0.0 ? 0.0 : (tau > 1.0 ? 1.0 : tau);
+    P2 p{0, 0};
+    for (int it = 0; it < 6; ++it) {
+        const double t2 = tau * tau, t3 = t2 * tau;
+        const double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + tau, h01 = -2 * t3 + 3 * t2, h11 = t3 - t2;
+        const double d00 = 6 * t2 - 6 * tau, d10 = 3 * t2 - 4 * tau + 1, d01 = -6 * t2 + 6 * tau, d11 = 3 * t2 - 2 * tau;
+        p = {h00 * x0.x + h10 * m0.x + h01 * x1.x + h11 * m1.x, h00 * x0.y + h10 * m0.y + h01 * x1.y + h11 * m1.y};
+        const P2 dp{d00 * x0.x + d10 * m0.x + d01 * x1.x + d11 * m1.x, d00 * x0.y + d10 * m0.y + d01 * x1.y + d11 * m1.y};
+        const double f = p.x * p.x + p.y * p.y - R * R;
+        const double df = 2 * (p.x * dp.x + p.y * dp.y);
+        if (df == 0.0) break;
+        tau -= f / df;
+        tau = tau < 0.0 ? 0.0 : (tau > 1.0 ? 1.0 : tau);
+    }
+    return atan2(x0.x * p.y - x0.y * p.x, x0.x * p.x + x0.y * p.y);
+}
+
+constexpr int kMaxK = 8;
+
+__global__ void __launch_bounds__(128) k_orbit_data(uint64_t seed, int64_t n_orbits, int K, Norm nrm,
+                                                    double step_frac, TrainSample* __restrict__ X,
+                                                    int8_t* __restrict__ lab, unsigned long long* stats) {
+    const double eps = nrm.t_eps;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_orbits;
+         n += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t s = seed ^ (0xD1B54A32D192ED03ull * (uint64_t)(n + 1));
+        const double lrc = log(double(nrm.rc_lo)) + unif(s) * (log(double(nrm.rc_hi)) - log(double(nrm.rc_lo)));
+        const double rc = exp(lrc);
+        // impact parameter: uniform in [0, b_max], or uniform in the transform t (dense near sqrt 27)
+        double b;
+        if (unif(s) < 0.5) {
+            b = unif(s) * nrm.b_max;
+        } else {
+            const double t_lo = -log1p(1.0 / eps);
+            const double t_hi = log1p((nrm.b_max / kSqrt27d - 1.0) / eps);
+            const double tt = t_lo + unif(s) * (t_hi - t_lo);
+            const double beta = (tt < 0 ? -1.0 : 1.0) * eps * expm1(fabs(tt));
+            b = kSqrt27d * (1.0 + beta);
+        }
+        const double bgeo = rc / sqrt(1.0 - 2.0 / rc);  // a ray from rc reaches at most this b
+        if (b > 0.999 * bgeo) b = unif(s) * 0.999 * bgeo;
+        const double beta = b / kSqrt27d - 1.0;
+        // initial state: static observer at rc, local angle alpha to the inward radial direction
+        const double f = sqrt(1.0 - 2.0 / rc);
+        const double sa = b * f / rc, ca = sqrt(1.0 - sa * sa);
+        double vr = -ca * f, vt = sa;
+        const double vn = rsqrt(vr * vr + vt * vt);
+        vr *= vn;
+        vt *= vn;
+        const double h = rc * vt, m3h2 = -3.0 * h * h;
+        const float x1 = float((lrc - log(double(nrm.rc_lo))) / (log(double(nrm.rc_hi)) - log(double(nrm.rc_lo))) * 2.0 - 1.0);
+        const float x2 = float(bhr::orbit::b_transform<double>(beta, eps) * nrm.t_scale);
+        // targets along the path (sigma ascending = path order); the last one is the exit
+        double sig[kMaxK], uk[kMaxK];
+        int nt = 0;
+        bhr::orbit::Roots<double> R{};
+        const double uc = 1.0 / rc;
+        const bool turns = beta > 0.0;
+        if (turns) {
+            R = bhr::orbit::roots<double, 40>(beta);
+            for (int k = 0; k < K - 1; ++k) {
+                double sg;
+                do {
+                    sg = 2.0 * unif(s) - 1.0;
+                } while (fabs(sg) < 0.01);
+                sig[nt++] = sg;
+            }
+            sig[nt++] = bhr::orbit::sigma_exit<double>(double(nrm.ue), R);
+            for (int a = 1; a < nt; ++a)  // insertion sort
+                for (int c = a; c > 0 && sig[c] < sig[c - 1]; --c) {
+                    const double tmp = sig[c];
+                    sig[c] = sig[c - 1];
+                    sig[c - 1] = tmp;
+                }
+            for (int k = 0; k < nt; ++k) uk[k] = bhr::orbit::u_of_sigma<double>(sig[k], uc, R);
+        }
+        // integrate
+        P2 x{rc, 0.0}, v{vr, vt};
+        double phi = 0.0, r = rc;
+        int next = 0, status = 0;
+        double phis[kMaxK];
+        const double Ic = turns ? bhr::orbit::sweep_to_turn<double, 40>(uc, R) : 0.0;
+        for (int it = 0; it < 400000; ++it) {
+            const double vlen = sqrt(v.x * v.x + v.y * v.y);
+            const double dt = step_frac * r / vlen, hdt = 0.5 * dt;
+            const P2 k1v = acc2(x, m3h2), k1x = v;
+            const P2 k2v = acc2({x.x + hdt * k1x.x, x.y + hdt * k1x.y}, m3h2), k2x{v.x + hdt * k1v.x, v.y + hdt * k1v.y};
+            const P2 k3v = acc2({x.x + hdt * k2x.x, x.y + hdt * k2x.y}, m3h2), k3x{v.x + hdt * k2v.x, v.y + hdt * k2v.y};
+            const P2 k4v = acc2({x.x + dt * k3x.x, x.y + dt * k3x.y}, m3h2), k4x{v.x + dt * k3v.x, v.y + dt * k3v.y};
+            const double s6 = dt / 6.0;
+            const P2 xn{x.x + s6 * (k1x.x + 2 * k2x.x + 2 * k3x.x + k4x.x), x.y + s6 * (k1x.y + 2 * k2x.y + 2 * k3x.y + k4x.y)};
+            const P2 vnw{v.x + s6 * (k1v.x + 2 * k2v.x + 2 * k3v.x + k4v.x), v.y + s6 * (k1v.y + 2 * k2v.y + 2 * k3v.y + k4v.y)};
+            const double rn = sqrt(xn.x * xn.x + xn.y * xn.y);
+            const double dphi = atan2(x.x * xn.y - x.y * xn.x, x.x * xn.x + x.y * xn.y);
+            const bool in0 = (x.x * v.x + x.y * v.y) < 0.0;
+            const bool in1 = (xn.x * vnw.x + xn.y * vnw.y) < 0.0;
+            // targets reached in this step: ingoing leg (sigma < 0): r falls through 1/u while ingoing;
+            // outgoing leg: r rises through 1/u while outgoing
+            while (turns && next < nt) {
+                const double Rk = 1.0 / uk[next];
+                bool hit;
+                if (sig[next] < 0.0) hit = in0 && rn <= Rk && r > Rk;
+                else hit = !in1 && rn >= Rk && r < Rk;
+                if (!hit) break;
+                phis[next] = phi + hermite_angle(x, {v.x * dt, v.y * dt}, xn, {vnw.x * dt, vnw.y * dt}, r, rn, Rk);
+                ++next;
+            }
+            (void)in1;
+            x = xn;
+            v = vnw;
+            r = rn;
+            phi += dphi;
+            if (r < 2.0001) {
+                status = 2;
+                break;
+            }
+            if (r > 1.0 / double(nrm.ue) && !(x.x * v.x + x.y * v.y < 0.0)) {
+                status = 1;
+                break;
+            }
+        }
+        const int64_t base = n * K;
+        if (status == 1 && turns && next == nt) {
+            for (int k = 0; k < nt; ++k) {
+                const double I = bhr::orbit::sweep_to_turn<double, bhr::orbit::kBaseDup>(uk[k], R);
+                const double Icb = bhr::orbit::sweep_to_turn<double, bhr::orbit::kBaseDup>(uc, R);
+                const double base_phi = sig[k] < 0.0 ? Icb - I : Icb + I;
+                X[base + k] = TrainSample{x1, x2, float(sig[k]), float((phis[k] - base_phi) / nrm.y_scale)};
+                lab[base + k] = 0;
+            }
+            atomicAdd(&stats[0], 1ull);
+        } else if (status == 2) {
+            for (int k = 0; k < K; ++k) {
+                X[base + k] = TrainSample{x1, x2, 1.0f, 0.0f};
+                lab[base + k] = 1;
+            }
+            atomicAdd(&stats[1], 1ull);
+        } else {
+            for (int k = 0; k < K; ++k) {
+                X[base + k] = TrainSample{x1, x2, 1.0f, 0.0f};
+                lab[base + k] = 2;
+            }
+            atomicAdd(&stats[2], 1ull);
+        }
+        (void)Ic;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// training: fused forward + backward per warp (32 samples), gradients summed in shared memory
+
+constexpr int kTrainWarps = 4;
+
+struct WarpAct {                      // per warp, BF16 [32 rows][kLd]
+    __nv_bfloat16 z1[32 * kLd], h1[32 * kLd], z2[32 * kLd], h2[32 * kLd], dz2[32 * kLd], dz3[32 * kLd];
+    float4 x[32];
+    float y[32];
+    int lab[32];
+};
+
+struct TrainSmem {
+    SmemNet N;
+    SmemNetT T;
+    float g[kNParams];                // gradient accumulators (flat layout of the parameters)
+    float loss[3];                    // sum of squared y error, sum of BCE, y-sample count
+    WarpAct w[kTrainWarps];
+};
+
+// sum over the 8 groups g (lanes with equal t) of a value, result valid in lanes with g == 0
+__device__ __forceinline__ float sum_over_g(float v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 16);
+    return v;
+}
+
+// dW[out][in] += sum over the warp's 32 rows of dz[row][out] * h[row][in] (BF16 MMA, K = 32 rows)
+__device__ void mma_weight_grad(const __nv_bfloat16* dz, const __nv_bfloat16* h, float* gW, int g, int t) {
+#pragma unroll 1
+    for (int mo = 0; mo < 4; ++mo) {
+        float C[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) C[j][0] = C[j][1] = C[j][2] = C[j][3] = 0.f;
+#pragma unroll
+        for (int ki = 0; ki < 2; ++ki) {
+            const int r0 = 16 * ki + 2 * t;
+            const int o0 = 16 * mo + g;
+            uint32_t A[4];
+            A[0] = pack2(dz[r0 * kLd + o0], dz[(r0 + 1) * kLd + o0]);
+            A[1] = pack2(dz[r0 * kLd + o0 + 8], dz[(r0 + 1) * kLd + o0 + 8]);
+            A[2] = pack2(dz[(r0 + 8) * kLd + o0], dz[(r0 + 9) * kLd + o0]);
+            A[3] = pack2(dz[(r0 + 8) * kLd + o0 + 8], dz[(r0 + 9) * kLd + o0 + 8]);
+            const uint32_t (&Ar)[4] = A;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int n0 = 8 * j + g;
+                const uint32_t b0 = pack2(h[r0 * kLd + n0], h[(r0 + 1) * kLd + n0]);
+                const uint32_t b1 = pack2(h[(r0 + 8) * kLd + n0], h[(r0 + 9) * kLd + n0]);
+                mma_bf16(C[j], Ar, b0, b1);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int o = 16 * mo + g, i = 8 * j + 2 * t;
+            atomicAdd(&gW[o * kH + i], C[j][0]);
+            atomicAdd(&gW[o * kH + i + 1], C[j][1]);
+            atomicAdd(&gW[(o + 8) * kH + i], C[j][2]);
+            atomicAdd(&gW[(o + 8) * kH + i + 1], C[j][3]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kTrainWarps, 1) k_train_step(
+    const float* __restrict__ P, const TrainSample* __restrict__ X, const int8_t* __restrict__ lab,
+    int64_t n_samples, const int64_t* __restrict__ idx, int batch, uint64_t seed, float w_u, float w_c,
+    float* __restrict__ G, float* __restrict__ loss_out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
+    load_net(S.N, &S.T, P);
+    for (int k = threadIdx.x; k < kNParams; k += blockDim.x) S.g[k] = 0.f;
+    if (threadIdx.x < 3) S.loss[threadIdx.x] = 0.f;
+    __syncthreads();
+    const SmemNet& N = S.N;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    WarpAct& W = S.w[warp];
+    const float inv_b = 1.0f / float(batch);
+    float l_y = 0.f, l_c = 0.f, n_y = 0.f;
+    const int tiles = batch / 32;
+    for (int tile = blockIdx.x * kTrainWarps + warp; tile < tiles; tile += gridDim.x * kTrainWarps) {
+        // ---- load 32 samples
+        const int64_t e = (int64_t)tile * 32 + lane;
+        int64_t si;
+        if (idx) si = idx[e];
+        else si = int64_t(splitmix(seed ^ (0x9E3779B97F4A7C15ull * uint64_t(e + 1))) % uint64_t(n_samples));
+        const TrainSample ts = X[si];
+        W.x[lane] = make_float4(ts.x1, ts.x2, ts.sigma, 0.f);
+        W.y[lane] = ts.y;
+        W.lab[lane] = lab[si];
+        __syncwarp();
+#pragma unroll 1
+        for (int mt = 0; mt < 2; ++mt) {
+            const int ra = 16 * mt + g, rb = ra + 8;
+            uint32_t A[4][4];
+            float C[8][4];
+            // ---- forward
+            layer1<true>(N, W.x[ra], W.x[rb], A, t, W.z1, W.h1, ra, rb);
+            mma_layer(N.w2, N.b2, A, C, g, t);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int f = 8 * j + 2 * t;
+                W.z2[ra * kLd + f] = __float2bfloat16_rn(C[j][0]);
+                W.z2[ra * kLd + f + 1] = __float2bfloat16_rn(C[j][1]);
+                W.z2[rb * kLd + f] = __float2bfloat16_rn(C[j][2]);
+                W.z2[rb * kLd + f + 1] = __float2bfloat16_rn(C[j][3]);
+                W.h2[ra * kLd + f] = __float2bfloat16_rn(silu(C[j][0]));
+                W.h2[ra * kLd + f + 1] = __float2bfloat16_rn(silu(C[j][1]));
+                W.h2[rb * kLd + f] = __float2bfloat16_rn(silu(C[j][2]));
+                W.h2[rb * kLd + f + 1] = __float2bfloat16_rn(silu(C[j][3]));
+            }
+            act_pack(C, A);
+            float Z3[8][4];
+            mma_layer(N.w3, N.b3, A, Z3, g, t);
+            float o[2][2];
+            out_layer(N, Z3, o, t);
+            // ---- loss and output gradients (rows ra, rb)
+            float dy[2], dc[2];
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+                const int row = rr ? rb : ra;
+                const int lb = W.lab[row];
+                const bool yok = lb == 0;
+                const float err = o[rr][0] - W.y[row];
+                dy[rr] = yok ? 2.0f * w_u * err * inv_b : 0.f;
+                const float target = lb == 1 ? 1.f : 0.f;
+                const float p = 1.0f / (1.0f + __expf(-o[rr][1]));
+                const bool cok = lb != 2;
+                dc[rr] = cok ? w_c * (p - target) * inv_b : 0.f;
+                if (t == 0) {
+                    if (yok) {
+                        l_y += err * err;
+                        n_y += 1.f;
+                    }
+                    if (cok) l_c += fmaxf(o[rr][1], 0.f) - o[rr][1] * target + log1pf(__expf(-fabsf(o[rr][1])));
+                }
+            }
+            // ---- output layer gradients and dz3
+            float D[8][4];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int f = 8 * j + 2 * t;
+                float gw[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, gb[2] = {0.f, 0.f};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int rr = c >> 1, ff = f + (c & 1);
+                    const float h3 = silu(Z3[j][c]);
+                    gw[0][c & 1] += dy[rr] * h3;
+                    gw[1][c & 1] += dc[rr] * h3;
+                    const float dh = dy[rr] * N.w4[ff] + dc[rr] * N.w4[kH + ff];
+                    D[j][c] = dh * silu_grad(Z3[j][c]);
+                    gb[c & 1] += D[j][c];
+                }
+                float v00 = sum_over_g(gw[0][0]), v01 = sum_over_g(gw[0][1]);
+                float v10 = sum_over_g(gw[1][0]), v11 = sum_over_g(gw[1][1]);
+                float b0 = sum_over_g(gb[0]), b1 = sum_over_g(gb[1]);
+                if (g == 0) {
+                    atomicAdd(&S.g[kW4 + f], v00);
+                    atomicAdd(&S.g[kW4 + f + 1], v01);
+                    atomicAdd(&S.g[kW4 + kH + f], v10);
+                    atomicAdd(&S.g[kW4 + kH + f + 1], v11);
+                    atomicAdd(&S.g[kB3 + f], b0);
+                    atomicAdd(&S.g[kB3 + f + 1], b1);
+                }
+                W.dz3[ra * kLd + f] = __float2bfloat16_rn(D[j][0]);
+                W.dz3[ra * kLd + f + 1] = __float2bfloat16_rn(D[j][1]);
+                W.dz3[rb * kLd + f] = __float2bfloat16_rn(D[j][2]);
+                W.dz3[rb * kLd + f + 1] = __float2bfloat16_rn(D[j][3]);
+            }
+            {
+                float gb0 = dy[0] + dy[1], gb1 = dc[0] + dc[1];
+                gb0 = sum_over_g(gb0);
+                gb1 = sum_over_g(gb1);
+                if (lane == 0) {
+                    atomicAdd(&S.g[kB4], gb0);
+                    atomicAdd(&S.g[kB4 + 1], gb1);
+                }
+            }
+            // ---- dh2 = dz3 W3, dz2 = dh2 silu'(z2)
+            pack_only(D, A);
+            mma_layer(S.T.w3t, nullptr, A, C, g, t);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int f = 8 * j + 2 * t;
+                float gb[2] = {0.f, 0.f};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int row = (c >> 1) ? rb : ra, ff = f + (c & 1);
+                    C[j][c] *= silu_grad(__bfloat162float(W.z2[row * kLd + ff]));
+                    gb[c & 1] += C[j][c];
+                    W.dz2[row * kLd + ff] = __float2bfloat16_rn(C[j][c]);
+                }
+                const float b0 = sum_over_g(gb[0]), b1 = sum_over_g(gb[1]);
+                if (g == 0) {
+                    atomicAdd(&S.g[kB2 + f], b0);
+                    atomicAdd(&S.g[kB2 + f + 1], b1);
+                }
+            }
+            // ---- dh1 = dz2 W2, dz1 = dh1 silu'(z1); layer-1 gradients in FP32
+            pack_only(C, A);
+            float E[8][4];
+            mma_layer(S.T.w2t, nullptr, A, E, g, t);
+            const float4 xa = W.x[ra], xb = W.x[rb];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int f = 8 * j + 2 * t + h;
+                    const float da = E[j][h] * silu_grad(__bfloat162float(W.z1[ra * kLd + f]));
+                    const float db = E[j][2 + h] * silu_grad(__bfloat162float(W.z1[rb * kLd + f]));
+                    const float g0 = sum_over_g(da * xa.x + db * xb.x);
+                    const float g1 = sum_over_g(da * xa.y + db * xb.y);
+                    const float g2 = sum_over_g(da * xa.z + db * xb.z);
+                    const float gb = sum_over_g(da + db);
+                    if (g == 0) {
+                        atomicAdd(&S.g[kW1 + 3 * f], g0);
+                        atomicAdd(&S.g[kW1 + 3 * f + 1], g1);
+                        atomicAdd(&S.g[kW1 + 3 * f + 2], g2);
+                        atomicAdd(&S.g[kB1 + f], gb);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // ---- hidden weight gradients over the 32 rows
+        mma_weight_grad(W.dz3, W.h2, &S.g[kW3], g, t);
+        mma_weight_grad(W.dz2, W.h1, &S.g[kW2], g, t);
+        __syncwarp();
+    }
+    if (t == 0) {
+        atomicAdd(&S.loss[0], l_y);
+        atomicAdd(&S.loss[1], l_c);
+        atomicAdd(&S.loss[2], n_y);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kNParams; k += blockDim.x) atomicAdd(&G[k], S.g[k]);
+    if (threadIdx.x < 3) atomicAdd(&loss_out[threadIdx.x], S.loss[threadIdx.x]);
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
+                       float* __restrict__ v, int step, float lr, float b1, float b2, float eps) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kNParams) return;
+    const float g = gr[k];
+    const float mk = b1 * m[k] + (1.f - b1) * g;
+    const float vk = b2 * v[k] + (1.f - b2) * g * g;
+    m[k] = mk;
+    v[k] = vk;
+    const float mh = mk / (1.f - powf(b1, float(step)));
+    const float vh = vk / (1.f - powf(b2, float(step)));
+    p[k] -= lr * mh / (sqrtf(vh) + eps);
+}
+
+// Plain forward pass over n queries (tests and the gradient check): one warp per 32 queries.
+__global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ P, const float4* __restrict__ q,
+                                                   float2* __restrict__ out, int n) {
+    __shared__ SmemNet N;
+    __shared__ float4 qs[4][32];
+    __shared__ float2 os[4][32];
+    load_net(N, nullptr, P);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int base = (blockIdx.x * 4 + warp) * 32; base < n; base += gridDim.x * 4 * 32) {
+        const int k = base + lane;
+        qs[warp][lane] = k < n ? q[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncwarp();
+        mlp_eval32(N, qs[warp], os[warp]);
+        if (k < n) out[k] = os[warp][lane];
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// inference: one warp traces 32 rays at a time
+
+constexpr int kInferWarps = 8;
+constexpr int kMaxQ = 128;  // exit query per ray + up to 3 crossing queries per ray
+
+struct InferSmem {
+    SmemNet N;
+    float4 q[kInferWarps][kMaxQ];
+    float2 o[kInferWarps][kMaxQ];
+};
+
+__device__ __forceinline__ unsigned long long warp_append_ull(unsigned long long* ctr) {
+    const unsigned m = __activemask();
+    const int leader = __ffs(m) - 1;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(ctr, (unsigned long long)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_constant__ SurrView sv,
+                                                                const float* __restrict__ P, WorkQueue* q,
+                                                                int* __restrict__ fb_list) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+    load_net(S.N, nullptr, P);
+    __syncthreads();
+    const DevView& w = sv.view;
+    const Rule& R = sv.rule;
+    const Norm& nm = sv.norm;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* qb = S.q[warp];
+    float2* ob = S.o[warp];
+    const float lrc_lo = logf(nm.rc_lo), lrc_span = logf(nm.rc_hi) - logf(nm.rc_lo);
+    const float beta_band = nm.band / kSqrt27f;
+    unsigned long long n_surr = 0, n_dis = 0;
+    for (;;) {
+        unsigned long long chunk = 0;
+        if (lane == 0) chunk = atomicAdd(&q->next_chunk, 1ull);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        const int64_t base = (int64_t)chunk * 32;
+        if (base >= w.nrays) break;
+        const int ray = int(base + lane);
+        const bool valid = ray < w.nrays;
+        // ---- ray setup and routing
+        bool sur = valid;
+        const int j = valid ? ray / w.width : 0, i = valid ? ray - j * w.width : 0;
+        const RayInit<float> ri = setup_ray<float>(w, R, i, j);
+        const V3<float> cam{w.cam[0], w.cam[1], w.cam[2]};
+        float b = ri.b;
+        float beta = b / kSqrt27f - 1.0f;
+        if (sur && fabsf(beta) < 0.02f) {  // near the photon sphere: impact parameter in FP64
+            const RayInit<double> rd = setup_ray<double>(w, R, i, j);
+            beta = float(rd.b / kSqrt27d - 1.0);
+            b = float(rd.b);
+        }
+        sur = sur && dot3(cam, ri.v) < 0.f && w.rcam >= nm.rc_lo && w.rcam <= nm.rc_hi && b <= nm.b_max &&
+              beta >= beta_band;
+        // orbital plane: e1 along the camera, e2 along the tangential part of the velocity
+        const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
+        const float ve = dot3(ri.v, e1);
+        V3<float> e2{ri.v.x - ve * e1.x, ri.v.y - ve * e1.y, ri.v.z - ve * e1.z};
+        const float e2n = dot3(e2, e2);
+        sur = sur && e2n > 1e-12f;
+        const float e2i = rsqrtf(fmaxf(e2n, 1e-30f));
+        e2 = {e2.x * e2i, e2.y * e2i, e2.z * e2i};
+        orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
+        const float uc = 1.0f / w.rcam;
+        sur = sur && uc < Rt.u2 * 0.9999f;
+        // ---- closed-form baseline and queries
+        const float Ic = orbit::sweep_to_turn<float, orbit::kBaseDup>(uc, Rt);
+        const float Ie = orbit::sweep_to_turn<float, orbit::kBaseDup>(nm.ue, Rt);
+        const float phi0 = Ic + Ie;
+        const float x1 = (logf(w.rcam) - lrc_lo) / lrc_span * 2.0f - 1.0f;
+        const float x2 = orbit::b_transform<float>(beta, nm.t_eps) * nm.t_scale;
+        qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
+        // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
+        float phin = atan2f(-e1.y, e2.y);
+        if (phin < 0.f) phin += 3.14159265358979f;
+        if (phin >= 3.14159265358979f) phin -= 3.14159265358979f;
+        sur = sur && (fabsf(e1.y) + fabsf(e2.y)) > 1e-6f;
+        int nplane = 0, ncand = 0;
+        float cu[3] = {0.f, 0.f, 0.f};
+        int ck[3] = {0, 0, 0};
+        bool cleg[3] = {false, false, false};
+        if (sur) {
+            const float rlo = R.disk_inner * 0.97f, rhi = R.disk_outer * 1.03f;
+            for (int k = 0; k < 16; ++k) {
+                const float phk = phin + float(k) * 3.14159265358979f;
+                if (phk >= phi0) break;
+                ++nplane;
+                if (ncand < 3 && R.disk_mode == BHR_DISK_THIN) {
+                    const bool leg = phk > Ic;
+                    const float u = orbit::invert_sweep<float, orbit::kBaseDup, 4>(leg ? phk - Ic : Ic - phk, Rt);
+                    const float rb = 1.0f / u;
+                    if (rb >= rlo && rb <= rhi) {
+                        cu[ncand] = u;
+                        ck[ncand] = k;
+                        cleg[ncand] = leg;
+                        ++ncand;
+                    }
+                }
+            }
+        }
+        // crossing queries after the 32 exit queries
+        int off = ncand;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, off, d);
+            if (lane >= d) off += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, off, 31);
+        off -= ncand;
+        for (int c = 0; c < ncand; ++c) {
+            const float u = cu[c];
+            const float sg = cleg[c] ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f))
+                                     : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
+            qb[32 + off + c] = make_float4(x1, x2, sg, 0.f);
+        }
+        __syncwarp();
+        // ---- network: all queries of the warp, 32 at a time
+        const int nq = 32 + total;
+        for (int qb0 = 0; qb0 < nq; qb0 += 32) mlp_eval32(S.N, qb + qb0, ob + qb0);
+        // ---- results
+        const float2 oe = ob[lane];
+        if (sur && oe.y > 0.f) {  // the learned capture flag disagrees with b > sqrt(27): integrator decides
+            sur = false;
+            ++n_dis;
+        }
+        if (valid && !sur) fb_list[warp_append_ull(&q->fb_count)] = ray;
+        if (sur) {
+            ++n_surr;
+            const float phi = phi0 + oe.x * nm.y_scale;
+            float sp, cp;
+            sincosf(phi, &sp, &cp);
+            const float ue = nm.ue;
+            const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
+            const V3<float> xt{-sp * e1.x + cp * e2.x, -sp * e1.y + cp * e2.y, -sp * e1.z + cp * e2.z};
+            const float re = 1.0f / ue;
+            const V3<float> xe{xr.x * re, xr.y * re, xr.z * re};
+            // velocity at the exit: along dx/dphi = sqrt(P)/u^2 xr + xt/u, with |v|^2 from the energy
+            // integral of x'' = -3 h^2 x / r^5: |v|^2 = |v0|^2 - 2 h^2 / rc^3 + 2 h^2 u^3
+            const float sP = orbit::dudphi<float>(ue, Rt);
+            V3<float> T{sP * re * re * xr.x + re * xt.x, sP * re * re * xr.y + re * xt.y, sP * re * re * xr.z + re * xt.z};
+            const float vmag = sqrtf(fmaxf(1.0f - ri.h2 * w.two_over_r3 + 2.0f * ri.h2 * ue * ue * ue, 1e-12f));
+            const float Ti = vmag * rsqrtf(dot3(T, T));
+            T = {T.x * Ti, T.y * Ti, T.z * Ti};
+            const V3<float> d = far_field_dir(xe, T, ri.h2);
+            // crossings, in march order, inside [disk_inner, disk_outer]
+            float cr[3] = {0.f, 0.f, 0.f}, cph[3] = {0.f, 0.f, 0.f};
+            int nrec = 0;
+            for (int c = 0; c < ncand; ++c) {
+                const float dphi = ob[32 + off + c].x * nm.y_scale;
+                const float u = cu[c];
+                const float sPu = orbit::dudphi<float>(u, Rt);
+                const float us = cleg[c] ? u + dphi * sPu : u - dphi * sPu;
+                const float rs = 1.0f / us;
+                if (rs >= R.disk_inner && rs <= R.disk_outer && nrec < 3) {
+                    const float phk = phin + float(ck[c]) * 3.14159265358979f;
+                    float s2, c2;
+                    sincosf(phk, &s2, &c2);
+                    const float hx = rs * (c2 * e1.x + s2 * e2.x), hz = rs * (c2 * e1.z + s2 * e2.z);
+                    cr[nrec] = rs;
+                    cph[nrec] = atan2f(hz, hx);
+                    ++nrec;
+                }
+            }
+            const uint32_t w0 = uint32_t(BHR_STATUS_ESCAPED) | (uint32_t(nrec) << 8) |
+                                (uint32_t(BHR_FLAG_SURROGATE) << 16) | (uint32_t(min(nplane, 255)) << 24);
+            float4* p = reinterpret_cast<float4*>(w.out + ray);
+            p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
+            p[1] = make_float4(d.z, 1.0f / Rt.u2, 0.f, 0.f);
+            p[2] = make_float4(ri.b_axis, b, cr[0], cr[1]);
+            p[3] = make_float4(cr[2], cph[0], cph[1], cph[2]);
+        }
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_surr += __shfl_xor_sync(0xffffffffu, n_surr, o);
+        n_dis += __shfl_xor_sync(0xffffffffu, n_dis, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&q->surr_rays, n_surr);
+        if (n_dis) atomicAdd(&q->capture_disagree, n_dis);
+    }
+}
+
+}  // namespace
+
+int train_smem_bytes() { return int(sizeof(TrainSmem)); }
+
+cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
+                                   cudaStream_t st) {
+    const int smem = int(sizeof(InferSmem));
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_surrogate<<<grid, 32 * kInferWarps, smem, st>>>(sv, params, q, fb_list);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_orbit_data(uint64_t seed, int64_t n_orbits, int k_per_orbit, const Norm& nrm, double step_frac,
+                              TrainSample* X, int8_t* lab, unsigned long long* stats, int grid, cudaStream_t st) {
+    if (k_per_orbit < 2 || k_per_orbit > kMaxK) return cudaErrorInvalidValue;
+    k_orbit_data<<<grid, 128, 0, st>>>(seed, n_orbits, k_per_orbit, nrm, step_frac, X, lab, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_train_step(const float* params, const TrainSample* X, const int8_t* lab, int64_t n_samples,
+                              const int64_t* idx, int batch, uint64_t seed, float w_u, float w_c, float* grads,
+                              float* loss, int grid, cudaStream_t st) {
+    const int smem = train_smem_bytes();
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_train_step, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_train_step<<<grid, 32 * kTrainWarps, smem, st>>>(params, X, lab, n_samples, idx, batch, seed, w_u, w_c, grads,
+                                                        loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
+                        float beta2, float eps, cudaStream_t st) {
+    k_adam<<<(kNParams + 255) / 256, 256, 0, st>>>(params, grads, m, v, step, lr, beta1, beta2, eps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int grid, cudaStream_t st) {
+    k_mlp_infer<<<grid, 128, 0, st>>>(params, q, out, n);
+    return cudaGetLastError();
+}
+
+}  // namespace surr
+}  // namespace bhr

@@ -1,0 +1,64 @@
+// Learned orbit surrogate: network layout, normalisation and kernel entry points.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+#include "march.cuh"
+
+namespace bhr {
+namespace surr {
+
+constexpr int kH = 64;     // hidden width
+constexpr int kIn = 3;     // (log r_cam, transform of b / sqrt(27), orbit coordinate sigma)
+constexpr int kOut = 2;    // (scaled polar-angle residual, capture logit)
+constexpr int kLd = 72;    // bf16 row stride of weight / activation tiles in shared memory
+
+// Flat FP32 parameter block (master weights); W[o][i] row-major.
+constexpr int kW1 = 0;               // [64][3]
+constexpr int kB1 = kW1 + kH * kIn;  // [64]
+constexpr int kW2 = kB1 + kH;        // [64][64]
+constexpr int kB2 = kW2 + kH * kH;   // [64]
+constexpr int kW3 = kB2 + kH;        // [64][64]
+constexpr int kB3 = kW3 + kH * kH;   // [64]
+constexpr int kW4 = kB3 + kH;        // [2][64]
+constexpr int kB4 = kW4 + kOut * kH; // [2]
+constexpr int kNParams = kB4 + kOut; // 8706
+
+// Input normalisation and the trained range (stored with the weights).
+struct Norm {
+    float rc_lo, rc_hi;   // trained camera radii
+    float b_max;          // trained impact parameters [0, b_max]
+    float t_eps;          // b transform: t = sign(beta) ln(1 + |beta| / t_eps)
+    float t_scale;        // x2 = t * t_scale
+    float y_scale;        // polar-angle residual = y * y_scale
+    float band;           // |b - sqrt(27)| below this falls back to the integrator
+    float ue;             // exit u of the training orbits (1 / escape radius)
+};
+
+struct TrainSample {      // one training sample (16 bytes) + label
+    float x1, x2, sigma, y;
+};
+
+// label: 0 escaped (y valid), 1 captured, 2 unusable (budget)
+cudaError_t launch_orbit_data(uint64_t seed, int64_t n_orbits, int k_per_orbit, const Norm& nrm, double step_frac,
+                              TrainSample* X, int8_t* lab, unsigned long long* stats, int grid, cudaStream_t st);
+cudaError_t launch_train_step(const float* params, const TrainSample* X, const int8_t* lab, int64_t n_samples,
+                              const int64_t* idx, int batch, uint64_t seed, float w_u, float w_c, float* grads,
+                              float* loss, int grid, cudaStream_t st);
+cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
+                        float beta2, float eps, cudaStream_t st);
+cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int grid, cudaStream_t st);
+
+struct SurrView {
+    DevView view;
+    Rule rule;
+    Norm norm;
+};
+cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
+                                   cudaStream_t st);
+int train_smem_bytes();
+
+}  // namespace surr
+}  // namespace bhr

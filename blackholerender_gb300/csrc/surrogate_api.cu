@@ -1,0 +1,413 @@
+// C ABI of the learned orbit surrogate (include/bhr.h, "surrogate" section): creation, training
+// data from the integrator, training, parameter access, the gradient check hook, save/load, and
+// the surrogate-plus-fallback trace.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bhr.h"
+#include "host_views.h"
+#include "kernels.cuh"
+#include "surrogate.cuh"
+
+using bhr::surr::kNParams;
+
+struct bhr_surrogate {
+    int device = 0;
+    int sms = 0;
+    bhr::surr::Norm norm{};
+    float* params = nullptr;  // FP32 master weights (device)
+    float* grads = nullptr;
+    float* adam_m = nullptr;
+    float* adam_v = nullptr;
+    int adam_step = 0;
+    bhr::surr::TrainSample* X = nullptr;  // training samples (device)
+    int8_t* lab = nullptr;
+    int64_t n_samples = 0;
+    unsigned long long* stats = nullptr;  // data generation counters (device, 4)
+    float* loss = nullptr;                // per-step loss sums (device, 3 * loss_cap)
+    int loss_cap = 0;
+    bhr::WorkQueue* q = nullptr;          // per view of a trace: [2v] surrogate pass, [2v+1] fallback march
+    int64_t nq = 0;
+    int last_nviews = 0;
+    int* fb = nullptr;                    // fallback ray list
+    int64_t fb_cap = 0;
+    unsigned long long last[4] = {0, 0, 0, 0};
+    cudaStream_t last_stream = nullptr;
+    bool have_last = false;
+};
+
+namespace {
+
+int fail(int code, const std::string& msg) {
+    bhr::set_last_error(msg);
+    return code;
+}
+int cfail(cudaError_t e, const char* what) { return fail(BHR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)); }
+
+struct DevGuard {
+    int prev = 0;
+    explicit DevGuard(int dev) {
+        cudaGetDevice(&prev);
+        cudaSetDevice(dev);
+    }
+    ~DevGuard() { cudaSetDevice(prev); }
+};
+
+template <class T>
+cudaError_t grow(T** p, int64_t* cap, int64_t need) {
+    if (need <= *cap) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, sizeof(T) * size_t(need));
+    if (e == cudaSuccess) *cap = need;
+    return e;
+}
+
+// Glorot-uniform initialisation, deterministic from the seed (host side).
+void init_params(std::vector<float>& P, uint64_t seed) {
+    uint64_t s = seed * 0x9E3779B97F4A7C15ull + 1;
+    auto unif = [&]() {
+        s ^= s << 13;
+        s ^= s >> 7;
+        s ^= s << 17;
+        return double(s >> 11) * (1.0 / 9007199254740992.0);
+    };
+    P.assign(kNParams, 0.f);
+    auto fill = [&](int off, int n_out, int n_in) {
+        const double a = std::sqrt(6.0 / double(n_in + n_out));
+        for (int k = 0; k < n_out * n_in; ++k) P[off + k] = float((2.0 * unif() - 1.0) * a);
+    };
+    fill(bhr::surr::kW1, bhr::surr::kH, bhr::surr::kIn);
+    fill(bhr::surr::kW2, bhr::surr::kH, bhr::surr::kH);
+    fill(bhr::surr::kW3, bhr::surr::kH, bhr::surr::kH);
+    fill(bhr::surr::kW4, bhr::surr::kOut, bhr::surr::kH);
+}
+
+constexpr uint32_t kMagic = 0x53524842u;  // "BHRS"
+constexpr uint32_t kVersion = 1;
+
+}  // namespace
+
+extern "C" {
+
+int bhr_surrogate_default_config(bhr_surrogate_config* c) {
+    if (!c) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_default_config: NULL");
+    std::memset(c, 0, sizeof *c);
+    c->rc_lo = 6.0f;
+    c->rc_hi = 200.0f;
+    c->b_max = 60.0f;
+    c->band = 2e-3f;
+    c->t_eps = 1e-3f;
+    c->t_scale = 0.125f;
+    c->y_scale = 0.02f;
+    c->escape_r = 1000.0f;
+    return BHR_OK;
+}
+
+int bhr_surrogate_create(bhr_surrogate** out, int device, const bhr_surrogate_config* cfg, uint64_t seed) {
+    if (!out) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_create: NULL");
+    *out = nullptr;
+    bhr_surrogate_config c;
+    if (cfg) c = *cfg;
+    else bhr_surrogate_default_config(&c);
+    if (!(c.rc_lo > 2.0f && c.rc_hi > c.rc_lo && c.b_max > 5.2f && c.band > 0.0f && c.t_eps > 0.0f &&
+          c.y_scale > 0.0f && c.escape_r > c.rc_hi))
+        return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_create: inconsistent configuration");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return fail(BHR_ERR_CUDA, "bhr_surrogate_create: no such CUDA device");
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, device);
+    if (prop.major * 10 + prop.minor != 103)
+        return fail(BHR_ERR_UNSUPPORTED, "bhr_surrogate_create: this library is built for sm_103a only");
+    DevGuard dg(device);
+    bhr_surrogate* s = new bhr_surrogate();
+    s->device = device;
+    s->sms = prop.multiProcessorCount;
+    s->norm = bhr::surr::Norm{c.rc_lo, c.rc_hi, c.b_max, c.t_eps, c.t_scale, c.y_scale, c.band, 1.0f / c.escape_r};
+    std::vector<float> P;
+    init_params(P, seed);
+    cudaError_t e = cudaMalloc(&s->params, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMalloc(&s->grads, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMalloc(&s->adam_m, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMalloc(&s->adam_v, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMalloc(&s->stats, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(s->params, P.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(s->adam_m, 0, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMemset(s->adam_v, 0, sizeof(float) * kNParams);
+    if (e != cudaSuccess) {
+        bhr_surrogate_destroy(s);
+        return fail(BHR_ERR_OOM, std::string("bhr_surrogate_create: ") + cudaGetErrorString(e));
+    }
+    *out = s;
+    return BHR_OK;
+}
+
+int bhr_surrogate_destroy(bhr_surrogate* s) {
+    if (!s) return BHR_OK;
+    DevGuard dg(s->device);
+    for (void* p : {(void*)s->params, (void*)s->grads, (void*)s->adam_m, (void*)s->adam_v, (void*)s->X,
+                    (void*)s->lab, (void*)s->stats, (void*)s->loss, (void*)s->q, (void*)s->fb})
+        if (p) cudaFree(p);
+    delete s;
+    return BHR_OK;
+}
+
+int bhr_surrogate_generate(bhr_surrogate* s, int64_t n_orbits, int samples_per_orbit, uint64_t seed,
+                           void* stream, uint64_t* counts) {
+    if (!s || n_orbits <= 0 || samples_per_orbit < 2 || samples_per_orbit > 8)
+        return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_generate: bad arguments (2..8 samples per orbit)");
+    DevGuard dg(s->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t n = n_orbits * samples_per_orbit;
+    if (s->X) cudaFree(s->X);
+    if (s->lab) cudaFree(s->lab);
+    s->X = nullptr;
+    s->lab = nullptr;
+    s->n_samples = 0;
+    cudaError_t e = cudaMalloc(&s->X, sizeof(bhr::surr::TrainSample) * size_t(n));
+    if (e == cudaSuccess) e = cudaMalloc(&s->lab, size_t(n));
+    if (e != cudaSuccess) return fail(BHR_ERR_OOM, std::string("bhr_surrogate_generate: ") + cudaGetErrorString(e));
+    e = cudaMemsetAsync(s->stats, 0, sizeof(unsigned long long) * 4, st);
+    if (e == cudaSuccess)
+        e = bhr::surr::launch_orbit_data(seed, n_orbits, samples_per_orbit, s->norm, 0.004, s->X, s->lab, s->stats,
+                                         s->sms * 16, st);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_generate");
+    s->n_samples = n;
+    if (counts) {
+        unsigned long long h[4];
+        e = cudaMemcpyAsync(h, s->stats, sizeof h, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cfail(e, "bhr_surrogate_generate");
+        for (int k = 0; k < 3; ++k) counts[k] = h[k];
+    }
+    return BHR_OK;
+}
+
+int bhr_surrogate_train(bhr_surrogate* s, int steps, int batch, float lr_max, float lr_min, float w_capture,
+                        uint64_t seed, void* stream, float* loss_out) {
+    if (!s || steps <= 0 || batch <= 0 || batch % 32 != 0 || !(lr_max > 0.0f) || lr_min < 0.0f)
+        return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_train: bad arguments (batch must be a multiple of 32)");
+    if (!s->X || s->n_samples == 0) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_train: generate training data first");
+    DevGuard dg(s->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (steps > s->loss_cap) {
+        if (s->loss) cudaFree(s->loss);
+        s->loss = nullptr;
+        s->loss_cap = 0;
+        cudaError_t e = cudaMalloc(&s->loss, sizeof(float) * 3 * size_t(steps));
+        if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_train: loss buffer");
+        s->loss_cap = steps;
+    }
+    cudaError_t e = cudaMemsetAsync(s->loss, 0, sizeof(float) * 3 * size_t(steps), st);
+    const int grid = s->sms;
+    for (int k = 0; e == cudaSuccess && k < steps; ++k) {
+        const double frac = steps > 1 ? double(k) / double(steps - 1) : 1.0;
+        const float lr = float(lr_min + 0.5 * (lr_max - lr_min) * (1.0 + std::cos(3.141592653589793 * frac)));
+        e = cudaMemsetAsync(s->grads, 0, sizeof(float) * kNParams, st);
+        if (e == cudaSuccess)
+            e = bhr::surr::launch_train_step(s->params, s->X, s->lab, s->n_samples, nullptr, batch,
+                                             seed + 0x632BE59BD9B4E019ull * uint64_t(s->adam_step + 1), 1.0f,
+                                             w_capture, s->grads, s->loss + 3 * k, grid, st);
+        if (e == cudaSuccess)
+            e = bhr::surr::launch_adam(s->params, s->grads, s->adam_m, s->adam_v, ++s->adam_step, lr, 0.9f, 0.999f,
+                                       1e-8f, st);
+    }
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_train");
+    if (loss_out) {
+        std::vector<float> h(3 * size_t(steps));
+        e = cudaMemcpyAsync(h.data(), s->loss, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cfail(e, "bhr_surrogate_train");
+        for (int k = 0; k < steps; ++k) {
+            const float ny = h[3 * k + 2] > 0 ? h[3 * k + 2] : 1.0f;
+            loss_out[2 * k] = h[3 * k] / ny;                 // mean squared error of y
+            loss_out[2 * k + 1] = h[3 * k + 1] / float(batch);  // mean capture BCE
+        }
+    }
+    return BHR_OK;
+}
+
+int bhr_surrogate_samples(bhr_surrogate* s, int64_t offset, int64_t n, float* out, int8_t* labels) {
+    if (!s || !out || !labels || offset < 0 || n <= 0 || offset + n > s->n_samples)
+        return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_samples: range outside the generated samples");
+    DevGuard dg(s->device);
+    cudaError_t e = cudaMemcpy(out, s->X + offset, sizeof(bhr::surr::TrainSample) * size_t(n), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(labels, s->lab + offset, size_t(n), cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? BHR_OK : cfail(e, "bhr_surrogate_samples");
+}
+
+int bhr_surrogate_params(bhr_surrogate* s, float* out, int n) {
+    if (!s || !out || n != kNParams) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_params: n must be the parameter count");
+    DevGuard dg(s->device);
+    cudaError_t e = cudaMemcpy(out, s->params, sizeof(float) * kNParams, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? BHR_OK : cfail(e, "bhr_surrogate_params");
+}
+
+int bhr_surrogate_set_params(bhr_surrogate* s, const float* in, int n) {
+    if (!s || !in || n != kNParams) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_set_params: n must be the parameter count");
+    DevGuard dg(s->device);
+    cudaError_t e = cudaMemcpy(s->params, in, sizeof(float) * kNParams, cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? BHR_OK : cfail(e, "bhr_surrogate_set_params");
+}
+
+int bhr_surrogate_param_count(void) { return kNParams; }
+
+int bhr_surrogate_gradients(bhr_surrogate* s, const float* samples, const int8_t* labels, int n, float w_capture,
+                            float* grad_out, float* loss_out) {
+    if (!s || !samples || !labels || !grad_out || n <= 0 || n % 32 != 0)
+        return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_gradients: n must be a positive multiple of 32");
+    DevGuard dg(s->device);
+    bhr::surr::TrainSample* X = nullptr;
+    int8_t* L = nullptr;
+    int64_t* idx = nullptr;
+    float *G = nullptr, *loss = nullptr;
+    std::vector<int64_t> hidx(static_cast<size_t>(n));
+    for (int k = 0; k < n; ++k) hidx[size_t(k)] = k;
+    cudaError_t e = cudaMalloc(&X, sizeof(bhr::surr::TrainSample) * size_t(n));
+    if (e == cudaSuccess) e = cudaMalloc(&L, size_t(n));
+    if (e == cudaSuccess) e = cudaMalloc(&idx, sizeof(int64_t) * size_t(n));
+    if (e == cudaSuccess) e = cudaMalloc(&G, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMalloc(&loss, sizeof(float) * 3);
+    if (e == cudaSuccess) e = cudaMemcpy(X, samples, sizeof(bhr::surr::TrainSample) * size_t(n), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(L, labels, size_t(n), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(idx, hidx.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(G, 0, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMemset(loss, 0, sizeof(float) * 3);
+    if (e == cudaSuccess)
+        e = bhr::surr::launch_train_step(s->params, X, L, n, idx, n, 0, 1.0f, w_capture, G, loss, s->sms, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(grad_out, G, sizeof(float) * kNParams, cudaMemcpyDeviceToHost);
+    float hl[3] = {0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(hl, loss, sizeof hl, cudaMemcpyDeviceToHost);
+    for (void* p : {(void*)X, (void*)L, (void*)idx, (void*)G, (void*)loss})
+        if (p) cudaFree(p);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_gradients");
+    if (loss_out) {
+        loss_out[0] = hl[0];
+        loss_out[1] = hl[1];
+        loss_out[2] = hl[2];
+    }
+    return BHR_OK;
+}
+
+int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out) {
+    if (!s || !queries || !out || n <= 0) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_eval: bad arguments");
+    DevGuard dg(s->device);
+    float4* q = nullptr;
+    float2* o = nullptr;
+    std::vector<float4> hq(static_cast<size_t>(n));
+    for (int k = 0; k < n; ++k) hq[size_t(k)] = make_float4(queries[3 * k], queries[3 * k + 1], queries[3 * k + 2], 0.f);
+    cudaError_t e = cudaMalloc(&q, sizeof(float4) * size_t(n));
+    if (e == cudaSuccess) e = cudaMalloc(&o, sizeof(float2) * size_t(n));
+    if (e == cudaSuccess) e = cudaMemcpy(q, hq.data(), sizeof(float4) * size_t(n), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = bhr::surr::launch_mlp_infer(s->params, q, o, n, s->sms * 4, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(out, o, sizeof(float2) * size_t(n), cudaMemcpyDeviceToHost);
+    if (q) cudaFree(q);
+    if (o) cudaFree(o);
+    return e == cudaSuccess ? BHR_OK : cfail(e, "bhr_surrogate_eval");
+}
+
+int bhr_surrogate_save(bhr_surrogate* s, const char* path) {
+    if (!s || !path) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_save: NULL");
+    std::vector<float> P(kNParams);
+    const int rc = bhr_surrogate_params(s, P.data(), kNParams);
+    if (rc != BHR_OK) return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(BHR_ERR_IO, std::string("bhr_surrogate_save: cannot open ") + path);
+    const uint32_t hdr[3] = {kMagic, kVersion, uint32_t(kNParams)};
+    bool ok = std::fwrite(hdr, sizeof hdr, 1, f) == 1 && std::fwrite(&s->norm, sizeof s->norm, 1, f) == 1 &&
+              std::fwrite(&s->adam_step, sizeof s->adam_step, 1, f) == 1 &&
+              std::fwrite(P.data(), sizeof(float), P.size(), f) == P.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? BHR_OK : fail(BHR_ERR_IO, "bhr_surrogate_save: write failed");
+}
+
+int bhr_surrogate_load(bhr_surrogate* s, const char* path) {
+    if (!s || !path) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_load: NULL");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(BHR_ERR_IO, std::string("bhr_surrogate_load: cannot open ") + path);
+    uint32_t hdr[3];
+    bhr::surr::Norm nm{};
+    int step = 0;
+    std::vector<float> P(kNParams);
+    bool ok = std::fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == kMagic && hdr[1] == kVersion &&
+              hdr[2] == uint32_t(kNParams) && std::fread(&nm, sizeof nm, 1, f) == 1 &&
+              std::fread(&step, sizeof step, 1, f) == 1 && std::fread(P.data(), sizeof(float), P.size(), f) == P.size();
+    std::fclose(f);
+    if (!ok) return fail(BHR_ERR_IO, std::string("bhr_surrogate_load: not a surrogate file: ") + path);
+    s->norm = nm;
+    s->adam_step = step;
+    return bhr_surrogate_set_params(s, P.data(), kNParams);
+}
+
+int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev, void* stream) {
+    if (!s || !views || nviews <= 0 || !out_dev) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace: bad arguments");
+    int64_t biggest = 0;
+    for (int k = 0; k < nviews; ++k) {
+        std::string msg;
+        const int rc = bhr::host::check_view(views[k], k, &msg);
+        if (rc != BHR_OK) return fail(rc, "bhr_surrogate_trace: " + msg);
+        if (views[k].term_mode != BHR_TERM_CONFIG || !views[k].lensing || views[k].far_mode)
+            return fail(BHR_ERR_UNSUPPORTED, "bhr_surrogate_trace: the surrogate is trained for the CONFIG rule with lensing");
+        if (std::fabs(1.0f / views[k].escape_r - s->norm.ue) > 1e-9f)
+            return fail(BHR_ERR_UNSUPPORTED, "bhr_surrogate_trace: view escape radius differs from the trained one");
+        if (!out_dev[k] || reinterpret_cast<uintptr_t>(out_dev[k]) % 16 != 0)
+            return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace: output buffers must be 16-byte aligned");
+        biggest = std::max<int64_t>(biggest, int64_t(views[k].width) * views[k].height);
+    }
+    DevGuard dg(s->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = grow(&s->fb, &s->fb_cap, biggest);
+    if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews));
+    if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
+    for (int k = 0; e == cudaSuccess && k < nviews; ++k) {
+        bhr::WorkQueue* qv = s->q + 2 * k;
+        bhr::surr::SurrView sv{};
+        sv.view = bhr::host::make_dev_view(views[k], out_dev[k]);
+        sv.rule = bhr::host::make_rule(views[k]);
+        sv.norm = s->norm;
+        e = cudaMemsetAsync(qv, 0, sizeof(bhr::WorkQueue) * 2, st);
+        if (e == cudaSuccess) e = bhr::surr::launch_surrogate_trace(sv, s->params, qv, s->fb, s->sms * 2, st);
+        if (e == cudaSuccess) {
+            bhr::LaunchCfg cfg{};
+            cfg.block = 512;
+            cfg.variant = bhr::rule_variant(sv.rule);
+            cfg.grid = s->sms * std::max(1, bhr::march_blocks_per_sm(512, cfg.variant, false, false));
+            cfg.chunk = 64;
+            cfg.refill = 8;
+            const bhr::Scratch sc{qv + 1, nullptr, nullptr};
+            e = bhr::launch_march_list(sv.view, sv.rule, sc, s->fb, &qv[0].fb_count, cfg, st);
+        }
+    }
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace");
+    s->last_stream = st;
+    s->last_nviews = nviews;
+    s->have_last = true;
+    return BHR_OK;
+}
+
+int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
+    if (!s || !out) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_stats: NULL");
+    if (!s->have_last) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_stats: no trace yet");
+    DevGuard dg(s->device);
+    std::vector<bhr::WorkQueue> q(2 * size_t(s->last_nviews));
+    cudaError_t e = cudaStreamSynchronize(s->last_stream);
+    if (e == cudaSuccess) e = cudaMemcpy(q.data(), s->q, sizeof(bhr::WorkQueue) * q.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace_stats");
+    for (int k = 0; k < 4; ++k) out[k] = 0;
+    for (int v = 0; v < s->last_nviews; ++v) {
+        out[0] += q[2 * v].surr_rays;
+        out[1] += q[2 * v].fb_count;
+        out[2] += q[2 * v].capture_disagree;
+        out[3] += q[2 * v + 1].steps;
+    }
+    return BHR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+// Closed-form orbit skeleton of the learned surrogate (device, templated on float/double).
+//
+// Every ray lies in the plane through the hole spanned by the camera position and the initial
+// velocity. In that plane u = 1/r obeys the first integral of the Binet equation u'' + u = 3u^2,
+// the orbit shape of x'' = -3 h^2 x / r^5 (shaders/geodesic.glsl:3-5, src/physics/Geodesic.h:4-6):
+//     (du/dphi)^2 = P(u) = 2u^3 - u^2 + 1/b^2 = 2 (u - u1)(u - u2)(u - u3).
+// For b > sqrt(27) the roots are real, u1 < 0 < u2 < u3, and an ingoing ray turns at u2. The
+// polar angle swept between u = a and the turning point is
+//     I(a) = sqrt(2) sqrt(u2 - a) R_F((a - u1)(u3 - u2), (u2 - u1)(u3 - u2), (u3 - a)(u2 - u1))
+// (Carlson's symmetric elliptic integral; B. C. Carlson, Numer. Algorithms 10 (1995), the
+// duplication theorem and its Taylor series). The surrogate evaluates R_F with kBaseDup
+// duplication steps only: that cheap baseline is what the network corrects.
+//
+// Position along an ingoing-then-outgoing orbit is the signed coordinate
+//     sigma = -sqrt((u2 - u) / (u2 - uc))   ingoing leg  (camera -1 .. turning point 0)
+//     sigma = +sqrt((u2 - u) / u2)          outgoing leg (turning point 0 .. infinity 1)
+// in which the polar angle is smooth across the turning point.
+#pragma once
+#include <cstdint>
+
+namespace bhr {
+namespace orbit {
+
+constexpr int kBaseDup = 1;  // R_F duplication steps of the baseline
+
+template <class T> __host__ __device__ __forceinline__ T tsqrt(T x);
+template <> __host__ __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
+template <> __host__ __device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
+
+template <class T> struct Roots {
+    T u1, u2, u3;
+    T d32;  // u3 - u2, formed without cancellation
+    bool ok;
+};
+
+// Roots of 2u^3 - u^2 + 1/b^2 for b = sqrt(27) (1 + beta), beta > 0, written around the double
+// root u = 1/3 of the critical orbit: with u = 1/3 + w, w^2 (1 + 2w) = D,
+// D = 1/27 - 1/b^2 = beta (2 + beta) / (27 (1 + beta)^2); Newton from w = +-sqrt(D).
+template <class T, int kIters>
+__host__ __device__ __forceinline__ Roots<T> roots(T beta) {
+    Roots<T> r;
+    r.ok = beta > T(0);
+    const T ob = T(1) + beta;
+    const T D = beta * (T(2) + beta) / (T(27) * ob * ob);
+    const T sd = tsqrt<T>(D > T(0) ? D : T(0));
+    T wp = sd, wm = -sd;
+#pragma unroll
+    for (int k = 0; k < kIters; ++k) {
+        wp -= (wp * wp * (T(1) + T(2) * wp) - D) / (wp * (T(2) + T(6) * wp));
+        wm -= (wm * wm * (T(1) + T(2) * wm) - D) / (wm * (T(2) + T(6) * wm));
+    }
+    r.u2 = T(1) / T(3) + wm;
+    r.u3 = T(1) / T(3) + wp;
+    r.u1 = T(0.5) - r.u2 - r.u3;
+    r.d32 = wp - wm;
+    return r;
+}
+
+// Carlson R_F(x, y, z) with N duplication steps and the fifth-order Taylor series.
+template <class T, int N>
+__host__ __device__ __forceinline__ T rf(T x, T y, T z) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const T sx = tsqrt<T>(x), sy = tsqrt<T>(y), sz = tsqrt<T>(z);
+        const T lam = sx * sy + sy * sz + sz * sx;
+        x = T(0.25) * (x + lam);
+        y = T(0.25) * (y + lam);
+        z = T(0.25) * (z + lam);
+    }
+    const T A = (x + y + z) * T(1.0 / 3.0);
+    const T iA = T(1) / A;
+    const T X = T(1) - x * iA, Y = T(1) - y * iA, Z = -(X + Y);
+    const T E2 = X * Y - Z * Z, E3 = X * Y * Z;
+    const T s = T(1) - E2 * T(0.1) + E3 * T(1.0 / 14.0) + E2 * E2 * T(1.0 / 24.0) - T(3.0 / 44.0) * E2 * E3;
+    return s / tsqrt<T>(A);
+}
+
+// I(a): polar angle between u = a and the turning point u2 (a <= u2).
+template <class T, int N>
+__host__ __device__ __forceinline__ T sweep_to_turn(T a, const Roots<T>& R) {
+    const T da = R.u2 - a;
+    const T X = (a - R.u1) * R.d32;
+    const T Y = (R.u2 - R.u1) * R.d32;
+    const T Z = (R.u3 - a) * (R.u2 - R.u1);
+    return T(1.4142135623730951) * tsqrt<T>(da > T(0) ? da : T(0)) * rf<T, N>(X, Y, Z);
+}
+
+// u at orbit coordinate sigma (see the file comment).
+template <class T>
+__host__ __device__ __forceinline__ T u_of_sigma(T sigma, T uc, const Roots<T>& R) {
+    const T s2 = sigma * sigma;
+    return sigma < T(0) ? R.u2 - s2 * (R.u2 - uc) : R.u2 - s2 * R.u2;
+}
+
+// sigma of the exit radius u_e on the outgoing leg.
+template <class T>
+__host__ __device__ __forceinline__ T sigma_exit(T ue, const Roots<T>& R) {
+    const T q = (R.u2 - ue) / R.u2;
+    return tsqrt<T>(q > T(0) ? q : T(0));
+}
+
+// Baseline polar angle from the camera to orbit coordinate sigma: Ic -+ I(u(sigma)).
+template <class T, int N>
+__host__ __device__ __forceinline__ T phi_base(T sigma, T uc, T Ic, const Roots<T>& R) {
+    const T I = sweep_to_turn<T, N>(u_of_sigma(sigma, uc, R), R);
+    return sigma < T(0) ? Ic - I : Ic + I;
+}
+
+// sqrt(P(u)) = |du/dphi| on the orbit.
+template <class T>
+__host__ __device__ __forceinline__ T dudphi(T u, const Roots<T>& R) {
+    const T p = T(2) * (u - R.u1) * (R.u2 - u) * (R.u3 - u);
+    return tsqrt<T>(p > T(0) ? p : T(0));
+}
+
+// Solves I(u) = target for u in [0, u2] on the baseline, by Newton in s = sqrt(u2 - u), where
+// dI/ds = 2 / sqrt(2 (u - u1)(u3 - u)) is smooth through the turning point.
+template <class T, int N, int kIters>
+__host__ __device__ __forceinline__ T invert_sweep(T target, const Roots<T>& R) {
+    // I(s) ~ s * sqrt(2) R_F at the turning point for the first guess
+    const T X0 = (R.u2 - R.u1) * R.d32;
+    const T Z0 = R.d32 * (R.u2 - R.u1);
+    const T slope0 = T(1.4142135623730951) * rf<T, N>(X0, X0, Z0);
+    const T smax = tsqrt<T>(R.u2);
+    T s = target / slope0;
+    s = s < T(0) ? T(0) : (s > smax ? smax : s);
+#pragma unroll
+    for (int k = 0; k < kIters; ++k) {
+        const T u = R.u2 - s * s;
+        const T f = sweep_to_turn<T, N>(u, R) - target;
+        const T g = T(2) / tsqrt<T>(T(2) * (u - R.u1) * (R.u3 - u));
+        s -= f / g;
+        s = s < T(0) ? T(0) : (s > smax ? smax : s);
+    }
+    return R.u2 - s * s;
+}
+
+// Monotone transform of b / sqrt(27): t = sign(beta) ln(1 + |beta| / eps).
+template <class T>
+__host__ __device__ __forceinline__ T b_transform(T beta, T eps) {
+    const T a = beta < T(0) ? -beta : beta;
+    const T t = log1p(a / eps);
+    return beta < T(0) ? -t : t;
+}
+
+}  // namespace orbit
+}  // namespace bhr

@@ -199,6 +199,54 @@ int bhr_trace_host(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* con
  * resolves the array's device address (cudaGetSymbolAddress, which may load the module): make
  * it before any stream capture. */
 int bhr_trace_noalloc(const bhr_view* view, bhr_hit* out_dev, void* cuda_stream);
+/* ---- learned orbit surrogate ------------------------------------------------------------
+ * A small MLP (3 -> 64 -> 64 -> 64 -> 2, SiLU; BF16 tensor-core hidden layers with FP32
+ * accumulation) corrects a closed-form elliptic-integral skeleton of the orbital-plane orbit
+ * u(phi; r_cam, b) and predicts the capture flag; it is trained on orbits the FP64 integrator
+ * generates. Rays near b = sqrt(27), captured, outgoing or outside the trained range fall back
+ * to the plain integrator. No counterpart in the reference (the reference only integrates). */
+typedef struct bhr_surrogate bhr_surrogate;
+typedef struct bhr_surrogate_config {
+    float rc_lo, rc_hi;    /* trained camera radii (6, 200) */
+    float b_max;           /* trained impact parameters [0, b_max] (60) */
+    float band;            /* |b - sqrt(27)| below this falls back to the integrator (2e-3) */
+    float t_eps, t_scale;  /* input transform of b (1e-3, 0.125) */
+    float y_scale;         /* output scale of the polar-angle residual (0.02) */
+    float escape_r;        /* exit radius of the training orbits (1000, the CONFIG rule) */
+    int32_t reserved[8];
+} bhr_surrogate_config;
+int bhr_surrogate_default_config(bhr_surrogate_config* cfg);
+int bhr_surrogate_create(bhr_surrogate** s, int device, const bhr_surrogate_config* cfg, uint64_t seed);
+int bhr_surrogate_destroy(bhr_surrogate* s);
+/* Integrates n_orbits orbits (FP64 RK4 in the orbital plane) and keeps samples_per_orbit (2..8)
+ * training samples of each; counts (may be NULL): escaped, captured, unusable orbits. */
+int bhr_surrogate_generate(bhr_surrogate* s, int64_t n_orbits, int samples_per_orbit, uint64_t seed,
+                           void* cuda_stream, uint64_t* counts);
+/* Adam with a cosine learning-rate schedule; loss_out (may be NULL): 2 floats per step (mean
+ * squared error of the scaled residual, mean capture cross-entropy). */
+int bhr_surrogate_train(bhr_surrogate* s, int steps, int batch, float lr_max, float lr_min, float w_capture,
+                        uint64_t seed, void* cuda_stream, float* loss_out);
+/* Copies generated samples [offset, offset + n) to the host: n x {x1, x2, sigma, y}, labels. */
+int bhr_surrogate_samples(bhr_surrogate* s, int64_t offset, int64_t n, float* out, int8_t* labels);
+int bhr_surrogate_param_count(void);
+int bhr_surrogate_params(bhr_surrogate* s, float* out, int n);
+int bhr_surrogate_set_params(bhr_surrogate* s, const float* in, int n);
+/* One forward + backward pass over exactly these samples (n x {x1, x2, sigma, y}, labels 0
+ * escaped / 1 captured / 2 ignored; n a multiple of 32): the summed gradients of
+ * mean(w_u (y_pred - y)^2) + w_capture mean(BCE), and loss sums {sum err^2, sum BCE, n_y}. */
+int bhr_surrogate_gradients(bhr_surrogate* s, const float* samples, const int8_t* labels, int n, float w_capture,
+                            float* grad_out, float* loss_out);
+/* Forward pass: n queries {x1, x2, sigma} -> n x {y, capture logit}. */
+int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out);
+int bhr_surrogate_save(bhr_surrogate* s, const char* path);
+int bhr_surrogate_load(bhr_surrogate* s, const char* path);
+/* Surrogate-plus-fallback trace (CONFIG rule, lensing on): stream-ordered like bhr_trace. */
+int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
+                        void* cuda_stream);
+/* Of the last bhr_surrogate_trace: rays answered by the surrogate, rays sent to the integrator,
+ * capture-flag disagreements (also sent to the integrator), integrator steps of the fallback. */
+int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out4);
+
 /* Statistics of the last bhr_trace on ctx (synchronises that call's stream). */
 int bhr_trace_stats(bhr_ctx* ctx, bhr_stats* stats);
 /* Per-view latency of the last multi-view bhr_trace: milliseconds from the start of the

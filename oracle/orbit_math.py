@@ -1,0 +1,90 @@
+"""Closed-form orbit pieces of the surrogate, restated in numpy FP64 -- TEST INFRASTRUCTURE ONLY.
+
+These are the checker's versions of blackholerender_gb300/csrc/surrogate_math.cuh. For a photon
+in Schwarzschild (G = c = M = 1) with impact parameter b, u = 1/r obeys the first integral of
+the Binet equation u'' + u = 3u^2 (the orbit shape of x'' = -3 h^2 x / r^5,
+shaders/geodesic.glsl:3-5 and src/physics/Geodesic.h:4-6):
+
+    (du/dphi)^2 = P(u) = 2u^3 - u^2 + 1/b^2 = 2 (u - u1)(u - u2)(u - u3)
+
+With b > sqrt(27) the roots are real, u1 < 0 < u2 < u3, and u2 is the turning point of an
+ingoing ray. The polar angle swept between u = a and the turning point is the elliptic
+integral
+
+    I(a) = int_a^u2 du / sqrt(P(u)) = sqrt(2) sqrt(u2 - a) R_F(X, Y, Z),
+    X = (a - u1)(u3 - u2),  Y = (u2 - u1)(u3 - u2),  Z = (u3 - a)(u2 - u1)
+
+(Carlson's symmetric form, B. C. Carlson, "Numerical computation of real or complex elliptic
+integrals", Numer. Algorithms 10 (1995); DLMF 19.29.4 with homogeneity). R_F is evaluated by
+the duplication theorem followed by its fifth-order Taylor series; the surrogate's baseline
+uses a single duplication step and learns the remainder.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+SQRT27 = 27.0 ** 0.5
+
+
+def roots(beta):
+    """Roots u1 < u2 < u3 of 2u^3 - u^2 + 1/b^2 for b = sqrt(27)(1 + beta), beta > 0.
+
+    Written around the double root u = 1/3 of the critical orbit: with u = 1/3 + w,
+    P = w^2 (1 + 2w) - D, D = 1/27 - 1/b^2 = beta (2 + beta) / (27 (1 + beta)^2), so the two
+    roots near 1/3 are found relative to 1/3 without cancellation (Newton from +-sqrt(D)).
+    """
+    beta = np.asarray(beta, dtype=np.float64)
+    D = beta * (2.0 + beta) / (27.0 * (1.0 + beta) ** 2)
+    sd = np.sqrt(D)
+    wp, wm = sd.copy(), -sd.copy()
+    for _ in range(40):  # w^2 (1 + 2w) = D
+        wp = wp - (wp * wp * (1 + 2 * wp) - D) / (2 * wp + 6 * wp * wp)
+        wm = wm - (wm * wm * (1 + 2 * wm) - D) / (2 * wm + 6 * wm * wm)
+    u2 = 1.0 / 3.0 + wm
+    u3 = 1.0 / 3.0 + wp
+    u1 = 0.5 - u2 - u3  # roots of 2u^3 - u^2 + c sum to 1/2
+    return u1, u2, u3, wp - wm
+
+
+def rf(x, y, z, ndup=None, tol=1e-16):
+    """Carlson R_F by duplication (ndup steps, or until converged) + the Taylor series."""
+    x, y, z = (np.asarray(v, dtype=np.float64).copy() for v in (x, y, z))
+    n = 0
+    while True:
+        A = (x + y + z) / 3.0
+        dev = np.max(np.abs(np.stack([x, y, z]) - A) / A)
+        if (ndup is not None and n >= ndup) or (ndup is None and dev < tol ** (1 / 6)):
+            break
+        sx, sy, sz = np.sqrt(x), np.sqrt(y), np.sqrt(z)
+        lam = sx * sy + sy * sz + sz * sx
+        x, y, z = (x + lam) / 4.0, (y + lam) / 4.0, (z + lam) / 4.0
+        n += 1
+    A = (x + y + z) / 3.0
+    X, Y = 1.0 - x / A, 1.0 - y / A
+    Z = -(X + Y)
+    E2 = X * Y - Z * Z
+    E3 = X * Y * Z
+    return (1.0 - E2 / 10.0 + E3 / 14.0 + E2 * E2 / 24.0 - 3.0 * E2 * E3 / 44.0) / np.sqrt(A)
+
+
+def sweep_to_turn(a, beta, ndup=None):
+    """I(a): polar angle between u = a and the turning point u2."""
+    u1, u2, u3, d32 = roots(beta)
+    a = np.asarray(a, dtype=np.float64)
+    X = (a - u1) * d32
+    Y = (u2 - u1) * d32
+    Z = (u3 - a) * (u2 - u1)
+    return np.sqrt(2.0) * np.sqrt(np.maximum(u2 - a, 0.0)) * rf(X, Y, Z, ndup)
+
+
+def phi_of_u(u, uc, beta, leg, ndup=None):
+    """Polar angle from the camera (u = uc, ingoing) to u on leg 0 (ingoing) or 1 (outgoing)."""
+    Ic = sweep_to_turn(uc, beta, ndup)
+    Iu = sweep_to_turn(u, beta, ndup)
+    return np.where(np.asarray(leg) == 0, Ic - Iu, Ic + Iu)
+
+
+def b_transform(b, eps=1e-3):
+    """Monotone transform of b / sqrt(27): t = sign(beta) ln(1 + |beta| / eps)."""
+    beta = np.asarray(b, dtype=np.float64) / SQRT27 - 1.0
+    return np.sign(beta) * np.log1p(np.abs(beta) / eps)

@@ -1,0 +1,106 @@
+"""ctypes helpers around the surrogate entry points of libbhr.so for the tests."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from blackholerender_gb300 import _abi
+
+
+class Surrogate:
+    def __init__(self, device=0, seed=1, **cfg):
+        L = _abi.lib()
+        c = _abi.SurrogateConfig()
+        _abi.check(L.bhr_surrogate_default_config(ctypes.byref(c)))
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        self.cfg = c
+        self.h = ctypes.c_void_p()
+        _abi.check(L.bhr_surrogate_create(ctypes.byref(self.h), device, ctypes.byref(c), seed))
+
+    def close(self):
+        if self.h:
+            _abi.lib().bhr_surrogate_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def nparams():
+        return _abi.lib().bhr_surrogate_param_count()
+
+    def params(self):
+        p = np.zeros(self.nparams(), dtype=np.float32)
+        _abi.check(_abi.lib().bhr_surrogate_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _abi.check(_abi.lib().bhr_surrogate_set_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(p)))
+
+    def gradients(self, samples, labels, w_c):
+        s = np.ascontiguousarray(samples, dtype=np.float32)
+        lab = np.ascontiguousarray(labels, dtype=np.int8)
+        g = np.zeros(self.nparams(), dtype=np.float32)
+        loss = np.zeros(3, dtype=np.float32)
+        F = ctypes.POINTER(ctypes.c_float)
+        _abi.check(_abi.lib().bhr_surrogate_gradients(self.h, s.ctypes.data_as(F),
+                                                      lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), len(s),
+                                                      ctypes.c_float(w_c), g.ctypes.data_as(F), loss.ctypes.data_as(F)))
+        return loss, g
+
+    def eval(self, queries):
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        out = np.zeros((len(q), 2), dtype=np.float32)
+        F = ctypes.POINTER(ctypes.c_float)
+        _abi.check(_abi.lib().bhr_surrogate_eval(self.h, q.ctypes.data_as(F), len(q), out.ctypes.data_as(F)))
+        return out
+
+    def generate(self, n_orbits, per_orbit=4, seed=7):
+        c = (ctypes.c_uint64 * 3)()
+        _abi.check(_abi.lib().bhr_surrogate_generate(self.h, n_orbits, per_orbit, seed, None, c))
+        return list(c)
+
+    def samples(self, offset, n):
+        out = np.zeros((n, 4), dtype=np.float32)
+        lab = np.zeros(n, dtype=np.int8)
+        _abi.check(_abi.lib().bhr_surrogate_samples(self.h, offset, n, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                    lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+        return out, lab
+
+    def features_to_orbit(self, X):
+        """(r_cam, beta) of training features (inverse of the input transform)."""
+        c = self.cfg
+        lrc = (X[:, 0].astype(np.float64) + 1.0) / 2.0 * (np.log(c.rc_hi) - np.log(c.rc_lo)) + np.log(c.rc_lo)
+        t = X[:, 1].astype(np.float64) / c.t_scale
+        beta = np.sign(t) * c.t_eps * np.expm1(np.abs(t))
+        return np.exp(lrc), beta
+
+    def train(self, steps, batch=8192, lr_max=2e-3, lr_min=1e-5, w_c=0.01, seed=11):
+        loss = np.zeros(2 * steps, dtype=np.float32)
+        _abi.check(_abi.lib().bhr_surrogate_train(self.h, steps, batch, ctypes.c_float(lr_max), ctypes.c_float(lr_min),
+                                                  ctypes.c_float(w_c), seed, None,
+                                                  loss.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return loss.reshape(steps, 2)
+
+    def save(self, path):
+        _abi.check(_abi.lib().bhr_surrogate_save(self.h, str(path).encode()))
+
+    def load(self, path):
+        _abi.check(_abi.lib().bhr_surrogate_load(self.h, str(path).encode()))
+
+    def trace(self, views, outs, stream):
+        n = len(views)
+        arr = (_abi.View * n)(*views)
+        ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
+        _abi.check(_abi.lib().bhr_surrogate_trace(self.h, arr, n, ptrs, ctypes.c_void_p(stream.cuda_stream)))
+
+    def trace_stats(self):
+        o = (ctypes.c_uint64 * 4)()
+        _abi.check(_abi.lib().bhr_surrogate_trace_stats(self.h, o))
+        return {"surrogate": o[0], "fallback": o[1], "capture_disagree": o[2], "fallback_steps": o[3]}

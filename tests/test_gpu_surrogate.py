@@ -1,0 +1,76 @@
+"""Learned orbit surrogate: gradient check of the GPU training kernels against the FP64 CPU
+network, training data from the integrator against the exact elliptic integral, and a short
+training run."""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "oracle"))
+import mlp_ref  # noqa: E402
+import orbit_math  # noqa: E402
+from surrogate_lib import Surrogate  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def test_gradients_match_fp64_reference():
+    s = Surrogate(seed=3)
+    rng = np.random.default_rng(0)
+    n = 256
+    samples = np.column_stack([rng.uniform(-1, 1, (n, 3)), rng.normal(0, 0.3, n)]).astype(np.float32)
+    labels = rng.choice([0, 0, 0, 1, 2], n).astype(np.int8)
+    p = s.params()
+    loss_g, g_gpu = s.gradients(samples, labels, 0.05)
+    loss_c, g_cpu = mlp_ref.loss_and_grad(p, samples, labels, 0.05, quantize=True)
+    assert abs(loss_g[2] - loss_c[2]) < 0.5
+    assert abs(loss_g[0] - loss_c[0]) < 1e-2 * loss_c[0] + 1e-6
+    for name, (o, sz) in mlp_ref.OFF.items():
+        a, b = g_gpu[o:o + sz].astype(np.float64), g_cpu[o:o + sz]
+        cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30)
+        assert _rel(a, b) < 3e-2 and cos > 0.999, (name, _rel(a, b), cos)
+    # forward pass of the inference kernel against the same reference
+    q = samples[:64, :3]
+    out = s.eval(q)
+    ref, _ = mlp_ref.forward(p, q.astype(np.float64), quantize=True)
+    assert np.max(np.abs(out - ref)) < 1e-2 * np.max(np.abs(ref)) + 1e-4
+
+
+def test_training_data_matches_exact_orbits():
+    # the integrator's polar angle at each sample, minus the closed-form baseline, against the exact
+    # elliptic integral (Carlson R_F to convergence) minus the same baseline
+    s = Surrogate(seed=5)
+    counts = s.generate(4096, per_orbit=4, seed=21)
+    assert counts[0] > 2000 and counts[1] > 100 and counts[2] < 0.02 * sum(counts)
+    X, lab = s.samples(0, 4096 * 4)
+    m = lab == 0
+    rc, beta = s.features_to_orbit(X[m])
+    sig = X[m, 2].astype(np.float64)
+    uc = 1.0 / rc
+    u1, u2, u3, d32 = orbit_math.roots(beta)
+    u = np.where(sig < 0, u2 - sig ** 2 * (u2 - uc), u2 - sig ** 2 * u2)
+    leg = (sig > 0).astype(int)
+    exact = orbit_math.phi_of_u(u, uc, beta, leg, ndup=None)
+    base = orbit_math.phi_of_u(u, uc, beta, leg, ndup=1)
+    y_exact = (exact - base) / s.cfg.y_scale
+    err = np.abs(X[m, 3] - y_exact) * s.cfg.y_scale
+    far = np.abs(beta) > 4e-4   # outside the fallback band
+    assert np.percentile(err[far], 99) < 2e-6 and err[far].max() < 2e-5, (np.percentile(err[far], 99), err[far].max())
+    # captured orbits are exactly those with b < sqrt(27)
+    rc_c, beta_c = s.features_to_orbit(X[lab == 1])
+    assert np.all(beta_c < 1e-4)
+
+
+def test_short_training_reduces_loss():
+    s = Surrogate(seed=9)
+    s.generate(200_000, per_orbit=4, seed=3)
+    hist = s.train(600, batch=8192, lr_max=3e-3)
+    first = hist[:20, 0].mean()
+    last = hist[-20:, 0].mean()
+    assert np.all(np.isfinite(hist))
+    assert last < 0.2 * first, (first, last)
