@@ -179,13 +179,13 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                     }
                     cview = v;
                     cbeg = ((int64_t)base - views[v].chunk_start) * chunk;
-                    cend = min(cbeg + (int64_t)chunk, kList ? list_len : views[v].nrays);
+                    cend = min(cbeg + (int64_t)chunk, (kList && !kMulti) ? list_len : views[v].nrays);
                 }
                 const int n = (int)min((int64_t)32, cend - cbeg);
                 const DevView& w = views[cview];
                 bool keep = false;
                 RayInit<float> ri;
-                const int my = kList ? (lane < n ? list[cbeg + lane] : 0) : (int)(cbeg + lane);
+                const int my = kList ? (lane < n ? list[(kMulti ? w.list_off : 0) + cbeg + lane] : 0) : (int)(cbeg + lane);
                 if (lane < n) {
                     const int j = my / w.width;
                     const int i = my - j * w.width;
@@ -378,6 +378,36 @@ __global__ void __launch_bounds__(512) k_march_list(const __grid_constant__ DevV
                                                  Pool{s_pool[wid], nullptr}, list, n);
 }
 
+// The surrogate's fallback rays of several views in one launch: view v's list is
+// list[list_off_v .. list_off_v + qv[2v].fb_count) (counts written on the device).
+template <int kTerm, int kDisk>
+__global__ void __launch_bounds__(512) k_march_multi_list(const __grid_constant__ ViewBatch batch, const Scratch sc,
+                                                          const int* list, const WorkQueue* qv, int chunk,
+                                                          int refill_min) {
+    __shared__ float s_pool[512 / 32][kPoolFields * kPool];
+    __shared__ uint8_t s_pool_view[512 / 32][kPool];
+    __shared__ DevView s_views[kMaxViews];
+    __shared__ int64_t s_total;
+    const int nwords = batch.nviews * (int)(sizeof(DevView) / 4);
+    for (int k = threadIdx.x; k < nwords; k += 512)
+        reinterpret_cast<uint32_t*>(s_views)[k] = reinterpret_cast<const uint32_t*>(batch.views)[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t acc = 0;
+        for (int v = 0; v < batch.nviews; ++v) {
+            const int64_t n = (int64_t)qv[2 * v].fb_count;
+            s_views[v].nrays = n;
+            s_views[v].chunk_start = acc;
+            acc += (n + chunk - 1) / chunk;
+        }
+        s_total = acc;
+    }
+    __syncthreads();
+    const int wid = threadIdx.x >> 5;
+    march_warp<true, kTerm, kDisk, false, true>(s_views, batch.nviews, s_total, batch.rule, sc, chunk, refill_min,
+                                                Pool{s_pool[wid], s_pool_view[wid]}, list, 0);
+}
+
 __global__ void __launch_bounds__(128) k_march_fp64_one(const __grid_constant__ DevView view,
                                                         const __grid_constant__ Rule rule, const Scratch sc) {
     march_fp64<false>(&view, rule, sc);
@@ -474,6 +504,20 @@ cudaError_t launch_march_list(const DevView& v, const Rule& r, const Scratch& s,
     const int grid = c.grid > 0 ? c.grid : 1;
     void* args[] = {(void*)&v, (void*)&r, (void*)&s, (void*)&list, (void*)&list_len, &chunk, &refill};
     return cudaLaunchKernel(fn, dim3(grid), dim3(512), args, 0, st);
+}
+
+cudaError_t launch_march_multi_list(const ViewBatch& b, const Scratch& s, const int* list, const WorkQueue* qv,
+                                    const LaunchCfg& c, cudaStream_t st) {
+    int chunk = c.chunk, refill = c.refill;
+    const void* fn;
+    switch (c.variant) {
+        case kVariantConfigThin: fn = (const void*)k_march_multi_list<BHR_TERM_CONFIG, BHR_DISK_THIN>; break;
+        case kVariantShaderThin: fn = (const void*)k_march_multi_list<BHR_TERM_SHADER, BHR_DISK_THIN>; break;
+        case kVariantCpuNone: fn = (const void*)k_march_multi_list<BHR_TERM_CPU, BHR_DISK_NONE>; break;
+        default: fn = (const void*)k_march_multi_list<-1, -1>; break;
+    }
+    void* args[] = {(void*)&b, (void*)&s, (void*)&list, (void*)&qv, &chunk, &refill};
+    return cudaLaunchKernel(fn, dim3(c.grid > 0 ? c.grid : 1), dim3(512), args, 0, st);
 }
 
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed) {

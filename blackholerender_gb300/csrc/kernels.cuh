@@ -74,6 +74,10 @@ cudaError_t launch_march_fp64_multi(const ViewBatch& b, const Scratch& s, int gr
 // The FP32 march over a list of pixel indices of one view (512 threads per block, c.grid blocks).
 cudaError_t launch_march_list(const DevView& v, const Rule& r, const Scratch& s, const int* list,
                               const unsigned long long* list_len, const LaunchCfg& c, cudaStream_t st);
+// The FP32 march over per-view pixel lists of several views sharing one rule; view v's list
+// starts at list + views[v].list_off and its length is qv[2v].fb_count.
+cudaError_t launch_march_multi_list(const ViewBatch& b, const Scratch& s, const int* list, const WorkQueue* qv,
+                                    const LaunchCfg& c, cudaStream_t st);
 // Max resident blocks per SM of an FP32 march kernel (occupancy API).
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed);
 

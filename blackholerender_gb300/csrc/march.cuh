@@ -51,6 +51,7 @@ struct DevView {
     int64_t chunk_start; // first work chunk of this view (multi-view launches)
     int64_t nrays;       // width * height
     bhr_hit* out;        // device hit buffer of this view
+    int64_t list_off;    // offset of this view's pixel list (list launches)
 };
 
 template <class T> struct M;

@@ -303,14 +303,15 @@ __global__ void __launch_bounds__(128) k_orbit_data(uint64_t seed, int64_t n_orb
         const bool turns = beta > 0.0;
         if (turns) {
             R = bhr::orbit::roots<double, 40>(beta);
-            for (int k = 0; k < K - 1; ++k) {
+            const double se = bhr::orbit::sigma_exit<double>(double(nrm.ue), R);
+            for (int k = 0; k < K - 1; ++k) {  // uniform on [-1, exit], away from the turning point
                 double sg;
                 do {
-                    sg = 2.0 * unif(s) - 1.0;
+                    sg = -1.0 + unif(s) * (1.0 + se);
                 } while (fabs(sg) < 0.01);
                 sig[nt++] = sg;
             }
-            sig[nt++] = bhr::orbit::sigma_exit<double>(double(nrm.ue), R);
+            sig[nt++] = se;
             for (int a = 1; a < nt; ++a)  // insertion sort
                 for (int c = a; c > 0 && sig[c] < sig[c - 1]; --c) {
                     const double tmp = sig[c];
@@ -365,7 +366,9 @@ __global__ void __launch_bounds__(128) k_orbit_data(uint64_t seed, int64_t n_orb
             }
         }
         const int64_t base = n * K;
-        if (status == 1 && turns && next == nt) {
+        // orbits well inside the fallback band are never queried: keep them out of the regression
+        const bool in_band = fabs(beta) < 0.5 * double(nrm.band) / kSqrt27d;
+        if (status == 1 && turns && next == nt && !in_band) {
             for (int k = 0; k < nt; ++k) {
                 const double I = bhr::orbit::sweep_to_turn<double, bhr::orbit::kBaseDup>(uk[k], R);
                 const double Icb = bhr::orbit::sweep_to_turn<double, bhr::orbit::kBaseDup>(uc, R);
@@ -685,7 +688,13 @@ __device__ __forceinline__ unsigned long long warp_append_ull(unsigned long long
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_constant__ SurrView sv,
+// Impact parameter of pixel (i, j) in FP64 (near the photon sphere), kept out of line: it is
+// rare and its FP64 code would otherwise crowd the kernel's instruction cache.
+__device__ __noinline__ double impact_parameter_fp64(const DevView& w, const Rule& R, int i, int j) {
+    return setup_ray<double>(w, R, i, j).b;
+}
+
+__global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
                                                                 const float* __restrict__ P, WorkQueue* q,
                                                                 int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -717,9 +726,9 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_con
         float b = ri.b;
         float beta = b / kSqrt27f - 1.0f;
         if (sur && fabsf(beta) < 0.02f) {  // near the photon sphere: impact parameter in FP64
-            const RayInit<double> rd = setup_ray<double>(w, R, i, j);
-            beta = float(rd.b / kSqrt27d - 1.0);
-            b = float(rd.b);
+            const double bd = impact_parameter_fp64(w, R, i, j);
+            beta = float(bd / kSqrt27d - 1.0);
+            b = float(bd);
         }
         sur = sur && dot3(cam, ri.v) < 0.f && w.rcam >= nm.rc_lo && w.rcam <= nm.rc_hi && b <= nm.b_max &&
               beta >= beta_band;
@@ -746,12 +755,14 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_con
         if (phin < 0.f) phin += 3.14159265358979f;
         if (phin >= 3.14159265358979f) phin -= 3.14159265358979f;
         sur = sur && (fabsf(e1.y) + fabsf(e2.y)) > 1e-6f;
+        // up to 3 crossing candidates (u on the baseline orbit, crossing index k, outgoing leg),
+        // kept in registers: slot c holds u_c, k in bits 8c..8c+6 of ckl, leg in bit 8c+7
         int nplane = 0, ncand = 0;
-        float cu[3] = {0.f, 0.f, 0.f};
-        int ck[3] = {0, 0, 0};
-        bool cleg[3] = {false, false, false};
+        float cu0 = 0.f, cu1 = 0.f, cu2 = 0.f;
+        uint32_t ckl = 0;
         if (sur) {
             const float rlo = R.disk_inner * 0.97f, rhi = R.disk_outer * 1.03f;
+#pragma unroll 1
             for (int k = 0; k < 16; ++k) {
                 const float phk = phin + float(k) * 3.14159265358979f;
                 if (phk >= phi0) break;
@@ -761,9 +772,10 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_con
                     const float u = orbit::invert_sweep<float, orbit::kBaseDup, 4>(leg ? phk - Ic : Ic - phk, Rt);
                     const float rb = 1.0f / u;
                     if (rb >= rlo && rb <= rhi) {
-                        cu[ncand] = u;
-                        ck[ncand] = k;
-                        cleg[ncand] = leg;
+                        if (ncand == 0) cu0 = u;
+                        else if (ncand == 1) cu1 = u;
+                        else cu2 = u;
+                        ckl |= (uint32_t(k) | (leg ? 0x80u : 0u)) << (8 * ncand);
                         ++ncand;
                     }
                 }
@@ -778,15 +790,20 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_con
         }
         const int total = __shfl_sync(0xffffffffu, off, 31);
         off -= ncand;
-        for (int c = 0; c < ncand; ++c) {
-            const float u = cu[c];
-            const float sg = cleg[c] ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f))
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (c < ncand) {
+                const float u = c == 0 ? cu0 : (c == 1 ? cu1 : cu2);
+                const bool leg = (ckl >> (8 * c + 7)) & 1u;
+                const float sg = leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f))
                                      : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
-            qb[32 + off + c] = make_float4(x1, x2, sg, 0.f);
+                qb[32 + off + c] = make_float4(x1, x2, sg, 0.f);
+            }
         }
         __syncwarp();
         // ---- network: all queries of the warp, 32 at a time
         const int nq = 32 + total;
+#pragma unroll 1
         for (int qb0 = 0; qb0 < nq; qb0 += 32) mlp_eval32(S.N, qb + qb0, ob + qb0);
         // ---- results
         const float2 oe = ob[lane];
@@ -814,22 +831,28 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_con
             T = {T.x * Ti, T.y * Ti, T.z * Ti};
             const V3<float> d = far_field_dir(xe, T, ri.h2);
             // crossings, in march order, inside [disk_inner, disk_outer]
-            float cr[3] = {0.f, 0.f, 0.f}, cph[3] = {0.f, 0.f, 0.f};
+            float cr0 = 0.f, cr1 = 0.f, cr2 = 0.f, cp0 = 0.f, cp1 = 0.f, cp2 = 0.f;
             int nrec = 0;
-            for (int c = 0; c < ncand; ++c) {
-                const float dphi = ob[32 + off + c].x * nm.y_scale;
-                const float u = cu[c];
-                const float sPu = orbit::dudphi<float>(u, Rt);
-                const float us = cleg[c] ? u + dphi * sPu : u - dphi * sPu;
-                const float rs = 1.0f / us;
-                if (rs >= R.disk_inner && rs <= R.disk_outer && nrec < 3) {
-                    const float phk = phin + float(ck[c]) * 3.14159265358979f;
-                    float s2, c2;
-                    sincosf(phk, &s2, &c2);
-                    const float hx = rs * (c2 * e1.x + s2 * e2.x), hz = rs * (c2 * e1.z + s2 * e2.z);
-                    cr[nrec] = rs;
-                    cph[nrec] = atan2f(hz, hx);
-                    ++nrec;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if (c < ncand) {
+                    const float dphi = ob[32 + off + c].x * nm.y_scale;
+                    const float u = c == 0 ? cu0 : (c == 1 ? cu1 : cu2);
+                    const uint32_t kl = (ckl >> (8 * c)) & 0xffu;
+                    const float sPu = orbit::dudphi<float>(u, Rt);
+                    const float us = (kl & 0x80u) ? u + dphi * sPu : u - dphi * sPu;
+                    const float rs = 1.0f / us;
+                    if (rs >= R.disk_inner && rs <= R.disk_outer) {
+                        const float phk = phin + float(kl & 0x7fu) * 3.14159265358979f;
+                        float s2, c2;
+                        sincosf(phk, &s2, &c2);
+                        const float hx = rs * (c2 * e1.x + s2 * e2.x), hz = rs * (c2 * e1.z + s2 * e2.z);
+                        const float ph = atan2f(hz, hx);
+                        if (nrec == 0) { cr0 = rs; cp0 = ph; }
+                        else if (nrec == 1) { cr1 = rs; cp1 = ph; }
+                        else { cr2 = rs; cp2 = ph; }
+                        ++nrec;
+                    }
                 }
             }
             const uint32_t w0 = uint32_t(BHR_STATUS_ESCAPED) | (uint32_t(nrec) << 8) |
@@ -837,8 +860,8 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_surrogate(const __grid_con
             float4* p = reinterpret_cast<float4*>(w.out + ray);
             p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
             p[1] = make_float4(d.z, 1.0f / Rt.u2, 0.f, 0.f);
-            p[2] = make_float4(ri.b_axis, b, cr[0], cr[1]);
-            p[3] = make_float4(cr[2], cph[0], cph[1], cph[2]);
+            p[2] = make_float4(ri.b_axis, b, cr0, cr1);
+            p[3] = make_float4(cr2, cp0, cp1, cp2);
         }
         __syncwarp();
     }
@@ -862,6 +885,8 @@ cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, Work
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(k_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_surrogate, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (e != cudaSuccess) return e;
         attr = true;
     }

@@ -363,26 +363,50 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
     }
     DevGuard dg(s->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaError_t e = grow(&s->fb, &s->fb_cap, biggest);
-    if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews));
+    // per-view fallback lists, one after the other
+    std::vector<int64_t> off(size_t(nviews) + 1, 0);
+    for (int k = 0; k < nviews; ++k) off[size_t(k) + 1] = off[size_t(k)] + int64_t(views[k].width) * views[k].height;
+    cudaError_t e = grow(&s->fb, &s->fb_cap, off[size_t(nviews)]);
+    if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
+    e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
+    // 1) the surrogate pass of every view
+    std::vector<bhr::DevView> dvs(static_cast<size_t>(nviews));
+    std::vector<bhr::Rule> rules(static_cast<size_t>(nviews));
+    bool one_rule = true;
     for (int k = 0; e == cudaSuccess && k < nviews; ++k) {
-        bhr::WorkQueue* qv = s->q + 2 * k;
         bhr::surr::SurrView sv{};
         sv.view = bhr::host::make_dev_view(views[k], out_dev[k]);
+        sv.view.list_off = off[size_t(k)];
         sv.rule = bhr::host::make_rule(views[k]);
         sv.norm = s->norm;
-        e = cudaMemsetAsync(qv, 0, sizeof(bhr::WorkQueue) * 2, st);
-        if (e == cudaSuccess) e = bhr::surr::launch_surrogate_trace(sv, s->params, qv, s->fb, s->sms * 2, st);
-        if (e == cudaSuccess) {
-            bhr::LaunchCfg cfg{};
-            cfg.block = 512;
-            cfg.variant = bhr::rule_variant(sv.rule);
+        dvs[size_t(k)] = sv.view;
+        rules[size_t(k)] = sv.rule;
+        one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
+        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3, st);
+    }
+    // 2) the integrator on the fallback rays: one launch for all views when they share a rule
+    bhr::LaunchCfg cfg{};
+    cfg.block = 512;
+    cfg.chunk = 64;
+    cfg.refill = 8;
+    if (e == cudaSuccess && one_rule && nviews <= bhr::kMaxViews) {
+        static thread_local bhr::ViewBatch b;
+        b.nviews = nviews;
+        b.rule = rules[0];
+        b.total_chunks = 0;
+        for (int k = 0; k < nviews; ++k) b.views[k] = dvs[size_t(k)];
+        cfg.variant = bhr::rule_variant(b.rule);
+        cfg.grid = s->sms * std::max(1, bhr::march_blocks_per_sm(512, cfg.variant, true, false));
+        const bhr::Scratch sc{s->q + 2 * nviews, nullptr, nullptr};
+        e = bhr::launch_march_multi_list(b, sc, s->fb, s->q, cfg, st);
+    } else {
+        for (int k = 0; e == cudaSuccess && k < nviews; ++k) {
+            cfg.variant = bhr::rule_variant(rules[size_t(k)]);
             cfg.grid = s->sms * std::max(1, bhr::march_blocks_per_sm(512, cfg.variant, false, false));
-            cfg.chunk = 64;
-            cfg.refill = 8;
-            const bhr::Scratch sc{qv + 1, nullptr, nullptr};
-            e = bhr::launch_march_list(sv.view, sv.rule, sc, s->fb, &qv[0].fb_count, cfg, st);
+            const bhr::Scratch sc{s->q + 2 * k + 1, nullptr, nullptr};
+            e = bhr::launch_march_list(dvs[size_t(k)], rules[size_t(k)], sc, s->fb + off[size_t(k)],
+                                       &s->q[2 * k].fb_count, cfg, st);
         }
     }
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace");
@@ -396,7 +420,7 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
     if (!s || !out) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_stats: NULL");
     if (!s->have_last) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_stats: no trace yet");
     DevGuard dg(s->device);
-    std::vector<bhr::WorkQueue> q(2 * size_t(s->last_nviews));
+    std::vector<bhr::WorkQueue> q(2 * size_t(s->last_nviews) + 1);
     cudaError_t e = cudaStreamSynchronize(s->last_stream);
     if (e == cudaSuccess) e = cudaMemcpy(q.data(), s->q, sizeof(bhr::WorkQueue) * q.size(), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace_stats");
@@ -407,6 +431,7 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
         out[2] += q[2 * v].capture_disagree;
         out[3] += q[2 * v + 1].steps;
     }
+    out[3] += q[2 * size_t(s->last_nviews)].steps;
     return BHR_OK;
 }
 

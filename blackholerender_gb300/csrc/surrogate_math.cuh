@@ -33,13 +33,37 @@ template <class T> struct Roots {
     bool ok;
 };
 
-// Roots of 2u^3 - u^2 + 1/b^2 for b = sqrt(27) (1 + beta), beta > 0, written around the double
-// root u = 1/3 of the critical orbit: with u = 1/3 + w, w^2 (1 + 2w) = D,
-// D = 1/27 - 1/b^2 = beta (2 + beta) / (27 (1 + beta)^2); Newton from w = +-sqrt(D).
+template <class T> __host__ __device__ __forceinline__ T tsin(T x);
+template <> __host__ __device__ __forceinline__ float tsin<float>(float x) { return sinf(x); }
+template <> __host__ __device__ __forceinline__ double tsin<double>(double x) { return sin(x); }
+template <class T> __host__ __device__ __forceinline__ T tcos(T x);
+template <> __host__ __device__ __forceinline__ float tcos<float>(float x) { return cosf(x); }
+template <> __host__ __device__ __forceinline__ double tcos<double>(double x) { return cos(x); }
+template <class T> __host__ __device__ __forceinline__ T tasin(T x);
+template <> __host__ __device__ __forceinline__ float tasin<float>(float x) { return asinf(x); }
+template <> __host__ __device__ __forceinline__ double tasin<double>(double x) { return asin(x); }
+
+// Roots of 2u^3 - u^2 + 1/b^2 for b = sqrt(27) (1 + beta), beta > 0.
+// Near the critical orbit (beta < 0.1), around its double root u = 1/3: with u = 1/3 + w,
+// w^2 (1 + 2w) = D, D = 1/27 - 1/b^2 = beta (2 + beta) / (27 (1 + beta)^2); Newton from +-sqrt(D).
+// Elsewhere the trigonometric solution of the cubic with theta = 2 asin(sqrt(27)/b), written in
+// products of sines so that no root is a difference of nearly equal terms:
+//   u2 = 2/3 sin(theta/6) sin(2pi/3 - theta/6),  u3 = 2/3 cos(theta/6 + pi/6) cos(theta/6 - pi/6),
+//   u3 - u2 = sin((pi - theta)/3) / sqrt(3).
 template <class T, int kIters>
 __host__ __device__ __forceinline__ Roots<T> roots(T beta) {
     Roots<T> r;
     r.ok = beta > T(0);
+    if (beta >= T(0.1)) {
+        const T th = T(2) * tasin<T>(T(1) / (T(1) + beta));  // sqrt(27) / b = 1 / (1 + beta)
+        const T a = th * T(1.0 / 6.0);
+        const T pi = T(3.14159265358979323846);
+        r.u2 = T(2.0 / 3.0) * tsin<T>(a) * tsin<T>(T(2) * pi / T(3) - a);
+        r.u3 = T(2.0 / 3.0) * tcos<T>(a + pi / T(6)) * tcos<T>(a - pi / T(6));
+        r.u1 = T(0.5) - r.u2 - r.u3;
+        r.d32 = tsin<T>((pi - th) / T(3)) * T(0.57735026918962576);
+        return r;
+    }
     const T ob = T(1) + beta;
     const T D = beta * (T(2) + beta) / (T(27) * ob * ob);
     const T sd = tsqrt<T>(D > T(0) ? D : T(0));

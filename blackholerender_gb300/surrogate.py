@@ -1,11 +1,18 @@
-"""ctypes helpers around the surrogate entry points of libbhr.so for the tests."""
+"""The learned orbit surrogate: a context object over the bhr_surrogate_* entry points.
+
+Typical use: generate training orbits with the integrator, train on the GPU, save; later load
+the checkpoint and trace views with the surrogate-plus-fallback path.
+"""
 from __future__ import annotations
 
 import ctypes
+from pathlib import Path
 
 import numpy as np
 
-from blackholerender_gb300 import _abi
+from . import _abi
+
+DEFAULT_CHECKPOINT = Path(__file__).resolve().parent / "data" / "surrogate.bhrs"
 
 
 class Surrogate:
@@ -94,7 +101,20 @@ class Surrogate:
     def load(self, path):
         _abi.check(_abi.lib().bhr_surrogate_load(self.h, str(path).encode()))
 
-    def trace(self, views, outs, stream):
+    def trace(self, views, outs=None, stream=None):
+        """Surrogate-plus-fallback trace into device tensors (allocated if None); returns them."""
+        import torch
+
+        if isinstance(views, _abi.View):
+            views = [views]
+        if outs is None:
+            outs = [torch.empty(v.rays * 64, dtype=torch.uint8, device="cuda") for v in views]
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        self.trace_ptrs(views, outs, stream)
+        return outs
+
+    def trace_ptrs(self, views, outs, stream):
         n = len(views)
         arr = (_abi.View * n)(*views)
         ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])

@@ -10,7 +10,7 @@ import pytest
 sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "oracle"))
 import mlp_ref  # noqa: E402
 import orbit_math  # noqa: E402
-from surrogate_lib import Surrogate  # noqa: E402
+from blackholerender_gb300.surrogate import Surrogate  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
