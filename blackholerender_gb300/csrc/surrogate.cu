@@ -688,6 +688,22 @@ __device__ __forceinline__ unsigned long long warp_append_ull(unsigned long long
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// sin and cos of x (|x| < 1e4): Cody-Waite reduction by pi/2 with a two-part constant, then
+// Taylor polynomials on [-pi/4, pi/4] (truncation below 3e-9) and the quadrant rotation.
+__device__ __forceinline__ void sincos_rr(float x, float* sn, float* cs) {
+    const float k = rintf(x * 0.63661977236758134f);
+    float r = fmaf(-k, 1.57079637050628662f, x);
+    r = fmaf(k, 4.37113900018624e-8f, r);
+    const float r2 = r * r;
+    const float sp = r * fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, 2.7557319e-6f, -1.9841270e-4f), 8.3333333e-3f),
+                                       -1.6666667e-1f), 1.0f);
+    const float cp = fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, 2.4801587e-5f, -1.3888889e-3f), 4.1666667e-2f), -0.5f), 1.0f);
+    const int q = int(k) & 3;
+    const float s0 = (q & 1) ? cp : sp, c0 = (q & 1) ? sp : cp;
+    *sn = (q & 2) ? -s0 : s0;
+    *cs = ((q + 1) & 2) ? -c0 : c0;
+}
+
 // Impact parameter of pixel (i, j) in FP64 (near the photon sphere), kept out of line: it is
 // rare and its FP64 code would otherwise crowd the kernel's instruction cache.
 __device__ __noinline__ double impact_parameter_fp64(const DevView& w, const Rule& R, int i, int j) {
@@ -707,7 +723,6 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* qb = S.q[warp];
     float2* ob = S.o[warp];
-    const float lrc_lo = logf(nm.rc_lo), lrc_span = logf(nm.rc_hi) - logf(nm.rc_lo);
     const float beta_band = nm.band / kSqrt27f;
     unsigned long long n_surr = 0, n_dis = 0;
     for (;;) {
@@ -741,14 +756,15 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
         const float e2i = rsqrtf(fmaxf(e2n, 1e-30f));
         e2 = {e2.x * e2i, e2.y * e2i, e2.z * e2i};
         orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
-        const float uc = 1.0f / w.rcam;
+        const float uc = sv.uc;
         sur = sur && uc < Rt.u2 * 0.9999f;
         // ---- closed-form baseline and queries
         const float Ic = orbit::sweep_to_turn<float, orbit::kBaseDup>(uc, Rt);
         const float Ie = orbit::sweep_to_turn<float, orbit::kBaseDup>(nm.ue, Rt);
         const float phi0 = Ic + Ie;
-        const float x1 = (logf(w.rcam) - lrc_lo) / lrc_span * 2.0f - 1.0f;
-        const float x2 = orbit::b_transform<float>(beta, nm.t_eps) * nm.t_scale;
+        const float x1 = sv.x1;
+        const float tb = __logf(1.0f + fabsf(beta) / nm.t_eps);  // 1 + |beta|/eps >= 1.19 here
+        const float x2 = (beta < 0.f ? -tb : tb) * nm.t_scale;
         qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
         // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
         float phin = atan2f(-e1.y, e2.y);
@@ -816,7 +832,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             ++n_surr;
             const float phi = phi0 + oe.x * nm.y_scale;
             float sp, cp;
-            sincosf(phi, &sp, &cp);
+            sincos_rr(phi, &sp, &cp);
             const float ue = nm.ue;
             const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
             const V3<float> xt{-sp * e1.x + cp * e2.x, -sp * e1.y + cp * e2.y, -sp * e1.z + cp * e2.z};
@@ -845,7 +861,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                     if (rs >= R.disk_inner && rs <= R.disk_outer) {
                         const float phk = phin + float(kl & 0x7fu) * 3.14159265358979f;
                         float s2, c2;
-                        sincosf(phk, &s2, &c2);
+                        sincos_rr(phk, &s2, &c2);
                         const float hx = rs * (c2 * e1.x + s2 * e2.x), hz = rs * (c2 * e1.z + s2 * e2.z);
                         const float ph = atan2f(hz, hx);
                         if (nrec == 0) { cr0 = rs; cp0 = ph; }

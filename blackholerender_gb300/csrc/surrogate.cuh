@@ -55,6 +55,8 @@ struct SurrView {
     DevView view;
     Rule rule;
     Norm norm;
+    float x1;  // network input 1 of this view (scaled log r_cam)
+    float uc;  // 1 / r_cam
 };
 cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
                                    cudaStream_t st);

@@ -380,6 +380,9 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
         sv.view.list_off = off[size_t(k)];
         sv.rule = bhr::host::make_rule(views[k]);
         sv.norm = s->norm;
+        sv.x1 = float((std::log(double(sv.view.rcam)) - std::log(double(s->norm.rc_lo))) /
+                          (std::log(double(s->norm.rc_hi)) - std::log(double(s->norm.rc_lo))) * 2.0 - 1.0);
+        sv.uc = 1.0f / sv.view.rcam;
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;

@@ -33,16 +33,6 @@ template <class T> struct Roots {
     bool ok;
 };
 
-template <class T> __host__ __device__ __forceinline__ T tsin(T x);
-template <> __host__ __device__ __forceinline__ float tsin<float>(float x) { return sinf(x); }
-template <> __host__ __device__ __forceinline__ double tsin<double>(double x) { return sin(x); }
-template <class T> __host__ __device__ __forceinline__ T tcos(T x);
-template <> __host__ __device__ __forceinline__ float tcos<float>(float x) { return cosf(x); }
-template <> __host__ __device__ __forceinline__ double tcos<double>(double x) { return cos(x); }
-template <class T> __host__ __device__ __forceinline__ T tasin(T x);
-template <> __host__ __device__ __forceinline__ float tasin<float>(float x) { return asinf(x); }
-template <> __host__ __device__ __forceinline__ double tasin<double>(double x) { return asin(x); }
-
 // Roots of 2u^3 - u^2 + 1/b^2 for b = sqrt(27) (1 + beta), beta > 0.
 // Near the critical orbit (beta < 0.1), around its double root u = 1/3: with u = 1/3 + w,
 // w^2 (1 + 2w) = D, D = 1/27 - 1/b^2 = beta (2 + beta) / (27 (1 + beta)^2); Newton from +-sqrt(D).
@@ -50,18 +40,30 @@ template <> __host__ __device__ __forceinline__ double tasin<double>(double x) {
 // products of sines so that no root is a difference of nearly equal terms:
 //   u2 = 2/3 sin(theta/6) sin(2pi/3 - theta/6),  u3 = 2/3 cos(theta/6 + pi/6) cos(theta/6 - pi/6),
 //   u3 - u2 = sin((pi - theta)/3) / sqrt(3).
+// sin(theta/6) comes from Newton on the triple-angle identity, so no library trigonometry is used.
 template <class T, int kIters>
 __host__ __device__ __forceinline__ Roots<T> roots(T beta) {
     Roots<T> r;
     r.ok = beta > T(0);
     if (beta >= T(0.1)) {
-        const T th = T(2) * tasin<T>(T(1) / (T(1) + beta));  // sqrt(27) / b = 1 / (1 + beta)
-        const T a = th * T(1.0 / 6.0);
-        const T pi = T(3.14159265358979323846);
-        r.u2 = T(2.0 / 3.0) * tsin<T>(a) * tsin<T>(T(2) * pi / T(3) - a);
-        r.u3 = T(2.0 / 3.0) * tcos<T>(a + pi / T(6)) * tcos<T>(a - pi / T(6));
+        // a = theta / 6 = asin(sqrt(27)/b) / 3 from sin(3a) = 3s - 4s^3 = y, s = sin(a) <= 0.371
+        // (Newton; f' = 3 - 12 s^2 >= 1.35 here), then products of s and c = cos(a):
+        //   u2 = s (sqrt(3) c + s) / 3,  u3 = (3 c^2 - s^2) / 6 ... written without cancellation,
+        //   u3 - u2 = (sqrt(3) (c^2 - s^2) - 2 s c) / 3 / sqrt(3) * sqrt(3)   (sin(pi/3 - 2a) / sqrt(3))
+        const T y = T(1) / (T(1) + beta);
+        T sa = y * T(1.0 / 3.0);
+#pragma unroll 1
+        for (int k = 0; k < 5; ++k) sa -= (T(3) * sa - T(4) * sa * sa * sa - y) / (T(3) - T(12) * sa * sa);
+        const T ca = tsqrt<T>(T(1) - sa * sa);
+        const T r3 = T(1.7320508075688772);
+        // u2 = 2/3 sin(a) sin(2pi/3 - a) = 2/3 s (r3/2 c + s/2)
+        r.u2 = T(1.0 / 3.0) * sa * (r3 * ca + sa);
+        // u3 = 2/3 cos(a + pi/6) cos(a - pi/6) = 2/3 ((r3/2 c)^2 - (s/2)^2)
+        r.u3 = T(1.0 / 6.0) * (T(3) * ca * ca - sa * sa);
         r.u1 = T(0.5) - r.u2 - r.u3;
-        r.d32 = tsin<T>((pi - th) / T(3)) * T(0.57735026918962576);
+        // u3 - u2 = sin(pi/3 - 2a) / sqrt(3) = (r3/2 cos 2a - 1/2 sin 2a) / r3
+        const T c2a = ca * ca - sa * sa, s2a = T(2) * sa * ca;
+        r.d32 = (T(0.5) * c2a - T(0.5) / r3 * s2a);
         return r;
     }
     const T ob = T(1) + beta;
@@ -83,7 +85,7 @@ __host__ __device__ __forceinline__ Roots<T> roots(T beta) {
 // Carlson R_F(x, y, z) with N duplication steps and the fifth-order Taylor series.
 template <class T, int N>
 __host__ __device__ __forceinline__ T rf(T x, T y, T z) {
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < N; ++k) {
         const T sx = tsqrt<T>(x), sy = tsqrt<T>(y), sz = tsqrt<T>(z);
         const T lam = sx * sy + sy * sz + sz * sx;
@@ -148,7 +150,7 @@ __host__ __device__ __forceinline__ T invert_sweep(T target, const Roots<T>& R) 
     const T smax = tsqrt<T>(R.u2);
     T s = target / slope0;
     s = s < T(0) ? T(0) : (s > smax ? smax : s);
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < kIters; ++k) {
         const T u = R.u2 - s * s;
         const T f = sweep_to_turn<T, N>(u, R) - target;
