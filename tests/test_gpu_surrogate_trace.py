@@ -1,0 +1,99 @@
+"""Surrogate-plus-fallback trace with the committed checkpoint against the FP64 oracle, and what
+the trained network gains over the method without it (the closed-form baseline alone, and the
+plain integrator)."""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+import parity
+from blackholerender_gb300 import FLAG_FALLBACK, FLAG_SURROGATE, TERM_CONFIG, Tracer, hits_numpy, workloads
+from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT, Surrogate
+
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "oracle"))
+
+pytestmark = pytest.mark.gpu
+
+# stated tolerances of the surrogate path against the FP64 oracle of the same rule
+DIR_MAX_RAD = 1e-4        # every surrogate ray outside the fallback band
+CROSS_R_REL_P99 = 1e-3    # the reference's own chord interpolation of the crossing is ~5e-4
+EDGE_REL = 1e-3           # crossings this close to a disk edge are ambiguous (both ways)
+
+
+@pytest.fixture(scope="module")
+def surrogate():
+    s = Surrogate(seed=2)
+    s.load(DEFAULT_CHECKPOINT)
+    yield s
+    s.close()
+
+
+def test_surrogate_c2_against_fp64_oracle(surrogate):
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG)[:4]
+    outs = surrogate.trace(views)
+    torch.cuda.synchronize()
+    st = surrogate.trace_stats()
+    assert st["surrogate"] > 0.9 * sum(v.rays for v in views)
+    rng = np.random.default_rng(5)
+    angs, rels = [], []
+    for v, o in zip(views, outs):
+        g = hits_numpy(o.cpu())
+        assert np.all((g["flags"] & (FLAG_SURROGATE | FLAG_FALLBACK)) != 0)  # every ray answered once
+        idx = rng.choice(v.rays, 5000, replace=False)
+        ref = O.trace_pixels(v, idx, fp64=True)
+        gg = g[idx]
+        rep = parity.compare(gg, ref, max_steps=v.max_steps, band=2e-3, edge_rel=EDGE_REL)
+        assert rep.class_mismatch == 0, rep.as_dict()
+        sm = ((gg["flags"] & FLAG_SURROGATE) != 0) & (ref["status"] == 1)
+        angs.append(O.angle(gg["dir"][sm], ref["dir"][sm]))
+        eq = sm & (gg["ncross"] == ref["ncross"])
+        for k in range(3):
+            m = eq & (ref["ncross"] > k)
+            rels.append(np.abs(gg["cross_r"][m, k] - ref["cross_r"][m, k]) / ref["cross_r"][m, k])
+    a = np.concatenate(angs)
+    r = np.concatenate(rels)
+    assert a.max() < DIR_MAX_RAD, (np.percentile(a, 99), a.max())
+    assert np.percentile(r, 99) < CROSS_R_REL_P99, np.percentile(r, 99)
+
+
+def test_network_gain_over_closed_form_baseline(surrogate):
+    # held-out orbits from the integrator: polar-angle error at the exit with and without the network
+    s = Surrogate(seed=4)
+    s.generate(50_000, per_orbit=4, seed=987654)
+    X, lab = s.samples(0, 200_000)
+    s.close()
+    exit_ = np.zeros(len(lab), bool)
+    exit_[3::4] = True
+    rc, beta = surrogate.features_to_orbit(X)
+    m = (lab == 0) & exit_ & (np.abs(beta) > 2e-3 / 27 ** 0.5)
+    pred = surrogate.eval(X[m, :3])[:, 0]
+    net = np.abs(pred - X[m, 3]) * surrogate.cfg.y_scale
+    base = np.abs(X[m, 3]) * surrogate.cfg.y_scale
+    assert np.percentile(net, 99) < 1e-4 and net.max() < 5e-4, (np.percentile(net, 99), net.max())
+    assert np.percentile(base, 99) > 100 * np.percentile(net, 99)
+
+
+def test_surrogate_path_faster_than_plain(surrogate):
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG)[:8]
+    outs = [torch.empty(v.rays * 64, dtype=torch.uint8, device="cuda") for v in views]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    with Tracer(0) as tr:
+        t_plain = timed(lambda: tr.trace(views, outs))
+    t_surr = timed(lambda: surrogate.trace(views, outs))
+    assert t_surr < t_plain / 1.2, (t_surr, t_plain)
