@@ -8,11 +8,16 @@ capture at r < 2.0001 -- 33.2 M rays per step. Inputs are camera views (no datas
 outputs are 64-byte hit records (2.1 GB per step, larger than L2, and L2 is also flushed
 between timed steps).
 
-  value  Mrays/s of the traced rays, device-timed with CUDA events on the launch stream
-  e2e    the same through bhr_trace_host: host views in, records in pinned host memory out,
-         device->host copies inside the timed region
-  roofline  the march kernel's FP32 FLOP rate (160 FLOP per executed step + 60 per ray)
-         against a measured FP32 peak (cuBLAS SGEMM, TF32 off) -- the path is FP32-pipe bound
+  value  Mrays/s of the learned-surrogate path (network + closed-form orbit, with the plain
+         integrator as fallback for near-critical, captured and out-of-range rays), device-timed
+         with CUDA events on the launch stream; the plain FP32 integrator on the same 16 views is
+         timed right after it (config.plain_mrays_s) and the two paths' escape directions are
+         compared ray by ray (config.agreement_vs_plain_fp32_rad)
+  e2e    the same through bhr_surrogate_trace_host: host views in, records in pinned host memory
+         out, device->host copies inside the timed region
+  roofline  the surrogate pass against the BF16 tensor peak (17,024 FLOP per network query);
+         roofline_plain: the plain march against a measured FP32 peak (160 FLOP per executed step
+         + 60 per ray, cuBLAS SGEMM with TF32 off as the FP32 denominator)
   cpu_baseline  the CPU restatement of the same march (oracle/, FP64) on all host cores,
          on a bounded sample of the same workload
 
@@ -29,6 +34,7 @@ import os
 import statistics
 import subprocess
 import sys
+import threading
 import time
 from pathlib import Path
 
@@ -42,6 +48,7 @@ METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "
 UNIT = "Mrays/s"
 F_STEP = 160  # FP32 FLOP per executed march step (FMA = 2)
 F_SETUP = 60  # FP32 FLOP per ray (ray generation, initial velocity, constants)
+F_MLP = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)  # BF16-equivalent FLOP per network query
 WORKLOAD = ("16 poses (seed 0) x 1920x1080, FOV 60, 450 steps (High preset), thin disk [6,20], "
             "escape r>1000, capture r<2.0001")
 
@@ -61,24 +68,35 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        self.lines = []
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
-                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "50",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
         except OSError:
             self.proc = None
+            return self
+        self.reader = threading.Thread(target=self._read, daemon=True)
+        self.reader.start()
         return self
 
+    def _read(self):
+        for ln in self.proc.stdout:
+            if ln.strip():
+                self.lines.append(ln)
+
+    def samples(self) -> int:
+        return len(self.lines)
+
     def __exit__(self, *exc):
-        self.lines = []
         if self.proc is not None:
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+                self.proc.wait()
+            self.reader.join(timeout=5)
 
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
@@ -205,7 +223,8 @@ def fp32_peak_tflops(dev) -> float:
 def run_gpu(args):
     import torch
 
-    from blackholerender_gb300 import HIT_BYTES, PREC_FP32, TERM_CONFIG, Tracer, workloads
+    from blackholerender_gb300 import FLAG_SURROGATE, HIT_BYTES, PREC_FP32, TERM_CONFIG, Tracer, hits_numpy, workloads
+    from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT, Surrogate
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -218,68 +237,99 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    views = workloads.c2_views(TERM_CONFIG)
+    views = workloads.c2_views(TERM_CONFIG)[:args.views]
     rays = sum(v.rays for v in views)
     tr = Tracer(local, block_size=args.block, chunk=args.chunk, refill=args.refill)
+    sur = Surrogate(device=local, seed=2)
+    trained_here = None
+    if DEFAULT_CHECKPOINT.exists() and not args.retrain:
+        sur.load(DEFAULT_CHECKPOINT)
+    else:  # train on this GPU with the library's own kernels (about 20 s)
+        t0 = time.perf_counter()
+        sur.generate(10_000_000, per_orbit=4, seed=7920)
+        sur.train(100_000, batch=16384, lr_max=2e-3, lr_min=1e-6)
+        trained_here = time.perf_counter() - t0
     outs = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step():
-        if args.launch == "multi":
-            tr.trace(views, outs, PREC_FP32, stream=stream)
-            return 1
-        for v, o in zip(views, outs):
-            tr.trace([v], [o], PREC_FP32, stream=stream)
-        return len(views)
+    def step_surrogate():
+        sur.trace_ptrs(views, outs, stream)
+        return len(views) + 1  # one surrogate kernel per view + one fallback march
+
+    def step_plain():
+        tr.trace(views, outs, PREC_FP32, stream=stream)
+        return 1
 
     for _ in range(max(args.warmup, 0)):
-        step()
-    torch.cuda.synchronize(dev)
-    # executed steps of one pass (identical every pass: the march is deterministic)
-    if args.launch == "multi":
-        tr.trace(views, outs, PREC_FP32, stream=stream)
-        steps_exec = tr.stats().steps
-    else:
-        steps_exec = 0
-        for v, o in zip(views, outs):
-            tr.trace([v], [o], PREC_FP32, stream=stream)
-            steps_exec += tr.stats().steps
+        step_plain()
+        step_surrogate()
     torch.cuda.synchronize(dev)
 
-    if dist:
-        dist.barrier()
+    # agreement of the surrogate path with the plain FP32 integrator on the same rays (no oracle)
+    step_plain()
     torch.cuda.synchronize(dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    launches = 0
-    with ClockSampler(local) as clk:
-        for k in range(args.steps):
+    plain_host = [hits_numpy(o.cpu()) for o in outs[:4]]
+    step_surrogate()
+    torch.cuda.synchronize(dev)
+    st = sur.trace_stats()
+    ang = []
+    for o, hp in zip(outs[:4], plain_host):
+        hs = hits_numpy(o.cpu())
+        m = ((hs["flags"] & FLAG_SURROGATE) != 0) & (hp["status"] == 1)
+        a = hs["dir"][m].astype(np.float64)
+        b = hp["dir"][m].astype(np.float64)
+        ang.append(np.arctan2(np.linalg.norm(np.cross(a, b), axis=1), np.sum(a * b, axis=1)))
+    ang = np.concatenate(ang)
+    agreement = {"p50": float(np.percentile(ang, 50)), "p99": float(np.percentile(ang, 99)),
+                 "max": float(ang.max()), "rays": int(len(ang))}
+    # phase times of one surrogate trace (dominant kernel: the surrogate pass)
+    step_surrogate()
+    t_pass, t_fb = sur.trace_times_ms()
+
+    def timed(step, k_steps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k_steps)]
+        launches = 0
+        for k in range(k_steps):
             flush.zero_()  # evict L2 between timed steps (outside the timed events)
             ev[k][0].record(stream)
             launches += step()
             ev[k][1].record(stream)
         torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) for a, b in ev], launches
+
     if dist:
         dist.barrier()
-    per_step = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(per_step)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        t_wait = time.perf_counter()  # keep the GPU loaded until the sampler reports (<= 3 s, untimed)
+        while clk.samples() < 2 and time.perf_counter() - t_wait < 3.0:
+            step_surrogate()
+            torch.cuda.synchronize(dev)
+        per_step, launches = timed(step_surrogate, args.steps)
     if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.barrier()
+    total_ms = sum(per_step)
+    per_plain, _ = timed(step_plain, args.steps)
+    plain_ms = sum(per_plain) / args.steps
+    if dist:
+        t = torch.tensor([total_ms, plain_ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms, plain_ms = float(t[0].item()), float(t[1].item())
     ms_per_step = total_ms / args.steps
     value = rays * world / (ms_per_step * 1e-3) / 1e6
+    plain_value = rays * world / (plain_ms * 1e-3) / 1e6
 
-    # ---- end to end through the host-buffer entry point
+    # ---- end to end through the host-buffer entry point (records in pinned host memory)
     host = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, pin_memory=True) for v in views]
     host_np = [h.numpy() for h in host]
-    tr.trace_host(views, host_np, PREC_FP32)
+    sur.trace_host(views, host_np)
     e2e_steps = max(2, min(args.steps, 5))
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        tr.trace_host(views, host_np, PREC_FP32)
+        sur.trace_host(views, host_np)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     if dist:
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
@@ -287,34 +337,44 @@ def run_gpu(args):
         e2e_s = float(t.item())
     e2e = {"value": rays * world / e2e_s / 1e6, "unit": UNIT,
            "h2d_bytes_per_step": len(views) * 160, "d2h_bytes_per_step": rays * HIT_BYTES,
-           "ms_per_step": e2e_s * 1e3, "api": "bhr_trace_host (pinned host records)"}
+           "ms_per_step": e2e_s * 1e3, "api": "bhr_surrogate_trace_host (pinned host records)"}
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the march kernel
-    flop = steps_exec * F_STEP + rays * F_SETUP
-    ms_per_launch = ms_per_step * (1 if args.launch == "multi" else 1.0 / len(views))
-    flop_per_launch = flop if args.launch == "multi" else flop / len(views)
-    achieved = flop_per_launch / (ms_per_launch * 1e-3) / 1e12
-    peak_meas = fp32_peak_tflops(dev)
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    nominal = sms * 128 * 2 * 2.07e9 / 1e12
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
+    # ---- roofline of the dominant kernel (the surrogate pass): tensor pipe, MLP FLOPs
+    peaks = {}
+    pfile = ROOT / "MEASURED_PEAKS.json"
+    if pfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get(f"k_march_{args.launch}")
+            peaks = json.loads(pfile.read_text())
         except Exception:
-            traffic = None
-    roof = {"bound": "fp32", "achieved": achieved, "peak": peak_meas, "unit": "TFLOP/s",
-            "frac": achieved / peak_meas, "traffic": traffic,
-            "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (FP32 FMA pipe)",
-            "nominal_peak": nominal, "frac_of_nominal": achieved / nominal,
-            "flop_per_launch": flop_per_launch, "ms_per_launch": ms_per_launch,
-            "algorithm": f"{F_STEP} FLOP per executed step + {F_SETUP} per ray; {steps_exec / rays:.2f} steps/ray"}
+            peaks = {}
+    bf16_peak = peaks.get("bf16_tflops")
+    peak_src = "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS)" if bf16_peak else "fallback 1900 TFLOP/s"
+    bf16_peak = bf16_peak or 1900.0
+    mlp_flop = st["mlp_queries"] * F_MLP
+    achieved = mlp_flop / (t_pass * 1e-3) / 1e12
+    fp32_peak = fp32_peak_tflops(dev)
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": achieved / bf16_peak, "traffic": None, "peak_source": peak_src,
+            "kernel": "k_surrogate (one launch per view; ms below is the 16-view pass)",
+            "algorithm": f"{F_MLP} BF16 FLOP per network query; {st['mlp_queries']} queries "
+                         f"({st['mlp_queries'] / max(st['surrogate'], 1):.2f} per surrogate ray)",
+            "pass_ms": t_pass, "fallback_ms": t_fb,
+            "note": "the pass is issue-bound on the CUDA cores (ray setup, closed-form orbit, activations);"
+                    " the tensor pipe is not its limit"}
+    steps_plain = None
+    tr.trace(views, outs, PREC_FP32, stream=stream)
+    steps_plain = tr.stats().steps
+    plain_flop = steps_plain * F_STEP + rays * F_SETUP
+    roof_plain = {"bound": "fp32", "achieved": plain_flop / (plain_ms * 1e-3) / 1e12, "peak": fp32_peak,
+                  "unit": "TFLOP/s", "frac": plain_flop / (plain_ms * 1e-3) / 1e12 / fp32_peak,
+                  "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off",
+                  "algorithm": f"{F_STEP} FLOP per executed step + {F_SETUP} per ray; "
+                               f"{steps_plain / rays:.2f} steps/ray"}
 
     cpu = None
     if not args.no_cpu and world == 1:
@@ -326,16 +386,25 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "views": len(views), "rays_per_step": rays, "method": "plain",
-                   "launch": args.launch, "l2": "inputs are camera views; 2.1 GB of records per step and a "
-                   "256 MiB L2 flush between timed steps", "parallelism": f"replicas x{world}"},
+        "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic",
+        "config": {"workload": WORKLOAD if len(views) == 16 else f"first {len(views)} of: {WORKLOAD}",
+                   "views": len(views), "rays_per_step": rays,
+                   "method": "learned surrogate + plain FP32 integrator fallback",
+                   "plain_mrays_s": plain_value, "plain_ms_per_step": plain_ms,
+                   "speedup_vs_plain": value / plain_value,
+                   "surrogate_fraction": st["surrogate"] / rays, "fallback_rays": st["fallback"],
+                   "capture_flag_disagreements": st["capture_disagree"],
+                   "agreement_vs_plain_fp32_rad": agreement,
+                   "checkpoint": "trained in this run" if trained_here else str(DEFAULT_CHECKPOINT.relative_to(ROOT)),
+                   "train_s": trained_here,
+                   "l2": "inputs are camera views; 2.1 GB of records per step and a 256 MiB L2 flush between "
+                         "timed steps", "parallelism": f"replicas x{world}"},
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": roof,
+        "roofline_plain": roof_plain,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "steps_per_ray": steps_exec / rays,
         "per_step_ms": per_step,
     }
     print(json.dumps(line), flush=True)
@@ -346,15 +415,16 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--launch", default="multi", choices=["multi", "one"])
+    ap.add_argument("--retrain", action="store_true", help="train the surrogate here instead of loading it")
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--refill", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--views", type=int, default=16, help="first N of the 16 poses (small profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")

@@ -24,6 +24,8 @@ struct WorkQueue {
     unsigned long long surr_rays;    // rays answered by the surrogate
     unsigned long long fb_count;     // rays the surrogate sent to the integrator
     unsigned long long capture_disagree;  // surrogate capture flag disagreed with b vs sqrt(27)
+    unsigned long long mlp_queries;  // network queries of surrogate rays (exit + crossings)
+    unsigned long long mlp_rows;     // network rows evaluated (32 per batch, padding included)
     unsigned long long view_t_end[kMaxViews];  // globaltimer when a view's last ray finished
 };
 

@@ -724,7 +724,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
     float4* qb = S.q[warp];
     float2* ob = S.o[warp];
     const float beta_band = nm.band / kSqrt27f;
-    unsigned long long n_surr = 0, n_dis = 0;
+    unsigned long long n_surr = 0, n_dis = 0, n_q = 0, n_rows = 0;
     for (;;) {
         unsigned long long chunk = 0;
         if (lane == 0) chunk = atomicAdd(&q->next_chunk, 1ull);
@@ -821,6 +821,8 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
         const int nq = 32 + total;
 #pragma unroll 1
         for (int qb0 = 0; qb0 < nq; qb0 += 32) mlp_eval32(S.N, qb + qb0, ob + qb0);
+        n_rows += (unsigned long long)((nq + 31) / 32) * (lane == 0 ? 32 : 0);
+        n_q += sur ? 1 + ncand : 0;
         // ---- results
         const float2 oe = ob[lane];
         if (sur && oe.y > 0.f) {  // the learned capture flag disagrees with b > sqrt(27): integrator decides
@@ -884,9 +886,12 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
     for (int o = 16; o > 0; o >>= 1) {
         n_surr += __shfl_xor_sync(0xffffffffu, n_surr, o);
         n_dis += __shfl_xor_sync(0xffffffffu, n_dis, o);
+        n_q += __shfl_xor_sync(0xffffffffu, n_q, o);
     }
     if (lane == 0) {
         atomicAdd(&q->surr_rays, n_surr);
+        atomicAdd(&q->mlp_queries, n_q);
+        atomicAdd(&q->mlp_rows, n_rows);
         if (n_dis) atomicAdd(&q->capture_disagree, n_dis);
     }
 }

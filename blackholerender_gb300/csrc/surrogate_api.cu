@@ -39,6 +39,11 @@ struct bhr_surrogate {
     unsigned long long last[4] = {0, 0, 0, 0};
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // start, surrogate pass done, fallback done
+    // bhr_surrogate_trace_host: device staging and two streams
+    bhr_hit* staging = nullptr;
+    int64_t staging_rays = 0;
+    cudaStream_t hs[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -141,6 +146,7 @@ int bhr_surrogate_create(bhr_surrogate** out, int device, const bhr_surrogate_co
     if (e == cudaSuccess) e = cudaMemcpy(s->params, P.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(s->adam_m, 0, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMemset(s->adam_v, 0, sizeof(float) * kNParams);
+    for (int k = 0; e == cudaSuccess && k < 3; ++k) e = cudaEventCreate(&s->ev[k]);
     if (e != cudaSuccess) {
         bhr_surrogate_destroy(s);
         return fail(BHR_ERR_OOM, std::string("bhr_surrogate_create: ") + cudaGetErrorString(e));
@@ -153,8 +159,12 @@ int bhr_surrogate_destroy(bhr_surrogate* s) {
     if (!s) return BHR_OK;
     DevGuard dg(s->device);
     for (void* p : {(void*)s->params, (void*)s->grads, (void*)s->adam_m, (void*)s->adam_v, (void*)s->X,
-                    (void*)s->lab, (void*)s->stats, (void*)s->loss, (void*)s->q, (void*)s->fb})
+                    (void*)s->lab, (void*)s->stats, (void*)s->loss, (void*)s->q, (void*)s->fb, (void*)s->staging})
         if (p) cudaFree(p);
+    for (cudaEvent_t& e : s->ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t& st : s->hs)
+        if (st) cudaStreamDestroy(st);
     delete s;
     return BHR_OK;
 }
@@ -370,6 +380,7 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
     if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
     e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
     // 1) the surrogate pass of every view
     std::vector<bhr::DevView> dvs(static_cast<size_t>(nviews));
     std::vector<bhr::Rule> rules(static_cast<size_t>(nviews));
@@ -388,6 +399,7 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
         e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3, st);
     }
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     // 2) the integrator on the fallback rays: one launch for all views when they share a rule
     bhr::LaunchCfg cfg{};
     cfg.block = 512;
@@ -412,11 +424,82 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
                                        &s->q[2 * k].fb_count, cfg, st);
         }
     }
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[2], st);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace");
     s->last_stream = st;
     s->last_nviews = nviews;
     s->have_last = true;
     return BHR_OK;
+}
+
+int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2) {
+    if (!s || !ms2) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_times: NULL");
+    if (!s->have_last) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_times: no trace yet");
+    DevGuard dg(s->device);
+    cudaError_t e = cudaEventSynchronize(s->ev[2]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms2[0], s->ev[0], s->ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms2[1], s->ev[1], s->ev[2]);
+    return e == cudaSuccess ? BHR_OK : cfail(e, "bhr_surrogate_trace_times");
+}
+
+int bhr_surrogate_trace_host(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_host) {
+    if (!s || !views || nviews <= 0 || !out_host) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_host: bad arguments");
+    int64_t biggest = 0;
+    for (int k = 0; k < nviews; ++k) {
+        if (!out_host[k]) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_host: output buffer is NULL");
+        biggest = std::max<int64_t>(biggest, int64_t(views[k].width) * views[k].height);
+    }
+    DevGuard dg(s->device);
+    const int64_t half = std::max<int64_t>(biggest, int64_t(1) << 22);
+    cudaError_t e = cudaSuccess;
+    if (half > s->staging_rays) {
+        if (s->staging) cudaFree(s->staging);
+        s->staging = nullptr;
+        s->staging_rays = 0;
+        e = cudaMalloc(&s->staging, sizeof(bhr_hit) * size_t(2 * half));
+        if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace_host: staging");
+        s->staging_rays = half;
+    }
+    for (int k = 0; e == cudaSuccess && k < 2; ++k)
+        if (!s->hs[k]) e = cudaStreamCreateWithFlags(&s->hs[k], cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace_host");
+    int rc = BHR_OK;
+    std::vector<bhr_hit*> dst;
+    int g = 0;
+    // groups of views that fit one staging half; the group's records go to the host on its
+    // stream while the next group is traced on the other
+    for (int k0 = 0; rc == BHR_OK && k0 < nviews; ++g) {
+        int k1 = k0;
+        int64_t acc = 0;
+        while (k1 < nviews && k1 - k0 < bhr::kMaxViews) {
+            const int64_t n = int64_t(views[k1].width) * views[k1].height;
+            if (acc + n > s->staging_rays && k1 > k0) break;
+            acc += n;
+            ++k1;
+        }
+        cudaStream_t st = s->hs[g & 1];
+        bhr_hit* base = s->staging + (g & 1) * s->staging_rays;
+        dst.clear();
+        int64_t off = 0;
+        for (int k = k0; k < k1; ++k) {
+            dst.push_back(base + off);
+            off += int64_t(views[k].width) * views[k].height;
+        }
+        rc = bhr_surrogate_trace(s, views + k0, k1 - k0, dst.data(), st);
+        off = 0;
+        for (int k = k0; rc == BHR_OK && k < k1; ++k) {
+            const int64_t n = int64_t(views[k].width) * views[k].height;
+            e = cudaMemcpyAsync(out_host[k], base + off, sizeof(bhr_hit) * size_t(n), cudaMemcpyDeviceToHost, st);
+            if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_trace_host: copy");
+            off += n;
+        }
+        k0 = k1;
+    }
+    for (cudaStream_t st : s->hs) {
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess && rc == BHR_OK) rc = cfail(e, "bhr_surrogate_trace_host: synchronize");
+    }
+    return rc;
 }
 
 int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
@@ -427,12 +510,14 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
     cudaError_t e = cudaStreamSynchronize(s->last_stream);
     if (e == cudaSuccess) e = cudaMemcpy(q.data(), s->q, sizeof(bhr::WorkQueue) * q.size(), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace_stats");
-    for (int k = 0; k < 4; ++k) out[k] = 0;
+    for (int k = 0; k < 6; ++k) out[k] = 0;
     for (int v = 0; v < s->last_nviews; ++v) {
         out[0] += q[2 * v].surr_rays;
         out[1] += q[2 * v].fb_count;
         out[2] += q[2 * v].capture_disagree;
         out[3] += q[2 * v + 1].steps;
+        out[4] += q[2 * v].mlp_queries;
+        out[5] += q[2 * v].mlp_rows;
     }
     out[3] += q[2 * size_t(s->last_nviews)].steps;
     return BHR_OK;

@@ -120,7 +120,23 @@ class Surrogate:
         ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
         _abi.check(_abi.lib().bhr_surrogate_trace(self.h, arr, n, ptrs, ctypes.c_void_p(stream.cuda_stream)))
 
+    def trace_host(self, views, outs):
+        """bhr_surrogate_trace_host: records land in host arrays (one per view)."""
+        n = len(views)
+        for v, o in zip(views, outs):
+            if o.nbytes < v.rays * 64:
+                raise ValueError("host output buffer too small")
+        arr = (_abi.View * n)(*views)
+        ptrs = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
+        _abi.check(_abi.lib().bhr_surrogate_trace_host(self.h, arr, n, ptrs))
+
+    def trace_times_ms(self):
+        o = (ctypes.c_float * 2)()
+        _abi.check(_abi.lib().bhr_surrogate_trace_times(self.h, o))
+        return float(o[0]), float(o[1])
+
     def trace_stats(self):
-        o = (ctypes.c_uint64 * 4)()
+        o = (ctypes.c_uint64 * 6)()
         _abi.check(_abi.lib().bhr_surrogate_trace_stats(self.h, o))
-        return {"surrogate": o[0], "fallback": o[1], "capture_disagree": o[2], "fallback_steps": o[3]}
+        return {"surrogate": o[0], "fallback": o[1], "capture_disagree": o[2], "fallback_steps": o[3],
+                "mlp_queries": o[4], "mlp_rows": o[5]}

@@ -243,9 +243,14 @@ int bhr_surrogate_load(bhr_surrogate* s, const char* path);
 /* Surrogate-plus-fallback trace (CONFIG rule, lensing on): stream-ordered like bhr_trace. */
 int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
                         void* cuda_stream);
+/* Host-memory variant (records copied to out_host[k]; synchronous), as bhr_trace_host. */
+int bhr_surrogate_trace_host(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_host);
+/* Device time of the last bhr_surrogate_trace: ms2[0] surrogate pass, ms2[1] fallback march. */
+int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2);
 /* Of the last bhr_surrogate_trace: rays answered by the surrogate, rays sent to the integrator,
- * capture-flag disagreements (also sent to the integrator), integrator steps of the fallback. */
-int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out4);
+ * capture-flag disagreements (also sent to the integrator), integrator steps of the fallback,
+ * network queries of surrogate rays, network rows evaluated (batches of 32, padding included). */
+int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out6);
 
 /* Statistics of the last bhr_trace on ctx (synchronises that call's stream). */
 int bhr_trace_stats(bhr_ctx* ctx, bhr_stats* stats);
