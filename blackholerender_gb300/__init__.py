@@ -15,7 +15,8 @@ from . import _abi
 from ._abi import (  # noqa: F401
     DISK_NONE, DISK_THIN, DISK_VOLUMETRIC, FLAG_FALLBACK, FLAG_FP64, FLAG_NONFINITE, FLAG_SURROGATE,
     HIT_DTYPE, METHOD_PLAIN, METHOD_SURROGATE, PREC_FP32, PREC_MIXED, SQRT27, STATUS_BUDGET,
-    STATUS_CAPTURED, STATUS_ESCAPED, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, Options, Stats, View,
+    STATUS_CAPTURED, STATUS_ESCAPED, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, LaunchShape, Options, Stats,
+    View,
 )
 
 HIT_BYTES = 64
@@ -65,10 +66,10 @@ class Tracer:
     """A bhr context on one CUDA device (bhr_create / bhr_trace / bhr_destroy)."""
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, chunk: int = 0,
-                 refill: int = 0):
+                 refill: int = 0, tile_w: int = 0):
         L = _abi.lib()
         self._ctx = ctypes.c_void_p()
-        opts = Options(device, block_size, blocks_per_sm, chunk, refill)
+        opts = Options(device, block_size, blocks_per_sm, chunk, refill, tile_w)
         _abi.check(L.bhr_create(ctypes.byref(self._ctx), ctypes.byref(opts)))
         self.device = device
 
@@ -137,3 +138,81 @@ class Tracer:
         out = (ctypes.c_double * nviews)()
         _abi.check(_abi.lib().bhr_trace_view_times(self._ctx, out, nviews), self._ctx)
         return np.array(out[:], dtype=np.float64)
+
+    # ---- launch shapes, autotuner, graph plans
+    @property
+    def launch_shape(self) -> LaunchShape:
+        sh = LaunchShape()
+        _abi.check(_abi.lib().bhr_get_launch_shape(self._ctx, ctypes.byref(sh)), self._ctx)
+        return sh
+
+    @launch_shape.setter
+    def launch_shape(self, sh: LaunchShape) -> None:
+        _abi.check(_abi.lib().bhr_set_launch_shape(self._ctx, ctypes.byref(sh)), self._ctx)
+
+    def autotune(self, views: Sequence[View], outs, precision: int = PREC_FP32, reps: int = 3) -> LaunchShape:
+        """bhr_autotune on device tensors `outs` (one per view); returns the chosen shape."""
+        n = len(views)
+        arr = (View * n)(*views)
+        ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
+        best = LaunchShape()
+        _abi.check(_abi.lib().bhr_autotune(self._ctx, arr, n, ptrs, precision, reps, ctypes.byref(best)), self._ctx)
+        return best
+
+    def plan(self, views: Sequence[View], outs, precision: int = PREC_FP32, autotune: bool = False) -> "Plan":
+        return Plan(self, views, outs, precision, autotune)
+
+
+class Plan:
+    """bhr_plan_*: a fixed batch of views traced by one instantiated CUDA graph."""
+
+    def __init__(self, tracer: Tracer, views: Sequence[View], outs, precision: int = PREC_FP32,
+                 autotune: bool = False):
+        self._tracer = tracer
+        self._outs = list(outs)  # keeps the bound device buffers alive
+        n = len(views)
+        self.nviews = n
+        arr = (View * n)(*views)
+        ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in self._outs])
+        self._p = ctypes.c_void_p()
+        _abi.check(_abi.lib().bhr_plan_create(tracer._ctx, arr, n, ptrs, precision, int(autotune),
+                                              ctypes.byref(self._p)), tracer._ctx)
+
+    def launch(self, stream=None) -> None:
+        import torch
+
+        if stream is None:
+            stream = torch.cuda.current_stream(torch.device("cuda", self._tracer.device))
+        _abi.check(_abi.lib().bhr_plan_launch(self._p, ctypes.c_void_p(stream.cuda_stream)), self._tracer._ctx)
+
+    def update(self, views: Sequence[View]) -> None:
+        n = len(views)
+        arr = (View * n)(*views)
+        _abi.check(_abi.lib().bhr_plan_update(self._p, arr, n), self._tracer._ctx)
+
+    @property
+    def launch_shape(self) -> LaunchShape:
+        sh = LaunchShape()
+        _abi.check(_abi.lib().bhr_plan_launch_shape(self._p, ctypes.byref(sh)), self._tracer._ctx)
+        return sh
+
+    def stats(self) -> Stats:
+        s = Stats()
+        _abi.check(_abi.lib().bhr_plan_stats(self._p, ctypes.byref(s)), self._tracer._ctx)
+        return s
+
+    def view_times_ms(self) -> np.ndarray:
+        out = (ctypes.c_double * self.nviews)()
+        _abi.check(_abi.lib().bhr_plan_view_times(self._p, out, self.nviews), self._tracer._ctx)
+        return np.array(out[:], dtype=np.float64)
+
+    def close(self) -> None:
+        if self._p:
+            _abi.lib().bhr_plan_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

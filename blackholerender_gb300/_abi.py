@@ -91,8 +91,23 @@ class Options(ctypes.Structure):
         ("blocks_per_sm", ctypes.c_int32),
         ("chunk", ctypes.c_int32),
         ("refill", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("tile_w", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
+
+
+class LaunchShape(ctypes.Structure):
+    _fields_ = [
+        ("block_size", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+        ("chunk", ctypes.c_int32),
+        ("refill", ctypes.c_int32),
+        ("tile_w", ctypes.c_int32),
+        ("ms", ctypes.c_float),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Stats(ctypes.Structure):
@@ -140,6 +155,9 @@ SIGNATURES = {
     "bhr_view_apply_preset": (ctypes.c_int, [_VP, ctypes.c_int]),
     "bhr_view_look_at": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "bhr_view_set_fov": (ctypes.c_int, [_VP, ctypes.c_float]),
+    "bhr_look_rotation": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "bhr_view_set_pose": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float)]),
     "bhr_view_orbit_pose": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "bhr_view_rays": (ctypes.c_int64, [_VP]),
     "bhr_trace": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, _P]),
@@ -147,6 +165,18 @@ SIGNATURES = {
     "bhr_trace_noalloc": (ctypes.c_int, [_VP, _P, _P]),
     "bhr_trace_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
     "bhr_trace_view_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "bhr_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),
+    "bhr_set_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),
+    "bhr_autotune": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(LaunchShape)]),
+    "bhr_plan_create": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(_P)]),
+    "bhr_plan_update": (ctypes.c_int, [_P, _VP, ctypes.c_int]),
+    "bhr_plan_launch": (ctypes.c_int, [_P, _P]),
+    "bhr_plan_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),
+    "bhr_plan_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
+    "bhr_plan_view_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "bhr_plan_destroy": (ctypes.c_int, [_P]),
 }
 
 class SurrogateConfig(ctypes.Structure):

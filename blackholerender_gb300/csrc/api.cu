@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -18,18 +19,30 @@
 #include "host_views.h"
 #include "kernels.cuh"
 
-struct bhr_ctx {
-    int device = 0;
-    int sms = 0;
-    int block = 512;        // threads per block of the FP32 march
-    int blocks_per_sm = 0;  // 0: as many as fit
-    int chunk = 64;         // rays per work chunk
-    int refill = 8;         // idle lanes that trigger a refill
-    bhr::WorkQueue* q = nullptr;  // one per batch slot
+// Device scratch of a trace: one work queue per launch batch, and the FP64 queues of MIXED.
+struct TraceScratch {
+    bhr::WorkQueue* q = nullptr;
     int nq = 0;
     int2* band = nullptr;
     bhr::PromoEntry* promo = nullptr;
-    int64_t scratch_rays = 0;  // capacity of band / promo in rays
+    int64_t rays = 0;  // capacity of band / promo in rays
+    void release() {
+        if (q) cudaFree(q);
+        if (band) cudaFree(band);
+        if (promo) cudaFree(promo);
+        q = nullptr;
+        band = nullptr;
+        promo = nullptr;
+        nq = 0;
+        rays = 0;
+    }
+};
+
+struct bhr_ctx {
+    int device = 0;
+    int sms = 0;
+    bhr_launch_shape shape{512, 0, 64, 8, 32, 0.0f};  // launch shape of the FP32 march
+    TraceScratch scr;
     // bhr_trace_host: device staging (two halves) and two streams, created on first use
     bhr_hit* staging = nullptr;
     int64_t staging_rays = 0;  // rays per half
@@ -39,7 +52,25 @@ struct bhr_ctx {
     std::vector<std::pair<int, int>> last_slots;  // (work queue, view slot) per view of the last trace
     int last_nviews = 0;
     bool have_last = false;
+    std::map<std::string, bhr_launch_shape> tuned;  // autotuner results by workload signature
     std::string err;
+};
+
+// A batch of views traced by one instantiated CUDA graph (bhr_plan_*).
+struct bhr_plan {
+    bhr_ctx* ctx = nullptr;
+    std::vector<bhr_view> views;
+    std::vector<bhr_hit*> out;
+    int precision = BHR_PREC_FP32;
+    bhr_launch_shape shape{};
+    TraceScratch scr;  // the plan's own: the graph holds these addresses
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int batches = 0;
+    std::vector<std::pair<int, int>> slots;
+    cudaStream_t last_stream = nullptr;
+    bool launched = false;
 };
 
 namespace {
@@ -70,39 +101,172 @@ using bhr::host::shader_r_esc_min;
 
 bool same_rule(const bhr::Rule& a, const bhr::Rule& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
 
-int ensure_scratch(bhr_ctx* c, int nbatches, int64_t rays, bool mixed) {
-    if (nbatches > c->nq) {
-        if (c->q) cudaFree(c->q);
-        c->q = nullptr;
-        c->nq = 0;
-        cudaError_t e = cudaMalloc(&c->q, sizeof(bhr::WorkQueue) * size_t(nbatches));
+int ensure_scratch(bhr_ctx* c, TraceScratch& scr, int nbatches, int64_t rays, bool mixed) {
+    if (nbatches > scr.nq) {
+        if (scr.q) cudaFree(scr.q);
+        scr.q = nullptr;
+        scr.nq = 0;
+        cudaError_t e = cudaMalloc(&scr.q, sizeof(bhr::WorkQueue) * size_t(nbatches));
         if (e != cudaSuccess) return fail(c, BHR_ERR_OOM, std::string("work queue: ") + cudaGetErrorString(e));
-        c->nq = nbatches;
+        scr.nq = nbatches;
     }
-    if (mixed && rays > c->scratch_rays) {
-        if (c->band) cudaFree(c->band);
-        if (c->promo) cudaFree(c->promo);
-        c->band = nullptr;
-        c->promo = nullptr;
-        c->scratch_rays = 0;
-        cudaError_t e = cudaMalloc(&c->band, sizeof(int2) * size_t(rays));
-        if (e == cudaSuccess) e = cudaMalloc(&c->promo, sizeof(bhr::PromoEntry) * size_t(rays));
+    if (mixed && rays > scr.rays) {
+        if (scr.band) cudaFree(scr.band);
+        if (scr.promo) cudaFree(scr.promo);
+        scr.band = nullptr;
+        scr.promo = nullptr;
+        scr.rays = 0;
+        cudaError_t e = cudaMalloc(&scr.band, sizeof(int2) * size_t(rays));
+        if (e == cudaSuccess) e = cudaMalloc(&scr.promo, sizeof(bhr::PromoEntry) * size_t(rays));
         if (e != cudaSuccess) return fail(c, BHR_ERR_OOM, std::string("FP64 queue: ") + cudaGetErrorString(e));
-        c->scratch_rays = rays;
+        scr.rays = rays;
     }
     return BHR_OK;
 }
 
-bhr::LaunchCfg make_cfg(const bhr_ctx* c, int variant, bool multi, bool mixed) {
+int check_shape(bhr_ctx* c, const bhr_launch_shape& s) {
+    if (s.block_size != 256 && s.block_size != 512)
+        return fail(c, BHR_ERR_INVALID_ARG, "launch shape: block_size must be 256 or 512");
+    if (s.blocks_per_sm < 0 || s.chunk < 0 || s.refill < 0 || s.refill > 32)
+        return fail(c, BHR_ERR_INVALID_ARG, "launch shape: blocks_per_sm, chunk >= 0 and refill in 0..32");
+    if (s.tile_w != 0 && s.tile_w != 32 && s.tile_w != 16 && s.tile_w != 8)
+        return fail(c, BHR_ERR_INVALID_ARG, "launch shape: tile_w must be 32, 16 or 8");
+    return BHR_OK;
+}
+
+bhr::LaunchCfg make_cfg(const bhr_ctx* c, const bhr_launch_shape& sh, int variant, bool multi, bool mixed) {
     bhr::LaunchCfg cfg{};
-    cfg.block = c->block;
+    cfg.block = sh.block_size;
     cfg.variant = variant;
     const int fit = std::max(1, bhr::march_blocks_per_sm(cfg.block, variant, multi, mixed));
-    const int bps = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, fit) : fit;
+    const int bps = sh.blocks_per_sm > 0 ? std::min(sh.blocks_per_sm, fit) : fit;
     cfg.grid = c->sms * bps;
-    cfg.refill = std::max(1, std::min(c->refill, 32));
-    cfg.chunk = std::max(32, c->chunk);
+    cfg.refill = std::max(1, std::min(sh.refill > 0 ? sh.refill : 8, 32));
+    cfg.chunk = (std::max(32, sh.chunk > 0 ? sh.chunk : 64) + 31) / 32 * 32;
     return cfg;
+}
+
+int tile_of(const bhr_launch_shape& sh) { return sh.tile_w == 16 || sh.tile_w == 8 ? sh.tile_w : 32; }
+
+int validate(bhr_ctx* c, const char* who, const bhr_view* views, int nviews, bhr_hit* const* out, int precision,
+             int64_t* rays_out) {
+    if (!views || nviews <= 0 || !out) return fail(c, BHR_ERR_INVALID_ARG, std::string(who) + ": no views or outputs");
+    if (precision != BHR_PREC_FP32 && precision != BHR_PREC_MIXED)
+        return fail(c, BHR_ERR_INVALID_ARG, std::string(who) + ": unknown precision");
+    int64_t rays = 0;
+    for (int k = 0; k < nviews; ++k) {
+        const int rc = check_view(c, views[k], k);
+        if (rc != BHR_OK) return rc;
+        if (!out[k]) return fail(c, BHR_ERR_INVALID_ARG, std::string(who) + ": output buffer " + std::to_string(k) + " is NULL");
+        if (reinterpret_cast<uintptr_t>(out[k]) % 16 != 0)
+            return fail(c, BHR_ERR_INVALID_ARG, std::string(who) + ": output buffers must be 16-byte aligned");
+        rays += int64_t(views[k].width) * views[k].height;
+    }
+    *rays_out = rays;
+    return BHR_OK;
+}
+
+// Launch sequence of one trace (views already validated): views grouped by rule, one
+// persistent launch per group and per kMaxViews views, each with its own work queue.
+// Stream-ordered; captures cleanly into a graph (no host synchronisation, no allocation
+// once `scr` is large enough).
+int run_trace(bhr_ctx* c, const bhr_launch_shape& shape, TraceScratch& scr, const bhr_view* views, int nviews,
+              bhr_hit* const* out_dev, int precision, int64_t rays, cudaStream_t st,
+              std::vector<std::pair<int, int>>* slots_out, int* batches_out) {
+    const bool mixed = precision == BHR_PREC_MIXED;
+    std::vector<bhr::Rule> rules;
+    std::vector<std::vector<int>> groups;
+    for (int k = 0; k < nviews; ++k) {
+        const bhr::Rule r = make_rule(views[k]);
+        size_t g = 0;
+        while (g < rules.size() && !same_rule(rules[g], r)) ++g;
+        if (g == rules.size()) {
+            rules.push_back(r);
+            groups.emplace_back();
+        }
+        groups[g].push_back(k);
+    }
+    int nb = 0;
+    for (const auto& g : groups) nb += int((g.size() + bhr::kMaxViews - 1) / bhr::kMaxViews);
+    int rc = ensure_scratch(c, scr, nb, rays, mixed);
+    const int fp64_grid = c->sms * 8;
+    const int tile = tile_of(shape);
+    int bi = 0;
+    std::vector<std::pair<int, int>> slots(size_t(nviews), {0, 0});
+    for (size_t g = 0; rc == BHR_OK && g < groups.size(); ++g) {
+        const bhr::Rule& rule = rules[g];
+        const int variant = bhr::rule_variant(rule);
+        const std::vector<int>& members = groups[g];
+        for (size_t m0 = 0; rc == BHR_OK && m0 < members.size(); m0 += bhr::kMaxViews, ++bi) {
+            bhr::Scratch sc{scr.q + bi, scr.band, scr.promo};
+            cudaError_t e = cudaMemsetAsync(sc.q, 0, sizeof(bhr::WorkQueue), st);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(c, e, "trace: cudaMemsetAsync");
+                break;
+            }
+            const size_t nv = std::min<size_t>(bhr::kMaxViews, members.size() - m0);
+            if (nviews == 1) {
+                const bhr::DevView dv = make_dev_view(views[0], out_dev[0], tile);
+                e = bhr::launch_march_one(dv, rule, sc, mixed, make_cfg(c, shape, variant, false, mixed), st);
+                if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_one(dv, rule, sc, fp64_grid, st);
+            } else {
+                static thread_local bhr::ViewBatch b;  // ~12 KB, passed by value as a kernel parameter
+                const bhr::LaunchCfg cfg = make_cfg(c, shape, variant, true, mixed);
+                b.nviews = int(nv);
+                b.rule = rule;
+                int64_t chunk_acc = 0;
+                for (size_t k = 0; k < nv; ++k) {
+                    const int vi = members[m0 + k];
+                    slots[size_t(vi)] = {bi, int(k)};
+                    b.views[k] = make_dev_view(views[vi], out_dev[vi], tile);
+                    b.views[k].chunk_start = chunk_acc;
+                    chunk_acc += (b.views[k].work + cfg.chunk - 1) / cfg.chunk;
+                }
+                b.total_chunks = chunk_acc;
+                e = bhr::launch_march_multi(b, sc, mixed, cfg, st);
+                if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_multi(b, sc, fp64_grid, st);
+            }
+            if (e != cudaSuccess) rc = cuda_fail(c, e, "trace: kernel launch");
+        }
+    }
+    if (rc == BHR_OK) {
+        if (slots_out) *slots_out = std::move(slots);
+        if (batches_out) *batches_out = nb;
+    }
+    return rc;
+}
+
+int read_queues(bhr_ctx* c, const TraceScratch& scr, int batches, cudaStream_t st, std::vector<bhr::WorkQueue>* qs,
+                const char* who) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(st);
+    qs->resize(size_t(batches));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(qs->data(), scr.q, sizeof(bhr::WorkQueue) * qs->size(), cudaMemcpyDeviceToHost);
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? BHR_OK : cuda_fail(c, e, who);
+}
+
+void sum_stats(const std::vector<bhr::WorkQueue>& qs, int64_t rays, bhr_stats* s) {
+    std::memset(s, 0, sizeof *s);
+    s->rays = uint64_t(rays);
+    for (const auto& q : qs) {
+        s->steps += q.steps;
+        s->fp64_rays += q.fp64_rays;
+        s->fp64_steps += q.fp64_steps;
+        s->nonfinite += q.nonfinite;
+    }
+}
+
+void view_times(const std::vector<bhr::WorkQueue>& qs, const std::vector<std::pair<int, int>>& slots, double* ms,
+                int nviews) {
+    for (int k = 0; k < nviews; ++k) {
+        const bhr::WorkQueue& q = qs[size_t(slots[size_t(k)].first)];
+        const int s = slots[size_t(k)].second;
+        ms[k] = q.view_t_end[s] >= q.t_start ? double(q.view_t_end[s] - q.t_start) * 1e-6 : -1.0;
+    }
 }
 
 }  // namespace
@@ -153,18 +317,20 @@ int bhr_create(bhr_ctx** out, const bhr_options* opts) {
     cudaSetDevice(c->device);
     c->sms = prop.multiProcessorCount;
     if (opts) {
-        if (opts->block_size == 256 || opts->block_size == 512) {
-            c->block = opts->block_size;
-        } else if (opts->block_size != 0) {
+        bhr_launch_shape sh = c->shape;
+        if (opts->block_size != 0) sh.block_size = opts->block_size;
+        if (opts->chunk > 0) sh.chunk = opts->chunk;
+        if (opts->refill > 0) sh.refill = opts->refill;
+        if (opts->blocks_per_sm > 0) sh.blocks_per_sm = opts->blocks_per_sm;
+        if (opts->tile_w != 0) sh.tile_w = opts->tile_w;
+        if (check_shape(nullptr, sh) != BHR_OK) {
             cudaSetDevice(prev);
             delete c;
-            return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_create: block_size must be 0, 256 or 512");
+            return BHR_ERR_INVALID_ARG;
         }
-        if (opts->chunk > 0) c->chunk = opts->chunk;
-        if (opts->refill > 0) c->refill = opts->refill;
-        if (opts->blocks_per_sm > 0) c->blocks_per_sm = opts->blocks_per_sm;
+        c->shape = sh;
     }
-    const int rc = ensure_scratch(c, 1, 0, false);
+    const int rc = ensure_scratch(c, c->scr, 1, 0, false);
     cudaSetDevice(prev);
     if (rc != BHR_OK) {
         delete c;
@@ -179,9 +345,7 @@ int bhr_destroy(bhr_ctx* c) {
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(c->device);
-    if (c->q) cudaFree(c->q);
-    if (c->band) cudaFree(c->band);
-    if (c->promo) cudaFree(c->promo);
+    c->scr.release();
     if (c->staging) cudaFree(c->staging);
     for (cudaStream_t& st : c->hstream)
         if (st) cudaStreamDestroy(st);
@@ -262,16 +426,21 @@ int bhr_view_set_fov(bhr_view* v, float fov_deg) {
     return BHR_OK;
 }
 
-int bhr_view_look_at(bhr_view* v, const double pos[3], const double target[3]) {
-    if (!v || !pos || !target) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_look_at: NULL argument");
-    // Camera.cpp:12-23 lookRotation(from, target, up = (0,1,0)), then basis() = mat3_cast(quat)
-    const double fd[3] = {target[0] - pos[0], target[1] - pos[1], target[2] - pos[2]};
+int bhr_look_rotation(const double from[3], const double target[3], const float up_in[3], float q_out[4]) {
+    if (!from || !target || !q_out) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_look_rotation: NULL argument");
+    // Camera.cpp:12-23 lookRotation(from, target, up), camera looking down -Z
+    const double fd[3] = {target[0] - from[0], target[1] - from[1], target[2] - from[2]};
     const double len = std::sqrt(fd[0] * fd[0] + fd[1] * fd[1] + fd[2] * fd[2]);
     float f[3] = {0.0f, 0.0f, -1.0f};
     if (len > 0.0)
         for (int k = 0; k < 3; ++k) f[k] = float(fd[k] / len);
     float u[3] = {0.0f, 1.0f, 0.0f};
-    if (std::fabs(f[0] * u[0] + f[1] * u[1] + f[2] * u[2]) > 0.999f) {
+    if (up_in)
+        for (int k = 0; k < 3; ++k) u[k] = up_in[k];
+    const float ul = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    if (!(ul > 0.0f)) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_look_rotation: up vector is zero");
+    const float un[3] = {u[0] * (1.0f / ul), u[1] * (1.0f / ul), u[2] * (1.0f / ul)};
+    if (std::fabs(f[0] * un[0] + f[1] * un[1] + f[2] * un[2]) > 0.999f) {
         u[0] = 0.0f; u[1] = 0.0f; u[2] = -1.0f;
     }
     float r[3] = {f[1] * u[2] - u[1] * f[2], f[2] * u[0] - u[2] * f[0], f[0] * u[1] - u[0] * f[1]};
@@ -296,17 +465,33 @@ int bhr_view_look_at(bhr_view* v, const double pos[3], const double target[3]) {
         default: qw = (m[0][1] - m[1][0]) * mult; qx = (m[2][0] + m[0][2]) * mult; qy = (m[1][2] + m[2][1]) * mult; qz = bv; break;
     }
     const float qn = 1.0f / std::sqrt(qw * qw + qx * qx + qy * qy + qz * qz);
-    qw *= qn; qx *= qn; qy *= qn; qz *= qn;
-    // quaternion -> rotation matrix (columns right, up, back)
+    q_out[0] = qw * qn;
+    q_out[1] = qx * qn;
+    q_out[2] = qy * qn;
+    q_out[3] = qz * qn;
+    return BHR_OK;
+}
+
+int bhr_view_set_pose(bhr_view* v, const double pos[3], const float q[4]) {
+    if (!v || !pos || !q) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_set_pose: NULL argument");
+    // uCamBasis = mat3_cast(orientation), columns right, up, back (Camera.cpp:67, Renderer.cpp:250)
+    const float qw = q[0], qx = q[1], qy = q[2], qz = q[3];
     const float xx = qx * qx, yy = qy * qy, zz = qz * qz, xz = qx * qz, xy = qx * qy, yz = qy * qz;
     const float wx = qw * qx, wy = qw * qy, wz = qw * qz;
     float* B = v->cam_basis;
     B[0] = 1.0f - 2.0f * (yy + zz); B[1] = 2.0f * (xy + wz);        B[2] = 2.0f * (xz - wy);
     B[3] = 2.0f * (xy - wz);        B[4] = 1.0f - 2.0f * (xx + zz); B[5] = 2.0f * (yz + wx);
     B[6] = 2.0f * (xz + wy);        B[7] = 2.0f * (yz - wx);        B[8] = 1.0f - 2.0f * (xx + yy);
-    // uCamPos = vec3(Camera::position())
+    // uCamPos = vec3(Camera::position()) (Renderer.cpp:249)
     for (int k = 0; k < 3; ++k) v->cam_pos[k] = float(pos[k]);
     return BHR_OK;
+}
+
+int bhr_view_look_at(bhr_view* v, const double pos[3], const double target[3]) {
+    if (!v || !pos || !target) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_view_look_at: NULL argument");
+    float q[4];
+    const int rc = bhr_look_rotation(pos, target, nullptr, q);
+    return rc == BHR_OK ? bhr_view_set_pose(v, pos, q) : rc;
 }
 
 int bhr_view_orbit_pose(bhr_view* v, double r, double incl, double azim) {
@@ -324,82 +509,20 @@ int64_t bhr_view_rays(const bhr_view* v) {
 int bhr_trace(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out_dev, int precision, int method,
               void* cuda_stream) {
     if (!c) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_trace: ctx is NULL");
-    if (!views || nviews <= 0 || !out_dev) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: no views or outputs");
-    if (precision != BHR_PREC_FP32 && precision != BHR_PREC_MIXED)
-        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: unknown precision");
     if (method != BHR_METHOD_PLAIN && method != BHR_METHOD_SURROGATE)
         return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: unknown method");
     if (method == BHR_METHOD_SURROGATE)
         return fail(c, BHR_ERR_NOT_READY, "bhr_trace: the surrogate runs through bhr_surrogate_trace");
     int64_t rays = 0;
-    for (int k = 0; k < nviews; ++k) {
-        const int rc = check_view(c, views[k], k);
-        if (rc != BHR_OK) return rc;
-        if (!out_dev[k]) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: output buffer " + std::to_string(k) + " is NULL");
-        if (reinterpret_cast<uintptr_t>(out_dev[k]) % 16 != 0)
-            return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: output buffers must be 16-byte aligned");
-        rays += int64_t(views[k].width) * views[k].height;
-    }
-    const bool mixed = precision == BHR_PREC_MIXED;
-    // group views by rule (one launch per group and per kMaxViews views)
-    std::vector<bhr::Rule> rules;
-    std::vector<std::vector<int>> groups;
-    for (int k = 0; k < nviews; ++k) {
-        const bhr::Rule r = make_rule(views[k]);
-        size_t g = 0;
-        while (g < rules.size() && !same_rule(rules[g], r)) ++g;
-        if (g == rules.size()) {
-            rules.push_back(r);
-            groups.emplace_back();
-        }
-        groups[g].push_back(k);
-    }
-    int nb = 0;
-    for (const auto& g : groups) nb += int((g.size() + bhr::kMaxViews - 1) / bhr::kMaxViews);
+    int rc = validate(c, "bhr_trace", views, nviews, out_dev, precision, &rays);
+    if (rc != BHR_OK) return rc;
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(c->device);
-    int rc = ensure_scratch(c, nb, rays, mixed);
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
-    const int fp64_grid = c->sms * 8;
-    int bi = 0;
-    std::vector<std::pair<int, int>> slots(size_t(nviews), {0, 0});
-    for (size_t g = 0; rc == BHR_OK && g < groups.size(); ++g) {
-        const bhr::Rule& rule = rules[g];
-        const int variant = bhr::rule_variant(rule);
-        const std::vector<int>& members = groups[g];
-        for (size_t m0 = 0; rc == BHR_OK && m0 < members.size(); m0 += bhr::kMaxViews, ++bi) {
-            bhr::Scratch sc{c->q + bi, c->band, c->promo};
-            cudaError_t e = cudaMemsetAsync(sc.q, 0, sizeof(bhr::WorkQueue), st);
-            if (e != cudaSuccess) {
-                rc = cuda_fail(c, e, "bhr_trace: cudaMemsetAsync");
-                break;
-            }
-            const size_t nv = std::min<size_t>(bhr::kMaxViews, members.size() - m0);
-            if (nviews == 1) {
-                const bhr::DevView dv = make_dev_view(views[0], out_dev[0]);
-                e = bhr::launch_march_one(dv, rule, sc, mixed, make_cfg(c, variant, false, mixed), st);
-                if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_one(dv, rule, sc, fp64_grid, st);
-            } else {
-                static thread_local bhr::ViewBatch b;  // ~12 KB, passed by value as a kernel parameter
-                const bhr::LaunchCfg cfg = make_cfg(c, variant, true, mixed);
-                b.nviews = int(nv);
-                b.rule = rule;
-                int64_t chunk_acc = 0;
-                for (size_t k = 0; k < nv; ++k) {
-                    const int vi = members[m0 + k];
-                    slots[size_t(vi)] = {bi, int(k)};
-                    b.views[k] = make_dev_view(views[vi], out_dev[vi]);
-                    b.views[k].chunk_start = chunk_acc;
-                    chunk_acc += (b.views[k].nrays + cfg.chunk - 1) / cfg.chunk;
-                }
-                b.total_chunks = chunk_acc;
-                e = bhr::launch_march_multi(b, sc, mixed, cfg, st);
-                if (e == cudaSuccess && mixed) e = bhr::launch_march_fp64_multi(b, sc, fp64_grid, st);
-            }
-            if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace: kernel launch");
-        }
-    }
+    std::vector<std::pair<int, int>> slots;
+    int nb = 0;
+    rc = run_trace(c, c->shape, c->scr, views, nviews, out_dev, precision, rays, st, &slots, &nb);
     if (rc == BHR_OK) {
         c->last_stream = st;
         c->last_batches = nb;
@@ -484,21 +607,10 @@ int bhr_trace_stats(bhr_ctx* c, bhr_stats* s) {
     if (!c || !s) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_stats: NULL argument");
     std::memset(s, 0, sizeof *s);
     if (!c->have_last) return fail(c, BHR_ERR_NOT_READY, "bhr_trace_stats: no trace on this context yet");
-    int prev = 0;
-    cudaGetDevice(&prev);
-    cudaSetDevice(c->device);
-    cudaError_t e = cudaStreamSynchronize(c->last_stream);
-    std::vector<bhr::WorkQueue> qs(size_t(c->last_batches));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(qs.data(), c->q, sizeof(bhr::WorkQueue) * qs.size(), cudaMemcpyDeviceToHost);
-    cudaSetDevice(prev);
-    if (e != cudaSuccess) return cuda_fail(c, e, "bhr_trace_stats");
-    for (const auto& q : qs) {
-        s->steps += q.steps;
-        s->fp64_rays += q.fp64_rays;
-        s->fp64_steps += q.fp64_steps;
-        s->nonfinite += q.nonfinite;
-    }
+    std::vector<bhr::WorkQueue> qs;
+    const int rc = read_queues(c, c->scr, c->last_batches, c->last_stream, &qs, "bhr_trace_stats");
+    if (rc != BHR_OK) return rc;
+    sum_stats(qs, 0, s);
     return BHR_OK;
 }
 
@@ -506,20 +618,307 @@ int bhr_trace_view_times(bhr_ctx* c, double* ms, int nviews) {
     if (!c || !ms || nviews <= 0) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_view_times: bad argument");
     if (!c->have_last || c->last_nviews != nviews || nviews == 1)
         return fail(c, BHR_ERR_NOT_READY, "bhr_trace_view_times: needs the last trace to be a multi-view trace");
+    std::vector<bhr::WorkQueue> qs;
+    const int rc = read_queues(c, c->scr, c->last_batches, c->last_stream, &qs, "bhr_trace_view_times");
+    if (rc != BHR_OK) return rc;
+    view_times(qs, c->last_slots, ms, nviews);
+    return BHR_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// launch shapes and the autotuner
+
+int bhr_get_launch_shape(const bhr_ctx* c, bhr_launch_shape* sh) {
+    if (!c || !sh) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_get_launch_shape: NULL argument");
+    *sh = c->shape;
+    return BHR_OK;
+}
+
+int bhr_set_launch_shape(bhr_ctx* c, const bhr_launch_shape* sh) {
+    if (!c || !sh) return fail(c, BHR_ERR_INVALID_ARG, "bhr_set_launch_shape: NULL argument");
+    const int rc = check_shape(c, *sh);
+    if (rc != BHR_OK) return rc;
+    c->shape = *sh;
+    if (c->shape.tile_w == 0) c->shape.tile_w = 32;
+    return BHR_OK;
+}
+
+namespace {
+
+std::string signature(const bhr_view* views, int nviews, int precision) {
+    std::string k = "p" + std::to_string(precision);
+    for (int i = 0; i < nviews; ++i) {
+        const bhr_view& v = views[i];
+        char buf[96];
+        std::snprintf(buf, sizeof buf, "|%dx%d:%d:%d%d%d%d", v.width, v.height, v.max_steps, v.term_mode, v.disk_mode,
+                      v.lensing, v.far_mode);
+        k += buf;
+    }
+    return k;
+}
+
+// Median time of `reps` traces with shape `sh` after one warm-up (synchronous, stream st).
+int time_shape(bhr_ctx* c, const bhr_launch_shape& sh, const bhr_view* views, int nviews, bhr_hit* const* out,
+               int precision, int64_t rays, int reps, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+    std::vector<float> t;
+    for (int r = 0; r <= reps; ++r) {
+        cudaEventRecord(e0, st);
+        int rc = run_trace(c, sh, c->scr, views, nviews, out, precision, rays, st, nullptr, nullptr);
+        if (rc != BHR_OK) return rc;
+        cudaEventRecord(e1, st);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) return cuda_fail(c, e, "bhr_autotune");
+        float x = 0.f;
+        cudaEventElapsedTime(&x, e0, e1);
+        if (r > 0) t.push_back(x);
+    }
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return BHR_OK;
+}
+
+}  // namespace
+
+int bhr_autotune(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out_dev, int precision, int reps,
+                 bhr_launch_shape* best) {
+    if (!c) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_autotune: ctx is NULL");
+    int64_t rays = 0;
+    int rc = validate(c, "bhr_autotune", views, nviews, out_dev, precision, &rays);
+    if (rc != BHR_OK) return rc;
+    reps = std::max(1, std::min(reps, 20));
+    const std::string key = signature(views, nviews, precision);
+    auto hit = c->tuned.find(key);
+    if (hit != c->tuned.end()) {
+        c->shape = hit->second;
+        if (best) *best = hit->second;
+        return BHR_OK;
+    }
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(c->device);
-    cudaError_t e = cudaStreamSynchronize(c->last_stream);
-    std::vector<bhr::WorkQueue> qs(size_t(c->last_batches));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(qs.data(), c->q, sizeof(bhr::WorkQueue) * qs.size(), cudaMemcpyDeviceToHost);
-    cudaSetDevice(prev);
-    if (e != cudaSuccess) return cuda_fail(c, e, "bhr_trace_view_times");
-    for (int k = 0; k < nviews; ++k) {
-        const bhr::WorkQueue& q = qs[size_t(c->last_slots[size_t(k)].first)];
-        const int s = c->last_slots[size_t(k)].second;
-        ms[k] = q.view_t_end[s] >= q.t_start ? double(q.view_t_end[s] - q.t_start) * 1e-6 : -1.0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_autotune: stream / events");
+    bhr_launch_shape top{512, 0, 64, 8, 32, 0.0f};
+    float top_ms = 1e30f;
+    auto trial = [&](bhr_launch_shape sh) {
+        if (rc != BHR_OK) return;
+        float ms = 0.f;
+        rc = time_shape(c, sh, views, nviews, out_dev, precision, rays, reps, st, e0, e1, &ms);
+        if (rc == BHR_OK && ms < top_ms) {
+            top_ms = ms;
+            sh.ms = ms;
+            top = sh;
+        }
+    };
+    // stage 1: block size x chunk (rows, refill 8)
+    for (int block : {256, 512})
+        for (int chunk : {32, 64, 128, 256}) trial(bhr_launch_shape{block, 0, chunk, 8, 32, 0.0f});
+    // stage 2: refill threshold
+    const bhr_launch_shape s1 = top;
+    for (int refill : {4, 16, 24}) trial(bhr_launch_shape{s1.block_size, 0, s1.chunk, refill, 32, 0.0f});
+    // stage 3: pixel tiles
+    const bhr_launch_shape s2 = top;
+    for (int tile : {16, 8}) trial(bhr_launch_shape{s2.block_size, 0, s2.chunk, s2.refill, tile, 0.0f});
+    // stage 4: fewer resident blocks (less contention for the work queue and L1)
+    const bhr_launch_shape s3 = top;
+    if (rc == BHR_OK) {
+        const int variant = bhr::rule_variant(make_rule(views[0]));
+        const int fit = bhr::march_blocks_per_sm(s3.block_size, variant, nviews > 1, precision == BHR_PREC_MIXED);
+        if (fit > 1) trial(bhr_launch_shape{s3.block_size, fit - 1, s3.chunk, s3.refill, s3.tile_w, 0.0f});
     }
+    if (st) cudaStreamDestroy(st);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaSetDevice(prev);
+    if (rc != BHR_OK) return rc;
+    c->shape = top;
+    c->tuned[key] = top;
+    if (best) *best = top;
+    return BHR_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// plans
+
+namespace {
+
+int plan_capture(bhr_plan* p, cudaGraph_t* g) {
+    bhr_ctx* c = p->ctx;
+    int64_t rays = 0;
+    for (const bhr_view& v : p->views) rays += int64_t(v.width) * v.height;
+    cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bhr_plan: begin capture");
+    int rc = run_trace(c, p->shape, p->scr, p->views.data(), int(p->views.size()), p->out.data(), p->precision, rays,
+                       p->cap, &p->slots, &p->batches);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(p->cap, &graph);
+    if (rc != BHR_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "bhr_plan: end capture");
+    *g = graph;
+    return BHR_OK;
+}
+
+}  // namespace
+
+int bhr_plan_create(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out_dev, int precision,
+                    int autotune, bhr_plan** out) {
+    if (!c || !out) return fail(c, BHR_ERR_INVALID_ARG, "bhr_plan_create: NULL argument");
+    *out = nullptr;
+    int64_t rays = 0;
+    int rc = validate(c, "bhr_plan_create", views, nviews, out_dev, precision, &rays);
+    if (rc != BHR_OK) return rc;
+    if (autotune) {
+        rc = bhr_autotune(c, views, nviews, out_dev, precision, 3, nullptr);
+        if (rc != BHR_OK) return rc;
+    }
+    bhr_plan* p = new (std::nothrow) bhr_plan();
+    if (!p) return fail(c, BHR_ERR_OOM, "bhr_plan_create: out of host memory");
+    p->ctx = c;
+    p->views.assign(views, views + nviews);
+    p->out.assign(out_dev, out_dev + nviews);
+    p->precision = precision;
+    p->shape = c->shape;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_plan_create: stream");
+    // one eager trace on the plan's own scratch: allocates it, sets kernel attributes and
+    // checks every launch before anything is captured
+    if (rc == BHR_OK)
+        rc = run_trace(c, p->shape, p->scr, views, nviews, out_dev, precision, rays, p->cap, &p->slots, &p->batches);
+    if (rc == BHR_OK) {
+        e = cudaStreamSynchronize(p->cap);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_plan_create: first trace");
+    }
+    if (rc == BHR_OK) rc = plan_capture(p, &p->graph);
+    if (rc == BHR_OK) {
+        e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_plan_create: instantiate");
+    }
+    cudaSetDevice(prev);
+    if (rc != BHR_OK) {
+        bhr_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return BHR_OK;
+}
+
+int bhr_plan_update(bhr_plan* p, const bhr_view* views, int nviews) {
+    if (!p) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_plan_update: plan is NULL");
+    bhr_ctx* c = p->ctx;
+    if (!views || nviews != int(p->views.size()))
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_plan_update: the view count must stay the same");
+    for (int k = 0; k < nviews; ++k) {
+        const int rc = check_view(c, views[k], k);
+        if (rc != BHR_OK) return rc;
+        const bhr_view& o = p->views[size_t(k)];
+        if (views[k].width != o.width || views[k].height != o.height ||
+            !same_rule(make_rule(views[k]), make_rule(o)))
+            return fail(c, BHR_ERR_INVALID_ARG, "bhr_plan_update: view " + std::to_string(k) +
+                                                    " changes its size or rule; create a new plan");
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const std::vector<bhr_view> old = p->views;
+    p->views.assign(views, views + nviews);
+    cudaGraph_t g = nullptr;
+    int rc = plan_capture(p, &g);
+    if (rc == BHR_OK) {
+        cudaGraphExecUpdateResultInfo info{};
+        cudaError_t e = cudaGraphExecUpdate(p->exec, g, &info);
+        if (e != cudaSuccess) {
+            // topology changed (should not happen for same sizes and rules): instantiate afresh
+            cudaGetLastError();
+            cudaGraphExec_t x = nullptr;
+            e = cudaGraphInstantiate(&x, g, 0);
+            if (e == cudaSuccess) {
+                cudaGraphExecDestroy(p->exec);
+                p->exec = x;
+            } else {
+                rc = cuda_fail(c, e, "bhr_plan_update: instantiate");
+            }
+        }
+    }
+    if (rc == BHR_OK) {
+        if (p->graph) cudaGraphDestroy(p->graph);
+        p->graph = g;
+    } else {
+        if (g) cudaGraphDestroy(g);
+        p->views = old;
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int bhr_plan_launch(bhr_plan* p, void* cuda_stream) {
+    if (!p || !p->exec) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_plan_launch: plan is NULL or empty");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(p->ctx->device);
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    cudaError_t e = cudaGraphLaunch(p->exec, st);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_fail(p->ctx, e, "bhr_plan_launch");
+    p->last_stream = st;
+    p->launched = true;
+    return BHR_OK;
+}
+
+int bhr_plan_launch_shape(const bhr_plan* p, bhr_launch_shape* sh) {
+    if (!p || !sh) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_plan_launch_shape: NULL argument");
+    *sh = p->shape;
+    return BHR_OK;
+}
+
+int bhr_plan_stats(bhr_plan* p, bhr_stats* s) {
+    if (!p || !s) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_plan_stats: NULL argument");
+    if (!p->launched) return fail(p->ctx, BHR_ERR_NOT_READY, "bhr_plan_stats: the plan was not launched yet");
+    std::vector<bhr::WorkQueue> qs;
+    const int rc = read_queues(p->ctx, p->scr, p->batches, p->last_stream, &qs, "bhr_plan_stats");
+    if (rc != BHR_OK) return rc;
+    int64_t rays = 0;
+    for (const bhr_view& v : p->views) rays += int64_t(v.width) * v.height;
+    sum_stats(qs, rays, s);
+    return BHR_OK;
+}
+
+int bhr_plan_view_times(bhr_plan* p, double* ms, int nviews) {
+    if (!p || !ms || nviews != int(p->views.size()))
+        return fail(p ? p->ctx : nullptr, BHR_ERR_INVALID_ARG, "bhr_plan_view_times: bad argument");
+    if (!p->launched || nviews == 1)
+        return fail(p->ctx, BHR_ERR_NOT_READY, "bhr_plan_view_times: needs a launched multi-view plan");
+    std::vector<bhr::WorkQueue> qs;
+    const int rc = read_queues(p->ctx, p->scr, p->batches, p->last_stream, &qs, "bhr_plan_view_times");
+    if (rc != BHR_OK) return rc;
+    view_times(qs, p->slots, ms, nviews);
+    return BHR_OK;
+}
+
+int bhr_plan_destroy(bhr_plan* p) {
+    if (!p) return BHR_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(p->ctx->device);
+    if (p->launched && p->last_stream) cudaStreamSynchronize(p->last_stream);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->cap) {
+        cudaStreamSynchronize(p->cap);
+        cudaStreamDestroy(p->cap);
+    }
+    p->scr.release();
+    cudaSetDevice(prev);
+    delete p;
     return BHR_OK;
 }
 

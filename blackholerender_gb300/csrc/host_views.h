@@ -44,7 +44,8 @@ inline int check_view(const bhr_view& v, int k, std::string* msg) {
 
 // setTraceUniforms (Renderer.cpp:242-356) + the per-ray constants of blackhole.frag:77-89 that
 // depend only on the view, in float with the reference's operation order.
-inline DevView make_dev_view(const bhr_view& v, bhr_hit* out) {
+// tile_w: pixel width of the tile a warp's 32 consecutive work items cover (32, 16 or 8).
+inline DevView make_dev_view(const bhr_view& v, bhr_hit* out, int tile_w = 32) {
     DevView d{};
     for (int k = 0; k < 3; ++k) d.cam[k] = v.cam_pos[k];
     for (int k = 0; k < 9; ++k) d.basis[k] = v.cam_basis[k];
@@ -66,6 +67,15 @@ inline DevView make_dev_view(const bhr_view& v, bhr_hit* out) {
     for (int k = 0; k < 3; ++k) d.cam_d[k] = double(v.cam_pos[k]);
     d.chunk_start = 0;
     d.nrays = int64_t(v.width) * v.height;
+    d.tile_shift = tile_w == 16 ? 4 : (tile_w == 8 ? 3 : 5);
+    if (d.tile_shift == 5) {
+        d.tiles_x = 0;
+        d.work = d.nrays;
+    } else {
+        const int tw = 1 << d.tile_shift, th = 32 >> d.tile_shift;
+        d.tiles_x = (v.width + tw - 1) / tw;
+        d.work = int64_t(d.tiles_x) * ((v.height + th - 1) / th) * 32;
+    }
     d.out = out;
     return d;
 }

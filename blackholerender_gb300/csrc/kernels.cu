@@ -4,7 +4,8 @@
 //   warp. Retired lanes are refilled from a per-warp ring of rays that were set up 32 at a time
 //   (convergent) into shared memory, so ray setup never runs one lane at a time and the step
 //   loop stays full. Work comes from a global chunk counter (context scratch), `chunk`
-//   consecutive pixels at a time. A record is 64 B: a lane writes its two start words when the
+//   consecutive work items at a time: pixels in row-major order, or (tile_shift < 5) 32-pixel
+//   tiles of 16x2 or 8x4 pixels, so that a setup batch covers a compact patch of the image. A record is 64 B: a lane writes its two start words when the
 //   ray starts and its two end words when it retires, each a whole 32 B sector, so lane-
 //   scattered stores move no extra DRAM bytes.
 //     k_march_one:   one view; view and rule are __grid_constant__ parameters (constant bank).
@@ -14,6 +15,9 @@
 //   and rays that reach r < promote_r hand their state to the FP64 queue.
 // k_march_fp64_*: drains the FP64 queue in double precision.
 #include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
 
 #include "kernels.cuh"
 #include "march.cuh"
@@ -179,14 +183,29 @@ __device__ __forceinline__ void march_warp(const DevView* views, int nviews, int
                     }
                     cview = v;
                     cbeg = ((int64_t)base - views[v].chunk_start) * chunk;
-                    cend = min(cbeg + (int64_t)chunk, (kList && !kMulti) ? list_len : views[v].nrays);
+                    cend = min(cbeg + (int64_t)chunk,
+                               kList ? (kMulti ? views[v].nrays : list_len) : views[v].work);
                 }
                 const int n = (int)min((int64_t)32, cend - cbeg);
                 const DevView& w = views[cview];
                 bool keep = false;
                 RayInit<float> ri;
-                const int my = kList ? (lane < n ? list[(kMulti ? w.list_off : 0) + cbeg + lane] : 0) : (int)(cbeg + lane);
-                if (lane < n) {
+                bool inside = lane < n;
+                int my;
+                if constexpr (kList) {
+                    my = inside ? list[(kMulti ? w.list_off : 0) + cbeg + lane] : 0;
+                } else if (w.tile_shift == 5) {
+                    my = (int)(cbeg + lane);
+                } else {  // work item -> pixel of a (1 << tile_shift) x (32 >> tile_shift) tile
+                    const int64_t m = cbeg + lane;
+                    const int t = (int)(m >> 5), l = (int)(m & 31);
+                    const int ty = t / w.tiles_x, tx = t - ty * w.tiles_x;
+                    const int pi = (tx << w.tile_shift) + (l & ((1 << w.tile_shift) - 1));
+                    const int pj = ty * (32 >> w.tile_shift) + (l >> w.tile_shift);
+                    inside = inside && pi < w.width && pj < w.height;
+                    my = pj * w.width + pi;
+                }
+                if (inside) {
                     const int j = my / w.width;
                     const int i = my - j * w.width;
                     ri = setup_ray<float>(w, R, i, j);
@@ -344,7 +363,7 @@ __global__ void __launch_bounds__(BS) k_march_one(const __grid_constant__ DevVie
     __shared__ float s_pool[BS / 32][kPoolFields * kPool];
     note_start(sc.q);
     const int wid = threadIdx.x >> 5;
-    const int64_t total_chunks = (view.nrays + chunk - 1) / chunk;
+    const int64_t total_chunks = (view.work + chunk - 1) / chunk;
     march_warp<false, kTerm, kDisk, kMixed>(&view, 1, total_chunks, rule, sc, chunk, refill_min,
                                             Pool{s_pool[wid], nullptr});
 }
@@ -521,10 +540,17 @@ cudaError_t launch_march_multi_list(const ViewBatch& b, const Scratch& s, const 
 }
 
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed) {
+    // cached per kernel, so that traces captured into a graph make no occupancy queries
+    static std::mutex mu;
+    static std::map<const void*, int> cache;
     const void* fn = pick_kernel(block, variant, multi, mixed);
     if (!fn) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto it = cache.find(fn);
+    if (it != cache.end()) return it->second;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, 0) != cudaSuccess) return 0;
+    cache[fn] = n;
     return n;
 }
 

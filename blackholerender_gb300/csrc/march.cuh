@@ -47,9 +47,13 @@ struct DevView {
     float baxis_scale;   // inversesqrt(max(1 - 2/rcam, 1e-6))  impactParameterAboutAxis
     float step_scale, disk_step;
     float two_over_r3;   // 2 / rcam^3 (impact parameter from h)
+    int32_t tile_shift;  // a warp's 32 consecutive work items cover a (1 << tile_shift) x (32 >> tile_shift)
+                         // pixel tile; 5 = plain row-major order (work item = pixel index)
+    int32_t tiles_x;     // tiles per pixel row (tile_shift < 5)
     double cam_d[3];     // the same float uniforms promoted, for the FP64 path
     int64_t chunk_start; // first work chunk of this view (multi-view launches)
     int64_t nrays;       // width * height
+    int64_t work;        // work items: nrays, or tiles * 32 (tile_shift < 5; edge tiles padded)
     bhr_hit* out;        // device hit buffer of this view
     int64_t list_off;    // offset of this view's pixel list (list launches)
 };

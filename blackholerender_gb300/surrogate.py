@@ -14,6 +14,26 @@ from . import _abi
 
 DEFAULT_CHECKPOINT = Path(__file__).resolve().parent / "data" / "surrogate.bhrs"
 
+CHECKPOINT_MAGIC = 0x53524842  # "BHRS"
+NORM_FIELDS = ("rc_lo", "rc_hi", "b_max", "t_eps", "t_scale", "y_scale", "band", "ue")
+
+
+def read_checkpoint(path) -> dict:
+    """Reads a checkpoint written by bhr_surrogate_save without a GPU: header (magic, version,
+    parameter count), the input normalisation, the Adam step and the FP32 parameters in the
+    flat layout [W1 (64x3), b1, W2 (64x64), b2, W3 (64x64), b3, W4 (2x64), b4]."""
+    raw = Path(path).read_bytes()
+    magic, version, n = np.frombuffer(raw, dtype="<u4", count=3)
+    if magic != CHECKPOINT_MAGIC or version != 1:
+        raise ValueError(f"{path}: not a surrogate checkpoint (magic {magic:#x}, version {version})")
+    norm = np.frombuffer(raw, dtype="<f4", count=len(NORM_FIELDS), offset=12)
+    step = int(np.frombuffer(raw, dtype="<i4", count=1, offset=12 + 4 * len(NORM_FIELDS))[0])
+    off = 16 + 4 * len(NORM_FIELDS)
+    if len(raw) != off + 4 * int(n):
+        raise ValueError(f"{path}: size {len(raw)} does not match {n} parameters")
+    params = np.frombuffer(raw, dtype="<f4", count=int(n), offset=off).copy()
+    return {"norm": dict(zip(NORM_FIELDS, map(float, norm))), "adam_step": step, "params": params}
+
 
 class Surrogate:
     def __init__(self, device=0, seed=1, **cfg):

@@ -53,8 +53,12 @@ class MT19937_64:
         return y & _MASK
 
     def uniform(self, lo: float, hi: float) -> float:
-        u = (self() >> 11) * (1.0 / 9007199254740992.0)
-        return lo + (hi - lo) * u
+        """std::uniform_real_distribution<double>(lo, hi) as libstdc++ draws it: one 64-bit
+        output scaled by 2^-64 (generate_canonical, kept below 1), then u (hi - lo) + lo."""
+        u = float(self()) / 18446744073709551616.0
+        if u >= 1.0:
+            u = math.nextafter(1.0, 0.0)
+        return u * (hi - lo) + lo
 
 
 PRESET_BY_BUDGET = {200: 0, 300: 1, 450: 2, 700: 3}

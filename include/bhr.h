@@ -133,8 +133,22 @@ typedef struct bhr_options {
     int32_t blocks_per_sm; /* 0 = autotuned / default */
     int32_t chunk;         /* rays a warp takes from the work queue at once, 0 = default */
     int32_t refill;        /* idle lanes before a warp refills, 0 = default */
-    int32_t reserved[3];
+    int32_t tile_w;        /* pixel tile of a warp's 32 work items: 32 (32x1 rows), 16 (16x2), 8 (8x4); 0 = 32 */
+    int32_t reserved[2];
 } bhr_options;
+
+/* Launch shape of the FP32 march (block and tile shapes). bhr_autotune measures candidates;
+ * every shape gives bit-identical hit records, only the speed differs. */
+typedef struct bhr_launch_shape {
+    int32_t block_size;    /* threads per block: 256 or 512 */
+    int32_t blocks_per_sm; /* resident blocks per SM, 0 = as many as fit */
+    int32_t chunk;         /* work items a warp claims at once (rounded up to a multiple of 32) */
+    int32_t refill;        /* idle lanes of a warp that trigger its refill, 1..32 */
+    int32_t tile_w;        /* pixel tile of 32 consecutive work items: 32, 16 or 8 pixels wide */
+    float ms;              /* bhr_autotune: median time of one trace with this shape, else 0 */
+} bhr_launch_shape;
+
+typedef struct bhr_plan bhr_plan;
 
 /* Per-call statistics, filled by bhr_trace_stats after the stream work completed. */
 typedef struct bhr_stats {
@@ -165,6 +179,12 @@ int bhr_view_apply_preset(bhr_view* v, int preset);
  * (Camera.cpp:12-23,67): float basis through a unit quaternion, up (0,1,0) with the
  * (0,0,-1) fallback when |dot(f, up)| > 0.999. Sets cam_pos and cam_basis. */
 int bhr_view_look_at(bhr_view* v, const double pos[3], const double target[3]);
+/* Camera.cpp:12-23 lookRotation(from, target, up): unit quaternion (w, x, y, z) of a camera at
+ * `from` looking at `target` (up NULL = +Y). */
+int bhr_look_rotation(const double from[3], const double target[3], const float up[3], float quat_wxyz[4]);
+/* Camera pose -> uCamPos / uCamBasis (Renderer.cpp:249-250): position, and the basis
+ * mat3_cast(orientation) with columns right, up, back. */
+int bhr_view_set_pose(bhr_view* v, const double pos[3], const float quat_wxyz[4]);
 /* tan_half_fov from a vertical FOV in degrees, as Renderer.cpp:246 (float arithmetic). */
 int bhr_view_set_fov(bhr_view* v, float fov_deg);
 /* Pose on a sphere: pos = r (sin i sin a, cos i, sin i cos a), looking at the hole. */
@@ -257,6 +277,36 @@ int bhr_trace_stats(bhr_ctx* ctx, bhr_stats* stats);
 /* Per-view latency of the last multi-view bhr_trace: milliseconds from the start of the
  * launch to the moment the view's last ray finished (synchronises that call's stream). */
 int bhr_trace_view_times(bhr_ctx* ctx, double* ms, int nviews);
+
+/* ---- launch shapes and the autotuner ------------------------------------------------ */
+/* No counterpart in the reference (its march is one fragment-shader draw whose scheduling the
+ * GL driver owns); these choose how the persistent march kernel covers a batch of views. */
+int bhr_get_launch_shape(const bhr_ctx* ctx, bhr_launch_shape* shape);
+int bhr_set_launch_shape(bhr_ctx* ctx, const bhr_launch_shape* shape);
+/* Times candidate shapes on this workload (staged search over block size and chunk, then
+ * refill, tile and blocks per SM; one warm-up and `reps` timed traces each, CUDA events, the
+ * median), makes the fastest the context's shape and returns it in `best` (may be NULL).
+ * Synchronous; writes the outputs. A repeated call with the same workload signature (views'
+ * sizes, budgets and rules, precision) returns the cached result without measuring. */
+int bhr_autotune(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* out_dev, int precision, int reps,
+                 bhr_launch_shape* best);
+
+/* ---- plans: a fixed batch of views replayed as one CUDA graph ------------------------- */
+/* The batched launch of many views (uneven sizes and budgets, one persistent kernel per rule
+ * and 64 views) captured once into a CUDA graph with its own device scratch, then replayed by
+ * bhr_plan_launch. autotune != 0 runs bhr_autotune first. The output buffers stay bound to the
+ * plan. bhr_plan_update changes camera and budget fields of the views (same count, sizes,
+ * rules and outputs) by re-capturing and updating the instantiated graph in place. The
+ * reference's closest counterpart is one Renderer::render per frame (src/Renderer.h:61). */
+int bhr_plan_create(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* out_dev, int precision,
+                    int autotune, bhr_plan** plan);
+int bhr_plan_update(bhr_plan* plan, const bhr_view* views, int nviews);
+int bhr_plan_launch(bhr_plan* plan, void* cuda_stream);
+int bhr_plan_launch_shape(const bhr_plan* plan, bhr_launch_shape* shape);
+/* after the launch's stream work completed: */
+int bhr_plan_stats(bhr_plan* plan, bhr_stats* stats);
+int bhr_plan_view_times(bhr_plan* plan, double* ms, int nviews); /* completion of each view after launch start */
+int bhr_plan_destroy(bhr_plan* plan);
 
 #ifdef __cplusplus
 }

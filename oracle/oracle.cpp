@@ -152,6 +152,25 @@ int oracle_cpu_trace(const double cam[3], const double dir[3], int max_steps, do
     return BHR_OK;
 }
 
+// Single components in double, for pinning against the reference's own functions:
+// rk4Step (geodesic.glsl:16-23 / Geodesic.h:27-34) in place on x, v;
+// initialVelocity (geodesic.glsl:27-34 / Geodesic.h:40-47);
+// farFieldDirection (geodesic.glsl:43-53 / Geodesic.h:65-75).
+void oracle_rk4_step(double x[3], double v[3], double h2, double dt) {
+    V3<double> X{x[0], x[1], x[2]}, V{v[0], v[1], v[2]};
+    rk4Step(X, V, h2, dt);
+    x[0] = X.x, x[1] = X.y, x[2] = X.z;
+    v[0] = V.x, v[1] = V.y, v[2] = V.z;
+}
+void oracle_initial_velocity(const double cam[3], const double dir[3], double out[3]) {
+    const V3<double> r = initialVelocity(V3<double>{cam[0], cam[1], cam[2]}, V3<double>{dir[0], dir[1], dir[2]});
+    out[0] = r.x, out[1] = r.y, out[2] = r.z;
+}
+void oracle_far_field(const double x[3], const double v[3], double h2, double out[3]) {
+    const V3<double> r = farFieldDirection(V3<double>{x[0], x[1], x[2]}, V3<double>{v[0], v[1], v[2]}, h2);
+    out[0] = r.x, out[1] = r.y, out[2] = r.z;
+}
+
 int oracle_hit_size(void) { return static_cast<int>(sizeof(bhr_hit)); }
 int oracle_view_size(void) { return static_cast<int>(sizeof(bhr_view)); }
 

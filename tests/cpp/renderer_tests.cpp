@@ -1,0 +1,193 @@
+// Checks of the C++ host interface (include/bhr_renderer.hpp), in the style of the reference's
+// tests/geodesic_tests.cpp: host-only checks always; with `--gpu <file>` also a traced frame
+// (the 256x144 view at r = 30, inclination 85 deg, 200 steps) through Renderer::render,
+// renderTo and renderHost, whose records are written to <file> for the oracle comparison the
+// Python test driver makes.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bhr_renderer.hpp"
+
+static int g_failures = 0;
+static int g_checks = 0;
+
+#define CHECK(cond, msg)                                                    \
+    do {                                                                    \
+        ++g_checks;                                                         \
+        if (cond) {                                                         \
+            std::printf("  ok    %s\n", msg);                               \
+        } else {                                                            \
+            ++g_failures;                                                   \
+            std::printf("  FAIL  %s   (%s:%d)\n", msg, __FILE__, __LINE__); \
+        }                                                                   \
+    } while (0)
+
+static bhr::Camera orbitCamera(double r, double incl, double az) {
+    bhr::Camera c;
+    c.setPosition(bhr::Vec3d{r * std::sin(incl) * std::sin(az), r * std::cos(incl), r * std::sin(incl) * std::cos(az)});
+    c.lookAt(bhr::Vec3d{0.0, 0.0, 0.0});
+    return c;
+}
+
+static void testPresets() {
+    std::printf("quality presets (Settings::applyPreset)\n");
+    const int steps[4] = {200, 300, 450, 700};
+    const float scale[4] = {0.10f, 0.07f, 0.05f, 0.035f};
+    const float disk[4] = {0.35f, 0.30f, 0.18f, 0.10f};
+    for (int p = 0; p < 4; ++p) {
+        bhr::Settings s;
+        s.applyPreset(p);
+        char msg[96];
+        std::snprintf(msg, sizeof msg, "preset %d: %d steps, step scale %.3f, disk step %.2f", p, steps[p], scale[p], disk[p]);
+        CHECK(s.maxSteps == steps[p] && s.stepScale == scale[p] && s.diskStep == disk[p], msg);
+    }
+    bhr::Settings s;
+    s.maxSteps = 123;
+    s.applyPreset(bhr::PRESET_CUSTOM);
+    CHECK(s.maxSteps == 123, "custom preset keeps the fields");
+}
+
+static void testCameraBasis() {
+    std::printf("camera basis (lookRotation, mat3_cast)\n");
+    bhr::Camera c;  // default bookmark: (0, 2.6, 24.9) looking at the hole
+    float B[9];
+    c.basis(B);
+    double orth = 0.0;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double d = 0.0;
+            for (int k = 0; k < 3; ++k) d += double(B[3 * a + k]) * B[3 * b + k];
+            orth = std::max(orth, std::fabs(d - (a == b ? 1.0 : 0.0)));
+        }
+    char msg[128];
+    std::snprintf(msg, sizeof msg, "columns orthonormal (max error %.1e)", orth);
+    CHECK(orth < 1e-6, msg);
+    const bhr::Vec3d p = c.position();
+    const double r = c.radius();
+    const double back_dot = (B[6] * p.x + B[7] * p.y + B[8] * p.z) / r;  // back column points away from the hole
+    std::snprintf(msg, sizeof msg, "back column = position / r (cos %.8f)", back_dot);
+    CHECK(back_dot > 1.0 - 1e-6, msg);
+    CHECK(std::fabs(B[1]) < 1e-6, "right column is horizontal (roll 0)");
+    CHECK(B[4] > 0.0f, "up column points up");
+    // top-down bookmark: looking along -Y with up (0,1,0) takes the (0,0,-1) fallback (Camera.cpp:17)
+    bhr::Camera top;
+    top.setPosition(bhr::Vec3d{0.0, 32.0, 0.001});
+    top.lookAt(bhr::Vec3d{0.0, 0.0, 0.0});
+    top.basis(B);
+    bool finite = true;
+    for (float e : B) finite = finite && std::isfinite(e);
+    CHECK(finite && B[7] > 0.99f, "top-down view: finite basis, back column along +Y");
+}
+
+static void testFrameToView() {
+    std::printf("FrameInput -> bhr_view (setTraceUniforms)\n");
+    bhr::Settings s;
+    s.applyPreset(bhr::PRESET_LOW);
+    s.renderScale = 0.5f;
+    s.diskOuter = 24.0f;
+    const bhr::Camera cam = orbitCamera(30.0, 85.0 * M_PI / 180.0, 0.0);
+    bhr::FrameInput in;
+    in.camera = &cam;
+    in.settings = &s;
+    in.windowW = 1920;
+    in.windowH = 1080;
+    bhr_view v{};
+    CHECK(bhr::Renderer::makeView(in, &v), "complete input converts");
+    CHECK(v.width == 960 && v.height == 540, "internal size = lround(window * renderScale)");
+    CHECK(v.max_steps == 200 && v.step_scale == 0.10f && v.disk_step == 0.35f, "preset fields carried");
+    CHECK(std::fabs(v.tan_half_fov - std::tan(60.0f * 0.01745329252f * 0.5f)) < 1e-7f, "tan(fov/2) as Renderer.cpp:246");
+    CHECK(v.r_esc_min == 30.0f, "shader rEscMin = max(1.25 r_out, 12)");
+    CHECK(v.disk_mode == BHR_DISK_THIN && v.lensing == 1 && v.far_mode == 0, "disk, lensing and far mode carried");
+    CHECK(std::fabs(v.cam_pos[1] - float(30.0 * std::cos(85.0 * M_PI / 180.0))) < 1e-5f, "camera position carried");
+    s.renderScale = 0.001f;
+    bhr::Renderer::makeView(in, &v);
+    CHECK(v.width == 192 && v.height == 108, "renderScale clamps at 0.1");
+    in.windowW = 10;
+    in.windowH = 10;
+    s.renderScale = 1.0f;
+    bhr::Renderer::makeView(in, &v);
+    CHECK(v.width == 16 && v.height == 16, "internal size at least 16");
+    bhr::FrameInput bad;
+    CHECK(!bhr::Renderer::makeView(bad, &v), "missing camera / settings is refused");
+}
+
+static void testErrors() {
+    std::printf("error reporting (bool + log line, no exceptions)\n");
+    bhr_view v{};
+    bhr_view_init(&v, BHR_TERM_SHADER);
+    v.width = 0;
+    bhr_hit* outs[1] = {nullptr};
+    CHECK(bhr_trace(nullptr, &v, 1, outs, BHR_PREC_FP32, BHR_METHOD_PLAIN, nullptr) == BHR_ERR_INVALID_ARG,
+          "bhr_trace without a context is an argument error");
+    CHECK(std::strlen(bhr_last_error(nullptr)) > 0, "the error has a message");
+    CHECK(bhr_view_apply_preset(&v, 9) == BHR_ERR_INVALID_ARG, "unknown preset is refused");
+    CHECK(bhr_view_set_fov(&v, 190.0f) == BHR_ERR_INVALID_ARG, "fov >= 180 is refused");
+}
+
+static int testGpu(const char* path) {
+    std::printf("traced frame (256x144, r=30, inclination 85 deg, 200 steps)\n");
+    std::string logged;
+    bhr::Renderer R;
+    R.setLogger([&](const std::string& m) { logged = m; });
+    if (!R.init(0)) {
+        std::printf("  FAIL  init: %s\n", logged.c_str());
+        return 1;
+    }
+    bhr::Settings s;
+    s.applyPreset(bhr::PRESET_LOW);
+    const bhr::Camera cam = orbitCamera(30.0, 85.0 * M_PI / 180.0, 0.0);
+    bhr::FrameInput in;
+    in.camera = &cam;
+    in.settings = &s;
+    in.windowW = 256;
+    in.windowH = 144;
+    in.termMode = BHR_TERM_CONFIG;
+    CHECK(R.render(in), "render");
+    CHECK(R.width() == 256 && R.height() == 144, "records at the internal size");
+    const size_t n = 256 * 144;
+    std::vector<bhr_hit> a(n), b, c(n);
+    CHECK(cudaMemcpy(a.data(), R.hits(), n * sizeof(bhr_hit), cudaMemcpyDeviceToHost) == cudaSuccess, "read back");
+    CHECK(R.renderHost(in, b), "renderHost");
+    bhr_hit* d = nullptr;
+    cudaMalloc(&d, n * sizeof(bhr_hit));
+    cudaStream_t st;
+    cudaStreamCreate(&st);
+    CHECK(R.renderTo(in, d, st), "renderTo on a stream");
+    cudaStreamSynchronize(st);
+    cudaMemcpy(c.data(), d, n * sizeof(bhr_hit), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    cudaStreamDestroy(st);
+    CHECK(b.size() == n && std::memcmp(a.data(), b.data(), n * sizeof(bhr_hit)) == 0, "renderHost = render");
+    CHECK(std::memcmp(a.data(), c.data(), n * sizeof(bhr_hit)) == 0, "renderTo = render");
+    int esc = 0, cap = 0, disk = 0;
+    for (const bhr_hit& h : a) {
+        esc += h.status == BHR_STATUS_ESCAPED;
+        cap += h.status == BHR_STATUS_CAPTURED;
+        disk += h.ncross > 0;
+    }
+    char msg[128];
+    std::snprintf(msg, sizeof msg, "escaped %d, captured %d, disk %d of %zu", esc, cap, disk, n);
+    CHECK(esc > 0 && cap > 0 && disk > 0 && esc + cap <= int(n), msg);
+    bhr::FrameInput bad = in;
+    bad.windowW = 0;
+    CHECK(!R.render(bad) && !logged.empty(), "bad input: false and a log line");
+    FILE* f = std::fopen(path, "wb");
+    const bool wrote = f && std::fwrite(a.data(), sizeof(bhr_hit), n, f) == n;
+    if (f) std::fclose(f);
+    CHECK(wrote, "records written");
+    R.shutdown();
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    testPresets();
+    testCameraBasis();
+    testFrameToView();
+    testErrors();
+    if (argc == 3 && std::strcmp(argv[1], "--gpu") == 0) testGpu(argv[2]);
+    std::printf("\n%d checks, %d failures\n", g_checks, g_failures);
+    return g_failures == 0 ? 0 : 1;
+}

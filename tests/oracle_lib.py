@@ -42,6 +42,9 @@ def lib():
         L.oracle_march_ray.argtypes = [VP, D, D, ctypes.c_int, ctypes.c_void_p, D]
         L.oracle_cpu_trace.argtypes = [D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, D,
                                        ctypes.POINTER(ctypes.c_int), D]
+        L.oracle_rk4_step.argtypes = [D, D, ctypes.c_double, ctypes.c_double]
+        L.oracle_initial_velocity.argtypes = [D, D, D]
+        L.oracle_far_field.argtypes = [D, D, ctypes.c_double, D]
         assert L.oracle_hit_size() == 64 and L.oracle_view_size() == ctypes.sizeof(View)
         _lib = L
     return _lib

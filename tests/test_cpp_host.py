@@ -1,0 +1,58 @@
+"""The C++ host interface (include/bhr_renderer.hpp): tests/cpp/renderer_tests.cpp compiled
+against libbhr.so. Host checks run without a GPU; the traced frame is compared with the FP64
+oracle and with the same view traced through the C ABI from Python."""
+from __future__ import annotations
+
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+SRC = ROOT / "tests" / "cpp" / "renderer_tests.cpp"
+EXE = ROOT / "tests" / "cpp" / "_build" / "renderer_tests"
+CUDA = Path("/usr/local/cuda")
+
+
+def build() -> Path:
+    from blackholerender_gb300._abi import LIB_PATH
+
+    if not LIB_PATH.exists():
+        pytest.skip("libbhr.so is not built")
+    deps = [SRC, ROOT / "include" / "bhr_renderer.hpp", ROOT / "include" / "bhr.h", LIB_PATH]
+    if EXE.exists() and EXE.stat().st_mtime > max(p.stat().st_mtime for p in deps):
+        return EXE
+    EXE.parent.mkdir(parents=True, exist_ok=True)
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", f"-I{ROOT / 'include'}", f"-I{CUDA / 'include'}",
+           str(SRC), "-o", str(EXE), f"-L{LIB_PATH.parent}", "-lbhr", f"-L{CUDA / 'lib64'}", "-lcudart",
+           f"-Wl,-rpath,{LIB_PATH.parent}", f"-Wl,-rpath,{CUDA / 'lib64'}"]
+    subprocess.run(cmd, check=True)
+    return EXE
+
+
+def test_cpp_host_checks():
+    r = subprocess.run([str(build())], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
+    assert " 0 failures" in r.stdout
+
+
+@pytest.mark.gpu
+def test_cpp_renderer_frame_vs_oracle(tmp_path):
+    import parity
+    from blackholerender_gb300 import HIT_DTYPE, TERM_CONFIG, Tracer, hits_numpy, workloads
+
+    out = tmp_path / "frame.bin"
+    r = subprocess.run([str(build()), "--gpu", str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
+    got = np.fromfile(out, dtype=HIT_DTYPE)
+    v = workloads.c1_view(TERM_CONFIG)
+    assert len(got) == v.rays
+    with Tracer(0) as t:
+        (o,) = t.trace([v])
+        import torch
+
+        torch.cuda.synchronize()
+        direct = hits_numpy(o.cpu())
+    assert np.array_equal(got.view(np.uint8), direct.view(np.uint8))  # same view, same kernel
+    parity.check_fp32(got, v, where="C++ Renderer frame")

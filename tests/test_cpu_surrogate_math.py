@@ -1,0 +1,90 @@
+"""The surrogate's checkers without a GPU: the closed-form orbit restatement (oracle/orbit_math.py)
+against independent numerics, the FP64 network reference (oracle/mlp_ref.py) against finite
+differences, and the committed checkpoint read on the host."""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "oracle"))
+
+import mlp_ref  # noqa: E402
+import orbit_math as om  # noqa: E402
+
+from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT, read_checkpoint  # noqa: E402
+
+
+@pytest.mark.parametrize("beta", [1e-3, 0.02, 0.3, 2.0, 10.0])
+def test_roots_solve_the_cubic(beta):
+    b = om.SQRT27 * (1.0 + beta)
+    u1, u2, u3, d32 = om.roots(beta)
+    ref = np.sort(np.roots([2.0, -1.0, 0.0, 1.0 / (b * b)]).real)
+    assert np.allclose([u1, u2, u3], ref, rtol=1e-10, atol=1e-13)
+    assert abs(d32 - (u3 - u2)) < 1e-12
+    assert u1 < 0 < u2 < u3
+
+
+def test_carlson_rf_against_scipy():
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(1)
+    x, y, z = rng.uniform(1e-3, 5.0, size=(3, 200))
+    assert np.allclose(om.rf(x, y, z), sp.elliprf(x, y, z), rtol=1e-13)
+    # truncated after one duplication step: the surrogate's baseline, accurate to ~1e-3 at worst here
+    assert np.max(np.abs(om.rf(x, y, z, ndup=1) / sp.elliprf(x, y, z) - 1.0)) < 3e-2
+
+
+@pytest.mark.parametrize("beta", [0.01, 0.2, 3.0])
+def test_sweep_equals_quadrature(beta):
+    integ = pytest.importorskip("scipy.integrate")
+    b = om.SQRT27 * (1.0 + beta)
+    u1, u2, u3, _ = om.roots(beta)
+    for a in (0.0, 0.3 * u2, 0.9 * u2):
+        # u = u2 - s^2 removes the turning-point singularity: du / sqrt(P) = 2 ds / sqrt(2 (u - u1)(u3 - u))
+        def f(s):
+            return 2.0 / np.sqrt(2.0 * (u2 - s * s - u1) * (u3 - u2 + s * s))
+
+        val, _ = integ.quad(f, 0.0, np.sqrt(u2 - a), epsabs=1e-13, epsrel=1e-12, limit=200)
+        assert abs(float(om.sweep_to_turn(a, beta)) - val) < 1e-9 * max(1.0, val), (a, val)
+    # the whole deflection: 2 I(0) - pi approaches 4/b for large b (weak field)
+    if beta > 1:
+        defl = 2.0 * float(om.sweep_to_turn(0.0, beta)) - np.pi
+        assert abs(defl - 4.0 / b) / (4.0 / b) < 0.2
+
+
+def test_mlp_reference_gradient_matches_finite_differences():
+    rng = np.random.default_rng(3)
+    p = rng.normal(scale=0.3, size=mlp_ref.NPARAMS)
+    x = rng.uniform(-1, 1, size=(24, 3))
+    y = rng.normal(size=24)
+    lab = rng.integers(0, 3, size=24)
+    samples = np.concatenate([x, y[:, None]], axis=1)
+    w_c = 0.7
+
+    def loss(q):
+        s, _ = mlp_ref.loss_and_grad(q, samples, lab, w_c, quantize=False)
+        n = len(samples)
+        return s[0] / n + w_c * s[1] / n
+
+    _, g = mlp_ref.loss_and_grad(p, samples, lab, w_c, quantize=False)
+    for k in rng.choice(mlp_ref.NPARAMS, 60, replace=False):
+        e = np.zeros_like(p)
+        e[k] = 1e-6
+        fd = (loss(p + e) - loss(p - e)) / 2e-6
+        assert abs(fd - g[k]) <= 1e-6 + 1e-5 * abs(g[k]), (k, fd, g[k])
+
+
+def test_committed_checkpoint_reads_on_the_host():
+    ck = read_checkpoint(DEFAULT_CHECKPOINT)
+    assert len(ck["params"]) == mlp_ref.NPARAMS and np.all(np.isfinite(ck["params"]))
+    nm = ck["norm"]
+    assert (nm["rc_lo"], nm["rc_hi"], nm["b_max"]) == (6.0, 200.0, 60.0)
+    assert abs(nm["band"] - 2e-3) < 1e-9 and ck["adam_step"] > 0
+    # the trained network's corrections stay small where it was trained (y is scaled by y_scale)
+    rng = np.random.default_rng(0)
+    q = np.stack([rng.uniform(-1, 1, 256), rng.uniform(0.2, 1.0, 256), rng.uniform(-1, 1, 256)], axis=1)
+    out, _ = mlp_ref.forward(ck["params"].astype(np.float64), q)
+    assert np.all(np.isfinite(out)) and np.max(np.abs(out[:, 0])) * nm["y_scale"] < 0.2
