@@ -412,6 +412,64 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_side_workload(args):
+    """--workload c3 | c4: the other configurations' throughput, one JSON line (not the headline).
+    c3: 3840x2160, FOV 40, 700 steps, r = 20, inclination 88 deg, mixed FP32/FP64 precision.
+    c4: 64 views of uneven size and budget (seed 1) as one autotuned CUDA-graph plan, with
+        per-view latency."""
+    import torch
+
+    from blackholerender_gb300 import HIT_BYTES, PREC_MIXED, PREC_FP32, TERM_CONFIG, Tracer, workloads
+
+    dev = torch.device("cuda", 0)
+    tr = Tracer(0)
+    if args.workload == "c3":
+        views = [workloads.c3_view(TERM_CONFIG)]
+        precision = PREC_MIXED
+        name = "3840x2160, FOV 40, 700 steps, r=20, inclination 88 deg, mixed FP32/FP64 (band 1e-2, r<2.5)"
+    else:
+        views = workloads.c4_views(TERM_CONFIG)
+        precision = PREC_FP32
+        name = "64 views (seed 1), 320x180..3840x2160 log-uniform, FOV 30-90, r 6.5-200, budgets 200-700"
+    rays = sum(v.rays for v in views)
+    outs = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+    t0 = time.perf_counter()
+    plan = tr.plan(views, outs, precision=precision, autotune=True)
+    tune_s = time.perf_counter() - t0
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        plan.launch(st)
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(0) as clk:
+        for a, b in ev:
+            flush.zero_()
+            a.record(st)
+            plan.launch(st)
+            b.record(st)
+        torch.cuda.synchronize(dev)
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(per) / len(per)
+    stats = plan.stats()
+    line = {"metric": f"Mrays/s ({args.workload})", "value": rays / (ms * 1e-3) / 1e6, "unit": "Mrays/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+            "higher_is_better": True, "dtype": "f32+f64" if precision == PREC_MIXED else "f32",
+            "data": "synthetic", "config": {"workload": name, "rays_per_step": rays, "views": len(views),
+                                            "graph": True, "autotune_s": tune_s,
+                                            "launch_shape": plan.launch_shape.as_dict()},
+            "gpu_launches": (1 + (1 if precision == PREC_MIXED else 0)) * args.steps,
+            "march_steps_per_ray": stats.steps / rays, "fp64_rays": stats.fp64_rays,
+            "fp64_steps": stats.fp64_steps, "clocks": clk.summary()}
+    if len(views) > 1:
+        lat = plan.view_times_ms()
+        line["view_latency_ms"] = {"p50": float(np.median(lat)), "p90": float(np.percentile(lat, 90)),
+                                   "max": float(lat.max())}
+    print(json.dumps(line), flush=True)
+    plan.close()
+    tr.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -425,11 +483,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--views", type=int, default=16, help="first N of the 16 poses (small profiling cases)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
+                    help="c2: the headline (16 poses at 1080p); c3 / c4: the other configurations")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "c2":
+        run_side_workload(args)
     else:
         run_gpu(args)
 

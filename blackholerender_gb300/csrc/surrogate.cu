@@ -193,23 +193,117 @@ __device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][
     o[1][1] = pb1 + N.b4[1];
 }
 
-// Forward pass of 32 queries held in shared memory (q[r] = {x1, x2, sigma, -}); all 32 lanes.
-__device__ void mlp_eval32(const SmemNet& N, const float4* q, float2* out) {
+// ---------------------------------------------------------------------------------------
+// inference forward pass on half-scaled weights
+//
+// With W1, b1, W2, b2, W3, b3 multiplied by 1/2 when they are staged (exact in FP32 and BF16),
+// every hidden pre-activation comes out as h = z / 2 exactly (the FP32 accumulation of halved
+// products is the halved accumulation), and silu(z) = z/2 (1 + tanh(z/2)) = fma(h, tanh h, h):
+// the same bits as the training kernel's silu(z), one multiply fewer per activation.
+
+__device__ void load_net_half(SmemNet& N, const float* __restrict__ P) {
+    for (int k = threadIdx.x; k < kH * kH; k += blockDim.x) {
+        const int o = k / kH, i = k % kH;
+        N.w2[o * kLd + i] = __float2bfloat16_rn(0.5f * P[kW2 + k]);
+        N.w3[o * kLd + i] = __float2bfloat16_rn(0.5f * P[kW3 + k]);
+    }
+    for (int f = threadIdx.x; f < kH; f += blockDim.x) {
+        N.w1[f] = make_float4(0.5f * P[kW1 + 3 * f], 0.5f * P[kW1 + 3 * f + 1], 0.5f * P[kW1 + 3 * f + 2],
+                              0.5f * P[kB1 + f]);
+        N.b2[f] = 0.5f * P[kB2 + f];
+        N.b3[f] = 0.5f * P[kB3 + f];
+        N.w4[f] = P[kW4 + f];
+        N.w4[kH + f] = P[kW4 + kH + f];
+    }
+    if (threadIdx.x < kOut) N.b4[threadIdx.x] = P[kB4 + threadIdx.x];
+}
+
+__device__ __forceinline__ float silu_h(float h) { return fmaf(h, tanh_sfu(h), h); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+
+// C = A W^T + bias for a 64x64 BF16 layer; the B fragments of four k-steps of an n-tile come from
+// two ldmatrix.x4 (lane L addresses row 8j + L%8, columns 8 (L/8) + 16 i0 of W[n][k]).
+__device__ __forceinline__ void mma_layer_ldsm(const __nv_bfloat16* W, const float* bias, const uint32_t (&A)[4][4],
+                                               float (&C)[8][4], int lane, int t) {
+    const __nv_bfloat16* wl = W + (lane & 7) * kLd + 8 * (lane >> 3);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float c0 = bias[8 * j + 2 * t], c1 = bias[8 * j + 2 * t + 1];
+        C[j][0] = c0;
+        C[j][1] = c1;
+        C[j][2] = c0;
+        C[j][3] = c1;
+        uint32_t b[8];
+        ldsm_x4(b[0], b[1], b[2], b[3], wl + 8 * j * kLd);
+        ldsm_x4(b[4], b[5], b[6], b[7], wl + 8 * j * kLd + 32);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) mma_bf16(C[j], A[i], b[2 * i], b[2 * i + 1]);
+    }
+}
+
+// Forward pass of the queries q[0 .. 16 ntiles) in shared memory (q[r] = {x1, x2, sigma, -}),
+// one 16-row tile at a time; all 32 lanes. Rows past the caller's count compute garbage that
+// nobody reads.
+__device__ void mlp_eval_tiles(const SmemNet& N, const float4* q, float2* out, int ntiles) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll 1
-    for (int mt = 0; mt < 2; ++mt) {
+    for (int mt = 0; mt < ntiles; ++mt) {
         const int ra = 16 * mt + g, rb = ra + 8;
+        const float4 xa = q[ra], xb = q[rb];
         uint32_t A[4][4];
         float C[8][4];
-        layer1<false>(N, q[ra], q[rb], A, t, nullptr, nullptr, ra, rb);
-        mma_layer(N.w2, N.b2, A, C, g, t);
-        act_pack(C, A);
-        mma_layer(N.w3, N.b3, A, C, g, t);
-        float o[2][2];
-        out_layer(N, C, o, t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float ha[4], hb[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int f = 16 * i + 2 * t + (k & 1) + ((k & 2) ? 8 : 0);
+                const float4 w = N.w1[f];
+                ha[k] = silu_h(fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w))));
+                hb[k] = silu_h(fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w))));
+            }
+            A[i][0] = pack_bf16(ha[0], ha[1]);
+            A[i][1] = pack_bf16(hb[0], hb[1]);
+            A[i][2] = pack_bf16(ha[2], ha[3]);
+            A[i][3] = pack_bf16(hb[2], hb[3]);
+        }
+        mma_layer_ldsm(N.w2, N.b2, A, C, lane, t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            A[i][0] = pack_bf16(silu_h(C[2 * i][0]), silu_h(C[2 * i][1]));
+            A[i][1] = pack_bf16(silu_h(C[2 * i][2]), silu_h(C[2 * i][3]));
+            A[i][2] = pack_bf16(silu_h(C[2 * i + 1][0]), silu_h(C[2 * i + 1][1]));
+            A[i][3] = pack_bf16(silu_h(C[2 * i + 1][2]), silu_h(C[2 * i + 1][3]));
+        }
+        mma_layer_ldsm(N.w3, N.b3, A, C, lane, t);
+        float pa0 = 0.f, pa1 = 0.f, pb0 = 0.f, pb1 = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int f = 8 * j + 2 * t;
+            const float h00 = silu_h(C[j][0]), h01 = silu_h(C[j][1]), h10 = silu_h(C[j][2]), h11 = silu_h(C[j][3]);
+            const float2 w0 = *reinterpret_cast<const float2*>(&N.w4[f]);
+            const float2 w1 = *reinterpret_cast<const float2*>(&N.w4[kH + f]);
+            pa0 = fmaf(w0.x, h00, fmaf(w0.y, h01, pa0));
+            pa1 = fmaf(w1.x, h00, fmaf(w1.y, h01, pa1));
+            pb0 = fmaf(w0.x, h10, fmaf(w0.y, h11, pb0));
+            pb1 = fmaf(w1.x, h10, fmaf(w1.y, h11, pb1));
+        }
+#pragma unroll
+        for (int m = 1; m <= 2; m <<= 1) {
+            pa0 += __shfl_xor_sync(0xffffffffu, pa0, m);
+            pa1 += __shfl_xor_sync(0xffffffffu, pa1, m);
+            pb0 += __shfl_xor_sync(0xffffffffu, pb0, m);
+            pb1 += __shfl_xor_sync(0xffffffffu, pb1, m);
+        }
         if (t == 0) {
-            out[ra] = make_float2(o[0][0], o[0][1]);
-            out[rb] = make_float2(o[1][0], o[1][1]);
+            out[ra] = make_float2(pa0 + N.b4[0], pa1 + N.b4[1]);
+            out[rb] = make_float2(pb0 + N.b4[0], pb1 + N.b4[1]);
         }
     }
     __syncwarp();
@@ -650,17 +744,17 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, floa
 // Plain forward pass over n queries (tests and the gradient check): one warp per 32 queries.
 __global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ P, const float4* __restrict__ q,
                                                    float2* __restrict__ out, int n) {
-    __shared__ SmemNet N;
+    __shared__ __align__(16) SmemNet N;
     __shared__ float4 qs[4][32];
     __shared__ float2 os[4][32];
-    load_net(N, nullptr, P);
+    load_net_half(N, P);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int base = (blockIdx.x * 4 + warp) * 32; base < n; base += gridDim.x * 4 * 32) {
         const int k = base + lane;
         qs[warp][lane] = k < n ? q[k] : make_float4(0.f, 0.f, 0.f, 0.f);
         __syncwarp();
-        mlp_eval32(N, qs[warp], os[warp]);
+        mlp_eval_tiles(N, qs[warp], os[warp], 2);
         if (k < n) out[k] = os[warp][lane];
         __syncwarp();
     }
@@ -715,7 +809,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                                                                 int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
-    load_net(S.N, nullptr, P);
+    load_net_half(S.N, P);
     __syncthreads();
     const DevView& w = sv.view;
     const Rule& R = sv.rule;
@@ -817,11 +911,11 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             }
         }
         __syncwarp();
-        // ---- network: all queries of the warp, 32 at a time
+        // ---- network: all queries of the warp, 16 rows at a time
         const int nq = 32 + total;
-#pragma unroll 1
-        for (int qb0 = 0; qb0 < nq; qb0 += 32) mlp_eval32(S.N, qb + qb0, ob + qb0);
-        n_rows += (unsigned long long)((nq + 31) / 32) * (lane == 0 ? 32 : 0);
+        const int ntiles = (nq + 15) >> 4;
+        mlp_eval_tiles(S.N, qb, ob, ntiles);
+        n_rows += lane == 0 ? (unsigned long long)(16 * ntiles) : 0ull;
         n_q += sur ? 1 + ncand : 0;
         // ---- results
         const float2 oe = ob[lane];

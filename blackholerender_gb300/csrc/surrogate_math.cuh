@@ -23,9 +23,49 @@ namespace orbit {
 
 constexpr int kBaseDup = 1;  // R_F duplication steps of the baseline
 
-template <class T> __host__ __device__ __forceinline__ T tsqrt(T x);
-template <> __host__ __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
-template <> __host__ __device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
+// Arithmetic of the closed form. The double path (training targets) is exact IEEE. The float
+// path (inference) uses the SFU's approximate square root and reciprocal (PTX sqrt.approx /
+// rcp.approx, a few units in the last place): the baseline it feeds is corrected by the network,
+// whose residual is three orders of magnitude larger, and the Newton iterations correct their
+// own update errors.
+template <class T> struct FM;
+template <> struct FM<double> {
+    static __host__ __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __host__ __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+    static __host__ __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static __host__ __device__ __forceinline__ double div_sqrt(double a, double b) { return a / ::sqrt(b); }
+};
+template <> struct FM<float> {
+    static __host__ __device__ __forceinline__ float sqrt(float x) {
+#ifdef __CUDA_ARCH__
+        float y;
+        asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+        return y;
+#else
+        return ::sqrtf(x);
+#endif
+    }
+    static __host__ __device__ __forceinline__ float rcp(float x) {
+#ifdef __CUDA_ARCH__
+        float y;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+        return y;
+#else
+        return 1.0f / x;
+#endif
+    }
+    static __host__ __device__ __forceinline__ float div(float a, float b) { return a * rcp(b); }
+    static __host__ __device__ __forceinline__ float div_sqrt(float a, float b) {
+#ifdef __CUDA_ARCH__
+        float y;
+        asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(b));
+        return a * y;
+#else
+        return a / ::sqrtf(b);
+#endif
+    }
+};
+template <class T> __host__ __device__ __forceinline__ T tsqrt(T x) { return FM<T>::sqrt(x); }
 
 template <class T> struct Roots {
     T u1, u2, u3;
@@ -50,10 +90,10 @@ __host__ __device__ __forceinline__ Roots<T> roots(T beta) {
         // (Newton; f' = 3 - 12 s^2 >= 1.35 here), then products of s and c = cos(a):
         //   u2 = s (sqrt(3) c + s) / 3,  u3 = (3 c^2 - s^2) / 6 ... written without cancellation,
         //   u3 - u2 = (sqrt(3) (c^2 - s^2) - 2 s c) / 3 / sqrt(3) * sqrt(3)   (sin(pi/3 - 2a) / sqrt(3))
-        const T y = T(1) / (T(1) + beta);
+        const T y = FM<T>::rcp(T(1) + beta);
         T sa = y * T(1.0 / 3.0);
 #pragma unroll 1
-        for (int k = 0; k < 5; ++k) sa -= (T(3) * sa - T(4) * sa * sa * sa - y) / (T(3) - T(12) * sa * sa);
+        for (int k = 0; k < 5; ++k) sa -= FM<T>::div(T(3) * sa - T(4) * sa * sa * sa - y, T(3) - T(12) * sa * sa);
         const T ca = tsqrt<T>(T(1) - sa * sa);
         const T r3 = T(1.7320508075688772);
         // u2 = 2/3 sin(a) sin(2pi/3 - a) = 2/3 s (r3/2 c + s/2)
@@ -67,13 +107,13 @@ __host__ __device__ __forceinline__ Roots<T> roots(T beta) {
         return r;
     }
     const T ob = T(1) + beta;
-    const T D = beta * (T(2) + beta) / (T(27) * ob * ob);
+    const T D = FM<T>::div(beta * (T(2) + beta), T(27) * ob * ob);
     const T sd = tsqrt<T>(D > T(0) ? D : T(0));
     T wp = sd, wm = -sd;
 #pragma unroll
     for (int k = 0; k < kIters; ++k) {
-        wp -= (wp * wp * (T(1) + T(2) * wp) - D) / (wp * (T(2) + T(6) * wp));
-        wm -= (wm * wm * (T(1) + T(2) * wm) - D) / (wm * (T(2) + T(6) * wm));
+        wp -= FM<T>::div(wp * wp * (T(1) + T(2) * wp) - D, wp * (T(2) + T(6) * wp));
+        wm -= FM<T>::div(wm * wm * (T(1) + T(2) * wm) - D, wm * (T(2) + T(6) * wm));
     }
     r.u2 = T(1) / T(3) + wm;
     r.u3 = T(1) / T(3) + wp;
@@ -94,11 +134,11 @@ __host__ __device__ __forceinline__ T rf(T x, T y, T z) {
         z = T(0.25) * (z + lam);
     }
     const T A = (x + y + z) * T(1.0 / 3.0);
-    const T iA = T(1) / A;
+    const T iA = FM<T>::rcp(A);
     const T X = T(1) - x * iA, Y = T(1) - y * iA, Z = -(X + Y);
     const T E2 = X * Y - Z * Z, E3 = X * Y * Z;
     const T s = T(1) - E2 * T(0.1) + E3 * T(1.0 / 14.0) + E2 * E2 * T(1.0 / 24.0) - T(3.0 / 44.0) * E2 * E3;
-    return s / tsqrt<T>(A);
+    return FM<T>::div_sqrt(s, A);
 }
 
 // I(a): polar angle between u = a and the turning point u2 (a <= u2).
@@ -148,14 +188,14 @@ __host__ __device__ __forceinline__ T invert_sweep(T target, const Roots<T>& R) 
     const T Z0 = R.d32 * (R.u2 - R.u1);
     const T slope0 = T(1.4142135623730951) * rf<T, N>(X0, X0, Z0);
     const T smax = tsqrt<T>(R.u2);
-    T s = target / slope0;
+    T s = FM<T>::div(target, slope0);
     s = s < T(0) ? T(0) : (s > smax ? smax : s);
 #pragma unroll 1
     for (int k = 0; k < kIters; ++k) {
         const T u = R.u2 - s * s;
         const T f = sweep_to_turn<T, N>(u, R) - target;
-        const T g = T(2) / tsqrt<T>(T(2) * (u - R.u1) * (R.u3 - u));
-        s -= f / g;
+        // dI/ds = 2 / sqrt(2 (u - u1)(u3 - u)): the step is f / (dI/ds)
+        s -= f * T(0.5) * tsqrt<T>(T(2) * (u - R.u1) * (R.u3 - u));
         s = s < T(0) ? T(0) : (s > smax ? smax : s);
     }
     return R.u2 - s * s;

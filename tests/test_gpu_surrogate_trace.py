@@ -56,8 +56,52 @@ def test_surrogate_c2_against_fp64_oracle(surrogate):
             rels.append(np.abs(gg["cross_r"][m, k] - ref["cross_r"][m, k]) / ref["cross_r"][m, k])
     a = np.concatenate(angs)
     r = np.concatenate(rels)
+    print(f"\nsurrogate vs same-rule FP64 oracle: {len(a)} escaped surrogate rays, direction p50 "
+          f"{np.percentile(a, 50):.2e} p99 {np.percentile(a, 99):.2e} max {a.max():.2e} rad; crossing radius "
+          f"p99 {np.percentile(r, 99):.2e} (relative, {len(r)} crossings)")
     assert a.max() < DIR_MAX_RAD, (np.percentile(a, 99), a.max())
     assert np.percentile(r, 99) < CROSS_R_REL_P99, np.percentile(r, 99)
+
+
+def test_surrogate_and_plain_vs_converged_orbit(surrogate):
+    """The same-rule oracle measures rounding only; the 1e-4 rad bar is also checked against the
+    converged orbit (step scale 0.002, no disk step clamp, tolerance of the reference's own
+    known-answer tests), next to the plain FP32 kernel's distance from it at 450 steps."""
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG)[:4]
+    outs = surrogate.trace(views)
+    torch.cuda.synchronize()
+    sur = [hits_numpy(o.cpu()) for o in outs]
+    with Tracer(0) as tr:
+        pl = tr.trace(views)
+        torch.cuda.synchronize()
+        plain = [hits_numpy(o.cpu()) for o in pl]
+    rng = np.random.default_rng(8)
+    a_s, a_p, a_r = [], [], []
+    for v, g, p in zip(views, sur, plain):
+        fine = v.copy()
+        fine.step_scale = 0.002
+        fine.ds_floor = 1e-4
+        fine.max_steps = 200000
+        fine.disk_mode = 0  # no slab clamp: the converged orbit itself (crossings are not compared)
+        idx = rng.choice(v.rays, 1500, replace=False)
+        ref = O.trace_pixels(fine, idx, fp64=True)
+        rule = O.trace_pixels(v, idx, fp64=True)
+        gs, gp = g[idx], p[idx]
+        ok = (ref["status"] == 1) & (np.abs(ref["b"].astype(np.float64) - 27 ** 0.5) > 2e-3)
+        ms = ok & ((gs["flags"] & FLAG_SURROGATE) != 0)
+        assert np.all(gs["status"][ms] == 1)
+        a_s.append(O.angle(gs["dir"][ms], ref["dir"][ms]))
+        mp = ok & (gp["status"] == 1)
+        a_p.append(O.angle(gp["dir"][mp], ref["dir"][mp]))
+        mr = ok & (rule["status"] == 1)
+        a_r.append(O.angle(rule["dir"][mr], ref["dir"][mr]))
+    a_s, a_p, a_r = (np.concatenate(x) for x in (a_s, a_p, a_r))
+    print(f"\nvs converged FP64 orbit: surrogate p99 {np.percentile(a_s, 99):.2e} max {a_s.max():.2e}; "
+          f"plain FP32 (450 steps) p99 {np.percentile(a_p, 99):.2e} max {a_p.max():.2e}; "
+          f"same-rule FP64 p99 {np.percentile(a_r, 99):.2e} max {a_r.max():.2e} rad")
+    assert a_s.max() < DIR_MAX_RAD, (np.percentile(a_s, 99), a_s.max())
 
 
 def test_network_gain_over_closed_form_baseline(surrogate):
@@ -73,6 +117,8 @@ def test_network_gain_over_closed_form_baseline(surrogate):
     pred = surrogate.eval(X[m, :3])[:, 0]
     net = np.abs(pred - X[m, 3]) * surrogate.cfg.y_scale
     base = np.abs(X[m, 3]) * surrogate.cfg.y_scale
+    print(f"\nheld-out exit angles: network p99 {np.percentile(net, 99):.2e} max {net.max():.2e}; closed-form "
+          f"baseline alone p99 {np.percentile(base, 99):.2e} max {base.max():.2e} rad")
     assert np.percentile(net, 99) < 1e-4 and net.max() < 5e-4, (np.percentile(net, 99), net.max())
     assert np.percentile(base, 99) > 100 * np.percentile(net, 99)
 
@@ -96,4 +142,5 @@ def test_surrogate_path_faster_than_plain(surrogate):
     with Tracer(0) as tr:
         t_plain = timed(lambda: tr.trace(views, outs))
     t_surr = timed(lambda: surrogate.trace(views, outs))
+    print(f"\n8 poses: plain {t_plain:.2f} ms, surrogate + fallback {t_surr:.2f} ms ({t_plain / t_surr:.2f}x)")
     assert t_surr < t_plain / 1.2, (t_surr, t_plain)
