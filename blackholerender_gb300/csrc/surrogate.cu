@@ -761,15 +761,37 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ P, 
 }
 
 // ---------------------------------------------------------------------------------------
-// inference: one warp traces 32 rays at a time
+// inference: one warp traces 32 rays at a time, in phases that hand state on through shared
+// memory, so that little is live in registers across the network and no lane waits on
+// another lane's crossing loop:
+//   1  per ray (lane): setup and routing, orbital plane, roots, closed-form angle at the camera
+//      and at the exit, the exit query, and the disk-plane crossings inside the disk's angle
+//      range on either leg (candidates, found without inverting the orbit)
+//   2  per candidate, spread over the warp's lanes: baseline inversion u(phi), crossing query
+//   3  the network on all of the warp's queries, 16 rows at a time
+//   4  per candidate: corrected crossing radius and azimuth; per ray: capture-flag check,
+//      exit direction and the record
 
 constexpr int kInferWarps = 8;
-constexpr int kMaxQ = 128;  // exit query per ray + up to 3 crossing queries per ray
+constexpr int kMaxCand = 3;                   // crossings kept per ray (the record holds 3)
+constexpr int kMaxQ = 32 + 32 * kMaxCand;     // exit query per ray + crossing queries
+
+struct RayStage {  // per warp, structure of arrays over its 32 rays
+    float u1[32], u2[32], u3[32], d32[32];
+    float ic[32], phi0[32], phin[32], x2[32];
+    float e2x[32], e2y[32], e2z[32];
+    float h2[32], baxis[32], b[32];
+    uint32_t info[32];  // bits 0-1 candidates, 2 surrogate, 3-10 plane crossings, 11+5c candidate c (k | leg << 4)
+};
 
 struct InferSmem {
     SmemNet N;
     float4 q[kInferWarps][kMaxQ];
     float2 o[kInferWarps][kMaxQ];
+    RayStage st[kInferWarps];
+    int task[kInferWarps][32 * kMaxCand];     // owner lane << 2 | candidate
+    float tu[kInferWarps][32 * kMaxCand];     // inverted u, then the corrected radius (< 0: outside the disk)
+    float tphi[kInferWarps][32 * kMaxCand];   // azimuth of the corrected crossing
 };
 
 __device__ __forceinline__ unsigned long long warp_append_ull(unsigned long long* ctr) {
@@ -798,10 +820,26 @@ __device__ __forceinline__ void sincos_rr(float x, float* sn, float* cs) {
     *cs = ((q + 1) & 2) ? -c0 : c0;
 }
 
-// Impact parameter of pixel (i, j) in FP64 (near the photon sphere), kept out of line: it is
-// rare and its FP64 code would otherwise crowd the kernel's instruction cache.
-__device__ __noinline__ double impact_parameter_fp64(const DevView& w, const Rule& R, int i, int j) {
-    return setup_ray<double>(w, R, i, j).b;
+// Impact parameter of pixel (i, j) in FP64, for rays near the photon sphere, where the FP32
+// value (relative error ~1e-7) would move the exit angle by more than the error budget:
+// b = r_cam sin(alpha) / sqrt(1 - 2 / r_cam) (Geodesic.h:50-54), alpha the angle between the
+// ray and the radial direction, from the unnormalised pixel direction (blackhole.frag:68-72)
+// in double. The view constants arrive in double. Out of line: rare, and its FP64 code would
+// otherwise crowd the instruction cache.
+__device__ __noinline__ double impact_parameter_fp64(const SurrView& sv, int i, int j) {
+    const DevView& w = sv.view;
+    const double pxx = double(i) + 0.5 + double(w.jitter[0]);
+    const double pxy = double(j) + 0.5 + double(w.jitter[1]);
+    const double th = double(w.tan_half);
+    const double cx = (pxx * sv.inv_w2 - 1.0) * th * sv.aspect_d;
+    const double cy = (pxy * sv.inv_h2 - 1.0) * th;
+    const double dx = double(w.basis[0]) * cx + double(w.basis[3]) * cy - double(w.basis[6]);
+    const double dy = double(w.basis[1]) * cx + double(w.basis[4]) * cy - double(w.basis[7]);
+    const double dz = double(w.basis[2]) * cx + double(w.basis[5]) * cy - double(w.basis[8]);
+    const double* rh = sv.rhat_d;
+    const double px = rh[1] * dz - rh[2] * dy, py = rh[2] * dx - rh[0] * dz, pz = rh[0] * dy - rh[1] * dx;
+    const double s2 = (px * px + py * py + pz * pz) / (dx * dx + dy * dy + dz * dz);
+    return sv.b_scale_d * ::sqrt(s2);
 }
 
 __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
@@ -817,8 +855,15 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* qb = S.q[warp];
     float2* ob = S.o[warp];
+    RayStage& G = S.st[warp];
+    int* task = S.task[warp];
+    float* tu = S.tu[warp];
+    float* tphi = S.tphi[warp];
+    constexpr float kPi = 3.14159265358979f;
     const float beta_band = nm.band / kSqrt27f;
-    unsigned long long n_surr = 0, n_dis = 0, n_q = 0, n_rows = 0;
+    const float uc = sv.uc, x1 = sv.x1;
+    const bool thin = R.disk_mode == BHR_DISK_THIN;
+    uint32_t n_surr = 0, n_dis = 0, n_q = 0, n_rows = 0;
     for (;;) {
         unsigned long long chunk = 0;
         if (lane == 0) chunk = atomicAdd(&q->next_chunk, 1ull);
@@ -827,71 +872,89 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
         if (base >= w.nrays) break;
         const int ray = int(base + lane);
         const bool valid = ray < w.nrays;
-        // ---- ray setup and routing
-        bool sur = valid;
-        const int j = valid ? ray / w.width : 0, i = valid ? ray - j * w.width : 0;
-        const RayInit<float> ri = setup_ray<float>(w, R, i, j);
-        const V3<float> cam{w.cam[0], w.cam[1], w.cam[2]};
-        float b = ri.b;
-        float beta = b / kSqrt27f - 1.0f;
-        if (sur && fabsf(beta) < 0.02f) {  // near the photon sphere: impact parameter in FP64
-            const double bd = impact_parameter_fp64(w, R, i, j);
-            beta = float(bd / kSqrt27d - 1.0);
-            b = float(bd);
-        }
-        sur = sur && dot3(cam, ri.v) < 0.f && w.rcam >= nm.rc_lo && w.rcam <= nm.rc_hi && b <= nm.b_max &&
-              beta >= beta_band;
-        // orbital plane: e1 along the camera, e2 along the tangential part of the velocity
-        const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
-        const float ve = dot3(ri.v, e1);
-        V3<float> e2{ri.v.x - ve * e1.x, ri.v.y - ve * e1.y, ri.v.z - ve * e1.z};
-        const float e2n = dot3(e2, e2);
-        sur = sur && e2n > 1e-12f;
-        const float e2i = rsqrtf(fmaxf(e2n, 1e-30f));
-        e2 = {e2.x * e2i, e2.y * e2i, e2.z * e2i};
-        orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
-        const float uc = sv.uc;
-        sur = sur && uc < Rt.u2 * 0.9999f;
-        // ---- closed-form baseline and queries
-        const float Ic = orbit::sweep_to_turn<float, orbit::kBaseDup>(uc, Rt);
-        const float Ie = orbit::sweep_to_turn<float, orbit::kBaseDup>(nm.ue, Rt);
-        const float phi0 = Ic + Ie;
-        const float x1 = sv.x1;
-        const float tb = __logf(1.0f + fabsf(beta) / nm.t_eps);  // 1 + |beta|/eps >= 1.19 here
-        const float x2 = (beta < 0.f ? -tb : tb) * nm.t_scale;
-        qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
-        // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
-        float phin = atan2f(-e1.y, e2.y);
-        if (phin < 0.f) phin += 3.14159265358979f;
-        if (phin >= 3.14159265358979f) phin -= 3.14159265358979f;
-        sur = sur && (fabsf(e1.y) + fabsf(e2.y)) > 1e-6f;
-        // up to 3 crossing candidates (u on the baseline orbit, crossing index k, outgoing leg),
-        // kept in registers: slot c holds u_c, k in bits 8c..8c+6 of ckl, leg in bit 8c+7
-        int nplane = 0, ncand = 0;
-        float cu0 = 0.f, cu1 = 0.f, cu2 = 0.f;
-        uint32_t ckl = 0;
-        if (sur) {
-            const float rlo = R.disk_inner * 0.97f, rhi = R.disk_outer * 1.03f;
+        // ---- phase 1: per ray
+        int ncand = 0;
+        {
+            bool sur = valid;
+            const int j = valid ? ray / w.width : 0, i = valid ? ray - j * w.width : 0;
+            const RayInit<float> ri = setup_ray<float>(w, R, i, j);
+            const V3<float> cam{w.cam[0], w.cam[1], w.cam[2]};
+            float b = ri.b;
+            float beta = b * (1.0f / kSqrt27f) - 1.0f;
+            if (sur && fabsf(beta) < 0.02f) {  // near the photon sphere: impact parameter in FP64
+                const double bd = impact_parameter_fp64(sv, i, j);
+                beta = float(bd * (1.0 / kSqrt27d) - 1.0);
+                b = float(bd);
+            }
+            sur = sur && dot3(cam, ri.v) < 0.f && w.rcam >= nm.rc_lo && w.rcam <= nm.rc_hi && b <= nm.b_max &&
+                  beta >= beta_band;
+            // orbital plane: e1 along the camera, e2 along the tangential part of the velocity
+            const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
+            const float ve = dot3(ri.v, e1);
+            V3<float> e2{ri.v.x - ve * e1.x, ri.v.y - ve * e1.y, ri.v.z - ve * e1.z};
+            const float e2n = dot3(e2, e2);
+            sur = sur && e2n > 1e-12f;
+            const float e2i = rsqrtf(fmaxf(e2n, 1e-30f));
+            e2 = {e2.x * e2i, e2.y * e2i, e2.z * e2i};
+            const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
+            sur = sur && uc < Rt.u2 * 0.9999f;
+            // closed-form baseline at the camera and at the exit
+            const float Ic = orbit::sweep_to_turn<float, orbit::kBaseDup>(uc, Rt);
+            const float Ie = orbit::sweep_to_turn<float, orbit::kBaseDup>(nm.ue, Rt);
+            const float phi0 = Ic + Ie;
+            const float tb = __logf(1.0f + fabsf(beta) * (1.0f / nm.t_eps));  // 1 + |beta|/eps >= 1.19 here
+            const float x2 = (beta < 0.f ? -tb : tb) * nm.t_scale;
+            qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
+            // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
+            float phin = atan2f(-e1.y, e2.y);
+            if (phin < 0.f) phin += kPi;
+            if (phin >= kPi) phin -= kPi;
+            sur = sur && (fabsf(e1.y) + fabsf(e2.y)) > 1e-6f;
+            int nplane = 0;
+            uint32_t cw = 0;
+            if (sur) {
 #pragma unroll 1
-            for (int k = 0; k < 16; ++k) {
-                const float phk = phin + float(k) * 3.14159265358979f;
-                if (phk >= phi0) break;
-                ++nplane;
-                if (ncand < 3 && R.disk_mode == BHR_DISK_THIN) {
-                    const bool leg = phk > Ic;
-                    const float u = orbit::invert_sweep<float, orbit::kBaseDup, 4>(leg ? phk - Ic : Ic - phk, Rt);
-                    const float rb = 1.0f / u;
-                    if (rb >= rlo && rb <= rhi) {
-                        if (ncand == 0) cu0 = u;
-                        else if (ncand == 1) cu1 = u;
-                        else cu2 = u;
-                        ckl |= (uint32_t(k) | (leg ? 0x80u : 0u)) << (8 * ncand);
-                        ++ncand;
+                for (int k = 0; k < 16; ++k) {
+                    if (phin + float(k) * kPi >= phi0) break;
+                    ++nplane;
+                }
+                if (thin) {
+                    // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning
+                    // point, |phi_k - Ic|, lies between the sweeps to those radii (or to the
+                    // turning point, where the orbit stays outside them)
+                    const float Ilo = orbit::sweep_to_turn<float, orbit::kBaseDup>(
+                        fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt);
+                    const float Ihi = orbit::sweep_to_turn<float, orbit::kBaseDup>(
+                        fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt);
+#pragma unroll 1
+                    for (int k = 0; k < nplane && ncand < kMaxCand; ++k) {
+                        const float phk = phin + float(k) * kPi;
+                        const bool leg = phk > Ic;
+                        const float tg = leg ? phk - Ic : Ic - phk;
+                        if (tg >= Ilo && tg <= Ihi) {
+                            cw |= (uint32_t(k) | (leg ? 16u : 0u)) << (11 + 5 * ncand);
+                            ++ncand;
+                        }
                     }
                 }
             }
+            G.u1[lane] = Rt.u1;
+            G.u2[lane] = Rt.u2;
+            G.u3[lane] = Rt.u3;
+            G.d32[lane] = Rt.d32;
+            G.ic[lane] = Ic;
+            G.phi0[lane] = phi0;
+            G.phin[lane] = phin;
+            G.x2[lane] = x2;
+            G.e2x[lane] = e2.x;
+            G.e2y[lane] = e2.y;
+            G.e2z[lane] = e2.z;
+            G.h2[lane] = ri.h2;
+            G.baxis[lane] = ri.b_axis;
+            G.b[lane] = b;
+            G.info[lane] = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw;
         }
-        // crossing queries after the 32 exit queries
+        // ---- phase 2: crossing candidates, compacted over the lanes
         int off = ncand;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -900,80 +963,121 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
         }
         const int total = __shfl_sync(0xffffffffu, off, 31);
         off -= ncand;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            if (c < ncand) {
-                const float u = c == 0 ? cu0 : (c == 1 ? cu1 : cu2);
-                const bool leg = (ckl >> (8 * c + 7)) & 1u;
-                const float sg = leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f))
-                                     : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
-                qb[32 + off + c] = make_float4(x1, x2, sg, 0.f);
-            }
+        for (int c = 0; c < ncand; ++c) task[off + c] = (lane << 2) | c;
+        __syncwarp();
+#pragma unroll 1
+        for (int t = lane; t < total; t += 32) {
+            const int own = task[t] >> 2, c = task[t] & 3;
+            orbit::Roots<float> Rt;
+            Rt.u1 = G.u1[own];
+            Rt.u2 = G.u2[own];
+            Rt.u3 = G.u3[own];
+            Rt.d32 = G.d32[own];
+            const uint32_t kl = (G.info[own] >> (11 + 5 * c)) & 31u;
+            const float phk = G.phin[own] + float(kl & 15u) * kPi;
+            const float Ic = G.ic[own];
+            const bool leg = (kl & 16u) != 0;
+            const float u = orbit::invert_sweep<float, orbit::kBaseDup, 4>(leg ? phk - Ic : Ic - phk, Rt);
+            const float sg = leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f)) : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
+            qb[32 + t] = make_float4(x1, G.x2[own], sg, 0.f);
+            tu[t] = u;
         }
         __syncwarp();
-        // ---- network: all queries of the warp, 16 rows at a time
-        const int nq = 32 + total;
-        const int ntiles = (nq + 15) >> 4;
+        // ---- phase 3: the network on all queries of the warp
+        const int ntiles = (32 + total + 15) >> 4;
         mlp_eval_tiles(S.N, qb, ob, ntiles);
-        n_rows += lane == 0 ? (unsigned long long)(16 * ntiles) : 0ull;
-        n_q += sur ? 1 + ncand : 0;
-        // ---- results
-        const float2 oe = ob[lane];
-        if (sur && oe.y > 0.f) {  // the learned capture flag disagrees with b > sqrt(27): integrator decides
-            sur = false;
-            ++n_dis;
+        n_rows += lane == 0 ? uint32_t(16 * ntiles) : 0u;
+        // ---- phase 4: corrected crossings (per candidate), then records (per ray)
+#pragma unroll 1
+        for (int t = lane; t < total; t += 32) {
+            const int own = task[t] >> 2, c = task[t] & 3;
+            orbit::Roots<float> Rt;
+            Rt.u1 = G.u1[own];
+            Rt.u2 = G.u2[own];
+            Rt.u3 = G.u3[own];
+            const uint32_t kl = (G.info[own] >> (11 + 5 * c)) & 31u;
+            const float u = tu[t];
+            const float dphi = ob[32 + t].x * nm.y_scale;
+            const float sPu = orbit::dudphi<float>(u, Rt);
+            const float us = (kl & 16u) ? u + dphi * sPu : u - dphi * sPu;
+            const float rs = 1.0f / us;
+            float rr = -1.f, ph = 0.f;
+            if (rs >= R.disk_inner && rs <= R.disk_outer) {
+                float s2, c2;
+                sincos_rr(G.phin[own] + float(kl & 15u) * kPi, &s2, &c2);
+                const float hx = rs * (c2 * w.rhat[0] + s2 * G.e2x[own]);
+                const float hz = rs * (c2 * w.rhat[2] + s2 * G.e2z[own]);
+                ph = atan2f(hz, hx);
+                rr = rs;
+            }
+            tu[t] = rr;
+            tphi[t] = ph;
         }
-        if (valid && !sur) fb_list[warp_append_ull(&q->fb_count)] = ray;
-        if (sur) {
-            ++n_surr;
-            const float phi = phi0 + oe.x * nm.y_scale;
-            float sp, cp;
-            sincos_rr(phi, &sp, &cp);
-            const float ue = nm.ue;
-            const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
-            const V3<float> xt{-sp * e1.x + cp * e2.x, -sp * e1.y + cp * e2.y, -sp * e1.z + cp * e2.z};
-            const float re = 1.0f / ue;
-            const V3<float> xe{xr.x * re, xr.y * re, xr.z * re};
-            // velocity at the exit: along dx/dphi = sqrt(P)/u^2 xr + xt/u, with |v|^2 from the energy
-            // integral of x'' = -3 h^2 x / r^5: |v|^2 = |v0|^2 - 2 h^2 / rc^3 + 2 h^2 u^3
-            const float sP = orbit::dudphi<float>(ue, Rt);
-            V3<float> T{sP * re * re * xr.x + re * xt.x, sP * re * re * xr.y + re * xt.y, sP * re * re * xr.z + re * xt.z};
-            const float vmag = sqrtf(fmaxf(1.0f - ri.h2 * w.two_over_r3 + 2.0f * ri.h2 * ue * ue * ue, 1e-12f));
-            const float Ti = vmag * rsqrtf(dot3(T, T));
-            T = {T.x * Ti, T.y * Ti, T.z * Ti};
-            const V3<float> d = far_field_dir(xe, T, ri.h2);
-            // crossings, in march order, inside [disk_inner, disk_outer]
-            float cr0 = 0.f, cr1 = 0.f, cr2 = 0.f, cp0 = 0.f, cp1 = 0.f, cp2 = 0.f;
-            int nrec = 0;
+        __syncwarp();
+        {
+            const uint32_t info = G.info[lane];
+            bool sur = (info & 4u) != 0;
+            const float2 oe = ob[lane];
+            n_q += sur ? 1u + uint32_t(ncand) : 0u;
+            if (sur && oe.y > 0.f) {  // the learned capture flag disagrees with b > sqrt(27): integrator decides
+                sur = false;
+                ++n_dis;
+            }
+            if (valid && !sur) fb_list[warp_append_ull(&q->fb_count)] = ray;
+            if (sur) {
+                ++n_surr;
+                orbit::Roots<float> Rt;
+                Rt.u1 = G.u1[lane];
+                Rt.u2 = G.u2[lane];
+                Rt.u3 = G.u3[lane];
+                const float phi = G.phi0[lane] + oe.x * nm.y_scale;
+                float sp, cp;
+                sincos_rr(phi, &sp, &cp);
+                const float ue = nm.ue;
+                const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
+                const V3<float> e2{G.e2x[lane], G.e2y[lane], G.e2z[lane]};
+                const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
+                const V3<float> xt{-sp * e1.x + cp * e2.x, -sp * e1.y + cp * e2.y, -sp * e1.z + cp * e2.z};
+                const float re = 1.0f / ue;
+                const V3<float> xe{xr.x * re, xr.y * re, xr.z * re};
+                // velocity at the exit: along dx/dphi = sqrt(P)/u^2 xr + xt/u, with |v|^2 from the energy
+                // integral of x'' = -3 h^2 x / r^5: |v|^2 = |v0|^2 - 2 h^2 / rc^3 + 2 h^2 u^3
+                const float h2 = G.h2[lane];
+                const float sP = orbit::dudphi<float>(ue, Rt);
+                V3<float> T{sP * re * re * xr.x + re * xt.x, sP * re * re * xr.y + re * xt.y,
+                            sP * re * re * xr.z + re * xt.z};
+                const float vmag = sqrtf(fmaxf(1.0f - h2 * w.two_over_r3 + 2.0f * h2 * ue * ue * ue, 1e-12f));
+                const float Ti = vmag * rsqrtf(dot3(T, T));
+                T = {T.x * Ti, T.y * Ti, T.z * Ti};
+                const V3<float> d = far_field_dir(xe, T, h2);
+                // crossings inside [disk_inner, disk_outer], in march order
+                float cr[3] = {0.f, 0.f, 0.f}, cph[3] = {0.f, 0.f, 0.f};
+                int nrec = 0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                if (c < ncand) {
-                    const float dphi = ob[32 + off + c].x * nm.y_scale;
-                    const float u = c == 0 ? cu0 : (c == 1 ? cu1 : cu2);
-                    const uint32_t kl = (ckl >> (8 * c)) & 0xffu;
-                    const float sPu = orbit::dudphi<float>(u, Rt);
-                    const float us = (kl & 0x80u) ? u + dphi * sPu : u - dphi * sPu;
-                    const float rs = 1.0f / us;
-                    if (rs >= R.disk_inner && rs <= R.disk_outer) {
-                        const float phk = phin + float(kl & 0x7fu) * 3.14159265358979f;
-                        float s2, c2;
-                        sincos_rr(phk, &s2, &c2);
-                        const float hx = rs * (c2 * e1.x + s2 * e2.x), hz = rs * (c2 * e1.z + s2 * e2.z);
-                        const float ph = atan2f(hz, hx);
-                        if (nrec == 0) { cr0 = rs; cp0 = ph; }
-                        else if (nrec == 1) { cr1 = rs; cp1 = ph; }
-                        else { cr2 = rs; cp2 = ph; }
-                        ++nrec;
+                for (int c = 0; c < kMaxCand; ++c) {
+                    if (c < ncand) {
+                        const float rr = tu[off + c];
+                        if (rr > 0.f) {
+                            const float pp = tphi[off + c];
+                            cr[0] = nrec == 0 ? rr : cr[0];
+                            cph[0] = nrec == 0 ? pp : cph[0];
+                            cr[1] = nrec == 1 ? rr : cr[1];
+                            cph[1] = nrec == 1 ? pp : cph[1];
+                            cr[2] = nrec == 2 ? rr : cr[2];
+                            cph[2] = nrec == 2 ? pp : cph[2];
+                            ++nrec;
+                        }
                     }
                 }
+                const uint32_t nplane = (info >> 3) & 0xffu;
+                const uint32_t w0 = uint32_t(BHR_STATUS_ESCAPED) | (uint32_t(nrec) << 8) |
+                                    (uint32_t(BHR_FLAG_SURROGATE) << 16) | (nplane << 24);
+                float4* p = reinterpret_cast<float4*>(w.out + ray);
+                p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
+                p[1] = make_float4(d.z, 1.0f / Rt.u2, 0.f, 0.f);
+                p[2] = make_float4(G.baxis[lane], G.b[lane], cr[0], cr[1]);
+                p[3] = make_float4(cr[2], cph[0], cph[1], cph[2]);
             }
-            const uint32_t w0 = uint32_t(BHR_STATUS_ESCAPED) | (uint32_t(nrec) << 8) |
-                                (uint32_t(BHR_FLAG_SURROGATE) << 16) | (uint32_t(min(nplane, 255)) << 24);
-            float4* p = reinterpret_cast<float4*>(w.out + ray);
-            p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
-            p[1] = make_float4(d.z, 1.0f / Rt.u2, 0.f, 0.f);
-            p[2] = make_float4(ri.b_axis, b, cr0, cr1);
-            p[3] = make_float4(cr2, cp0, cp1, cp2);
         }
         __syncwarp();
     }
@@ -983,10 +1087,10 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
         n_q += __shfl_xor_sync(0xffffffffu, n_q, o);
     }
     if (lane == 0) {
-        atomicAdd(&q->surr_rays, n_surr);
-        atomicAdd(&q->mlp_queries, n_q);
-        atomicAdd(&q->mlp_rows, n_rows);
-        if (n_dis) atomicAdd(&q->capture_disagree, n_dis);
+        atomicAdd(&q->surr_rays, (unsigned long long)n_surr);
+        atomicAdd(&q->mlp_queries, (unsigned long long)n_q);
+        atomicAdd(&q->mlp_rows, (unsigned long long)n_rows);
+        if (n_dis) atomicAdd(&q->capture_disagree, (unsigned long long)n_dis);
     }
 }
 

@@ -57,6 +57,11 @@ struct SurrView {
     Norm norm;
     float x1;  // network input 1 of this view (scaled log r_cam)
     float uc;  // 1 / r_cam
+    // double constants of the view for the FP64 impact parameter near the photon sphere
+    double inv_w2, inv_h2;  // 2 / width, 2 / height
+    double aspect_d;        // width / height
+    double rhat_d[3];       // camera direction from the float camera position
+    double b_scale_d;       // r_cam / sqrt(1 - 2 / r_cam)
 };
 cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
                                    cudaStream_t st);

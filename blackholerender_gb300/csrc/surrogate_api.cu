@@ -394,6 +394,17 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
         sv.x1 = float((std::log(double(sv.view.rcam)) - std::log(double(s->norm.rc_lo))) /
                           (std::log(double(s->norm.rc_hi)) - std::log(double(s->norm.rc_lo))) * 2.0 - 1.0);
         sv.uc = 1.0f / sv.view.rcam;
+        {
+            const double cx = views[k].cam_pos[0], cy = views[k].cam_pos[1], cz = views[k].cam_pos[2];
+            const double rc = std::sqrt(cx * cx + cy * cy + cz * cz);
+            sv.inv_w2 = 2.0 / double(views[k].width);
+            sv.inv_h2 = 2.0 / double(views[k].height);
+            sv.aspect_d = double(views[k].width) / double(views[k].height);
+            sv.rhat_d[0] = cx / rc;
+            sv.rhat_d[1] = cy / rc;
+            sv.rhat_d[2] = cz / rc;
+            sv.b_scale_d = rc / std::sqrt(std::max(1.0 - 2.0 / rc, 1e-300));
+        }
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
