@@ -775,13 +775,16 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ P, 
 constexpr int kInferWarps = 8;
 constexpr int kMaxCand = 3;                   // crossings kept per ray (the record holds 3)
 constexpr int kMaxQ = 32 + 32 * kMaxCand;     // exit query per ray + crossing queries
+constexpr int kCapDup = 3;                    // R_F duplication steps of the captured-orbit closed form
+constexpr uint32_t kCapBit = 1u << 26;        // stage info: the ray's orbit is captured
 
 struct RayStage {  // per warp, structure of arrays over its 32 rays
     float u1[32], u2[32], u3[32], d32[32];
     float ic[32], phi0[32], phin[32], x2[32];
     float e2x[32], e2y[32], e2z[32];
     float h2[32], baxis[32], b[32];
-    uint32_t info[32];  // bits 0-1 candidates, 2 surrogate, 3-10 plane crossings, 11+5c candidate c (k | leg << 4)
+    uint32_t info[32];  // bits 0-1 candidates, 2 surrogate, 3-10 plane crossings, 11+5c candidate c (k | leg << 4),
+                        // 26 captured orbit
 };
 
 struct InferSmem {
@@ -842,7 +845,65 @@ __device__ __noinline__ double impact_parameter_fp64(const SurrView& sv, int i, 
     return sv.b_scale_d * ::sqrt(s2);
 }
 
-__global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
+// Phase-1 work of a captured orbit, out of line: it runs for the rays of the shadow only, and
+// inlined it would crowd the instruction cache of every warp.
+struct CapStage {
+    float u1, A, k2, K;  // the orbit (orbit::CapOrbit without c)
+    float Ic;            // F(theta(u_camera))
+    float phi0;          // angle from the camera to the capture radius
+    float Ilo, Ihi;      // angles from the camera to 1.03 r_out and 0.97 r_in (empty range: Ilo > Ihi)
+};
+
+__device__ __noinline__ CapStage cap_stage(float beta, float uc, float capture_r, float disk_inner, float disk_outer,
+                                           bool range) {
+    const orbit::CapOrbit<float> C = orbit::cap_orbit<float, kCapDup>(beta);
+    CapStage o;
+    o.u1 = C.u1;
+    o.A = C.A;
+    o.k2 = C.k2;
+    o.K = C.K;
+    const float s2a = rsqrtf(2.0f * C.A);
+    o.Ic = orbit::cap_F<float, kCapDup>(uc, C);
+    o.phi0 = (orbit::cap_F<float, kCapDup>(1.0f / capture_r, C) - o.Ic) * s2a;
+    o.Ilo = 1.f;
+    o.Ihi = 0.f;
+    if (range) {
+        // crossing k lies in [0.97 r_in, 1.03 r_out] iff phi_k lies between the angles from the
+        // camera to those radii on the way in (clipped to the camera and the capture radius)
+        const float ua = fmaxf(1.0f / (disk_outer * 1.03f), uc);
+        const float ub = fminf(1.0f / (disk_inner * 0.97f), 1.0f / capture_r);
+        if (ua < ub) {
+            o.Ilo = (orbit::cap_F<float, kCapDup>(ua, C) - o.Ic) * s2a;
+            o.Ihi = (orbit::cap_F<float, kCapDup>(ub, C) - o.Ic) * s2a;
+        }
+    }
+    return o;
+}
+
+// u of a captured orbit at angle phk from the camera: Newton on phi(u) = phk with
+// dphi/du = 1 / sqrt(P(u)), kept in [u_camera, 1 / capture_r]. Out of line for the same reason.
+__device__ __noinline__ float cap_invert(float u1, float A, float k2, float K, float b, float Fc, float phk, float uc,
+                                         float capture_r, float disk_inner, float disk_outer) {
+    orbit::CapOrbit<float> C;
+    C.u1 = u1;
+    C.A = A;
+    C.k2 = k2;
+    C.K = K;
+    const float cb = 1.0f / b;
+    C.c = cb * cb;
+    const float s2a = rsqrtf(2.0f * A);
+    const float uh = 1.0f / capture_r;
+    float u = fminf(fmaxf(0.5f * (1.0f / (disk_inner * 0.97f) + 1.0f / (disk_outer * 1.03f)), uc), uh);
+#pragma unroll 1
+    for (int it = 0; it < 6; ++it) {
+        const float f = (orbit::cap_F<float, kCapDup>(u, C) - Fc) * s2a - phk;
+        const float P = fmaxf(2.0f * u * u * u - u * u + C.c, 0.f);
+        u = fminf(fmaxf(u - f * sqrtf(P), uc), uh);
+    }
+    return u;
+}
+
+__global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_constant__ SurrView sv,
                                                                 const float* __restrict__ P, WorkQueue* q,
                                                                 int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -886,8 +947,11 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                 beta = float(bd * (1.0 / kSqrt27d) - 1.0);
                 b = float(bd);
             }
+            // captured orbits (b < sqrt(27)) are answered too: the network gives their capture flag,
+            // the closed form their crossings (no turning point, no learned residual)
+            const bool cap = beta < 0.f;
             sur = sur && dot3(cam, ri.v) < 0.f && w.rcam >= nm.rc_lo && w.rcam <= nm.rc_hi && b <= nm.b_max &&
-                  beta >= beta_band;
+                  fabsf(beta) >= beta_band;
             // orbital plane: e1 along the camera, e2 along the tangential part of the velocity
             const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
             const float ve = dot3(ri.v, e1);
@@ -896,15 +960,33 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             sur = sur && e2n > 1e-12f;
             const float e2i = rsqrtf(fmaxf(e2n, 1e-30f));
             e2 = {e2.x * e2i, e2.y * e2i, e2.z * e2i};
-            const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
-            sur = sur && uc < Rt.u2 * 0.9999f;
-            // closed-form baseline at the camera and at the exit
-            const float Ic = orbit::sweep_to_turn<float, orbit::kBaseDup>(uc, Rt);
-            const float Ie = orbit::sweep_to_turn<float, orbit::kBaseDup>(nm.ue, Rt);
-            const float phi0 = Ic + Ie;
             const float tb = __logf(1.0f + fabsf(beta) * (1.0f / nm.t_eps));  // 1 + |beta|/eps >= 1.19 here
             const float x2 = (beta < 0.f ? -tb : tb) * nm.t_scale;
-            qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
+            // stage slots: escaping orbit: u1 u2 u3 d32, Ic = angle camera -> turning point, phi0 = angle
+            // camera -> exit; captured orbit: u1, A, k^2, K, Ic = F(camera), phi0 = angle camera -> horizon
+            float s0, s1, s2, s3, Ic, phi0;
+            float Ilo = 1.f, Ihi = 0.f;  // angle range of the disk's crossings (from the turning point / camera)
+            if (!cap) {
+                const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
+                sur = sur && uc < Rt.u2 * 0.9999f;
+                // closed-form baseline at the camera and at the exit
+                Ic = orbit::sweep_to_turn<float, orbit::kBaseDup>(uc, Rt);
+                phi0 = Ic + orbit::sweep_to_turn<float, orbit::kBaseDup>(nm.ue, Rt);
+                qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
+                if (sur && thin) {
+                    // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
+                    // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
+                    // where the orbit stays outside them)
+                    Ilo = orbit::sweep_to_turn<float, orbit::kBaseDup>(fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt);
+                    Ihi = orbit::sweep_to_turn<float, orbit::kBaseDup>(fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt);
+                }
+                s0 = Rt.u1, s1 = Rt.u2, s2 = Rt.u3, s3 = Rt.d32;
+            } else {
+                const CapStage cs = cap_stage(beta, uc, R.capture_r, R.disk_inner, R.disk_outer, sur && thin);
+                qb[lane] = make_float4(x1, x2, 1.0f, 0.f);  // the capture flag is trained at sigma = 1
+                Ic = cs.Ic, phi0 = cs.phi0, Ilo = cs.Ilo, Ihi = cs.Ihi;
+                s0 = cs.u1, s1 = cs.A, s2 = cs.k2, s3 = cs.K;
+            }
             // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
             float phin = atan2f(-e1.y, e2.y);
             if (phin < 0.f) phin += kPi;
@@ -918,30 +1000,21 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                     if (phin + float(k) * kPi >= phi0) break;
                     ++nplane;
                 }
-                if (thin) {
-                    // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning
-                    // point, |phi_k - Ic|, lies between the sweeps to those radii (or to the
-                    // turning point, where the orbit stays outside them)
-                    const float Ilo = orbit::sweep_to_turn<float, orbit::kBaseDup>(
-                        fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt);
-                    const float Ihi = orbit::sweep_to_turn<float, orbit::kBaseDup>(
-                        fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt);
 #pragma unroll 1
-                    for (int k = 0; k < nplane && ncand < kMaxCand; ++k) {
-                        const float phk = phin + float(k) * kPi;
-                        const bool leg = phk > Ic;
-                        const float tg = leg ? phk - Ic : Ic - phk;
-                        if (tg >= Ilo && tg <= Ihi) {
-                            cw |= (uint32_t(k) | (leg ? 16u : 0u)) << (11 + 5 * ncand);
-                            ++ncand;
-                        }
+                for (int k = 0; k < nplane && ncand < kMaxCand; ++k) {
+                    const float phk = phin + float(k) * kPi;
+                    const bool leg = !cap && phk > Ic;
+                    const float tg = cap ? phk : (leg ? phk - Ic : Ic - phk);
+                    if (tg >= Ilo && tg <= Ihi) {
+                        cw |= (uint32_t(k) | (leg ? 16u : 0u)) << (11 + 5 * ncand);
+                        ++ncand;
                     }
                 }
             }
-            G.u1[lane] = Rt.u1;
-            G.u2[lane] = Rt.u2;
-            G.u3[lane] = Rt.u3;
-            G.d32[lane] = Rt.d32;
+            G.u1[lane] = s0;
+            G.u2[lane] = s1;
+            G.u3[lane] = s2;
+            G.d32[lane] = s3;
             G.ic[lane] = Ic;
             G.phi0[lane] = phi0;
             G.phin[lane] = phin;
@@ -952,7 +1025,8 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             G.h2[lane] = ri.h2;
             G.baxis[lane] = ri.b_axis;
             G.b[lane] = b;
-            G.info[lane] = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw;
+            G.info[lane] = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw |
+                           (cap ? kCapBit : 0u);
         }
         // ---- phase 2: crossing candidates, compacted over the lanes
         int off = ncand;
@@ -968,18 +1042,25 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
 #pragma unroll 1
         for (int t = lane; t < total; t += 32) {
             const int own = task[t] >> 2, c = task[t] & 3;
-            orbit::Roots<float> Rt;
-            Rt.u1 = G.u1[own];
-            Rt.u2 = G.u2[own];
-            Rt.u3 = G.u3[own];
-            Rt.d32 = G.d32[own];
-            const uint32_t kl = (G.info[own] >> (11 + 5 * c)) & 31u;
+            const uint32_t info = G.info[own];
+            const uint32_t kl = (info >> (11 + 5 * c)) & 31u;
             const float phk = G.phin[own] + float(kl & 15u) * kPi;
             const float Ic = G.ic[own];
-            const bool leg = (kl & 16u) != 0;
-            const float u = orbit::invert_sweep<float, orbit::kBaseDup, 4>(leg ? phk - Ic : Ic - phk, Rt);
-            const float sg = leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f)) : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
-            qb[32 + t] = make_float4(x1, G.x2[own], sg, 0.f);
+            float u, sg = 0.f;
+            if (!(info & kCapBit)) {
+                orbit::Roots<float> Rt;
+                Rt.u1 = G.u1[own];
+                Rt.u2 = G.u2[own];
+                Rt.u3 = G.u3[own];
+                Rt.d32 = G.d32[own];
+                const bool leg = (kl & 16u) != 0;
+                u = orbit::invert_sweep<float, orbit::kBaseDup, 4>(leg ? phk - Ic : Ic - phk, Rt);
+                sg = leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f)) : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
+            } else {
+                u = cap_invert(G.u1[own], G.u2[own], G.u3[own], G.d32[own], G.b[own], Ic, phk, uc, R.capture_r,
+                               R.disk_inner, R.disk_outer);
+            }
+            qb[32 + t] = make_float4(x1, G.x2[own], sg, 0.f);  // captured: a row nobody reads
             tu[t] = u;
         }
         __syncwarp();
@@ -991,15 +1072,19 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
 #pragma unroll 1
         for (int t = lane; t < total; t += 32) {
             const int own = task[t] >> 2, c = task[t] & 3;
-            orbit::Roots<float> Rt;
-            Rt.u1 = G.u1[own];
-            Rt.u2 = G.u2[own];
-            Rt.u3 = G.u3[own];
-            const uint32_t kl = (G.info[own] >> (11 + 5 * c)) & 31u;
+            const uint32_t info = G.info[own];
+            const uint32_t kl = (info >> (11 + 5 * c)) & 31u;
             const float u = tu[t];
-            const float dphi = ob[32 + t].x * nm.y_scale;
-            const float sPu = orbit::dudphi<float>(u, Rt);
-            const float us = (kl & 16u) ? u + dphi * sPu : u - dphi * sPu;
+            float us = u;
+            if (!(info & kCapBit)) {  // escaping orbit: the network's correction of the baseline
+                orbit::Roots<float> Rt;
+                Rt.u1 = G.u1[own];
+                Rt.u2 = G.u2[own];
+                Rt.u3 = G.u3[own];
+                const float dphi = ob[32 + t].x * nm.y_scale;
+                const float sPu = orbit::dudphi<float>(u, Rt);
+                us = (kl & 16u) ? u + dphi * sPu : u - dphi * sPu;
+            }
             const float rs = 1.0f / us;
             float rr = -1.f, ph = 0.f;
             if (rs >= R.disk_inner && rs <= R.disk_outer) {
@@ -1017,39 +1102,48 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
         {
             const uint32_t info = G.info[lane];
             bool sur = (info & 4u) != 0;
+            const bool cap = (info & kCapBit) != 0;
             const float2 oe = ob[lane];
-            n_q += sur ? 1u + uint32_t(ncand) : 0u;
-            if (sur && oe.y > 0.f) {  // the learned capture flag disagrees with b > sqrt(27): integrator decides
+            n_q += sur ? 1u + (cap ? 0u : uint32_t(ncand)) : 0u;
+            if (sur && (oe.y > 0.f) != cap) {  // the learned capture flag disagrees with b vs sqrt(27): integrator decides
                 sur = false;
                 ++n_dis;
             }
             if (valid && !sur) fb_list[warp_append_ull(&q->fb_count)] = ray;
             if (sur) {
                 ++n_surr;
-                orbit::Roots<float> Rt;
-                Rt.u1 = G.u1[lane];
-                Rt.u2 = G.u2[lane];
-                Rt.u3 = G.u3[lane];
-                const float phi = G.phi0[lane] + oe.x * nm.y_scale;
-                float sp, cp;
-                sincos_rr(phi, &sp, &cp);
-                const float ue = nm.ue;
-                const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
-                const V3<float> e2{G.e2x[lane], G.e2y[lane], G.e2z[lane]};
-                const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
-                const V3<float> xt{-sp * e1.x + cp * e2.x, -sp * e1.y + cp * e2.y, -sp * e1.z + cp * e2.z};
-                const float re = 1.0f / ue;
-                const V3<float> xe{xr.x * re, xr.y * re, xr.z * re};
-                // velocity at the exit: along dx/dphi = sqrt(P)/u^2 xr + xt/u, with |v|^2 from the energy
-                // integral of x'' = -3 h^2 x / r^5: |v|^2 = |v0|^2 - 2 h^2 / rc^3 + 2 h^2 u^3
-                const float h2 = G.h2[lane];
-                const float sP = orbit::dudphi<float>(ue, Rt);
-                V3<float> T{sP * re * re * xr.x + re * xt.x, sP * re * re * xr.y + re * xt.y,
-                            sP * re * re * xr.z + re * xt.z};
-                const float vmag = sqrtf(fmaxf(1.0f - h2 * w.two_over_r3 + 2.0f * h2 * ue * ue * ue, 1e-12f));
-                const float Ti = vmag * rsqrtf(dot3(T, T));
-                T = {T.x * Ti, T.y * Ti, T.z * Ti};
-                const V3<float> d = far_field_dir(xe, T, h2);
+                // captured: no direction (as TraceResult::dir), closest approach = the capture radius
+                V3<float> d{0.f, 0.f, 0.f};
+                float min_r = R.capture_r;
+                uint32_t status = BHR_STATUS_CAPTURED;
+                if (!cap) {
+                    orbit::Roots<float> Rt;
+                    Rt.u1 = G.u1[lane];
+                    Rt.u2 = G.u2[lane];
+                    Rt.u3 = G.u3[lane];
+                    const float phi = G.phi0[lane] + oe.x * nm.y_scale;
+                    float sp, cp;
+                    sincos_rr(phi, &sp, &cp);
+                    const float ue = nm.ue;
+                    const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
+                    const V3<float> e2{G.e2x[lane], G.e2y[lane], G.e2z[lane]};
+                    const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
+                    const V3<float> xt{-sp * e1.x + cp * e2.x, -sp * e1.y + cp * e2.y, -sp * e1.z + cp * e2.z};
+                    const float re = 1.0f / ue;
+                    const V3<float> xe{xr.x * re, xr.y * re, xr.z * re};
+                    // velocity at the exit: along dx/dphi = sqrt(P)/u^2 xr + xt/u, with |v|^2 from the energy
+                    // integral of x'' = -3 h^2 x / r^5: |v|^2 = |v0|^2 - 2 h^2 / rc^3 + 2 h^2 u^3
+                    const float h2 = G.h2[lane];
+                    const float sP = orbit::dudphi<float>(ue, Rt);
+                    V3<float> T{sP * re * re * xr.x + re * xt.x, sP * re * re * xr.y + re * xt.y,
+                                sP * re * re * xr.z + re * xt.z};
+                    const float vmag = sqrtf(fmaxf(1.0f - h2 * w.two_over_r3 + 2.0f * h2 * ue * ue * ue, 1e-12f));
+                    const float Ti = vmag * rsqrtf(dot3(T, T));
+                    T = {T.x * Ti, T.y * Ti, T.z * Ti};
+                    d = far_field_dir(xe, T, h2);
+                    min_r = 1.0f / Rt.u2;
+                    status = BHR_STATUS_ESCAPED;
+                }
                 // crossings inside [disk_inner, disk_outer], in march order
                 float cr[3] = {0.f, 0.f, 0.f}, cph[3] = {0.f, 0.f, 0.f};
                 int nrec = 0;
@@ -1070,11 +1164,10 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                     }
                 }
                 const uint32_t nplane = (info >> 3) & 0xffu;
-                const uint32_t w0 = uint32_t(BHR_STATUS_ESCAPED) | (uint32_t(nrec) << 8) |
-                                    (uint32_t(BHR_FLAG_SURROGATE) << 16) | (nplane << 24);
+                const uint32_t w0 = status | (uint32_t(nrec) << 8) | (uint32_t(BHR_FLAG_SURROGATE) << 16) | (nplane << 24);
                 float4* p = reinterpret_cast<float4*>(w.out + ray);
                 p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
-                p[1] = make_float4(d.z, 1.0f / Rt.u2, 0.f, 0.f);
+                p[1] = make_float4(d.z, min_r, 0.f, 0.f);
                 p[2] = make_float4(G.baxis[lane], G.b[lane], cr[0], cr[1]);
                 p[3] = make_float4(cr[2], cph[0], cph[1], cph[2]);
             }

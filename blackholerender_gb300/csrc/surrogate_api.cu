@@ -408,13 +408,15 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
-        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3, st);
+        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 2, st);
     }
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     // 2) the integrator on the fallback rays: one launch for all views when they share a rule
+    // the fallback rays are few and the near-critical ones long: claims of 32 spread them over
+    // as many warps as possible, so the launch ends with its slowest ray, not a warp's queue
     bhr::LaunchCfg cfg{};
     cfg.block = 512;
-    cfg.chunk = 64;
+    cfg.chunk = 32;
     cfg.refill = 8;
     if (e == cudaSuccess && one_rule && nviews <= bhr::kMaxViews) {
         static thread_local bhr::ViewBatch b;

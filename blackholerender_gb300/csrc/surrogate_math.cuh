@@ -34,6 +34,7 @@ template <> struct FM<double> {
     static __host__ __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
     static __host__ __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __host__ __device__ __forceinline__ double div_sqrt(double a, double b) { return a / ::sqrt(b); }
+    static __host__ __device__ __forceinline__ double cbrt(double x) { return ::cbrt(x); }
 };
 template <> struct FM<float> {
     static __host__ __device__ __forceinline__ float sqrt(float x) {
@@ -55,6 +56,7 @@ template <> struct FM<float> {
 #endif
     }
     static __host__ __device__ __forceinline__ float div(float a, float b) { return a * rcp(b); }
+    static __host__ __device__ __forceinline__ float cbrt(float x) { return ::cbrtf(x); }
     static __host__ __device__ __forceinline__ float div_sqrt(float a, float b) {
 #ifdef __CUDA_ARCH__
         float y;
@@ -199,6 +201,47 @@ __host__ __device__ __forceinline__ T invert_sweep(T target, const Roots<T>& R) 
         s = s < T(0) ? T(0) : (s > smax ? smax : s);
     }
     return R.u2 - s * s;
+}
+
+// ---- captured orbits (b < sqrt(27)): P(u) = 2 (u - u1)((u - p)^2 + q^2) has one real root
+// u1 < 0 and u rises from the camera to the horizon without turning. With A^2 = (p - u1)^2 + q^2,
+// w = u - u1 and cos(theta) = (A - w) / (A + w), the substitution of Byrd & Friedman (1971, 239.00)
+// gives int du / sqrt(P) = F(theta, k) / sqrt(2 A), k^2 = (A + p - u1) / (2 A), the incomplete
+// elliptic integral of the first kind F(theta, k) = sin(theta) R_F(cos^2, 1 - k^2 sin^2, 1)
+// for theta <= pi/2 and 2 K(k) - F(pi - theta, k) beyond.
+template <class T> struct CapOrbit {
+    T u1, A, k2, K;  // real root, A, k^2, K(k) = R_F(0, 1 - k^2, 1)
+    T c;             // 1 / b^2
+};
+
+template <class T, int N>
+__host__ __device__ __forceinline__ CapOrbit<T> cap_orbit(T beta) {
+    CapOrbit<T> o;
+    const T ob = T(1) + beta;
+    o.c = FM<T>::rcp(T(27) * ob * ob);
+    // the real root of 2u^3 - u^2 + c: Newton from -cbrt(c/2), where the cubic is -u^2 < 0; the
+    // cubic is increasing and concave for u < 0, so the iterates rise monotonically to the root
+    T u = -FM<T>::cbrt(T(0.5) * o.c);
+#pragma unroll 1
+    for (int k = 0; k < 6; ++k) u -= FM<T>::div(T(2) * u * u * u - u * u + o.c, T(6) * u * u - T(2) * u);
+    o.u1 = u;
+    const T p = T(0.5) * (T(0.5) - u);               // the roots sum to 1/2
+    const T A2 = -FM<T>::div(o.c, T(2) * u) - T(2) * p * u + u * u;  // (p - u1)^2 + q^2, p^2 + q^2 = -c / (2 u1)
+    o.A = tsqrt<T>(A2);
+    o.k2 = FM<T>::div(o.A + p - u, T(2) * o.A);
+    o.K = rf<T, N>(T(0), T(1) - o.k2, T(1));
+    return o;
+}
+
+// F(theta(u), k) of the captured orbit.
+template <class T, int N>
+__host__ __device__ __forceinline__ T cap_F(T u, const CapOrbit<T>& o) {
+    const T w = u - o.u1;
+    const T apw = o.A + w;
+    const T cth = FM<T>::div(o.A - w, apw);
+    const T sth = T(2) * tsqrt<T>(o.A * w) * FM<T>::rcp(apw);
+    const T f0 = sth * rf<T, N>(cth * cth, T(1) - o.k2 * sth * sth, T(1));
+    return cth < T(0) ? T(2) * o.K - f0 : f0;
 }
 
 // Monotone transform of b / sqrt(27): t = sign(beta) ln(1 + |beta| / eps).
