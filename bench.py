@@ -244,10 +244,10 @@ def run_gpu(args):
     trained_here = None
     if DEFAULT_CHECKPOINT.exists() and not args.retrain:
         sur.load(DEFAULT_CHECKPOINT)
-    else:  # train on this GPU with the library's own kernels (about 20 s)
+    else:  # train on this GPU with the library's own kernels (about 30 s)
         t0 = time.perf_counter()
         sur.generate(10_000_000, per_orbit=4, seed=7920)
-        sur.train(100_000, batch=16384, lr_max=2e-3, lr_min=1e-6)
+        sur.train(200_000, batch=16384, lr_max=2e-3, lr_min=1e-6)
         trained_here = time.perf_counter() - t0
     outs = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)

@@ -464,8 +464,9 @@ __global__ void __launch_bounds__(128) k_orbit_data(uint64_t seed, int64_t n_orb
         const bool in_band = fabs(beta) < 0.5 * double(nrm.band) / kSqrt27d;
         if (status == 1 && turns && next == nt && !in_band) {
             for (int k = 0; k < nt; ++k) {
-                const double I = bhr::orbit::sweep_to_turn<double, bhr::orbit::kBaseDup>(uk[k], R);
-                const double Icb = bhr::orbit::sweep_to_turn<double, bhr::orbit::kBaseDup>(uc, R);
+                const double bl = bhr::orbit::base_blend<double>(beta);
+                const double I = bhr::orbit::base_sweep<double>(uk[k], R, bl);
+                const double Icb = bhr::orbit::base_sweep<double>(uc, R, bl);
                 const double base_phi = sig[k] < 0.0 ? Icb - I : Icb + I;
                 X[base + k] = TrainSample{x1, x2, float(sig[k]), float((phis[k] - base_phi) / nrm.y_scale)};
                 lab[base + k] = 0;
@@ -970,15 +971,16 @@ __global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_
                 const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
                 sur = sur && uc < Rt.u2 * 0.9999f;
                 // closed-form baseline at the camera and at the exit
-                Ic = orbit::sweep_to_turn<float, orbit::kBaseDup>(uc, Rt);
-                phi0 = Ic + orbit::sweep_to_turn<float, orbit::kBaseDup>(nm.ue, Rt);
+                const float bl = orbit::base_blend<float>(beta);
+                Ic = orbit::base_sweep<float>(uc, Rt, bl);
+                phi0 = Ic + orbit::base_sweep<float>(nm.ue, Rt, bl);
                 qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
                 if (sur && thin) {
                     // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
                     // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
                     // where the orbit stays outside them)
-                    Ilo = orbit::sweep_to_turn<float, orbit::kBaseDup>(fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt);
-                    Ihi = orbit::sweep_to_turn<float, orbit::kBaseDup>(fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt);
+                    Ilo = orbit::base_sweep<float>(fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt, bl);
+                    Ihi = orbit::base_sweep<float>(fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt, bl);
                 }
                 s0 = Rt.u1, s1 = Rt.u2, s2 = Rt.u3, s3 = Rt.d32;
             } else {
@@ -1054,7 +1056,9 @@ __global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_
                 Rt.u3 = G.u3[own];
                 Rt.d32 = G.d32[own];
                 const bool leg = (kl & 16u) != 0;
-                u = orbit::invert_sweep<float, orbit::kBaseDup, 4>(leg ? phk - Ic : Ic - phk, Rt);
+                // the blend weight from the ray's roots: beta from u2 would cost a cubic; b is staged
+                const float bl = orbit::base_blend<float>(G.b[own] * (1.0f / kSqrt27f) - 1.0f);
+                u = orbit::invert_sweep<float, 4>(leg ? phk - Ic : Ic - phk, Rt, bl);
                 sg = leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f)) : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
             } else {
                 u = cap_invert(G.u1[own], G.u2[own], G.u3[own], G.d32[own], G.b[own], Ic, phk, uc, R.capture_r,

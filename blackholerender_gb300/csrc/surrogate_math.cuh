@@ -9,7 +9,8 @@
 //     I(a) = sqrt(2) sqrt(u2 - a) R_F((a - u1)(u3 - u2), (u2 - u1)(u3 - u2), (u3 - a)(u2 - u1))
 // (Carlson's symmetric elliptic integral; B. C. Carlson, Numer. Algorithms 10 (1995), the
 // duplication theorem and its Taylor series). The surrogate evaluates R_F with kBaseDup
-// duplication steps only: that cheap baseline is what the network corrects.
+// duplication steps only (one more near the photon sphere, base_sweep): that cheap baseline is
+// what the network corrects.
 //
 // Position along an ingoing-then-outgoing orbit is the signed coordinate
 //     sigma = -sqrt((u2 - u) / (u2 - uc))   ingoing leg  (camera -1 .. turning point 0)
@@ -153,6 +154,26 @@ __host__ __device__ __forceinline__ T sweep_to_turn(T a, const Roots<T>& R) {
     return T(1.4142135623730951) * tsqrt<T>(da > T(0) ? da : T(0)) * rf<T, N>(X, Y, Z);
 }
 
+// The baseline the network corrects. With one duplication step the closed form's error grows
+// towards the photon sphere (to ~0.07 rad), beyond what a BF16 network resolves to 1e-4 rad;
+// there a second step (error ~4^-6 of the first) is blended in: weight 1 for beta < kBlendLo,
+// 0 for beta > kBlendHi, smoothstep between, so the residual the network learns stays smooth.
+constexpr double kBlendLo = 0.002, kBlendHi = 0.02;
+
+template <class T>
+__host__ __device__ __forceinline__ T base_blend(T beta) {
+    T x = (T(kBlendHi) - beta) * T(1.0 / (kBlendHi - kBlendLo));
+    x = x < T(0) ? T(0) : (x > T(1) ? T(1) : x);
+    return x * x * (T(3) - T(2) * x);
+}
+
+template <class T>
+__host__ __device__ __forceinline__ T base_sweep(T a, const Roots<T>& R, T blend) {
+    const T I1 = sweep_to_turn<T, kBaseDup>(a, R);
+    if (!(blend > T(0))) return I1;
+    return I1 + blend * (sweep_to_turn<T, kBaseDup + 1>(a, R) - I1);
+}
+
 // u at orbit coordinate sigma (see the file comment).
 template <class T>
 __host__ __device__ __forceinline__ T u_of_sigma(T sigma, T uc, const Roots<T>& R) {
@@ -181,21 +202,21 @@ __host__ __device__ __forceinline__ T dudphi(T u, const Roots<T>& R) {
     return tsqrt<T>(p > T(0) ? p : T(0));
 }
 
-// Solves I(u) = target for u in [0, u2] on the baseline, by Newton in s = sqrt(u2 - u), where
-// dI/ds = 2 / sqrt(2 (u - u1)(u3 - u)) is smooth through the turning point.
-template <class T, int N, int kIters>
-__host__ __device__ __forceinline__ T invert_sweep(T target, const Roots<T>& R) {
+// Solves I(u) = target for u in [0, u2] on the baseline (base_sweep), by Newton in
+// s = sqrt(u2 - u), where dI/ds = 2 / sqrt(2 (u - u1)(u3 - u)) is smooth through the turning point.
+template <class T, int kIters>
+__host__ __device__ __forceinline__ T invert_sweep(T target, const Roots<T>& R, T blend) {
     // I(s) ~ s * sqrt(2) R_F at the turning point for the first guess
     const T X0 = (R.u2 - R.u1) * R.d32;
     const T Z0 = R.d32 * (R.u2 - R.u1);
-    const T slope0 = T(1.4142135623730951) * rf<T, N>(X0, X0, Z0);
+    const T slope0 = T(1.4142135623730951) * rf<T, kBaseDup>(X0, X0, Z0);
     const T smax = tsqrt<T>(R.u2);
     T s = FM<T>::div(target, slope0);
     s = s < T(0) ? T(0) : (s > smax ? smax : s);
 #pragma unroll 1
     for (int k = 0; k < kIters; ++k) {
         const T u = R.u2 - s * s;
-        const T f = sweep_to_turn<T, N>(u, R) - target;
+        const T f = base_sweep<T>(u, R, blend) - target;
         // dI/ds = 2 / sqrt(2 (u - u1)(u3 - u)): the step is f / (dI/ds)
         s -= f * T(0.5) * tsqrt<T>(T(2) * (u - R.u1) * (R.u3 - u));
         s = s < T(0) ? T(0) : (s > smax ? smax : s);
@@ -225,7 +246,7 @@ __host__ __device__ __forceinline__ CapOrbit<T> cap_orbit(T beta) {
 #pragma unroll 1
     for (int k = 0; k < 6; ++k) u -= FM<T>::div(T(2) * u * u * u - u * u + o.c, T(6) * u * u - T(2) * u);
     o.u1 = u;
-    const T p = T(0.5) * (T(0.5) - u);               // the roots sum to 1/2
+    const T p = T(0.5) * (T(0.5) - u);                               // the roots sum to 1/2
     const T A2 = -FM<T>::div(o.c, T(2) * u) - T(2) * p * u + u * u;  // (p - u1)^2 + q^2, p^2 + q^2 = -c / (2 u1)
     o.A = tsqrt<T>(A2);
     o.k2 = FM<T>::div(o.A + p - u, T(2) * o.A);

@@ -19,7 +19,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--orbits", type=float, default=1e7)
     ap.add_argument("--per-orbit", type=int, default=4)
-    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--steps", type=int, default=200000)
     ap.add_argument("--batch", type=int, default=16384)
     ap.add_argument("--lr-max", type=float, default=2e-3)
     ap.add_argument("--lr-min", type=float, default=1e-6)

@@ -77,6 +77,24 @@ def sweep_to_turn(a, beta, ndup=None):
     return np.sqrt(2.0) * np.sqrt(np.maximum(u2 - a, 0.0)) * rf(X, Y, Z, ndup)
 
 
+BLEND_LO, BLEND_HI = 0.002, 0.02
+
+
+def base_blend(beta):
+    """Weight of the two-step closed form in the surrogate's baseline (surrogate_math.cuh
+    base_blend): 1 below beta = 0.002, 0 above 0.02, smoothstep between."""
+    x = np.clip((BLEND_HI - np.asarray(beta, dtype=np.float64)) / (BLEND_HI - BLEND_LO), 0.0, 1.0)
+    return x * x * (3.0 - 2.0 * x)
+
+
+def base_sweep(a, beta):
+    """The baseline the network corrects: I(a) with one duplication step, blended with two steps
+    near the photon sphere."""
+    w = base_blend(beta)
+    i1 = sweep_to_turn(a, beta, ndup=1)
+    return i1 + w * (sweep_to_turn(a, beta, ndup=2) - i1)
+
+
 def phi_of_u(u, uc, beta, leg, ndup=None):
     """Polar angle from the camera (u = uc, ingoing) to u on leg 0 (ingoing) or 1 (outgoing)."""
     Ic = sweep_to_turn(uc, beta, ndup)
@@ -88,3 +106,33 @@ def b_transform(b, eps=1e-3):
     """Monotone transform of b / sqrt(27): t = sign(beta) ln(1 + |beta| / eps)."""
     beta = np.asarray(b, dtype=np.float64) / SQRT27 - 1.0
     return np.sign(beta) * np.log1p(np.abs(beta) / eps)
+
+
+def cap_orbit(beta):
+    """Captured orbit (b < sqrt(27), beta < 0): the real root u1 < 0 of 2u^3 - u^2 + 1/b^2, A with
+    A^2 = (p - u1)^2 + q^2 for the complex pair p +- iq, k^2 = (A + p - u1) / (2A), and K(k).
+    Restates orbit::cap_orbit of blackholerender_gb300/csrc/surrogate_math.cuh in FP64."""
+    beta = float(beta)
+    c = 1.0 / (27.0 * (1.0 + beta) ** 2)
+    u = -np.cbrt(c / 2.0)
+    for _ in range(60):
+        u -= (2 * u ** 3 - u ** 2 + c) / (6 * u ** 2 - 2 * u)
+    p = 0.5 * (0.5 - u)
+    A = np.sqrt(-c / (2 * u) - 2 * p * u + u * u)
+    k2 = (A + p - u) / (2 * A)
+    return u, A, k2, float(rf(0.0, 1.0 - k2, 1.0)), c
+
+
+def cap_angle(u, uc, beta):
+    """Polar angle swept by a captured orbit from u = uc (camera) to u: F(theta(u), k) - F(theta(uc), k),
+    divided by sqrt(2A), with cos(theta) = (A - w) / (A + w), w = u - u1 (Byrd & Friedman 239.00)."""
+    u1, A, k2, K, _ = cap_orbit(beta)
+
+    def F(x):
+        w = np.asarray(x, dtype=np.float64) - u1
+        ct = (A - w) / (A + w)
+        st = 2.0 * np.sqrt(A * w) / (A + w)
+        f0 = st * rf(ct * ct, 1.0 - k2 * st * st, np.ones_like(ct))
+        return np.where(ct < 0.0, 2.0 * K - f0, f0)
+
+    return (F(u) - F(uc)) / np.sqrt(2.0 * A)

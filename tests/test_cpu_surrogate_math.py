@@ -88,3 +88,25 @@ def test_committed_checkpoint_reads_on_the_host():
     q = np.stack([rng.uniform(-1, 1, 256), rng.uniform(0.2, 1.0, 256), rng.uniform(-1, 1, 256)], axis=1)
     out, _ = mlp_ref.forward(ck["params"].astype(np.float64), q)
     assert np.all(np.isfinite(out)) and np.max(np.abs(out[:, 0])) * nm["y_scale"] < 0.2
+
+
+@pytest.mark.parametrize("beta", [-0.9, -0.3, -0.05, -2e-3, -4e-4])
+def test_captured_orbit_angle_equals_quadrature(beta):
+    integ = pytest.importorskip("scipy.integrate")
+    u1, A, k2, K, c = om.cap_orbit(beta)
+    assert abs(2 * u1 ** 3 - u1 ** 2 + c) < 1e-15 and u1 < 0
+    uc = 1.0 / 30.0
+    for u in (0.05, 0.17, 0.3, 1.0 / 2.0001):
+        val, _ = integ.quad(lambda t: 1.0 / np.sqrt(2 * t ** 3 - t ** 2 + c), uc, u, epsabs=1e-13, epsrel=1e-12,
+                            limit=500)
+        assert abs(float(om.cap_angle(u, uc, beta)) - val) < 1e-10 * max(1.0, val), (u, val)
+
+
+def test_blended_baseline_is_closer_near_the_photon_sphere():
+    """Near b = sqrt(27) the one-step closed form misses by up to ~1e-1 rad; the blended baseline
+    (two steps there) stays within ~1e-4 of the exact integral, and equals one step far away."""
+    for beta, tol in ((5e-4, 2e-4), (2e-3, 2e-4), (0.1, 2e-2), (1.0, 5e-3)):
+        exact = float(om.sweep_to_turn(0.0, beta))
+        assert abs(float(om.base_sweep(0.0, beta)) - exact) < tol, beta
+    assert om.base_blend(0.05) == 0.0 and om.base_blend(1e-3) == 1.0
+    assert abs(float(om.sweep_to_turn(0.0, 5e-4, ndup=1)) - float(om.sweep_to_turn(0.0, 5e-4))) > 1e-2

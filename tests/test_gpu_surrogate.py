@@ -56,7 +56,8 @@ def test_training_data_matches_exact_orbits():
     u = np.where(sig < 0, u2 - sig ** 2 * (u2 - uc), u2 - sig ** 2 * u2)
     leg = (sig > 0).astype(int)
     exact = orbit_math.phi_of_u(u, uc, beta, leg, ndup=None)
-    base = orbit_math.phi_of_u(u, uc, beta, leg, ndup=1)
+    ic_b, iu_b = orbit_math.base_sweep(uc, beta), orbit_math.base_sweep(u, beta)  # the blended baseline
+    base = np.where(leg == 0, ic_b - iu_b, ic_b + iu_b)
     y_exact = (exact - base) / s.cfg.y_scale
     err = np.abs(X[m, 3] - y_exact) * s.cfg.y_scale
     far = np.abs(beta) > 4e-4   # outside the fallback band

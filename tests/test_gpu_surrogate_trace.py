@@ -110,6 +110,46 @@ def test_surrogate_and_plain_vs_converged_orbit(surrogate):
     assert a_s.max() < DIR_MAX_RAD, (np.percentile(a_s, 99), a_s.max())
 
 
+def test_surrogate_near_the_photon_ring(surrogate):
+    """Rays just outside the fallback band, |b - sqrt(27)| in [2e-3, 5e-2], where the deflection is
+    most sensitive to b and random pixel samples rarely land: every escaped surrogate ray within
+    1e-4 rad of the converged FP64 orbit; against the same-rule FP64 oracle within 1e-4 rad plus
+    that oracle's own distance from the converged orbit (its step-size error near the ring)."""
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG)[:8]
+    outs = surrogate.trace(views)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(21)
+    e_conv, e_rule, e_rule_conv, dist = [], [], [], []
+    for v, o in zip(views, outs):
+        g = hits_numpy(o.cpu())
+        d = np.abs(g["b"].astype(np.float64) - 27 ** 0.5)
+        cand = np.nonzero(((g["flags"] & FLAG_SURROGATE) != 0) & (g["status"] == 1) & (d < 5e-2))[0]
+        idx = rng.choice(cand, min(len(cand), 800), replace=False)
+        fine = v.copy()
+        fine.step_scale = 0.002
+        fine.ds_floor = 1e-4
+        fine.max_steps = 400000
+        fine.disk_mode = 0
+        conv = O.trace_pixels(fine, idx, fp64=True)
+        rule = O.trace_pixels(v, idx, fp64=True)
+        ok = (conv["status"] == 1) & (rule["status"] == 1)
+        gg = g[idx][ok]
+        e_conv.append(O.angle(gg["dir"], conv["dir"][ok]))
+        e_rule.append(O.angle(gg["dir"], rule["dir"][ok]))
+        e_rule_conv.append(O.angle(rule["dir"][ok], conv["dir"][ok]))
+        dist.append(np.abs(conv["b"][ok].astype(np.float64) - 27 ** 0.5))
+    e_conv, e_rule, e_rule_conv, dist = (np.concatenate(x) for x in (e_conv, e_rule, e_rule_conv, dist))
+    assert len(e_conv) > 2000 and dist.min() < 3e-3
+    for lo, hi in ((2e-3, 5e-3), (5e-3, 1e-2), (1e-2, 2e-2), (2e-2, 5e-2)):
+        m = (dist >= lo) & (dist < hi)
+        print(f"\n|b - sqrt27| in [{lo}, {hi}): {m.sum()} rays; vs converged max {e_conv[m].max():.2e}; "
+              f"vs same-rule max {e_rule[m].max():.2e} (same-rule vs converged max {e_rule_conv[m].max():.2e})")
+    assert e_conv.max() < DIR_MAX_RAD, e_conv.max()
+    assert np.all(e_rule < DIR_MAX_RAD + e_rule_conv), (e_rule - e_rule_conv).max()
+
+
 def test_network_gain_over_closed_form_baseline(surrogate):
     # held-out orbits from the integrator: polar-angle error at the exit with and without the network
     s = Surrogate(seed=4)
