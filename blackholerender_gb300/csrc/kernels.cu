@@ -289,7 +289,7 @@ __device__ __forceinline__ void note_start(WorkQueue* q) {
 
 // FP64 continuation: band rays from scratch, then promoted FP32 states. One ray per thread
 // with dynamic fetch; FP64 runs at a small fraction of the FP32 rate, so the queues are short.
-template <bool kMulti>
+template <bool kMulti, int kTerm, int kDisk>
 __device__ __forceinline__ void march_fp64(const DevView* views, const Rule& R, const Scratch sc) {
     WorkQueue* q = sc.q;
     const unsigned long long nband = q->band_count;
@@ -338,7 +338,7 @@ __device__ __forceinline__ void march_fp64(const DevView* views, const Rule& R, 
         }
         const DevView& w = views[vs];
         bhr_hit* rec = w.out + ray;
-        while (!march_step<double, -1, -1, false>(R, w.max_steps, (double)w.disk_step, s, rec)) {
+        while (!march_step<double, kTerm, kDisk, false>(R, w.max_steps, (double)w.disk_step, s, rec)) {
         }
         steps_sum += s.steps - base_steps;
         const bool bad = nonfinite_state(s);
@@ -427,14 +427,16 @@ __global__ void __launch_bounds__(512) k_march_multi_list(const __grid_constant_
                                                 Pool{s_pool[wid], s_pool_view[wid]}, list, 0);
 }
 
+template <int kTerm, int kDisk>
 __global__ void __launch_bounds__(128) k_march_fp64_one(const __grid_constant__ DevView view,
                                                         const __grid_constant__ Rule rule, const Scratch sc) {
-    march_fp64<false>(&view, rule, sc);
+    march_fp64<false, kTerm, kDisk>(&view, rule, sc);
 }
 
+template <int kTerm, int kDisk>
 __global__ void __launch_bounds__(128) k_march_fp64_multi(const __grid_constant__ ViewBatch batch,
                                                           const Scratch sc) {
-    march_fp64<true>(batch.views, batch.rule, sc);
+    march_fp64<true, kTerm, kDisk>(batch.views, batch.rule, sc);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -501,12 +503,22 @@ cudaError_t launch_march_multi(const ViewBatch& b, const Scratch& s, bool mixed,
 }
 
 cudaError_t launch_march_fp64_one(const DevView& v, const Rule& r, const Scratch& s, int grid, cudaStream_t st) {
-    k_march_fp64_one<<<grid, 128, 0, st>>>(v, r, s);
+    switch (rule_variant(r)) {
+        case kVariantConfigThin: k_march_fp64_one<BHR_TERM_CONFIG, BHR_DISK_THIN><<<grid, 128, 0, st>>>(v, r, s); break;
+        case kVariantShaderThin: k_march_fp64_one<BHR_TERM_SHADER, BHR_DISK_THIN><<<grid, 128, 0, st>>>(v, r, s); break;
+        case kVariantCpuNone: k_march_fp64_one<BHR_TERM_CPU, BHR_DISK_NONE><<<grid, 128, 0, st>>>(v, r, s); break;
+        default: k_march_fp64_one<-1, -1><<<grid, 128, 0, st>>>(v, r, s); break;
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_march_fp64_multi(const ViewBatch& b, const Scratch& s, int grid, cudaStream_t st) {
-    k_march_fp64_multi<<<grid, 128, 0, st>>>(b, s);
+    switch (rule_variant(b.rule)) {
+        case kVariantConfigThin: k_march_fp64_multi<BHR_TERM_CONFIG, BHR_DISK_THIN><<<grid, 128, 0, st>>>(b, s); break;
+        case kVariantShaderThin: k_march_fp64_multi<BHR_TERM_SHADER, BHR_DISK_THIN><<<grid, 128, 0, st>>>(b, s); break;
+        case kVariantCpuNone: k_march_fp64_multi<BHR_TERM_CPU, BHR_DISK_NONE><<<grid, 128, 0, st>>>(b, s); break;
+        default: k_march_fp64_multi<-1, -1><<<grid, 128, 0, st>>>(b, s); break;
+    }
     return cudaGetLastError();
 }
 
