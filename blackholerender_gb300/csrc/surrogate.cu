@@ -201,15 +201,22 @@ __device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][
 // products is the halved accumulation), and silu(z) = z/2 (1 + tanh(z/2)) = fma(h, tanh h, h):
 // the same bits as the training kernel's silu(z), one multiply fewer per activation.
 
-__device__ void load_net_half(SmemNet& N, const float* __restrict__ P) {
+// kFoldX1: every query of the launch has the same first input x1 (one view: x1 = scaled log r_cam),
+// so its term is folded into the first-layer bias and w1[f] holds {w_x2, w_sigma, w_x1 x1 + b, 0}/2.
+template <bool kFoldX1>
+__device__ void load_net_half(SmemNet& N, const float* __restrict__ P, float x1 = 0.f) {
     for (int k = threadIdx.x; k < kH * kH; k += blockDim.x) {
         const int o = k / kH, i = k % kH;
         N.w2[o * kLd + i] = __float2bfloat16_rn(0.5f * P[kW2 + k]);
         N.w3[o * kLd + i] = __float2bfloat16_rn(0.5f * P[kW3 + k]);
     }
     for (int f = threadIdx.x; f < kH; f += blockDim.x) {
-        N.w1[f] = make_float4(0.5f * P[kW1 + 3 * f], 0.5f * P[kW1 + 3 * f + 1], 0.5f * P[kW1 + 3 * f + 2],
-                              0.5f * P[kB1 + f]);
+        if (kFoldX1)
+            N.w1[f] = make_float4(0.5f * P[kW1 + 3 * f + 1], 0.5f * P[kW1 + 3 * f + 2],
+                                  0.5f * fmaf(P[kW1 + 3 * f], x1, P[kB1 + f]), 0.f);
+        else
+            N.w1[f] = make_float4(0.5f * P[kW1 + 3 * f], 0.5f * P[kW1 + 3 * f + 1], 0.5f * P[kW1 + 3 * f + 2],
+                                  0.5f * P[kB1 + f]);
         N.b2[f] = 0.5f * P[kB2 + f];
         N.b3[f] = 0.5f * P[kB3 + f];
         N.w4[f] = P[kW4 + f];
@@ -250,6 +257,7 @@ __device__ __forceinline__ void mma_layer_ldsm(const __nv_bfloat16* W, const flo
 // Forward pass of the queries q[0 .. 16 ntiles) in shared memory (q[r] = {x1, x2, sigma, -}),
 // one 16-row tile at a time; all 32 lanes. Rows past the caller's count compute garbage that
 // nobody reads.
+template <bool kFoldX1>
 __device__ void mlp_eval_tiles(const SmemNet& N, const float4* q, float2* out, int ntiles) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll 1
@@ -265,8 +273,13 @@ __device__ void mlp_eval_tiles(const SmemNet& N, const float4* q, float2* out, i
             for (int k = 0; k < 4; ++k) {
                 const int f = 16 * i + 2 * t + (k & 1) + ((k & 2) ? 8 : 0);
                 const float4 w = N.w1[f];
-                ha[k] = silu_h(fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w))));
-                hb[k] = silu_h(fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w))));
+                if (kFoldX1) {
+                    ha[k] = silu_h(fmaf(w.x, xa.y, fmaf(w.y, xa.z, w.z)));
+                    hb[k] = silu_h(fmaf(w.x, xb.y, fmaf(w.y, xb.z, w.z)));
+                } else {
+                    ha[k] = silu_h(fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w))));
+                    hb[k] = silu_h(fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w))));
+                }
             }
             A[i][0] = pack_bf16(ha[0], ha[1]);
             A[i][1] = pack_bf16(hb[0], hb[1]);
@@ -748,14 +761,14 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ P, 
     __shared__ __align__(16) SmemNet N;
     __shared__ float4 qs[4][32];
     __shared__ float2 os[4][32];
-    load_net_half(N, P);
+    load_net_half<false>(N, P);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int base = (blockIdx.x * 4 + warp) * 32; base < n; base += gridDim.x * 4 * 32) {
         const int k = base + lane;
         qs[warp][lane] = k < n ? q[k] : make_float4(0.f, 0.f, 0.f, 0.f);
         __syncwarp();
-        mlp_eval_tiles(N, qs[warp], os[warp], 2);
+        mlp_eval_tiles<false>(N, qs[warp], os[warp], 2);
         if (k < n) out[k] = os[warp][lane];
         __syncwarp();
     }
@@ -909,7 +922,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_
                                                                 int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
-    load_net_half(S.N, P);
+    load_net_half<true>(S.N, P, sv.x1);
     __syncthreads();
     const DevView& w = sv.view;
     const Rule& R = sv.rule;
@@ -975,13 +988,6 @@ __global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_
                 Ic = orbit::base_sweep<float>(uc, Rt, bl);
                 phi0 = Ic + orbit::base_sweep<float>(nm.ue, Rt, bl);
                 qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
-                if (sur && thin) {
-                    // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
-                    // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
-                    // where the orbit stays outside them)
-                    Ilo = orbit::base_sweep<float>(fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt, bl);
-                    Ihi = orbit::base_sweep<float>(fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt, bl);
-                }
                 s0 = Rt.u1, s1 = Rt.u2, s2 = Rt.u3, s3 = Rt.d32;
             } else {
                 const CapStage cs = cap_stage(beta, uc, R.capture_r, R.disk_inner, R.disk_outer, sur && thin);
@@ -1001,6 +1007,16 @@ __global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_
                 for (int k = 0; k < 16; ++k) {
                     if (phin + float(k) * kPi >= phi0) break;
                     ++nplane;
+                }
+                if (!cap && thin && nplane > 0) {
+                    // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
+                    // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
+                    // where the orbit stays outside them)
+                    orbit::Roots<float> Rt;
+                    Rt.u1 = s0, Rt.u2 = s1, Rt.u3 = s2, Rt.d32 = s3;
+                    const float bl = orbit::base_blend<float>(beta);
+                    Ilo = orbit::base_sweep<float>(fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt, bl);
+                    Ihi = orbit::base_sweep<float>(fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt, bl);
                 }
 #pragma unroll 1
                 for (int k = 0; k < nplane && ncand < kMaxCand; ++k) {
@@ -1070,7 +1086,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_
         __syncwarp();
         // ---- phase 3: the network on all queries of the warp
         const int ntiles = (32 + total + 15) >> 4;
-        mlp_eval_tiles(S.N, qb, ob, ntiles);
+        mlp_eval_tiles<true>(S.N, qb, ob, ntiles);
         n_rows += lane == 0 ? uint32_t(16 * ntiles) : 0u;
         // ---- phase 4: corrected crossings (per candidate), then records (per ray)
 #pragma unroll 1

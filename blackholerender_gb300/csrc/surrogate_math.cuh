@@ -94,9 +94,13 @@ __host__ __device__ __forceinline__ Roots<T> roots(T beta) {
         //   u2 = s (sqrt(3) c + s) / 3,  u3 = (3 c^2 - s^2) / 6 ... written without cancellation,
         //   u3 - u2 = (sqrt(3) (c^2 - s^2) - 2 s c) / 3 / sqrt(3) * sqrt(3)   (sin(pi/3 - 2a) / sqrt(3))
         const T y = FM<T>::rcp(T(1) + beta);
-        T sa = y * T(1.0 / 3.0);
+        // first guess from the series of the inverse, s = y/3 + 4 y^3/81 + 16 y^5/729 + ... (within
+        // 5% at beta = 0.1); Newton then reaches FP32 precision in 3 steps and FP64 in 5
+        const T y2 = y * y;
+        T sa = y * (T(1.0 / 3.0) + y2 * (T(4.0 / 81.0) + y2 * T(16.0 / 729.0)));
+        constexpr int kNewton = sizeof(T) == 4 ? 3 : 5;
 #pragma unroll 1
-        for (int k = 0; k < 5; ++k) sa -= FM<T>::div(T(3) * sa - T(4) * sa * sa * sa - y, T(3) - T(12) * sa * sa);
+        for (int k = 0; k < kNewton; ++k) sa -= FM<T>::div(T(3) * sa - T(4) * sa * sa * sa - y, T(3) - T(12) * sa * sa);
         const T ca = tsqrt<T>(T(1) - sa * sa);
         const T r3 = T(1.7320508075688772);
         // u2 = 2/3 sin(a) sin(2pi/3 - a) = 2/3 s (r3/2 c + s/2)
