@@ -159,6 +159,20 @@ class Tracer:
         _abi.check(_abi.lib().bhr_autotune(self._ctx, arr, n, ptrs, precision, reps, ctypes.byref(best)), self._ctx)
         return best
 
+    def lens_table(self, cam_r: float, method: int = METHOD_PLAIN, out=None, stream=None):
+        """bhr_lens_table: the 1024 x 1024 lens table (log r, [angle j][ray i]) as a device tensor."""
+        import torch
+
+        dev = torch.device("cuda", self.device)
+        if out is None:
+            out = torch.empty((_abi.LENS_PHIS, _abi.LENS_RAYS), dtype=torch.float32, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        _abi.check(_abi.lib().bhr_lens_table(self._ctx, ctypes.c_float(cam_r), method,
+                                             ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream)),
+                   self._ctx)
+        return out
+
     def plan(self, views: Sequence[View], outs, precision: int = PREC_FP32, autotune: bool = False) -> "Plan":
         return Plan(self, views, outs, precision, autotune)
 

@@ -44,6 +44,8 @@ METHOD_PLAIN = 0
 METHOD_SURROGATE = 1
 
 SQRT27 = 27.0 ** 0.5
+LENS_RAYS = 1024
+LENS_PHIS = 1024
 
 
 class View(ctypes.Structure):
@@ -165,6 +167,9 @@ SIGNATURES = {
     "bhr_trace_noalloc": (ctypes.c_int, [_VP, _P, _P]),
     "bhr_trace_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
     "bhr_trace_view_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "bhr_lens_table": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int, _P, _P]),
+    "bhr_lens_alpha": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
+    "bhr_shadow_angular_radius": (ctypes.c_double, [ctypes.c_double]),
     "bhr_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),
     "bhr_set_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),
     "bhr_autotune": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int,

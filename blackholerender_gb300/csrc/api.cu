@@ -626,6 +626,32 @@ int bhr_trace_view_times(bhr_ctx* c, double* ms, int nviews) {
 }
 
 // ---------------------------------------------------------------------------------------
+// lens table
+
+int bhr_lens_table(bhr_ctx* c, float cam_r, int method, float* table, void* cuda_stream) {
+    if (!c || !table) return fail(c, BHR_ERR_INVALID_ARG, "bhr_lens_table: NULL argument");
+    if (!(cam_r > 2.01f) || !std::isfinite(cam_r))
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_lens_table: cam_r must be finite and outside r = 2.01");
+    if (method != BHR_METHOD_PLAIN && method != BHR_METHOD_SURROGATE)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_lens_table: unknown method");
+    if (method == BHR_METHOD_SURROGATE && !(cam_r > 3.0f))
+        return fail(c, BHR_ERR_UNSUPPORTED, "bhr_lens_table: the closed form needs a camera outside the photon sphere");
+    if (reinterpret_cast<uintptr_t>(table) % 16 != 0)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_lens_table: table must be 16-byte aligned");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const cudaError_t e =
+        bhr::launch_lens_table(cam_r, method == BHR_METHOD_SURROGATE, table, static_cast<cudaStream_t>(cuda_stream));
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? BHR_OK : cuda_fail(c, e, "bhr_lens_table");
+}
+
+float bhr_lens_alpha(float u, float alpha_crit) { return bhr::lens_alpha_host(u, alpha_crit); }
+
+double bhr_shadow_angular_radius(double r) { return bhr::lens_alpha_crit(r); }
+
+// ---------------------------------------------------------------------------------------
 // launch shapes and the autotuner
 
 int bhr_get_launch_shape(const bhr_ctx* c, bhr_launch_shape* sh) {

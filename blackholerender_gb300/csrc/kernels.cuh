@@ -80,6 +80,11 @@ cudaError_t launch_march_list(const DevView& v, const Rule& r, const Scratch& s,
 // starts at list + views[v].list_off and its length is qv[2v].fb_count.
 cudaError_t launch_march_multi_list(const ViewBatch& b, const Scratch& s, const int* list, const WorkQueue* qv,
                                     const LaunchCfg& c, cudaStream_t st);
+// Lens table of a camera at cam_r (lens.cu): the reference's RK4 construction, or (closed_form)
+// every texel from the closed-form orbit. table: BHR_LENS_PHIS x BHR_LENS_RAYS floats on the device.
+cudaError_t launch_lens_table(float cam_r, int closed_form, float* table, cudaStream_t st);
+double lens_alpha_crit(double r);
+float lens_alpha_host(float u, float ac);
 // Max resident blocks per SM of an FP32 march kernel (occupancy API).
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed);
 

@@ -192,6 +192,45 @@ template <class T> struct RayState {
 
 enum : uint32_t { kStatusShift = 12, kNcrossShift = 8, kPromote = 4 };
 
+// rk4Step (geodesic.glsl:16-23) for x'' = a(x) = k(x) x, k(x) = -3 h2 / r^5, with ri = 1/|x|
+// already known. With h = dt/2 and c_j = h k(x_j) the stages are x2 = x + h v, x3 = x2 + h c1 x1,
+// x4 = x + dt v + dt c2 x2, and the update collapses to
+//   x' = x + (dt v + (dt/3)(c1 x1 + c2 x2 + c3 x3))
+//   v' = v + (1/3)(c1 x1 + 2 c2 x2 + 2 c3 x3 + c4 x4)
+// (algebraically the reference's k-sums; no slope vector is formed, one rounding onto x).
+template <class T>
+__device__ __forceinline__ void rk4_update(V3<T>& xs, V3<T>& vs, T h2, T dt, T ri) {
+    const T hdt = T(0.5) * dt;
+    const T hm = hdt * (T(-3) * h2);
+    const V3<T> x = xs, v = vs;
+    T q2 = ri * ri;
+    const T c1 = hm * ri * (q2 * q2);
+    const V3<T> x2{x.x + hdt * v.x, x.y + hdt * v.y, x.z + hdt * v.z};
+    const V3<T> q1{c1 * x.x, c1 * x.y, c1 * x.z};                      // c1 x1
+    T q = M<T>::rsqrt(dot3(x2, x2));
+    q2 = q * q;
+    const T c2 = hm * q * (q2 * q2);
+    V3<T> P{c2 * x2.x, c2 * x2.y, c2 * x2.z};                          // c2 x2
+    const T g = hdt * c1;
+    const V3<T> x3{x2.x + g * x.x, x2.y + g * x.y, x2.z + g * x.z};
+    q = M<T>::rsqrt(dot3(x3, x3));
+    q2 = q * q;
+    const T c3 = hm * q * (q2 * q2);
+    P = {P.x + c3 * x3.x, P.y + c3 * x3.y, P.z + c3 * x3.z};           // + c3 x3
+    const V3<T> dv{dt * v.x, dt * v.y, dt * v.z};
+    const T e = dt * c2;
+    const V3<T> x4{x2.x + hdt * v.x + e * x2.x, x2.y + hdt * v.y + e * x2.y, x2.z + hdt * v.z + e * x2.z};
+    q = M<T>::rsqrt(dot3(x4, x4));
+    q2 = q * q;
+    const T c4 = hm * q * (q2 * q2);
+    const V3<T> W{q1.x + P.x, q1.y + P.y, q1.z + P.z};
+    const T dt3 = dt * T(1.0 / 3.0);
+    xs = {x.x + (dv.x + dt3 * W.x), x.y + (dv.y + dt3 * W.y), x.z + (dv.z + dt3 * W.z)};
+    const V3<T> U{W.x + P.x + c4 * x4.x, W.y + P.y + c4 * x4.y, W.z + P.z + c4 * x4.z};
+    const T third = T(1.0 / 3.0);
+    vs = {v.x + third * U.x, v.y + third * U.y, v.z + third * U.z};
+}
+
 // Compile-time variant of the loop body: kTerm = BHR_TERM_* or -1 (rule read at run time,
 // with lensing and far mode); kDisk = BHR_DISK_NONE / BHR_DISK_THIN or -1.
 template <int kTerm, int kDisk>
@@ -265,42 +304,7 @@ __device__ __forceinline__ bool march_step(const Rule& R, int max_steps, T disk_
     const T dt = ds * vi;
     const V3<T> x0 = s.x;
     if (lensing) {
-        // rk4Step (geodesic.glsl:16-23) for x'' = a(x) = k(x) x, k(x) = -3 h2 / r^5. With
-        // h = dt/2 and c_j = h k(x_j) the stages are x2 = x + h v, x3 = x2 + h c1 x1,
-        // x4 = x + dt v + dt c2 x2, and the update collapses to
-        //   x' = x + (dt v + (dt/3)(c1 x1 + c2 x2 + c3 x3))
-        //   v' = v + (1/3)(c1 x1 + 2 c2 x2 + 2 c3 x3 + c4 x4)
-        // (algebraically the reference's k-sums; no slope vector is formed).
-        const T hdt = T(0.5) * dt;
-        const T hm = hdt * (T(-3) * s.h2);
-        const V3<T> x = s.x, v = s.v;
-        T q2 = ri * ri;
-        const T c1 = hm * ri * (q2 * q2);
-        const V3<T> x2{x.x + hdt * v.x, x.y + hdt * v.y, x.z + hdt * v.z};
-        const V3<T> q1{c1 * x.x, c1 * x.y, c1 * x.z};                      // c1 x1
-        T q = M<T>::rsqrt(dot3(x2, x2));
-        q2 = q * q;
-        const T c2 = hm * q * (q2 * q2);
-        V3<T> P{c2 * x2.x, c2 * x2.y, c2 * x2.z};                          // c2 x2
-        const T g = hdt * c1;
-        const V3<T> x3{x2.x + g * x.x, x2.y + g * x.y, x2.z + g * x.z};
-        q = M<T>::rsqrt(dot3(x3, x3));
-        q2 = q * q;
-        const T c3 = hm * q * (q2 * q2);
-        P = {P.x + c3 * x3.x, P.y + c3 * x3.y, P.z + c3 * x3.z};           // + c3 x3
-        const V3<T> dv{dt * v.x, dt * v.y, dt * v.z};
-        const T e = dt * c2;
-        const V3<T> x4{x2.x + hdt * v.x + e * x2.x, x2.y + hdt * v.y + e * x2.y, x2.z + hdt * v.z + e * x2.z};
-        q = M<T>::rsqrt(dot3(x4, x4));
-        q2 = q * q;
-        const T c4 = hm * q * (q2 * q2);
-        const V3<T> W{q1.x + P.x, q1.y + P.y, q1.z + P.z};
-        const T dt3 = dt * T(1.0 / 3.0);
-        // one rounding onto x per step: x' = x + (dt v + (dt/3) W)
-        s.x = {x.x + (dv.x + dt3 * W.x), x.y + (dv.y + dt3 * W.y), x.z + (dv.z + dt3 * W.z)};
-        const V3<T> U{W.x + P.x + c4 * x4.x, W.y + P.y + c4 * x4.y, W.z + P.z + c4 * x4.z};
-        const T third = T(1.0 / 3.0);
-        s.v = {v.x + third * U.x, v.y + third * U.y, v.z + third * U.z};
+        rk4_update(s.x, s.v, s.h2, dt, ri);
     } else {
         s.x = {s.x.x + s.v.x * dt, s.x.y + s.v.y * dt, s.x.z + s.v.z * dt};
     }

@@ -278,6 +278,21 @@ int bhr_trace_stats(bhr_ctx* ctx, bhr_stats* stats);
  * launch to the moment the view's last ray finished (synchronises that call's stream). */
 int bhr_trace_view_times(bhr_ctx* ctx, double* ms, int nviews);
 
+/* ---- lens table (the second consumer of the integrator) ------------------------------ */
+/* The star-disruption renderer's lens table (shaders/gas_lens.comp:10-43, gas_lens.glsl:13-21,
+ * built by GasParticleRenderer::buildLensTable, src/GasParticles.cpp:161-171): for a camera at
+ * radius cam_r, a fan of BHR_LENS_RAYS rays in one plane through the hole at local angles
+ * alpha = bhr_lens_alpha((i + 0.5) / BHR_LENS_RAYS, bhr_shadow_angular_radius(cam_r)), and
+ * table[j * BHR_LENS_RAYS + i] = log r of ray i after sweeping j 2 pi / (BHR_LENS_PHIS - 1)
+ * around the hole (log 2 once captured, log 2e5 once escaped). method BHR_METHOD_PLAIN: the
+ * reference's RK4 construction (FP32); BHR_METHOD_SURROGATE: every texel from the closed-form
+ * orbit, in parallel (cam_r > 3, outside the photon sphere). table_dev: device memory, 4 MiB. */
+#define BHR_LENS_RAYS 1024
+#define BHR_LENS_PHIS 1024
+int bhr_lens_table(bhr_ctx* ctx, float cam_r, int method, float* table_dev, void* cuda_stream);
+float bhr_lens_alpha(float u, float alpha_crit);         /* lensAlpha, gas_lens.glsl:13-17 */
+double bhr_shadow_angular_radius(double r);              /* shadowAngularRadius, Geodesic.h:78-82 */
+
 /* ---- launch shapes and the autotuner ------------------------------------------------ */
 /* No counterpart in the reference (its march is one fragment-shader draw whose scheduling the
  * GL driver owns); these choose how the persistent march kernel covers a batch of views. */

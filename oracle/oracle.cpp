@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "march.hpp"
+#include "lens.hpp"
 
 using namespace oracle;
 
@@ -169,6 +170,21 @@ void oracle_initial_velocity(const double cam[3], const double dir[3], double ou
 void oracle_far_field(const double x[3], const double v[3], double h2, double out[3]) {
     const V3<double> r = farFieldDirection(V3<double>{x[0], x[1], x[2]}, V3<double>{v[0], v[1], v[2]}, h2);
     out[0] = r.x, out[1] = r.y, out[2] = r.z;
+}
+
+// The lens table of a camera at cam_r (gas_lens.comp): 1024 x 1024 floats, table[j * 1024 + i],
+// alpha_crit = the shadow's angular radius at cam_r (the reference passes it as a float uniform).
+int oracle_lens_table(float cam_r, float alpha_crit, float* table, int nthreads, int fp64) {
+    if (!table || !(cam_r > 2.0f)) return BHR_ERR_INVALID_ARG;
+    if (fp64)
+        parallel_for(oracle::kLensRays, nthreads, 1, [&](int64_t i) {
+            oracle::lensRay<double>(int(i), double(cam_r), double(alpha_crit), table);
+        });
+    else
+        parallel_for(oracle::kLensRays, nthreads, 1, [&](int64_t i) {
+            oracle::lensRay<float>(int(i), cam_r, alpha_crit, table);
+        });
+    return BHR_OK;
 }
 
 int oracle_hit_size(void) { return static_cast<int>(sizeof(bhr_hit)); }

@@ -42,6 +42,7 @@ def lib():
         L.oracle_march_ray.argtypes = [VP, D, D, ctypes.c_int, ctypes.c_void_p, D]
         L.oracle_cpu_trace.argtypes = [D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, D,
                                        ctypes.POINTER(ctypes.c_int), D]
+        L.oracle_lens_table.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.oracle_rk4_step.argtypes = [D, D, ctypes.c_double, ctypes.c_double]
         L.oracle_initial_velocity.argtypes = [D, D, D]
         L.oracle_far_field.argtypes = [D, D, ctypes.c_double, D]
@@ -80,6 +81,15 @@ def trace_pixels(view: View, idx: np.ndarray, fp64: bool = True, threads: int | 
     out = np.zeros(len(idx), dtype=HIT_DTYPE)
     rc = lib().oracle_trace_pixels(ctypes.byref(view), idx.ctypes.data, len(idx), out.ctypes.data,
                                    threads or nthreads(), int(fp64))
+    assert rc == 0, rc
+    return out
+
+
+def lens_table(cam_r: float, alpha_crit: float, fp64: bool = True, threads: int | None = None) -> np.ndarray:
+    """The reference's lens-table construction (gas_lens.comp) on the CPU: [1024 angles][1024 rays]."""
+    out = np.zeros((1024, 1024), dtype=np.float32)
+    rc = lib().oracle_lens_table(ctypes.c_float(cam_r), ctypes.c_float(alpha_crit), out.ctypes.data,
+                                 threads or nthreads(), int(fp64))
     assert rc == 0, rc
     return out
 
