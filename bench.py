@@ -253,12 +253,20 @@ def run_gpu(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    # both paths as the library's CUDA-graph plans (one graph launch per step); the plain path
+    # with the launch shape its autotuner picks for these views
+    sur.trace_ptrs(views, outs, stream)
+    torch.cuda.synchronize(dev)
+    plan_s = sur.plan(views, outs)
+    plan_p = tr.plan(views, outs, PREC_FP32, autotune=True)
+    plain_shape = plan_p.launch_shape.as_dict()
+
     def step_surrogate():
-        sur.trace_ptrs(views, outs, stream)
+        plan_s.launch(stream)
         return len(views) + 1  # one surrogate kernel per view + one fallback march
 
     def step_plain():
-        tr.trace(views, outs, PREC_FP32, stream=stream)
+        plan_p.launch(stream)
         return 1
 
     for _ in range(max(args.warmup, 0)):
@@ -283,8 +291,8 @@ def run_gpu(args):
     ang = np.concatenate(ang)
     agreement = {"p50": float(np.percentile(ang, 50)), "p99": float(np.percentile(ang, 99)),
                  "max": float(ang.max()), "rays": int(len(ang))}
-    # phase times of one surrogate trace (dominant kernel: the surrogate pass)
-    step_surrogate()
+    # phase times of one (eager) surrogate trace (dominant kernel: the surrogate pass)
+    sur.trace_ptrs(views, outs, stream)
     t_pass, t_fb = sur.trace_times_ms()
 
     def timed(step, k_steps):
@@ -366,9 +374,8 @@ def run_gpu(args):
             "pass_ms": t_pass, "fallback_ms": t_fb,
             "note": "the pass is issue-bound on the CUDA cores (ray setup, closed-form orbit, activations);"
                     " the tensor pipe is not its limit"}
-    steps_plain = None
-    tr.trace(views, outs, PREC_FP32, stream=stream)
-    steps_plain = tr.stats().steps
+    plan_p.launch(stream)
+    steps_plain = plan_p.stats().steps
     plain_flop = steps_plain * F_STEP + rays * F_SETUP
     roof_plain = {"bound": "fp32", "achieved": plain_flop / (plain_ms * 1e-3) / 1e12, "peak": fp32_peak,
                   "unit": "TFLOP/s", "frac": plain_flop / (plain_ms * 1e-3) / 1e12 / fp32_peak,
@@ -391,6 +398,7 @@ def run_gpu(args):
                    "views": len(views), "rays_per_step": rays,
                    "method": "learned surrogate + plain FP32 integrator fallback",
                    "plain_mrays_s": plain_value, "plain_ms_per_step": plain_ms,
+                   "plain_launch_shape": plain_shape, "graph_plans": True,
                    "speedup_vs_plain": value / plain_value,
                    "surrogate_fraction": st["surrogate"] / rays, "fallback_rays": st["fallback"],
                    "capture_flag_disagreements": st["capture_disagree"],
@@ -408,6 +416,8 @@ def run_gpu(args):
         "per_step_ms": per_step,
     }
     print(json.dumps(line), flush=True)
+    plan_s.close()
+    plan_p.close()
     if dist:
         dist.destroy_process_group()
 

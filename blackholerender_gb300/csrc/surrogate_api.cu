@@ -3,9 +3,11 @@
 // the surrogate-plus-fallback trace.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -39,6 +41,7 @@ struct bhr_surrogate {
     unsigned long long last[4] = {0, 0, 0, 0};
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
+    bool last_from_plan = false;  // the last trace was a graph replay (its events do not time)
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // start, surrogate pass done, fallback done
     // bhr_surrogate_trace_host: device staging and two streams
     bhr_hit* staging = nullptr;
@@ -442,12 +445,93 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
     s->last_stream = st;
     s->last_nviews = nviews;
     s->have_last = true;
+    s->last_from_plan = false;
+    return BHR_OK;
+}
+
+// A fixed batch of views traced by one CUDA graph of bhr_surrogate_trace (bhr_surrogate_plan_*).
+struct bhr_surrogate_plan {
+    bhr_surrogate* s = nullptr;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int nviews = 0;
+};
+
+int bhr_surrogate_plan_destroy(bhr_surrogate_plan* p) {
+    if (!p) return BHR_OK;
+    DevGuard dg(p->s->device);
+    if (p->s->have_last && p->s->last_stream) cudaStreamSynchronize(p->s->last_stream);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->cap) {
+        cudaStreamSynchronize(p->cap);
+        cudaStreamDestroy(p->cap);
+    }
+    delete p;
+    return BHR_OK;
+}
+
+int bhr_surrogate_plan_create(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
+                              bhr_surrogate_plan** out) {
+    if (!s || !out) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_plan_create: NULL argument");
+    *out = nullptr;
+    bhr_surrogate_plan* p = new (std::nothrow) bhr_surrogate_plan();
+    if (!p) return fail(BHR_ERR_OOM, "bhr_surrogate_plan_create: out of host memory");
+    p->s = s;
+    p->nviews = nviews;
+    DevGuard dg(s->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        bhr_surrogate_plan_destroy(p);
+        return cfail(e, "bhr_surrogate_plan_create: stream");
+    }
+    // one eager trace: checks the views, sizes the work memory, sets the kernel attributes
+    int rc = bhr_surrogate_trace(s, views, nviews, out_dev, p->cap);
+    if (rc == BHR_OK) {
+        e = cudaStreamSynchronize(p->cap);
+        if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_create: first trace");
+    }
+    if (rc == BHR_OK) {
+        e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_create: begin capture");
+    }
+    if (rc == BHR_OK) {
+        const int rt = bhr_surrogate_trace(s, views, nviews, out_dev, p->cap);
+        e = cudaStreamEndCapture(p->cap, &p->graph);
+        if (rt != BHR_OK) rc = rt;
+        else if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_create: end capture");
+    }
+    if (rc == BHR_OK) {
+        e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+        if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_create: instantiate");
+    }
+    if (rc != BHR_OK) {
+        bhr_surrogate_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return BHR_OK;
+}
+
+int bhr_surrogate_plan_launch(bhr_surrogate_plan* p, void* stream) {
+    if (!p || !p->exec) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_plan_launch: plan is NULL or empty");
+    DevGuard dg(p->s->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = cudaGraphLaunch(p->exec, st);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_plan_launch");
+    p->s->last_stream = st;
+    p->s->last_nviews = p->nviews;
+    p->s->have_last = true;
+    p->s->last_from_plan = true;
     return BHR_OK;
 }
 
 int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2) {
     if (!s || !ms2) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_times: NULL");
     if (!s->have_last) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_times: no trace yet");
+    if (s->last_from_plan)
+        return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_times: phase times come from bhr_surrogate_trace, not from plan replays");
     DevGuard dg(s->device);
     cudaError_t e = cudaEventSynchronize(s->ev[2]);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms2[0], s->ev[0], s->ev[1]);

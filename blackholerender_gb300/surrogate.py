@@ -140,6 +140,10 @@ class Surrogate:
         ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
         _abi.check(_abi.lib().bhr_surrogate_trace(self.h, arr, n, ptrs, ctypes.c_void_p(stream.cuda_stream)))
 
+    def plan(self, views, outs):
+        """bhr_surrogate_plan_*: the trace of these views into these device tensors as one CUDA graph."""
+        return SurrogatePlan(self, views, outs)
+
     def trace_host(self, views, outs):
         """bhr_surrogate_trace_host: records land in host arrays (one per view)."""
         n = len(views)
@@ -160,3 +164,34 @@ class Surrogate:
         _abi.check(_abi.lib().bhr_surrogate_trace_stats(self.h, o))
         return {"surrogate": o[0], "fallback": o[1], "capture_disagree": o[2], "fallback_steps": o[3],
                 "mlp_queries": o[4], "mlp_rows": o[5]}
+
+
+class SurrogatePlan:
+    """A fixed batch of views traced by the surrogate as one replayed CUDA graph."""
+
+    def __init__(self, sur: Surrogate, views, outs):
+        self._sur = sur
+        self._outs = list(outs)
+        n = len(views)
+        arr = (_abi.View * n)(*views)
+        ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in self._outs])
+        self._p = ctypes.c_void_p()
+        _abi.check(_abi.lib().bhr_surrogate_plan_create(sur.h, arr, n, ptrs, ctypes.byref(self._p)))
+
+    def launch(self, stream=None):
+        import torch
+
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        _abi.check(_abi.lib().bhr_surrogate_plan_launch(self._p, ctypes.c_void_p(stream.cuda_stream)))
+
+    def close(self):
+        if self._p:
+            _abi.lib().bhr_surrogate_plan_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -265,6 +265,16 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
                         void* cuda_stream);
 /* Host-memory variant (records copied to out_host[k]; synchronous), as bhr_trace_host. */
 int bhr_surrogate_trace_host(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_host);
+/* The same trace of a fixed batch of views captured once into a CUDA graph and replayed: the 2 x
+ * nviews + 1 launches of a trace become one graph launch. The plan uses the surrogate's work
+ * memory and outputs: replays and traces on the same surrogate must not overlap on the GPU.
+ * bhr_surrogate_trace_stats covers replays too; bhr_surrogate_trace_times only eager traces.
+ * No counterpart in the reference. */
+typedef struct bhr_surrogate_plan bhr_surrogate_plan;
+int bhr_surrogate_plan_create(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
+                              bhr_surrogate_plan** plan);
+int bhr_surrogate_plan_launch(bhr_surrogate_plan* plan, void* cuda_stream);
+int bhr_surrogate_plan_destroy(bhr_surrogate_plan* plan);
 /* Device time of the last bhr_surrogate_trace: ms2[0] surrogate pass, ms2[1] fallback march. */
 int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2);
 /* Of the last bhr_surrogate_trace: rays answered by the surrogate, rays sent to the integrator,

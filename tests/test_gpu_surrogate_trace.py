@@ -190,3 +190,30 @@ def test_surrogate_path_faster_than_plain(surrogate):
     t_surr = timed(lambda: surrogate.trace(views, outs))
     print(f"\n8 poses: plain {t_plain:.2f} ms, surrogate + fallback {t_surr:.2f} ms ({t_plain / t_surr:.2f}x)")
     assert t_surr < t_plain / 1.2, (t_surr, t_plain)
+
+
+def test_surrogate_plan_replays_the_trace(surrogate):
+    """bhr_surrogate_plan_*: the trace of a batch captured into one CUDA graph and replayed gives
+    the records of bhr_surrogate_trace, bit for bit, with its statistics."""
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG, width=480, height=270)[:6]
+    want = surrogate.trace(views)
+    torch.cuda.synchronize()
+    want = [o.cpu().numpy() for o in want]
+    st_want = surrogate.trace_stats()
+    outs = [torch.zeros(v.rays * 64, dtype=torch.uint8, device="cuda") for v in views]
+    p = surrogate.plan(views, outs)
+    for _ in range(2):
+        for o in outs:
+            o.zero_()
+        p.launch()
+        torch.cuda.synchronize()
+        for a, b in zip(want, outs):
+            assert np.array_equal(a, b.cpu().numpy())
+        assert surrogate.trace_stats() == st_want
+    from blackholerender_gb300 import BhrError
+
+    with pytest.raises(BhrError):  # phase times are an eager trace's
+        surrogate.trace_times_ms()
+    p.close()
