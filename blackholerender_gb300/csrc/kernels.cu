@@ -27,7 +27,7 @@ namespace bhr {
 namespace {
 
 constexpr int kPool = 64;  // ring entries per warp (two setup batches)
-constexpr int kStepsPerCheck = 2;
+constexpr int kStepsPerCheck = 3;  // steps between a warp's retire checks (2: +4%, 4: +1.4% time on the 16 poses)
 constexpr float kSqrt27f = 5.19615242270663f;
 
 __device__ __forceinline__ unsigned long long globaltimer() {
