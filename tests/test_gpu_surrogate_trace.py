@@ -217,3 +217,31 @@ def test_surrogate_plan_replays_the_trace(surrogate):
     with pytest.raises(BhrError):  # phase times are an eager trace's
         surrogate.trace_times_ms()
     p.close()
+
+
+def test_surrogate_host_buffers_and_uneven_views(surrogate):
+    """The 64 uneven views (sizes, FOVs, camera radii 6.5-200, budgets 200-700) through
+    bhr_surrogate_trace_host: equal to the device-buffer trace, classification equal to the FP64
+    oracle outside the band, surrogate directions within 1e-4 rad of it at the 99th percentile."""
+    import torch
+
+    from blackholerender_gb300 import HIT_DTYPE
+
+    views = workloads.c4_views(TERM_CONFIG, scale=0.01)
+    dev = surrogate.trace(views)
+    torch.cuda.synchronize()
+    dev = [hits_numpy(o.cpu()) for o in dev]
+    host = [np.zeros(v.rays, dtype=HIT_DTYPE) for v in views]
+    surrogate.trace_host(views, host)
+    rng = np.random.default_rng(17)
+    angs = []
+    for v, a, h in zip(views, dev, host):
+        assert np.array_equal(a.view(np.uint8), h.view(np.uint8))
+        idx = rng.choice(v.rays, min(v.rays, 300), replace=False)
+        ref = O.trace_pixels(v, idx, fp64=True)
+        rep = parity.compare(h[idx], ref, max_steps=v.max_steps, band=2e-3, edge_rel=EDGE_REL)
+        assert rep.class_mismatch == 0, (v.width, v.height, rep.as_dict())
+        m = ((h["flags"][idx] & FLAG_SURROGATE) != 0) & (ref["status"] == 1)
+        angs.append(O.angle(h["dir"][idx][m], ref["dir"][m]))
+    a = np.concatenate(angs)
+    assert len(a) > 5000 and np.percentile(a, 99) < DIR_MAX_RAD, np.percentile(a, 99)
