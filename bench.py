@@ -366,8 +366,18 @@ def run_gpu(args):
     mlp_flop = st["mlp_queries"] * F_MLP
     achieved = mlp_flop / (t_pass * 1e-3) / 1e12
     fp32_peak = fp32_peak_tflops(dev)
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:  # DRAM bytes of one k_surrogate launch (one view) from the committed ncu capture
+            traffic = json.loads(tfile.read_text())["k_surrogate"]["dram_bytes_per_launch"]
+        except (KeyError, ValueError):
+            traffic = None
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-            "frac": achieved / bf16_peak, "traffic": None, "peak_source": peak_src,
+            "frac": achieved / bf16_peak, "traffic": traffic,
+            "traffic_note": "dram read+write bytes per k_surrogate launch (one view, ncu); algorithmic writes "
+                            "are 64 B x 2.07 M rays = 133 MB, the rest of the dirty lines stay in L2",
+            "peak_source": peak_src,
             "kernel": "k_surrogate (one launch per view; ms below is the 16-view pass)",
             "algorithm": f"{F_MLP} BF16 FLOP per network query; {st['mlp_queries']} queries "
                          f"({st['mlp_queries'] / max(st['surrogate'], 1):.2f} per surrogate ray)",
