@@ -15,8 +15,8 @@ from . import _abi
 from ._abi import (  # noqa: F401
     DISK_NONE, DISK_THIN, DISK_VOLUMETRIC, FLAG_FALLBACK, FLAG_FP64, FLAG_NONFINITE, FLAG_SURROGATE,
     HIT_DTYPE, METHOD_PLAIN, METHOD_SURROGATE, PREC_FP32, PREC_MIXED, SQRT27, STATUS_BUDGET,
-    STATUS_CAPTURED, STATUS_ESCAPED, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, LaunchShape, Options, Stats,
-    View,
+    STATUS_CAPTURED, STATUS_ESCAPED, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, LaunchShape, Options,
+    ShadeParams, Stats, View,
 )
 
 HIT_BYTES = 64
@@ -173,8 +173,61 @@ class Tracer:
                    self._ctx)
         return out
 
+    def shade(self, views: Sequence[View], hits, params: ShadeParams | None = None, outs=None, stream=None):
+        """bhr_shade: hit records (device tensors) -> linear RGB images (height, width, 4) float32.
+
+        rgb is the fragment shader's colour without the sky cube's term; alpha is that term's
+        weight. Returns the output tensors."""
+        import torch
+
+        dev = torch.device("cuda", self.device)
+        n = len(views)
+        if params is None:
+            params = shade_params()
+        if outs is None:
+            outs = [torch.empty((v.height, v.width, 4), dtype=torch.float32, device=dev) for v in views]
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        arr = (View * n)(*views)
+        hp = (ctypes.c_void_p * n)(*[h.data_ptr() for h in hits])
+        op = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
+        _abi.check(_abi.lib().bhr_shade(self._ctx, arr, n, hp, ctypes.byref(params), op,
+                                        ctypes.c_void_p(stream.cuda_stream)), self._ctx)
+        return outs
+
+    def noise_bake(self, seed: int = 7, out=None, stream=None):
+        """bhr_noise_bake: the disk's 128^3 noise volume as a device int16 tensor of half bits."""
+        import torch
+
+        dev = torch.device("cuda", self.device)
+        if out is None:
+            out = torch.empty((_abi.NOISE_SIZE,) * 3, dtype=torch.int16, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        _abi.check(_abi.lib().bhr_noise_bake(self._ctx, seed, ctypes.c_void_p(out.data_ptr()),
+                                             ctypes.c_void_p(stream.cuda_stream)), self._ctx)
+        return out
+
     def plan(self, views: Sequence[View], outs, precision: int = PREC_FP32, autotune: bool = False) -> "Plan":
         return Plan(self, views, outs, precision, autotune)
+
+
+def shade_params(**fields) -> ShadeParams:
+    """bhr_shade_default_params (the reference's Settings defaults), then the given fields."""
+    p = ShadeParams()
+    _abi.check(_abi.lib().bhr_shade_default_params(ctypes.byref(p)))
+    for k, val in fields.items():
+        if not hasattr(p, k):
+            raise AttributeError(f"bhr_shade_params has no field {k}")
+        setattr(p, k, val)
+    return p
+
+
+def blackbody_lut() -> np.ndarray:
+    """bhr_blackbody_lut: (256, 4) float32, rgb of luminance 1 and a = Y / Y(6500 K)."""
+    out = np.zeros((_abi.BLACKBODY_LUT, 4), dtype=np.float32)
+    _abi.check(_abi.lib().bhr_blackbody_lut(out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+    return out
 
 
 class Plan:

@@ -46,6 +46,8 @@ METHOD_SURROGATE = 1
 SQRT27 = 27.0 ** 0.5
 LENS_RAYS = 1024
 LENS_PHIS = 1024
+NOISE_SIZE = 128       # BHR_NOISE_SIZE
+BLACKBODY_LUT = 256    # BHR_BLACKBODY_LUT
 
 
 class View(ctypes.Structure):
@@ -112,6 +114,29 @@ class LaunchShape(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ShadeParams(ctypes.Structure):
+    """bhr_shade_params: the shading uniforms of Renderer::setTraceUniforms (Renderer.cpp:327-346)."""
+
+    _fields_ = [
+        ("disk_density", ctypes.c_float),
+        ("disk_opacity", ctypes.c_float),
+        ("disk_peak_temp", ctypes.c_float),
+        ("disk_brightness", ctypes.c_float),
+        ("disk_noise_scale", ctypes.c_float),
+        ("disk_noise_strength", ctypes.c_float),
+        ("disk_time", ctypes.c_float),
+        ("disk_warmth", ctypes.c_float),
+        ("disk_inflow", ctypes.c_float),
+        ("doppler_strength", ctypes.c_float),
+        ("sky_brightness", ctypes.c_float),
+        ("star_density", ctypes.c_float),
+        ("star_brightness", ctypes.c_float),
+        ("shadow_overlay", ctypes.c_int32),
+        ("noise_seed", ctypes.c_uint32),
+        ("reserved", ctypes.c_int32 * 5),
+    ]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("rays", ctypes.c_uint64),
@@ -144,6 +169,7 @@ HIT_DTYPE = np.dtype(
 )
 assert HIT_DTYPE.itemsize == 64
 assert ctypes.sizeof(View) == 160
+assert ctypes.sizeof(ShadeParams) == 80
 
 # every entry point include/bhr.h declares, with its ctypes signature
 _P = ctypes.c_void_p
@@ -170,6 +196,11 @@ SIGNATURES = {
     "bhr_lens_table": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int, _P, _P]),
     "bhr_lens_alpha": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
     "bhr_shadow_angular_radius": (ctypes.c_double, [ctypes.c_double]),
+    "bhr_shade_default_params": (ctypes.c_int, [ctypes.POINTER(ShadeParams)]),
+    "bhr_shade": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(ShadeParams),
+                                 ctypes.POINTER(_P), _P]),
+    "bhr_noise_bake": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P]),
+    "bhr_blackbody_lut": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "bhr_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),
     "bhr_set_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),
     "bhr_autotune": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int,

@@ -17,7 +17,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libbhr.so"
-SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu", "surrogate_api.cu", "lens.cu"]
+SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu", "surrogate_api.cu", "lens.cu", "shade.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -30,7 +30,10 @@ def _nvcc() -> str:
 
 # Device float code flushes denormals (as GLSL does): rsqrt and the fast divide then map to
 # single SFU instructions without subnormal fix-up sequences. FP64 code is unaffected.
-DEVICE_FLAGS = {"kernels.cu": ["-ftz=true"], "surrogate.cu": ["-ftz=true"], "lens.cu": ["-ftz=true"]}
+DEVICE_FLAGS = {"kernels.cu": ["-ftz=true"], "surrogate.cu": ["-ftz=true"], "lens.cu": ["-ftz=true"],
+                # shading: IEEE +, -, *, / and sqrt without contraction, so that the noise volume
+                # and every non-transcendental step round as the CPU restatement does
+                "shade.cu": ["-fmad=false"]}
 
 
 def _flags() -> list[str]:

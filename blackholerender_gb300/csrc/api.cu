@@ -18,6 +18,7 @@
 #include "bhr.h"
 #include "host_views.h"
 #include "kernels.cuh"
+#include "shade.cuh"
 
 // Device scratch of a trace: one work queue per launch batch, and the FP64 queues of MIXED.
 struct TraceScratch {
@@ -53,6 +54,11 @@ struct bhr_ctx {
     int last_nviews = 0;
     bool have_last = false;
     std::map<std::string, bhr_launch_shape> tuned;  // autotuner results by workload signature
+    // shading: the blackbody table and the disk's noise volume, made on first use
+    float4* lut = nullptr;
+    uint16_t* noise = nullptr;
+    uint32_t noise_seed = 0;
+    bool noise_ready = false;
     std::string err;
 };
 
@@ -347,6 +353,8 @@ int bhr_destroy(bhr_ctx* c) {
     cudaSetDevice(c->device);
     c->scr.release();
     if (c->staging) cudaFree(c->staging);
+    if (c->lut) cudaFree(c->lut);
+    if (c->noise) cudaFree(c->noise);
     for (cudaStream_t& st : c->hstream)
         if (st) cudaStreamDestroy(st);
     cudaSetDevice(prev);
@@ -648,6 +656,129 @@ int bhr_lens_table(bhr_ctx* c, float cam_r, int method, float* table, void* cuda
 }
 
 float bhr_lens_alpha(float u, float alpha_crit) { return bhr::lens_alpha_host(u, alpha_crit); }
+
+// ---------------------------------------------------------------------------------------
+// shading
+
+int bhr_shade_default_params(bhr_shade_params* p) {
+    if (!p) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_shade_default_params: NULL argument");
+    std::memset(p, 0, sizeof *p);
+    // Settings defaults (Settings.h:32-55) at full disk fade, DiskTextures.cpp:106 noise seed
+    p->disk_density = 1.0f;
+    p->disk_opacity = 2.0f;
+    p->disk_peak_temp = 6000.0f;
+    p->disk_brightness = 5.5f;
+    p->disk_noise_scale = 1.0f;
+    p->disk_noise_strength = 0.85f;
+    p->disk_time = 0.0f;
+    p->disk_warmth = 0.4f;
+    p->disk_inflow = 0.0f;
+    p->doppler_strength = 0.0f;
+    p->sky_brightness = 1.0f;
+    p->star_density = 1.0f;
+    p->star_brightness = 1.0f;
+    p->shadow_overlay = 0;
+    p->noise_seed = 7u;
+    return BHR_OK;
+}
+
+int bhr_blackbody_lut(float* out) {
+    if (!out) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_blackbody_lut: NULL argument");
+    bhr::blackbody_lut_host(out);
+    return BHR_OK;
+}
+
+int bhr_noise_bake(bhr_ctx* c, uint32_t seed, uint16_t* out, void* cuda_stream) {
+    if (!c || !out) return fail(c, BHR_ERR_INVALID_ARG, "bhr_noise_bake: NULL argument");
+    if (reinterpret_cast<uintptr_t>(out) % 16 != 0)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_noise_bake: out must be 16-byte aligned");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const cudaError_t e = bhr::launch_noise_bake(seed, out, static_cast<cudaStream_t>(cuda_stream));
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? BHR_OK : cuda_fail(c, e, "bhr_noise_bake");
+}
+
+namespace {
+
+// The blackbody table and the noise volume of `seed`, complete before the call returns.
+int ensure_shade_resources(bhr_ctx* c, uint32_t seed, cudaStream_t st) {
+    if (!c->lut) {
+        std::vector<float> host(size_t(BHR_BLACKBODY_LUT) * 4);
+        bhr::blackbody_lut_host(host.data());
+        cudaError_t e = cudaMalloc(&c->lut, host.size() * sizeof(float));
+        if (e != cudaSuccess) {
+            c->lut = nullptr;
+            return cuda_fail(c, e, "bhr_shade: blackbody table");
+        }
+        e = cudaMemcpy(c->lut, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(c, e, "bhr_shade: blackbody table");
+    }
+    if (!c->noise) {
+        const cudaError_t e = cudaMalloc(&c->noise, size_t(BHR_NOISE_SIZE) * BHR_NOISE_SIZE * BHR_NOISE_SIZE * 2);
+        if (e != cudaSuccess) {
+            c->noise = nullptr;
+            return cuda_fail(c, e, "bhr_shade: noise volume");
+        }
+        c->noise_ready = false;
+    }
+    if (!c->noise_ready || c->noise_seed != seed) {
+        cudaError_t e = bhr::launch_noise_bake(seed, c->noise, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "bhr_shade: noise bake");
+        c->noise_seed = seed;
+        c->noise_ready = true;
+    }
+    return BHR_OK;
+}
+
+}  // namespace
+
+int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* const* hits, const bhr_shade_params* p,
+              float* const* rgba, void* cuda_stream) {
+    if (!c || !views || nviews <= 0 || !hits || !p || !rgba)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade: NULL argument or no views");
+    for (int k = 0; k < nviews; ++k) {
+        const bhr_view& v = views[k];
+        const std::string at = "bhr_shade: view " + std::to_string(k);
+        if (v.width <= 0 || v.height <= 0) return fail(c, BHR_ERR_INVALID_ARG, at + ": width and height must be positive");
+        if (v.disk_mode == BHR_DISK_VOLUMETRIC)
+            return fail(c, BHR_ERR_UNSUPPORTED, at + ": the volumetric disk is shaded inside its march");
+        if (!hits[k] || !rgba[k]) return fail(c, BHR_ERR_INVALID_ARG, at + ": NULL buffer");
+        if (reinterpret_cast<uintptr_t>(hits[k]) % 16 != 0 || reinterpret_cast<uintptr_t>(rgba[k]) % 16 != 0)
+            return fail(c, BHR_ERR_INVALID_ARG, at + ": buffers must be 16-byte aligned");
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    int rc = ensure_shade_resources(c, p->noise_seed, st);
+    for (int k = 0; k < nviews && rc == BHR_OK; ++k) {
+        const bhr_view& v = views[k];
+        bhr::ShadeArgs a{};
+        for (int i = 0; i < 3; ++i) a.cam[i] = v.cam_pos[i];
+        for (int i = 0; i < 9; ++i) a.basis[i] = v.cam_basis[i];
+        a.tan_half = v.tan_half_fov;
+        a.jitter[0] = v.jitter[0];
+        a.jitter[1] = v.jitter[1];
+        a.width = v.width;
+        a.height = v.height;
+        a.disk_inner = v.disk_inner;
+        a.disk_outer = v.disk_outer;
+        a.disk_thin = v.disk_mode == BHR_DISK_THIN;
+        a.far_mode = v.far_mode;
+        a.p = *p;
+        a.hits = hits[k];
+        a.out = reinterpret_cast<float4*>(rgba[k]);
+        a.noise = c->noise;
+        a.lut = c->lut;
+        const cudaError_t e = bhr::launch_shade(a, st);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_shade: kernel launch");
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
 
 double bhr_shadow_angular_radius(double r) { return bhr::lens_alpha_crit(r); }
 

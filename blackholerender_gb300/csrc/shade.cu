@@ -1,0 +1,462 @@
+// The consumer of the hit records: the fragment shader's shading of a traced pixel when the
+// disk is thin and no bodies, gas or universe sky are on screen.
+//   k_noise_bake  noise_bake.comp:9-26 (fbm of periodic gradient noise, common.glsl:16-77,
+//                 plus a ridged octave) into a 128^3 half volume, one thread per texel
+//   k_shade       per pixel: the recorded crossings shaded by thinDiskSample (disk.glsl:113-129)
+//                 and composited front to back (blackhole.frag:209-216,234); the sky's analytic
+//                 star layers (sky.glsl:26-118) for escaped rays, with the footprint from 2x2-quad
+//                 differences of escDir (blackhole.frag:297-310); shadow overlay and NaN clear
+//                 (:354-359,377-379). The sky cube's weight goes to the alpha channel.
+// Block of 32 x 8 pixels: every 2x2 quad (even-aligned, as the rasteriser's) lies inside one
+// block, so the derivative exchange is one shared-memory round. The blackbody table (4 KiB)
+// is staged in shared memory; the noise volume (4 MiB) is read through L1/L2.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "bhr.h"
+#include "shade.cuh"
+
+namespace bhr {
+
+namespace {
+
+constexpr int kN = BHR_NOISE_SIZE, kLut = BHR_BLACKBODY_LUT;
+constexpr int kBX = 32, kBY = 8;
+constexpr float kPi = 3.14159265358979f, kTwoPi = 6.28318530717959f;
+
+struct F3 { float x, y, z; };
+__device__ __forceinline__ F3 add(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 scale(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ F3 divs(F3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 cross(F3 a, F3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float len(F3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ F3 normalize(F3 a) { return divs(a, len(a)); }
+__device__ __forceinline__ float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }  // GLSL mix
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+__device__ __forceinline__ float smoothstep(float e0, float e1, float x) {
+    const float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+
+// common.glsl:16-22 pcg3d, the three lanes updated in sequence
+__device__ __forceinline__ uint3 pcg3d(uint3 v) {
+    v.x = v.x * 1664525u + 1013904223u;
+    v.y = v.y * 1664525u + 1013904223u;
+    v.z = v.z * 1664525u + 1013904223u;
+    v.x += v.y * v.z;
+    v.y += v.z * v.x;
+    v.z += v.x * v.y;
+    v.x ^= v.x >> 16;
+    v.y ^= v.y >> 16;
+    v.z ^= v.z >> 16;
+    v.x += v.y * v.z;
+    v.y += v.z * v.x;
+    v.z += v.x * v.y;
+    return v;
+}
+
+// common.glsl:33-39 grad3: a unit gradient from the hashed lattice point
+__device__ __forceinline__ F3 grad3(int cx, int cy, int cz, uint32_t salt) {
+    const uint3 h = pcg3d(make_uint3(uint32_t(cx) + salt, uint32_t(cy) + (salt * 3u + 11u), uint32_t(cz) + (salt * 7u + 29u)));
+    const float s = 1.0f / 4294967296.0f;
+    const F3 g{float(h.x) * s * 2.0f - 1.0f, float(h.y) * s * 2.0f - 1.0f, float(h.z) * s * 2.0f - 1.0f};
+    return scale(g, 1.0f / sqrtf(fmaxf(dot(g, g), 1e-8f)));
+}
+
+__device__ __forceinline__ float fade(float t) { return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f); }
+
+// common.glsl:58-77 pgnoise3: gradient noise whose lattice wraps every `period` cells
+__device__ float pgnoise3(F3 p, int period, uint32_t salt) {
+    const float ix = floorf(p.x), iy = floorf(p.y), iz = floorf(p.z);
+    const F3 f{p.x - ix, p.y - iy, p.z - iz};
+    const F3 u{fade(f.x), fade(f.y), fade(f.z)};
+    const int c[3] = {int(ix), int(iy), int(iz)};
+    int c0[3], c1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        c0[k] = ((c[k] % period) + period) % period;
+        c1[k] = ((c[k] + 1) % period + period) % period;
+    }
+    float n[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+        const F3 g = grad3(ox ? c1[0] : c0[0], oy ? c1[1] : c0[1], oz ? c1[2] : c0[2], salt);
+        n[k] = dot(g, F3{f.x - float(ox), f.y - float(oy), f.z - float(oz)});
+    }
+    const float nx00 = mixf(n[0], n[1], u.x), nx10 = mixf(n[2], n[3], u.x);
+    const float nx01 = mixf(n[4], n[5], u.x), nx11 = mixf(n[6], n[7], u.x);
+    return 1.4f * mixf(mixf(nx00, nx10, u.y), mixf(nx01, nx11, u.y), u.z);
+}
+
+__global__ void __launch_bounds__(256) k_noise_bake(uint32_t seed, uint16_t* __restrict__ out) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= kN * kN * kN) return;
+    const int x = idx % kN, y = (idx / kN) % kN, z = idx / (kN * kN);
+    const F3 uvw{(float(x) + 0.5f) / float(kN), (float(y) + 0.5f) / float(kN), (float(z) + 0.5f) / float(kN)};
+    float sum = 0.0f, amp = 0.55f, norm = 0.0f;
+    int period = 4;
+#pragma unroll 1
+    for (int o = 0; o < 6; ++o) {
+        sum += amp * pgnoise3(scale(uvw, float(period)), period, seed + uint32_t(o) * 131u);
+        norm += amp;
+        amp *= 0.55f;
+        period *= 2;
+    }
+    float n = clampf(0.5f + 0.5f * (sum / norm) * 1.6f, 0.0f, 1.0f);
+    const float ridge = 1.0f - fabsf(pgnoise3(scale(uvw, 8.0f), 8, seed + 977u));
+    n = mixf(n, n * ridge * 1.3f, 0.35f);
+    out[idx] = __half_as_ushort(__float2half_rn(n));  // the R16F store
+}
+
+// ---------------------------------------------------------------- shading
+
+struct Tex {
+    const uint16_t* noise;
+    const float4* lut;  // shared memory
+};
+
+// blackbody.glsl:7-16: log-temperature lookup, linear filter, clamp to edge; Wien-tail fade
+__device__ __forceinline__ float4 blackbody(const Tex& tx, float T) {
+    const float Tc = clampf(T, 1000.0f, 40000.0f);
+    const float t = (logf(Tc) - logf(1000.0f)) / (logf(40000.0f) - logf(1000.0f));
+    const float u = t * float(kLut) - 0.5f;
+    const float fl = floorf(u);
+    const float a = u - fl;
+    const int i0 = min(max(int(fl), 0), kLut - 1), i1 = min(max(int(fl) + 1, 0), kLut - 1);
+    const float4 p = tx.lut[i0], q = tx.lut[i1];
+    float4 o{mixf(p.x, q.x, a), mixf(p.y, q.y, a), mixf(p.z, q.z, a), mixf(p.w, q.w, a)};
+    const float under = clampf(T / 1000.0f, 0.0f, 1.0f);
+    o.w *= under * under * under * under * under * under;
+    return o;
+}
+
+__device__ __forceinline__ float texel(const Tex& tx, int x, int y, int z) {
+    return __half2float(__ushort_as_half(__ldg(tx.noise + (size_t(z) * kN + y) * kN + x)));
+}
+
+// texture(uNoise3d, c).r: trilinear, REPEAT
+__device__ float noise_sample(const Tex& tx, F3 c) {
+    const float ux = c.x * float(kN) - 0.5f, uy = c.y * float(kN) - 0.5f, uz = c.z * float(kN) - 0.5f;
+    const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+    const float ax = ux - fx, ay = uy - fy, az = uz - fz;
+    const int x0 = ((int(fx) % kN) + kN) % kN, y0 = ((int(fy) % kN) + kN) % kN, z0 = ((int(fz) % kN) + kN) % kN;
+    const int x1 = (x0 + 1) % kN, y1 = (y0 + 1) % kN, z1 = (z0 + 1) % kN;
+    const float c00 = mixf(texel(tx, x0, y0, z0), texel(tx, x1, y0, z0), ax);
+    const float c10 = mixf(texel(tx, x0, y1, z0), texel(tx, x1, y1, z0), ax);
+    const float c01 = mixf(texel(tx, x0, y0, z1), texel(tx, x1, y0, z1), ax);
+    const float c11 = mixf(texel(tx, x0, y1, z1), texel(tx, x1, y1, z1), ax);
+    return mixf(mixf(c00, c10, ay), mixf(c01, c11, ay), az);
+}
+
+__device__ __forceinline__ float glsl_mod(float x, float y) { return x - y * floorf(x / y); }
+
+// disk.glsl:45-63 diskNoise at the mid-plane (yOverH = 0)
+__device__ float disk_noise(const Tex& tx, const bhr_shade_params& P, float r, float phi) {
+    const float omega = powf(r, -1.5f);
+    const float t = P.disk_time;
+    const float Pd = 60.0f;
+    const float t1 = glsl_mod(t, Pd);
+    const float t2 = glsl_mod(t + 0.5f * Pd, Pd);
+    const float w2 = fabsf(2.0f * t1 / Pd - 1.0f);
+    const float rep = fmaxf(1.0f, floorf(2.0f * P.disk_noise_scale + 0.5f));
+    const float lr = logf(r) * 3.2f * P.disk_noise_scale;
+    const float yy = 0.0f * 0.35f;
+    const float k = rep / kTwoPi;
+    const F3 c1{(phi + omega * t1) * k, lr + P.disk_inflow * omega * t1, yy};
+    const F3 c2{(phi + omega * t2) * k, lr + 0.37f + P.disk_inflow * omega * t2, yy + 0.61f};
+    return mixf(noise_sample(tx, c1), noise_sample(tx, c2), w2);
+}
+
+// thinDiskSample (disk.glsl:113-129) at a recorded crossing: radiance (rgb) and alpha
+__device__ float4 thin_disk_sample(const Tex& tx, const ShadeArgs& A, float r, float phi, float b_axis, float rcam) {
+    const bhr_shade_params& P = A.p;
+    if (r < A.disk_inner || r > A.disk_outer) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float n = disk_noise(tx, P, r, phi);
+    const float f = smoothstep(0.32f, 0.78f, n);
+    const float pattern = mixf(1.0f, mixf(0.08f, 1.4f, f), P.disk_noise_strength);
+    const float emit = mixf(1.0f, mixf(0.22f, 1.35f, f * f), P.disk_noise_strength);
+    // diskRadialProfile (disk.glsl:81-85)
+    const float r_in = A.disk_inner, r_out = A.disk_outer;
+    const float inner = smoothstep(r_in, r_in + 0.25f, r);
+    const float outer = 1.0f - smoothstep(r_out * 0.55f, r_out, r);
+    const float radial = inner * outer * powf(r_in / fmaxf(r, r_in), 1.2f);
+    const float dens = P.disk_density * radial * pattern;
+    // diskTempProfile (disk.glsl:26-30)
+    const float x = r_in / fmaxf(r, r_in);
+    const float prof = powf(x, 0.75f) * powf(fmaxf(1.0f - sqrtf(x), 0.0f), 0.25f) / 0.48796f;
+    const float T = P.disk_peak_temp * prof * mixf(1.0f, 0.85f + 0.3f * emit, 0.5f);
+    // redshiftFactor (disk.glsl:36-41)
+    const float omega = powf(r, -1.5f);
+    const float ut = 1.0f / sqrtf(fmaxf(1.0f - 3.0f / r, 0.02f));
+    const float lapse = sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f));
+    const float g_phys = 1.0f / (lapse * ut * fmaxf(1.0f - omega * b_axis, 0.05f));
+    const float g = mixf(1.0f, g_phys, P.doppler_strength);
+    const float4 bb = blackbody(tx, T * g);
+    // opticalDepthScale (disk.glsl:67-71)
+    const float lapse_em = sqrtf(fmaxf(1.0f - 2.0f / r, 1e-4f));
+    const float ods = mixf(1.0f, lapse_em / (g_phys * lapse), P.doppler_strength);
+    const float alpha = 1.0f - expf(-dens * P.disk_opacity * 0.6f * ods);
+    // diskTint (disk.glsl:21)
+    const float w = P.disk_warmth;
+    const float s = bb.w * P.disk_brightness * emit;
+    return make_float4(bb.x * mixf(1.0f, 1.0f, w) * s, bb.y * mixf(1.0f, 0.80f, w) * s, bb.z * mixf(1.0f, 0.58f, w) * s,
+                       alpha);
+}
+
+struct Footprint {
+    F3 e1, e2;
+    float r11, r12, r22, gi11, gi12, gi22, det_gi, det, mu;
+};
+
+// sky.glsl:26-48 makeFootprint (QR of the screen-to-sky Jacobian [a b])
+__device__ Footprint make_footprint(F3 d, F3 a, F3 b, float omega0) {
+    Footprint f;
+    const float min_axis = 1e-3f * sqrtf(omega0);
+    const float la_raw = len(a);
+    const float la = fmaxf(la_raw, min_axis);
+    f.e1 = la_raw > 1e-12f ? divs(a, la_raw) : normalize(cross(d, F3{1e-3f, 1.0f + 1e-3f, 1e-3f}));
+    const float b1 = dot(b, f.e1);
+    const F3 bp = sub(b, scale(f.e1, b1));
+    const float lbp_raw = len(bp);
+    const float lbp = fmaxf(lbp_raw, min_axis);
+    f.e2 = lbp_raw > 1e-3f * min_axis ? divs(bp, lbp_raw) : normalize(cross(d, f.e1));
+    f.r11 = 1.0f / la;
+    f.r12 = -b1 / (la * lbp);
+    f.r22 = 1.0f / lbp;
+    f.gi11 = f.r11 * f.r11 + f.r12 * f.r12;
+    f.gi12 = f.r12 * f.r22;
+    f.gi22 = f.r22 * f.r22;
+    f.det_gi = (f.r11 * f.r22) * (f.r11 * f.r22);
+    const float area = la * lbp;
+    f.det = area * area;
+    f.mu = fminf(omega0 / area, 1e4f);
+    return f;
+}
+
+// sky.glsl:54-103 starLayer: stars in the lattice cells around d that meet the unit sphere,
+// each a sky-space Gaussian convolved with the pixel's screen-space Gaussian
+__device__ F3 star_layer(const Tex& tx, F3 d, const Footprint& fp, float N, float prob, float flux, float sig_star,
+                         float omega0, uint32_t salt, float g_shift) {
+    const float footprint_cells = powf(fp.det, 0.25f) * N;
+    const float w = smoothstep(0.8f, 2.5f, footprint_cells);
+    const float4 bavg = blackbody(tx, 5600.0f * g_shift);
+    const float aw = prob * N * N * 9.517f * flux * omega0;
+    const F3 avg{bavg.x * aw, bavg.y * aw, bavg.z * aw};
+    F3 sum{0.f, 0.f, 0.f};
+    if (w < 1.0f) {
+        const float s2 = sig_star * sig_star;
+        const float px2 = 0.45f;
+        const float saa = px2 + s2 * fp.gi11, sab = s2 * fp.gi12, sbb = px2 + s2 * fp.gi22;
+        const float det_s = px2 * px2 + px2 * s2 * (fp.gi11 + fp.gi22) + s2 * s2 * fp.det_gi;
+        const float inv_det_s = 1.0f / det_s;
+        const float isaa = sbb * inv_det_s, isab = -sab * inv_det_s, isbb = saa * inv_det_s;
+        const float norm = fp.mu / (kTwoPi * sqrtf(det_s));
+        const int c0x = int(floorf(d.x * N)), c0y = int(floorf(d.y * N)), c0z = int(floorf(d.z * N));
+        const float s_in = 1.0f - 0.5f / N, s_out = 1.0f + 0.5f / N;
+        const float s_in2 = s_in * s_in, s_out2 = s_out * s_out;
+        const float k16 = 1.0f / 65536.0f;
+        const uint32_t sy = salt * 7u + 1u, sz = salt * 13u + 2u;
+#pragma unroll 1
+        for (int cell = 0; cell < 27; ++cell) {
+            const int cx = c0x + cell % 3 - 1, cy = c0y + (cell / 3) % 3 - 1, cz = c0z + cell / 9 - 1;
+            const uint3 h = pcg3d(make_uint3(uint32_t(cx) + salt, uint32_t(cy) + sy, uint32_t(cz) + sz));
+            const float ux = float(h.x >> 16) * k16;
+            if (ux > prob) continue;
+            const float q0 = (float(cx) + float(h.x & 0xffffu) * k16) / N;
+            const float q1 = (float(cy) + float(h.y >> 16) * k16) / N;
+            const float q2 = (float(cz) + float(h.y & 0xffffu) * k16) / N;
+            const float ql2 = q0 * q0 + q1 * q1 + q2 * q2;
+            if (ql2 < s_in2 || ql2 > s_out2) continue;
+            const float iq = 1.0f / sqrtf(ql2);
+            const F3 delta{q0 * iq - d.x, q1 * iq - d.y, q2 * iq - d.z};
+            const float d1 = dot(fp.e1, delta), d2 = dot(fp.e2, delta);
+            const float sp = fp.r11 * d1 + fp.r12 * d2;
+            const float sq = fp.r22 * d2;
+            const float e = isaa * sp * sp + 2.0f * isab * sp * sq + isbb * sq * sq;
+            if (!(e < 30.0f)) continue;
+            const float uy = float(h.z >> 16) * k16, uz = float(h.z & 0xffffu) * k16;
+            const float F = flux * powf(fmaxf(uy, 2e-4f), -1.0f);
+            const float T = expf(mixf(logf(3000.0f), logf(22000.0f), powf(uz, 1.7f)));
+            const float4 bb = blackbody(tx, T * g_shift);
+            const float k = F * norm * expf(-0.5f * e);
+            sum = add(sum, F3{mixf(1.0f, bb.x, 0.7f) * k, mixf(1.0f, bb.y, 0.7f) * k, mixf(1.0f, bb.z, 0.7f) * k});
+        }
+    }
+    if (!isfinite(sum.x) || !isfinite(sum.y) || !isfinite(sum.z)) sum = F3{0.f, 0.f, 0.f};
+    sum = F3{fminf(sum.x, 64.0f), fminf(sum.y, 64.0f), fminf(sum.z, 64.0f)};
+    return F3{mixf(sum.x, avg.x, w), mixf(sum.y, avg.y, w), mixf(sum.z, avg.z, w)};
+}
+
+// blackhole.frag:68-72 primary direction of pixel (i, j), any i, j (quad partners outside the
+// image included)
+__device__ __forceinline__ F3 primary_dir(const ShadeArgs& A, int i, int j) {
+    const float pxx = float(i) + 0.5f + A.jitter[0], pxy = float(j) + 0.5f + A.jitter[1];
+    const float ndcx = pxx / float(A.width) * 2.0f - 1.0f, ndcy = pxy / float(A.height) * 2.0f - 1.0f;
+    const float aspect = float(A.width) / float(A.height);
+    const F3 dc = normalize(F3{ndcx * A.tan_half * aspect, ndcy * A.tan_half, -1.0f});
+    const float* B = A.basis;
+    return normalize(F3{B[0] * dc.x + B[3] * dc.y + B[6] * dc.z, B[1] * dc.x + B[4] * dc.y + B[7] * dc.z,
+                        B[2] * dc.x + B[5] * dc.y + B[8] * dc.z});
+}
+
+__global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ ShadeArgs A) {
+    __shared__ float4 s_lut[kLut];
+    __shared__ float s_esc[3][kBY][kBX];
+    __shared__ float s_dir[3][kBY][kBX];
+    __shared__ int s_e[kBY][kBX];
+    const int tid = threadIdx.y * kBX + threadIdx.x;
+    for (int k = tid; k < kLut; k += kBX * kBY) s_lut[k] = A.lut[k];
+    const Tex tx{A.noise, s_lut};
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    const bool in = i < A.width && j < A.height;
+    const bhr_shade_params& P = A.p;
+    const F3 cam{A.cam[0], A.cam[1], A.cam[2]};
+    const float rcam = len(cam);
+    const F3 dir = primary_dir(A, i, j);
+    __syncthreads();  // the table is staged
+
+    F3 col{0.f, 0.f, 0.f};
+    float trans = 1.0f;
+    bool esc = false;
+    F3 esc_dir = dir;
+    if (in) {
+        const float4* rec = reinterpret_cast<const float4*>(A.hits + int64_t(j) * A.width + i);
+        const float4 w0 = __ldg(rec), w1 = __ldg(rec + 1);
+        const uint32_t head = __float_as_uint(w0.x);
+        const int status = int(head & 0xffu), ncross = int((head >> 8) & 0xffu);
+        bool opaque = false;
+        if (A.disk_thin && ncross > 0) {
+            const float4 w2 = __ldg(rec + 2), w3 = __ldg(rec + 3);
+            const float cr[3] = {w2.z, w2.w, w3.x}, cp[3] = {w3.y, w3.z, w3.w};
+            const float b_axis = w2.x;
+            for (int k = 0; k < ncross && k < 3; ++k) {
+                const float4 d = thin_disk_sample(tx, A, cr[k], cp[k], b_axis, rcam);
+                col = add(col, F3{trans * d.x * d.w, trans * d.y * d.w, trans * d.z * d.w});
+                trans *= 1.0f - d.w;
+                if (trans < 0.004f) {
+                    opaque = true;
+                    break;
+                }
+            }
+        }
+        if (status == BHR_STATUS_ESCAPED) esc_dir = F3{w0.z, w0.w, w1.x};
+        esc = status == BHR_STATUS_ESCAPED && !opaque;
+    }
+    const int tx_ = threadIdx.x, ty_ = threadIdx.y;
+    s_esc[0][ty_][tx_] = esc_dir.x;
+    s_esc[1][ty_][tx_] = esc_dir.y;
+    s_esc[2][ty_][tx_] = esc_dir.z;
+    s_dir[0][ty_][tx_] = dir.x;
+    s_dir[1][ty_][tx_] = dir.y;
+    s_dir[2][ty_][tx_] = dir.z;
+    s_e[ty_][tx_] = esc ? 1 : 0;
+    __syncthreads();
+    if (!in) return;
+
+    const float pixel_angle = 2.0f * A.tan_half / float(A.height);
+    const float omega0 = pixel_angle * pixel_angle;
+    const float g = mixf(1.0f, 1.0f / sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f)), P.doppler_strength);
+    const float g4 = g * g * g * g;
+    float alpha = 0.0f;
+    if (esc) {
+        const int x0 = tx_ & ~1, x1 = x0 + 1, y0 = ty_ & ~1, y1 = y0 + 1;
+        const bool mixed = s_e[ty_][x0] != s_e[ty_][x1] || s_e[y0][tx_] != s_e[y1][tx_];
+        const float(*src)[kBY][kBX] = mixed ? s_dir : s_esc;
+        const F3 ddx{src[0][ty_][x1] - src[0][ty_][x0], src[1][ty_][x1] - src[1][ty_][x0], src[2][ty_][x1] - src[2][ty_][x0]};
+        const F3 ddy{src[0][y1][tx_] - src[0][y0][tx_], src[1][y1][tx_] - src[1][y0][tx_], src[2][y1][tx_] - src[2][y0][tx_]};
+        const Footprint fp = make_footprint(esc_dir, ddx, ddy, omega0);
+        const float sb = P.star_brightness * g4;
+        const F3 s1 = star_layer(tx, esc_dir, fp, 200.0f, 0.40f * P.star_density, 0.0045f * sb, 0.0004f, omega0, 11u, g);
+        const F3 s2 = star_layer(tx, esc_dir, fp, 48.0f, 0.25f * P.star_density, 0.06f * sb, 0.0011f, omega0, 23u, g);
+        const F3 sky = add(s1, s2);
+        col = add(col, F3{trans * sky.x, trans * sky.y, trans * sky.z});
+        alpha = trans * (P.sky_brightness * g4);
+    }
+    if (P.shadow_overlay && !A.far_mode) {
+        const float ang = acosf(clampf(dot(dir, F3{-cam.x / rcam, -cam.y / rcam, -cam.z / rcam}), -1.0f, 1.0f));
+        // shadowAngularRadius (geodesic.glsl:56-60)
+        const float s = fminf(1.0f, 5.19615242270663f / rcam * sqrtf(fmaxf(1.0f - 2.0f / rcam, 0.0f)));
+        const float a = asinf(s);
+        const float edge = rcam >= 3.0f ? a : kPi - a;
+        const float dd = fabsf(ang - edge) / pixel_angle;
+        const float k = 0.85f * (1.0f - smoothstep(0.8f, 1.8f, dd));
+        col = F3{mixf(col.x, 0.1f, k), mixf(col.y, 1.0f, k), mixf(col.z, 0.2f, k)};
+        alpha *= 1.0f - k;
+    }
+    if (!isfinite(col.x) || !isfinite(col.y) || !isfinite(col.z)) {
+        col = F3{0.f, 0.f, 0.f};
+        alpha = 0.0f;
+    }
+    A.out[int64_t(j) * A.width + i] = make_float4(fmaxf(col.x, 0.0f), fmaxf(col.y, 0.0f), fmaxf(col.z, 0.0f), alpha);
+}
+
+// ---------------------------------------------------------------- blackbody table (host, double)
+
+double lobe(double l, double mu, double s1, double s2) {
+    const double t = (l - mu) / (l < mu ? s1 : s2);
+    return std::exp(-0.5 * t * t);
+}
+
+// CIE 1931 2-degree colour matching functions as the multi-lobe Gaussian fits of Wyman, Sloan
+// and Shirley (2013), times Planck's law, summed over 380..780 nm in 1 nm steps
+void tristimulus(double T, double& X, double& Y, double& Z) {
+    const double h = 6.62607015e-34, c = 2.99792458e8, kb = 1.380649e-23;
+    X = Y = Z = 0.0;
+    for (int nm = 380; nm <= 780; ++nm) {
+        const double l = double(nm);
+        const double x = 1.056 * lobe(l, 599.8, 37.9, 31.0) + 0.362 * lobe(l, 442.0, 16.0, 26.7) -
+                         0.065 * lobe(l, 501.1, 20.4, 26.2);
+        const double y = 0.821 * lobe(l, 568.8, 46.9, 40.5) + 0.286 * lobe(l, 530.9, 16.3, 31.1);
+        const double z = 1.217 * lobe(l, 437.0, 11.8, 36.0) + 0.681 * lobe(l, 459.0, 26.0, 13.8);
+        const double lm = l * 1e-9;
+        const double b = (2.0 * h * c * c) / (lm * lm * lm * lm * lm) / (std::exp((h * c) / (lm * kb * T)) - 1.0);
+        X += b * x;
+        Y += b * y;
+        Z += b * z;
+    }
+}
+
+}  // namespace
+
+void blackbody_lut_host(float* out) {
+    double Xr, Yr, Zr;
+    tristimulus(6500.0, Xr, Yr, Zr);
+    const double lo = std::log(1000.0), hi = std::log(40000.0);
+    for (int i = 0; i < kLut; ++i) {
+        const double T = std::exp(lo + (hi - lo) * (double(i) / (kLut - 1)));
+        double X, Y, Z;
+        tristimulus(T, X, Y, Z);
+        // XYZ -> linear sRGB (D65), negative lobes clipped, normalised to luminance 1
+        const double r = std::max(3.2406 * X - 1.5372 * Y - 0.4986 * Z, 0.0);
+        const double g = std::max(-0.9689 * X + 1.8758 * Y + 0.0415 * Z, 0.0);
+        const double b = std::max(0.0557 * X - 0.2040 * Y + 1.0570 * Z, 0.0);
+        const double lum = 0.2126 * r + 0.7152 * g + 0.0722 * b;
+        const double inv = lum > 0.0 ? 1.0 / lum : 0.0;
+        out[4 * i + 0] = float(r * inv);
+        out[4 * i + 1] = float(g * inv);
+        out[4 * i + 2] = float(b * inv);
+        out[4 * i + 3] = float(Y / Yr);
+    }
+}
+
+cudaError_t launch_noise_bake(uint32_t seed, uint16_t* out, cudaStream_t st) {
+    const int n = kN * kN * kN;
+    k_noise_bake<<<(n + 255) / 256, 256, 0, st>>>(seed, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t st) {
+    const dim3 grid((a.width + kBX - 1) / kBX, (a.height + kBY - 1) / kBY);
+    k_shade<<<grid, dim3(kBX, kBY), 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace bhr

@@ -1,0 +1,31 @@
+// Launch arguments of the shading consumer (shade.cu), filled by the C ABI (api.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bhr.h"
+
+namespace bhr {
+
+struct ShadeArgs {
+    float cam[3];      // uCamPos
+    float basis[9];    // uCamBasis, column-major
+    float tan_half;    // uTanHalfFov
+    float jitter[2];
+    int32_t width, height;
+    float disk_inner, disk_outer;
+    int32_t disk_thin;  // uDiskMode == DISK_THIN
+    int32_t far_mode;
+    bhr_shade_params p;
+    const bhr_hit* hits;
+    float4* out;
+    const uint16_t* noise;  // BHR_NOISE_SIZE^3 half
+    const float4* lut;      // BHR_BLACKBODY_LUT entries
+};
+
+cudaError_t launch_noise_bake(uint32_t seed, uint16_t* out, cudaStream_t st);
+cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t st);
+void blackbody_lut_host(float* out);  // BHR_BLACKBODY_LUT x 4 floats, in double like the CPU bake
+
+}  // namespace bhr

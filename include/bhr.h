@@ -303,6 +303,56 @@ int bhr_lens_table(bhr_ctx* ctx, float cam_r, int method, float* table_dev, void
 float bhr_lens_alpha(float u, float alpha_crit);         /* lensAlpha, gas_lens.glsl:13-17 */
 double bhr_shadow_angular_radius(double r);              /* shadowAngularRadius, Geodesic.h:78-82 */
 
+/* ---- shading: hit records -> image (the consumer of the hit records) ------------------ */
+/* What blackhole.frag does with the march's result when the disk is thin and no bodies, gas
+ * or universe sky are on screen (uUniverse = 0, BHS_BODIES 0, BHS_GAS 0):
+ *   - each recorded crossing shaded by thinDiskSample (disk.glsl:113-129) and composited front
+ *     to back (blackhole.frag:209-216), the ray turning opaque below transmittance 0.004 (:234);
+ *   - escaped, non-opaque rays get the sky (sky.glsl:105-118) with the footprint built from the
+ *     screen-space derivatives of escDir (blackhole.frag:297-310; fine 2x2-quad differences,
+ *     the unlensed footprint where a quad mixes escaped and other pixels);
+ *   - the shadow overlay (:354-359), the NaN clear and the clamp at 0 (:377-379).
+ * The sky cube (textureGrad(uSkyCube, ...) in sampleSky: galaxies, nebulae and the Milky Way
+ * that SkyBaker bakes) is the caller's: rgba[3] is the weight of that term, transmittance x
+ * skyBrightness x g^4 (x the overlay's 1 - k), so the reference's fragColor.rgb is
+ * rgba.rgb + rgba.a * skyCube(escDir). The analytic star layers are included in rgba.rgb.
+ * Disk noise comes from the context's 128^3 R16F noise volume (noise_bake.comp, baked on first
+ * use and again when noise_seed changes) and colours from the blackbody LUT
+ * (DiskTextures.cpp:65-91). Texture filtering uses exact weights (GL's hardware rounds the
+ * linear-filter weights to 8 bits). Output: float4 per pixel, row-major with row 0 at the
+ * bottom like the hit records, 16-byte aligned device memory. */
+#define BHR_NOISE_SIZE 128    /* DiskTextures::kNoiseSize */
+#define BHR_BLACKBODY_LUT 256 /* DiskTextures::kLutSize: rgb of luminance 1, a = Y / Y(6500 K) */
+typedef struct bhr_shade_params {
+    float disk_density;        /* uDiskDensity        Settings.h:38  (1.0) */
+    float disk_opacity;        /* uDiskOpacity        diskOpacity x fade strength (2.0) */
+    float disk_peak_temp;      /* uDiskPeakTemp       Kelvin (6000) */
+    float disk_brightness;     /* uDiskBrightness     diskBrightness x fade strength (5.5) */
+    float disk_noise_scale;    /* uDiskNoiseScale     (1.0) */
+    float disk_noise_strength; /* uDiskNoiseStrength  (0.85) */
+    float disk_time;           /* uDiskTime           flow clock in M, [0, 60) */
+    float disk_warmth;         /* uDiskWarmth         (0.4) */
+    float disk_inflow;         /* uDiskInflow         (0; 0.08 for the debris disk) */
+    float doppler_strength;    /* uDopplerStrength    0 film look, 1 physical (0) */
+    float sky_brightness;      /* uSkyBrightness      weight of the caller's sky cube (1.0) */
+    float star_density;        /* uStarDensity        (1.0) */
+    float star_brightness;     /* uStarBrightness     (1.0) */
+    int32_t shadow_overlay;    /* uShadowOverlay      (0) */
+    uint32_t noise_seed;       /* noise_bake.comp uSeed, DiskTextures.cpp:106 (7) */
+    int32_t reserved[5];
+} bhr_shade_params;
+int bhr_shade_default_params(bhr_shade_params* p);
+/* Shades nviews views: hits_dev[k] holds view k's records (from any trace entry point),
+ * rgba_dev[k] gets width x height float4. Stream-ordered like bhr_trace. */
+int bhr_shade(bhr_ctx* ctx, const bhr_view* views, int nviews, const bhr_hit* const* hits_dev,
+              const bhr_shade_params* params, float* const* rgba_dev, void* cuda_stream);
+/* The disk's noise volume (noise_bake.comp): BHR_NOISE_SIZE^3 IEEE half values, texel
+ * (x, y, z) at (z N + y) N + x, into device memory. */
+int bhr_noise_bake(bhr_ctx* ctx, uint32_t seed, uint16_t* out_dev, void* cuda_stream);
+/* The blackbody table (DiskTextures::bakeBlackbodyLut) into host memory: BHR_BLACKBODY_LUT x 4
+ * floats, entry i at T = exp(log 1000 + (log 40000 - log 1000) i / 255). */
+int bhr_blackbody_lut(float* out_host);
+
 /* ---- launch shapes and the autotuner ------------------------------------------------ */
 /* No counterpart in the reference (its march is one fragment-shader draw whose scheduling the
  * GL driver owns); these choose how the persistent march kernel covers a batch of views. */

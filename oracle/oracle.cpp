@@ -10,6 +10,7 @@
 
 #include "march.hpp"
 #include "lens.hpp"
+#include "shade.hpp"
 
 using namespace oracle;
 
@@ -185,6 +186,45 @@ int oracle_lens_table(float cam_r, float alpha_crit, float* table, int nthreads,
             oracle::lensRay<float>(int(i), cam_r, alpha_crit, table);
         });
     return BHR_OK;
+}
+
+// The disk's noise volume (noise_bake.comp) as IEEE half values, texel (x, y, z) at (z N + y) N + x.
+int oracle_noise_bake(uint32_t seed, uint16_t* out, int nthreads) {
+    if (!out) return BHR_ERR_INVALID_ARG;
+    const int N = oracle::shade::kNoiseN;
+    parallel_for(int64_t(N) * N, nthreads, 16, [&](int64_t zy) {
+        const int z = int(zy / N), y = int(zy % N);
+        for (int x = 0; x < N; ++x)
+            out[zy * N + x] = oracle::shade::to_half(oracle::shade::noise_texel(x, y, z, seed));
+    });
+    return BHR_OK;
+}
+
+// The blackbody table (DiskTextures::bakeBlackbodyLut): BHR_BLACKBODY_LUT x 4 floats.
+int oracle_blackbody_lut(float* out) {
+    if (!out) return BHR_ERR_INVALID_ARG;
+    oracle::shade::blackbody_lut(out);
+    return BHR_OK;
+}
+
+// Shades one view from its hit records with the given noise volume and table; rgba gets
+// width x height x 4 floats.
+int oracle_shade_view(const bhr_view* v, const bhr_hit* hits, const bhr_shade_params* p, const uint16_t* noise,
+                      const float* lut, float* rgba, int nthreads) {
+    if (!v || !hits || !p || !noise || !lut || !rgba || v->width <= 0 || v->height <= 0) return BHR_ERR_INVALID_ARG;
+    const oracle::shade::Tex tx{noise, lut};
+    parallel_for(v->height, nthreads, 1, [&](int64_t j) { oracle::shade::shade_view(tx, *p, *v, hits, rgba, j, j + 1); });
+    return BHR_OK;
+}
+
+// Single components, for known-answer tests: the shader's redshiftFactor (disk.glsl:36-41) and
+// the CIE XYZ of a blackbody at T (the table's integral, DiskTextures.cpp:32-41).
+float oracle_redshift_factor(float r, float b_axis, float rcam) { return oracle::shade::redshift_factor(r, b_axis, rcam); }
+void oracle_blackbody_xyz(double T, double out[3]) { oracle::shade::xyz_of(T, out[0], out[1], out[2]); }
+uint16_t oracle_to_half(float x) { return oracle::shade::to_half(x); }
+void oracle_pcg3d(const uint32_t in[3], uint32_t out[3]) {
+    const oracle::shade::U3 h = oracle::shade::pcg3d({in[0], in[1], in[2]});
+    out[0] = h.x, out[1] = h.y, out[2] = h.z;
 }
 
 int oracle_hit_size(void) { return static_cast<int>(sizeof(bhr_hit)); }

@@ -48,4 +48,9 @@ void ref_far_field(const double x[3], const double v[3], double h2, double out[3
     out[0] = r.x; out[1] = r.y; out[2] = r.z;
 }
 
+// redshiftFactor (Geodesic.h:90-95), the CPU mirror of the disk shader's factor
+double ref_redshift_factor(double r_emit, double b_axis, double r_cam) {
+    return bhs::physics::redshiftFactor(r_emit, b_axis, r_cam);
+}
+
 }  // extern "C"

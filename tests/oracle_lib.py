@@ -12,7 +12,7 @@ from pathlib import Path
 
 import numpy as np
 
-from blackholerender_gb300 import HIT_DTYPE, View
+from blackholerender_gb300 import HIT_DTYPE, ShadeParams, View
 
 ROOT = Path(__file__).resolve().parent.parent
 ORACLE_DIR = ROOT / "oracle"
@@ -46,6 +46,16 @@ def lib():
         L.oracle_rk4_step.argtypes = [D, D, ctypes.c_double, ctypes.c_double]
         L.oracle_initial_velocity.argtypes = [D, D, D]
         L.oracle_far_field.argtypes = [D, D, ctypes.c_double, D]
+        L.oracle_noise_bake.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int]
+        L.oracle_blackbody_lut.argtypes = [ctypes.c_void_p]
+        L.oracle_shade_view.argtypes = [VP, ctypes.c_void_p, ctypes.POINTER(ShadeParams), ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.oracle_redshift_factor.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float]
+        L.oracle_redshift_factor.restype = ctypes.c_float
+        L.oracle_blackbody_xyz.argtypes = [ctypes.c_double, D]
+        L.oracle_to_half.argtypes = [ctypes.c_float]
+        L.oracle_to_half.restype = ctypes.c_uint16
+        L.oracle_pcg3d.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         assert L.oracle_hit_size() == 64 and L.oracle_view_size() == ctypes.sizeof(View)
         _lib = L
     return _lib
@@ -61,6 +71,8 @@ def ref_lib():
         D = ctypes.POINTER(ctypes.c_double)
         L.ref_trace.argtypes = [D, D, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, D,
                                 ctypes.POINTER(ctypes.c_int), D]
+        L.ref_redshift_factor.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.ref_redshift_factor.restype = ctypes.c_double
         _ref = L
     return _ref
 
@@ -129,3 +141,54 @@ def angle(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     c = np.linalg.norm(np.cross(a, b), axis=-1)
     d = np.sum(a * b, axis=-1)
     return np.arctan2(c, d)
+
+
+# ---------------------------------------------------------------- shading
+
+def noise_bake(seed: int = 7, threads: int | None = None) -> np.ndarray:
+    """The disk's noise volume (noise_bake.comp) as uint16 half bits, shape (z, y, x)."""
+    out = np.zeros((128, 128, 128), dtype=np.uint16)
+    rc = lib().oracle_noise_bake(seed, out.ctypes.data, threads or nthreads())
+    assert rc == 0
+    return out
+
+
+def blackbody_lut() -> np.ndarray:
+    out = np.zeros((256, 4), dtype=np.float32)
+    assert lib().oracle_blackbody_lut(out.ctypes.data) == 0
+    return out
+
+
+def shade_view(view: View, hits: np.ndarray, params: ShadeParams, noise: np.ndarray, lut: np.ndarray,
+               threads: int | None = None) -> np.ndarray:
+    """Shades one view from its records; (height, width, 4) float32."""
+    hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    noise = np.ascontiguousarray(noise, dtype=np.uint16)
+    lut = np.ascontiguousarray(lut, dtype=np.float32)
+    assert hits.size == view.width * view.height and noise.size == 128 ** 3 and lut.size == 1024
+    out = np.zeros((view.height, view.width, 4), dtype=np.float32)
+    rc = lib().oracle_shade_view(ctypes.byref(view), hits.ctypes.data, ctypes.byref(params), noise.ctypes.data,
+                                 lut.ctypes.data, out.ctypes.data, threads or nthreads())
+    assert rc == 0
+    return out
+
+
+def redshift_factor(r: float, b_axis: float, rcam: float) -> float:
+    return lib().oracle_redshift_factor(r, b_axis, rcam)
+
+
+def blackbody_xyz(T: float) -> np.ndarray:
+    out = np.zeros(3)
+    lib().oracle_blackbody_xyz(T, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return out
+
+
+def pcg3d(v) -> tuple[int, int, int]:
+    a = np.asarray(v, dtype=np.uint32)
+    o = np.zeros(3, dtype=np.uint32)
+    lib().oracle_pcg3d(a.ctypes.data, o.ctypes.data)
+    return tuple(int(x) for x in o)
+
+
+def to_half(x: float) -> int:
+    return int(lib().oracle_to_half(x))

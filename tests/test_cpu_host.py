@@ -43,6 +43,7 @@ def test_struct_layouts_match_the_header(tmp_path):
         "bhr_stats": [f for f, _ in _abi.Stats._fields_],
         "bhr_launch_shape": [f for f, _ in _abi.LaunchShape._fields_],
         "bhr_surrogate_config": [f for f, _ in _abi.SurrogateConfig._fields_],
+        "bhr_shade_params": [f for f, _ in _abi.ShadeParams._fields_],
         "bhr_hit": list(_abi.HIT_DTYPE.names),
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bhr.h"', "int main(void) {"]
@@ -57,7 +58,8 @@ def test_struct_layouts_match_the_header(tmp_path):
     got = dict(ln.split() for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True)
                .stdout.splitlines())
     py = {"bhr_view": _abi.View, "bhr_options": _abi.Options, "bhr_stats": _abi.Stats,
-          "bhr_launch_shape": _abi.LaunchShape, "bhr_surrogate_config": _abi.SurrogateConfig}
+          "bhr_launch_shape": _abi.LaunchShape, "bhr_surrogate_config": _abi.SurrogateConfig,
+          "bhr_shade_params": _abi.ShadeParams}
     for st, cls in py.items():
         assert int(got[st]) == ctypes.sizeof(cls), st
         for f, _ in cls._fields_:
