@@ -490,6 +490,97 @@ def run_side_workload(args):
     tr.close()
 
 
+def cpu_shade_sample(view, hits, params, seconds: float):
+    """The oracle's shading (FP32 restatement, all host threads) of one view's records, repeated
+    until `seconds` elapse; returns (Mpixels/s, threads). The noise volume is baked first,
+    outside the timed region, as the GPU path bakes it once per seed."""
+    L = _oracle()
+    threads = os.cpu_count() or 1
+    noise = np.zeros(128 ** 3, dtype=np.uint16)
+    lut = np.zeros(256 * 4, dtype=np.float32)
+    assert L.oracle_noise_bake(ctypes.c_uint32(params.noise_seed), ctypes.c_void_p(noise.ctypes.data), threads) == 0
+    assert L.oracle_blackbody_lut(ctypes.c_void_p(lut.ctypes.data)) == 0
+    out = np.zeros(view.rays * 4, dtype=np.float32)
+    px = 0
+    t0 = time.perf_counter()
+    while True:
+        rc = L.oracle_shade_view(ctypes.byref(view), ctypes.c_void_p(hits.ctypes.data), ctypes.byref(params),
+                                 ctypes.c_void_p(noise.ctypes.data), ctypes.c_void_p(lut.ctypes.data),
+                                 ctypes.c_void_p(out.ctypes.data), threads)
+        assert rc == 0
+        px += view.rays
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            return px / dt / 1e6, threads
+
+
+def run_shade_workload(args):
+    """--workload shade: the consumer of the hit records. The 16 poses at 1920x1080 are traced
+    once (plain FP32 plan, untimed); each step shades all 16 views from their records
+    (bhr_shade: thin disk, star sky, default look). One JSON line, not the headline."""
+    import torch
+
+    from blackholerender_gb300 import HIT_BYTES, TERM_CONFIG, Tracer, hits_numpy, shade_params, workloads
+
+    dev = torch.device("cuda", 0)
+    tr = Tracer(0)
+    views = workloads.c2_views(TERM_CONFIG)[: args.views]
+    px = sum(v.rays for v in views)
+    hits = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+    tr.trace(views, hits)
+    params = shade_params()
+    outs = [torch.empty((v.height, v.width, 4), dtype=torch.float32, device=dev) for v in views]
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        tr.shade(views, hits, params, outs, st)
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(0) as clk:
+        for a, b in ev:
+            flush.zero_()
+            a.record(st)
+            tr.shade(views, hits, params, outs, st)
+            b.record(st)
+        torch.cuda.synchronize(dev)
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(per) / len(per)
+    peaks = {}
+    pfile = ROOT / "MEASURED_PEAKS.json"
+    if pfile.exists():
+        try:
+            peaks = json.loads(pfile.read_text())
+        except Exception:
+            peaks = {}
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    bytes_px = HIT_BYTES + 16  # one record read, one float4 written
+    achieved = px * bytes_px / (ms * 1e-3) / 1e9
+    esc = sum(int((hits_numpy(h.cpu())["status"] == 1).sum()) for h in hits[:1]) / views[0].rays
+    line = {"metric": "Mpixels/s (shade)", "value": px / (ms * 1e-3) / 1e6, "unit": "Mpixels/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"shade {len(views)} poses (seed 0) at 1920x1080 from plain FP32 records; thin "
+                                   "disk + analytic star layers, default look", "pixels_per_step": px,
+                       "l2": "flushed (256 MiB write) between steps", "escaped_fraction_view0": esc},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "bytes_per_pixel": bytes_px, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get(
+                             "hbm_gbs") else "fallback 6800 GB/s",
+                         "note": "ALU-bound: 54 hashed lattice cells of the two star layers per escaped pixel"},
+            "gpu_launches": len(views) * args.steps, "clocks": clk.summary()}
+    if not args.no_cpu:
+        small = views[0].copy()
+        small.width, small.height = 480, 270
+        (h,) = tr.trace([small])
+        torch.cuda.synchronize(dev)
+        hs = np.ascontiguousarray(hits_numpy(h.cpu()))
+        mpx, threads = cpu_shade_sample(small, hs, params, min(args.cpu_seconds, 10.0))
+        line["cpu_baseline"] = {"value": mpx, "unit": "Mpixels/s", "cores": threads, "kind": "port",
+                                "sample": "oracle shading of pose 0 at 480x270, repeated for up to 10 s",
+                                "cpu": cpu_model()}
+    print(json.dumps(line), flush=True)
+    tr.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -503,13 +594,16 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--views", type=int, default=16, help="first N of the 16 poses (small profiling cases)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
-                    help="c2: the headline (16 poses at 1080p); c3 / c4: the other configurations")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "shade"],
+                    help="c2: the headline (16 poses at 1080p); c3 / c4: the other configurations; "
+                         "shade: the records' shading consumer")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "shade":
+        run_shade_workload(args)
     elif args.workload != "c2":
         run_side_workload(args)
     else:

@@ -769,6 +769,10 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         a.disk_thin = v.disk_mode == BHR_DISK_THIN;
         a.far_mode = v.far_mode;
         a.p = *p;
+        a.ln_1000 = std::log(1000.0f);
+        a.ln_40000 = std::log(40000.0f);
+        a.ln_3000 = std::log(3000.0f);
+        a.ln_22000 = std::log(22000.0f);
         a.hits = hits[k];
         a.out = reinterpret_cast<float4*>(rgba[k]);
         a.noise = c->noise;

@@ -7,13 +7,15 @@
 //                 star layers (sky.glsl:26-118) for escaped rays, with the footprint from 2x2-quad
 //                 differences of escDir (blackhole.frag:297-310); shadow overlay and NaN clear
 //                 (:354-359,377-379). The sky cube's weight goes to the alpha channel.
-// Block of 32 x 8 pixels: every 2x2 quad (even-aligned, as the rasteriser's) lies inside one
-// block, so the derivative exchange is one shared-memory round. The blackbody table (4 KiB)
-// is staged in shared memory; the noise volume (4 MiB) is read through L1/L2.
+// Block of 32 x 8 pixels in warps of 8 x 4: every 2x2 quad (even-aligned, as the rasteriser's)
+// lies inside one warp, so the derivative exchange is two shuffles. The star layers run per
+// warp over the union of its pixels' lattice cells. The blackbody table (4 KiB) is staged in
+// shared memory; the noise volume (4 MiB) is read through L1/L2.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 
 #include "bhr.h"
@@ -121,12 +123,13 @@ __global__ void __launch_bounds__(256) k_noise_bake(uint32_t seed, uint16_t* __r
 struct Tex {
     const uint16_t* noise;
     const float4* lut;  // shared memory
+    float ln_1000, ln_40000;
 };
 
 // blackbody.glsl:7-16: log-temperature lookup, linear filter, clamp to edge; Wien-tail fade
 __device__ __forceinline__ float4 blackbody(const Tex& tx, float T) {
     const float Tc = clampf(T, 1000.0f, 40000.0f);
-    const float t = (logf(Tc) - logf(1000.0f)) / (logf(40000.0f) - logf(1000.0f));
+    const float t = (logf(Tc) - tx.ln_1000) / (tx.ln_40000 - tx.ln_1000);
     const float u = t * float(kLut) - 0.5f;
     const float fl = floorf(u);
     const float a = u - fl;
@@ -241,53 +244,177 @@ __device__ Footprint make_footprint(F3 d, F3 a, F3 b, float omega0) {
     return f;
 }
 
-// sky.glsl:54-103 starLayer: stars in the lattice cells around d that meet the unit sphere,
-// each a sky-space Gaussian convolved with the pixel's screen-space Gaussian
-__device__ F3 star_layer(const Tex& tx, F3 d, const Footprint& fp, float N, float prob, float flux, float sig_star,
-                         float omega0, uint32_t salt, float g_shift) {
-    const float footprint_cells = powf(fp.det, 0.25f) * N;
-    const float w = smoothstep(0.8f, 2.5f, footprint_cells);
-    const float4 bavg = blackbody(tx, 5600.0f * g_shift);
-    const float aw = prob * N * N * 9.517f * flux * omega0;
-    const F3 avg{bavg.x * aw, bavg.y * aw, bavg.z * aw};
+// One star of a layer, as starLayer finds it in lattice cell c (sky.glsl:79-92): the unit
+// direction q / |q|, flux F and colour sc. Lane-independent: computed once per warp.
+struct StarSlot {
+    float qx, qy, qz, F, r, g, b;
+    int cx, cy, cz;
+};
+
+struct Layer {
+    float N, inv_n, prob, flux, s_in2, s_out2, cull_lo, cull_hi;
+    uint32_t salt, sy, sz;
+};
+
+__device__ __forceinline__ Layer make_layer(float N, float prob, float flux, uint32_t salt) {
+    Layer L;
+    L.N = N;
+    L.inv_n = 1.0f / N;
+    L.prob = prob;
+    L.flux = flux;
+    const float s_in = 1.0f - 0.5f / N, s_out = 1.0f + 0.5f / N;
+    L.s_in2 = s_in * s_in;
+    L.s_out2 = s_out * s_out;
+    // a cell whose cube [c, c + 1) / N misses the shell holds no star: skipped before hashing
+    // (conservative, with a relative margin of 1e-4)
+    L.cull_lo = L.s_out2 * 1.0001f;
+    L.cull_hi = L.s_in2 * 0.9999f;
+    L.salt = salt;
+    L.sy = salt * 7u + 1u;
+    L.sz = salt * 13u + 2u;
+    return L;
+}
+
+// The star of cell (cx, cy, cz), if it is lit (ux <= prob) and on the shell.
+__device__ bool star_of_cell(const Tex& tx, const ShadeArgs& A, const Layer& L, float g_shift, int cx, int cy, int cz,
+                             StarSlot& st) {
+    const float lx = float(cx) * L.inv_n, ly = float(cy) * L.inv_n, lz = float(cz) * L.inv_n;
+    const float hx = lx + L.inv_n, hy = ly + L.inv_n, hz = lz + L.inv_n;
+    const float nx = fminf(fmaxf(0.0f, lx), hx), ny = fminf(fmaxf(0.0f, ly), hy), nz = fminf(fmaxf(0.0f, lz), hz);
+    const float fx = fmaxf(lx * lx, hx * hx), fy = fmaxf(ly * ly, hy * hy), fz = fmaxf(lz * lz, hz * hz);
+    if (nx * nx + ny * ny + nz * nz > L.cull_lo || fx + fy + fz < L.cull_hi) return false;
+    const uint3 h = pcg3d(make_uint3(uint32_t(cx) + L.salt, uint32_t(cy) + L.sy, uint32_t(cz) + L.sz));
+    const float k16 = 1.0f / 65536.0f;
+    const float ux = float(h.x >> 16) * k16;
+    if (ux > L.prob) return false;
+    const float q0 = (float(cx) + float(h.x & 0xffffu) * k16) * L.inv_n;
+    const float q1 = (float(cy) + float(h.y >> 16) * k16) * L.inv_n;
+    const float q2 = (float(cz) + float(h.y & 0xffffu) * k16) * L.inv_n;
+    const float ql2 = q0 * q0 + q1 * q1 + q2 * q2;
+    if (ql2 < L.s_in2 || ql2 > L.s_out2) return false;
+    const float iq = 1.0f / sqrtf(ql2);
+    const float uy = float(h.z >> 16) * k16, uz = float(h.z & 0xffffu) * k16;
+    st.qx = q0 * iq;
+    st.qy = q1 * iq;
+    st.qz = q2 * iq;
+    st.F = L.flux / fmaxf(uy, 2e-4f);  // flux * pow(max(u.y, 2e-4), -1)
+    const float T = expf(mixf(A.ln_3000, A.ln_22000, powf(uz, 1.7f)));
+    const float4 bb = blackbody(tx, T * g_shift);
+    st.r = mixf(1.0f, bb.x, 0.7f);
+    st.g = mixf(1.0f, bb.y, 0.7f);
+    st.b = mixf(1.0f, bb.z, 0.7f);
+    st.cx = cx;
+    st.cy = cy;
+    st.cz = cz;
+    return true;
+}
+
+// A pixel's per-layer constants: the covariance of its star Gaussians (sky.glsl:66-73).
+struct LanePart {
+    float isaa, isab, isbb, norm;
+    F3 d;
+    const Footprint* fp;
+};
+
+__device__ __forceinline__ void star_add(const StarSlot& t, const LanePart& P, F3& sum) {
+    const F3 delta{t.qx - P.d.x, t.qy - P.d.y, t.qz - P.d.z};
+    const float d1 = dot(P.fp->e1, delta), d2 = dot(P.fp->e2, delta);
+    const float sp = P.fp->r11 * d1 + P.fp->r12 * d2;
+    const float sq = P.fp->r22 * d2;
+    const float e = P.isaa * sp * sp + 2.0f * P.isab * sp * sq + P.isbb * sq * sq;
+    if (!(e < 30.0f)) return;  // also skips NaN
+    const float k = t.F * P.norm * expf(-0.5f * e);
+    sum = add(sum, F3{t.r * k, t.g * k, t.b * k});
+}
+
+constexpr int kMaxBox = 1024;  // union boxes of up to this many cells are scanned by the warp
+
+// warp-wide min / max by xor butterflies (every lane gets the result)
+__device__ __forceinline__ int warp_min(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// sky.glsl:54-103 starLayer for the 32 pixels of a warp (all lanes call it; `active` lanes
+// are escaped pixels). A pixel's stars come from the 27 cells around c0 = floor(d N), summed in
+// the order z, y, x of the cell. The warp scans the union box of its pixels' cells in that same
+// lexicographic order, 32 cells at a time: each lane hashes one cell, the lit stars on the
+// shell are compacted into shared memory, then every lane adds those inside its own 27 cells.
+// A pixel therefore sums exactly the stars, in exactly the order, of its own loop. Warps whose
+// box is larger (directions spread wide near the photon ring) run the per-pixel loop.
+__device__ F3 star_layer_warp(const Tex& tx, const ShadeArgs& A, bool active, F3 d, const Footprint& fp,
+                              const Layer& L, float sig_star, float omega0, float g_shift, StarSlot* list) {
+    const int lane = threadIdx.x & 31;
+    float w = 1.0f;
+    F3 avg{0.f, 0.f, 0.f};
+    LanePart P{0.f, 0.f, 0.f, 0.f, d, &fp};
+    int c0x = 0, c0y = 0, c0z = 0;
+    bool loop = false;
+    if (active) {
+        const float footprint_cells = powf(fp.det, 0.25f) * L.N;
+        w = smoothstep(0.8f, 2.5f, footprint_cells);
+        const float4 bavg = blackbody(tx, 5600.0f * g_shift);
+        const float aw = L.prob * L.N * L.N * 9.517f * L.flux * omega0;
+        avg = F3{bavg.x * aw, bavg.y * aw, bavg.z * aw};
+        loop = w < 1.0f;
+        if (loop) {
+            const float s2 = sig_star * sig_star;
+            const float px2 = 0.45f;
+            const float saa = px2 + s2 * fp.gi11, sab = s2 * fp.gi12, sbb = px2 + s2 * fp.gi22;
+            const float det_s = px2 * px2 + px2 * s2 * (fp.gi11 + fp.gi22) + s2 * s2 * fp.det_gi;
+            const float inv_det_s = 1.0f / det_s;
+            P.isaa = sbb * inv_det_s;
+            P.isab = -sab * inv_det_s;
+            P.isbb = saa * inv_det_s;
+            P.norm = fp.mu / (kTwoPi * sqrtf(det_s));
+            c0x = int(floorf(d.x * L.N));
+            c0y = int(floorf(d.y * L.N));
+            c0z = int(floorf(d.z * L.N));
+        }
+    }
     F3 sum{0.f, 0.f, 0.f};
-    if (w < 1.0f) {
-        const float s2 = sig_star * sig_star;
-        const float px2 = 0.45f;
-        const float saa = px2 + s2 * fp.gi11, sab = s2 * fp.gi12, sbb = px2 + s2 * fp.gi22;
-        const float det_s = px2 * px2 + px2 * s2 * (fp.gi11 + fp.gi22) + s2 * s2 * fp.det_gi;
-        const float inv_det_s = 1.0f / det_s;
-        const float isaa = sbb * inv_det_s, isab = -sab * inv_det_s, isbb = saa * inv_det_s;
-        const float norm = fp.mu / (kTwoPi * sqrtf(det_s));
-        const int c0x = int(floorf(d.x * N)), c0y = int(floorf(d.y * N)), c0z = int(floorf(d.z * N));
-        const float s_in = 1.0f - 0.5f / N, s_out = 1.0f + 0.5f / N;
-        const float s_in2 = s_in * s_in, s_out2 = s_out * s_out;
-        const float k16 = 1.0f / 65536.0f;
-        const uint32_t sy = salt * 7u + 1u, sz = salt * 13u + 2u;
+    const unsigned any_loop = __ballot_sync(0xffffffffu, loop);
+    if (any_loop != 0u) {
+        const int bx = warp_min(loop ? c0x - 1 : INT_MAX);
+        const int by = warp_min(loop ? c0y - 1 : INT_MAX);
+        const int bz = warp_min(loop ? c0z - 1 : INT_MAX);
+        const int ex = warp_max(loop ? c0x + 1 : INT_MIN);
+        const int ey = warp_max(loop ? c0y + 1 : INT_MIN);
+        const int ez = warp_max(loop ? c0z + 1 : INT_MIN);
+        const long long nx = (long long)ex - bx + 1, ny = (long long)ey - by + 1, nz = (long long)ez - bz + 1;
+        if (nx * ny * nz <= kMaxBox) {
+            const int vol = int(nx * ny * nz), sx = int(nx), sxy = int(nx * ny);
+            for (int base = 0; base < vol; base += 32) {
+                const int cell = base + lane;
+                StarSlot st;
+                bool star = false;
+                if (cell < vol)
+                    star = star_of_cell(tx, A, L, g_shift, bx + cell % sx, by + (cell % sxy) / sx, bz + cell / sxy, st);
+                const unsigned m = __ballot_sync(0xffffffffu, star);
+                if (star) list[__popc(m & ((1u << lane) - 1u))] = st;
+                __syncwarp();
+                const int n = __popc(m);
+                if (loop) {
+                    for (int s = 0; s < n; ++s) {
+                        const StarSlot t = list[s];
+                        if (abs(t.cx - c0x) <= 1 && abs(t.cy - c0y) <= 1 && abs(t.cz - c0z) <= 1) star_add(t, P, sum);
+                    }
+                }
+                __syncwarp();
+            }
+        } else if (loop) {
 #pragma unroll 1
-        for (int cell = 0; cell < 27; ++cell) {
-            const int cx = c0x + cell % 3 - 1, cy = c0y + (cell / 3) % 3 - 1, cz = c0z + cell / 9 - 1;
-            const uint3 h = pcg3d(make_uint3(uint32_t(cx) + salt, uint32_t(cy) + sy, uint32_t(cz) + sz));
-            const float ux = float(h.x >> 16) * k16;
-            if (ux > prob) continue;
-            const float q0 = (float(cx) + float(h.x & 0xffffu) * k16) / N;
-            const float q1 = (float(cy) + float(h.y >> 16) * k16) / N;
-            const float q2 = (float(cz) + float(h.y & 0xffffu) * k16) / N;
-            const float ql2 = q0 * q0 + q1 * q1 + q2 * q2;
-            if (ql2 < s_in2 || ql2 > s_out2) continue;
-            const float iq = 1.0f / sqrtf(ql2);
-            const F3 delta{q0 * iq - d.x, q1 * iq - d.y, q2 * iq - d.z};
-            const float d1 = dot(fp.e1, delta), d2 = dot(fp.e2, delta);
-            const float sp = fp.r11 * d1 + fp.r12 * d2;
-            const float sq = fp.r22 * d2;
-            const float e = isaa * sp * sp + 2.0f * isab * sp * sq + isbb * sq * sq;
-            if (!(e < 30.0f)) continue;
-            const float uy = float(h.z >> 16) * k16, uz = float(h.z & 0xffffu) * k16;
-            const float F = flux * powf(fmaxf(uy, 2e-4f), -1.0f);
-            const float T = expf(mixf(logf(3000.0f), logf(22000.0f), powf(uz, 1.7f)));
-            const float4 bb = blackbody(tx, T * g_shift);
-            const float k = F * norm * expf(-0.5f * e);
-            sum = add(sum, F3{mixf(1.0f, bb.x, 0.7f) * k, mixf(1.0f, bb.y, 0.7f) * k, mixf(1.0f, bb.z, 0.7f) * k});
+            for (int cell = 0; cell < 27; ++cell) {
+                StarSlot t;
+                if (star_of_cell(tx, A, L, g_shift, c0x + cell % 3 - 1, c0y + (cell / 3) % 3 - 1, c0z + cell / 9 - 1, t))
+                    star_add(t, P, sum);
+            }
         }
     }
     if (!isfinite(sum.x) || !isfinite(sum.y) || !isfinite(sum.z)) sum = F3{0.f, 0.f, 0.f};
@@ -307,15 +434,23 @@ __device__ __forceinline__ F3 primary_dir(const ShadeArgs& A, int i, int j) {
                         B[2] * dc.x + B[5] * dc.y + B[8] * dc.z});
 }
 
+// Fine derivative over the quad: v(odd) - v(even) along the axis whose partner is lane ^ mask.
+__device__ __forceinline__ F3 quad_diff(F3 v, int lane, int mask) {
+    const F3 o{__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask),
+               __shfl_xor_sync(0xffffffffu, v.z, mask)};
+    return (lane & mask) ? sub(v, o) : sub(o, v);
+}
+
+// A block is 4 x 2 warps, a warp 8 x 4 pixels (lane = 8 y + x): the 2x2 quads of the
+// rasteriser (even-aligned) sit inside a warp, with partners at lane ^ 1 (x) and lane ^ 8 (y).
 __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ ShadeArgs A) {
     __shared__ float4 s_lut[kLut];
-    __shared__ float s_esc[3][kBY][kBX];
-    __shared__ float s_dir[3][kBY][kBX];
-    __shared__ int s_e[kBY][kBX];
-    const int tid = threadIdx.y * kBX + threadIdx.x;
+    __shared__ StarSlot s_star[kBX * kBY / 32][32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int k = tid; k < kLut; k += kBX * kBY) s_lut[k] = A.lut[k];
-    const Tex tx{A.noise, s_lut};
-    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    const Tex tx{A.noise, s_lut, A.ln_1000, A.ln_40000};
+    const int i = blockIdx.x * kBX + (warp & 3) * 8 + (lane & 7);
+    const int j = blockIdx.y * kBY + (warp >> 2) * 4 + (lane >> 3);
     const bool in = i < A.width && j < A.height;
     const bhr_shade_params& P = A.p;
     const F3 cam{A.cam[0], A.cam[1], A.cam[2]};
@@ -338,9 +473,9 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
             const float cr[3] = {w2.z, w2.w, w3.x}, cp[3] = {w3.y, w3.z, w3.w};
             const float b_axis = w2.x;
             for (int k = 0; k < ncross && k < 3; ++k) {
-                const float4 d = thin_disk_sample(tx, A, cr[k], cp[k], b_axis, rcam);
-                col = add(col, F3{trans * d.x * d.w, trans * d.y * d.w, trans * d.z * d.w});
-                trans *= 1.0f - d.w;
+                const float4 dk = thin_disk_sample(tx, A, cr[k], cp[k], b_axis, rcam);
+                col = add(col, F3{trans * dk.x * dk.w, trans * dk.y * dk.w, trans * dk.z * dk.w});
+                trans *= 1.0f - dk.w;
                 if (trans < 0.004f) {
                     opaque = true;
                     break;
@@ -350,32 +485,33 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
         if (status == BHR_STATUS_ESCAPED) esc_dir = F3{w0.z, w0.w, w1.x};
         esc = status == BHR_STATUS_ESCAPED && !opaque;
     }
-    const int tx_ = threadIdx.x, ty_ = threadIdx.y;
-    s_esc[0][ty_][tx_] = esc_dir.x;
-    s_esc[1][ty_][tx_] = esc_dir.y;
-    s_esc[2][ty_][tx_] = esc_dir.z;
-    s_dir[0][ty_][tx_] = dir.x;
-    s_dir[1][ty_][tx_] = dir.y;
-    s_dir[2][ty_][tx_] = dir.z;
-    s_e[ty_][tx_] = esc ? 1 : 0;
-    __syncthreads();
-    if (!in) return;
+    // blackhole.frag:297-306: derivatives of escDir; the unlensed footprint where a quad mixes
+    // escaped and other pixels (a partner outside the image counts as not escaped)
+    // (both shuffles run in every lane: a short-circuit || would leave lanes out of the second
+    // full-mask shuffle, which is undefined)
+    const int e = esc ? 1 : 0;
+    const int ex = __shfl_xor_sync(0xffffffffu, e, 1);
+    const int ey = __shfl_xor_sync(0xffffffffu, e, 8);
+    const bool mixed = ex != e || ey != e;
+    const F3 ddx_l = quad_diff(esc_dir, lane, 1), ddy_l = quad_diff(esc_dir, lane, 8);
+    const F3 ddx_0 = quad_diff(dir, lane, 1), ddy_0 = quad_diff(dir, lane, 8);
+    const F3 ddx = mixed ? ddx_0 : ddx_l, ddy = mixed ? ddy_0 : ddy_l;
 
     const float pixel_angle = 2.0f * A.tan_half / float(A.height);
     const float omega0 = pixel_angle * pixel_angle;
     const float g = mixf(1.0f, 1.0f / sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f)), P.doppler_strength);
     const float g4 = g * g * g * g;
+    Footprint fp{};
+    if (esc) fp = make_footprint(esc_dir, ddx, ddy, omega0);
+    const float sb = P.star_brightness * g4;
+    StarSlot* list = s_star[warp];
+    const F3 s1 = star_layer_warp(tx, A, esc, esc_dir, fp, make_layer(200.0f, 0.40f * P.star_density, 0.0045f * sb, 11u),
+                                  0.0004f, omega0, g, list);
+    const F3 s2 = star_layer_warp(tx, A, esc, esc_dir, fp, make_layer(48.0f, 0.25f * P.star_density, 0.06f * sb, 23u),
+                                  0.0011f, omega0, g, list);
+    if (!in) return;
     float alpha = 0.0f;
     if (esc) {
-        const int x0 = tx_ & ~1, x1 = x0 + 1, y0 = ty_ & ~1, y1 = y0 + 1;
-        const bool mixed = s_e[ty_][x0] != s_e[ty_][x1] || s_e[y0][tx_] != s_e[y1][tx_];
-        const float(*src)[kBY][kBX] = mixed ? s_dir : s_esc;
-        const F3 ddx{src[0][ty_][x1] - src[0][ty_][x0], src[1][ty_][x1] - src[1][ty_][x0], src[2][ty_][x1] - src[2][ty_][x0]};
-        const F3 ddy{src[0][y1][tx_] - src[0][y0][tx_], src[1][y1][tx_] - src[1][y0][tx_], src[2][y1][tx_] - src[2][y0][tx_]};
-        const Footprint fp = make_footprint(esc_dir, ddx, ddy, omega0);
-        const float sb = P.star_brightness * g4;
-        const F3 s1 = star_layer(tx, esc_dir, fp, 200.0f, 0.40f * P.star_density, 0.0045f * sb, 0.0004f, omega0, 11u, g);
-        const F3 s2 = star_layer(tx, esc_dir, fp, 48.0f, 0.25f * P.star_density, 0.06f * sb, 0.0011f, omega0, 23u, g);
         const F3 sky = add(s1, s2);
         col = add(col, F3{trans * sky.x, trans * sky.y, trans * sky.z});
         alpha = trans * (P.sky_brightness * g4);
@@ -455,7 +591,7 @@ cudaError_t launch_noise_bake(uint32_t seed, uint16_t* out, cudaStream_t st) {
 
 cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t st) {
     const dim3 grid((a.width + kBX - 1) / kBX, (a.height + kBY - 1) / kBY);
-    k_shade<<<grid, dim3(kBX, kBY), 0, st>>>(a);
+    k_shade<<<grid, kBX * kBY, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -18,6 +18,7 @@ struct ShadeArgs {
     int32_t disk_thin;  // uDiskMode == DISK_THIN
     int32_t far_mode;
     bhr_shade_params p;
+    float ln_1000, ln_40000, ln_3000, ln_22000;  // logf of the constants, from the host's libm
     const bhr_hit* hits;
     float4* out;
     const uint16_t* noise;  // BHR_NOISE_SIZE^3 half

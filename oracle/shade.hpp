@@ -40,7 +40,8 @@ inline float length(F3 a) { return std::sqrt(dot(a, a)); }
 inline F3 divs(F3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
 inline F3 normalize(F3 a) { return divs(a, length(a)); }
 inline float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }  // GLSL mix
-inline float clampf(float x, float lo, float hi) { return std::min(std::max(x, lo), hi); }
+// min / max as fminf / fmaxf (and the GPU's FMNMX): a NaN operand yields the other one
+inline float clampf(float x, float lo, float hi) { return std::fmin(std::fmax(x, lo), hi); }
 inline float smoothstep(float e0, float e1, float x) {
     const float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
     return t * t * (3.0f - 2.0f * t);
@@ -61,7 +62,7 @@ inline F3 grad3(int cx, int cy, int cz, uint32_t salt) {
     const U3 h = pcg3d({uint32_t(cx) + salt, uint32_t(cy) + (salt * 3u + 11u), uint32_t(cz) + (salt * 7u + 29u)});
     const float s = 1.0f / 4294967296.0f;
     const F3 g{float(h.x) * s * 2.0f - 1.0f, float(h.y) * s * 2.0f - 1.0f, float(h.z) * s * 2.0f - 1.0f};
-    return g * (1.0f / std::sqrt(std::max(dot(g, g), 1e-8f)));
+    return g * (1.0f / std::sqrt(std::fmax(dot(g, g), 1e-8f)));
 }
 inline float pgnoise3(F3 p, int period, uint32_t salt) {
     const F3 i{std::floor(p.x), std::floor(p.y), std::floor(p.z)};
@@ -170,9 +171,9 @@ inline void blackbody_lut(float* out) {
         const double T = std::exp(lo + (hi - lo) * (double(i) / (kLutN - 1)));
         double X, Y, Z;
         xyz_of(T, X, Y, Z);
-        const double r = std::max(3.2406 * X - 1.5372 * Y - 0.4986 * Z, 0.0);
-        const double g = std::max(-0.9689 * X + 1.8758 * Y + 0.0415 * Z, 0.0);
-        const double b = std::max(0.0557 * X - 0.2040 * Y + 1.0570 * Z, 0.0);
+        const double r = std::fmax(3.2406 * X - 1.5372 * Y - 0.4986 * Z, 0.0);
+        const double g = std::fmax(-0.9689 * X + 1.8758 * Y + 0.0415 * Z, 0.0);
+        const double b = std::fmax(0.0557 * X - 0.2040 * Y + 1.0570 * Z, 0.0);
         const double lum = 0.2126 * r + 0.7152 * g + 0.0722 * b;
         const double inv = lum > 0.0 ? 1.0 / lum : 0.0;
         out[4 * i + 0] = float(r * inv);
@@ -220,16 +221,16 @@ inline float noise_sample(const Tex& tx, F3 c) {
 }
 
 inline float disk_temp_profile(float r_in, float r) {
-    const float x = r_in / std::max(r, r_in);
-    const float f = std::pow(x, 0.75f) * std::pow(std::max(1.0f - std::sqrt(x), 0.0f), 0.25f);
+    const float x = r_in / std::fmax(r, r_in);
+    const float f = std::pow(x, 0.75f) * std::pow(std::fmax(1.0f - std::sqrt(x), 0.0f), 0.25f);
     return f / 0.48796f;
 }
 inline float kepler_omega(float r) { return std::pow(r, -1.5f); }
 inline float redshift_factor(float r, float b_axis, float rcam) {
     const float omega = kepler_omega(r);
-    const float ut = 1.0f / std::sqrt(std::max(1.0f - 3.0f / r, 0.02f));
-    const float lapse = std::sqrt(std::max(1.0f - 2.0f / rcam, 1e-4f));
-    return 1.0f / (lapse * ut * std::max(1.0f - omega * b_axis, 0.05f));
+    const float ut = 1.0f / std::sqrt(std::fmax(1.0f - 3.0f / r, 0.02f));
+    const float lapse = std::sqrt(std::fmax(1.0f - 2.0f / rcam, 1e-4f));
+    return 1.0f / (lapse * ut * std::fmax(1.0f - omega * b_axis, 0.05f));
 }
 inline float glsl_mod(float x, float y) { return x - y * std::floor(x / y); }
 
@@ -240,7 +241,7 @@ inline float disk_noise(const Tex& tx, const bhr_shade_params& P, float r, float
     const float t1 = glsl_mod(t, Pd);
     const float t2 = glsl_mod(t + 0.5f * Pd, Pd);
     const float w2 = std::fabs(2.0f * t1 / Pd - 1.0f);
-    const float rep = std::max(1.0f, std::floor(2.0f * P.disk_noise_scale + 0.5f));
+    const float rep = std::fmax(1.0f, std::floor(2.0f * P.disk_noise_scale + 0.5f));
     const float lr = std::log(r) * 3.2f * P.disk_noise_scale;
     const float yy = y_over_h * 0.35f;
     const float k = rep / kTwoPi;
@@ -249,14 +250,14 @@ inline float disk_noise(const Tex& tx, const bhr_shade_params& P, float r, float
     return mixf(noise_sample(tx, c1), noise_sample(tx, c2), w2);
 }
 inline float optical_depth_scale(const bhr_shade_params& P, float r, float g_phys, float rcam) {
-    const float lapse_em = std::sqrt(std::max(1.0f - 2.0f / r, 1e-4f));
-    const float lapse_cam = std::sqrt(std::max(1.0f - 2.0f / rcam, 1e-4f));
+    const float lapse_em = std::sqrt(std::fmax(1.0f - 2.0f / r, 1e-4f));
+    const float lapse_cam = std::sqrt(std::fmax(1.0f - 2.0f / rcam, 1e-4f));
     return mixf(1.0f, lapse_em / (g_phys * lapse_cam), P.doppler_strength);
 }
 inline float disk_radial_profile(float r_in, float r_out, float r) {
     const float inner = smoothstep(r_in, r_in + 0.25f, r);
     const float outer = 1.0f - smoothstep(r_out * 0.55f, r_out, r);
-    return inner * outer * std::pow(r_in / std::max(r, r_in), 1.2f);
+    return inner * outer * std::pow(r_in / std::fmax(r, r_in), 1.2f);
 }
 
 // thinDiskSample at a recorded crossing (r = |hit.xz|, phi = atan(hit.z, hit.x))
@@ -287,12 +288,12 @@ inline Footprint make_footprint(F3 d, F3 a, F3 b, float omega0) {
     Footprint f;
     const float min_axis = 1e-3f * std::sqrt(omega0);
     const float la_raw = length(a);
-    const float la = std::max(la_raw, min_axis);
+    const float la = std::fmax(la_raw, min_axis);
     f.e1 = la_raw > 1e-12f ? divs(a, la_raw) : normalize(cross(d, F3{1e-3f, 1.0f + 1e-3f, 1e-3f}));
     const float b1 = dot(b, f.e1);
     const F3 bp = b - f.e1 * b1;
     const float lbp_raw = length(bp);
-    const float lbp = std::max(lbp_raw, min_axis);
+    const float lbp = std::fmax(lbp_raw, min_axis);
     f.e2 = lbp_raw > 1e-3f * min_axis ? divs(bp, lbp_raw) : normalize(cross(d, f.e1));
     f.r11 = 1.0f / la;
     f.r12 = -b1 / (la * lbp);
@@ -303,7 +304,7 @@ inline Footprint make_footprint(F3 d, F3 a, F3 b, float omega0) {
     f.det_gi = (f.r11 * f.r22) * (f.r11 * f.r22);
     const float area = la * lbp;
     f.det = area * area;
-    f.mu = std::min(omega0 / area, 1e4f);
+    f.mu = std::fmin(omega0 / area, 1e4f);
     return f;
 }
 
@@ -329,6 +330,7 @@ inline F3 star_layer(const Tex& tx, F3 d, const Footprint& fp, float N, float pr
         const float s_in = 1.0f - 0.5f / N, s_out = 1.0f + 0.5f / N;
         const float s_in2 = s_in * s_in, s_out2 = s_out * s_out;
         const float k16 = 1.0f / 65536.0f;
+        const float inv_n = 1.0f / N;  // (c + u2) / N as a product, pow(x, -1) as 1 / x
         for (int dz = -1; dz <= 1; ++dz)
             for (int dy = -1; dy <= 1; ++dy)
                 for (int dx = -1; dx <= 1; ++dx) {
@@ -339,7 +341,7 @@ inline F3 star_layer(const Tex& tx, F3 d, const Footprint& fp, float N, float pr
                     if (ux > prob) continue;
                     const F3 u2{float(h.x & 0xffffu) * k16, float(h.y >> 16u) * k16, float(h.y & 0xffffu) * k16};
                     const float uy = float(h.z >> 16u) * k16, uz = float(h.z & 0xffffu) * k16;
-                    const F3 q{(float(c[0]) + u2.x) / N, (float(c[1]) + u2.y) / N, (float(c[2]) + u2.z) / N};
+                    const F3 q{(float(c[0]) + u2.x) * inv_n, (float(c[1]) + u2.y) * inv_n, (float(c[2]) + u2.z) * inv_n};
                     const float ql2 = dot(q, q);
                     if (ql2 < s_in2 || ql2 > s_out2) continue;
                     const F3 delta = q * (1.0f / std::sqrt(ql2)) - d;
@@ -348,7 +350,7 @@ inline F3 star_layer(const Tex& tx, F3 d, const Footprint& fp, float N, float pr
                     const float sq = fp.r22 * d2;
                     const float e = isaa * sp * sp + 2.0f * isab * sp * sq + isbb * sq * sq;
                     if (!(e < 30.0f)) continue;
-                    const float F = flux * std::pow(std::max(uy, 2e-4f), -1.0f);
+                    const float F = flux / std::fmax(uy, 2e-4f);
                     const float T = std::exp(mixf(std::log(3000.0f), std::log(22000.0f), std::pow(uz, 1.7f)));
                     const RGBA bb = blackbody(tx, T * g_shift);
                     const float k = F * norm * std::exp(-0.5f * e);
@@ -356,7 +358,7 @@ inline F3 star_layer(const Tex& tx, F3 d, const Footprint& fp, float N, float pr
                 }
     }
     if (!std::isfinite(sum.x) || !std::isfinite(sum.y) || !std::isfinite(sum.z)) sum = {0, 0, 0};
-    sum = {std::min(sum.x, 64.0f), std::min(sum.y, 64.0f), std::min(sum.z, 64.0f)};
+    sum = {std::fmin(sum.x, 64.0f), std::fmin(sum.y, 64.0f), std::fmin(sum.z, 64.0f)};
     return {mixf(sum.x, avg.x, w), mixf(sum.y, avg.y, w), mixf(sum.z, avg.z, w)};
 }
 
@@ -372,7 +374,7 @@ inline F3 primary_dir(const bhr_view& v, int i, int j) {
 }
 
 inline float shadow_angular_radius(float r) {
-    const float s = std::min(1.0f, 5.19615242270663f / r * std::sqrt(std::max(1.0f - 2.0f / r, 0.0f)));
+    const float s = std::fmin(1.0f, 5.19615242270663f / r * std::sqrt(std::fmax(1.0f - 2.0f / r, 0.0f)));
     const float a = std::asin(s);
     return r >= 3.0f ? a : kPi - a;
 }
@@ -418,7 +420,7 @@ inline void shade_view(const Tex& tx, const bhr_shade_params& P, const bhr_view&
     const float tan_half = v.tan_half_fov;
     const float pixel_angle = 2.0f * tan_half / float(H);
     const float omega0 = pixel_angle * pixel_angle;
-    const float g = mixf(1.0f, 1.0f / std::sqrt(std::max(1.0f - 2.0f / rcam, 1e-4f)), P.doppler_strength);
+    const float g = mixf(1.0f, 1.0f / std::sqrt(std::fmax(1.0f - 2.0f / rcam, 1e-4f)), P.doppler_strength);
     const float g4 = g * g * g * g;
     auto state = [&](int i, int j) {
         return composite_disk(tx, P, v, hits[int64_t(j) * W + i], i, j, rcam);
@@ -472,9 +474,9 @@ inline void shade_view(const Tex& tx, const bhr_shade_params& P, const bhr_view&
                 alpha = 0.0f;
             }
             float* o = rgba + 4 * (int64_t(j) * W + i);
-            o[0] = std::max(col.x, 0.0f);
-            o[1] = std::max(col.y, 0.0f);
-            o[2] = std::max(col.z, 0.0f);
+            o[0] = std::fmax(col.x, 0.0f);
+            o[1] = std::fmax(col.y, 0.0f);
+            o[2] = std::fmax(col.z, 0.0f);
             o[3] = alpha;
         }
 }

@@ -126,6 +126,33 @@ def test_surrogate_records_shade_like_the_plain_ones(tracer, tex):
     assert abs(lum_s.sum() / lum_p.sum() - 1.0) < 1e-2
 
 
+def test_non_finite_records(tracer, tex):
+    """Records with NaN and infinite directions and crossing radii shade as the restatement
+    shades them (finite images, no star light along a NaN direction)."""
+    import torch
+
+    v = workloads.c1_view(TERM_CONFIG)
+    (h,) = tracer.trace([v])
+    torch.cuda.synchronize()
+    hits = hits_numpy(h.cpu()).copy()
+    rng = np.random.default_rng(4)
+    k = rng.choice(hits.size, 200, replace=False)
+    hits["dir"][k[:80], 0] = np.nan
+    hits["dir"][k[80:120], 1] = np.inf
+    hits["cross_r"][k[120:160], 0] = np.nan
+    hits["ncross"][k[120:160]] = 1
+    hits["cross_phi"][k[160:], 0] = -np.inf
+    hits["ncross"][k[160:]] = 1
+    hd = torch.from_numpy(hits.view(np.uint8)).cuda()
+    p = shade_params()
+    (img,) = tracer.shade([v], [hd], p)
+    torch.cuda.synchronize()
+    img = img.cpu().numpy()
+    ref = O.shade_view(v, hits, p, *tex)
+    assert np.all(np.isfinite(img)) and np.all(np.isfinite(ref))
+    _compare(img, ref, "non-finite records")
+
+
 def test_shade_argument_errors(tracer):
     import torch
 
