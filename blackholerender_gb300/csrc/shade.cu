@@ -47,6 +47,12 @@ __device__ __forceinline__ float smoothstep(float e0, float e1, float x) {
     return t * t * (3.0f - 2.0f * t);
 }
 
+// exp, log and pow of the shading: the SFU approximations, as GLSL's exp / log / pow compile to
+// on the GPU (a few ulp; the noise bake uses none of them and stays exact)
+__device__ __forceinline__ float gexp(float x) { return __expf(x); }
+__device__ __forceinline__ float glog(float x) { return __logf(x); }
+__device__ __forceinline__ float gpow(float x, float y) { return __powf(x, y); }
+
 // common.glsl:16-22 pcg3d, the three lanes updated in sequence
 __device__ __forceinline__ uint3 pcg3d(uint3 v) {
     v.x = v.x * 1664525u + 1013904223u;
@@ -129,7 +135,7 @@ struct Tex {
 // blackbody.glsl:7-16: log-temperature lookup, linear filter, clamp to edge; Wien-tail fade
 __device__ __forceinline__ float4 blackbody(const Tex& tx, float T) {
     const float Tc = clampf(T, 1000.0f, 40000.0f);
-    const float t = (logf(Tc) - tx.ln_1000) / (tx.ln_40000 - tx.ln_1000);
+    const float t = (glog(Tc) - tx.ln_1000) / (tx.ln_40000 - tx.ln_1000);
     const float u = t * float(kLut) - 0.5f;
     const float fl = floorf(u);
     const float a = u - fl;
@@ -163,14 +169,14 @@ __device__ __forceinline__ float glsl_mod(float x, float y) { return x - y * flo
 
 // disk.glsl:45-63 diskNoise at the mid-plane (yOverH = 0)
 __device__ float disk_noise(const Tex& tx, const bhr_shade_params& P, float r, float phi) {
-    const float omega = powf(r, -1.5f);
+    const float omega = gpow(r, -1.5f);
     const float t = P.disk_time;
     const float Pd = 60.0f;
     const float t1 = glsl_mod(t, Pd);
     const float t2 = glsl_mod(t + 0.5f * Pd, Pd);
     const float w2 = fabsf(2.0f * t1 / Pd - 1.0f);
     const float rep = fmaxf(1.0f, floorf(2.0f * P.disk_noise_scale + 0.5f));
-    const float lr = logf(r) * 3.2f * P.disk_noise_scale;
+    const float lr = glog(r) * 3.2f * P.disk_noise_scale;
     const float yy = 0.0f * 0.35f;
     const float k = rep / kTwoPi;
     const F3 c1{(phi + omega * t1) * k, lr + P.disk_inflow * omega * t1, yy};
@@ -190,14 +196,14 @@ __device__ float4 thin_disk_sample(const Tex& tx, const ShadeArgs& A, float r, f
     const float r_in = A.disk_inner, r_out = A.disk_outer;
     const float inner = smoothstep(r_in, r_in + 0.25f, r);
     const float outer = 1.0f - smoothstep(r_out * 0.55f, r_out, r);
-    const float radial = inner * outer * powf(r_in / fmaxf(r, r_in), 1.2f);
+    const float radial = inner * outer * gpow(r_in / fmaxf(r, r_in), 1.2f);
     const float dens = P.disk_density * radial * pattern;
     // diskTempProfile (disk.glsl:26-30)
     const float x = r_in / fmaxf(r, r_in);
-    const float prof = powf(x, 0.75f) * powf(fmaxf(1.0f - sqrtf(x), 0.0f), 0.25f) / 0.48796f;
+    const float prof = gpow(x, 0.75f) * gpow(fmaxf(1.0f - sqrtf(x), 0.0f), 0.25f) / 0.48796f;
     const float T = P.disk_peak_temp * prof * mixf(1.0f, 0.85f + 0.3f * emit, 0.5f);
     // redshiftFactor (disk.glsl:36-41)
-    const float omega = powf(r, -1.5f);
+    const float omega = gpow(r, -1.5f);
     const float ut = 1.0f / sqrtf(fmaxf(1.0f - 3.0f / r, 0.02f));
     const float lapse = sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f));
     const float g_phys = 1.0f / (lapse * ut * fmaxf(1.0f - omega * b_axis, 0.05f));
@@ -206,7 +212,7 @@ __device__ float4 thin_disk_sample(const Tex& tx, const ShadeArgs& A, float r, f
     // opticalDepthScale (disk.glsl:67-71)
     const float lapse_em = sqrtf(fmaxf(1.0f - 2.0f / r, 1e-4f));
     const float ods = mixf(1.0f, lapse_em / (g_phys * lapse), P.doppler_strength);
-    const float alpha = 1.0f - expf(-dens * P.disk_opacity * 0.6f * ods);
+    const float alpha = 1.0f - gexp(-dens * P.disk_opacity * 0.6f * ods);
     // diskTint (disk.glsl:21)
     const float w = P.disk_warmth;
     const float s = bb.w * P.disk_brightness * emit;
@@ -298,7 +304,7 @@ __device__ bool star_of_cell(const Tex& tx, const ShadeArgs& A, const Layer& L, 
     st.qy = q1 * iq;
     st.qz = q2 * iq;
     st.F = L.flux / fmaxf(uy, 2e-4f);  // flux * pow(max(u.y, 2e-4), -1)
-    const float T = expf(mixf(A.ln_3000, A.ln_22000, powf(uz, 1.7f)));
+    const float T = gexp(mixf(A.ln_3000, A.ln_22000, gpow(uz, 1.7f)));
     const float4 bb = blackbody(tx, T * g_shift);
     st.r = mixf(1.0f, bb.x, 0.7f);
     st.g = mixf(1.0f, bb.y, 0.7f);
@@ -323,7 +329,7 @@ __device__ __forceinline__ void star_add(const StarSlot& t, const LanePart& P, F
     const float sq = P.fp->r22 * d2;
     const float e = P.isaa * sp * sp + 2.0f * P.isab * sp * sq + P.isbb * sq * sq;
     if (!(e < 30.0f)) return;  // also skips NaN
-    const float k = t.F * P.norm * expf(-0.5f * e);
+    const float k = t.F * P.norm * gexp(-0.5f * e);
     sum = add(sum, F3{t.r * k, t.g * k, t.b * k});
 }
 
@@ -357,7 +363,7 @@ __device__ F3 star_layer_warp(const Tex& tx, const ShadeArgs& A, bool active, F3
     int c0x = 0, c0y = 0, c0z = 0;
     bool loop = false;
     if (active) {
-        const float footprint_cells = powf(fp.det, 0.25f) * L.N;
+        const float footprint_cells = gpow(fp.det, 0.25f) * L.N;
         w = smoothstep(0.8f, 2.5f, footprint_cells);
         const float4 bavg = blackbody(tx, 5600.0f * g_shift);
         const float aw = L.prob * L.N * L.N * 9.517f * L.flux * omega0;
