@@ -9,11 +9,14 @@
 //     farMode} (src/Renderer.h:24-53)
 //   bhs::Renderer::init / shutdown / render          bhr::Renderer::init / shutdown / render
 //     (src/Renderer.h:58-61)
-//   Renderer::setTraceUniforms (Renderer.cpp:242-356) bhr::Renderer::makeView
+//   Renderer::setTraceUniforms (Renderer.cpp:242-356) bhr::Renderer::makeView, makeShadeParams
+//   the frame's colour (blackhole.frag's fragColor)  bhr::Renderer::renderImage (bhr_shade)
 //
 // render() traces the frame into hit records the Renderer owns (as the reference's renderer
 // owns its targets, Renderer.cpp:125-145); renderTo() writes caller-owned device records on a
-// caller stream; renderHost() returns host records. The internal resolution follows
+// caller stream; renderHost() returns host records; renderImage() traces and shades the frame
+// into a float4 image the Renderer owns (the sky cube's term left to the caller, its weight in
+// alpha). The internal resolution follows
 // Renderer::render (Renderer.cpp:667-669): max(16, lround(window * clamp(renderScale, 0.1, 2)))
 // (the reference's dynamic-resolution factor is a frame-time controller of the GL pipeline
 // and is not part of this path). Errors follow the reference's convention: a bool result and
@@ -53,6 +56,19 @@ struct Settings {
     float diskOuter = 20.0f;
     float diskThickness = 0.035f;
     float fovDeg = 60.0f;
+    // shading fields (Settings.h:32-55)
+    float dopplerStrength = 0.0f;
+    float diskDensity = 1.0f;
+    float diskOpacity = 2.0f;
+    float diskPeakTemp = 6000.0f;
+    float diskBrightness = 5.5f;
+    float diskNoiseScale = 1.0f;
+    float diskNoiseStrength = 0.85f;
+    float diskWarmth = 0.4f;
+    float starDensity = 1.0f;
+    float starBrightness = 1.0f;
+    float skyBrightness = 1.0f;
+    bool showShadowOverlay = false;
 
     // Quality presets (Settings.cpp:12-35); PRESET_CUSTOM leaves the fields alone.
     void applyPreset(int p) {
@@ -116,6 +132,8 @@ struct FrameInput {
     bool farMode = false;            // camera far from the hole: straight rays (App.cpp:506)
     int termMode = BHR_TERM_SHADER;  // BHR_TERM_*: the shader's own rule by default
     float jitter[2] = {0.0f, 0.0f};  // sub-pixel offset of accumulated frames (0 for parity)
+    float diskTime = 0.0f;           // disk flow clock in M, [0, 60) (App.cpp:458-459)
+    float diskFade = 1.0f;           // steady disk's fade (1 = shown; <= 0.01 = not marched)
 };
 
 class Renderer {
@@ -140,6 +158,11 @@ public:
     }
 
     void shutdown() {
+        if (image_) {
+            cudaFree(image_);
+            image_ = nullptr;
+            image_capacity_ = 0;
+        }
         if (records_) {
             cudaFree(records_);
             records_ = nullptr;
@@ -183,8 +206,32 @@ public:
         v->disk_thickness = s.diskThickness;
         v->lensing = s.lensing ? 1 : 0;
         v->far_mode = in.farMode ? 1 : 0;
+        if (in.diskFade <= 0.01f) v->disk_mode = BHR_DISK_NONE;  // the faded disk is not marched (Renderer.cpp:327)
         if (in.termMode == BHR_TERM_SHADER)  // rEscMin = max(1.25 r_out, 12) (blackhole.frag:89)
             v->r_esc_min = std::max(1.25f * s.diskOuter, 12.0f);
+        return true;
+    }
+
+    // The shading uniforms of setTraceUniforms (Renderer.cpp:316-346) for the steady disk: its
+    // opacity and brightness scaled by the fade.
+    static bool makeShadeParams(const FrameInput& in, bhr_shade_params* p) {
+        if (!in.settings || !p || bhr_shade_default_params(p) != BHR_OK) return false;
+        const Settings& s = *in.settings;
+        const float strength = std::clamp(in.diskFade, 0.0f, 1.0f);
+        p->disk_density = s.diskDensity;
+        p->disk_opacity = s.diskOpacity * strength;
+        p->disk_peak_temp = s.diskPeakTemp;
+        p->disk_brightness = s.diskBrightness * strength;
+        p->disk_noise_scale = s.diskNoiseScale;
+        p->disk_noise_strength = s.diskNoiseStrength;
+        p->disk_time = in.diskTime;
+        p->disk_warmth = s.diskWarmth;
+        p->disk_inflow = 0.0f;
+        p->doppler_strength = s.dopplerStrength;
+        p->sky_brightness = s.skyBrightness;
+        p->star_density = s.starDensity;
+        p->star_brightness = s.starBrightness;
+        p->shadow_overlay = s.showShadowOverlay ? 1 : 0;
         return true;
     }
 
@@ -233,7 +280,30 @@ public:
         return true;
     }
 
+    // Traces and shades a frame: image() holds width() x height() float4 (linear rgb without
+    // the sky cube's term, alpha = that term's weight), row 0 at the bottom.
+    bool renderImage(const FrameInput& in, int precision = BHR_PREC_FP32) {
+        if (!render(in, precision)) return false;
+        bhr_view v{};
+        bhr_shade_params p{};
+        if (!makeView(in, &v) || !makeShadeParams(in, &p)) return logError("renderImage: incomplete FrameInput", nullptr);
+        const size_t n = size_t(v.width) * size_t(v.height);
+        if (n > image_capacity_) {
+            if (image_) cudaFree(image_);
+            image_ = nullptr;
+            image_capacity_ = 0;
+            if (cudaMalloc(&image_, n * 4 * sizeof(float)) != cudaSuccess)
+                return logError("renderImage: cannot allocate the image", nullptr);
+            image_capacity_ = n;
+        }
+        const bhr_hit* const hits[1] = {records_};
+        float* const outs[1] = {image_};
+        if (bhr_shade(ctx_, &v, 1, hits, &p, outs, nullptr) != BHR_OK) return logError("renderImage", ctx_);
+        return true;
+    }
+
     const bhr_hit* hits() const { return records_; }  // device records of the last render()
+    const float* image() const { return image_; }      // device float4 image of the last renderImage()
     int width() const { return width_; }
     int height() const { return height_; }
     bhr_ctx* context() const { return ctx_; }
@@ -251,6 +321,8 @@ private:
     int device_ = 0;
     bhr_hit* records_ = nullptr;
     size_t capacity_ = 0;
+    float* image_ = nullptr;
+    size_t image_capacity_ = 0;
     int width_ = 0, height_ = 0;
     LogFn log_;
 };

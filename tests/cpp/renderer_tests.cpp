@@ -127,6 +127,31 @@ static void testErrors() {
     CHECK(bhr_view_set_fov(&v, 190.0f) == BHR_ERR_INVALID_ARG, "fov >= 180 is refused");
 }
 
+static void testShadeParams() {
+    std::printf("shading uniforms\n");
+    bhr::Settings s;
+    const bhr::Camera cam = orbitCamera(30.0, 85.0 * M_PI / 180.0, 0.0);
+    bhr::FrameInput in;
+    in.camera = &cam;
+    in.settings = &s;
+    in.windowW = 64;
+    in.windowH = 36;
+    in.diskTime = 12.5f;
+    bhr_shade_params p{};
+    CHECK(bhr::Renderer::makeShadeParams(in, &p), "complete input converts");
+    CHECK(p.disk_opacity == 2.0f && p.disk_brightness == 5.5f && p.disk_peak_temp == 6000.0f && p.noise_seed == 7u,
+          "Settings defaults at full fade, noise seed 7");
+    CHECK(p.disk_time == 12.5f && p.shadow_overlay == 0, "disk clock and overlay carried");
+    bhr::FrameInput faded = in;
+    faded.diskFade = 0.0f;
+    bhr_view fv{};
+    CHECK(bhr::Renderer::makeView(faded, &fv) && fv.disk_mode == BHR_DISK_NONE, "a faded disk is not marched");
+    CHECK(bhr::Renderer::makeShadeParams(faded, &p) && p.disk_opacity == 0.0f && p.disk_brightness == 0.0f,
+          "a faded disk neither absorbs nor shines");
+    faded.diskFade = 0.25f;
+    CHECK(bhr::Renderer::makeShadeParams(faded, &p) && p.disk_opacity == 0.5f, "opacity scales with the fade");
+}
+
 static int testGpu(const char* path) {
     std::printf("traced frame (256x144, r=30, inclination 85 deg, 200 steps)\n");
     std::string logged;
@@ -178,6 +203,20 @@ static int testGpu(const char* path) {
     const bool wrote = f && std::fwrite(a.data(), sizeof(bhr_hit), n, f) == n;
     if (f) std::fclose(f);
     CHECK(wrote, "records written");
+    // the frame's colour: traced and shaded; written beside the records for the parity check
+    CHECK(R.renderImage(in), "renderImage");
+    std::vector<float> img(n * 4);
+    CHECK(cudaMemcpy(img.data(), R.image(), img.size() * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess,
+          "read back the image");
+    int lit = 0;
+    for (size_t k = 0; k < n; ++k) lit += img[4 * k] + img[4 * k + 1] + img[4 * k + 2] > 0.0f;
+    std::snprintf(msg, sizeof msg, "%d of %zu pixels lit", lit, n);
+    CHECK(lit > int(n / 2), msg);
+    const std::string ipath = std::string(path) + ".rgba";
+    FILE* g = std::fopen(ipath.c_str(), "wb");
+    const bool wrote_img = g && std::fwrite(img.data(), sizeof(float), img.size(), g) == img.size();
+    if (g) std::fclose(g);
+    CHECK(wrote_img, "image written");
     R.shutdown();
     return 0;
 }
@@ -187,6 +226,7 @@ int main(int argc, char** argv) {
     testCameraBasis();
     testFrameToView();
     testErrors();
+    testShadeParams();
     if (argc == 3 && std::strcmp(argv[1], "--gpu") == 0) testGpu(argv[2]);
     std::printf("\n%d checks, %d failures\n", g_checks, g_failures);
     return g_failures == 0 ? 0 : 1;

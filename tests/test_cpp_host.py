@@ -1,6 +1,7 @@
 """The C++ host interface (include/bhr_renderer.hpp): tests/cpp/renderer_tests.cpp compiled
 against libbhr.so. Host checks run without a GPU; the traced frame is compared with the FP64
-oracle and with the same view traced through the C ABI from Python."""
+oracle and with the same view traced through the C ABI from Python, and its shaded image with
+the CPU restatement of the shading."""
 from __future__ import annotations
 
 import subprocess
@@ -56,3 +57,12 @@ def test_cpp_renderer_frame_vs_oracle(tmp_path):
         direct = hits_numpy(o.cpu())
     assert np.array_equal(got.view(np.uint8), direct.view(np.uint8))  # same view, same kernel
     parity.check_fp32(got, v, where="C++ Renderer frame")
+    # the image renderImage shaded from those records, against the CPU restatement of the shading
+    import oracle_lib as O
+    from blackholerender_gb300 import shade_params
+
+    img = np.fromfile(str(out) + ".rgba", dtype=np.float32).reshape(v.height, v.width, 4)
+    p = shade_params()
+    ref = O.shade_view(v, got, p, O.noise_bake(p.noise_seed), O.blackbody_lut())
+    d = np.abs(img - ref)
+    assert np.mean(np.any(d > 1e-4 * np.abs(ref) + 1e-7, axis=-1)) <= 2e-3 and d.max() < 1e-3
