@@ -514,6 +514,15 @@ def cpu_shade_sample(view, hits, params, seconds: float):
             return px / dt / 1e6, threads
 
 
+def shade_traffic():
+    """DRAM bytes of one k_shade launch (one 1080p view) from the committed ncu capture."""
+    tfile = ROOT / "profiles" / "traffic.json"
+    try:
+        return json.loads(tfile.read_text())["k_shade"]["dram_bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def run_shade_workload(args):
     """--workload shade: the consumer of the hit records. The 16 poses at 1920x1080 are traced
     once (plain FP32 plan, untimed); each step shades all 16 views from their records
@@ -565,7 +574,9 @@ def run_shade_workload(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "bytes_per_pixel": bytes_px, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get(
                              "hbm_gbs") else "fallback 6800 GB/s",
-                         "note": "ALU-bound: 54 hashed lattice cells of the two star layers per escaped pixel"},
+                         "traffic": shade_traffic(),
+                         "note": "issue-bound on the CUDA cores (star hashes and Gaussians); traffic is one "
+                                 "view's launch from the committed ncu capture (writes partly still in L2)"},
             "gpu_launches": len(views) * args.steps, "clocks": clk.summary()}
     if not args.no_cpu:
         small = views[0].copy()
