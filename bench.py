@@ -592,6 +592,52 @@ def run_shade_workload(args):
     tr.close()
 
 
+def run_vol_workload(args):
+    """--workload vol: the volumetric disk (the reference's default disk) on the 16 poses at
+    1920x1080, 450 steps, default look; each step marches the 16 views (bhr_trace_volumetric)
+    into records and (rgb, transmittance). One JSON line, not the headline."""
+    import torch
+
+    from blackholerender_gb300 import DISK_VOLUMETRIC, HIT_BYTES, TERM_CONFIG, Tracer, hits_numpy, shade_params, workloads
+
+    dev = torch.device("cuda", 0)
+    tr = Tracer(0)
+    views = workloads.c2_views(TERM_CONFIG)[: args.views]
+    for v in views:
+        v.disk_mode = DISK_VOLUMETRIC
+    rays = sum(v.rays for v in views)
+    p = shade_params()
+    hits = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+    rgbt = [torch.empty((v.height, v.width, 4), dtype=torch.float32, device=dev) for v in views]
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        tr.trace_volumetric(views, p, hits, rgbt, st)
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(0) as clk:
+        for a, b in ev:
+            flush.zero_()
+            a.record(st)
+            tr.trace_volumetric(views, p, hits, rgbt, st)
+            b.record(st)
+        torch.cuda.synchronize(dev)
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(per) / len(per)
+    h0 = hits_numpy(hits[0].cpu())
+    steps = sum(int(hits_numpy(h.cpu())["steps"].astype(np.int64).sum()) for h in hits)
+    line = {"metric": "Mrays/s (volumetric disk)", "value": rays / (ms * 1e-3) / 1e6, "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{len(views)} poses (seed 0) x 1920x1080, FOV 60, 450 steps, volumetric disk "
+                                   "[6, 20], default look", "rays_per_step": rays,
+                       "l2": "flushed (256 MiB write) between steps",
+                       "opaque_fraction_view0": float(np.mean(h0["status"] == 4))},
+            "march_steps_per_ray": steps / rays, "gpu_launches": len(views) * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    tr.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -605,9 +651,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--views", type=int, default=16, help="first N of the 16 poses (small profiling cases)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "shade"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "shade", "vol"],
                     help="c2: the headline (16 poses at 1080p); c3 / c4: the other configurations; "
-                         "shade: the records' shading consumer")
+                         "shade: the records' shading consumer; vol: the volumetric disk march")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
@@ -615,6 +661,8 @@ def main():
         run_reference(args)
     elif args.workload == "shade":
         run_shade_workload(args)
+    elif args.workload == "vol":
+        run_vol_workload(args)
     elif args.workload != "c2":
         run_side_workload(args)
     else:

@@ -15,7 +15,7 @@ from . import _abi
 from ._abi import (  # noqa: F401
     DISK_NONE, DISK_THIN, DISK_VOLUMETRIC, FLAG_FALLBACK, FLAG_FP64, FLAG_NONFINITE, FLAG_SURROGATE,
     HIT_DTYPE, METHOD_PLAIN, METHOD_SURROGATE, PREC_FP32, PREC_MIXED, SQRT27, STATUS_BUDGET,
-    STATUS_CAPTURED, STATUS_ESCAPED, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, LaunchShape, Options,
+    STATUS_CAPTURED, STATUS_ESCAPED, STATUS_OPAQUE, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, LaunchShape, Options,
     ShadeParams, Stats, View,
 )
 
@@ -194,6 +194,30 @@ class Tracer:
         _abi.check(_abi.lib().bhr_shade(self._ctx, arr, n, hp, ctypes.byref(params), op,
                                         ctypes.c_void_p(stream.cuda_stream)), self._ctx)
         return outs
+
+    def trace_volumetric(self, views: Sequence[View], params: ShadeParams | None = None, hits=None, rgbt=None,
+                         stream=None):
+        """bhr_trace_volumetric: marches views with the volumetric disk. Returns (hits, rgbt): the
+        records (uint8 device tensors) and (height, width, 4) float32 tensors of the gathered rgb
+        and transmittance, which shade() completes in place with the sky."""
+        import torch
+
+        dev = torch.device("cuda", self.device)
+        n = len(views)
+        if params is None:
+            params = shade_params()
+        if hits is None:
+            hits = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+        if rgbt is None:
+            rgbt = [torch.empty((v.height, v.width, 4), dtype=torch.float32, device=dev) for v in views]
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        arr = (View * n)(*views)
+        hp = (ctypes.c_void_p * n)(*[h.data_ptr() for h in hits])
+        op = (ctypes.c_void_p * n)(*[o.data_ptr() for o in rgbt])
+        _abi.check(_abi.lib().bhr_trace_volumetric(self._ctx, arr, n, hp, ctypes.byref(params), op,
+                                                   ctypes.c_void_p(stream.cuda_stream)), self._ctx)
+        return hits, rgbt
 
     def noise_bake(self, seed: int = 7, out=None, stream=None):
         """bhr_noise_bake: the disk's 128^3 noise volume as a device int16 tensor of half bits."""

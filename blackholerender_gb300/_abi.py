@@ -24,6 +24,7 @@ ERR_IO = -7
 STATUS_ESCAPED = 1
 STATUS_CAPTURED = 2
 STATUS_BUDGET = 3
+STATUS_OPAQUE = 4
 
 FLAG_FP64 = 0x01
 FLAG_SURROGATE = 0x02
@@ -199,6 +200,8 @@ SIGNATURES = {
     "bhr_shade_default_params": (ctypes.c_int, [ctypes.POINTER(ShadeParams)]),
     "bhr_shade": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(ShadeParams),
                                  ctypes.POINTER(_P), _P]),
+    "bhr_trace_volumetric": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(ShadeParams),
+                                            ctypes.POINTER(_P), _P]),
     "bhr_noise_bake": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P]),
     "bhr_blackbody_lut": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "bhr_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),

@@ -19,6 +19,7 @@
 #include "host_views.h"
 #include "kernels.cuh"
 #include "shade.cuh"
+#include "vol.cuh"
 
 // Device scratch of a trace: one work queue per launch batch, and the FP64 queues of MIXED.
 struct TraceScratch {
@@ -743,8 +744,6 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         const bhr_view& v = views[k];
         const std::string at = "bhr_shade: view " + std::to_string(k);
         if (v.width <= 0 || v.height <= 0) return fail(c, BHR_ERR_INVALID_ARG, at + ": width and height must be positive");
-        if (v.disk_mode == BHR_DISK_VOLUMETRIC)
-            return fail(c, BHR_ERR_UNSUPPORTED, at + ": the volumetric disk is shaded inside its march");
         if (!hits[k] || !rgba[k]) return fail(c, BHR_ERR_INVALID_ARG, at + ": NULL buffer");
         if (reinterpret_cast<uintptr_t>(hits[k]) % 16 != 0 || reinterpret_cast<uintptr_t>(rgba[k]) % 16 != 0)
             return fail(c, BHR_ERR_INVALID_ARG, at + ": buffers must be 16-byte aligned");
@@ -767,6 +766,7 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         a.disk_inner = v.disk_inner;
         a.disk_outer = v.disk_outer;
         a.disk_thin = v.disk_mode == BHR_DISK_THIN;
+        a.volumetric = v.disk_mode == BHR_DISK_VOLUMETRIC;
         a.far_mode = v.far_mode;
         a.p = *p;
         a.ln_1000 = std::log(1000.0f);
@@ -779,6 +779,48 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         a.lut = c->lut;
         const cudaError_t e = bhr::launch_shade(a, st);
         if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_shade: kernel launch");
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int bhr_trace_volumetric(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* hits, const bhr_shade_params* p,
+                         float* const* rgbt, void* cuda_stream) {
+    if (!c || !views || nviews <= 0 || !hits || !p || !rgbt)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_volumetric: NULL argument or no views");
+    for (int k = 0; k < nviews; ++k) {
+        const bhr_view& v = views[k];
+        const std::string at = "bhr_trace_volumetric: view " + std::to_string(k);
+        if (v.width <= 0 || v.height <= 0 || v.max_steps < 0)
+            return fail(c, BHR_ERR_INVALID_ARG, at + ": width and height must be positive, max_steps >= 0");
+        if (v.disk_mode != BHR_DISK_VOLUMETRIC)
+            return fail(c, BHR_ERR_INVALID_ARG, at + ": disk_mode must be BHR_DISK_VOLUMETRIC (bhr_trace marches the others)");
+        if (v.term_mode != BHR_TERM_SHADER && v.term_mode != BHR_TERM_CONFIG)
+            return fail(c, BHR_ERR_UNSUPPORTED, at + ": the volumetric disk is marched under the SHADER or CONFIG rule");
+        if (!(v.disk_step > 0.0f) || !(v.disk_thickness > 0.0f))
+            return fail(c, BHR_ERR_INVALID_ARG, at + ": disk_step and disk_thickness must be positive");
+        if (!hits[k] || !rgbt[k]) return fail(c, BHR_ERR_INVALID_ARG, at + ": NULL buffer");
+        if (reinterpret_cast<uintptr_t>(hits[k]) % 16 != 0 || reinterpret_cast<uintptr_t>(rgbt[k]) % 16 != 0)
+            return fail(c, BHR_ERR_INVALID_ARG, at + ": buffers must be 16-byte aligned");
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    int rc = ensure_shade_resources(c, p->noise_seed, st);
+    for (int k = 0; k < nviews && rc == BHR_OK; ++k) {
+        bhr::VolArgs a{};
+        a.view = bhr::host::make_dev_view(views[k], hits[k]);
+        a.rule = bhr::host::make_rule(views[k]);
+        a.p = *p;
+        a.ln_1000 = std::log(1000.0f);
+        a.ln_40000 = std::log(40000.0f);
+        a.thick = views[k].disk_thickness;
+        a.noise = c->noise;
+        a.lut = c->lut;
+        a.rgbt = reinterpret_cast<float4*>(rgbt[k]);
+        const cudaError_t e = bhr::launch_march_vol(a, st);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace_volumetric: kernel launch");
     }
     cudaSetDevice(prev);
     return rc;

@@ -20,55 +20,14 @@
 
 #include "bhr.h"
 #include "shade.cuh"
+#include "shade_math.cuh"
 
 namespace bhr {
 
 namespace {
 
-constexpr int kN = BHR_NOISE_SIZE, kLut = BHR_BLACKBODY_LUT;
+using namespace shading;
 constexpr int kBX = 32, kBY = 8;
-constexpr float kPi = 3.14159265358979f, kTwoPi = 6.28318530717959f;
-
-struct F3 { float x, y, z; };
-__device__ __forceinline__ F3 add(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ F3 scale(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ F3 divs(F3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
-__device__ __forceinline__ float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ F3 cross(F3 a, F3 b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-__device__ __forceinline__ float len(F3 a) { return sqrtf(dot(a, a)); }
-__device__ __forceinline__ F3 normalize(F3 a) { return divs(a, len(a)); }
-__device__ __forceinline__ float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }  // GLSL mix
-__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
-__device__ __forceinline__ float smoothstep(float e0, float e1, float x) {
-    const float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
-    return t * t * (3.0f - 2.0f * t);
-}
-
-// exp, log and pow of the shading: the SFU approximations, as GLSL's exp / log / pow compile to
-// on the GPU (a few ulp; the noise bake uses none of them and stays exact)
-__device__ __forceinline__ float gexp(float x) { return __expf(x); }
-__device__ __forceinline__ float glog(float x) { return __logf(x); }
-__device__ __forceinline__ float gpow(float x, float y) { return __powf(x, y); }
-
-// common.glsl:16-22 pcg3d, the three lanes updated in sequence
-__device__ __forceinline__ uint3 pcg3d(uint3 v) {
-    v.x = v.x * 1664525u + 1013904223u;
-    v.y = v.y * 1664525u + 1013904223u;
-    v.z = v.z * 1664525u + 1013904223u;
-    v.x += v.y * v.z;
-    v.y += v.z * v.x;
-    v.z += v.x * v.y;
-    v.x ^= v.x >> 16;
-    v.y ^= v.y >> 16;
-    v.z ^= v.z >> 16;
-    v.x += v.y * v.z;
-    v.y += v.z * v.x;
-    v.z += v.x * v.y;
-    return v;
-}
 
 // common.glsl:33-39 grad3: a unit gradient from the hashed lattice point
 __device__ __forceinline__ F3 grad3(int cx, int cy, int cz, uint32_t salt) {
@@ -125,100 +84,6 @@ __global__ void __launch_bounds__(256) k_noise_bake(uint32_t seed, uint16_t* __r
 }
 
 // ---------------------------------------------------------------- shading
-
-struct Tex {
-    const uint16_t* noise;
-    const float4* lut;  // shared memory
-    float ln_1000, ln_40000;
-};
-
-// blackbody.glsl:7-16: log-temperature lookup, linear filter, clamp to edge; Wien-tail fade
-__device__ __forceinline__ float4 blackbody(const Tex& tx, float T) {
-    const float Tc = clampf(T, 1000.0f, 40000.0f);
-    const float t = (glog(Tc) - tx.ln_1000) / (tx.ln_40000 - tx.ln_1000);
-    const float u = t * float(kLut) - 0.5f;
-    const float fl = floorf(u);
-    const float a = u - fl;
-    const int i0 = min(max(int(fl), 0), kLut - 1), i1 = min(max(int(fl) + 1, 0), kLut - 1);
-    const float4 p = tx.lut[i0], q = tx.lut[i1];
-    float4 o{mixf(p.x, q.x, a), mixf(p.y, q.y, a), mixf(p.z, q.z, a), mixf(p.w, q.w, a)};
-    const float under = clampf(T / 1000.0f, 0.0f, 1.0f);
-    o.w *= under * under * under * under * under * under;
-    return o;
-}
-
-__device__ __forceinline__ float texel(const Tex& tx, int x, int y, int z) {
-    return __half2float(__ushort_as_half(__ldg(tx.noise + (size_t(z) * kN + y) * kN + x)));
-}
-
-// texture(uNoise3d, c).r: trilinear, REPEAT
-__device__ float noise_sample(const Tex& tx, F3 c) {
-    const float ux = c.x * float(kN) - 0.5f, uy = c.y * float(kN) - 0.5f, uz = c.z * float(kN) - 0.5f;
-    const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
-    const float ax = ux - fx, ay = uy - fy, az = uz - fz;
-    const int x0 = ((int(fx) % kN) + kN) % kN, y0 = ((int(fy) % kN) + kN) % kN, z0 = ((int(fz) % kN) + kN) % kN;
-    const int x1 = (x0 + 1) % kN, y1 = (y0 + 1) % kN, z1 = (z0 + 1) % kN;
-    const float c00 = mixf(texel(tx, x0, y0, z0), texel(tx, x1, y0, z0), ax);
-    const float c10 = mixf(texel(tx, x0, y1, z0), texel(tx, x1, y1, z0), ax);
-    const float c01 = mixf(texel(tx, x0, y0, z1), texel(tx, x1, y0, z1), ax);
-    const float c11 = mixf(texel(tx, x0, y1, z1), texel(tx, x1, y1, z1), ax);
-    return mixf(mixf(c00, c10, ay), mixf(c01, c11, ay), az);
-}
-
-__device__ __forceinline__ float glsl_mod(float x, float y) { return x - y * floorf(x / y); }
-
-// disk.glsl:45-63 diskNoise at the mid-plane (yOverH = 0)
-__device__ float disk_noise(const Tex& tx, const bhr_shade_params& P, float r, float phi) {
-    const float omega = gpow(r, -1.5f);
-    const float t = P.disk_time;
-    const float Pd = 60.0f;
-    const float t1 = glsl_mod(t, Pd);
-    const float t2 = glsl_mod(t + 0.5f * Pd, Pd);
-    const float w2 = fabsf(2.0f * t1 / Pd - 1.0f);
-    const float rep = fmaxf(1.0f, floorf(2.0f * P.disk_noise_scale + 0.5f));
-    const float lr = glog(r) * 3.2f * P.disk_noise_scale;
-    const float yy = 0.0f * 0.35f;
-    const float k = rep / kTwoPi;
-    const F3 c1{(phi + omega * t1) * k, lr + P.disk_inflow * omega * t1, yy};
-    const F3 c2{(phi + omega * t2) * k, lr + 0.37f + P.disk_inflow * omega * t2, yy + 0.61f};
-    return mixf(noise_sample(tx, c1), noise_sample(tx, c2), w2);
-}
-
-// thinDiskSample (disk.glsl:113-129) at a recorded crossing: radiance (rgb) and alpha
-__device__ float4 thin_disk_sample(const Tex& tx, const ShadeArgs& A, float r, float phi, float b_axis, float rcam) {
-    const bhr_shade_params& P = A.p;
-    if (r < A.disk_inner || r > A.disk_outer) return make_float4(0.f, 0.f, 0.f, 0.f);
-    const float n = disk_noise(tx, P, r, phi);
-    const float f = smoothstep(0.32f, 0.78f, n);
-    const float pattern = mixf(1.0f, mixf(0.08f, 1.4f, f), P.disk_noise_strength);
-    const float emit = mixf(1.0f, mixf(0.22f, 1.35f, f * f), P.disk_noise_strength);
-    // diskRadialProfile (disk.glsl:81-85)
-    const float r_in = A.disk_inner, r_out = A.disk_outer;
-    const float inner = smoothstep(r_in, r_in + 0.25f, r);
-    const float outer = 1.0f - smoothstep(r_out * 0.55f, r_out, r);
-    const float radial = inner * outer * gpow(r_in / fmaxf(r, r_in), 1.2f);
-    const float dens = P.disk_density * radial * pattern;
-    // diskTempProfile (disk.glsl:26-30)
-    const float x = r_in / fmaxf(r, r_in);
-    const float prof = gpow(x, 0.75f) * gpow(fmaxf(1.0f - sqrtf(x), 0.0f), 0.25f) / 0.48796f;
-    const float T = P.disk_peak_temp * prof * mixf(1.0f, 0.85f + 0.3f * emit, 0.5f);
-    // redshiftFactor (disk.glsl:36-41)
-    const float omega = gpow(r, -1.5f);
-    const float ut = 1.0f / sqrtf(fmaxf(1.0f - 3.0f / r, 0.02f));
-    const float lapse = sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f));
-    const float g_phys = 1.0f / (lapse * ut * fmaxf(1.0f - omega * b_axis, 0.05f));
-    const float g = mixf(1.0f, g_phys, P.doppler_strength);
-    const float4 bb = blackbody(tx, T * g);
-    // opticalDepthScale (disk.glsl:67-71)
-    const float lapse_em = sqrtf(fmaxf(1.0f - 2.0f / r, 1e-4f));
-    const float ods = mixf(1.0f, lapse_em / (g_phys * lapse), P.doppler_strength);
-    const float alpha = 1.0f - gexp(-dens * P.disk_opacity * 0.6f * ods);
-    // diskTint (disk.glsl:21)
-    const float w = P.disk_warmth;
-    const float s = bb.w * P.disk_brightness * emit;
-    return make_float4(bb.x * mixf(1.0f, 1.0f, w) * s, bb.y * mixf(1.0f, 0.80f, w) * s, bb.z * mixf(1.0f, 0.58f, w) * s,
-                       alpha);
-}
 
 struct Footprint {
     F3 e1, e2;
@@ -469,17 +334,23 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
     bool esc = false;
     F3 esc_dir = dir;
     if (in) {
-        const float4* rec = reinterpret_cast<const float4*>(A.hits + int64_t(j) * A.width + i);
+        const int64_t k_pix = int64_t(j) * A.width + i;
+        const float4* rec = reinterpret_cast<const float4*>(A.hits + k_pix);
         const float4 w0 = __ldg(rec), w1 = __ldg(rec + 1);
         const uint32_t head = __float_as_uint(w0.x);
         const int status = int(head & 0xffu), ncross = int((head >> 8) & 0xffu);
         bool opaque = false;
-        if (A.disk_thin && ncross > 0) {
+        if (A.volumetric) {  // the volumetric march gathered the disk's light along the ray
+            const float4 m = A.out[k_pix];
+            col = F3{m.x, m.y, m.z};
+            trans = m.w;
+            opaque = status == BHR_STATUS_OPAQUE;
+        } else if (A.disk_thin && ncross > 0) {
             const float4 w2 = __ldg(rec + 2), w3 = __ldg(rec + 3);
             const float cr[3] = {w2.z, w2.w, w3.x}, cp[3] = {w3.y, w3.z, w3.w};
             const float b_axis = w2.x;
             for (int k = 0; k < ncross && k < 3; ++k) {
-                const float4 dk = thin_disk_sample(tx, A, cr[k], cp[k], b_axis, rcam);
+                const float4 dk = thin_disk_sample(tx, P, A.disk_inner, A.disk_outer, cr[k], cp[k], b_axis, rcam);
                 col = add(col, F3{trans * dk.x * dk.w, trans * dk.y * dk.w, trans * dk.z * dk.w});
                 trans *= 1.0f - dk.w;
                 if (trans < 0.004f) {

@@ -16,6 +16,7 @@ struct ShadeArgs {
     int32_t width, height;
     float disk_inner, disk_outer;
     int32_t disk_thin;  // uDiskMode == DISK_THIN
+    int32_t volumetric; // uDiskMode == DISK_VOLUMETRIC: `out` holds the march's (rgb, transmittance)
     int32_t far_mode;
     bhr_shade_params p;
     float ln_1000, ln_40000, ln_3000, ln_22000;  // logf of the constants, from the host's libm

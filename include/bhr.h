@@ -46,6 +46,7 @@ extern "C" {
 #define BHR_STATUS_ESCAPED 1   /* blackhole.frag status 1 */
 #define BHR_STATUS_CAPTURED 2  /* blackhole.frag status 2 (horizon test) */
 #define BHR_STATUS_BUDGET 3    /* step budget ran out; blackhole.frag:252 shades it as captured */
+#define BHR_STATUS_OPAQUE 4    /* volumetric disk: transmittance fell below 0.004 (blackhole.frag:234 status 3) */
 
 /* ---- bhr_hit.flags ----------------------------------------------------------------- */
 #define BHR_FLAG_FP64 0x01       /* some or all of the march ran in FP64 (mixed precision) */
@@ -56,7 +57,7 @@ extern "C" {
 /* ---- disk modes (src/Settings.h:7, shaders/common.glsl:12-14) ---------------------- */
 #define BHR_DISK_NONE 0
 #define BHR_DISK_THIN 1
-#define BHR_DISK_VOLUMETRIC 2 /* rejected with BHR_ERR_UNSUPPORTED */
+#define BHR_DISK_VOLUMETRIC 2 /* marched by bhr_trace_volumetric (bhr_trace refuses it) */
 
 /* ---- termination rules ------------------------------------------------------------- */
 /* SHADER: blackhole.frag:144,151-155 - capture r < 2.02, tolerance escape
@@ -343,9 +344,22 @@ typedef struct bhr_shade_params {
 } bhr_shade_params;
 int bhr_shade_default_params(bhr_shade_params* p);
 /* Shades nviews views: hits_dev[k] holds view k's records (from any trace entry point),
- * rgba_dev[k] gets width x height float4. Stream-ordered like bhr_trace. */
+ * rgba_dev[k] gets width x height float4. Stream-ordered like bhr_trace. A volumetric view
+ * (disk_mode BHR_DISK_VOLUMETRIC) is shaded in place: rgba_dev[k] holds what
+ * bhr_trace_volumetric gathered (rgb, transmittance) and gets the finished pixel. */
 int bhr_shade(bhr_ctx* ctx, const bhr_view* views, int nviews, const bhr_hit* const* hits_dev,
               const bhr_shade_params* params, float* const* rgba_dev, void* cuda_stream);
+/* The volumetric disk (the reference's default disk, Settings.h:22): blackhole.frag's march
+ * with uDiskMode == DISK_VOLUMETRIC. Inside the disk slab the step is clamped to 6 diskStep
+ * and each RK4 segment is sub-sampled along its cubic Hermite interpolant; every sample in
+ * the disk's volume adds emission and absorption (volumetricDiskStep, disk.glsl:88-110) with
+ * the look in `params`, and the ray turns opaque (BHR_STATUS_OPAQUE) once the transmittance
+ * falls below 0.004 (blackhole.frag:169-181,217-234). hits_dev[k] gets the records (no
+ * crossing slots), rgbt_dev[k] width x height float4 = (gathered rgb, transmittance); pass
+ * rgbt_dev[k] to bhr_shade as that view's rgba to add the sky. FP32; views must have
+ * disk_mode BHR_DISK_VOLUMETRIC and the SHADER or CONFIG rule. Stream-ordered. */
+int bhr_trace_volumetric(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* hits_dev,
+                         const bhr_shade_params* params, float* const* rgbt_dev, void* cuda_stream);
 /* The disk's noise volume (noise_bake.comp): BHR_NOISE_SIZE^3 IEEE half values, texel
  * (x, y, z) at (z N + y) N + x, into device memory. */
 int bhr_noise_bake(bhr_ctx* ctx, uint32_t seed, uint16_t* out_dev, void* cuda_stream);

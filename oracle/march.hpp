@@ -12,6 +12,9 @@
 //   shaders/disk.glsl:24,113-116      slab half-height, crossing radius/azimuth + range test
 //   shaders/blackhole.frag:67-93      ray generation and per-ray constants
 //   shaders/blackhole.frag:138-216,252  march loop (variant BHS_BODIES 0, BHS_GAS 0, thin disk)
+//   shaders/blackhole.frag:169-181,217-234  volumetric disk: the 6 diskStep clamp in the slab,
+//                                     Hermite sub-samples of each RK4 segment, opacity stop
+//                                     (the sample itself is the caller's `vol`, oracle/shade.hpp)
 //   src/physics/Geodesic.h:107-140    trace(), the CPU mirror's loop (BHR_TERM_CPU)
 // Vector formulas follow GLM/GLSL definitions (dot = (x+y)+z, normalize = v * (1/sqrt(dot)),
 // mix(a,b,t) = a*(1-t) + b*t) so the double path reproduces the reference's CPU code bit for
@@ -139,6 +142,16 @@ struct Result {
     T cross_r[3] = {0, 0, 0};
     T cross_phi[3] = {0, 0, 0};
     V3<T> x{0, 0, 0}, v{0, 0, 0};  // final state (for tests)
+    float col[3] = {0.0f, 0.0f, 0.0f};  // volumetric disk: emission gathered front to back
+    float trans = 1.0f;                 // and the transmittance left
+};
+
+// Sub-samples per segment are bounded: inside the slab ds <= 6 diskStep, so a finite segment
+// needs at most 7; the bound only stops a non-finite segment from looping.
+constexpr int kMaxSubSamples = 64;
+
+struct NoVolume {
+    template <class... A> void operator()(A&&...) const {}
 };
 
 // blackhole.frag:68-72: primary ray of pixel (i, j), row 0 at the bottom.
@@ -162,7 +175,9 @@ template <class T> inline bool finite3(V3<T> a) {
 }
 
 // blackhole.frag:77-93 (setup) + :138-253 (march), or Geodesic.h:107-140 for BHR_TERM_CPU.
-template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {
+// For BHR_DISK_VOLUMETRIC, vol(p, r_cyl, sub, res) shades one sub-sample of a segment in the
+// slab into res.col / res.trans (volumetricDiskStep).
+template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir, const Vol& vol) {
     Result<T> res;
     const bool lensing = R.lensing && !R.far_mode;
     V3<T> x = camPos;
@@ -214,21 +229,26 @@ template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {
                 }
             }
             T ds;
+            bool near_disk = false;
             if (shader_rule) {
                 ds = std::max(R.step_scale * r * farMul, R.ds_floor);
                 if (R.disk_mode != BHR_DISK_NONE) {
                     const T rcyl = std::sqrt(x.x * x.x + x.z * x.z);
                     if (rcyl > R.disk_inner - T(1) && rcyl < R.disk_outer + T(1)) {
                         const T outside = std::fabs(x.y) - slab * rcyl;
-                        if (outside > T(0))
+                        if (outside > T(0)) {
                             ds = std::min(ds, std::max(R.disk_step, outside / (std::fabs(v.y) / vlen + slab)));
+                        } else {
+                            near_disk = true;  // inside the slab: sub-sampled below (blackhole.frag:173-175)
+                            if (R.disk_mode == BHR_DISK_VOLUMETRIC) ds = std::min(ds, T(6) * R.disk_step);
+                        }
                     }
                 }
             } else {
                 ds = std::max(R.step_scale * r, R.ds_floor);
             }
             const T dt = ds / vlen;
-            const V3<T> x0 = x;
+            const V3<T> x0 = x, v0 = v;
             if (lensing)
                 rk4Step(x, v, h2, dt);
             else
@@ -247,6 +267,28 @@ template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {
                     }
                 }
             }
+            if (R.disk_mode == BHR_DISK_VOLUMETRIC && near_disk) {
+                // blackhole.frag:217-233: samples along the cubic Hermite interpolant of the segment
+                const T seg = length(x - x0);
+                const T nf = std::ceil(seg / R.disk_step);
+                const int n = std::isfinite(nf) ? std::min(std::max(1, int(std::min(nf, T(kMaxSubSamples)))), kMaxSubSamples) : 1;
+                const T sub = seg / T(n);
+                const V3<T> m0 = dt * v0, m1 = dt * v;
+                for (int k = 0; k < n; ++k) {
+                    const T t = (T(k) + T(0.5)) / T(n);
+                    const T t2 = t * t, t3 = t2 * t;
+                    const V3<T> p = (T(2) * t3 - T(3) * t2 + T(1)) * x0 + (t3 - T(2) * t2 + t) * m0 +
+                                    (T(-2) * t3 + T(3) * t2) * x + (t3 - t2) * m1;
+                    const T rm = std::sqrt(p.x * p.x + p.z * p.z);
+                    if (rm > R.disk_inner - T(0.5) && rm < R.disk_outer && std::fabs(p.y) < slab * rm)
+                        vol(p, rm, sub, res);
+                    if (res.trans < 0.004f) break;
+                }
+            }
+            if (res.trans < 0.004f) {  // blackhole.frag:234
+                status = BHR_STATUS_OPAQUE;
+                break;
+            }
             if (!finite3(x) || !finite3(v)) {
                 res.nonfinite = true;
                 break;
@@ -260,6 +302,10 @@ template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {
     res.x = x;
     res.v = v;
     return res;
+}
+
+template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {
+    return march(R, camPos, dir, NoVolume{});
 }
 
 template <class T> inline void toHit(const Result<T>& r, bhr_hit* o) {

@@ -3,6 +3,7 @@
 // never by the product library. The march itself is oracle/march.hpp.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <thread>
@@ -41,6 +42,17 @@ void parallel_for(int64_t n, int nthreads, int64_t grain, F&& fn) {
 bool view_ok(const bhr_view* v) {
     return v && v->width > 0 && v->height > 0 && v->max_steps >= 0 && v->disk_mode != BHR_DISK_VOLUMETRIC;
 }
+
+// The volumetric disk's sub-sample (oracle/shade.hpp vol_disk_step) in float, as the shader.
+struct VolumeSampler {
+    const oracle::shade::Tex* tx;
+    const bhr_shade_params* P;
+    float r_in, r_out, thick, rcam;
+    template <class T> void operator()(const V3<T>& p, T rm, T sub, Result<T>& res) const {
+        oracle::shade::vol_disk_step(*tx, *P, r_in, r_out, thick, oracle::shade::F3{float(p.x), float(p.y), float(p.z)},
+                                     float(rm), float(sub), float(res.b_axis), rcam, res.col, res.trans);
+    }
+};
 
 template <class T>
 void trace_one(const bhr_view& w, const Rule<T>& R, int64_t idx, bhr_hit* out) {
@@ -225,6 +237,48 @@ uint16_t oracle_to_half(float x) { return oracle::shade::to_half(x); }
 void oracle_pcg3d(const uint32_t in[3], uint32_t out[3]) {
     const oracle::shade::U3 h = oracle::shade::pcg3d({in[0], in[1], in[2]});
     out[0] = h.x, out[1] = h.y, out[2] = h.z;
+}
+
+// The volumetric disk's march of every pixel of a view: records, and rgbt[4 k] = the colour the
+// march gathered and the transmittance left (blackhole.frag:217-234).
+int oracle_trace_volumetric(const bhr_view* v, const bhr_shade_params* p, const uint16_t* noise, const float* lut,
+                            bhr_hit* out, float* rgbt, int nthreads, int fp64) {
+    if (!v || !p || !noise || !lut || !out || !rgbt || v->width <= 0 || v->height <= 0 || v->max_steps < 0 ||
+        v->disk_mode != BHR_DISK_VOLUMETRIC)
+        return BHR_ERR_INVALID_ARG;
+    const oracle::shade::Tex tx{noise, lut};
+    const float cx = v->cam_pos[0], cy = v->cam_pos[1], cz = v->cam_pos[2];
+    const VolumeSampler vs{&tx, p, v->disk_inner, v->disk_outer, v->disk_thickness, std::sqrt(cx * cx + cy * cy + cz * cz)};
+    const int64_t n = static_cast<int64_t>(v->width) * v->height;
+    auto one = [&](auto R, int64_t k) {
+        using T = decltype(R.step_scale);
+        const int i = static_cast<int>(k % v->width), j = static_cast<int>(k / v->width);
+        const V3<T> cam{T(v->cam_pos[0]), T(v->cam_pos[1]), T(v->cam_pos[2])};
+        const Result<T> r = march(R, cam, primaryRay<T>(*v, i, j), vs);
+        toHit(r, out + k);
+        for (int c = 0; c < 3; ++c) rgbt[4 * k + c] = r.col[c];
+        rgbt[4 * k + 3] = r.trans;
+    };
+    if (fp64) {
+        const Rule<double> R = Rule<double>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
+    } else {
+        const Rule<float> R = Rule<float>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
+    }
+    return BHR_OK;
+}
+
+// Shades a volumetric view: the records and the march's rgbt from oracle_trace_volumetric.
+int oracle_shade_volumetric(const bhr_view* v, const bhr_hit* hits, const float* rgbt, const bhr_shade_params* p,
+                            const uint16_t* noise, const float* lut, float* rgba, int nthreads) {
+    if (!v || !hits || !rgbt || !p || !noise || !lut || !rgba || v->width <= 0 || v->height <= 0 ||
+        v->disk_mode != BHR_DISK_VOLUMETRIC)
+        return BHR_ERR_INVALID_ARG;
+    const oracle::shade::Tex tx{noise, lut};
+    parallel_for(v->height, nthreads, 1,
+                 [&](int64_t j) { oracle::shade::shade_view(tx, *p, *v, hits, rgba, j, j + 1, rgbt); });
+    return BHR_OK;
 }
 
 int oracle_hit_size(void) { return static_cast<int>(sizeof(bhr_hit)); }

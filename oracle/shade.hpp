@@ -8,6 +8,7 @@
 //   shaders/blackbody.glsl:7-16             blackbody(T): LUT lookup + Wien-tail fade
 //   shaders/disk.glsl:21-48,81-85,113-129   diskTint, diskTempProfile, redshiftFactor, diskNoise,
 //                                           opticalDepthScale, diskRadialProfile, thinDiskSample
+//   shaders/disk.glsl:88-110                diskDensity, volumetricDiskStep (one slab sub-sample)
 //   shaders/blackhole.frag:209-216,234      front-to-back compositing of the crossings, opacity stop
 //   shaders/blackhole.frag:297-310          screen-space derivatives of escDir, mixed-quad rule
 //   shaders/sky.glsl:26-48,54-103,105-118   makeFootprint, starLayer, sampleSky (without the cube)
@@ -280,6 +281,35 @@ inline RGBA thin_disk_sample(const Tex& tx, const bhr_shade_params& P, const bhr
     return {bb.r * tint.x * s, bb.g * tint.y * s, bb.b * tint.z * s, alpha};
 }
 
+// volumetricDiskStep (disk.glsl:101-110) with diskDensity (:88-99): one segment of length ds
+// centred at p, r = |p.xz|, composited front to back into col / trans.
+inline void vol_disk_step(const Tex& tx, const bhr_shade_params& P, float r_in, float r_out, float thick, F3 p, float r,
+                          float ds, float b_axis, float rcam, float col[3], float& trans) {
+    const float H = std::fmax(thick * r, 1e-3f);
+    const float yh = p.y / H;
+    const float vert = std::exp(-yh * yh);
+    const float phi = std::atan2(p.z, p.x);
+    const float n = disk_noise(tx, P, r, phi, yh);
+    const float f = smoothstep(0.32f, 0.78f, n);
+    const float pattern = mixf(1.0f, mixf(0.08f, 1.4f, f), P.disk_noise_strength);
+    const float emit = mixf(1.0f, mixf(0.22f, 1.35f, f * f), P.disk_noise_strength);
+    const float puff = 1.0f + 0.6f * smoothstep(r_out * 0.4f, r_out, r) * (n - 0.5f);
+    const float dens = P.disk_density * disk_radial_profile(r_in, r_out, r) * vert * pattern * std::fmax(puff, 0.0f);
+    if (dens < 1e-4f) return;
+    const float T = P.disk_peak_temp * disk_temp_profile(r_in, r) * mixf(1.0f, 0.85f + 0.3f * emit, 0.5f);
+    const float g_phys = redshift_factor(r, b_axis, rcam);
+    const float g = mixf(1.0f, g_phys, P.doppler_strength);
+    const RGBA bb = blackbody(tx, T * g);
+    const float inward = std::pow(r_in / std::fmax(r, r_in), 0.6f);
+    const float w = P.disk_warmth;
+    const float s = bb.a * P.disk_brightness * emit * inward;
+    const float src[3] = {bb.r * mixf(1.0f, 1.0f, w) * s, bb.g * mixf(1.0f, 0.80f, w) * s, bb.b * mixf(1.0f, 0.58f, w) * s};
+    const float absorb = dens * P.disk_opacity * optical_depth_scale(P, r, g_phys, rcam);
+    const float a = 1.0f - std::exp(-absorb * ds);
+    for (int c = 0; c < 3; ++c) col[c] = col[c] + trans * src[c] * a;
+    trans *= 1.0f - a;
+}
+
 struct Footprint {
     F3 e1, e2;
     float r11, r12, r22, gi11, gi12, gi22, det_gi, det, mu;
@@ -388,14 +418,21 @@ struct PixelState {
     F3 dir;       // primary direction
 };
 
+// The disk's colour and transmittance in front of the sky: composited here from the thin
+// disk's crossings, or, for the volumetric disk, gathered by its march (rgbt[k] = rgb, T).
 inline PixelState composite_disk(const Tex& tx, const bhr_shade_params& P, const bhr_view& v, const bhr_hit& h, int i,
-                                 int j, float rcam) {
+                                 int j, float rcam, const float* rgbt) {
     PixelState s;
     s.col = {0, 0, 0};
     s.trans = 1.0f;
     s.dir = primary_dir(v, i, j);
     bool opaque = false;
-    if (v.disk_mode == BHR_DISK_THIN) {
+    if (v.disk_mode == BHR_DISK_VOLUMETRIC) {
+        const float* q = rgbt + 4 * (int64_t(j) * v.width + i);
+        s.col = {q[0], q[1], q[2]};
+        s.trans = q[3];
+        opaque = h.status == BHR_STATUS_OPAQUE;
+    } else if (v.disk_mode == BHR_DISK_THIN) {
         for (int k = 0; k < h.ncross && k < 3; ++k) {
             const RGBA d = thin_disk_sample(tx, P, v, h.cross_r[k], h.cross_phi[k], h.b_axis, rcam);
             s.col = s.col + F3{s.trans * d.r * d.a, s.trans * d.g * d.a, s.trans * d.b * d.a};
@@ -413,7 +450,7 @@ inline PixelState composite_disk(const Tex& tx, const bhr_shade_params& P, const
 
 // Shades every pixel of one view from its hit records; rgba[4 k + c], k = j * width + i.
 inline void shade_view(const Tex& tx, const bhr_shade_params& P, const bhr_view& v, const bhr_hit* hits, float* rgba,
-                       int64_t row_begin, int64_t row_end) {
+                       int64_t row_begin, int64_t row_end, const float* rgbt = nullptr) {
     const int W = v.width, H = v.height;
     const F3 cam{v.cam_pos[0], v.cam_pos[1], v.cam_pos[2]};
     const float rcam = length(cam);
@@ -423,7 +460,7 @@ inline void shade_view(const Tex& tx, const bhr_shade_params& P, const bhr_view&
     const float g = mixf(1.0f, 1.0f / std::sqrt(std::fmax(1.0f - 2.0f / rcam, 1e-4f)), P.doppler_strength);
     const float g4 = g * g * g * g;
     auto state = [&](int i, int j) {
-        return composite_disk(tx, P, v, hits[int64_t(j) * W + i], i, j, rcam);
+        return composite_disk(tx, P, v, hits[int64_t(j) * W + i], i, j, rcam, rgbt);
     };
     for (int64_t j = row_begin; j < row_end; ++j)
         for (int i = 0; i < W; ++i) {

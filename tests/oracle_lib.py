@@ -50,6 +50,10 @@ def lib():
         L.oracle_blackbody_lut.argtypes = [ctypes.c_void_p]
         L.oracle_shade_view.argtypes = [VP, ctypes.c_void_p, ctypes.POINTER(ShadeParams), ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.oracle_trace_volumetric.argtypes = [VP, ctypes.POINTER(ShadeParams), ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.oracle_shade_volumetric.argtypes = [VP, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ShadeParams),
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.oracle_redshift_factor.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.oracle_redshift_factor.restype = ctypes.c_float
         L.oracle_blackbody_xyz.argtypes = [ctypes.c_double, D]
@@ -192,3 +196,29 @@ def pcg3d(v) -> tuple[int, int, int]:
 
 def to_half(x: float) -> int:
     return int(lib().oracle_to_half(x))
+
+
+def trace_volumetric(view: View, params: ShadeParams, noise: np.ndarray, lut: np.ndarray, fp64: bool = True,
+                     threads: int | None = None):
+    """The volumetric disk's march of every pixel: (records, rgbt (height, width, 4))."""
+    noise = np.ascontiguousarray(noise, dtype=np.uint16)
+    lut = np.ascontiguousarray(lut, dtype=np.float32)
+    hits = np.zeros(view.width * view.height, dtype=HIT_DTYPE)
+    rgbt = np.zeros((view.height, view.width, 4), dtype=np.float32)
+    rc = lib().oracle_trace_volumetric(ctypes.byref(view), ctypes.byref(params), noise.ctypes.data, lut.ctypes.data,
+                                       hits.ctypes.data, rgbt.ctypes.data, threads or nthreads(), int(fp64))
+    assert rc == 0
+    return hits, rgbt
+
+
+def shade_volumetric(view: View, hits: np.ndarray, rgbt: np.ndarray, params: ShadeParams, noise: np.ndarray,
+                     lut: np.ndarray, threads: int | None = None) -> np.ndarray:
+    hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    rgbt = np.ascontiguousarray(rgbt, dtype=np.float32)
+    out = np.zeros((view.height, view.width, 4), dtype=np.float32)
+    rc = lib().oracle_shade_volumetric(ctypes.byref(view), hits.ctypes.data, rgbt.ctypes.data, ctypes.byref(params),
+                                       np.ascontiguousarray(noise, dtype=np.uint16).ctypes.data,
+                                       np.ascontiguousarray(lut, dtype=np.float32).ctypes.data, out.ctypes.data,
+                                       threads or nthreads())
+    assert rc == 0
+    return out
