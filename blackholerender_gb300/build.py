@@ -33,7 +33,7 @@ def _nvcc() -> str:
 DEVICE_FLAGS = {"kernels.cu": ["-ftz=true"], "surrogate.cu": ["-ftz=true"], "lens.cu": ["-ftz=true"],
                 # shading: IEEE +, -, *, / and sqrt without contraction, so that the noise volume
                 # and every non-transcendental step round as the CPU restatement does
-                "shade.cu": ["-fmad=false"], "vol.cu": ["-ftz=true"]}
+                "shade.cu": ["-fmad=false"], "vol.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]}
 
 
 def _flags() -> list[str]:

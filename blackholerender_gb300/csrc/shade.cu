@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
     const bhr_shade_params& P = A.p;
     const F3 cam{A.cam[0], A.cam[1], A.cam[2]};
     const float rcam = len(cam);
+    const DiskConsts C = disk_consts(P, rcam);
     const F3 dir = primary_dir(A, i, j);
     __syncthreads();  // the table is staged
 
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
             const float cr[3] = {w2.z, w2.w, w3.x}, cp[3] = {w3.y, w3.z, w3.w};
             const float b_axis = w2.x;
             for (int k = 0; k < ncross && k < 3; ++k) {
-                const float4 dk = thin_disk_sample(tx, P, A.disk_inner, A.disk_outer, cr[k], cp[k], b_axis, rcam);
+                const float4 dk = thin_disk_sample(tx, P, C, A.disk_inner, A.disk_outer, cr[k], cp[k], b_axis);
                 col = add(col, F3{trans * dk.x * dk.w, trans * dk.y * dk.w, trans * dk.z * dk.w});
                 trans *= 1.0f - dk.w;
                 if (trans < 0.004f) {

@@ -86,8 +86,9 @@ __device__ inline float noise_sample(const Tex& tx, F3 c) {
     const float ux = c.x * float(kN) - 0.5f, uy = c.y * float(kN) - 0.5f, uz = c.z * float(kN) - 0.5f;
     const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
     const float ax = ux - fx, ay = uy - fy, az = uz - fz;
-    const int x0 = ((int(fx) % kN) + kN) % kN, y0 = ((int(fy) % kN) + kN) % kN, z0 = ((int(fz) % kN) + kN) % kN;
-    const int x1 = (x0 + 1) % kN, y1 = (y0 + 1) % kN, z1 = (z0 + 1) % kN;
+    // REPEAT: the wrap of a power-of-two size is a mask (two's complement for negative texels)
+    const int x0 = int(fx) & (kN - 1), y0 = int(fy) & (kN - 1), z0 = int(fz) & (kN - 1);
+    const int x1 = (x0 + 1) & (kN - 1), y1 = (y0 + 1) & (kN - 1), z1 = (z0 + 1) & (kN - 1);
     const float c00 = mixf(texel(tx, x0, y0, z0), texel(tx, x1, y0, z0), ax);
     const float c10 = mixf(texel(tx, x0, y1, z0), texel(tx, x1, y1, z0), ax);
     const float c01 = mixf(texel(tx, x0, y0, z1), texel(tx, x1, y0, z1), ax);
@@ -97,28 +98,54 @@ __device__ inline float noise_sample(const Tex& tx, F3 c) {
 
 __device__ __forceinline__ float glsl_mod(float x, float y) { return x - y * floorf(x / y); }
 
-// disk.glsl:45-63 diskNoise: two phase-shifted copies of the flow-advected noise, cross-faded
-__device__ __forceinline__ float disk_noise(const Tex& tx, const bhr_shade_params& P, float r, float phi, float y_over_h) {
-    const float omega = gpow(r, -1.5f);
+// The constants of a view that diskNoise and the redshift recompute per sample in the shader:
+// the flow clock's two phases and cross-fade, the azimuthal repeat, the camera's lapse.
+struct DiskConsts {
+    float t1, t2, w2, k, lapse_cam;
+};
+__device__ __forceinline__ DiskConsts disk_consts(const bhr_shade_params& P, float rcam) {
+    DiskConsts C;
     const float t = P.disk_time;
     const float Pd = 60.0f;
-    const float t1 = glsl_mod(t, Pd);
-    const float t2 = glsl_mod(t + 0.5f * Pd, Pd);
-    const float w2 = fabsf(2.0f * t1 / Pd - 1.0f);
+    C.t1 = glsl_mod(t, Pd);
+    C.t2 = glsl_mod(t + 0.5f * Pd, Pd);
+    C.w2 = fabsf(2.0f * C.t1 / Pd - 1.0f);
     const float rep = fmaxf(1.0f, floorf(2.0f * P.disk_noise_scale + 0.5f));
+    C.k = rep / kTwoPi;
+    C.lapse_cam = sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f));
+    return C;
+}
+
+// x^y and its parts for x >= 0 as the SFU computes it, 2^(y log2 x) (0 at x = 0 for y > 0);
+// several powers of one base share its log2
+__device__ __forceinline__ float lg2a(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float ex2a(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// disk.glsl:45-63 diskNoise: two phase-shifted copies of the flow-advected noise, cross-faded;
+// omega = keplerOmega(r) = r^-1.5
+__device__ __forceinline__ float disk_noise(const Tex& tx, const bhr_shade_params& P, const DiskConsts& C, float r,
+                                            float phi, float y_over_h, float omega) {
     const float lr = glog(r) * 3.2f * P.disk_noise_scale;
     const float yy = y_over_h * 0.35f;
-    const float k = rep / kTwoPi;
-    const F3 c1{(phi + omega * t1) * k, lr + P.disk_inflow * omega * t1, yy};
-    const F3 c2{(phi + omega * t2) * k, lr + 0.37f + P.disk_inflow * omega * t2, yy + 0.61f};
-    return mixf(noise_sample(tx, c1), noise_sample(tx, c2), w2);
+    const F3 c1{(phi + omega * C.t1) * C.k, lr + P.disk_inflow * omega * C.t1, yy};
+    const F3 c2{(phi + omega * C.t2) * C.k, lr + 0.37f + P.disk_inflow * omega * C.t2, yy + 0.61f};
+    return mixf(noise_sample(tx, c1), noise_sample(tx, c2), C.w2);
 }
 
 // thinDiskSample (disk.glsl:113-129) at a recorded crossing: radiance (rgb) and alpha
-__device__ inline float4 thin_disk_sample(const Tex& tx, const bhr_shade_params& P, float r_in, float r_out, float r, float phi,
-                                   float b_axis, float rcam) {
+__device__ inline float4 thin_disk_sample(const Tex& tx, const bhr_shade_params& P, const DiskConsts& C, float r_in,
+                                          float r_out, float r, float phi, float b_axis) {
     if (r < r_in || r > r_out) return make_float4(0.f, 0.f, 0.f, 0.f);
-    const float n = disk_noise(tx, P, r, phi, 0.0f);
+    const float omega = gpow(r, -1.5f);
+    const float n = disk_noise(tx, P, C, r, phi, 0.0f, omega);
     const float f = smoothstep(0.32f, 0.78f, n);
     const float pattern = mixf(1.0f, mixf(0.08f, 1.4f, f), P.disk_noise_strength);
     const float emit = mixf(1.0f, mixf(0.22f, 1.35f, f * f), P.disk_noise_strength);
@@ -132,9 +159,8 @@ __device__ inline float4 thin_disk_sample(const Tex& tx, const bhr_shade_params&
     const float prof = gpow(x, 0.75f) * gpow(fmaxf(1.0f - sqrtf(x), 0.0f), 0.25f) / 0.48796f;
     const float T = P.disk_peak_temp * prof * mixf(1.0f, 0.85f + 0.3f * emit, 0.5f);
     // redshiftFactor (disk.glsl:36-41)
-    const float omega = gpow(r, -1.5f);
     const float ut = 1.0f / sqrtf(fmaxf(1.0f - 3.0f / r, 0.02f));
-    const float lapse = sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f));
+    const float lapse = C.lapse_cam;
     const float g_phys = 1.0f / (lapse * ut * fmaxf(1.0f - omega * b_axis, 0.05f));
     const float g = mixf(1.0f, g_phys, P.doppler_strength);
     const float4 bb = blackbody(tx, T * g);
@@ -151,32 +177,36 @@ __device__ inline float4 thin_disk_sample(const Tex& tx, const bhr_shade_params&
 
 // volumetricDiskStep (disk.glsl:88-110) with diskDensity (:88-99): emission and absorption of
 // one march segment of length ds centred at p (r = |p.xz|), front to back into col / trans.
-__device__ inline void vol_disk_step(const Tex& tx, const bhr_shade_params& P, float r_in, float r_out, float thick, F3 p,
-                              float r, float ds, float b_axis, float rcam, F3& col, float& trans) {
+// The radial profile is taken first: where it is zero the sample adds nothing (dens < 1e-4).
+__device__ inline void vol_disk_step(const Tex& tx, const bhr_shade_params& P, const DiskConsts& C, float r_in,
+                                     float r_out, float thick, F3 p, float r, float ds, float b_axis, F3& col,
+                                     float& trans) {
+    const float inner = smoothstep(r_in, r_in + 0.25f, r);
+    const float outer = 1.0f - smoothstep(r_out * 0.55f, r_out, r);
+    if (inner * outer == 0.0f) return;
+    const float x = r_in / fmaxf(r, r_in);
+    const float lx = lg2a(x);                     // x^1.2, x^0.75, x^0.6 share log2 x
+    const float radial = inner * outer * ex2a(1.2f * lx);
+    const float omega = ex2a(-1.5f * lg2a(r));    // keplerOmega(r)
     const float H = fmaxf(thick * r, 1e-3f);
     const float yh = p.y / H;
     const float vert = gexp(-yh * yh);
     const float phi = atan2f(p.z, p.x);
-    const float n = disk_noise(tx, P, r, phi, yh);
+    const float n = disk_noise(tx, P, C, r, phi, yh, omega);
     const float f = smoothstep(0.32f, 0.78f, n);
     const float pattern = mixf(1.0f, mixf(0.08f, 1.4f, f), P.disk_noise_strength);
     const float emit = mixf(1.0f, mixf(0.22f, 1.35f, f * f), P.disk_noise_strength);
     const float puff = 1.0f + 0.6f * smoothstep(r_out * 0.4f, r_out, r) * (n - 0.5f);
-    const float inner = smoothstep(r_in, r_in + 0.25f, r);
-    const float outer = 1.0f - smoothstep(r_out * 0.55f, r_out, r);
-    const float radial = inner * outer * gpow(r_in / fmaxf(r, r_in), 1.2f);
     const float dens = P.disk_density * radial * vert * pattern * fmaxf(puff, 0.0f);
     if (dens < 1e-4f) return;
-    const float x = r_in / fmaxf(r, r_in);
-    const float prof = gpow(x, 0.75f) * gpow(fmaxf(1.0f - sqrtf(x), 0.0f), 0.25f) / 0.48796f;
+    const float prof = ex2a(0.75f * lx) * ex2a(0.25f * lg2a(fmaxf(1.0f - sqrtf(x), 0.0f))) / 0.48796f;
     const float T = P.disk_peak_temp * prof * mixf(1.0f, 0.85f + 0.3f * emit, 0.5f);
-    const float omega = gpow(r, -1.5f);
     const float ut = 1.0f / sqrtf(fmaxf(1.0f - 3.0f / r, 0.02f));
-    const float lapse = sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f));
+    const float lapse = C.lapse_cam;
     const float g_phys = 1.0f / (lapse * ut * fmaxf(1.0f - omega * b_axis, 0.05f));
     const float g = mixf(1.0f, g_phys, P.doppler_strength);
     const float4 bb = blackbody(tx, T * g);
-    const float inward = gpow(r_in / fmaxf(r, r_in), 0.6f);
+    const float inward = ex2a(0.6f * lx);
     const float w = P.disk_warmth;
     const float s = bb.w * P.disk_brightness * emit * inward;
     const F3 source{bb.x * mixf(1.0f, 1.0f, w) * s, bb.y * mixf(1.0f, 0.80f, w) * s, bb.z * mixf(1.0f, 0.58f, w) * s};

@@ -47,8 +47,8 @@ __global__ void __launch_bounds__(256) k_march_vol(const __grid_constant__ VolAr
     F3 col{0.f, 0.f, 0.f};
     float trans = 1.0f;
     const bool lensing = R.lensing != 0;
-    const float rcam = w.rcam;
     const float b_axis = ri.b_axis;
+    const shading::DiskConsts C = shading::disk_consts(A.p, w.rcam);
     if (R.far_mode) {
         status = BHR_STATUS_ESCAPED;
     } else {
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_march_vol(const __grid_constant__ VolAr
                                h00 * x0.z + h10 * m0.z + h01 * x.z + h11 * m1.z};
                     const float rm = sqrtf(p.x * p.x + p.z * p.z);
                     if (rm > R.disk_inner - 0.5f && rm < R.disk_outer && fabsf(p.y) < R.slab * rm)
-                        shading::vol_disk_step(tx, A.p, R.disk_inner, R.disk_outer, A.thick, p, rm, sub, b_axis, rcam, col,
+                        shading::vol_disk_step(tx, A.p, C, R.disk_inner, R.disk_outer, A.thick, p, rm, sub, b_axis, col,
                                                trans);
                     if (trans < 0.004f) break;
                 }
