@@ -42,15 +42,14 @@ enum DiskMode : int { DISK_NONE = 0, DISK_THIN = 1, DISK_VOLUMETRIC = 2 };
 enum Preset : int { PRESET_LOW = 0, PRESET_MEDIUM = 1, PRESET_HIGH = 2, PRESET_ULTRA = 3, PRESET_CUSTOM = 4 };
 
 // The traced fields of the reference's Settings (those it marks BHS_TRACE, Settings.cpp:76-88),
-// with its defaults, except the disk mode: the volumetric disk is not part of this path, so
-// the default here is the thin disk.
+// with its defaults: the volumetric disk at the High preset.
 struct Settings {
     int preset = PRESET_HIGH;
     float renderScale = 1.0f;
     int maxSteps = 450;
     float stepScale = 0.05f;
     float diskStep = 0.18f;
-    int diskMode = DISK_THIN;
+    int diskMode = DISK_VOLUMETRIC;
     bool lensing = true;
     float diskInner = 6.0f;
     float diskOuter = 20.0f;
@@ -235,7 +234,9 @@ public:
         return true;
     }
 
-    // Traces a frame into the Renderer's own device records (hits(), internal size).
+    // Traces a frame into the Renderer's own device records (hits(), internal size). With the
+    // volumetric disk the march also gathers the disk's light into image() (rgb, transmittance),
+    // which renderImage() completes; the volumetric march is FP32.
     bool render(const FrameInput& in, int precision = BHR_PREC_FP32) {
         if (!ctx_ && !init(device_)) return false;
         bhr_view v{};
@@ -252,17 +253,34 @@ public:
         width_ = v.width;
         height_ = v.height;
         bhr_hit* const outs[1] = {records_};
+        if (v.disk_mode == BHR_DISK_VOLUMETRIC) {
+            bhr_shade_params p{};
+            if (!makeShadeParams(in, &p) || !ensureImage(n)) return logError("render: volumetric disk", nullptr);
+            float* const rgbt[1] = {image_};
+            if (bhr_trace_volumetric(ctx_, &v, 1, outs, &p, rgbt, nullptr) != BHR_OK) return logError("render", ctx_);
+            return true;
+        }
         if (bhr_trace(ctx_, &v, 1, outs, precision, BHR_METHOD_PLAIN, nullptr) != BHR_OK)
             return logError("render", ctx_);
         return true;
     }
 
-    // Traces into caller-owned device records (at least internalSize() pixels) on `stream`.
-    bool renderTo(const FrameInput& in, bhr_hit* out_dev, cudaStream_t stream, int precision = BHR_PREC_FP32) {
+    // Traces into caller-owned device records (at least internalSize() pixels) on `stream`;
+    // the volumetric disk also needs rgbt_dev (as many float4).
+    bool renderTo(const FrameInput& in, bhr_hit* out_dev, cudaStream_t stream, int precision = BHR_PREC_FP32,
+                  float* rgbt_dev = nullptr) {
         if (!ctx_ && !init(device_)) return false;
         bhr_view v{};
         if (!makeView(in, &v)) return logError("renderTo: incomplete FrameInput", nullptr);
         bhr_hit* const outs[1] = {out_dev};
+        if (v.disk_mode == BHR_DISK_VOLUMETRIC) {
+            bhr_shade_params p{};
+            if (!rgbt_dev || !makeShadeParams(in, &p))
+                return logError("renderTo: the volumetric disk needs an rgbt buffer", nullptr);
+            float* const rgbt[1] = {rgbt_dev};
+            if (bhr_trace_volumetric(ctx_, &v, 1, outs, &p, rgbt, stream) != BHR_OK) return logError("renderTo", ctx_);
+            return true;
+        }
         if (bhr_trace(ctx_, &v, 1, outs, precision, BHR_METHOD_PLAIN, stream) != BHR_OK)
             return logError("renderTo", ctx_);
         return true;
@@ -274,6 +292,12 @@ public:
         bhr_view v{};
         if (!makeView(in, &v)) return logError("renderHost: incomplete FrameInput", nullptr);
         out.resize(size_t(v.width) * size_t(v.height));
+        if (v.disk_mode == BHR_DISK_VOLUMETRIC) {  // device march, then one copy
+            if (!render(in, precision)) return false;
+            if (cudaMemcpy(out.data(), records_, out.size() * sizeof(bhr_hit), cudaMemcpyDeviceToHost) != cudaSuccess)
+                return logError("renderHost: copy", nullptr);
+            return true;
+        }
         bhr_hit* const outs[1] = {out.data()};
         if (bhr_trace_host(ctx_, &v, 1, outs, precision, BHR_METHOD_PLAIN) != BHR_OK)
             return logError("renderHost", ctx_);
@@ -287,15 +311,7 @@ public:
         bhr_view v{};
         bhr_shade_params p{};
         if (!makeView(in, &v) || !makeShadeParams(in, &p)) return logError("renderImage: incomplete FrameInput", nullptr);
-        const size_t n = size_t(v.width) * size_t(v.height);
-        if (n > image_capacity_) {
-            if (image_) cudaFree(image_);
-            image_ = nullptr;
-            image_capacity_ = 0;
-            if (cudaMalloc(&image_, n * 4 * sizeof(float)) != cudaSuccess)
-                return logError("renderImage: cannot allocate the image", nullptr);
-            image_capacity_ = n;
-        }
+        if (!ensureImage(size_t(v.width) * size_t(v.height))) return false;
         const bhr_hit* const hits[1] = {records_};
         float* const outs[1] = {image_};
         if (bhr_shade(ctx_, &v, 1, hits, &p, outs, nullptr) != BHR_OK) return logError("renderImage", ctx_);
@@ -309,6 +325,17 @@ public:
     bhr_ctx* context() const { return ctx_; }
 
 private:
+    bool ensureImage(size_t n) {
+        if (n <= image_capacity_) return true;
+        if (image_) cudaFree(image_);
+        image_ = nullptr;
+        image_capacity_ = 0;
+        if (cudaMalloc(&image_, n * 4 * sizeof(float)) != cudaSuccess)
+            return logError("cannot allocate the image", nullptr);
+        image_capacity_ = n;
+        return true;
+    }
+
     bool logError(const char* what, const bhr_ctx* c) {
         const char* m = bhr_last_error(c);
         const std::string line = std::string("bhr: ") + what + (m && *m ? std::string(": ") + m : std::string());

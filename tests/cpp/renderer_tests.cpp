@@ -100,7 +100,7 @@ static void testFrameToView() {
     CHECK(v.max_steps == 200 && v.step_scale == 0.10f && v.disk_step == 0.35f, "preset fields carried");
     CHECK(std::fabs(v.tan_half_fov - std::tan(60.0f * 0.01745329252f * 0.5f)) < 1e-7f, "tan(fov/2) as Renderer.cpp:246");
     CHECK(v.r_esc_min == 30.0f, "shader rEscMin = max(1.25 r_out, 12)");
-    CHECK(v.disk_mode == BHR_DISK_THIN && v.lensing == 1 && v.far_mode == 0, "disk, lensing and far mode carried");
+    CHECK(v.disk_mode == BHR_DISK_VOLUMETRIC && v.lensing == 1 && v.far_mode == 0, "disk (the default, volumetric), lensing and far mode carried");
     CHECK(std::fabs(v.cam_pos[1] - float(30.0 * std::cos(85.0 * M_PI / 180.0))) < 1e-5f, "camera position carried");
     s.renderScale = 0.001f;
     bhr::Renderer::makeView(in, &v);
@@ -163,6 +163,7 @@ static int testGpu(const char* path) {
     }
     bhr::Settings s;
     s.applyPreset(bhr::PRESET_LOW);
+    s.diskMode = bhr::DISK_THIN;
     const bhr::Camera cam = orbitCamera(30.0, 85.0 * M_PI / 180.0, 0.0);
     bhr::FrameInput in;
     in.camera = &cam;
@@ -217,6 +218,28 @@ static int testGpu(const char* path) {
     const bool wrote_img = g && std::fwrite(img.data(), sizeof(float), img.size(), g) == img.size();
     if (g) std::fclose(g);
     CHECK(wrote_img, "image written");
+    // the reference's default disk: volumetric, its light gathered by the march
+    bhr::Settings sv;
+    sv.applyPreset(bhr::PRESET_LOW);
+    CHECK(sv.diskMode == bhr::DISK_VOLUMETRIC, "the default disk is volumetric (Settings.h:22)");
+    bhr::FrameInput iv = in;
+    iv.settings = &sv;
+    CHECK(R.renderImage(iv), "renderImage with the volumetric disk");
+    std::vector<bhr_hit> hv(n);
+    std::vector<float> imv(n * 4);
+    cudaMemcpy(hv.data(), R.hits(), n * sizeof(bhr_hit), cudaMemcpyDeviceToHost);
+    cudaMemcpy(imv.data(), R.image(), imv.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    int vlit = 0, vcross = 0;
+    for (size_t k = 0; k < n; ++k) {
+        vlit += imv[4 * k] + imv[4 * k + 1] + imv[4 * k + 2] > 0.0f;
+        vcross += hv[k].ncross;
+    }
+    std::snprintf(msg, sizeof msg, "%d of %zu pixels lit, no crossing slots (%d)", vlit, n, vcross);
+    CHECK(vlit > int(n / 2) && vcross == 0, msg);
+    std::vector<bhr_hit> hh;
+    CHECK(R.renderHost(iv, hh) && hh.size() == n && std::memcmp(hh.data(), hv.data(), n * sizeof(bhr_hit)) == 0,
+          "renderHost = render with the volumetric disk");
+    CHECK(!R.renderTo(iv, nullptr, nullptr) && !logged.empty(), "renderTo without an rgbt buffer is refused");
     R.shutdown();
     return 0;
 }
