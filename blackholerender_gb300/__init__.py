@@ -15,7 +15,7 @@ from . import _abi
 from ._abi import (  # noqa: F401
     DISK_NONE, DISK_THIN, DISK_VOLUMETRIC, FLAG_FALLBACK, FLAG_FP64, FLAG_NONFINITE, FLAG_SURROGATE,
     HIT_DTYPE, METHOD_PLAIN, METHOD_SURROGATE, PREC_FP32, PREC_MIXED, SQRT27, STATUS_BUDGET,
-    STATUS_CAPTURED, STATUS_ESCAPED, STATUS_OPAQUE, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, LaunchShape, Options,
+    STATUS_CAPTURED, STATUS_ESCAPED, STATUS_OPAQUE, STATUS_BODY, Body, BODY_HIT_DTYPE, TERM_CONFIG, TERM_CPU, TERM_SHADER, BhrError, LaunchShape, Options,
     ShadeParams, Stats, View,
 )
 
@@ -218,6 +218,25 @@ class Tracer:
         _abi.check(_abi.lib().bhr_trace_volumetric(self._ctx, arr, n, hp, ctypes.byref(params), op,
                                                    ctypes.c_void_p(stream.cuda_stream)), self._ctx)
         return hits, rgbt
+
+    def trace_bodies(self, view: View, bodies: Sequence[Body], hits=None, body_hits=None, stream=None):
+        """bhr_trace_bodies: one view marched with bodies. Returns (hits, body_hits): uint8 device
+        tensors of bhr_hit and bhr_body_hit records."""
+        import torch
+
+        dev = torch.device("cuda", self.device)
+        if hits is None:
+            hits = torch.empty(view.rays * HIT_BYTES, dtype=torch.uint8, device=dev)
+        if body_hits is None:
+            body_hits = torch.empty(view.rays * 64, dtype=torch.uint8, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        n = len(bodies)
+        arr = (Body * max(n, 1))(*bodies)
+        _abi.check(_abi.lib().bhr_trace_bodies(self._ctx, ctypes.byref(view), arr, n, ctypes.c_void_p(hits.data_ptr()),
+                                               ctypes.c_void_p(body_hits.data_ptr()),
+                                               ctypes.c_void_p(stream.cuda_stream)), self._ctx)
+        return hits, body_hits
 
     def noise_bake(self, seed: int = 7, out=None, stream=None):
         """bhr_noise_bake: the disk's 128^3 noise volume as a device int16 tensor of half bits."""

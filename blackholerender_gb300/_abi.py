@@ -25,6 +25,7 @@ STATUS_ESCAPED = 1
 STATUS_CAPTURED = 2
 STATUS_BUDGET = 3
 STATUS_OPAQUE = 4
+STATUS_BODY = 5
 
 FLAG_FP64 = 0x01
 FLAG_SURROGATE = 0x02
@@ -138,6 +139,22 @@ class ShadeParams(ctypes.Structure):
     ]
 
 
+class Body(ctypes.Structure):
+    """bhr_body: the reference's BodyGpu (src/Bodies.h:40-49)."""
+
+    _fields_ = [(f, ctypes.c_float * 4) for f in ("pos_radius", "rel_pos", "look", "tint", "light", "light_color",
+                                                  "axis", "ring")]
+
+
+MAX_BODIES = 32
+
+# numpy view of bhr_body_hit (64 bytes)
+BODY_HIT_DTYPE = np.dtype([("body", np.int32), ("t", np.float32), ("ro", np.float32, (3,)), ("rd", np.float32, (3,)),
+                           ("x", np.float32, (3,)), ("near_mask", np.uint32), ("near_idx", np.int32),
+                           ("near_t", np.float32), ("travelled", np.float32), ("reserved", np.float32)])
+assert BODY_HIT_DTYPE.itemsize == 64
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("rays", ctypes.c_uint64),
@@ -202,6 +219,7 @@ SIGNATURES = {
                                  ctypes.POINTER(_P), _P]),
     "bhr_trace_volumetric": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(ShadeParams),
                                             ctypes.POINTER(_P), _P]),
+    "bhr_trace_bodies": (ctypes.c_int, [_P, _VP, ctypes.POINTER(Body), ctypes.c_int, _P, _P, _P]),
     "bhr_noise_bake": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P]),
     "bhr_blackbody_lut": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "bhr_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),

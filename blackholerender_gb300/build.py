@@ -17,7 +17,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libbhr.so"
-SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu", "surrogate_api.cu", "lens.cu", "shade.cu", "vol.cu"]
+SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu", "surrogate_api.cu", "lens.cu", "shade.cu", "vol.cu", "bodies.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,7 +33,8 @@ def _nvcc() -> str:
 DEVICE_FLAGS = {"kernels.cu": ["-ftz=true"], "surrogate.cu": ["-ftz=true"], "lens.cu": ["-ftz=true"],
                 # shading: IEEE +, -, *, / and sqrt without contraction, so that the noise volume
                 # and every non-transcendental step round as the CPU restatement does
-                "shade.cu": ["-fmad=false"], "vol.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]}
+                "shade.cu": ["-fmad=false"], "vol.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
+                "bodies.cu": ["-ftz=true"]}
 
 
 def _flags() -> list[str]:

@@ -18,6 +18,7 @@
 #include "bhr.h"
 #include "host_views.h"
 #include "kernels.cuh"
+#include "bodies.cuh"
 #include "shade.cuh"
 #include "vol.cuh"
 
@@ -687,6 +688,38 @@ int bhr_blackbody_lut(float* out) {
     if (!out) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_blackbody_lut: NULL argument");
     bhr::blackbody_lut_host(out);
     return BHR_OK;
+}
+
+int bhr_trace_bodies(bhr_ctx* c, const bhr_view* view, const bhr_body* bodies, int nbodies, bhr_hit* hits,
+                     bhr_body_hit* body_out, void* cuda_stream) {
+    if (!c || !view || !hits || !body_out || nbodies < 0 || (nbodies > 0 && !bodies))
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: NULL argument");
+    if (nbodies > BHR_MAX_BODIES)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: at most BHR_MAX_BODIES (32) bodies per view");
+    const bhr_view& v = *view;
+    if (v.width <= 0 || v.height <= 0 || v.max_steps < 0)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: width and height must be positive, max_steps >= 0");
+    if (v.disk_mode != BHR_DISK_NONE && v.disk_mode != BHR_DISK_THIN)
+        return fail(c, BHR_ERR_UNSUPPORTED, "bhr_trace_bodies: bodies are marched with a thin disk or none");
+    if (v.term_mode != BHR_TERM_SHADER && v.term_mode != BHR_TERM_CONFIG)
+        return fail(c, BHR_ERR_UNSUPPORTED, "bhr_trace_bodies: bodies are marched under the SHADER or CONFIG rule");
+    if (reinterpret_cast<uintptr_t>(hits) % 16 != 0 || reinterpret_cast<uintptr_t>(body_out) % 16 != 0)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: buffers must be 16-byte aligned");
+    for (int k = 0; k < nbodies; ++k)
+        if (!(bodies[k].pos_radius[3] > 0.0f))
+            return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: body " + std::to_string(k) + " has no positive radius");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    bhr::BodyArgs a{};
+    a.view = bhr::host::make_dev_view(v, hits);
+    a.rule = bhr::host::make_rule(v);
+    a.nbodies = nbodies;
+    a.body_out = body_out;
+    for (int k = 0; k < nbodies; ++k) a.bodies[k] = bodies[k];
+    const cudaError_t e = bhr::launch_march_bodies(a, static_cast<cudaStream_t>(cuda_stream));
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? BHR_OK : cuda_fail(c, e, "bhr_trace_bodies");
 }
 
 int bhr_noise_bake(bhr_ctx* c, uint32_t seed, uint16_t* out, void* cuda_stream) {

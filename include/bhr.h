@@ -47,6 +47,7 @@ extern "C" {
 #define BHR_STATUS_CAPTURED 2  /* blackhole.frag status 2 (horizon test) */
 #define BHR_STATUS_BUDGET 3    /* step budget ran out; blackhole.frag:252 shades it as captured */
 #define BHR_STATUS_OPAQUE 4    /* volumetric disk: transmittance fell below 0.004 (blackhole.frag:234 status 3) */
+#define BHR_STATUS_BODY 5      /* the march hit a body (blackhole.frag status 4) */
 
 /* ---- bhr_hit.flags ----------------------------------------------------------------- */
 #define BHR_FLAG_FP64 0x01       /* some or all of the march ran in FP64 (mixed precision) */
@@ -366,6 +367,42 @@ int bhr_noise_bake(bhr_ctx* ctx, uint32_t seed, uint16_t* out_dev, void* cuda_st
 /* The blackbody table (DiskTextures::bakeBlackbodyLut) into host memory: BHR_BLACKBODY_LUT x 4
  * floats, entry i at T = exp(log 1000 + (log 40000 - log 1000) i / 255). */
 int bhr_blackbody_lut(float* out_host);
+
+/* ---- bodies: planets and stars in the march (the BHS_BODIES variant) ------------------ */
+/* Spheres the march can hit (blackhole.frag:101-121,146-150,182-190,236-250): near-field
+ * bodies settled by a straight camera-relative ray while the geodesic has not bent away from
+ * it; short steps near the others and an intersection test on each step's chord. The layout is
+ * the reference's BodyGpu (src/Bodies.h:40-49, shaders/bodies.glsl:12-21), as packBodies fills
+ * it: at most BHR_MAX_BODIES per view (the shader's 32-bit masks). */
+#define BHR_MAX_BODIES 32
+typedef struct bhr_body {
+    float pos_radius[4];   /* xyz centre relative to the hole (M), w radius */
+    float rel_pos[4];      /* xyz centre relative to the camera, w kind (0 planet, 1 star) */
+    float look[4];         /* x look id, y seed, z atmosphere / plumes, w rotation (rad) */
+    float tint[4];         /* rgb albedo tint, w turbulence (stars) */
+    float light[4];        /* xyz unit direction towards its light, w intensity */
+    float light_color[4];  /* rgb light colour, a effective temperature (stars, K) */
+    float axis[4];         /* xyz unit spin / ring axis */
+    float ring[4];         /* x inner, y outer ring radius (0: none), z phase, w opacity */
+} bhr_body;
+/* What the shading after the loop needs of a body-aware march, per pixel (64 bytes). */
+typedef struct bhr_body_hit {
+    int32_t body;          /* hitBody: the body the march hit, -1 none */
+    float t;               /* hitT: distance along the hit chord */
+    float ro[3];           /* hitRo: start of the hit chord (hole frame) */
+    float rd[3];           /* hitRd: unit direction of the hit chord */
+    float x[3];            /* the ray's last position (the far-side straight test starts there) */
+    uint32_t near_mask;    /* bodies settled by the near-field test */
+    int32_t near_idx;      /* body the near-field straight ray hits, -1 none */
+    float near_t;          /* its distance along that ray */
+    float travelled;       /* path length marched */
+    float reserved;
+} bhr_body_hit;
+/* Marches one view (thin or no disk, SHADER or CONFIG rule) with `nbodies` bodies (host
+ * array): hits_dev gets the records (status BHR_STATUS_BODY when a body stopped the ray),
+ * body_dev width x height bhr_body_hit. Stream-ordered. */
+int bhr_trace_bodies(bhr_ctx* ctx, const bhr_view* view, const bhr_body* bodies, int nbodies, bhr_hit* hits_dev,
+                     bhr_body_hit* body_dev, void* cuda_stream);
 
 /* ---- launch shapes and the autotuner ------------------------------------------------ */
 /* No counterpart in the reference (its march is one fragment-shader draw whose scheduling the

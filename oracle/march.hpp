@@ -15,6 +15,8 @@
 //   shaders/blackhole.frag:169-181,217-234  volumetric disk: the 6 diskStep clamp in the slab,
 //                                     Hermite sub-samples of each RK4 segment, opacity stop
 //                                     (the sample itself is the caller's `vol`, oracle/shade.hpp)
+//   shaders/blackhole.frag:101-121,146-150,182-190,236-250  bodies (BHS_BODIES 1): near-field
+//                                     straight test, step clamps, chord intersections (`bod`)
 //   src/physics/Geodesic.h:107-140    trace(), the CPU mirror's loop (BHR_TERM_CPU)
 // Vector formulas follow GLM/GLSL definitions (dot = (x+y)+z, normalize = v * (1/sqrt(dot)),
 // mix(a,b,t) = a*(1-t) + b*t) so the double path reproduces the reference's CPU code bit for
@@ -154,6 +156,90 @@ struct NoVolume {
     template <class... A> void operator()(A&&...) const {}
 };
 
+// The march without bodies (BHS_BODIES 0).
+template <class T> struct NoBodies {
+    void setup(const V3<T>&, const V3<T>&, const V3<T>&, bool, T) {}
+    bool reached_near() const { return false; }
+    T clamp(const V3<T>&, T ds) const { return ds; }
+    void advance(T) {}
+    bool chord(const V3<T>&, const V3<T>&, T) { return false; }
+};
+
+// shaders/bodies.glsl:34-44 raySphere: nearest hit in (tMin, tMax), -1 if none
+template <class T> inline T raySphere(V3<T> ro, V3<T> rd, V3<T> c, T r, T tMin, T tMax) {
+    const V3<T> oc = ro - c;
+    const T b = dot(oc, rd);
+    const T cc = dot(oc, oc) - r * r;
+    const T disc = b * b - cc;
+    if (disc < T(0)) return T(-1);
+    const T s = std::sqrt(disc);
+    T t = -b - s;
+    if (t <= tMin) t = -b + s;  // inside the sphere
+    return (t > tMin && t < tMax) ? t : T(-1);
+}
+
+// The bodies of one view in the march (blackhole.frag:101-121 setup, :146-150 the near-field
+// hit at the loop head, :182-190 step clamps, :236-250 the chord test after each step).
+template <class T> struct BodyMarch {
+    const bhr_body* b = nullptr;
+    int n = 0;
+    V3<T> rd_near{0, 0, 0};
+    uint32_t near_mask = 0;
+    int near_idx = -1;
+    T near_t = T(1e30), near_tol = T(0), travelled = T(0);
+    int hit = -1;
+    V3<T> hit_ro{0, 0, 0}, hit_rd{0, 0, 0};
+    T hit_t = T(0);
+
+    static V3<T> xyz(const float* q) { return V3<T>{T(q[0]), T(q[1]), T(q[2])}; }
+
+    void setup(const V3<T>& cam, const V3<T>& v, const V3<T>& dir, bool lensing, T h2) {
+        const T rcam = length(cam);
+        rd_near = lensing ? normalize(v) : dir;
+        const T a_cam = lensing ? T(3) * h2 / std::max(rcam * rcam * rcam * rcam, T(1e-30)) : T(0);
+        for (int k = 0; k < n; ++k) {
+            const V3<T> rel = xyz(b[k].rel_pos);
+            const T R = T(b[k].pos_radius[3]);
+            const T t_straight = lensing ? std::sqrt(T(0.02) * R / std::max(a_cam, T(1e-30))) : T(1e30);
+            if (length(rel) + std::max(R, T(b[k].ring[1])) < t_straight) near_mask |= 1u << k;
+            const T t = raySphere(V3<T>{0, 0, 0}, rd_near, rel, R, T(0), std::min(t_straight, near_t));
+            if (t > T(0)) {
+                near_t = t;
+                near_idx = k;
+            }
+        }
+        near_tol = std::max(T(2e-6) * rcam, T(1e-9));
+    }
+    bool reached_near() const { return near_idx >= 0 && travelled + near_tol >= near_t; }
+    T clamp(const V3<T>& x, T ds) const {
+        if (near_idx >= 0) ds = std::min(ds, std::max(near_t - travelled, near_tol));
+        for (int k = 0; k < n; ++k) {
+            if (near_mask & (1u << k)) continue;
+            const T R = T(b[k].pos_radius[3]);
+            ds = std::min(ds, std::max(T(0.5) * (length(x - xyz(b[k].pos_radius)) - R), T(0.25) * R));
+        }
+        return ds;
+    }
+    void advance(T seg) { travelled += seg; }
+    bool chord(const V3<T>& x0, const V3<T>& x, T seg) {
+        if (n == 0 || !(seg > T(0))) return false;
+        const V3<T> sd = (x - x0) / seg;
+        T best = seg;
+        for (int k = 0; k < n; ++k) {
+            if (near_mask & (1u << k)) continue;
+            const T t = raySphere(x0, sd, xyz(b[k].pos_radius), T(b[k].pos_radius[3]), T(0), best);
+            if (t > T(0)) {
+                best = t;
+                hit = k;
+                hit_ro = x0;
+                hit_rd = sd;
+                hit_t = t;
+            }
+        }
+        return hit >= 0;
+    }
+};
+
 // blackhole.frag:68-72: primary ray of pixel (i, j), row 0 at the bottom.
 template <class T> inline V3<T> primaryRay(const bhr_view& w, int i, int j) {
     const T pxx = T(i) + T(0.5) + T(w.jitter[0]);
@@ -177,7 +263,7 @@ template <class T> inline bool finite3(V3<T> a) {
 // blackhole.frag:77-93 (setup) + :138-253 (march), or Geodesic.h:107-140 for BHR_TERM_CPU.
 // For BHR_DISK_VOLUMETRIC, vol(p, r_cyl, sub, res) shades one sub-sample of a segment in the
 // slab into res.col / res.trans (volumetricDiskStep).
-template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir, const Vol& vol) {
+template <class T, class Vol, class Bod> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir, const Vol& vol, Bod& bod) {
     Result<T> res;
     const bool lensing = R.lensing && !R.far_mode;
     V3<T> x = camPos;
@@ -196,6 +282,7 @@ template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3
         const T rc = length(camPos);
         res.b = h / std::sqrt(dot(v, v) - T(2) * h2 / (rc * rc * rc));
     }
+    bod.setup(camPos, v, dir, lensing, h2);
     const bool shader_rule = R.term_mode != BHR_TERM_CPU;
     const T farMul = shader_rule ? std::clamp((h - T(6)) / T(3), T(1), T(3)) : T(1);
     const T slab = T(2.5) * R.disk_thickness;  // diskSlabHalfHeight(r) = slab * r (disk.glsl:24)
@@ -214,6 +301,10 @@ template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3
                 break;
             }
             const T vlen = length(v);
+            if (bod.reached_near()) {  // reached the near-field body (blackhole.frag:146-150)
+                status = BHR_STATUS_BODY;
+                break;
+            }
             if (dot(x, v) > T(0)) {
                 bool esc = false;
                 if (R.term_mode == BHR_TERM_CONFIG) {
@@ -247,6 +338,7 @@ template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3
             } else {
                 ds = std::max(R.step_scale * r, R.ds_floor);
             }
+            ds = bod.clamp(x, ds);  // blackhole.frag:184-190
             const T dt = ds / vlen;
             const V3<T> x0 = x, v0 = v;
             if (lensing)
@@ -254,6 +346,8 @@ template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3
             else
                 x = x + v * dt;
             steps = i + 1;
+            const T seg = length(x - x0);
+            bod.advance(seg);
             if ((x.y > T(0)) != (x0.y > T(0))) {
                 if (res.nplane < 255) ++res.nplane;
                 if (R.disk_mode == BHR_DISK_THIN) {
@@ -269,7 +363,6 @@ template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3
             }
             if (R.disk_mode == BHR_DISK_VOLUMETRIC && near_disk) {
                 // blackhole.frag:217-233: samples along the cubic Hermite interpolant of the segment
-                const T seg = length(x - x0);
                 const T nf = std::ceil(seg / R.disk_step);
                 const int n = std::isfinite(nf) ? std::min(std::max(1, int(std::min(nf, T(kMaxSubSamples)))), kMaxSubSamples) : 1;
                 const T sub = seg / T(n);
@@ -289,6 +382,10 @@ template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3
                 status = BHR_STATUS_OPAQUE;
                 break;
             }
+            if (bod.chord(x0, x, seg)) {  // blackhole.frag:236-250
+                status = BHR_STATUS_BODY;
+                break;
+            }
             if (!finite3(x) || !finite3(v)) {
                 res.nonfinite = true;
                 break;
@@ -302,6 +399,11 @@ template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3
     res.x = x;
     res.v = v;
     return res;
+}
+
+template <class T, class Vol> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir, const Vol& vol) {
+    NoBodies<T> none;
+    return march(R, camPos, dir, vol, none);
 }
 
 template <class T> Result<T> march(const Rule<T>& R, V3<T> camPos, V3<T> dir) {

@@ -281,6 +281,44 @@ int oracle_shade_volumetric(const bhr_view* v, const bhr_hit* hits, const float*
     return BHR_OK;
 }
 
+// The body-aware march (BHS_BODIES 1) of every pixel of a view: records, and per pixel what the
+// shading after the loop needs (bhr_body_hit).
+int oracle_trace_bodies(const bhr_view* v, const bhr_body* bodies, int nb, bhr_hit* out, bhr_body_hit* bout,
+                        int nthreads, int fp64) {
+    if (!view_ok(v) || nb < 0 || nb > BHR_MAX_BODIES || (nb > 0 && !bodies) || !out || !bout) return BHR_ERR_INVALID_ARG;
+    const int64_t n = static_cast<int64_t>(v->width) * v->height;
+    auto one = [&](auto R, int64_t k) {
+        using T = decltype(R.step_scale);
+        const int i = static_cast<int>(k % v->width), j = static_cast<int>(k / v->width);
+        const V3<T> cam{T(v->cam_pos[0]), T(v->cam_pos[1]), T(v->cam_pos[2])};
+        BodyMarch<T> bm;
+        bm.b = bodies;
+        bm.n = nb;
+        const Result<T> r = march(R, cam, primaryRay<T>(*v, i, j), NoVolume{}, bm);
+        toHit(r, out + k);
+        bhr_body_hit& o = bout[k];
+        o = bhr_body_hit{};
+        // the loop-head near-field hit records only the body (blackhole.frag:147-149)
+        o.body = r.status == BHR_STATUS_BODY ? (bm.hit >= 0 ? bm.hit : bm.near_idx) : -1;
+        o.t = float(bm.hit_t);
+        o.ro[0] = float(bm.hit_ro.x), o.ro[1] = float(bm.hit_ro.y), o.ro[2] = float(bm.hit_ro.z);
+        o.rd[0] = float(bm.hit_rd.x), o.rd[1] = float(bm.hit_rd.y), o.rd[2] = float(bm.hit_rd.z);
+        o.x[0] = float(r.x.x), o.x[1] = float(r.x.y), o.x[2] = float(r.x.z);
+        o.near_mask = bm.near_mask;
+        o.near_idx = bm.near_idx;
+        o.near_t = float(bm.near_t);
+        o.travelled = float(bm.travelled);
+    };
+    if (fp64) {
+        const Rule<double> R = Rule<double>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
+    } else {
+        const Rule<float> R = Rule<float>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
+    }
+    return BHR_OK;
+}
+
 int oracle_hit_size(void) { return static_cast<int>(sizeof(bhr_hit)); }
 int oracle_view_size(void) { return static_cast<int>(sizeof(bhr_view)); }
 

@@ -12,7 +12,7 @@ from pathlib import Path
 
 import numpy as np
 
-from blackholerender_gb300 import HIT_DTYPE, ShadeParams, View
+from blackholerender_gb300 import BODY_HIT_DTYPE, HIT_DTYPE, Body, ShadeParams, View
 
 ROOT = Path(__file__).resolve().parent.parent
 ORACLE_DIR = ROOT / "oracle"
@@ -54,6 +54,8 @@ def lib():
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.oracle_shade_volumetric.argtypes = [VP, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ShadeParams),
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.oracle_trace_bodies.argtypes = [VP, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_int, ctypes.c_int]
         L.oracle_redshift_factor.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.oracle_redshift_factor.restype = ctypes.c_float
         L.oracle_blackbody_xyz.argtypes = [ctypes.c_double, D]
@@ -222,3 +224,15 @@ def shade_volumetric(view: View, hits: np.ndarray, rgbt: np.ndarray, params: Sha
                                        threads or nthreads())
     assert rc == 0
     return out
+
+
+def trace_bodies(view: View, bodies, fp64: bool = True, threads: int | None = None):
+    """The body-aware march of every pixel: (records, body records)."""
+    n = len(bodies)
+    arr = (Body * max(n, 1))(*bodies)
+    hits = np.zeros(view.width * view.height, dtype=HIT_DTYPE)
+    bh = np.zeros(view.width * view.height, dtype=BODY_HIT_DTYPE)
+    rc = lib().oracle_trace_bodies(ctypes.byref(view), ctypes.cast(arr, ctypes.c_void_p), n, hits.ctypes.data,
+                                   bh.ctypes.data, threads or nthreads(), int(fp64))
+    assert rc == 0
+    return hits, bh

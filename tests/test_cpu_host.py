@@ -44,6 +44,8 @@ def test_struct_layouts_match_the_header(tmp_path):
         "bhr_launch_shape": [f for f, _ in _abi.LaunchShape._fields_],
         "bhr_surrogate_config": [f for f, _ in _abi.SurrogateConfig._fields_],
         "bhr_shade_params": [f for f, _ in _abi.ShadeParams._fields_],
+        "bhr_body": [f for f, _ in _abi.Body._fields_],
+        "bhr_body_hit": list(_abi.BODY_HIT_DTYPE.names),
         "bhr_hit": list(_abi.HIT_DTYPE.names),
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bhr.h"', "int main(void) {"]
@@ -59,11 +61,14 @@ def test_struct_layouts_match_the_header(tmp_path):
                .stdout.splitlines())
     py = {"bhr_view": _abi.View, "bhr_options": _abi.Options, "bhr_stats": _abi.Stats,
           "bhr_launch_shape": _abi.LaunchShape, "bhr_surrogate_config": _abi.SurrogateConfig,
-          "bhr_shade_params": _abi.ShadeParams}
+          "bhr_shade_params": _abi.ShadeParams, "bhr_body": _abi.Body}
     for st, cls in py.items():
         assert int(got[st]) == ctypes.sizeof(cls), st
         for f, _ in cls._fields_:
             assert int(got[f"{st}.{f}"]) == getattr(cls, f).offset, (st, f)
+    assert int(got["bhr_body_hit"]) == _abi.BODY_HIT_DTYPE.itemsize == 64
+    for f in _abi.BODY_HIT_DTYPE.names:
+        assert int(got[f"bhr_body_hit.{f}"]) == _abi.BODY_HIT_DTYPE.fields[f][1], f
     assert int(got["bhr_hit"]) == _abi.HIT_DTYPE.itemsize == 64
     for f in _abi.HIT_DTYPE.names:
         assert int(got[f"bhr_hit.{f}"]) == _abi.HIT_DTYPE.fields[f][1], f

@@ -1,0 +1,97 @@
+"""The body-aware march on the GPU (bhr_trace_bodies) against the FP64 and FP32 CPU
+restatements: which rays stop on which body, the near-field and chord hit geometry, and the
+records of the rays that miss every body."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from blackholerender_gb300 import (BODY_HIT_DTYPE, DISK_NONE, DISK_THIN, DISK_VOLUMETRIC, SQRT27, STATUS_BODY,
+                                   TERM_CONFIG, TERM_SHADER, BhrError, Tracer, hits_numpy, make_view)
+from test_cpu_bodies import body
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tracer():
+    with Tracer(0) as t:
+        yield t
+
+
+def _scene(v):
+    cam = np.array(v.cam_pos, dtype=np.float64)
+    rhat = cam / np.linalg.norm(cam)
+    return [body(cam - 6.0 * rhat + np.array([0.5, 0.3, 0.0]), 0.6, cam),               # near field
+            body(-40.0 * rhat, 3.0, cam, ring=(4.0, 7.0, 0.0, 1.0)),                       # behind the hole
+            body(np.array([25.0, 2.0, -10.0]), 1.5, cam, kind=1.0),                        # off to the side
+            body(cam + np.array([0.3, -0.2, 0.0]) - 0.02 * rhat, 0.004, cam)]              # tiny, close by
+
+
+CASES = [("256x144 Low, thin disk, CONFIG", dict(term=TERM_CONFIG, width=256, height=144, preset=0,
+                                                 pose=(30.0, math.radians(80.0), 0.4), disk_mode=DISK_THIN), True),
+         ("160x90 Medium, no disk, shader rule", dict(term=TERM_SHADER, width=160, height=90, preset=1,
+                                                      pose=(25.0, math.radians(60.0), 1.0), disk_mode=DISK_NONE), False)]
+
+
+def _normals(bh, bodies, m):
+    """Unit normals at the chord hits m: (ro + rd t - centre) / |.|"""
+    c = np.array([bodies[k].pos_radius[:3] for k in bh["body"][m]], dtype=np.float64)
+    p = bh["ro"][m].astype(np.float64) + bh["rd"][m].astype(np.float64) * bh["t"][m, None].astype(np.float64) - c
+    return p / np.linalg.norm(p, axis=1, keepdims=True)
+
+
+@pytest.mark.parametrize("name,vk,has_chord", CASES, ids=[c[0] for c in CASES])
+def test_body_march_matches_the_oracle(tracer, name, vk, has_chord):
+    import torch
+
+    vk = dict(vk)
+    v = make_view(vk.pop("term"), **vk)
+    bodies = _scene(v)
+    h, bhd = tracer.trace_bodies(v, bodies)
+    torch.cuda.synchronize()
+    g = hits_numpy(h.cpu())
+    gb = bhd.cpu().numpy().view(np.uint8).reshape(-1).view(BODY_HIT_DTYPE)
+    r64, b64 = O.trace_bodies(v, bodies, fp64=True)
+    r32, b32 = O.trace_bodies(v, bodies, fp64=False)
+    amb = (np.abs(r64["b"] - SQRT27) < 1e-2) | (np.abs(r64["steps"].astype(int) - v.max_steps) <= 2)
+    mism = ((g["status"] != r64["status"]) | (gb["body"] != b64["body"])) & ~amb
+    mism32 = ((r32["status"] != r64["status"]) | (b32["body"] != b64["body"])) & ~amb
+    hit = (g["status"] == STATUS_BODY) & (r64["status"] == STATUS_BODY) & (gb["body"] == b64["body"])
+    chord = hit & (b64["t"] > 0)
+    near = hit & (b64["t"] == 0)
+    dn = np.abs(gb["near_t"][near] - b64["near_t"][near]) / b64["near_t"][near]
+    chord32 = chord & (r32["status"] == STATUS_BODY) & (b32["body"] == b64["body"]) & (b32["t"] > 0)
+    na = O.angle(_normals(gb, bodies, chord32), _normals(b64, bodies, chord32)) if chord32.any() else np.zeros(1)
+    na32 = O.angle(_normals(b32, bodies, chord32), _normals(b64, bodies, chord32)) if chord32.any() else np.zeros(1)
+    print(f"\n{name}: body hits {int(hit.sum())} (near {int(near.sum())}, chord {int(chord.sum())}), status/body "
+          f"mismatches {int(mism.sum())} (FP32 restatement {int(mism32.sum())}); chord-hit normal p99 "
+          f"{np.percentile(na, 99):.1e} rad (FP32 restatement {np.percentile(na32, 99):.1e}), near t rel max "
+          f"{dn.max() if dn.size else 0:.1e}")
+    assert hit.sum() > 50 and near.sum() > 0 and (chord.sum() > 0) == has_chord
+    assert mism.sum() <= max(3, 3 * mism32.sum())
+    assert np.all(gb["near_mask"] == b64["near_mask"])
+    assert (dn.max() if dn.size else 0) < 1e-4
+    assert np.percentile(na, 99) <= max(1e-4, 3 * np.percentile(na32, 99))
+    # the rays that miss every body: the same records as the plain march's parity bar
+    miss = (r64["status"] != STATUS_BODY) & (g["status"] != STATUS_BODY) & ~amb
+    esc = miss & (g["status"] == 1) & (r64["status"] == 1)
+    ang = O.angle(g["dir"][esc], r64["dir"][esc])
+    ang32 = O.angle(r32["dir"][esc], r64["dir"][esc])
+    assert np.percentile(ang, 99) <= max(2e-5, 3 * np.percentile(ang32, 99))
+
+
+def test_body_march_argument_errors(tracer):
+    v = make_view(TERM_CONFIG, width=8, height=8, disk_mode=DISK_VOLUMETRIC)
+    cam = np.array(v.cam_pos, dtype=np.float64)
+    with pytest.raises(BhrError) as e:
+        tracer.trace_bodies(v, [body(np.zeros(3) + 40, 1.0, cam)])
+    assert e.value.code == -5
+    v.disk_mode = DISK_THIN
+    with pytest.raises(BhrError) as e:
+        tracer.trace_bodies(v, [body(np.zeros(3) + 40, 1.0, cam)] * 33)
+    assert e.value.code == -1
+    with pytest.raises(BhrError) as e:
+        tracer.trace_bodies(v, [body(np.zeros(3) + 40, 0.0, cam)])
+    assert e.value.code == -1
