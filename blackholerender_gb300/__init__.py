@@ -238,6 +238,26 @@ class Tracer:
                                                ctypes.c_void_p(stream.cuda_stream)), self._ctx)
         return hits, body_hits
 
+    def shade_bodies(self, view: View, hits, body_hits, bodies: Sequence[Body], params: ShadeParams | None = None,
+                     out=None, stream=None):
+        """bhr_shade_bodies: shades a view marched by trace_bodies; (height, width, 4) float32."""
+        import torch
+
+        dev = torch.device("cuda", self.device)
+        if params is None:
+            params = shade_params()
+        if out is None:
+            out = torch.empty((view.height, view.width, 4), dtype=torch.float32, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        n = len(bodies)
+        arr = (Body * max(n, 1))(*bodies)
+        _abi.check(_abi.lib().bhr_shade_bodies(self._ctx, ctypes.byref(view), ctypes.c_void_p(hits.data_ptr()),
+                                               ctypes.c_void_p(body_hits.data_ptr()), arr, n, ctypes.byref(params),
+                                               ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream)),
+                   self._ctx)
+        return out
+
     def noise_bake(self, seed: int = 7, out=None, stream=None):
         """bhr_noise_bake: the disk's 128^3 noise volume as a device int16 tensor of half bits."""
         import torch

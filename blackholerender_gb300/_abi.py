@@ -135,7 +135,8 @@ class ShadeParams(ctypes.Structure):
         ("star_brightness", ctypes.c_float),
         ("shadow_overlay", ctypes.c_int32),
         ("noise_seed", ctypes.c_uint32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("time", ctypes.c_float),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 
@@ -220,6 +221,8 @@ SIGNATURES = {
     "bhr_trace_volumetric": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(ShadeParams),
                                             ctypes.POINTER(_P), _P]),
     "bhr_trace_bodies": (ctypes.c_int, [_P, _VP, ctypes.POINTER(Body), ctypes.c_int, _P, _P, _P]),
+    "bhr_shade_bodies": (ctypes.c_int, [_P, _VP, _P, _P, ctypes.POINTER(Body), ctypes.c_int, ctypes.POINTER(ShadeParams),
+                                        _P, _P]),
     "bhr_noise_bake": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P]),
     "bhr_blackbody_lut": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float)]),
     "bhr_get_launch_shape": (ctypes.c_int, [_P, ctypes.POINTER(LaunchShape)]),

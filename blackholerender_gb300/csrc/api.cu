@@ -801,6 +801,7 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         a.disk_thin = v.disk_mode == BHR_DISK_THIN;
         a.volumetric = v.disk_mode == BHR_DISK_VOLUMETRIC;
         a.far_mode = v.far_mode;
+        a.lensing = (v.lensing != 0 && v.far_mode == 0) ? 1 : 0;
         a.p = *p;
         a.ln_1000 = std::log(1000.0f);
         a.ln_40000 = std::log(40000.0f);
@@ -812,6 +813,59 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         a.lut = c->lut;
         const cudaError_t e = bhr::launch_shade(a, st);
         if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_shade: kernel launch");
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int bhr_shade_bodies(bhr_ctx* c, const bhr_view* view, const bhr_hit* hits, const bhr_body_hit* body,
+                     const bhr_body* bodies, int nbodies, const bhr_shade_params* p, float* rgba, void* cuda_stream) {
+    if (!c || !view || !hits || !body || !p || !rgba || nbodies < 0 || (nbodies > 0 && !bodies))
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade_bodies: NULL argument");
+    if (nbodies > BHR_MAX_BODIES)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade_bodies: at most BHR_MAX_BODIES (32) bodies per view");
+    const bhr_view& v = *view;
+    if (v.width <= 0 || v.height <= 0) return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade_bodies: width and height must be positive");
+    if (v.disk_mode == BHR_DISK_VOLUMETRIC)
+        return fail(c, BHR_ERR_UNSUPPORTED, "bhr_shade_bodies: bodies are shaded with a thin disk or none");
+    if (reinterpret_cast<uintptr_t>(hits) % 16 != 0 || reinterpret_cast<uintptr_t>(body) % 16 != 0 ||
+        reinterpret_cast<uintptr_t>(rgba) % 16 != 0)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade_bodies: buffers must be 16-byte aligned");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    int rc = ensure_shade_resources(c, p->noise_seed, st);
+    if (rc == BHR_OK) {
+        bhr::ShadeArgs a{};
+        for (int i = 0; i < 3; ++i) a.cam[i] = v.cam_pos[i];
+        for (int i = 0; i < 9; ++i) a.basis[i] = v.cam_basis[i];
+        a.tan_half = v.tan_half_fov;
+        a.jitter[0] = v.jitter[0];
+        a.jitter[1] = v.jitter[1];
+        a.width = v.width;
+        a.height = v.height;
+        a.disk_inner = v.disk_inner;
+        a.disk_outer = v.disk_outer;
+        a.disk_thin = v.disk_mode == BHR_DISK_THIN;
+        a.volumetric = 0;
+        a.far_mode = v.far_mode;
+        a.lensing = (v.lensing != 0 && v.far_mode == 0) ? 1 : 0;
+        a.p = *p;
+        a.ln_1000 = std::log(1000.0f);
+        a.ln_40000 = std::log(40000.0f);
+        a.ln_3000 = std::log(3000.0f);
+        a.ln_22000 = std::log(22000.0f);
+        a.hits = hits;
+        a.out = reinterpret_cast<float4*>(rgba);
+        a.noise = c->noise;
+        a.lut = c->lut;
+        bhr::BodyShadeArgs b{};
+        b.bh = body;
+        b.nbodies = nbodies;
+        for (int k = 0; k < nbodies; ++k) b.bodies[k] = bodies[k];
+        const cudaError_t e = bhr::launch_shade_bodies(a, b, st);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_shade_bodies: kernel launch");
     }
     cudaSetDevice(prev);
     return rc;

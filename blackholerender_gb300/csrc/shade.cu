@@ -20,6 +20,7 @@
 
 #include "bhr.h"
 #include "shade.cuh"
+#include "body_math.cuh"
 #include "shade_math.cuh"
 
 namespace bhr {
@@ -28,14 +29,6 @@ namespace {
 
 using namespace shading;
 constexpr int kBX = 32, kBY = 8;
-
-// common.glsl:33-39 grad3: a unit gradient from the hashed lattice point
-__device__ __forceinline__ F3 grad3(int cx, int cy, int cz, uint32_t salt) {
-    const uint3 h = pcg3d(make_uint3(uint32_t(cx) + salt, uint32_t(cy) + (salt * 3u + 11u), uint32_t(cz) + (salt * 7u + 29u)));
-    const float s = 1.0f / 4294967296.0f;
-    const F3 g{float(h.x) * s * 2.0f - 1.0f, float(h.y) * s * 2.0f - 1.0f, float(h.z) * s * 2.0f - 1.0f};
-    return scale(g, 1.0f / sqrtf(fmaxf(dot(g, g), 1e-8f)));
-}
 
 __device__ __forceinline__ float fade(float t) { return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f); }
 
@@ -314,7 +307,22 @@ __device__ __forceinline__ F3 quad_diff(F3 v, int lane, int mask) {
 
 // A block is 4 x 2 warps, a warp 8 x 4 pixels (lane = 8 y + x): the 2x2 quads of the
 // rasteriser (even-aligned) sit inside a warp, with partners at lane ^ 1 (x) and lane ^ 8 (y).
-__global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ ShadeArgs A) {
+// blackhole.frag:78,107 rdNear = normalize(initialVelocity(uCamPos, dir)) (dir when lensing is off)
+__device__ __forceinline__ F3 rd_near_of(F3 cam, float rcam, F3 d, bool lensing) {
+    if (!lensing) return d;
+    const F3 rhat = divs(cam, rcam);
+    const float nr = dot(d, rhat);
+    const F3 nperp = sub(d, scale(rhat, nr));
+    const float f = sqrtf(fmaxf(1.0f - 2.0f / rcam, 0.0f));
+    const F3 w = add(scale(rhat, nr * f), nperp);
+    const F3 v = scale(w, 1.0f / sqrtf(dot(w, w)));
+    return normalize(v);
+}
+
+// The shading of one block. With kBodies, the body records and bodies of B add what lies
+// behind the disk before the sky (blackhole.frag:255-296).
+template <bool kBodies>
+__device__ __forceinline__ void shade_block(const ShadeArgs& A, const BodyShadeArgs* B) {
     __shared__ float4 s_lut[kLut];
     __shared__ StarSlot s_star[kBX * kBY / 32][32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -328,6 +336,7 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
     const float rcam = len(cam);
     const DiskConsts C = disk_consts(P, rcam);
     const F3 dir = primary_dir(A, i, j);
+    const float pixel_angle = 2.0f * A.tan_half / float(A.height);
     __syncthreads();  // the table is staged
 
     F3 col{0.f, 0.f, 0.f};
@@ -361,7 +370,14 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
             }
         }
         if (status == BHR_STATUS_ESCAPED) esc_dir = F3{w0.z, w0.w, w1.x};
-        esc = status == BHR_STATUS_ESCAPED && !opaque;
+        int st = opaque ? int(BHR_STATUS_OPAQUE) : status;
+        if constexpr (kBodies) {
+            const bhr_body_hit bh = B->bh[k_pix];
+            const F3 rdn = rd_near_of(cam, rcam, dir, A.lensing != 0);
+            shade_bodies_after_march(tx, B->bodies, B->nbodies, bh, A.far_mode != 0, rcam, dir, rdn, pixel_angle, P.time, st,
+                                     esc_dir, col, trans);
+        }
+        esc = st == BHR_STATUS_ESCAPED;
     }
     // blackhole.frag:297-306: derivatives of escDir; the unlensed footprint where a quad mixes
     // escaped and other pixels (a partner outside the image counts as not escaped)
@@ -375,7 +391,6 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
     const F3 ddx_0 = quad_diff(dir, lane, 1), ddy_0 = quad_diff(dir, lane, 8);
     const F3 ddx = mixed ? ddx_0 : ddx_l, ddy = mixed ? ddy_0 : ddy_l;
 
-    const float pixel_angle = 2.0f * A.tan_half / float(A.height);
     const float omega0 = pixel_angle * pixel_angle;
     const float g = mixf(1.0f, 1.0f / sqrtf(fmaxf(1.0f - 2.0f / rcam, 1e-4f)), P.doppler_strength);
     const float g4 = g * g * g * g;
@@ -410,6 +425,13 @@ __global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ Sha
         alpha = 0.0f;
     }
     A.out[int64_t(j) * A.width + i] = make_float4(fmaxf(col.x, 0.0f), fmaxf(col.y, 0.0f), fmaxf(col.z, 0.0f), alpha);
+}
+
+__global__ void __launch_bounds__(kBX * kBY) k_shade(const __grid_constant__ ShadeArgs A) { shade_block<false>(A, nullptr); }
+
+__global__ void __launch_bounds__(kBX * kBY) k_shade_bodies(const __grid_constant__ ShadeArgs A,
+                                                            const __grid_constant__ BodyShadeArgs B) {
+    shade_block<true>(A, &B);
 }
 
 // ---------------------------------------------------------------- blackbody table (host, double)
@@ -470,6 +492,12 @@ cudaError_t launch_noise_bake(uint32_t seed, uint16_t* out, cudaStream_t st) {
 cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t st) {
     const dim3 grid((a.width + kBX - 1) / kBX, (a.height + kBY - 1) / kBY);
     k_shade<<<grid, kBX * kBY, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade_bodies(const ShadeArgs& a, const BodyShadeArgs& b, cudaStream_t st) {
+    const dim3 grid((a.width + kBX - 1) / kBX, (a.height + kBY - 1) / kBY);
+    k_shade_bodies<<<grid, kBX * kBY, 0, st>>>(a, b);
     return cudaGetLastError();
 }
 

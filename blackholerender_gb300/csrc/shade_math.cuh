@@ -56,6 +56,14 @@ __device__ __forceinline__ uint3 pcg3d(uint3 v) {
     return v;
 }
 
+// common.glsl:33-39 grad3: a unit gradient from the hashed lattice point
+__device__ __forceinline__ F3 grad3(int cx, int cy, int cz, uint32_t salt) {
+    const uint3 h = pcg3d(make_uint3(uint32_t(cx) + salt, uint32_t(cy) + (salt * 3u + 11u), uint32_t(cz) + (salt * 7u + 29u)));
+    const float s = 1.0f / 4294967296.0f;
+    const F3 g{float(h.x) * s * 2.0f - 1.0f, float(h.y) * s * 2.0f - 1.0f, float(h.z) * s * 2.0f - 1.0f};
+    return scale(g, 1.0f / sqrtf(fmaxf(dot(g, g), 1e-8f)));
+}
+
 struct Tex {
     const uint16_t* noise;
     const float4* lut;  // shared memory

@@ -341,7 +341,8 @@ typedef struct bhr_shade_params {
     float star_brightness;     /* uStarBrightness     (1.0) */
     int32_t shadow_overlay;    /* uShadowOverlay      (0) */
     uint32_t noise_seed;       /* noise_bake.comp uSeed, DiskTextures.cpp:106 (7) */
-    int32_t reserved[5];
+    float time;                /* uTime (Renderer.cpp:253): cloud drift and stellar granulation of bodies (0) */
+    int32_t reserved[4];
 } bhr_shade_params;
 int bhr_shade_default_params(bhr_shade_params* p);
 /* Shades nviews views: hits_dev[k] holds view k's records (from any trace entry point),
@@ -403,6 +404,14 @@ typedef struct bhr_body_hit {
  * body_dev width x height bhr_body_hit. Stream-ordered. */
 int bhr_trace_bodies(bhr_ctx* ctx, const bhr_view* view, const bhr_body* bodies, int nbodies, bhr_hit* hits_dev,
                      bhr_body_hit* body_dev, void* cuda_stream);
+/* Shades one view marched by bhr_trace_bodies (bhr_shade plus blackhole.frag:255-296): the hit
+ * body's surface (shadeBodySurface, bodies.glsl:224-292: nine planet looks, stars, an exploding
+ * photosphere), a body turning transparent letting the ray on, the bodies along the straight
+ * stretches before and after the march (with their rings), and the halos of the bodies the ray
+ * just missed; then the sky. params->time is uTime. rgba_dev as bhr_shade's. */
+int bhr_shade_bodies(bhr_ctx* ctx, const bhr_view* view, const bhr_hit* hits_dev, const bhr_body_hit* body_dev,
+                     const bhr_body* bodies, int nbodies, const bhr_shade_params* params, float* rgba_dev,
+                     void* cuda_stream);
 
 /* ---- launch shapes and the autotuner ------------------------------------------------ */
 /* No counterpart in the reference (its march is one fragment-shader draw whose scheduling the

@@ -12,6 +12,7 @@
 #include "march.hpp"
 #include "lens.hpp"
 #include "shade.hpp"
+#include "bodies.hpp"
 
 using namespace oracle;
 
@@ -316,6 +317,21 @@ int oracle_trace_bodies(const bhr_view* v, const bhr_body* bodies, int nb, bhr_h
         const Rule<float> R = Rule<float>::from_view(*v);
         parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
     }
+    return BHR_OK;
+}
+
+// Shades a view marched with bodies: its records, body records and the bodies.
+int oracle_shade_bodies(const bhr_view* v, const bhr_hit* hits, const bhr_body_hit* bh, const bhr_body* bodies, int nb,
+                        const bhr_shade_params* p, const uint16_t* noise, const float* lut, float* rgba, int nthreads) {
+    if (!v || !hits || !bh || (nb > 0 && !bodies) || nb < 0 || nb > BHR_MAX_BODIES || !p || !noise || !lut || !rgba ||
+        v->width <= 0 || v->height <= 0 || v->disk_mode == BHR_DISK_VOLUMETRIC)
+        return BHR_ERR_INVALID_ARG;
+    const oracle::shade::Tex tx{noise, lut};
+    const float cx = v->cam_pos[0], cy = v->cam_pos[1], cz = v->cam_pos[2];
+    const oracle::body::BodyPost post{&tx, bodies, nb, bh, v, std::sqrt(cx * cx + cy * cy + cz * cz),
+                                      2.0f * v->tan_half_fov / float(v->height), p->time};
+    parallel_for(v->height, nthreads, 1,
+                 [&](int64_t j) { oracle::shade::shade_view(tx, *p, *v, hits, rgba, j, j + 1, nullptr, post); });
     return BHR_OK;
 }
 

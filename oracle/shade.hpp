@@ -413,6 +413,7 @@ inline float shadow_angular_radius(float r) {
 struct PixelState {
     F3 col;
     float trans;
+    int status;   // the record's status; OPAQUE once the disk blocked the ray
     bool esc;     // status == escaped and not opaque (the shader's status == 1 after the loop)
     F3 esc_dir;   // escDir (the primary direction when the ray did not escape)
     F3 dir;       // primary direction
@@ -444,13 +445,21 @@ inline PixelState composite_disk(const Tex& tx, const bhr_shade_params& P, const
         }
     }
     s.esc = h.status == BHR_STATUS_ESCAPED && !opaque;
+    s.status = opaque ? BHR_STATUS_OPAQUE : int(h.status);
     s.esc_dir = h.status == BHR_STATUS_ESCAPED ? F3{h.dir[0], h.dir[1], h.dir[2]} : s.dir;
     return s;
 }
 
+// No further layers after the disk (no bodies on screen).
+struct NoPost {
+    void operator()(PixelState&, int, int) const {}
+};
+
 // Shades every pixel of one view from its hit records; rgba[4 k + c], k = j * width + i.
+// `post(state, i, j)` adds what lies behind the disk before the sky (the bodies, oracle/bodies.hpp).
+template <class Post = NoPost>
 inline void shade_view(const Tex& tx, const bhr_shade_params& P, const bhr_view& v, const bhr_hit* hits, float* rgba,
-                       int64_t row_begin, int64_t row_end, const float* rgbt = nullptr) {
+                       int64_t row_begin, int64_t row_end, const float* rgbt = nullptr, const Post& post = Post{}) {
     const int W = v.width, H = v.height;
     const F3 cam{v.cam_pos[0], v.cam_pos[1], v.cam_pos[2]};
     const float rcam = length(cam);
@@ -460,7 +469,9 @@ inline void shade_view(const Tex& tx, const bhr_shade_params& P, const bhr_view&
     const float g = mixf(1.0f, 1.0f / std::sqrt(std::fmax(1.0f - 2.0f / rcam, 1e-4f)), P.doppler_strength);
     const float g4 = g * g * g * g;
     auto state = [&](int i, int j) {
-        return composite_disk(tx, P, v, hits[int64_t(j) * W + i], i, j, rcam, rgbt);
+        PixelState s = composite_disk(tx, P, v, hits[int64_t(j) * W + i], i, j, rcam, rgbt);
+        post(s, i, j);
+        return s;
     };
     for (int64_t j = row_begin; j < row_end; ++j)
         for (int i = 0; i < W; ++i) {

@@ -56,6 +56,9 @@ def lib():
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.oracle_trace_bodies.argtypes = [VP, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_int, ctypes.c_int]
+        L.oracle_shade_bodies.argtypes = [VP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.POINTER(ShadeParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_int]
         L.oracle_redshift_factor.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.oracle_redshift_factor.restype = ctypes.c_float
         L.oracle_blackbody_xyz.argtypes = [ctypes.c_double, D]
@@ -236,3 +239,19 @@ def trace_bodies(view: View, bodies, fp64: bool = True, threads: int | None = No
                                    bh.ctypes.data, threads or nthreads(), int(fp64))
     assert rc == 0
     return hits, bh
+
+
+def shade_bodies(view: View, hits: np.ndarray, body_hits: np.ndarray, bodies, params: ShadeParams, noise: np.ndarray,
+                 lut: np.ndarray, threads: int | None = None) -> np.ndarray:
+    """Shades a view marched with bodies; (height, width, 4) float32."""
+    n = len(bodies)
+    arr = (Body * max(n, 1))(*bodies)
+    hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    body_hits = np.ascontiguousarray(body_hits, dtype=BODY_HIT_DTYPE)
+    out = np.zeros((view.height, view.width, 4), dtype=np.float32)
+    rc = lib().oracle_shade_bodies(ctypes.byref(view), hits.ctypes.data, body_hits.ctypes.data, ctypes.cast(arr, ctypes.c_void_p),
+                                   n, ctypes.byref(params), np.ascontiguousarray(noise, dtype=np.uint16).ctypes.data,
+                                   np.ascontiguousarray(lut, dtype=np.float32).ctypes.data, out.ctypes.data,
+                                   threads or nthreads())
+    assert rc == 0
+    return out

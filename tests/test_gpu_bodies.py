@@ -1,6 +1,7 @@
-"""The body-aware march on the GPU (bhr_trace_bodies) against the FP64 and FP32 CPU
-restatements: which rays stop on which body, the near-field and chord hit geometry, and the
-records of the rays that miss every body."""
+"""Bodies on the GPU against the CPU restatements: the body-aware march (bhr_trace_bodies:
+which rays stop on which body, the near-field and chord hit geometry, the records of the rays
+that miss every body, against FP64 and FP32) and the shading of bodies (bhr_shade_bodies: all
+nine planet looks, a star, an exploding photosphere, rings, translucency, halos)."""
 import math
 
 import numpy as np
@@ -95,3 +96,59 @@ def test_body_march_argument_errors(tracer):
     with pytest.raises(BhrError) as e:
         tracer.trace_bodies(v, [body(np.zeros(3) + 40, 0.0, cam)])
     assert e.value.code == -1
+
+
+def _gallery(v):
+    """Twelve bodies in front of the camera: the nine planet looks, a star, an exploding
+    photosphere, a ringed translucent planet."""
+    cam = np.array(v.cam_pos, dtype=np.float64)
+    B = np.array(v.cam_basis, dtype=np.float64).reshape(3, 3)  # rows: right, up, back (column-major basis)
+    right, up, back = B[0], B[1], B[2]
+    out = []
+    for k in range(12):
+        gx, gy = k % 4, k // 4
+        pos = cam - 9.0 * back + (gx - 1.5) * 2.2 * right + (gy - 1.0) * 2.2 * up
+        b = body(pos, 0.7, cam, kind=1.0 if k in (9, 10) else 0.0)
+        b.look[:] = (float(k % 9), float(100 + k), 0.5 if k in (2, 4, 7) else 0.0, 0.3 * k)
+        L = back + 0.4 * right + 0.5 * up
+        b.light[:] = (*(L / np.linalg.norm(L)), 1.5)
+        b.light_color[:] = (1.0, 0.95, 0.9, 5772.0 if k != 10 else 9000.0)
+        if k == 10:
+            b.tint[3] = 0.8   # turbulence: an exploding photosphere
+            b.look[2] = 3.0   # plumes per radius
+            b.ring[2] = 1.7   # its clock
+        if k == 11:
+            b.ring[:] = (0.9, 1.4, 0.0, 0.6)
+            b.axis[:3] = (0.2, 0.9, 0.3)
+        out.append(b)
+    return out
+
+
+def test_body_shading_matches_the_oracle(tracer):
+    import torch
+
+    from blackholerender_gb300 import shade_params
+
+    v = make_view(TERM_CONFIG, width=320, height=180, preset=0, pose=(30.0, math.radians(70.0), 0.4), disk_mode=DISK_THIN)
+    bodies = _gallery(v)
+    p = shade_params(time=37.0, doppler_strength=0.5)
+    h, bhd = tracer.trace_bodies(v, bodies)
+    img = tracer.shade_bodies(v, h, bhd, bodies, p)
+    noise = tracer.noise_bake(7)
+    torch.cuda.synchronize()
+    g = hits_numpy(h.cpu())
+    gb = bhd.cpu().numpy().view(np.uint8).reshape(-1).view(BODY_HIT_DTYPE)
+    img = img.cpu().numpy()
+    ref = O.shade_bodies(v, g, gb, bodies, p, noise.cpu().numpy().view(np.uint16), O.blackbody_lut())
+    on = g["status"] == STATUS_BODY
+    per_body = np.bincount(gb["body"][on], minlength=12)
+    d = np.abs(img - ref)
+    bad = np.any(d > 1e-4 * np.abs(ref) + 1e-6, axis=-1).reshape(-1)
+    r = (d / np.maximum(np.abs(ref), 1e-6)).reshape(-1, 4)
+    print(f"\nbody shading 320x180: body pixels {int(on.sum())}, per body {per_body.tolist()}; outside 1e-4: "
+          f"{int(bad.sum())} ({int(bad[on].sum())} on bodies), rel p99 on bodies {np.percentile(r[on], 99):.1e}, "
+          f"max |d| {d.max():.2e}")
+    assert np.all(per_body > 30)
+    assert np.all(np.isfinite(img))
+    assert bad.mean() <= 2e-3 and bad[on].mean() <= 2e-3
+    assert d.max() <= 1e-3 * max(1.0, float(np.abs(ref).max()))
