@@ -638,6 +638,65 @@ def run_vol_workload(args):
     tr.close()
 
 
+def run_bodies_workload(args):
+    """--workload bodies: the BHS_BODIES variant on the 16 poses at 1920x1080, 450 steps, thin disk,
+    twelve bodies in front of every camera (workloads.body_gallery). Each step marches the 16
+    views with their bodies (bhr_trace_bodies) and shades them (bhr_shade_bodies). One JSON line,
+    not the headline."""
+    import torch
+
+    from blackholerender_gb300 import HIT_BYTES, STATUS_BODY, TERM_CONFIG, Tracer, hits_numpy, shade_params, workloads
+
+    dev = torch.device("cuda", 0)
+    tr = Tracer(0)
+    views = workloads.c2_views(TERM_CONFIG)[: args.views]
+    scenes = [workloads.body_gallery(v) for v in views]
+    rays = sum(v.rays for v in views)
+    p = shade_params(time=10.0)
+    hits = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+    bh = [torch.empty(v.rays * 64, dtype=torch.uint8, device=dev) for v in views]
+    img = [torch.empty((v.height, v.width, 4), dtype=torch.float32, device=dev) for v in views]
+    st = torch.cuda.current_stream(dev)
+
+    def step():
+        for v, b, h, q in zip(views, scenes, hits, bh):
+            tr.trace_bodies(v, b, h, q, st)
+        mid = torch.cuda.Event(enable_timing=True)
+        mid.record(st)
+        for v, b, h, q, o in zip(views, scenes, hits, bh, img):
+            tr.shade_bodies(v, h, q, b, p, o, st)
+        return mid
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    rec = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            mid = step()
+            b.record(st)
+            rec.append((a, mid, b))
+        torch.cuda.synchronize(dev)
+    ms = sum(a.elapsed_time(b) for a, _, b in rec) / len(rec)
+    ms_trace = sum(a.elapsed_time(m) for a, m, _ in rec) / len(rec)
+    on = sum(int((hits_numpy(h.cpu())["status"] == STATUS_BODY).sum()) for h in hits)
+    line = {"metric": "Mrays/s (bodies: march + shading)", "value": rays / (ms * 1e-3) / 1e6, "unit": "Mrays/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{len(views)} poses (seed 0) x 1920x1080, FOV 60, 450 steps, thin disk, 12 bodies "
+                                   "per view (nine planet looks, a star, an exploding photosphere, a ringed translucent "
+                                   "planet), time 10", "rays_per_step": rays, "body_pixel_fraction": on / rays,
+                       "march_ms": ms_trace, "shade_ms": ms - ms_trace, "l2": "flushed (256 MiB write) between steps"},
+            "gpu_launches": 2 * len(views) * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    tr.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -651,9 +710,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--views", type=int, default=16, help="first N of the 16 poses (small profiling cases)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "shade", "vol"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "shade", "vol", "bodies"],
                     help="c2: the headline (16 poses at 1080p); c3 / c4: the other configurations; "
-                         "shade: the records' shading consumer; vol: the volumetric disk march")
+                         "shade: the records' shading consumer; vol: the volumetric disk march; "
+                         "bodies: the march and shading with bodies")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
@@ -663,6 +723,8 @@ def main():
         run_shade_workload(args)
     elif args.workload == "vol":
         run_vol_workload(args)
+    elif args.workload == "bodies":
+        run_bodies_workload(args)
     elif args.workload != "c2":
         run_side_workload(args)
     else:

@@ -138,6 +138,9 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
                 if (near_mask & (1u << b)) continue;
                 const float* pr = A.bodies[b].pos_radius;
                 const V3<float> d{x.x - pr[0], x.y - pr[1], x.z - pr[2]};
+                // a body farther than 2 ds + R cannot shorten the step: skipped without the sqrt
+                const float reach = 2.0f * ds + pr[3];
+                if (dot3(d, d) >= reach * reach) continue;
                 ds = fminf(ds, fmaxf(0.5f * (len3(d) - pr[3]), 0.25f * pr[3]));
             }
             const float dt = ds * vi;
@@ -172,6 +175,10 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
                 for (int b = 0; b < nb; ++b) {
                     if (near_mask & (1u << b)) continue;
                     const float* pr = A.bodies[b].pos_radius;
+                    // a sphere farther from the chord's start than its length plus R is out of reach
+                    const V3<float> d{x0.x - pr[0], x0.y - pr[1], x0.z - pr[2]};
+                    const float reach = seg + pr[3];
+                    if (dot3(d, d) > reach * reach) continue;
                     const float t = ray_sphere(x0, sd, xyz(pr), pr[3], 0.f, best);
                     if (t > 0.f) {
                         best = t;

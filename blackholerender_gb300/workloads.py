@@ -10,13 +10,14 @@ C4  64 views from seed 1, per view in draw order: pixel count log-uniform in
     r ~ log-U[6.5,200], inclination ~ U[0,90] deg, azimuth ~ U[0,2 pi), budget from
     {200,300,450,700} (preset Low..Ultra)
 All use the thin disk r in [6,20] (H/r 0.035), escape at r>1000 and capture at r<2.0001.
-A uniform draw is u = (x >> 11) * 2^-53 of one 64-bit engine output x.
+A uniform draw is libstdc++'s: u = x * 2^-64 of one 64-bit engine output x (kept below 1).
+Bodies: body_gallery places a fixed set of planets and stars in front of a view's camera.
 """
 from __future__ import annotations
 
 import math
 
-from . import TERM_CONFIG, View, make_view
+from . import TERM_CONFIG, Body, View, make_view
 
 _MASK = (1 << 64) - 1
 
@@ -106,4 +107,38 @@ def c4_views(term_mode: int = TERM_CONFIG, seed: int = 1, n: int = 64, scale: fl
         budget = (200, 300, 450, 700)[min(3, int(g.uniform(0.0, 4.0)))]
         out.append(make_view(term_mode, width=w, height=h, fov_deg=fov, preset=PRESET_BY_BUDGET[budget],
                              pose=(r, inc, az)))
+    return out
+
+
+def body_gallery(view: View, n: int = 12, distance: float = 9.0, radius: float = 0.7) -> list[Body]:
+    """n bodies on a grid 2.2 M apart, `distance` M in front of the view's camera: the nine
+    planet looks in turn, a star and an exploding photosphere among them, the last one ringed
+    and translucent. Light comes from behind the camera, up and to the right."""
+    cam = [float(c) for c in view.cam_pos]
+    B = [float(c) for c in view.cam_basis]
+    right, up, back = B[0:3], B[3:6], B[6:9]
+    lx = [back[k] + 0.4 * right[k] + 0.5 * up[k] for k in range(3)]
+    ln = math.sqrt(sum(c * c for c in lx))
+    out = []
+    for k in range(n):
+        gx, gy = k % 4, k // 4
+        pos = [cam[c] - distance * back[c] + (gx - 1.5) * 2.2 * right[c] + (gy - 1.0) * 2.2 * up[c] for c in range(3)]
+        b = Body()
+        star = k % 12 in (9, 10)
+        b.pos_radius[:] = (*pos, radius)
+        b.rel_pos[:] = (*(pos[c] - cam[c] for c in range(3)), 1.0 if star else 0.0)
+        b.look[:] = (float(k % 9), float(100 + k), 0.5 if k % 9 in (2, 4, 7) else 0.0, 0.3 * k)
+        b.tint[:] = (1.0, 1.0, 1.0, 0.0)
+        b.light[:] = (*(c / ln for c in lx), 1.5)
+        b.light_color[:] = (1.0, 0.95, 0.9, 9000.0 if k % 12 == 10 else 5772.0)
+        b.axis[:] = (0.0, 1.0, 0.0, 0.0)
+        b.ring[:] = (0.0, 0.0, 0.0, 1.0)
+        if k % 12 == 10:  # an exploding photosphere: turbulence, plumes per radius, its clock
+            b.tint[3] = 0.8
+            b.look[2] = 3.0
+            b.ring[2] = 1.7
+        if k % 12 == 11:  # rings, translucent
+            b.ring[:] = (0.9 * radius / 0.7, 1.4 * radius / 0.7, 0.0, 0.6)
+            b.axis[:3] = (0.2, 0.9, 0.3)
+        out.append(b)
     return out

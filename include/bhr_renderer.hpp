@@ -133,6 +133,8 @@ struct FrameInput {
     float jitter[2] = {0.0f, 0.0f};  // sub-pixel offset of accumulated frames (0 for parity)
     float diskTime = 0.0f;           // disk flow clock in M, [0, 60) (App.cpp:458-459)
     float diskFade = 1.0f;           // steady disk's fade (1 = shown; <= 0.01 = not marched)
+    float time = 0.0f;               // seconds since start (uTime: clouds and stars of bodies)
+    const std::vector<bhr_body>* bodies = nullptr;  // packBodies output (Renderer.h:43): the BHS_BODIES variant
 };
 
 class Renderer {
@@ -157,6 +159,11 @@ public:
     }
 
     void shutdown() {
+        if (body_hits_) {
+            cudaFree(body_hits_);
+            body_hits_ = nullptr;
+            body_capacity_ = 0;
+        }
         if (image_) {
             cudaFree(image_);
             image_ = nullptr;
@@ -231,6 +238,7 @@ public:
         p->star_density = s.starDensity;
         p->star_brightness = s.starBrightness;
         p->shadow_overlay = s.showShadowOverlay ? 1 : 0;
+        p->time = in.time;
         return true;
     }
 
@@ -253,6 +261,21 @@ public:
         width_ = v.width;
         height_ = v.height;
         bhr_hit* const outs[1] = {records_};
+        const int nb = in.bodies ? int(in.bodies->size()) : 0;
+        if (nb > 0) {  // the BHS_BODIES variant (Renderer.cpp:359-366)
+            if (v.disk_mode == BHR_DISK_VOLUMETRIC) return logError("render: bodies are marched with a thin disk or none", nullptr);
+            if (n > body_capacity_) {
+                if (body_hits_) cudaFree(body_hits_);
+                body_hits_ = nullptr;
+                body_capacity_ = 0;
+                if (cudaMalloc(&body_hits_, n * sizeof(bhr_body_hit)) != cudaSuccess)
+                    return logError("render: cannot allocate the body records", nullptr);
+                body_capacity_ = n;
+            }
+            if (bhr_trace_bodies(ctx_, &v, in.bodies->data(), nb, records_, body_hits_, nullptr) != BHR_OK)
+                return logError("render", ctx_);
+            return true;
+        }
         if (v.disk_mode == BHR_DISK_VOLUMETRIC) {
             bhr_shade_params p{};
             if (!makeShadeParams(in, &p) || !ensureImage(n)) return logError("render: volumetric disk", nullptr);
@@ -312,6 +335,12 @@ public:
         bhr_shade_params p{};
         if (!makeView(in, &v) || !makeShadeParams(in, &p)) return logError("renderImage: incomplete FrameInput", nullptr);
         if (!ensureImage(size_t(v.width) * size_t(v.height))) return false;
+        if (in.bodies && !in.bodies->empty()) {
+            if (bhr_shade_bodies(ctx_, &v, records_, body_hits_, in.bodies->data(), int(in.bodies->size()), &p, image_,
+                                 nullptr) != BHR_OK)
+                return logError("renderImage", ctx_);
+            return true;
+        }
         const bhr_hit* const hits[1] = {records_};
         float* const outs[1] = {image_};
         if (bhr_shade(ctx_, &v, 1, hits, &p, outs, nullptr) != BHR_OK) return logError("renderImage", ctx_);
@@ -320,6 +349,7 @@ public:
 
     const bhr_hit* hits() const { return records_; }  // device records of the last render()
     const float* image() const { return image_; }      // device float4 image of the last renderImage()
+    const bhr_body_hit* bodyHits() const { return body_hits_; }  // device body records of the last render() with bodies
     int width() const { return width_; }
     int height() const { return height_; }
     bhr_ctx* context() const { return ctx_; }
@@ -350,6 +380,8 @@ private:
     size_t capacity_ = 0;
     float* image_ = nullptr;
     size_t image_capacity_ = 0;
+    bhr_body_hit* body_hits_ = nullptr;
+    size_t body_capacity_ = 0;
     int width_ = 0, height_ = 0;
     LogFn log_;
 };

@@ -240,6 +240,43 @@ static int testGpu(const char* path) {
     CHECK(R.renderHost(iv, hh) && hh.size() == n && std::memcmp(hh.data(), hv.data(), n * sizeof(bhr_hit)) == 0,
           "renderHost = render with the volumetric disk");
     CHECK(!R.renderTo(iv, nullptr, nullptr) && !logged.empty(), "renderTo without an rgbt buffer is refused");
+    // bodies (the BHS_BODIES variant): a planet straight ahead stops the central rays
+    std::vector<bhr_body> bodies(1);
+    bhr_body& pl = bodies[0];
+    std::memset(&pl, 0, sizeof pl);
+    const bhr::Vec3d cp = cam.position();
+    const double cr = std::sqrt(cp.x * cp.x + cp.y * cp.y + cp.z * cp.z);
+    const double fr = 1.0 - 6.0 / cr;
+    const float pos[3] = {float(cp.x * fr), float(cp.y * fr), float(cp.z * fr)};
+    for (int k = 0; k < 3; ++k) {
+        pl.pos_radius[k] = pos[k];
+        pl.rel_pos[k] = float(pos[k] - (k == 0 ? cp.x : k == 1 ? cp.y : cp.z));
+    }
+    pl.pos_radius[3] = 0.8f;
+    pl.look[0] = 4.0f;  // the earth-like look
+    pl.look[1] = 7.0f;
+    pl.tint[0] = pl.tint[1] = pl.tint[2] = 1.0f;
+    pl.light[1] = 1.0f;
+    pl.light[3] = 1.0f;
+    pl.light_color[0] = pl.light_color[1] = pl.light_color[2] = 1.0f;
+    pl.axis[1] = 1.0f;
+    pl.ring[3] = 1.0f;
+    bhr::FrameInput ib = in;
+    ib.bodies = &bodies;
+    ib.time = 5.0f;
+    CHECK(R.renderImage(ib), "renderImage with a body");
+    std::vector<bhr_hit> hb(n);
+    std::vector<bhr_body_hit> bb(n);
+    cudaMemcpy(hb.data(), R.hits(), n * sizeof(bhr_hit), cudaMemcpyDeviceToHost);
+    cudaMemcpy(bb.data(), R.bodyHits(), n * sizeof(bhr_body_hit), cudaMemcpyDeviceToHost);
+    int onb = 0;
+    for (size_t k = 0; k < n; ++k) onb += hb[k].status == BHR_STATUS_BODY && bb[k].body == 0;
+    const size_t mid = (in.windowH / 2) * size_t(in.windowW) + in.windowW / 2;
+    std::snprintf(msg, sizeof msg, "%d pixels on the planet, the centre among them", onb);
+    CHECK(onb > 50 && hb[mid].status == BHR_STATUS_BODY, msg);
+    bhr::FrameInput ibv = ib;
+    ibv.settings = &sv;
+    CHECK(!R.render(ibv) && !logged.empty(), "bodies with the volumetric disk are refused");
     R.shutdown();
     return 0;
 }

@@ -9,7 +9,7 @@ import pytest
 
 import oracle_lib as O
 from blackholerender_gb300 import (BODY_HIT_DTYPE, DISK_NONE, DISK_THIN, DISK_VOLUMETRIC, SQRT27, STATUS_BODY,
-                                   TERM_CONFIG, TERM_SHADER, BhrError, Tracer, hits_numpy, make_view)
+                                   TERM_CONFIG, TERM_SHADER, BhrError, Tracer, hits_numpy, make_view, workloads)
 from test_cpu_bodies import body
 
 pytestmark = pytest.mark.gpu
@@ -98,39 +98,13 @@ def test_body_march_argument_errors(tracer):
     assert e.value.code == -1
 
 
-def _gallery(v):
-    """Twelve bodies in front of the camera: the nine planet looks, a star, an exploding
-    photosphere, a ringed translucent planet."""
-    cam = np.array(v.cam_pos, dtype=np.float64)
-    B = np.array(v.cam_basis, dtype=np.float64).reshape(3, 3)  # rows: right, up, back (column-major basis)
-    right, up, back = B[0], B[1], B[2]
-    out = []
-    for k in range(12):
-        gx, gy = k % 4, k // 4
-        pos = cam - 9.0 * back + (gx - 1.5) * 2.2 * right + (gy - 1.0) * 2.2 * up
-        b = body(pos, 0.7, cam, kind=1.0 if k in (9, 10) else 0.0)
-        b.look[:] = (float(k % 9), float(100 + k), 0.5 if k in (2, 4, 7) else 0.0, 0.3 * k)
-        L = back + 0.4 * right + 0.5 * up
-        b.light[:] = (*(L / np.linalg.norm(L)), 1.5)
-        b.light_color[:] = (1.0, 0.95, 0.9, 5772.0 if k != 10 else 9000.0)
-        if k == 10:
-            b.tint[3] = 0.8   # turbulence: an exploding photosphere
-            b.look[2] = 3.0   # plumes per radius
-            b.ring[2] = 1.7   # its clock
-        if k == 11:
-            b.ring[:] = (0.9, 1.4, 0.0, 0.6)
-            b.axis[:3] = (0.2, 0.9, 0.3)
-        out.append(b)
-    return out
-
-
 def test_body_shading_matches_the_oracle(tracer):
     import torch
 
     from blackholerender_gb300 import shade_params
 
     v = make_view(TERM_CONFIG, width=320, height=180, preset=0, pose=(30.0, math.radians(70.0), 0.4), disk_mode=DISK_THIN)
-    bodies = _gallery(v)
+    bodies = workloads.body_gallery(v)
     p = shade_params(time=37.0, doppler_strength=0.5)
     h, bhd = tracer.trace_bodies(v, bodies)
     img = tracer.shade_bodies(v, h, bhd, bodies, p)
