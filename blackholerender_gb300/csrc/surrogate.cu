@@ -917,7 +917,7 @@ __device__ __noinline__ float cap_invert(float u1, float A, float k2, float K, f
     return u;
 }
 
-__global__ void __launch_bounds__(32 * kInferWarps, 2) k_surrogate(const __grid_constant__ SurrView sv,
+__global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
                                                                 const float* __restrict__ P, WorkQueue* q,
                                                                 int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -411,7 +411,7 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
-        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 2, st);
+        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3, st);
     }
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     // 2) the integrator on the fallback rays: one launch for all views when they share a rule
