@@ -43,6 +43,11 @@ struct bhr_surrogate {
     bool have_last = false;
     bool last_from_plan = false;  // the last trace was a graph replay (its events do not time)
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // start, surrogate pass done, fallback done
+    // the views' surrogate launches alternate between two side streams (fork / join on the
+    // caller's stream), so each launch's last wave overlaps the next view's first; one pair per
+    // pipeline lane (lane 0: bhr_surrogate_trace and plans; lanes 0 and 1: the host-buffer path)
+    cudaStream_t side[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaEvent_t fork[2] = {nullptr, nullptr}, join[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     // bhr_surrogate_trace_host: device staging and two streams
     bhr_hit* staging = nullptr;
     int64_t staging_rays = 0;
@@ -150,6 +155,11 @@ int bhr_surrogate_create(bhr_surrogate** out, int device, const bhr_surrogate_co
     if (e == cudaSuccess) e = cudaMemset(s->adam_m, 0, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMemset(s->adam_v, 0, sizeof(float) * kNParams);
     for (int k = 0; e == cudaSuccess && k < 3; ++k) e = cudaEventCreate(&s->ev[k]);
+    for (int l = 0; e == cudaSuccess && l < 2; ++l) {
+        for (int k = 0; e == cudaSuccess && k < 2; ++k) e = cudaStreamCreateWithFlags(&s->side[l][k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork[l], cudaEventDisableTiming);
+        for (int k = 0; e == cudaSuccess && k < 2; ++k) e = cudaEventCreateWithFlags(&s->join[l][k], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
         bhr_surrogate_destroy(s);
         return fail(BHR_ERR_OOM, std::string("bhr_surrogate_create: ") + cudaGetErrorString(e));
@@ -166,6 +176,13 @@ int bhr_surrogate_destroy(bhr_surrogate* s) {
         if (p) cudaFree(p);
     for (cudaEvent_t& e : s->ev)
         if (e) cudaEventDestroy(e);
+    for (int l = 0; l < 2; ++l) {
+        for (cudaEvent_t& e : s->join[l])
+            if (e) cudaEventDestroy(e);
+        if (s->fork[l]) cudaEventDestroy(s->fork[l]);
+        for (cudaStream_t& st : s->side[l])
+            if (st) cudaStreamDestroy(st);
+    }
     for (cudaStream_t& st : s->hs)
         if (st) cudaStreamDestroy(st);
     delete s;
@@ -359,7 +376,19 @@ int bhr_surrogate_load(bhr_surrogate* s, const char* path) {
     return bhr_surrogate_set_params(s, P.data(), kNParams);
 }
 
+namespace {
+int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev, void* stream,
+                         int lane);
+}
+
 int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev, void* stream) {
+    return surrogate_trace_lane(s, views, nviews, out_dev, stream, 0);
+}
+
+namespace {
+// bhr_surrogate_trace on the side streams of pipeline lane `lane`.
+int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev, void* stream,
+                         int lane) {
     if (!s || !views || nviews <= 0 || !out_dev) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace: bad arguments");
     int64_t biggest = 0;
     for (int k = 0; k < nviews; ++k) {
@@ -384,7 +413,9 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
     e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
-    // 1) the surrogate pass of every view
+    if (e == cudaSuccess) e = cudaEventRecord(s->fork[lane], st);
+    for (int j = 0; e == cudaSuccess && j < 2; ++j) e = cudaStreamWaitEvent(s->side[lane][j], s->fork[lane], 0);
+    // 1) the surrogate pass of every view, alternating between the two side streams
     std::vector<bhr::DevView> dvs(static_cast<size_t>(nviews));
     std::vector<bhr::Rule> rules(static_cast<size_t>(nviews));
     bool one_rule = true;
@@ -411,7 +442,12 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
-        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3, st);
+        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3,
+                                              s->side[lane][k & 1]);
+    }
+    for (int j = 0; e == cudaSuccess && j < 2; ++j) {
+        e = cudaEventRecord(s->join[lane][j], s->side[lane][j]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, s->join[lane][j], 0);
     }
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     // 2) the integrator on the fallback rays: one launch for all views when they share a rule
@@ -448,6 +484,7 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
     s->last_from_plan = false;
     return BHR_OK;
 }
+}  // namespace
 
 // A fixed batch of views traced by one CUDA graph of bhr_surrogate_trace (bhr_surrogate_plan_*).
 struct bhr_surrogate_plan {
@@ -582,7 +619,7 @@ int bhr_surrogate_trace_host(bhr_surrogate* s, const bhr_view* views, int nviews
             dst.push_back(base + off);
             off += int64_t(views[k].width) * views[k].height;
         }
-        rc = bhr_surrogate_trace(s, views + k0, k1 - k0, dst.data(), st);
+        rc = surrogate_trace_lane(s, views + k0, k1 - k0, dst.data(), st, g & 1);
         off = 0;
         for (int k = k0; rc == BHR_OK && k < k1; ++k) {
             const int64_t n = int64_t(views[k].width) * views[k].height;
