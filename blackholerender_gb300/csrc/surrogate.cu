@@ -6,8 +6,9 @@
 // sign(beta) ln(1 + |beta|/eps) with beta = b / sqrt(27) - 1, x3 = orbit coordinate sigma
 // (surrogate_math.cuh); outputs y = (polar angle of the integrated orbit - closed-form baseline)
 // / y_scale at sigma, and a capture logit. The first and last layers run in FP32 on the CUDA
-// cores, the two 64x64 layers in BF16 on the tensor cores, activations rounded to BF16 between
-// them, exactly as in training. SiLU uses the SFU tanh: silu(z) = z/2 (1 + tanh(z/2)).
+// cores, the two 64x64 layers in BF16 on the tensor cores, every activation rounded to BF16, exactly
+// as in training. SiLU uses the SFU tanh: silu(z) = h + h tanh(h) with h = z/2. In inference the
+// output layer runs on the tensor cores too, with W4 split into three BF16 parts (FP32 accuracy).
 //
 // Fragment layout (PTX ISA, mma.m16n8k16 .bf16): with g = lane / 4, t = lane % 4, a thread holds
 // A rows g and g+8, columns 2t, 2t+1, 2t+8, 2t+9; B column g, rows 2t, 2t+1, 2t+8, 2t+9; C rows
@@ -34,10 +35,6 @@ __device__ __forceinline__ float tanh_sfu(float x) {
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float silu(float z) {
-    const float h = 0.5f * z;
-    return fmaf(h, tanh_sfu(h), h);
-}
 // d silu / dz = s + z s (1 - s), s = 1/2 + tanh(z/2)/2
 __device__ __forceinline__ float silu_grad(float z) {
     const float s = fmaf(0.5f, tanh_sfu(0.5f * z), 0.5f);
@@ -51,6 +48,15 @@ __device__ __forceinline__ uint32_t lds32(const __nv_bfloat16* p) { return *rein
 __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
     return uint32_t(__bfloat16_as_ushort(lo)) | (uint32_t(__bfloat16_as_ushort(hi)) << 16);
 }
+// silu of two half pre-activations h = z/2, fma(h, tanh h, h) in FP32, rounded to a BF16 pair (lo
+// in bits 0-15): a BF16 A-fragment register as it stands. (The packed tanh.approx.bf16x2 /
+// fma.rn.bf16x2 form measured 0.8% slower on the surrogate pass: the SFU spends the same time on
+// a packed pair as on two scalars, and the network is noisier.)
+__device__ __forceinline__ uint32_t silu2_h(float lo, float hi) {
+    return pack_bf16(fmaf(lo, tanh_sfu(lo), lo), fmaf(hi, tanh_sfu(hi), hi));
+}
+__device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
     asm volatile(
         "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -63,6 +69,10 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
 struct SmemNet {
     __nv_bfloat16 w2[kH * kLd];  // [out][in]
     __nv_bfloat16 w3[kH * kLd];
+    // inference only: the output layer as one n = 8 tile of BF16 B operands, [n][k]: rows 0-1 the
+    // BF16 parts of W4's two rows, rows 2-3 the BF16 parts of the remainders, rows 4-5 the rest
+    // (hi + mid + lo = W4 to 24 bits), rows 6-7 zero
+    __nv_bfloat16 w4s[8 * kLd];
     float4 w1[kH];               // {w[f][0], w[f][1], w[f][2], b[f]}
     float b2[kH], b3[kH];
     float w4[kOut * kH];
@@ -96,6 +106,8 @@ __device__ void load_net(SmemNet& N, SmemNetT* T, const float* __restrict__ P) {
     if (threadIdx.x < kOut) N.b4[threadIdx.x] = P[kB4 + threadIdx.x];
 }
 
+__device__ __forceinline__ void st_pair(__nv_bfloat16* p, uint32_t v) { *reinterpret_cast<uint32_t*>(p) = v; }
+
 // Layer 1 (FP32) for rows ra, rb of a 16-row tile: pre-activations z and BF16 A fragments of
 // silu(z) for the 16 features f = 16i + 2t + {0, 1, 8, 9} this thread owns.
 template <bool kStore>
@@ -103,26 +115,29 @@ __device__ __forceinline__ void layer1(const SmemNet& N, const float4& xa, const
                                        int t, __nv_bfloat16* zs, __nv_bfloat16* hs, int ra, int rb) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        float ha[4], hb[4];
+        float za[4], zb[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int f = 16 * i + 2 * t + (q & 1) + ((q & 2) ? 8 : 0);
             const float4 w = N.w1[f];
-            const float za = fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w)));
-            const float zb = fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w)));
-            ha[q] = silu(za);
-            hb[q] = silu(zb);
+            za[q] = fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w)));
+            zb[q] = fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w)));
             if (kStore) {
-                zs[ra * kLd + f] = __float2bfloat16_rn(za);
-                zs[rb * kLd + f] = __float2bfloat16_rn(zb);
-                hs[ra * kLd + f] = __float2bfloat16_rn(ha[q]);
-                hs[rb * kLd + f] = __float2bfloat16_rn(hb[q]);
+                zs[ra * kLd + f] = __float2bfloat16_rn(za[q]);
+                zs[rb * kLd + f] = __float2bfloat16_rn(zb[q]);
             }
         }
-        A[i][0] = pack_bf16(ha[0], ha[1]);
-        A[i][1] = pack_bf16(hb[0], hb[1]);
-        A[i][2] = pack_bf16(ha[2], ha[3]);
-        A[i][3] = pack_bf16(hb[2], hb[3]);
+        A[i][0] = silu2_h(0.5f * za[0], 0.5f * za[1]);
+        A[i][1] = silu2_h(0.5f * zb[0], 0.5f * zb[1]);
+        A[i][2] = silu2_h(0.5f * za[2], 0.5f * za[3]);
+        A[i][3] = silu2_h(0.5f * zb[2], 0.5f * zb[3]);
+        if (kStore) {
+            const int f = 16 * i + 2 * t;
+            st_pair(&hs[ra * kLd + f], A[i][0]);
+            st_pair(&hs[rb * kLd + f], A[i][1]);
+            st_pair(&hs[ra * kLd + f + 8], A[i][2]);
+            st_pair(&hs[rb * kLd + f + 8], A[i][3]);
+        }
     }
 }
 
@@ -145,14 +160,14 @@ __device__ __forceinline__ void mma_layer(const __nv_bfloat16* W, const float* b
     }
 }
 
-// C tiles (FP32) -> silu -> next layer's A fragments (BF16).
+// C tiles (FP32 pre-activations z) -> silu -> next layer's A fragments (BF16).
 __device__ __forceinline__ void act_pack(const float (&C)[8][4], uint32_t (&A)[4][4]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        A[i][0] = pack_bf16(silu(C[2 * i][0]), silu(C[2 * i][1]));
-        A[i][1] = pack_bf16(silu(C[2 * i][2]), silu(C[2 * i][3]));
-        A[i][2] = pack_bf16(silu(C[2 * i + 1][0]), silu(C[2 * i + 1][1]));
-        A[i][3] = pack_bf16(silu(C[2 * i + 1][2]), silu(C[2 * i + 1][3]));
+        A[i][0] = silu2_h(0.5f * C[2 * i][0], 0.5f * C[2 * i][1]);
+        A[i][1] = silu2_h(0.5f * C[2 * i][2], 0.5f * C[2 * i][3]);
+        A[i][2] = silu2_h(0.5f * C[2 * i + 1][0], 0.5f * C[2 * i + 1][1]);
+        A[i][3] = silu2_h(0.5f * C[2 * i + 1][2], 0.5f * C[2 * i + 1][3]);
     }
 }
 
@@ -173,7 +188,8 @@ __device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const int f = 8 * j + 2 * t;
-        const float h00 = silu(Z[j][0]), h01 = silu(Z[j][1]), h10 = silu(Z[j][2]), h11 = silu(Z[j][3]);
+        const uint32_t sa = silu2_h(0.5f * Z[j][0], 0.5f * Z[j][1]), sb = silu2_h(0.5f * Z[j][2], 0.5f * Z[j][3]);
+        const float h00 = bf_lo(sa), h01 = bf_hi(sa), h10 = bf_lo(sb), h11 = bf_hi(sb);
         const float w0a = N.w4[f], w0b = N.w4[f + 1], w1a = N.w4[kH + f], w1b = N.w4[kH + f + 1];
         pa0 = fmaf(w0a, h00, fmaf(w0b, h01, pa0));
         pa1 = fmaf(w1a, h00, fmaf(w1b, h01, pa1));
@@ -198,8 +214,8 @@ __device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][
 //
 // With W1, b1, W2, b2, W3, b3 multiplied by 1/2 when they are staged (exact in FP32 and BF16),
 // every hidden pre-activation comes out as h = z / 2 exactly (the FP32 accumulation of halved
-// products is the halved accumulation), and silu(z) = z/2 (1 + tanh(z/2)) = fma(h, tanh h, h):
-// the same bits as the training kernel's silu(z), one multiply fewer per activation.
+// products is the halved accumulation), so silu2_h takes the accumulators as they stand: the same
+// bits as the training kernel's activations, one multiply fewer per activation.
 
 // kFoldX1: every query of the launch has the same first input x1 (one view: x1 = scaled log r_cam),
 // so its term is folded into the first-layer bias and w1[f] holds {w_x2, w_sigma, w_x1 x1 + b, 0}/2.
@@ -222,10 +238,21 @@ __device__ void load_net_half(SmemNet& N, const float* __restrict__ P, float x1 
         N.w4[f] = P[kW4 + f];
         N.w4[kH + f] = P[kW4 + kH + f];
     }
+    // W4 = hi + mid + lo, each part BF16 (the differences are exact in FP32)
+    for (int k = threadIdx.x; k < 8 * kH; k += blockDim.x) {
+        const int n = k / kH, i = k % kH;
+        __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+        if (n < 6) {
+            const float w = P[kW4 + (n & 1) * kH + i];
+            const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+            const float r1 = w - __bfloat162float(hi);
+            const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+            v = n < 2 ? hi : n < 4 ? mid : __float2bfloat16_rn(r1 - __bfloat162float(mid));
+        }
+        N.w4s[n * kLd + i] = v;
+    }
     if (threadIdx.x < kOut) N.b4[threadIdx.x] = P[kB4 + threadIdx.x];
 }
-
-__device__ __forceinline__ float silu_h(float h) { return fmaf(h, tanh_sfu(h), h); }
 
 __device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
     const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -274,49 +301,55 @@ __device__ void mlp_eval_tiles(const SmemNet& N, const float4* q, float2* out, i
                 const int f = 16 * i + 2 * t + (k & 1) + ((k & 2) ? 8 : 0);
                 const float4 w = N.w1[f];
                 if (kFoldX1) {
-                    ha[k] = silu_h(fmaf(w.x, xa.y, fmaf(w.y, xa.z, w.z)));
-                    hb[k] = silu_h(fmaf(w.x, xb.y, fmaf(w.y, xb.z, w.z)));
+                    ha[k] = fmaf(w.x, xa.y, fmaf(w.y, xa.z, w.z));
+                    hb[k] = fmaf(w.x, xb.y, fmaf(w.y, xb.z, w.z));
                 } else {
-                    ha[k] = silu_h(fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w))));
-                    hb[k] = silu_h(fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w))));
+                    ha[k] = fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w)));
+                    hb[k] = fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w)));
                 }
             }
-            A[i][0] = pack_bf16(ha[0], ha[1]);
-            A[i][1] = pack_bf16(hb[0], hb[1]);
-            A[i][2] = pack_bf16(ha[2], ha[3]);
-            A[i][3] = pack_bf16(hb[2], hb[3]);
+            A[i][0] = silu2_h(ha[0], ha[1]);
+            A[i][1] = silu2_h(hb[0], hb[1]);
+            A[i][2] = silu2_h(ha[2], ha[3]);
+            A[i][3] = silu2_h(hb[2], hb[3]);
         }
         mma_layer_ldsm(N.w2, N.b2, A, C, lane, t);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            A[i][0] = pack_bf16(silu_h(C[2 * i][0]), silu_h(C[2 * i][1]));
-            A[i][1] = pack_bf16(silu_h(C[2 * i][2]), silu_h(C[2 * i][3]));
-            A[i][2] = pack_bf16(silu_h(C[2 * i + 1][0]), silu_h(C[2 * i + 1][1]));
-            A[i][3] = pack_bf16(silu_h(C[2 * i + 1][2]), silu_h(C[2 * i + 1][3]));
+            A[i][0] = silu2_h(C[2 * i][0], C[2 * i][1]);
+            A[i][1] = silu2_h(C[2 * i][2], C[2 * i][3]);
+            A[i][2] = silu2_h(C[2 * i + 1][0], C[2 * i + 1][1]);
+            A[i][3] = silu2_h(C[2 * i + 1][2], C[2 * i + 1][3]);
         }
         mma_layer_ldsm(N.w3, N.b3, A, C, lane, t);
-        float pa0 = 0.f, pa1 = 0.f, pb0 = 0.f, pb1 = 0.f;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int f = 8 * j + 2 * t;
-            const float h00 = silu_h(C[j][0]), h01 = silu_h(C[j][1]), h10 = silu_h(C[j][2]), h11 = silu_h(C[j][3]);
-            const float2 w0 = *reinterpret_cast<const float2*>(&N.w4[f]);
-            const float2 w1 = *reinterpret_cast<const float2*>(&N.w4[kH + f]);
-            pa0 = fmaf(w0.x, h00, fmaf(w0.y, h01, pa0));
-            pa1 = fmaf(w1.x, h00, fmaf(w1.y, h01, pa1));
-            pb0 = fmaf(w0.x, h10, fmaf(w0.y, h11, pb0));
-            pb1 = fmaf(w1.x, h10, fmaf(w1.y, h11, pb1));
+        for (int i = 0; i < 4; ++i) {
+            A[i][0] = silu2_h(C[2 * i][0], C[2 * i][1]);
+            A[i][1] = silu2_h(C[2 * i][2], C[2 * i][3]);
+            A[i][2] = silu2_h(C[2 * i + 1][0], C[2 * i + 1][1]);
+            A[i][3] = silu2_h(C[2 * i + 1][2], C[2 * i + 1][3]);
+        }
+        // output layer on the tensor core: column 2p + o of the n = 8 tile is part p of output o;
+        // the quad's lanes t hold parts t, so the outputs are the sums over t (b4 enters at t = 0)
+        float O[4];
+        O[0] = O[2] = t == 0 ? N.b4[0] : 0.f;
+        O[1] = O[3] = t == 0 ? N.b4[1] : 0.f;
+        {
+            const __nv_bfloat16* wl = N.w4s + (lane & 7) * kLd + 8 * (lane >> 3);
+            uint32_t b[8];
+            ldsm_x4(b[0], b[1], b[2], b[3], wl);
+            ldsm_x4(b[4], b[5], b[6], b[7], wl + 32);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) mma_bf16(O, A[i], b[2 * i], b[2 * i + 1]);
         }
 #pragma unroll
         for (int m = 1; m <= 2; m <<= 1) {
-            pa0 += __shfl_xor_sync(0xffffffffu, pa0, m);
-            pa1 += __shfl_xor_sync(0xffffffffu, pa1, m);
-            pb0 += __shfl_xor_sync(0xffffffffu, pb0, m);
-            pb1 += __shfl_xor_sync(0xffffffffu, pb1, m);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) O[c] += __shfl_xor_sync(0xffffffffu, O[c], m);
         }
         if (t == 0) {
-            out[ra] = make_float2(pa0 + N.b4[0], pa1 + N.b4[1]);
-            out[rb] = make_float2(pb0 + N.b4[0], pb1 + N.b4[1]);
+            out[ra] = make_float2(O[0], O[1]);
+            out[rb] = make_float2(O[2], O[3]);
         }
     }
     __syncwarp();
@@ -608,12 +641,16 @@ __global__ void __launch_bounds__(32 * kTrainWarps, 1) k_train_step(
                 W.z2[ra * kLd + f + 1] = __float2bfloat16_rn(C[j][1]);
                 W.z2[rb * kLd + f] = __float2bfloat16_rn(C[j][2]);
                 W.z2[rb * kLd + f + 1] = __float2bfloat16_rn(C[j][3]);
-                W.h2[ra * kLd + f] = __float2bfloat16_rn(silu(C[j][0]));
-                W.h2[ra * kLd + f + 1] = __float2bfloat16_rn(silu(C[j][1]));
-                W.h2[rb * kLd + f] = __float2bfloat16_rn(silu(C[j][2]));
-                W.h2[rb * kLd + f + 1] = __float2bfloat16_rn(silu(C[j][3]));
             }
             act_pack(C, A);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int f = 16 * i + 2 * t;
+                st_pair(&W.h2[ra * kLd + f], A[i][0]);
+                st_pair(&W.h2[rb * kLd + f], A[i][1]);
+                st_pair(&W.h2[ra * kLd + f + 8], A[i][2]);
+                st_pair(&W.h2[rb * kLd + f + 8], A[i][3]);
+            }
             float Z3[8][4];
             mma_layer(N.w3, N.b3, A, Z3, g, t);
             float o[2][2];
@@ -645,10 +682,13 @@ __global__ void __launch_bounds__(32 * kTrainWarps, 1) k_train_step(
             for (int j = 0; j < 8; ++j) {
                 const int f = 8 * j + 2 * t;
                 float gw[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, gb[2] = {0.f, 0.f};
+                const uint32_t sa = silu2_h(0.5f * Z3[j][0], 0.5f * Z3[j][1]);
+                const uint32_t sb = silu2_h(0.5f * Z3[j][2], 0.5f * Z3[j][3]);
+                const float hv[4] = {bf_lo(sa), bf_hi(sa), bf_lo(sb), bf_hi(sb)};
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     const int rr = c >> 1, ff = f + (c & 1);
-                    const float h3 = silu(Z3[j][c]);
+                    const float h3 = hv[c];
                     gw[0][c & 1] += dy[rr] * h3;
                     gw[1][c & 1] += dc[rr] * h3;
                     const float dh = dy[rr] * N.w4[ff] + dc[rr] * N.w4[kH + ff];

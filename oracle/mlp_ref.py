@@ -4,8 +4,9 @@ Mirrors blackholerender_gb300/csrc/surrogate.cu: 3 -> 64 -> 64 -> 64 -> 2, SiLU,
 the flat layout [W1 (64x3), b1, W2 (64x64), b2, W3 (64x64), b3, W4 (2x64), b4]. The loss of a
 batch of n samples (x1, x2, sigma, y) with labels (0 escaped, 1 captured, 2 ignored) is
     L = sum_i [label_i == 0] (y_pred_i - y_i)^2 / n + w_c sum_i [label_i != 2] BCE(logit_i, label_i == 1) / n.
-The GPU path rounds the hidden-layer weights and their input activations to BF16; with
-quantize=True this reference does the same, everything else in FP64.
+The GPU path rounds the hidden-layer weights and every activation (the output layer's inputs
+too) to BF16; with quantize=True this reference does the same, everything else in FP64 (the
+output layer's weights are FP32 on the GPU: three BF16 parts in inference).
 """
 from __future__ import annotations
 
@@ -50,15 +51,20 @@ def silu_grad(z):
     return s + z * s * (1.0 - s)
 
 
+def act(z, quantize=True):
+    """The network's activation: SiLU, rounded to BF16 as on the GPU when quantize is set."""
+    return bf16(silu(z)) if quantize else silu(z)
+
+
 def forward(p, x, quantize=True):
     d = unpack(p)
     q = bf16 if quantize else (lambda a: np.asarray(a, dtype=np.float64))
     z1 = x @ d["W1"].T + d["b1"]
-    h1 = silu(z1)
-    z2 = q(h1) @ q(d["W2"]).T + d["b2"]
-    h2 = silu(z2)
-    z3 = q(h2) @ q(d["W3"]).T + d["b3"]
-    h3 = silu(z3)
+    h1 = act(z1, quantize)
+    z2 = h1 @ q(d["W2"]).T + d["b2"]
+    h2 = act(z2, quantize)
+    z3 = h2 @ q(d["W3"]).T + d["b3"]
+    h3 = act(z3, quantize)
     out = h3 @ d["W4"].T + d["b4"]
     return out, (z1, h1, z2, h2, z3, h3)
 
@@ -86,10 +92,10 @@ def loss_and_grad(p, samples, labels, w_c, quantize=True):
     g["W4"] = dout.T @ h3
     g["b4"] = dout.sum(0)
     dz3 = (dout @ d["W4"]) * silu_grad(z3)
-    g["W3"] = dz3.T @ q(h2)
+    g["W3"] = dz3.T @ h2
     g["b3"] = dz3.sum(0)
     dz2 = (dz3 @ q(d["W3"])) * silu_grad(z2)
-    g["W2"] = dz2.T @ q(h1)
+    g["W2"] = dz2.T @ h1
     g["b2"] = dz2.sum(0)
     dz1 = (dz2 @ q(d["W2"])) * silu_grad(z1)
     g["W1"] = dz1.T @ x
