@@ -10,6 +10,13 @@
 // Shading the hit is the consumer's (bhr_shade_bodies); the march records where it happened.
 // One ray per thread, warps of 8 x 4 pixels; the bodies are kernel parameters (constant bank,
 // read warp-uniformly). FP32, like the shader.
+//
+// Clearance: each ray keeps a lower bound on its distance to the surface of every body the two
+// loops test. A step's chord shortens it by at most the chord's length (triangle inequality), so
+// the loops run only on steps where a body could shorten the step (within 2 ds) or be reached by
+// the chord; the other steps skip them. The bound carries a relative margin of 1e-5 against
+// FP32 rounding, so a skipped loop is one in which every body would have failed its own
+// squared-distance test: the records are the same bits as with the loops run on every step.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -86,6 +93,7 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
     V3<float> hit_ro{0.f, 0.f, 0.f}, hit_rd{0.f, 0.f, 0.f};
     float hit_t = 0.f;
     const bool thin = R.disk_mode == BHR_DISK_THIN;
+    float clear = -1.f;  // lower bound of |x - c| - R over the bodies the loops test; < 0: unknown
     if (R.far_mode) {
         status = BHR_STATUS_ESCAPED;
     } else {
@@ -134,14 +142,20 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
             }
             // land on the near-field hit; short steps near the other bodies (:184-190)
             if (near_idx >= 0) ds = fminf(ds, fmaxf(near_t - travelled, near_tol));
-            for (int b = 0; b < nb; ++b) {
-                if (near_mask & (1u << b)) continue;
-                const float* pr = A.bodies[b].pos_radius;
-                const V3<float> d{x.x - pr[0], x.y - pr[1], x.z - pr[2]};
-                // a body farther than 2 ds + R cannot shorten the step: skipped without the sqrt
-                const float reach = 2.0f * ds + pr[3];
-                if (dot3(d, d) >= reach * reach) continue;
-                ds = fminf(ds, fmaxf(0.5f * (len3(d) - pr[3]), 0.25f * pr[3]));
+            if (clear < 2.00002f * ds) {  // a body may be within 2 ds: the loop, and a fresh bound
+                clear = INFINITY;
+                for (int b = 0; b < nb; ++b) {
+                    if (near_mask & (1u << b)) continue;
+                    const float* pr = A.bodies[b].pos_radius;
+                    const V3<float> d{x.x - pr[0], x.y - pr[1], x.z - pr[2]};
+                    const float dd = dot3(d, d);
+                    const float dist = sqrtf(dd);
+                    clear = fminf(clear, fmaf(dist, 0.99999f, -pr[3]));
+                    // a body farther than 2 ds + R cannot shorten the step
+                    const float reach = 2.0f * ds + pr[3];
+                    if (dd >= reach * reach) continue;
+                    ds = fminf(ds, fmaxf(0.5f * (dist - pr[3]), 0.25f * pr[3]));
+                }
             }
             const float dt = ds * vi;
             const V3<float> x0 = x;
@@ -168,8 +182,9 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
                     }
                 }
             }
-            // the step's chord against the bodies not settled by the near-field test (:236-250)
-            if (nb > 0 && seg > 0.f) {
+            // the step's chord against the bodies not settled by the near-field test (:236-250);
+            // a chord shorter than the clearance at its start reaches no body
+            if (nb > 0 && seg > 0.f && 1.00001f * seg >= clear) {
                 const V3<float> sd{dx.x / seg, dx.y / seg, dx.z / seg};
                 float best = seg;
                 for (int b = 0; b < nb; ++b) {
@@ -193,6 +208,7 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
                     break;
                 }
             }
+            clear = fmaf(clear, 0.999999f, -1.0001f * seg);  // over-subtracts more than it rounds
         }
     }
     const bool nonfinite = !isfinite(dot3(x, x) + dot3(v, v));
