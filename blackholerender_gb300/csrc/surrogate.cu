@@ -19,6 +19,7 @@
 
 #include "surrogate.cuh"
 #include "surrogate_math.cuh"
+#include "tc_mlp.cuh"
 
 namespace bhr {
 namespace surr {
@@ -795,22 +796,44 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, floa
     p[k] -= lr * mh / (sqrtf(vh) + eps);
 }
 
-// Plain forward pass over n queries (tests and the gradient check): one warp per 32 queries.
-__global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ P, const float4* __restrict__ q,
-                                                   float2* __restrict__ out, int n) {
-    __shared__ __align__(16) SmemNet N;
-    __shared__ float4 qs[4][32];
-    __shared__ float2 os[4][32];
-    load_net_half<false>(N, P);
+// Plain forward pass over n queries (tests and the gradient check) on the tcgen05 network: one
+// warpgroup per block, 128 queries per tile. *status is set to 1 if a tensor-core wait ran out
+// (the tile's outputs are then NaN and the block stops).
+__global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ P, const float4* __restrict__ q,
+                                                      float2* __restrict__ out, int n, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tc::Net& N = *reinterpret_cast<tc::Net*>(smem_raw);
+    tc::Tile& T = *reinterpret_cast<tc::Tile*>(smem_raw + sizeof(tc::Net));
+    __shared__ uint32_t tmem_slot;
+    __shared__ int fail;
+    tc::load_net(N, P, false, 0.f);
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_u32(&T.mbar), 1);
+        fail = 0;
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(tc::smem_u32(&tmem_slot), tc::kTmemCols);
+    tc::fence_smem_async();
+    tc::fence_before();
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int base = (blockIdx.x * 4 + warp) * 32; base < n; base += gridDim.x * 4 * 32) {
-        const int k = base + lane;
-        qs[warp][lane] = k < n ? q[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-        __syncwarp();
-        mlp_eval_tiles<false>(N, qs[warp], os[warp], 2);
-        if (k < n) out[k] = os[warp][lane];
-        __syncwarp();
+    tc::fence_after();
+    const uint32_t tmem = tmem_slot;
+    uint32_t phase = 0;
+    for (int t0 = blockIdx.x * tc::kRows; t0 < n; t0 += gridDim.x * tc::kRows) {
+        const int row = t0 + int(threadIdx.x);
+        const float4 x = row < n ? q[row] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 o;
+        const bool ok = tc::mlp_tile(N, T, tmem, int(threadIdx.x), 1, phase, x, o);
+        if (!ok) fail = 1;
+        if (row < n) out[row] = ok ? o : make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+        __syncthreads();
+        if (fail) break;
+    }
+    if (fail && threadIdx.x == 0) atomicExch(status, 1);
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, tc::kTmemCols);
     }
 }
 
@@ -1294,8 +1317,9 @@ cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int grid, cudaStream_t st) {
-    k_mlp_infer<<<grid, 128, 0, st>>>(params, q, out, n);
+cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int* status, int grid,
+                             cudaStream_t st) {
+    k_mlp_infer<<<grid, 128, sizeof(tc::Net) + sizeof(tc::Tile), st>>>(params, q, out, n, status);
     return cudaGetLastError();
 }
 

@@ -49,7 +49,8 @@ cudaError_t launch_train_step(const float* params, const TrainSample* X, const i
                               float* loss, int grid, cudaStream_t st);
 cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
                         float beta2, float eps, cudaStream_t st);
-cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int grid, cudaStream_t st);
+cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int* status, int grid,
+                             cudaStream_t st);
 
 struct SurrView {
     DevView view;

@@ -331,16 +331,23 @@ int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out
     DevGuard dg(s->device);
     float4* q = nullptr;
     float2* o = nullptr;
+    int* status = nullptr;
+    int hstatus = 0;
     std::vector<float4> hq(static_cast<size_t>(n));
     for (int k = 0; k < n; ++k) hq[size_t(k)] = make_float4(queries[3 * k], queries[3 * k + 1], queries[3 * k + 2], 0.f);
     cudaError_t e = cudaMalloc(&q, sizeof(float4) * size_t(n));
     if (e == cudaSuccess) e = cudaMalloc(&o, sizeof(float2) * size_t(n));
+    if (e == cudaSuccess) e = cudaMalloc(&status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(status, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(q, hq.data(), sizeof(float4) * size_t(n), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = bhr::surr::launch_mlp_infer(s->params, q, o, n, s->sms * 4, nullptr);
+    if (e == cudaSuccess) e = bhr::surr::launch_mlp_infer(s->params, q, o, n, status, s->sms * 4, nullptr);
     if (e == cudaSuccess) e = cudaMemcpy(out, o, sizeof(float2) * size_t(n), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost);
     if (q) cudaFree(q);
     if (o) cudaFree(o);
-    return e == cudaSuccess ? BHR_OK : cfail(e, "bhr_surrogate_eval");
+    if (status) cudaFree(status);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_eval");
+    return hstatus ? fail(BHR_ERR_TIMEOUT, "bhr_surrogate_eval: a tensor-core completion wait ran out") : BHR_OK;
 }
 
 int bhr_surrogate_save(bhr_surrogate* s, const char* path) {

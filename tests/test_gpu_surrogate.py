@@ -75,3 +75,22 @@ def test_short_training_reduces_loss():
     last = hist[-20:, 0].mean()
     assert np.all(np.isfinite(hist))
     assert last < 0.2 * first, (first, last)
+
+
+def test_tensor_core_forward_pass_matches_reference():
+    """The evaluation kernel runs the network on tcgen05 (128-row tiles, TMEM accumulators, the
+    first layer and the biases as split BF16 products): against the FP64 network with the GPU's
+    BF16 roundings, on 8192 queries of the trained range."""
+    from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT
+    s = Surrogate(seed=1)
+    s.load(str(DEFAULT_CHECKPOINT))
+    rng = np.random.default_rng(5)
+    n = 8192
+    q = np.stack([rng.uniform(-1, 1, n), rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)], axis=1).astype(np.float32)
+    out = s.eval(q)
+    ref, _ = mlp_ref.forward(s.params().astype(np.float64), q.astype(np.float64), quantize=True)
+    assert np.all(np.isfinite(out))
+    scale = np.abs(ref).max(axis=0)
+    p99 = np.percentile(np.abs(out - ref), 99, axis=0)
+    # measured p99 4.1e-4 and 4.6e-5 of the output scales (tanh.approx and BF16 rounding flips)
+    assert p99[0] < 2e-3 * scale[0] and p99[1] < 3e-4 * scale[1], (p99, scale)
