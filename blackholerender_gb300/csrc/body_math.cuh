@@ -402,6 +402,15 @@ __device__ inline float4 nearest_body_straight(const Tex& tx, const bhr_body* bo
     for (int k = 0; k < nb; ++k) {
         if (skip & (1u << k)) continue;
         const F3 c = camera_frame ? xyz4(bodies[k].rel_pos) : xyz4(bodies[k].pos_radius);
+        {  // the sphere and its ring lie within ext of c: a ray passing wider, or a body behind the
+           // origin seen from outside, is missed by both tests below. The slack (1e-6 |oc|^2) is
+           // above both computations' FP32 rounding, so no hit is culled.
+            const F3 oc = sub(c, ro);
+            const float oo = dot(oc, oc), tc = dot(oc, rd);
+            const float ext = fmaxf(bodies[k].pos_radius[3], bodies[k].ring[1]);
+            const float lim = fmaf(ext, ext, fmaf(1e-6f, oo, 1e-6f));
+            if (oo - tc * tc > lim || (tc < 0.0f && oo > lim)) continue;
+        }
         float t_hit;
         const float4 col = trace_body(tx, bodies[k], c, ro, rd, best_t, t_hit, footprint, time);
         if (t_hit > 0.0f && t_hit < best_t) {
