@@ -59,6 +59,7 @@ struct bhr_ctx {
     // shading: the blackbody table and the disk's noise volume, made on first use
     float4* lut = nullptr;
     uint16_t* noise = nullptr;
+    uint4* noise8 = nullptr;  // the volume's per-texel neighbourhoods, as the samplers read it
     uint32_t noise_seed = 0;
     bool noise_ready = false;
     std::string err;
@@ -357,6 +358,7 @@ int bhr_destroy(bhr_ctx* c) {
     if (c->staging) cudaFree(c->staging);
     if (c->lut) cudaFree(c->lut);
     if (c->noise) cudaFree(c->noise);
+    if (c->noise8) cudaFree(c->noise8);
     for (cudaStream_t& st : c->hstream)
         if (st) cudaStreamDestroy(st);
     cudaSetDevice(prev);
@@ -749,16 +751,23 @@ int ensure_shade_resources(bhr_ctx* c, uint32_t seed, cudaStream_t st) {
         e = cudaMemcpy(c->lut, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cuda_fail(c, e, "bhr_shade: blackbody table");
     }
-    if (!c->noise) {
-        const cudaError_t e = cudaMalloc(&c->noise, size_t(BHR_NOISE_SIZE) * BHR_NOISE_SIZE * BHR_NOISE_SIZE * 2);
+    if (!c->noise || !c->noise8) {
+        const size_t texels = size_t(BHR_NOISE_SIZE) * BHR_NOISE_SIZE * BHR_NOISE_SIZE;
+        cudaError_t e = c->noise ? cudaSuccess : cudaMalloc(&c->noise, texels * 2);
         if (e != cudaSuccess) {
             c->noise = nullptr;
             return cuda_fail(c, e, "bhr_shade: noise volume");
+        }
+        e = cudaMalloc(&c->noise8, texels * sizeof(uint4));
+        if (e != cudaSuccess) {
+            c->noise8 = nullptr;
+            return cuda_fail(c, e, "bhr_shade: noise neighbourhoods");
         }
         c->noise_ready = false;
     }
     if (!c->noise_ready || c->noise_seed != seed) {
         cudaError_t e = bhr::launch_noise_bake(seed, c->noise, st);
+        if (e == cudaSuccess) e = bhr::launch_noise_expand(c->noise, c->noise8, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(c, e, "bhr_shade: noise bake");
         c->noise_seed = seed;
@@ -809,7 +818,7 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         a.ln_22000 = std::log(22000.0f);
         a.hits = hits[k];
         a.out = reinterpret_cast<float4*>(rgba[k]);
-        a.noise = c->noise;
+        a.noise8 = c->noise8;
         a.lut = c->lut;
         const cudaError_t e = bhr::launch_shade(a, st);
         if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_shade: kernel launch");
@@ -858,7 +867,7 @@ int bhr_shade_bodies(bhr_ctx* c, const bhr_view* view, const bhr_hit* hits, cons
         a.ln_22000 = std::log(22000.0f);
         a.hits = hits;
         a.out = reinterpret_cast<float4*>(rgba);
-        a.noise = c->noise;
+        a.noise8 = c->noise8;
         a.lut = c->lut;
         bhr::BodyShadeArgs b{};
         b.bh = body;
@@ -903,7 +912,7 @@ int bhr_trace_volumetric(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit*
         a.ln_1000 = std::log(1000.0f);
         a.ln_40000 = std::log(40000.0f);
         a.thick = views[k].disk_thickness;
-        a.noise = c->noise;
+        a.noise8 = c->noise8;
         a.lut = c->lut;
         a.rgbt = reinterpret_cast<float4*>(rgbt[k]);
         const cudaError_t e = bhr::launch_march_vol(a, st);

@@ -76,6 +76,21 @@ __global__ void __launch_bounds__(256) k_noise_bake(uint32_t seed, uint16_t* __r
     out[idx] = __half_as_ushort(__float2half_rn(n));  // the R16F store
 }
 
+// The baked volume's 2x2x2 REPEAT neighbourhood of every texel, as the sampler reads it: word 0
+// = (x, x+1) at (y, z), word 1 at (y+1, z), word 2 at (y, z+1), word 3 at (y+1, z+1); the lower
+// half of each word is x.
+__global__ void __launch_bounds__(256) k_noise_expand(const uint16_t* __restrict__ v, uint4* __restrict__ out) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= kN * kN * kN) return;
+    const int x = idx % kN, y = (idx / kN) % kN, z = idx / (kN * kN);
+    const int x1 = (x + 1) & (kN - 1), y1 = (y + 1) & (kN - 1), z1 = (z + 1) & (kN - 1);
+    auto pair = [&](int yy, int zz) {
+        const size_t row = (size_t(zz) * kN + yy) * kN;
+        return uint32_t(v[row + x]) | (uint32_t(v[row + x1]) << 16);
+    };
+    out[idx] = make_uint4(pair(y, z), pair(y1, z), pair(y, z1), pair(y1, z1));
+}
+
 // ---------------------------------------------------------------- shading
 
 struct Footprint {
@@ -327,7 +342,7 @@ __device__ __forceinline__ void shade_block(const ShadeArgs& A, const BodyShadeA
     __shared__ StarSlot s_star[kBX * kBY / 32][32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int k = tid; k < kLut; k += kBX * kBY) s_lut[k] = A.lut[k];
-    const Tex tx{A.noise, s_lut, A.ln_1000, A.ln_40000};
+    const Tex tx{A.noise8, s_lut, A.ln_1000, A.ln_40000};
     const int i = blockIdx.x * kBX + (warp & 3) * 8 + (lane & 7);
     const int j = blockIdx.y * kBY + (warp >> 2) * 4 + (lane >> 3);
     const bool in = i < A.width && j < A.height;
@@ -486,6 +501,12 @@ void blackbody_lut_host(float* out) {
 cudaError_t launch_noise_bake(uint32_t seed, uint16_t* out, cudaStream_t st) {
     const int n = kN * kN * kN;
     k_noise_bake<<<(n + 255) / 256, 256, 0, st>>>(seed, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_noise_expand(const uint16_t* vol, uint4* out, cudaStream_t st) {
+    const int n = kN * kN * kN;
+    k_noise_expand<<<(n + 255) / 256, 256, 0, st>>>(vol, out);
     return cudaGetLastError();
 }
 

@@ -23,7 +23,7 @@ struct ShadeArgs {
     float ln_1000, ln_40000, ln_3000, ln_22000;  // logf of the constants, from the host's libm
     const bhr_hit* hits;
     float4* out;
-    const uint16_t* noise;  // BHR_NOISE_SIZE^3 half
+    const uint4* noise8;    // BHR_NOISE_SIZE^3 texel neighbourhoods (launch_noise_expand)
     const float4* lut;      // BHR_BLACKBODY_LUT entries
 };
 
@@ -36,6 +36,9 @@ struct BodyShadeArgs {
 };
 
 cudaError_t launch_noise_bake(uint32_t seed, uint16_t* out, cudaStream_t st);
+// Per texel of the baked volume, its 2x2x2 neighbourhood with REPEAT as eight halves (16 B), so
+// that a trilinear sample is one load.
+cudaError_t launch_noise_expand(const uint16_t* vol, uint4* out, cudaStream_t st);
 cudaError_t launch_shade_bodies(const ShadeArgs& a, const BodyShadeArgs& b, cudaStream_t st);
 cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t st);
 void blackbody_lut_host(float* out);  // BHR_BLACKBODY_LUT x 4 floats, in double like the CPU bake

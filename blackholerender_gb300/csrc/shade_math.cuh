@@ -65,7 +65,7 @@ __device__ __forceinline__ F3 grad3(int cx, int cy, int cz, uint32_t salt) {
 }
 
 struct Tex {
-    const uint16_t* noise;
+    const uint4* noise8;  // per texel its 2x2x2 REPEAT neighbourhood, eight halves (k_noise_expand)
     const float4* lut;  // shared memory
     float ln_1000, ln_40000;
 };
@@ -85,8 +85,8 @@ __device__ __forceinline__ float4 blackbody(const Tex& tx, float T) {
     return o;
 }
 
-__device__ __forceinline__ float texel(const Tex& tx, int x, int y, int z) {
-    return __half2float(__ushort_as_half(__ldg(tx.noise + (size_t(z) * kN + y) * kN + x)));
+__device__ __forceinline__ float2 half2_bits(uint32_t u) {
+    return __half22float2(*reinterpret_cast<const __half2*>(&u));
 }
 
 // texture(uNoise3d, c).r: trilinear, REPEAT
@@ -96,11 +96,13 @@ __device__ inline float noise_sample(const Tex& tx, F3 c) {
     const float ax = ux - fx, ay = uy - fy, az = uz - fz;
     // REPEAT: the wrap of a power-of-two size is a mask (two's complement for negative texels)
     const int x0 = int(fx) & (kN - 1), y0 = int(fy) & (kN - 1), z0 = int(fz) & (kN - 1);
-    const int x1 = (x0 + 1) & (kN - 1), y1 = (y0 + 1) & (kN - 1), z1 = (z0 + 1) & (kN - 1);
-    const float c00 = mixf(texel(tx, x0, y0, z0), texel(tx, x1, y0, z0), ax);
-    const float c10 = mixf(texel(tx, x0, y1, z0), texel(tx, x1, y1, z0), ax);
-    const float c01 = mixf(texel(tx, x0, y0, z1), texel(tx, x1, y0, z1), ax);
-    const float c11 = mixf(texel(tx, x0, y1, z1), texel(tx, x1, y1, z1), ax);
+    // one 16-byte load: (x0, x1) pairs at (y0, z0), (y1, z0), (y0, z1), (y1, z1)
+    const uint4 q = __ldg(tx.noise8 + (size_t(z0) * kN + y0) * kN + x0);
+    const float2 p00 = half2_bits(q.x), p10 = half2_bits(q.y), p01 = half2_bits(q.z), p11 = half2_bits(q.w);
+    const float c00 = mixf(p00.x, p00.y, ax);
+    const float c10 = mixf(p10.x, p10.y, ax);
+    const float c01 = mixf(p01.x, p01.y, ax);
+    const float c11 = mixf(p11.x, p11.y, ax);
     return mixf(mixf(c00, c10, ay), mixf(c01, c11, ay), az);
 }
 

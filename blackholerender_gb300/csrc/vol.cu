@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) k_march_vol(const __grid_constant__ VolAr
     const int j = blockIdx.y * 8 + (warp >> 2) * 4 + (lane >> 3);
     if (i >= w.width || j >= w.height) return;
     const Rule& R = A.rule;
-    const shading::Tex tx{A.noise, s_lut, A.ln_1000, A.ln_40000};
+    const shading::Tex tx{A.noise8, s_lut, A.ln_1000, A.ln_40000};
     const RayInit<float> ri = setup_ray<float>(w, R, i, j);
     const int64_t k = int64_t(j) * w.width + i;
     bhr_hit* rec = w.out + k;

@@ -15,7 +15,7 @@ struct VolArgs {
     bhr_shade_params p;      // the disk's look (density, opacity, temperature, noise, Doppler)
     float ln_1000, ln_40000; // logf of the blackbody table's range, from the host's libm
     float thick;             // uDiskThickness (H / r)
-    const uint16_t* noise;   // BHR_NOISE_SIZE^3 half
+    const uint4* noise8;     // BHR_NOISE_SIZE^3 texel neighbourhoods (launch_noise_expand)
     const float4* lut;       // BHR_BLACKBODY_LUT entries
     float4* rgbt;            // per pixel: gathered rgb, transmittance
 };
