@@ -264,6 +264,7 @@ SIGNATURES.update({
     "bhr_surrogate_gradients": (ctypes.c_int, [_P, _F, ctypes.POINTER(ctypes.c_int8), ctypes.c_int, ctypes.c_float,
                                                _F, _F]),
     "bhr_surrogate_eval": (ctypes.c_int, [_P, _F, ctypes.c_int, _F]),
+    "bhr_surrogate_wait_selftest": (ctypes.c_int, [_P]),
     "bhr_surrogate_save": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "bhr_surrogate_load": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "bhr_surrogate_trace": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), _P]),

@@ -798,9 +798,11 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, floa
 
 // Plain forward pass over n queries (tests and the gradient check) on the tcgen05 network: one
 // warpgroup per block, 128 queries per tile. *status is set to 1 if a tensor-core wait ran out
-// (the tile's outputs are then NaN and the block stops).
+// (the tile's outputs are then NaN and the block stops). ctl.withhold is the self-test of that
+// path: no MMA is issued, so every wait runs out with nothing in flight.
 __global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ P, const float4* __restrict__ q,
-                                                      float2* __restrict__ out, int n, int* __restrict__ status) {
+                                                      float2* __restrict__ out, int n, int* __restrict__ status,
+                                                      const tc::TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     tc::Net& N = *reinterpret_cast<tc::Net*>(smem_raw);
     tc::Tile& T = *reinterpret_cast<tc::Tile*>(smem_raw + sizeof(tc::Net));
@@ -822,7 +824,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ 
         const int row = t0 + int(threadIdx.x);
         const float4 x = row < n ? q[row] : make_float4(0.f, 0.f, 0.f, 0.f);
         float2 o;
-        const bool ok = tc::mlp_tile(N, T, tmem, int(threadIdx.x), 1, phase, x, o);
+        const bool ok = tc::mlp_tile(N, T, tmem, int(threadIdx.x), 1, phase, x, o, ctl);
         if (!ok) fail = 1;
         if (row < n) out[row] = ok ? o : make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
         __syncthreads();
@@ -1318,8 +1320,11 @@ cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, i
 }
 
 cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int* status, int grid,
-                             cudaStream_t st) {
-    k_mlp_infer<<<grid, 128, sizeof(tc::Net) + sizeof(tc::Tile), st>>>(params, q, out, n, status);
+                             cudaStream_t st, long long wait_cycles, bool withhold) {
+    tc::TileCtl ctl;
+    if (wait_cycles > 0) ctl.wait_cycles = wait_cycles;
+    ctl.withhold = withhold;
+    k_mlp_infer<<<grid, 128, sizeof(tc::Net) + sizeof(tc::Tile), st>>>(params, q, out, n, status, ctl);
     return cudaGetLastError();
 }
 

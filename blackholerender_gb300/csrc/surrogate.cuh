@@ -49,8 +49,9 @@ cudaError_t launch_train_step(const float* params, const TrainSample* X, const i
                               float* loss, int grid, cudaStream_t st);
 cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
                         float beta2, float eps, cudaStream_t st);
+// wait_cycles <= 0: the default completion-wait limit; withhold: the timeout self-test
 cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int* status, int grid,
-                             cudaStream_t st);
+                             cudaStream_t st, long long wait_cycles = 0, bool withhold = false);
 
 struct SurrView {
     DevView view;

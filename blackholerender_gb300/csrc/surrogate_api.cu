@@ -350,6 +350,29 @@ int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out
     return hstatus ? fail(BHR_ERR_TIMEOUT, "bhr_surrogate_eval: a tensor-core completion wait ran out") : BHR_OK;
 }
 
+int bhr_surrogate_wait_selftest(bhr_surrogate* s) {
+    if (!s) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_wait_selftest: NULL");
+    DevGuard dg(s->device);
+    constexpr int n = 128;  // one tile, one block
+    float4* q = nullptr;
+    float2* o = nullptr;
+    int* status = nullptr;
+    int hstatus = 0;
+    cudaError_t e = cudaMalloc(&q, sizeof(float4) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&o, sizeof(float2) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(q, 0, sizeof(float4) * n);
+    if (e == cudaSuccess) e = cudaMemset(status, 0, sizeof(int));
+    if (e == cudaSuccess) e = bhr::surr::launch_mlp_infer(s->params, q, o, n, status, 1, nullptr, 100000000ll, true);
+    if (e == cudaSuccess) e = cudaMemcpy(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (q) cudaFree(q);
+    if (o) cudaFree(o);
+    if (status) cudaFree(status);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_wait_selftest");
+    return hstatus ? fail(BHR_ERR_TIMEOUT, "bhr_surrogate_wait_selftest: the withheld completions timed out and were reported")
+                   : fail(BHR_ERR_CUDA, "bhr_surrogate_wait_selftest: the withheld completions were not reported");
+}
+
 int bhr_surrogate_save(bhr_surrogate* s, const char* path) {
     if (!s || !path) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_save: NULL");
     std::vector<float> P(kNParams);

@@ -40,6 +40,13 @@ constexpr int kRows = 128;               // M of a tile: one row per thread of a
 constexpr uint32_t kTmemCols = 64;       // one N = 64 FP32 accumulator per warpgroup
 constexpr long long kWaitCycles = 4000000000ll;  // about 2 s of SM clock before a wait gives up
 
+// How a tile runs: the completion-wait limit in SM clocks, and (self-test only) whether the MMAs
+// and their commit are withheld, so that every wait runs out with nothing in flight.
+struct TileCtl {
+    long long wait_cycles = kWaitCycles;
+    bool withhold = false;
+};
+
 // byte offset of element (row, k) in a K-major no-swizzle tile with kc 16-byte chunks per row
 __host__ __device__ constexpr uint32_t kmaj(int row, int k, int kc) {
     return uint32_t(((row >> 3) * kc + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
@@ -160,7 +167,7 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
 }
 // bounded wait for the phase with the given parity (non-blocking polls against a clock
 // deadline); false if it did not complete
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     for (;;) {
         uint32_t ok;
@@ -170,7 +177,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
             : "r"(mbar), "r"(parity)
             : "memory");
         if (ok) return true;
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -250,11 +257,11 @@ constexpr uint32_t kI16 = idesc_bf16(128, 16);
 // MMA did not complete within the bounded wait (every later step of the tile still runs, with
 // bounded waits, so that the warpgroup's barriers stay matched).
 __device__ inline bool mlp_tile(const Net& N, Tile& T, uint32_t tmem, int row, int bar_id, uint32_t& phase, float4 x,
-                                float2& out) {
+                                float2& out, const TileCtl& ctl = TileCtl{}) {
     unsigned char* a = reinterpret_cast<unsigned char*>(T.a);
     const uint32_t a_s = smem_u32(T.a), mbar = smem_u32(&T.mbar);
     const uint32_t taddr = tmem + (uint32_t((row >> 5) * 32) << 16);
-    const bool issuer = row == 0;
+    const bool issuer = row == 0 && !ctl.withhold;
     bool ok = true;
     {  // layer-1 A row: x1h x1l x1h x2h x2l x2h sh sl sh 1 1 1 0 0 0 0
         const uint32_t x1h = bf_bits(x.x), x2h = bf_bits(x.y), sh = bf_bits(x.z);
@@ -273,7 +280,7 @@ __device__ inline bool mlp_tile(const Net& N, Tile& T, uint32_t tmem, int row, i
         mma(tmem, sdesc(a_s, 128, 256), sdesc(smem_u32(N.w1), 128, 256), kI64, 0u);
         commit(mbar);
     }
-    ok &= mbar_wait(mbar, phase);
+    ok &= mbar_wait(mbar, phase, ctl.wait_cycles);
     phase ^= 1u;
     fence_after();
     act_to_a(taddr, a, row);
@@ -292,7 +299,7 @@ __device__ inline bool mlp_tile(const Net& N, Tile& T, uint32_t tmem, int row, i
             mma(tmem, sdesc(smem_u32(N.ones), 128, 256), sdesc(smem_u32(B[l]), 128, 256), kI64, 1u);
             commit(mbar);
         }
-        ok &= mbar_wait(mbar, phase);
+        ok &= mbar_wait(mbar, phase, ctl.wait_cycles);
         phase ^= 1u;
         fence_after();
         act_to_a(taddr, a, row);
@@ -309,7 +316,7 @@ __device__ inline bool mlp_tile(const Net& N, Tile& T, uint32_t tmem, int row, i
         mma(tmem, sdesc(smem_u32(N.ones), 128, 256), sdesc(smem_u32(N.b4), 128, 256), kI16, 1u);
         commit(mbar);
     }
-    ok &= mbar_wait(mbar, phase);
+    ok &= mbar_wait(mbar, phase, ctl.wait_cycles);
     phase ^= 1u;
     fence_after();
     float c[8];

@@ -88,6 +88,11 @@ class Surrogate:
         _abi.check(_abi.lib().bhr_surrogate_eval(self.h, q.ctypes.data_as(F), len(q), out.ctypes.data_as(F)))
         return out
 
+    def wait_selftest(self):
+        """Runs the timeout self-test of the forward pass's bounded waits; returns the status code
+        (ERR_TIMEOUT when the expired waits were reported)."""
+        return int(_abi.lib().bhr_surrogate_wait_selftest(self.h))
+
     def generate(self, n_orbits, per_orbit=4, seed=7):
         c = (ctypes.c_uint64 * 3)()
         _abi.check(_abi.lib().bhr_surrogate_generate(self.h, n_orbits, per_orbit, seed, None, c))

@@ -258,8 +258,14 @@ int bhr_surrogate_set_params(bhr_surrogate* s, const float* in, int n);
  * mean(w_u (y_pred - y)^2) + w_capture mean(BCE), and loss sums {sum err^2, sum BCE, n_y}. */
 int bhr_surrogate_gradients(bhr_surrogate* s, const float* samples, const int8_t* labels, int n, float w_capture,
                             float* grad_out, float* loss_out);
-/* Forward pass: n queries {x1, x2, sigma} -> n x {y, capture logit}. */
+/* Forward pass: n queries {x1, x2, sigma} -> n x {y, capture logit} (tensor-core kernel with
+ * bounded completion waits; BHR_ERR_TIMEOUT if one ran out). */
 int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out);
+/* Self-test of the device-side timeout path (no reference counterpart): one tile of the forward
+ * pass with its MMAs withheld, so that every completion wait runs out after about 1e8 SM clocks
+ * with nothing in flight. Returns BHR_ERR_TIMEOUT when the kernel reported the expired waits (the
+ * expected result) and BHR_ERR_CUDA if it did not; the context stays usable either way. */
+int bhr_surrogate_wait_selftest(bhr_surrogate* s);
 int bhr_surrogate_save(bhr_surrogate* s, const char* path);
 int bhr_surrogate_load(bhr_surrogate* s, const char* path);
 /* Surrogate-plus-fallback trace (CONFIG rule, lensing on): stream-ordered like bhr_trace. */

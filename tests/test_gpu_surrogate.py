@@ -94,3 +94,16 @@ def test_tensor_core_forward_pass_matches_reference():
     p99 = np.percentile(np.abs(out - ref), 99, axis=0)
     # measured p99 4.1e-4 and 4.6e-5 of the output scales (tanh.approx and BF16 rounding flips)
     assert p99[0] < 2e-3 * scale[0] and p99[1] < 3e-4 * scale[1], (p99, scale)
+
+
+def test_tensor_core_wait_timeout_is_reported():
+    """The forward pass's completion waits are bounded: with the MMAs withheld (nothing in flight)
+    every wait runs out, the kernel reports it, the call returns ERR_TIMEOUT, and the context is
+    still usable for a normal pass afterwards."""
+    from blackholerender_gb300 import _abi
+    s = Surrogate(seed=2)
+    assert s.wait_selftest() == _abi.ERR_TIMEOUT
+    q = np.zeros((256, 3), dtype=np.float32)
+    out = s.eval(q)
+    ref, _ = mlp_ref.forward(s.params().astype(np.float64), q.astype(np.float64), quantize=True)
+    assert np.all(np.isfinite(out)) and np.max(np.abs(out - ref)) < 1e-2 * np.max(np.abs(ref)) + 1e-3
