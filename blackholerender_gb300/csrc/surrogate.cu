@@ -53,7 +53,7 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
 // in bits 0-15): a BF16 A-fragment register as it stands. (The packed tanh.approx.bf16x2 /
 // fma.rn.bf16x2 form measured 0.8% slower on the surrogate pass: the SFU spends the same time on
 // a packed pair as on two scalars, and the network is noisier.)
-__device__ __forceinline__ uint32_t silu2_h(float lo, float hi) {
+__device__ __forceinline__ uint32_t silu_pair_h(float lo, float hi) {
     return pack_bf16(fmaf(lo, tanh_sfu(lo), lo), fmaf(hi, tanh_sfu(hi), hi));
 }
 __device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
@@ -128,10 +128,10 @@ __device__ __forceinline__ void layer1(const SmemNet& N, const float4& xa, const
                 zs[rb * kLd + f] = __float2bfloat16_rn(zb[q]);
             }
         }
-        A[i][0] = silu2_h(0.5f * za[0], 0.5f * za[1]);
-        A[i][1] = silu2_h(0.5f * zb[0], 0.5f * zb[1]);
-        A[i][2] = silu2_h(0.5f * za[2], 0.5f * za[3]);
-        A[i][3] = silu2_h(0.5f * zb[2], 0.5f * zb[3]);
+        A[i][0] = silu_pair_h(0.5f * za[0], 0.5f * za[1]);
+        A[i][1] = silu_pair_h(0.5f * zb[0], 0.5f * zb[1]);
+        A[i][2] = silu_pair_h(0.5f * za[2], 0.5f * za[3]);
+        A[i][3] = silu_pair_h(0.5f * zb[2], 0.5f * zb[3]);
         if (kStore) {
             const int f = 16 * i + 2 * t;
             st_pair(&hs[ra * kLd + f], A[i][0]);
@@ -165,10 +165,10 @@ __device__ __forceinline__ void mma_layer(const __nv_bfloat16* W, const float* b
 __device__ __forceinline__ void act_pack(const float (&C)[8][4], uint32_t (&A)[4][4]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        A[i][0] = silu2_h(0.5f * C[2 * i][0], 0.5f * C[2 * i][1]);
-        A[i][1] = silu2_h(0.5f * C[2 * i][2], 0.5f * C[2 * i][3]);
-        A[i][2] = silu2_h(0.5f * C[2 * i + 1][0], 0.5f * C[2 * i + 1][1]);
-        A[i][3] = silu2_h(0.5f * C[2 * i + 1][2], 0.5f * C[2 * i + 1][3]);
+        A[i][0] = silu_pair_h(0.5f * C[2 * i][0], 0.5f * C[2 * i][1]);
+        A[i][1] = silu_pair_h(0.5f * C[2 * i][2], 0.5f * C[2 * i][3]);
+        A[i][2] = silu_pair_h(0.5f * C[2 * i + 1][0], 0.5f * C[2 * i + 1][1]);
+        A[i][3] = silu_pair_h(0.5f * C[2 * i + 1][2], 0.5f * C[2 * i + 1][3]);
     }
 }
 
@@ -189,7 +189,7 @@ __device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const int f = 8 * j + 2 * t;
-        const uint32_t sa = silu2_h(0.5f * Z[j][0], 0.5f * Z[j][1]), sb = silu2_h(0.5f * Z[j][2], 0.5f * Z[j][3]);
+        const uint32_t sa = silu_pair_h(0.5f * Z[j][0], 0.5f * Z[j][1]), sb = silu_pair_h(0.5f * Z[j][2], 0.5f * Z[j][3]);
         const float h00 = bf_lo(sa), h01 = bf_hi(sa), h10 = bf_lo(sb), h11 = bf_hi(sb);
         const float w0a = N.w4[f], w0b = N.w4[f + 1], w1a = N.w4[kH + f], w1b = N.w4[kH + f + 1];
         pa0 = fmaf(w0a, h00, fmaf(w0b, h01, pa0));
@@ -215,7 +215,7 @@ __device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][
 //
 // With W1, b1, W2, b2, W3, b3 multiplied by 1/2 when they are staged (exact in FP32 and BF16),
 // every hidden pre-activation comes out as h = z / 2 exactly (the FP32 accumulation of halved
-// products is the halved accumulation), so silu2_h takes the accumulators as they stand: the same
+// products is the halved accumulation), so silu_pair_h takes the accumulators as they stand: the same
 // bits as the training kernel's activations, one multiply fewer per activation.
 
 // kFoldX1: every query of the launch has the same first input x1 (one view: x1 = scaled log r_cam),
@@ -309,26 +309,26 @@ __device__ void mlp_eval_tiles(const SmemNet& N, const float4* q, float2* out, i
                     hb[k] = fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w)));
                 }
             }
-            A[i][0] = silu2_h(ha[0], ha[1]);
-            A[i][1] = silu2_h(hb[0], hb[1]);
-            A[i][2] = silu2_h(ha[2], ha[3]);
-            A[i][3] = silu2_h(hb[2], hb[3]);
+            A[i][0] = silu_pair_h(ha[0], ha[1]);
+            A[i][1] = silu_pair_h(hb[0], hb[1]);
+            A[i][2] = silu_pair_h(ha[2], ha[3]);
+            A[i][3] = silu_pair_h(hb[2], hb[3]);
         }
         mma_layer_ldsm(N.w2, N.b2, A, C, lane, t);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            A[i][0] = silu2_h(C[2 * i][0], C[2 * i][1]);
-            A[i][1] = silu2_h(C[2 * i][2], C[2 * i][3]);
-            A[i][2] = silu2_h(C[2 * i + 1][0], C[2 * i + 1][1]);
-            A[i][3] = silu2_h(C[2 * i + 1][2], C[2 * i + 1][3]);
+            A[i][0] = silu_pair_h(C[2 * i][0], C[2 * i][1]);
+            A[i][1] = silu_pair_h(C[2 * i][2], C[2 * i][3]);
+            A[i][2] = silu_pair_h(C[2 * i + 1][0], C[2 * i + 1][1]);
+            A[i][3] = silu_pair_h(C[2 * i + 1][2], C[2 * i + 1][3]);
         }
         mma_layer_ldsm(N.w3, N.b3, A, C, lane, t);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            A[i][0] = silu2_h(C[2 * i][0], C[2 * i][1]);
-            A[i][1] = silu2_h(C[2 * i][2], C[2 * i][3]);
-            A[i][2] = silu2_h(C[2 * i + 1][0], C[2 * i + 1][1]);
-            A[i][3] = silu2_h(C[2 * i + 1][2], C[2 * i + 1][3]);
+            A[i][0] = silu_pair_h(C[2 * i][0], C[2 * i][1]);
+            A[i][1] = silu_pair_h(C[2 * i][2], C[2 * i][3]);
+            A[i][2] = silu_pair_h(C[2 * i + 1][0], C[2 * i + 1][1]);
+            A[i][3] = silu_pair_h(C[2 * i + 1][2], C[2 * i + 1][3]);
         }
         // output layer on the tensor core: column 2p + o of the n = 8 tile is part p of output o;
         // the quad's lanes t hold parts t, so the outputs are the sums over t (b4 enters at t = 0)
@@ -683,8 +683,8 @@ __global__ void __launch_bounds__(32 * kTrainWarps, 1) k_train_step(
             for (int j = 0; j < 8; ++j) {
                 const int f = 8 * j + 2 * t;
                 float gw[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, gb[2] = {0.f, 0.f};
-                const uint32_t sa = silu2_h(0.5f * Z3[j][0], 0.5f * Z3[j][1]);
-                const uint32_t sb = silu2_h(0.5f * Z3[j][2], 0.5f * Z3[j][3]);
+                const uint32_t sa = silu_pair_h(0.5f * Z3[j][0], 0.5f * Z3[j][1]);
+                const uint32_t sb = silu_pair_h(0.5f * Z3[j][2], 0.5f * Z3[j][3]);
                 const float hv[4] = {bf_lo(sa), bf_hi(sa), bf_lo(sb), bf_hi(sb)};
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
