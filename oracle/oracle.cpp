@@ -242,18 +242,28 @@ void oracle_pcg3d(const uint32_t in[3], uint32_t out[3]) {
 
 // The volumetric disk's march of every pixel of a view: records, and rgbt[4 k] = the colour the
 // march gathered and the transmittance left (blackhole.frag:217-234).
-int oracle_trace_volumetric(const bhr_view* v, const bhr_shade_params* p, const uint16_t* noise, const float* lut,
-                            bhr_hit* out, float* rgbt, int nthreads, int fp64) {
+// The volumetric march of the listed pixels (idx = j * width + i; every pixel when idx is NULL):
+// out[k] and rgbt[4k..4k+3] belong to idx[k].
+int oracle_trace_volumetric_pixels(const bhr_view* v, const bhr_shade_params* p, const uint16_t* noise,
+                                   const float* lut, const int64_t* idx, int64_t n, bhr_hit* out, float* rgbt,
+                                   int nthreads, int fp64) {
     if (!v || !p || !noise || !lut || !out || !rgbt || v->width <= 0 || v->height <= 0 || v->max_steps < 0 ||
-        v->disk_mode != BHR_DISK_VOLUMETRIC)
+        v->disk_mode != BHR_DISK_VOLUMETRIC || n < 0)
         return BHR_ERR_INVALID_ARG;
+    const int64_t npix = static_cast<int64_t>(v->width) * v->height;
+    if (idx) {
+        for (int64_t k = 0; k < n; ++k)
+            if (idx[k] < 0 || idx[k] >= npix) return BHR_ERR_INVALID_ARG;
+    } else if (n != npix) {
+        return BHR_ERR_INVALID_ARG;
+    }
     const oracle::shade::Tex tx{noise, lut};
     const float cx = v->cam_pos[0], cy = v->cam_pos[1], cz = v->cam_pos[2];
     const VolumeSampler vs{&tx, p, v->disk_inner, v->disk_outer, v->disk_thickness, std::sqrt(cx * cx + cy * cy + cz * cz)};
-    const int64_t n = static_cast<int64_t>(v->width) * v->height;
     auto one = [&](auto R, int64_t k) {
         using T = decltype(R.step_scale);
-        const int i = static_cast<int>(k % v->width), j = static_cast<int>(k / v->width);
+        const int64_t px = idx ? idx[k] : k;
+        const int i = static_cast<int>(px % v->width), j = static_cast<int>(px / v->width);
         const V3<T> cam{T(v->cam_pos[0]), T(v->cam_pos[1]), T(v->cam_pos[2])};
         const Result<T> r = march(R, cam, primaryRay<T>(*v, i, j), vs);
         toHit(r, out + k);
@@ -270,6 +280,13 @@ int oracle_trace_volumetric(const bhr_view* v, const bhr_shade_params* p, const 
     return BHR_OK;
 }
 
+int oracle_trace_volumetric(const bhr_view* v, const bhr_shade_params* p, const uint16_t* noise, const float* lut,
+                            bhr_hit* out, float* rgbt, int nthreads, int fp64) {
+    if (!v || v->width <= 0 || v->height <= 0) return BHR_ERR_INVALID_ARG;
+    return oracle_trace_volumetric_pixels(v, p, noise, lut, nullptr, static_cast<int64_t>(v->width) * v->height, out,
+                                          rgbt, nthreads, fp64);
+}
+
 // Shades a volumetric view: the records and the march's rgbt from oracle_trace_volumetric.
 int oracle_shade_volumetric(const bhr_view* v, const bhr_hit* hits, const float* rgbt, const bhr_shade_params* p,
                             const uint16_t* noise, const float* lut, float* rgba, int nthreads) {
@@ -284,13 +301,22 @@ int oracle_shade_volumetric(const bhr_view* v, const bhr_hit* hits, const float*
 
 // The body-aware march (BHS_BODIES 1) of every pixel of a view: records, and per pixel what the
 // shading after the loop needs (bhr_body_hit).
-int oracle_trace_bodies(const bhr_view* v, const bhr_body* bodies, int nb, bhr_hit* out, bhr_body_hit* bout,
-                        int nthreads, int fp64) {
-    if (!view_ok(v) || nb < 0 || nb > BHR_MAX_BODIES || (nb > 0 && !bodies) || !out || !bout) return BHR_ERR_INVALID_ARG;
-    const int64_t n = static_cast<int64_t>(v->width) * v->height;
+// idx: the listed pixels (j * width + i), out[k] / bout[k] belonging to idx[k]; NULL: every pixel.
+int oracle_trace_bodies_pixels(const bhr_view* v, const bhr_body* bodies, int nb, const int64_t* idx, int64_t n,
+                               bhr_hit* out, bhr_body_hit* bout, int nthreads, int fp64) {
+    if (!view_ok(v) || nb < 0 || nb > BHR_MAX_BODIES || (nb > 0 && !bodies) || !out || !bout || n < 0)
+        return BHR_ERR_INVALID_ARG;
+    const int64_t npix = static_cast<int64_t>(v->width) * v->height;
+    if (idx) {
+        for (int64_t k = 0; k < n; ++k)
+            if (idx[k] < 0 || idx[k] >= npix) return BHR_ERR_INVALID_ARG;
+    } else if (n != npix) {
+        return BHR_ERR_INVALID_ARG;
+    }
     auto one = [&](auto R, int64_t k) {
         using T = decltype(R.step_scale);
-        const int i = static_cast<int>(k % v->width), j = static_cast<int>(k / v->width);
+        const int64_t px = idx ? idx[k] : k;
+        const int i = static_cast<int>(px % v->width), j = static_cast<int>(px / v->width);
         const V3<T> cam{T(v->cam_pos[0]), T(v->cam_pos[1]), T(v->cam_pos[2])};
         BodyMarch<T> bm;
         bm.b = bodies;
@@ -318,6 +344,13 @@ int oracle_trace_bodies(const bhr_view* v, const bhr_body* bodies, int nb, bhr_h
         parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
     }
     return BHR_OK;
+}
+
+int oracle_trace_bodies(const bhr_view* v, const bhr_body* bodies, int nb, bhr_hit* out, bhr_body_hit* bout,
+                        int nthreads, int fp64) {
+    if (!view_ok(v)) return BHR_ERR_INVALID_ARG;
+    return oracle_trace_bodies_pixels(v, bodies, nb, nullptr, static_cast<int64_t>(v->width) * v->height, out, bout,
+                                      nthreads, fp64);
 }
 
 // Shades a view marched with bodies: its records, body records and the bodies.

@@ -52,6 +52,11 @@ def lib():
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.oracle_trace_volumetric.argtypes = [VP, ctypes.POINTER(ShadeParams), ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.oracle_trace_volumetric_pixels.argtypes = [VP, ctypes.POINTER(ShadeParams), ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_int, ctypes.c_int]
+        L.oracle_trace_bodies_pixels.argtypes = [VP, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
+                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.oracle_shade_volumetric.argtypes = [VP, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ShadeParams),
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.oracle_trace_bodies.argtypes = [VP, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
@@ -216,6 +221,21 @@ def trace_volumetric(view: View, params: ShadeParams, noise: np.ndarray, lut: np
     return hits, rgbt
 
 
+def trace_volumetric_pixels(view: View, params: ShadeParams, noise: np.ndarray, lut: np.ndarray, idx: np.ndarray,
+                            fp64: bool = True, threads: int | None = None):
+    """The volumetric march of the listed pixels (j * width + i): (records, rgbt (n, 4))."""
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    noise = np.ascontiguousarray(noise, dtype=np.uint16)
+    lut = np.ascontiguousarray(lut, dtype=np.float32)
+    hits = np.zeros(len(idx), dtype=HIT_DTYPE)
+    rgbt = np.zeros((len(idx), 4), dtype=np.float32)
+    rc = lib().oracle_trace_volumetric_pixels(ctypes.byref(view), ctypes.byref(params), noise.ctypes.data,
+                                              lut.ctypes.data, idx.ctypes.data, len(idx), hits.ctypes.data,
+                                              rgbt.ctypes.data, threads or nthreads(), int(fp64))
+    assert rc == 0
+    return hits, rgbt
+
+
 def shade_volumetric(view: View, hits: np.ndarray, rgbt: np.ndarray, params: ShadeParams, noise: np.ndarray,
                      lut: np.ndarray, threads: int | None = None) -> np.ndarray:
     hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
@@ -237,6 +257,19 @@ def trace_bodies(view: View, bodies, fp64: bool = True, threads: int | None = No
     bh = np.zeros(view.width * view.height, dtype=BODY_HIT_DTYPE)
     rc = lib().oracle_trace_bodies(ctypes.byref(view), ctypes.cast(arr, ctypes.c_void_p), n, hits.ctypes.data,
                                    bh.ctypes.data, threads or nthreads(), int(fp64))
+    assert rc == 0
+    return hits, bh
+
+
+def trace_bodies_pixels(view: View, bodies, idx: np.ndarray, fp64: bool = True, threads: int | None = None):
+    """The body-aware march of the listed pixels (j * width + i): (records, body records)."""
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    n = len(bodies)
+    arr = (Body * max(n, 1))(*bodies)
+    hits = np.zeros(len(idx), dtype=HIT_DTYPE)
+    bh = np.zeros(len(idx), dtype=BODY_HIT_DTYPE)
+    rc = lib().oracle_trace_bodies_pixels(ctypes.byref(view), ctypes.cast(arr, ctypes.c_void_p), n, idx.ctypes.data,
+                                          len(idx), hits.ctypes.data, bh.ctypes.data, threads or nthreads(), int(fp64))
     assert rc == 0
     return hits, bh
 

@@ -189,3 +189,14 @@ def test_ring_in_front_of_the_sky():
     # hole's shadow is not drawn, as in the reference
     assert changed.sum() > 20
     assert np.all(img.reshape(-1, 4)[changed, 3] <= bare.reshape(-1, 4)[changed, 3] + 1e-6)
+
+
+def test_sampled_pixels_equal_the_whole_view():
+    """The restatement's sampled-pixel entry marches exactly the pixels the whole-view entry does."""
+    from blackholerender_gb300 import workloads
+    v = make_view(TERM_CONFIG, width=48, height=27, preset=2, pose=(30.0, math.radians(80.0), 0.4))
+    bodies = workloads.body_gallery(v)
+    h, bh = O.trace_bodies(v, bodies)
+    idx = np.array([0, 11, 500, 1295, 648, 649])
+    hs, bs = O.trace_bodies_pixels(v, bodies, idx)
+    assert hs.tobytes() == h[idx].tobytes() and bs.tobytes() == bh[idx].tobytes()

@@ -69,3 +69,15 @@ def test_fp32_restatement_against_fp64(tex):
           f"{np.median(d / scale):.2e} p99 {np.percentile(d / scale, 99):.2e}")
     assert agree > 0.995
     assert np.percentile(d / scale, 99) < 0.05
+
+
+def test_sampled_pixels_equal_the_whole_view():
+    """The restatement's sampled-pixel entry marches exactly the pixels the whole-view entry does."""
+    v = make_view(TERM_CONFIG, disk_mode=DISK_VOLUMETRIC, width=48, height=27, preset=0,
+                  pose=(30.0, np.radians(85.0), 0.0))
+    p = shade_params()
+    noise, lut = O.noise_bake(7), O.blackbody_lut()
+    h, c = O.trace_volumetric(v, p, noise, lut, fp64=True)
+    idx = np.array([0, 7, 300, 1295, 640, 641])
+    hs, cs = O.trace_volumetric_pixels(v, p, noise, lut, idx, fp64=True)
+    assert hs.tobytes() == h[idx].tobytes() and np.array_equal(cs, c.reshape(-1, 4)[idx])
