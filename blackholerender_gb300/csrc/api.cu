@@ -62,6 +62,10 @@ struct bhr_ctx {
     uint4* noise8 = nullptr;  // the volume's per-texel neighbourhoods, as the samplers read it
     uint32_t noise_seed = 0;
     bool noise_ready = false;
+    // per-view launches of bhr_shade / bhr_trace_volumetric alternate between two side streams,
+    // forked from and joined back to the caller's stream (made on first use)
+    cudaStream_t fan[2] = {nullptr, nullptr};
+    cudaEvent_t fan_fork = nullptr, fan_join[2] = {nullptr, nullptr};
     std::string err;
 };
 
@@ -360,6 +364,11 @@ int bhr_destroy(bhr_ctx* c) {
     if (c->noise) cudaFree(c->noise);
     if (c->noise8) cudaFree(c->noise8);
     for (cudaStream_t& st : c->hstream)
+        if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t& e : c->fan_join)
+        if (e) cudaEventDestroy(e);
+    if (c->fan_fork) cudaEventDestroy(c->fan_fork);
+    for (cudaStream_t& st : c->fan)
         if (st) cudaStreamDestroy(st);
     cudaSetDevice(prev);
     delete c;
@@ -738,6 +747,42 @@ int bhr_noise_bake(bhr_ctx* c, uint32_t seed, uint16_t* out, void* cuda_stream) 
 
 namespace {
 
+// Per-view launches spread over the context's two side streams: open() forks them from the
+// caller's stream, lane(k) is view k's stream, close() joins them back, so that one view's last
+// partial wave overlaps the next view's first. With one view everything stays on `st`.
+struct Fan {
+    bhr_ctx* c = nullptr;
+    cudaStream_t st = nullptr;
+    bool on = false;
+    cudaError_t open(bhr_ctx* ctx, cudaStream_t s, int nviews) {
+        c = ctx;
+        st = s;
+        on = nviews > 1;
+        if (!on) return cudaSuccess;
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; e == cudaSuccess && k < 2; ++k)
+            if (!c->fan[k]) e = cudaStreamCreateWithFlags(&c->fan[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess && !c->fan_fork) e = cudaEventCreateWithFlags(&c->fan_fork, cudaEventDisableTiming);
+        for (int k = 0; e == cudaSuccess && k < 2; ++k)
+            if (!c->fan_join[k]) e = cudaEventCreateWithFlags(&c->fan_join[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(c->fan_fork, st);
+        for (int k = 0; e == cudaSuccess && k < 2; ++k) e = cudaStreamWaitEvent(c->fan[k], c->fan_fork, 0);
+        if (e != cudaSuccess) on = false;
+        return e;
+    }
+    cudaStream_t lane(int k) const { return on ? c->fan[k & 1] : st; }
+    cudaError_t close() {
+        if (!on) return cudaSuccess;
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; e == cudaSuccess && k < 2; ++k) {
+            e = cudaEventRecord(c->fan_join[k], c->fan[k]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, c->fan_join[k], 0);
+        }
+        on = false;
+        return e;
+    }
+};
+
 // The blackbody table and the noise volume of `seed`, complete before the call returns.
 int ensure_shade_resources(bhr_ctx* c, uint32_t seed, cudaStream_t st) {
     if (!c->lut) {
@@ -795,6 +840,11 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
     cudaSetDevice(c->device);
     const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     int rc = ensure_shade_resources(c, p->noise_seed, st);
+    Fan fan;
+    if (rc == BHR_OK) {
+        const cudaError_t e = fan.open(c, st, nviews);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_shade: side streams");
+    }
     for (int k = 0; k < nviews && rc == BHR_OK; ++k) {
         const bhr_view& v = views[k];
         bhr::ShadeArgs a{};
@@ -820,8 +870,12 @@ int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* cons
         a.out = reinterpret_cast<float4*>(rgba[k]);
         a.noise8 = c->noise8;
         a.lut = c->lut;
-        const cudaError_t e = bhr::launch_shade(a, st);
+        const cudaError_t e = bhr::launch_shade(a, fan.lane(k));
         if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_shade: kernel launch");
+    }
+    {
+        const cudaError_t e = fan.close();
+        if (e != cudaSuccess && rc == BHR_OK) rc = cuda_fail(c, e, "bhr_shade: side streams");
     }
     cudaSetDevice(prev);
     return rc;
@@ -904,6 +958,11 @@ int bhr_trace_volumetric(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit*
     cudaSetDevice(c->device);
     const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     int rc = ensure_shade_resources(c, p->noise_seed, st);
+    Fan fan;
+    if (rc == BHR_OK) {
+        const cudaError_t e = fan.open(c, st, nviews);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace_volumetric: side streams");
+    }
     for (int k = 0; k < nviews && rc == BHR_OK; ++k) {
         bhr::VolArgs a{};
         a.view = bhr::host::make_dev_view(views[k], hits[k]);
@@ -915,8 +974,12 @@ int bhr_trace_volumetric(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit*
         a.noise8 = c->noise8;
         a.lut = c->lut;
         a.rgbt = reinterpret_cast<float4*>(rgbt[k]);
-        const cudaError_t e = bhr::launch_march_vol(a, st);
+        const cudaError_t e = bhr::launch_march_vol(a, fan.lane(k));
         if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace_volumetric: kernel launch");
+    }
+    {
+        const cudaError_t e = fan.close();
+        if (e != cudaSuccess && rc == BHR_OK) rc = cuda_fail(c, e, "bhr_trace_volumetric: side streams");
     }
     cudaSetDevice(prev);
     return rc;
