@@ -982,6 +982,47 @@ __device__ __noinline__ float cap_invert(float u1, float A, float k2, float K, f
     return u;
 }
 
+// The view's exit table: per half (0 captured, 1 escaping) and point i, x2_i = lo + i h, the
+// beta it encodes (the inverse of the x2 transform), the exit query the pass would make for that
+// beta, and the network's output through the same folded-x1 forward pass as k_surrogate.
+__global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ SurrView sv, const float* __restrict__ P,
+                                                    float2* __restrict__ table) {
+    __shared__ __align__(16) SmemNet N;
+    __shared__ float4 qs[8][32];
+    __shared__ float2 os[8][32];
+    load_net_half<true>(N, P, sv.x1);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Norm& nm = sv.norm;
+    for (int base = (blockIdx.x * 8 + warp) * 32; base < 2 * kExitTableN; base += gridDim.x * 8 * 32) {
+        const int k = base + lane;  // 2 kExitTableN is a multiple of 32
+        const int side = k / kExitTableN, i = k - side * kExitTableN;
+        const float x2 = fmaf(float(i), sv.tab_h[side], sv.tab_lo[side]);
+        const float mag = nm.t_eps * expm1f(fabsf(x2) / nm.t_scale);
+        float sigma = 1.0f;  // the capture flag is trained at sigma = 1
+        if (side == 1) sigma = orbit::sigma_exit<float>(nm.ue, orbit::roots<float, 4>(fmaxf(mag, 1e-7f)));
+        qs[warp][lane] = make_float4(sv.x1, x2, sigma, 0.f);
+        __syncwarp();
+        mlp_eval_tiles<true>(N, qs[warp], os[warp], 2);
+        table[k] = os[warp][lane];
+        __syncwarp();
+    }
+}
+
+// The exit query's network output from the view's table: Catmull-Rom in x2 on the ray's half.
+__device__ __forceinline__ float2 exit_from_table(const SurrView& sv, float x2, bool cap) {
+    const int side = cap ? 0 : 1;
+    const float2* T = sv.exit_table + side * kExitTableN;
+    const float u = (x2 - sv.tab_lo[side]) * sv.tab_inv_h[side];
+    const int i = min(max(int(floorf(u)), 1), kExitTableN - 3);
+    const float t = u - float(i);
+    const float2 p0 = __ldg(T + i - 1), p1 = __ldg(T + i), p2 = __ldg(T + i + 1), p3 = __ldg(T + i + 2);
+    auto cr = [t](float a, float b, float c, float d) {
+        return b + 0.5f * t * ((c - a) + t * ((2.f * a - 5.f * b + 4.f * c - d) + t * (3.f * (b - c) + d - a)));
+    };
+    return make_float2(cr(p0.x, p1.x, p2.x, p3.x), cr(p0.y, p1.y, p2.y, p3.y));
+}
+
 __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
                                                                 const float* __restrict__ P, WorkQueue* q,
                                                                 int* __restrict__ fb_list) {
@@ -1052,14 +1093,14 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                 const float bl = orbit::base_blend<float>(beta);
                 Ic = orbit::base_sweep<float>(uc, Rt, bl);
                 phi0 = Ic + orbit::base_sweep<float>(nm.ue, Rt, bl);
-                qb[lane] = make_float4(x1, x2, orbit::sigma_exit<float>(nm.ue, Rt), 0.f);
                 s0 = Rt.u1, s1 = Rt.u2, s2 = Rt.u3, s3 = Rt.d32;
             } else {
                 const CapStage cs = cap_stage(beta, uc, R.capture_r, R.disk_inner, R.disk_outer, sur && thin);
-                qb[lane] = make_float4(x1, x2, 1.0f, 0.f);  // the capture flag is trained at sigma = 1
                 Ic = cs.Ic, phi0 = cs.phi0, Ilo = cs.Ilo, Ihi = cs.Ihi;
                 s0 = cs.u1, s1 = cs.A, s2 = cs.k2, s3 = cs.K;
             }
+            // the exit query (x1, x2, sigma at the exit; sigma = 1 for the capture flag) from the table
+            ob[lane] = sur ? exit_from_table(sv, x2, cap) : make_float2(0.f, 0.f);
             // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
             float phin = atan2f(-e1.y, e2.y);
             if (phin < 0.f) phin += kPi;
@@ -1149,9 +1190,9 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             tu[t] = u;
         }
         __syncwarp();
-        // ---- phase 3: the network on all queries of the warp
-        const int ntiles = (32 + total + 15) >> 4;
-        mlp_eval_tiles<true>(S.N, qb, ob, ntiles);
+        // ---- phase 3: the network on the warp's crossing queries (the exit queries came from the table)
+        const int ntiles = (total + 15) >> 4;
+        if (ntiles > 0) mlp_eval_tiles<true>(S.N, qb + 32, ob + 32, ntiles);
         n_rows += lane == 0 ? uint32_t(16 * ntiles) : 0u;
         // ---- phase 4: corrected crossings (per candidate), then records (per ray)
 #pragma unroll 1
@@ -1189,7 +1230,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             bool sur = (info & 4u) != 0;
             const bool cap = (info & kCapBit) != 0;
             const float2 oe = ob[lane];
-            n_q += sur ? 1u + (cap ? 0u : uint32_t(ncand)) : 0u;
+            n_q += sur && !cap ? uint32_t(ncand) : 0u;
             if (sur && (oe.y > 0.f) != cap) {  // the learned capture flag disagrees with b vs sqrt(27): integrator decides
                 sur = false;
                 ++n_dis;
@@ -1316,6 +1357,11 @@ cudaError_t launch_train_step(const float* params, const TrainSample* X, const i
 cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
                         float beta2, float eps, cudaStream_t st) {
     k_adam<<<(kNParams + 255) / 256, 256, 0, st>>>(params, grads, m, v, step, lr, beta1, beta2, eps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_exit_table(const SurrView& sv, const float* params, float2* table, cudaStream_t st) {
+    k_exit_table<<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);
     return cudaGetLastError();
 }
 

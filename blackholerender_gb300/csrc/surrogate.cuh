@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 
 #include "kernels.cuh"
@@ -53,12 +54,20 @@ cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, i
 cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int* status, int grid,
                              cudaStream_t st, long long wait_cycles = 0, bool withhold = false);
 
+// The exit query of a ray, (x1, x2, sigma at the exit) for an escaping orbit and (x1, x2, 1) for a
+// captured one, depends on the view (x1) and on x2 alone: per view it is tabulated on
+// kExitTableN points of x2 for each half (0: captured, beta < 0; 1: escaping) and read back by
+// cubic interpolation.
+constexpr int kExitTableN = 4096;
+
 struct SurrView {
     DevView view;
     Rule rule;
     Norm norm;
     float x1;  // network input 1 of this view (scaled log r_cam)
     float uc;  // 1 / r_cam
+    const float2* exit_table;  // [2][kExitTableN] network outputs (y, capture logit)
+    float tab_lo[2], tab_h[2], tab_inv_h[2];  // x2 of a half's first point, spacing, 1 / spacing
     // double constants of the view for the FP64 impact parameter near the photon sphere
     double inv_w2, inv_h2;  // 2 / width, 2 / height
     double aspect_d;        // width / height
@@ -67,6 +76,22 @@ struct SurrView {
 };
 cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
                                    cudaStream_t st);
+// Fills the view's exit table (2 x kExitTableN rows through the network).
+cudaError_t launch_exit_table(const SurrView& sv, const float* params, float2* table, cudaStream_t st);
+// x2 ranges of the two halves: captured beta in [-1, -band / sqrt 27], escaping in
+// [band / sqrt 27, b_max / sqrt 27 - 1].
+inline void exit_table_range(const Norm& nm, float lo[2], float h[2]) {
+    const double s27 = 5.196152422706632;
+    auto x2 = [&](double beta) {
+        return (beta < 0 ? -1.0 : 1.0) * std::log1p(std::fabs(beta) / double(nm.t_eps)) * double(nm.t_scale);
+    };
+    const double b0 = double(nm.band) / s27;
+    const double ends[2][2] = {{x2(-1.0), x2(-b0)}, {x2(b0), x2(double(nm.b_max) / s27 - 1.0)}};
+    for (int s = 0; s < 2; ++s) {
+        lo[s] = float(ends[s][0]);
+        h[s] = float((ends[s][1] - ends[s][0]) / double(kExitTableN - 1));
+    }
+}
 int train_smem_bytes();
 
 }  // namespace surr

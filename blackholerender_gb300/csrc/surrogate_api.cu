@@ -38,6 +38,8 @@ struct bhr_surrogate {
     int last_nviews = 0;
     int* fb = nullptr;                    // fallback ray list
     int64_t fb_cap = 0;
+    float2* etab[2] = {nullptr, nullptr}; // per pipeline lane: the views' exit tables, [view][2][kExitTableN]
+    int64_t etab_cap[2] = {0, 0};
     unsigned long long last[4] = {0, 0, 0, 0};
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
@@ -172,7 +174,8 @@ int bhr_surrogate_destroy(bhr_surrogate* s) {
     if (!s) return BHR_OK;
     DevGuard dg(s->device);
     for (void* p : {(void*)s->params, (void*)s->grads, (void*)s->adam_m, (void*)s->adam_v, (void*)s->X,
-                    (void*)s->lab, (void*)s->stats, (void*)s->loss, (void*)s->q, (void*)s->fb, (void*)s->staging})
+                    (void*)s->lab, (void*)s->stats, (void*)s->loss, (void*)s->q, (void*)s->fb, (void*)s->staging,
+                    (void*)s->etab[0], (void*)s->etab[1]})
         if (p) cudaFree(p);
     for (cudaEvent_t& e : s->ev)
         if (e) cudaEventDestroy(e);
@@ -440,6 +443,8 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     for (int k = 0; k < nviews; ++k) off[size_t(k) + 1] = off[size_t(k)] + int64_t(views[k].width) * views[k].height;
     cudaError_t e = grow(&s->fb, &s->fb_cap, off[size_t(nviews)]);
     if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
+    constexpr int64_t kTab = 2 * bhr::surr::kExitTableN;  // table entries per view
+    if (e == cudaSuccess) e = grow(&s->etab[lane], &s->etab_cap[lane], kTab * std::max<int64_t>(nviews, 64));
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
     e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
@@ -458,6 +463,9 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         sv.x1 = float((std::log(double(sv.view.rcam)) - std::log(double(s->norm.rc_lo))) /
                           (std::log(double(s->norm.rc_hi)) - std::log(double(s->norm.rc_lo))) * 2.0 - 1.0);
         sv.uc = 1.0f / sv.view.rcam;
+        sv.exit_table = s->etab[lane] + kTab * k;
+        bhr::surr::exit_table_range(s->norm, sv.tab_lo, sv.tab_h);
+        for (int h = 0; h < 2; ++h) sv.tab_inv_h[h] = 1.0f / sv.tab_h[h];
         {
             const double cx = views[k].cam_pos[0], cy = views[k].cam_pos[1], cz = views[k].cam_pos[2];
             const double rc = std::sqrt(cx * cx + cy * cy + cz * cz);
@@ -472,8 +480,11 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
-        e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3,
-                                              s->side[lane][k & 1]);
+        // the view's exit table, then its pass, on the same side stream
+        e = bhr::surr::launch_exit_table(sv, s->params, s->etab[lane] + kTab * k, s->side[lane][k & 1]);
+        if (e == cudaSuccess)
+            e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3,
+                                                  s->side[lane][k & 1]);
     }
     for (int j = 0; e == cudaSuccess && j < 2; ++j) {
         e = cudaEventRecord(s->join[lane][j], s->side[lane][j]);
@@ -684,6 +695,9 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
         out[5] += q[2 * v].mlp_rows;
     }
     out[3] += q[2 * size_t(s->last_nviews)].steps;
+    // the exit tables' rows (2 kExitTableN per view, in full 16-row tiles)
+    out[4] += uint64_t(2 * bhr::surr::kExitTableN) * uint64_t(s->last_nviews);
+    out[5] += uint64_t(2 * bhr::surr::kExitTableN) * uint64_t(s->last_nviews);
     return BHR_OK;
 }
 
