@@ -986,7 +986,7 @@ __device__ __noinline__ float cap_invert(float u1, float A, float k2, float K, f
 // beta it encodes (the inverse of the x2 transform), the exit query the pass would make for that
 // beta, and the network's output through the same folded-x1 forward pass as k_surrogate.
 __global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ SurrView sv, const float* __restrict__ P,
-                                                    float2* __restrict__ table) {
+                                                    float4* __restrict__ table) {
     __shared__ __align__(16) SmemNet N;
     __shared__ float4 qs[8][32];
     __shared__ float2 os[8][32];
@@ -1004,23 +1004,25 @@ __global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ Surr
         qs[warp][lane] = make_float4(sv.x1, x2, sigma, 0.f);
         __syncwarp();
         mlp_eval_tiles<true>(N, qs[warp], os[warp], 2);
-        table[k] = os[warp][lane];
+        // point i is the first pair of entry i and the second of entry i - 1 (the last entry
+        // repeats its point)
+        float2* half = reinterpret_cast<float2*>(table);
+        const float2 o = os[warp][lane];
+        half[2 * k] = o;
+        if (i > 0) half[2 * k - 1] = o;
+        if (i == kExitTableN - 1) half[2 * k + 1] = o;
         __syncwarp();
     }
 }
 
-// The exit query's network output from the view's table: Catmull-Rom in x2 on the ray's half.
+// The exit query's network output from the view's table: linear in x2 on the ray's half.
 __device__ __forceinline__ float2 exit_from_table(const SurrView& sv, float x2, bool cap) {
     const int side = cap ? 0 : 1;
-    const float2* T = sv.exit_table + side * kExitTableN;
     const float u = (x2 - sv.tab_lo[side]) * sv.tab_inv_h[side];
-    const int i = min(max(int(floorf(u)), 1), kExitTableN - 3);
+    const int i = min(max(int(floorf(u)), 0), kExitTableN - 2);
     const float t = u - float(i);
-    const float2 p0 = __ldg(T + i - 1), p1 = __ldg(T + i), p2 = __ldg(T + i + 1), p3 = __ldg(T + i + 2);
-    auto cr = [t](float a, float b, float c, float d) {
-        return b + 0.5f * t * ((c - a) + t * ((2.f * a - 5.f * b + 4.f * c - d) + t * (3.f * (b - c) + d - a)));
-    };
-    return make_float2(cr(p0.x, p1.x, p2.x, p3.x), cr(p0.y, p1.y, p2.y, p3.y));
+    const float4 e = __ldg(sv.exit_table + side * kExitTableN + i);
+    return make_float2(fmaf(t, e.z - e.x, e.x), fmaf(t, e.w - e.y, e.y));
 }
 
 __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
@@ -1360,8 +1362,8 @@ cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_exit_table(const SurrView& sv, const float* params, float2* table, cudaStream_t st) {
-    k_exit_table<<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);
+cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, cudaStream_t st) {
+    k_exit_table<<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);  // one point per thread
     return cudaGetLastError();
 }
 

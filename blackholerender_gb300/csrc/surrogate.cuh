@@ -57,8 +57,8 @@ cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, 
 // The exit query of a ray, (x1, x2, sigma at the exit) for an escaping orbit and (x1, x2, 1) for a
 // captured one, depends on the view (x1) and on x2 alone: per view it is tabulated on
 // kExitTableN points of x2 for each half (0: captured, beta < 0; 1: escaping) and read back by
-// cubic interpolation.
-constexpr int kExitTableN = 4096;
+// linear interpolation. Entry i of a half holds points i and i + 1 (one 16-byte load).
+constexpr int kExitTableN = 8192;
 
 struct SurrView {
     DevView view;
@@ -66,7 +66,7 @@ struct SurrView {
     Norm norm;
     float x1;  // network input 1 of this view (scaled log r_cam)
     float uc;  // 1 / r_cam
-    const float2* exit_table;  // [2][kExitTableN] network outputs (y, capture logit)
+    const float4* exit_table;  // [2][kExitTableN] (y, logit) of points i and i + 1
     float tab_lo[2], tab_h[2], tab_inv_h[2];  // x2 of a half's first point, spacing, 1 / spacing
     // double constants of the view for the FP64 impact parameter near the photon sphere
     double inv_w2, inv_h2;  // 2 / width, 2 / height
@@ -77,7 +77,7 @@ struct SurrView {
 cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
                                    cudaStream_t st);
 // Fills the view's exit table (2 x kExitTableN rows through the network).
-cudaError_t launch_exit_table(const SurrView& sv, const float* params, float2* table, cudaStream_t st);
+cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, cudaStream_t st);
 // x2 ranges of the two halves: captured beta in [-1, -band / sqrt 27], escaping in
 // [band / sqrt 27, b_max / sqrt 27 - 1].
 inline void exit_table_range(const Norm& nm, float lo[2], float h[2]) {

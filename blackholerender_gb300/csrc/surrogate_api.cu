@@ -38,7 +38,7 @@ struct bhr_surrogate {
     int last_nviews = 0;
     int* fb = nullptr;                    // fallback ray list
     int64_t fb_cap = 0;
-    float2* etab[2] = {nullptr, nullptr}; // per pipeline lane: the views' exit tables, [view][2][kExitTableN]
+    float4* etab[2] = {nullptr, nullptr}; // per pipeline lane: the views' exit tables, [view][2][kExitTableN]
     int64_t etab_cap[2] = {0, 0};
     unsigned long long last[4] = {0, 0, 0, 0};
     cudaStream_t last_stream = nullptr;
