@@ -263,7 +263,7 @@ def run_gpu(args):
 
     def step_surrogate():
         plan_s.launch(stream)
-        return 2 * len(views) + 1  # per view its exit table and its surrogate kernel, + one fallback march
+        return 3 * len(views) + 1  # per view its exit and crossing tables and its pass, + one fallback march
 
     def step_plain():
         plan_p.launch(stream)
@@ -378,10 +378,11 @@ def run_gpu(args):
             "traffic_note": "dram read+write bytes per k_surrogate launch (one view, ncu); algorithmic writes "
                             "are 64 B x 2.07 M rays = 133 MB, the rest of the dirty lines stay in L2",
             "peak_source": peak_src,
-            "kernel": "k_surrogate with its k_exit_table (one of each per view; ms below is the 16-view pass)",
-            "algorithm": f"{F_MLP} BF16 FLOP per network query; {st['mlp_queries']} queries "
-                         f"({st['mlp_queries'] / max(st['surrogate'], 1):.2f} per surrogate ray: the crossing "
-                         f"queries, and 8192 exit-table rows per view)",
+            "kernel": "k_surrogate with its k_exit_table and k_cross_table (one of each per view; ms below is the "
+                      "16-view pass)",
+            "algorithm": f"{F_MLP} BF16 FLOP per network row; {st['mlp_queries']} rows "
+                         f"({st['mlp_queries'] / max(st['surrogate'], 1):.3f} per surrogate ray: the views' exit "
+                         f"and crossing tables, 81920 rows per view, which the rays interpolate)",
             "pass_ms": t_pass, "fallback_ms": t_fb,
             "note": "the pass is issue-bound on the CUDA cores (ray setup, closed-form orbit, activations);"
                     " the tensor pipe is not its limit"}

@@ -867,9 +867,7 @@ struct RayStage {  // per warp, structure of arrays over its 32 rays
 };
 
 struct InferSmem {
-    SmemNet N;
-    float4 q[kInferWarps][kMaxQ];
-    float2 o[kInferWarps][kMaxQ];
+    float2 o[kInferWarps][kMaxQ];  // network outputs: [0, 32) the exit queries, then the crossings
     RayStage st[kInferWarps];
     int task[kInferWarps][32 * kMaxCand];     // owner lane << 2 | candidate
     float tu[kInferWarps][32 * kMaxCand];     // inverted u, then the corrected radius (< 0: outside the disk)
@@ -1015,6 +1013,46 @@ __global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ Surr
     }
 }
 
+// The view's crossing table: the network's y at (x2_i, sigma_j) = (lo + i hx, -1 + j hs), each point
+// written into the (up to four) cells it is a corner of.
+__global__ void __launch_bounds__(256) k_cross_table(const __grid_constant__ SurrView sv, const float* __restrict__ P,
+                                                     float4* __restrict__ cells) {
+    __shared__ __align__(16) SmemNet N;
+    __shared__ float4 qs[8][32];
+    __shared__ float2 os[8][32];
+    load_net_half<true>(N, P, sv.x1);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int W = kCrossNs - 1;  // cells per row
+    const float hs = 2.0f / float(kCrossNs - 1);
+    float* c = reinterpret_cast<float*>(cells);
+    for (int base = (blockIdx.x * 8 + warp) * 32; base < kCrossNx * kCrossNs; base += gridDim.x * 8 * 32) {
+        const int k = base + lane;  // kCrossNx kCrossNs is a multiple of 32
+        const int i = k / kCrossNs, j = k - i * kCrossNs;
+        qs[warp][lane] = make_float4(sv.x1, fmaf(float(i), sv.cx_h, sv.tab_lo[1]), fmaf(float(j), hs, -1.0f), 0.f);
+        __syncwarp();
+        mlp_eval_tiles<true>(N, qs[warp], os[warp], 2);
+        const float y = os[warp][lane].x;
+        if (i < kCrossNx - 1 && j < W) c[4 * (i * W + j) + 0] = y;
+        if (i < kCrossNx - 1 && j > 0) c[4 * (i * W + j - 1) + 1] = y;
+        if (i > 0 && j < W) c[4 * ((i - 1) * W + j) + 2] = y;
+        if (i > 0 && j > 0) c[4 * ((i - 1) * W + j - 1) + 3] = y;
+        __syncwarp();
+    }
+}
+
+// The crossing query's y from the view's table: bilinear in (x2, sigma).
+__device__ __forceinline__ float cross_from_table(const SurrView& sv, float x2, float sigma) {
+    constexpr int W = kCrossNs - 1;
+    const float u = (x2 - sv.tab_lo[1]) * sv.cx_inv_h;
+    const float v = (sigma + 1.0f) * (0.5f * float(kCrossNs - 1));
+    const int i = min(max(int(floorf(u)), 0), kCrossNx - 2), j = min(max(int(floorf(v)), 0), kCrossNs - 2);
+    const float a = u - float(i), b = v - float(j);
+    const float4 q = __ldg(sv.cross_table + i * W + j);
+    const float lo = fmaf(b, q.y - q.x, q.x), hi = fmaf(b, q.w - q.z, q.z);
+    return fmaf(a, hi - lo, lo);
+}
+
 // The exit query's network output from the view's table: linear in x2 on the ray's half.
 __device__ __forceinline__ float2 exit_from_table(const SurrView& sv, float x2, bool cap) {
     const int side = cap ? 0 : 1;
@@ -1030,13 +1068,11 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                                                                 int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
-    load_net_half<true>(S.N, P, sv.x1);
-    __syncthreads();
+    (void)P;  // the network is read through the view's tables
     const DevView& w = sv.view;
     const Rule& R = sv.rule;
     const Norm& nm = sv.norm;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float4* qb = S.q[warp];
     float2* ob = S.o[warp];
     RayStage& G = S.st[warp];
     int* task = S.task[warp];
@@ -1044,7 +1080,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
     float* tphi = S.tphi[warp];
     constexpr float kPi = 3.14159265358979f;
     const float beta_band = nm.band / kSqrt27f;
-    const float uc = sv.uc, x1 = sv.x1;
+    const float uc = sv.uc;
     const bool thin = R.disk_mode == BHR_DISK_THIN;
     uint32_t n_surr = 0, n_dis = 0, n_q = 0, n_rows = 0;
     for (;;) {
@@ -1188,14 +1224,12 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                 u = cap_invert(G.u1[own], G.u2[own], G.u3[own], G.d32[own], G.b[own], Ic, phk, uc, R.capture_r,
                                R.disk_inner, R.disk_outer);
             }
-            qb[32 + t] = make_float4(x1, G.x2[own], sg, 0.f);  // captured: a row nobody reads
+            // the crossing query (x1, x2, sigma) of an escaping orbit from the view's table
+            ob[32 + t] = make_float2((info & kCapBit) ? 0.f : cross_from_table(sv, G.x2[own], sg), 0.f);
             tu[t] = u;
         }
         __syncwarp();
-        // ---- phase 3: the network on the warp's crossing queries (the exit queries came from the table)
-        const int ntiles = (total + 15) >> 4;
-        if (ntiles > 0) mlp_eval_tiles<true>(S.N, qb + 32, ob + 32, ntiles);
-        n_rows += lane == 0 ? uint32_t(16 * ntiles) : 0u;
+        // ---- (phase 3, the network, now runs in the views' tables)
         // ---- phase 4: corrected crossings (per candidate), then records (per ray)
 #pragma unroll 1
         for (int t = lane; t < total; t += 32) {
@@ -1232,7 +1266,6 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             bool sur = (info & 4u) != 0;
             const bool cap = (info & kCapBit) != 0;
             const float2 oe = ob[lane];
-            n_q += sur && !cap ? uint32_t(ncand) : 0u;
             if (sur && (oe.y > 0.f) != cap) {  // the learned capture flag disagrees with b vs sqrt(27): integrator decides
                 sur = false;
                 ++n_dis;
@@ -1359,6 +1392,11 @@ cudaError_t launch_train_step(const float* params, const TrainSample* X, const i
 cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
                         float beta2, float eps, cudaStream_t st) {
     k_adam<<<(kNParams + 255) / 256, 256, 0, st>>>(params, grads, m, v, step, lr, beta1, beta2, eps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cross_table(const SurrView& sv, const float* params, float4* cells, cudaStream_t st) {
+    k_cross_table<<<kCrossNx * kCrossNs / 256, 256, 0, st>>>(sv, params, cells);  // one point per thread
     return cudaGetLastError();
 }
 

@@ -59,6 +59,11 @@ cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, 
 // kExitTableN points of x2 for each half (0: captured, beta < 0; 1: escaping) and read back by
 // linear interpolation. Entry i of a half holds points i and i + 1 (one 16-byte load).
 constexpr int kExitTableN = 8192;
+// The crossing query of an escaping orbit, (x1, x2, sigma_k), is a function of (x2, sigma) per
+// view: tabulated on kCrossNx points of x2 (the escaping half's range) by kCrossNs of sigma in
+// [-1, 1], read by bilinear interpolation. Cell (i, j) holds its four corners (one 16-byte load).
+constexpr int kCrossNx = 512, kCrossNs = 128;
+constexpr int kCrossCells = (kCrossNx - 1) * (kCrossNs - 1);
 
 struct SurrView {
     DevView view;
@@ -68,6 +73,8 @@ struct SurrView {
     float uc;  // 1 / r_cam
     const float4* exit_table;  // [2][kExitTableN] (y, logit) of points i and i + 1
     float tab_lo[2], tab_h[2], tab_inv_h[2];  // x2 of a half's first point, spacing, 1 / spacing
+    const float4* cross_table;  // [kCrossCells] y at the cell's corners (i, j), (i, j+1), (i+1, j), (i+1, j+1)
+    float cx_h, cx_inv_h;       // the cross table's x2 spacing (first point tab_lo[1]) and its inverse
     // double constants of the view for the FP64 impact parameter near the photon sphere
     double inv_w2, inv_h2;  // 2 / width, 2 / height
     double aspect_d;        // width / height
@@ -78,6 +85,8 @@ cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, Work
                                    cudaStream_t st);
 // Fills the view's exit table (2 x kExitTableN rows through the network).
 cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, cudaStream_t st);
+// Fills the view's crossing table (kCrossNx x kCrossNs rows through the network).
+cudaError_t launch_cross_table(const SurrView& sv, const float* params, float4* cells, cudaStream_t st);
 // x2 ranges of the two halves: captured beta in [-1, -band / sqrt 27], escaping in
 // [band / sqrt 27, b_max / sqrt 27 - 1].
 inline void exit_table_range(const Norm& nm, float lo[2], float h[2]) {

@@ -40,6 +40,8 @@ struct bhr_surrogate {
     int64_t fb_cap = 0;
     float4* etab[2] = {nullptr, nullptr}; // per pipeline lane: the views' exit tables, [view][2][kExitTableN]
     int64_t etab_cap[2] = {0, 0};
+    float4* ctab[2] = {nullptr, nullptr}; // per pipeline lane: the views' crossing tables, [view][kCrossCells]
+    int64_t ctab_cap[2] = {0, 0};
     unsigned long long last[4] = {0, 0, 0, 0};
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
@@ -175,7 +177,7 @@ int bhr_surrogate_destroy(bhr_surrogate* s) {
     DevGuard dg(s->device);
     for (void* p : {(void*)s->params, (void*)s->grads, (void*)s->adam_m, (void*)s->adam_v, (void*)s->X,
                     (void*)s->lab, (void*)s->stats, (void*)s->loss, (void*)s->q, (void*)s->fb, (void*)s->staging,
-                    (void*)s->etab[0], (void*)s->etab[1]})
+                    (void*)s->etab[0], (void*)s->etab[1], (void*)s->ctab[0], (void*)s->ctab[1]})
         if (p) cudaFree(p);
     for (cudaEvent_t& e : s->ev)
         if (e) cudaEventDestroy(e);
@@ -343,7 +345,7 @@ int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out
     if (e == cudaSuccess) e = cudaMalloc(&status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(status, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(q, hq.data(), sizeof(float4) * size_t(n), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = bhr::surr::launch_mlp_infer(s->params, q, o, n, status, s->sms * 4, nullptr);
+    if (e == cudaSuccess) e = bhr::surr::launch_mlp_infer(s->params, q, o, n, status, s->sms * 3, nullptr);
     if (e == cudaSuccess) e = cudaMemcpy(out, o, sizeof(float2) * size_t(n), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost);
     if (q) cudaFree(q);
@@ -445,6 +447,8 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
     constexpr int64_t kTab = 2 * bhr::surr::kExitTableN;  // table entries per view
     if (e == cudaSuccess) e = grow(&s->etab[lane], &s->etab_cap[lane], kTab * std::max<int64_t>(nviews, 64));
+    constexpr int64_t kCells = bhr::surr::kCrossCells;
+    if (e == cudaSuccess) e = grow(&s->ctab[lane], &s->ctab_cap[lane], kCells * std::max<int64_t>(nviews, 16));
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
     e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
@@ -466,6 +470,9 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         sv.exit_table = s->etab[lane] + kTab * k;
         bhr::surr::exit_table_range(s->norm, sv.tab_lo, sv.tab_h);
         for (int h = 0; h < 2; ++h) sv.tab_inv_h[h] = 1.0f / sv.tab_h[h];
+        sv.cross_table = s->ctab[lane] + kCells * k;
+        sv.cx_h = sv.tab_h[1] * float(bhr::surr::kExitTableN - 1) / float(bhr::surr::kCrossNx - 1);
+        sv.cx_inv_h = 1.0f / sv.cx_h;
         {
             const double cx = views[k].cam_pos[0], cy = views[k].cam_pos[1], cz = views[k].cam_pos[2];
             const double rc = std::sqrt(cx * cx + cy * cy + cz * cz);
@@ -482,6 +489,8 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
         // the view's exit table, then its pass, on the same side stream
         e = bhr::surr::launch_exit_table(sv, s->params, s->etab[lane] + kTab * k, s->side[lane][k & 1]);
+        if (e == cudaSuccess)
+            e = bhr::surr::launch_cross_table(sv, s->params, s->ctab[lane] + kCells * k, s->side[lane][k & 1]);
         if (e == cudaSuccess)
             e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3,
                                                   s->side[lane][k & 1]);
@@ -695,9 +704,10 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
         out[5] += q[2 * v].mlp_rows;
     }
     out[3] += q[2 * size_t(s->last_nviews)].steps;
-    // the exit tables' rows (2 kExitTableN per view, in full 16-row tiles)
-    out[4] += uint64_t(2 * bhr::surr::kExitTableN) * uint64_t(s->last_nviews);
-    out[5] += uint64_t(2 * bhr::surr::kExitTableN) * uint64_t(s->last_nviews);
+    // the network runs in the views' tables: 2 kExitTableN + kCrossNx kCrossNs rows per view
+    const uint64_t rows = uint64_t(2 * bhr::surr::kExitTableN + bhr::surr::kCrossNx * bhr::surr::kCrossNs);
+    out[4] += rows * uint64_t(s->last_nviews);
+    out[5] += rows * uint64_t(s->last_nviews);
     return BHR_OK;
 }
 

@@ -287,8 +287,8 @@ int bhr_surrogate_plan_destroy(bhr_surrogate_plan* plan);
 int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2);
 /* Of the last bhr_surrogate_trace: rays answered by the surrogate, rays sent to the integrator,
  * capture-flag disagreements (also sent to the integrator), integrator steps of the fallback,
- * network queries (the crossing queries of surrogate rays and the 2 x 4096 rows of each view's
- * exit table), network rows evaluated (16-row tiles, padding included). */
+ * network rows (the views' exit and crossing tables: 2 x 8192 + 512 x 128 rows per view; the rays
+ * read them by interpolation), network rows evaluated (the same, in full 16-row tiles). */
 int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out6);
 
 /* Statistics of the last bhr_trace on ctx (synchronises that call's stream). */

@@ -110,6 +110,45 @@ def test_surrogate_and_plain_vs_converged_orbit(surrogate):
     assert a_s.max() < DIR_MAX_RAD, (np.percentile(a_s, 99), a_s.max())
 
 
+def test_surrogate_crossings_vs_converged_orbit(surrogate):
+    """Disk crossings of surrogate rays against the converged FP64 orbit with the thin disk
+    (step scale 0.002, the slab clamp landing it on the disk plane), where the chord interpolation
+    of the crossing is far below the 450-step rule's ~5e-4: the escaping crossings come from the
+    network's crossing table, the captured ones from the exact elliptic form."""
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG)[:4]
+    outs = surrogate.trace(views)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(31)
+    rel, rel_rule = [], []
+    for v, o in zip(views, outs):
+        g = hits_numpy(o.cpu())
+        has = np.flatnonzero(((g["flags"] & FLAG_SURROGATE) != 0) & (g["ncross"] > 0))
+        idx = rng.choice(has, min(1500, has.size), replace=False)
+        fine = v.copy()
+        fine.step_scale = 0.002
+        fine.ds_floor = 1e-4
+        fine.disk_step = 0.01
+        fine.max_steps = 200000
+        ref = O.trace_pixels(fine, idx, fp64=True)
+        rule = O.trace_pixels(v, idx, fp64=True)
+        gs = g[idx]
+        for k in range(3):
+            m = ((gs["ncross"] > k) & (ref["ncross"] == gs["ncross"]) & (rule["ncross"] == gs["ncross"])
+                 & (np.abs(ref["b"].astype(np.float64) - 27 ** 0.5) > 2e-3))
+            r = ref["cross_r"][m, k].astype(np.float64)
+            edge = (np.abs(r - v.disk_inner) < EDGE_REL * v.disk_inner) | (np.abs(r - v.disk_outer) < EDGE_REL * v.disk_outer)
+            rel.append(np.abs(gs["cross_r"][m, k] - r)[~edge] / r[~edge])
+            rel_rule.append(np.abs(rule["cross_r"][m, k] - r)[~edge] / r[~edge])
+    rel, rel_rule = np.concatenate(rel), np.concatenate(rel_rule)
+    print(f"\ncrossings vs the converged orbit: {rel.size} crossings, surrogate relative radius p50 "
+          f"{np.median(rel):.2e} p99 {np.percentile(rel, 99):.2e} max {rel.max():.2e}; the same-rule FP64 march "
+          f"p99 {np.percentile(rel_rule, 99):.2e} max {rel_rule.max():.2e}")
+    assert rel.size > 2000
+    assert np.percentile(rel, 99) < 2e-4 and np.percentile(rel, 99) < np.percentile(rel_rule, 99)
+
+
 def test_surrogate_near_the_photon_ring(surrogate):
     """Rays just outside the fallback band, |b - sqrt(27)| in [2e-3, 5e-2], where the deflection is
     most sensitive to b and random pixel samples rarely land: every escaped surrogate ray within
