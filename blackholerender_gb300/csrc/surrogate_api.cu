@@ -42,6 +42,7 @@ struct bhr_surrogate {
     int64_t etab_cap[2] = {0, 0};
     float4* ctab[2] = {nullptr, nullptr}; // per pipeline lane: the views' crossing tables, [view][kCrossCells]
     int64_t ctab_cap[2] = {0, 0};
+    uint64_t work_gen = 0;  // bumped whenever a trace reallocates its work memory (plans hold pointers into it)
     unsigned long long last[4] = {0, 0, 0, 0};
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
@@ -443,12 +444,16 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     // per-view fallback lists, one after the other
     std::vector<int64_t> off(size_t(nviews) + 1, 0);
     for (int k = 0; k < nviews; ++k) off[size_t(k) + 1] = off[size_t(k)] + int64_t(views[k].width) * views[k].height;
+    // what plans point into: the fallback list, the work queues and lane 0's tables (plans run on lane 0)
+    auto plan_memory = [&] { return s->fb_cap + s->nq + s->etab_cap[0] + s->ctab_cap[0]; };
+    const int64_t caps_before = plan_memory();
     cudaError_t e = grow(&s->fb, &s->fb_cap, off[size_t(nviews)]);
     if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
     constexpr int64_t kTab = 2 * bhr::surr::kExitTableN;  // table entries per view
     if (e == cudaSuccess) e = grow(&s->etab[lane], &s->etab_cap[lane], kTab * std::max<int64_t>(nviews, 64));
     constexpr int64_t kCells = bhr::surr::kCrossCells;
     if (e == cudaSuccess) e = grow(&s->ctab[lane], &s->ctab_cap[lane], kCells * std::max<int64_t>(nviews, 16));
+    if (plan_memory() != caps_before) ++s->work_gen;
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
     e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
@@ -543,6 +548,7 @@ struct bhr_surrogate_plan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int nviews = 0;
+    uint64_t work_gen = 0;  // the surrogate's work memory generation the graph was captured with
 };
 
 int bhr_surrogate_plan_destroy(bhr_surrogate_plan* p) {
@@ -593,6 +599,7 @@ int bhr_surrogate_plan_create(bhr_surrogate* s, const bhr_view* views, int nview
         e = cudaGraphInstantiate(&p->exec, p->graph, 0);
         if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_create: instantiate");
     }
+    p->work_gen = s->work_gen;
     if (rc != BHR_OK) {
         bhr_surrogate_plan_destroy(p);
         return rc;
@@ -605,6 +612,10 @@ int bhr_surrogate_plan_launch(bhr_surrogate_plan* p, void* stream) {
     if (!p || !p->exec) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_plan_launch: plan is NULL or empty");
     DevGuard dg(p->s->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (p->work_gen != p->s->work_gen)
+        return fail(BHR_ERR_NOT_READY,
+                    "bhr_surrogate_plan_launch: a larger trace reallocated the surrogate's work memory since this plan "
+                    "was made; destroy and recreate the plan");
     const cudaError_t e = cudaGraphLaunch(p->exec, st);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_plan_launch");
     p->s->last_stream = st;

@@ -275,7 +275,9 @@ int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr
 int bhr_surrogate_trace_host(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_host);
 /* The same trace of a fixed batch of views captured once into a CUDA graph and replayed: the 2 x
  * nviews + 1 launches of a trace become one graph launch. The plan uses the surrogate's work
- * memory and outputs: replays and traces on the same surrogate must not overlap on the GPU.
+ * memory and outputs: replays and traces on the same surrogate must not overlap on the GPU, and a
+ * later trace that needs more work memory (more rays or views) reallocates it, after which
+ * bhr_surrogate_plan_launch returns BHR_ERR_NOT_READY (recreate the plan).
  * bhr_surrogate_trace_stats covers replays too; bhr_surrogate_trace_times only eager traces.
  * No counterpart in the reference. */
 typedef struct bhr_surrogate_plan bhr_surrogate_plan;

@@ -285,3 +285,32 @@ def test_surrogate_host_buffers_and_uneven_views(surrogate):
         angs.append(O.angle(h["dir"][idx][m], ref["dir"][m]))
     a = np.concatenate(angs)
     assert len(a) > 5000 and np.percentile(a, 99) < DIR_MAX_RAD, np.percentile(a, 99)
+
+
+def test_surrogate_plan_refuses_after_work_memory_grows():
+    """A plan holds pointers into the surrogate's work memory: after a larger trace reallocates it
+    (here 20 views, past the crossing tables' 16-view allocation), the plan's launch is refused
+    with ERR_NOT_READY instead of replaying stale pointers; a recreated plan runs."""
+    import torch
+
+    from blackholerender_gb300 import BhrError, _abi
+
+    s = Surrogate(seed=1)
+    s.load(str(DEFAULT_CHECKPOINT))
+    small = workloads.c2_views(TERM_CONFIG, width=64, height=36)[:1]
+    outs = [torch.zeros(v.rays * 64, dtype=torch.uint8, device="cuda") for v in small]
+    p = s.plan(small, outs)
+    p.launch()
+    torch.cuda.synchronize()
+    s.trace(workloads.c2_views(TERM_CONFIG, width=64, height=36, n=20))
+    torch.cuda.synchronize()
+    with pytest.raises(BhrError) as e:
+        p.launch()
+    assert e.value.code == _abi.ERR_NOT_READY
+    p.close()
+    p = s.plan(small, outs)
+    p.launch()
+    torch.cuda.synchronize()
+    assert np.all((hits_numpy(outs[0].cpu())["flags"] & (FLAG_SURROGATE | FLAG_FALLBACK)) != 0)
+    p.close()
+    s.close()
