@@ -1,6 +1,6 @@
 // Learned orbit surrogate for sm_103a: training data from the FP64 integrator, a fused BF16
-// tensor-core MLP (mma.sync m16n8k16, FP32 accumulation) for training and inference, Adam, and
-// the surrogate trace with its fallback list.
+// tensor-core MLP (mma.sync m16n8k16, FP32 accumulation) for training and for the per-view tables
+// the trace reads, Adam, and the surrogate trace with its fallback list.
 //
 // Network (3 -> 64 -> 64 -> 64 -> 2, SiLU): inputs x1 = scaled log r_cam, x2 = scaled
 // sign(beta) ln(1 + |beta|/eps) with beta = b / sqrt(27) - 1, x3 = orbit coordinate sigma
@@ -841,14 +841,15 @@ __global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ 
 
 // ---------------------------------------------------------------------------------------
 // inference: one warp traces 32 rays at a time, in phases that hand state on through shared
-// memory, so that little is live in registers across the network and no lane waits on
-// another lane's crossing loop:
+// memory, so that no lane waits on another lane's crossing loop. The network itself runs in the
+// view's two tables (k_exit_table, k_cross_table, launched before the pass); the rays
+// interpolate them:
 //   1  per ray (lane): setup and routing, orbital plane, roots, closed-form angle at the camera
-//      and at the exit, the exit query, and the disk-plane crossings inside the disk's angle
-//      range on either leg (candidates, found without inverting the orbit)
-//   2  per candidate, spread over the warp's lanes: baseline inversion u(phi), crossing query
-//   3  the network on all of the warp's queries, 16 rows at a time
-//   4  per candidate: corrected crossing radius and azimuth; per ray: capture-flag check,
+//      and at the exit, the exit query from the exit table, and the disk-plane crossings inside
+//      the disk's angle range on either leg (candidates, found without inverting the orbit)
+//   2  per candidate, spread over the warp's lanes: baseline inversion u(phi), the crossing
+//      query from the crossing table
+//   3  per candidate: corrected crossing radius and azimuth; per ray: capture-flag check,
 //      exit direction and the record
 
 constexpr int kInferWarps = 8;
@@ -1229,8 +1230,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             tu[t] = u;
         }
         __syncwarp();
-        // ---- (phase 3, the network, now runs in the views' tables)
-        // ---- phase 4: corrected crossings (per candidate), then records (per ray)
+        // ---- phase 3: corrected crossings (per candidate), then records (per ray)
 #pragma unroll 1
         for (int t = lane; t < total; t += 32) {
             const int own = task[t] >> 2, c = task[t] & 3;
