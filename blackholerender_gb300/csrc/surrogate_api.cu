@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -445,15 +446,19 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     std::vector<int64_t> off(size_t(nviews) + 1, 0);
     for (int k = 0; k < nviews; ++k) off[size_t(k) + 1] = off[size_t(k)] + int64_t(views[k].width) * views[k].height;
     // what plans point into: the fallback list, the work queues and lane 0's tables (plans run on lane 0)
-    auto plan_memory = [&] { return s->fb_cap + s->nq + s->etab_cap[0] + s->ctab_cap[0]; };
-    const int64_t caps_before = plan_memory();
+    auto plan_memory = [&] {
+        return std::array<uintptr_t, 8>{uintptr_t(s->fb),      uintptr_t(s->fb_cap),      uintptr_t(s->q),
+                                        uintptr_t(s->nq),      uintptr_t(s->etab[0]),     uintptr_t(s->etab_cap[0]),
+                                        uintptr_t(s->ctab[0]), uintptr_t(s->ctab_cap[0])};
+    };
+    const auto before = plan_memory();
     cudaError_t e = grow(&s->fb, &s->fb_cap, off[size_t(nviews)]);
     if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
     constexpr int64_t kTab = 2 * bhr::surr::kExitTableN;  // table entries per view
     if (e == cudaSuccess) e = grow(&s->etab[lane], &s->etab_cap[lane], kTab * std::max<int64_t>(nviews, 64));
     constexpr int64_t kCells = bhr::surr::kCrossCells;
     if (e == cudaSuccess) e = grow(&s->ctab[lane], &s->ctab_cap[lane], kCells * std::max<int64_t>(nviews, 16));
-    if (plan_memory() != caps_before) ++s->work_gen;
+    if (plan_memory() != before) ++s->work_gen;
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
     e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
