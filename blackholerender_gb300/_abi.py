@@ -273,6 +273,7 @@ SIGNATURES.update({
     "bhr_surrogate_trace_times": (ctypes.c_int, [_P, _F]),
     "bhr_surrogate_plan_create": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "bhr_surrogate_plan_launch": (ctypes.c_int, [_P, _P]),
+    "bhr_surrogate_plan_update": (ctypes.c_int, [_P, _VP, ctypes.c_int]),
     "bhr_surrogate_plan_destroy": (ctypes.c_int, [_P]),
 })
 

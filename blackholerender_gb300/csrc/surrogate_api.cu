@@ -554,6 +554,8 @@ struct bhr_surrogate_plan {
     cudaGraphExec_t exec = nullptr;
     int nviews = 0;
     uint64_t work_gen = 0;  // the surrogate's work memory generation the graph was captured with
+    std::vector<bhr_view> views;  // the views and outputs of the captured trace
+    std::vector<bhr_hit*> outs;
 };
 
 int bhr_surrogate_plan_destroy(bhr_surrogate_plan* p) {
@@ -605,12 +607,61 @@ int bhr_surrogate_plan_create(bhr_surrogate* s, const bhr_view* views, int nview
         if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_create: instantiate");
     }
     p->work_gen = s->work_gen;
+    if (rc == BHR_OK) {
+        p->views.assign(views, views + nviews);
+        p->outs.assign(out_dev, out_dev + nviews);
+    }
     if (rc != BHR_OK) {
         bhr_surrogate_plan_destroy(p);
         return rc;
     }
     *out = p;
     return BHR_OK;
+}
+
+int bhr_surrogate_plan_update(bhr_surrogate_plan* p, const bhr_view* views, int nviews) {
+    if (!p || !p->exec) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_plan_update: plan is NULL or empty");
+    if (!views || nviews != p->nviews) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_plan_update: the view count must stay the same");
+    for (int k = 0; k < nviews; ++k)
+        if (views[k].width != p->views[size_t(k)].width || views[k].height != p->views[size_t(k)].height)
+            return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_plan_update: view " + std::to_string(k) +
+                                                 " changes its size; create a new plan");
+    bhr_surrogate* s = p->s;
+    if (p->work_gen != s->work_gen)
+        return fail(BHR_ERR_NOT_READY, "bhr_surrogate_plan_update: the surrogate's work memory was reallocated; "
+                                       "recreate the plan");
+    DevGuard dg(s->device);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_plan_update: begin capture");
+    int rc = surrogate_trace_lane(s, views, nviews, p->outs.data(), p->cap, 0);
+    e = cudaStreamEndCapture(p->cap, &g);
+    if (rc == BHR_OK && e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_update: end capture");
+    if (rc == BHR_OK && s->work_gen != p->work_gen)  // same sizes: nothing may have been reallocated
+        rc = fail(BHR_ERR_NOT_READY, "bhr_surrogate_plan_update: the work memory changed during the update");
+    if (rc == BHR_OK) {
+        cudaGraphExecUpdateResultInfo info{};
+        e = cudaGraphExecUpdate(p->exec, g, &info);
+        if (e != cudaSuccess) {  // a changed topology: instantiate afresh
+            cudaGetLastError();
+            cudaGraphExec_t x = nullptr;
+            e = cudaGraphInstantiate(&x, g, 0);
+            if (e == cudaSuccess) {
+                cudaGraphExecDestroy(p->exec);
+                p->exec = x;
+            } else {
+                rc = cfail(e, "bhr_surrogate_plan_update: instantiate");
+            }
+        }
+    }
+    if (rc == BHR_OK) {
+        if (p->graph) cudaGraphDestroy(p->graph);
+        p->graph = g;
+        p->views.assign(views, views + nviews);
+    } else if (g) {
+        cudaGraphDestroy(g);
+    }
+    return rc;
 }
 
 int bhr_surrogate_plan_launch(bhr_surrogate_plan* p, void* stream) {

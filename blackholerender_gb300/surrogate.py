@@ -190,6 +190,12 @@ class SurrogatePlan:
             stream = torch.cuda.current_stream()
         _abi.check(_abi.lib().bhr_surrogate_plan_launch(self._p, ctypes.c_void_p(stream.cuda_stream)))
 
+    def update(self, views):
+        """New cameras for the plan's views (same count and sizes)."""
+        n = len(views)
+        arr = (_abi.View * n)(*views)
+        _abi.check(_abi.lib().bhr_surrogate_plan_update(self._p, arr, n))
+
     def close(self):
         if self._p:
             _abi.lib().bhr_surrogate_plan_destroy(self._p)

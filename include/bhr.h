@@ -284,6 +284,9 @@ typedef struct bhr_surrogate_plan bhr_surrogate_plan;
 int bhr_surrogate_plan_create(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
                               bhr_surrogate_plan** plan);
 int bhr_surrogate_plan_launch(bhr_surrogate_plan* plan, void* cuda_stream);
+/* New cameras (and any other fields but the sizes) for the plan's views, as bhr_plan_update: the
+ * trace is re-captured with the same outputs and the instantiated graph updated in place. */
+int bhr_surrogate_plan_update(bhr_surrogate_plan* plan, const bhr_view* views, int nviews);
 int bhr_surrogate_plan_destroy(bhr_surrogate_plan* plan);
 /* Device time of the last bhr_surrogate_trace: ms2[0] surrogate pass, ms2[1] fallback march. */
 int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2);

@@ -259,6 +259,33 @@ def test_surrogate_plan_replays_the_trace(surrogate):
     p.close()
 
 
+def test_surrogate_plan_update_moves_the_cameras(surrogate):
+    """bhr_surrogate_plan_update: the plan re-captured for new cameras (same sizes) replays the
+    eager trace of the new views bit for bit; a size change is refused."""
+    import torch
+
+    from blackholerender_gb300 import BhrError
+
+    views = workloads.c2_views(TERM_CONFIG, width=320, height=180)[:4]
+    moved = workloads.c2_views(TERM_CONFIG, width=320, height=180, seed=5)[:4]
+    want = surrogate.trace(moved)
+    torch.cuda.synchronize()
+    want = [o.cpu().numpy() for o in want]
+    outs = [torch.zeros(v.rays * 64, dtype=torch.uint8, device="cuda") for v in views]
+    p = surrogate.plan(views, outs)
+    p.update(moved)
+    for o in outs:
+        o.zero_()
+    p.launch()
+    torch.cuda.synchronize()
+    for a, b in zip(want, outs):
+        assert np.array_equal(a, b.cpu().numpy())
+    bigger = workloads.c2_views(TERM_CONFIG, width=320, height=182)[:4]
+    with pytest.raises(BhrError):
+        p.update(bigger)
+    p.close()
+
+
 def test_surrogate_host_buffers_and_uneven_views(surrogate):
     """The 64 uneven views (sizes, FOVs, camera radii 6.5-200, budgets 200-700) through
     bhr_surrogate_trace_host: equal to the device-buffer trace, classification equal to the FP64
