@@ -45,8 +45,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "BASELINE.json").exists() else \
-    "Mrays/s at 1080p x 450 steps"
+METRIC = "Mrays/s at 1080p×450 steps: surrogate vs plain kernel, GB300, ≤1e-4 rad err"
 UNIT = "Mrays/s"
 F_STEP = 160  # FP32 FLOP per executed march step (FMA = 2)
 F_SETUP = 60  # FP32 FLOP per ray (ray generation, initial velocity, constants)
