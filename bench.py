@@ -9,10 +9,9 @@ outputs are 64-byte hit records (2.1 GB per step, larger than L2, and L2 is also
 between timed steps).
 
   value  Mrays/s of the learned-surrogate path (network + closed-form orbit, with the plain
-         integrator as fallback for near-critical, captured and out-of-range rays), device-timed
+         integrator as fallback for near-critical, outgoing and out-of-range rays), device-timed
          with CUDA events on the launch stream; the plain FP32 integrator on the same 16 views is
-         timed right after it (config.plain_mrays_s) and the two paths' escape directions are
-         compared ray by ray (config.agreement_vs_plain_fp32_rad)
+         timed right after it, into its own records (paths.plain_mrays_s)
   e2e    the same through bhr_surrogate_trace_host: host views in, records in pinned host memory
          out, device->host copies inside the timed region
   roofline  the surrogate pass against the measured HBM bandwidth (its algorithmic work is the 64-B
@@ -21,7 +20,11 @@ between timed steps).
          roofline_plain: the plain march against a measured FP32 peak (160 FLOP per executed step
          + 60 per ray, cuBLAS SGEMM with TF32 off as the FP32 denominator)
   cpu_baseline  the CPU restatement of the same march (oracle/, FP64) on all host cores,
-         on a bounded sample of the same workload
+         over every ray of the step (about 9 s on 16 cores)
+  accuracy  that CPU march then checks both GPU paths' records ray by ray: classification
+         mismatches over the whole step (class_mismatch_full), and, on every ray where the two
+         paths' directions differ by more than 5e-5 rad, both against the converged FP64 orbit
+         (surrogate_worst_vs_converged_rad)
 
 --impl reference times that CPU march alone, on all host threads, as the reference arm.
 Multi-GPU (torchrun): every rank traces its own copy of the 16 views (weak scaling, no
@@ -154,6 +157,102 @@ def cpu_march_sample(views, seconds: float, seed: int = 0, chunk: int = 32768):
             return rays / dt / 1e6, rays, threads, steps / rays
 
 
+SQRT27 = 27.0 ** 0.5
+
+
+def _near_edge(h, r_in: float, r_out: float, rel: float) -> np.ndarray:
+    near = np.zeros(len(h), dtype=bool)
+    for k in range(3):
+        r = h["cross_r"][:, k].astype(np.float64)
+        near |= (k < h["ncross"]) & ((np.abs(r - r_in) < rel * r_in) | (np.abs(r - r_out) < rel * r_out))
+    return near
+
+
+def class_mismatches(gpu, ref, view, band: float, edge_rel: float):
+    """(mismatches, compared): rays whose classification (status, and disk yes/no) differs from
+    the oracle's, among the rays outside the ill-conditioned sets: |b - sqrt 27| < band, the
+    oracle's ray ending within 2 steps of the budget, a crossing within edge_rel of a disk edge."""
+    amb = np.abs(ref["b"].astype(np.float64) - SQRT27) < band
+    amb |= np.abs(ref["steps"].astype(np.int64) - view.max_steps) <= 2
+    amb |= _near_edge(ref, view.disk_inner, view.disk_outer, edge_rel)
+    amb |= _near_edge(gpu, view.disk_inner, view.disk_outer, edge_rel)
+    same = (gpu["status"] == ref["status"]) & ((gpu["ncross"] > 0) == (ref["ncross"] > 0))
+    return int((~amb & ~same).sum()), int((~amb).sum())
+
+
+def _angle(a, b) -> np.ndarray:
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    return np.arctan2(np.linalg.norm(np.cross(a, b), axis=1), np.sum(a * b, axis=1))
+
+
+def cpu_baseline_and_check(views, outs_s, outs_p, disagree_rad: float = 5e-5):
+    """The cpu_baseline leg over the whole step: the FP64 CPU restatement of the march on every
+    ray of the 16 views, on all host threads (timed: the CPU baseline), used afterwards as the
+    checker of both GPU paths' records (the surrogate path's in outs_s, the plain FP32 path's in
+    outs_p): classification of every ray, and the converged FP64 orbit (step scale 0.002, no slab
+    clamp) on every ray where the two GPU paths' escape directions differ by more than
+    disagree_rad. Returns (cpu_baseline, accuracy)."""
+    from blackholerender_gb300 import FLAG_SURROGATE, HIT_DTYPE, hits_numpy
+
+    L = _oracle()
+    threads = os.cpu_count() or 1
+    t_cpu, t_conv, rays, steps = 0.0, 0.0, 0, 0
+    acc = {"class_mismatch_full": 0, "class_mismatch_full_plain": 0, "rays_compared": 0, "rays_compared_plain": 0,
+           "disagreeing_rays": 0, "converged_checked": 0, "surrogate_worst_vs_converged_rad": 0.0,
+           "plain_worst_vs_converged_rad": 0.0}
+    agree = []
+    for v, so, po in zip(views, outs_s, outs_p):
+        ref = np.zeros(v.rays, dtype=HIT_DTYPE)
+        t0 = time.perf_counter()
+        rc = L.oracle_trace_view(ctypes.byref(v), ctypes.c_void_p(ref.ctypes.data), threads, 1)
+        t_cpu += time.perf_counter() - t0
+        assert rc == 0
+        rays += v.rays
+        steps += int(ref["steps"].astype(np.int64).sum())
+        gs = hits_numpy(so.cpu())
+        gp = hits_numpy(po.cpu())
+        m, n = class_mismatches(gs, ref, v, 2e-3, 1e-3)
+        acc["class_mismatch_full"] += m
+        acc["rays_compared"] += n
+        m, n = class_mismatches(gp, ref, v, 1e-2, 1e-4)
+        acc["class_mismatch_full_plain"] += m
+        acc["rays_compared_plain"] += n
+        both = np.nonzero(((gs["flags"] & FLAG_SURROGATE) != 0) & (gs["status"] == 1) & (gp["status"] == 1))[0]
+        a = _angle(gs["dir"][both], gp["dir"][both])
+        agree.append(a)
+        idx = np.ascontiguousarray(both[a > disagree_rad], dtype=np.int64)
+        acc["disagreeing_rays"] += len(idx)
+        if len(idx):
+            fine = v.copy()
+            fine.step_scale, fine.ds_floor, fine.max_steps, fine.disk_mode = 0.002, 1e-4, 200000, 0
+            conv = np.zeros(len(idx), dtype=HIT_DTYPE)
+            t0 = time.perf_counter()
+            rc = L.oracle_trace_pixels(ctypes.byref(fine), ctypes.c_void_p(idx.ctypes.data), ctypes.c_int64(len(idx)),
+                                       ctypes.c_void_p(conv.ctypes.data), threads, 1)
+            t_conv += time.perf_counter() - t0
+            assert rc == 0
+            ok = conv["status"] == 1
+            acc["converged_checked"] += int(ok.sum())
+            es = _angle(gs["dir"][idx][ok], conv["dir"][ok])
+            ep = _angle(gp["dir"][idx][ok], conv["dir"][ok])
+            acc["surrogate_worst_vs_converged_rad"] = max(acc["surrogate_worst_vs_converged_rad"],
+                                                          float(es.max(initial=0.0)))
+            acc["plain_worst_vs_converged_rad"] = max(acc["plain_worst_vs_converged_rad"], float(ep.max(initial=0.0)))
+    agree = np.concatenate(agree)
+    acc["agreement_vs_plain_fp32_rad"] = {"p50": float(np.percentile(agree, 50)), "p99": float(np.percentile(agree, 99)),
+                                          "max": float(agree.max()), "rays": int(len(agree))}
+    acc["converged_s"] = t_conv
+    acc["note"] = ("every ray of the step against the FP64 oracle of the same rule: classification outside the "
+                   "photon-sphere band (2e-3 surrogate path, 1e-2 plain), the budget's last 2 steps and disk-edge "
+                   "crossings; on the rays where the two GPU paths differ by more than 5e-5 rad, both against the "
+                   "converged FP64 orbit (step scale 0.002)")
+    cpu = {"value": rays / t_cpu / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"every ray of the step ({rays} rays, {t_cpu:.1f} s), FP64 CPU restatement of the march, "
+                     f"{steps / rays:.1f} steps/ray, {cpu_model()}"}
+    return cpu, acc
+
+
 def cpu_model() -> str:
     try:
         for ln in Path("/proc/cpuinfo").read_text().splitlines():
@@ -164,14 +263,38 @@ def cpu_model() -> str:
     return "unknown"
 
 
+def oracle_c2_views(term_mode: int):
+    """The 16 poses' views built by the oracle (no product library mapped); byte-equal to the
+    library's views (tests/test_cpu_host.py)."""
+    from blackholerender_gb300 import View, workloads
+
+    L = _oracle()
+    L.oracle_orbit_view.argtypes = [ctypes.POINTER(View), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_float, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    out = []
+    for r, inc, az in workloads.c2_poses():
+        v = View()
+        assert L.oracle_orbit_view(ctypes.byref(v), term_mode, 2, 1920, 1080, 60.0, r, inc, az) == 0
+        out.append(v)
+    return out
+
+
+def step_config(views) -> dict:
+    """The `config` both arms print: the workload of one step."""
+    rays = sum(v.rays for v in views)
+    return {"workload": WORKLOAD if len(views) == 16 else f"first {len(views)} of: {WORKLOAD}",
+            "views": len(views), "rays_per_step": rays,
+            "l2": "inputs are camera views; 2.1 GB of records per step and a 256 MiB L2 flush between timed steps"}
+
+
 # ----------------------------------------------------------------------------- reference arm
 def run_reference(args):
-    from blackholerender_gb300 import TERM_CONFIG, workloads
+    from blackholerender_gb300 import TERM_CONFIG
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    views = workloads.c2_views(TERM_CONFIG)
+    views = oracle_c2_views(TERM_CONFIG)[:args.views]
     per_step_s = 4.0
     for _ in range(args.warmup):
         cpu_march_sample(views, 0.5, seed=99)
@@ -190,8 +313,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "path": "CPU march, oracle/ restatement (reference's CPU integrator "
-                   "rule set; the shader itself cannot run here)", "cpu": cpu_model()},
+        "config": step_config(views),
+        "path": "CPU march, oracle/ restatement of the shader march (FP64; the shader itself cannot run here); "
+                "views built by the oracle, no product library loaded",
+        "cpu": cpu_model(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -224,7 +349,7 @@ def fp32_peak_tflops(dev) -> float:
 def run_gpu(args):
     import torch
 
-    from blackholerender_gb300 import FLAG_SURROGATE, HIT_BYTES, PREC_FP32, TERM_CONFIG, Tracer, hits_numpy, workloads
+    from blackholerender_gb300 import HIT_BYTES, PREC_FP32, TERM_CONFIG, Tracer, workloads
     from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT, Surrogate
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -251,15 +376,16 @@ def run_gpu(args):
         sur.train(200_000, batch=16384, lr_max=2e-3, lr_min=1e-6)
         trained_here = time.perf_counter() - t0
     outs = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+    outs_p = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    # both paths as the library's CUDA-graph plans (one graph launch per step); the plain path
-    # with the launch shape its autotuner picks for these views
+    # both paths as the library's CUDA-graph plans (one graph launch per step), each into its own
+    # records; the plain path with the launch shape its autotuner picks for these views
     sur.trace_ptrs(views, outs, stream)
     torch.cuda.synchronize(dev)
     plan_s = sur.plan(views, outs)
-    plan_p = tr.plan(views, outs, PREC_FP32, autotune=True)
+    plan_p = tr.plan(views, outs_p, PREC_FP32, autotune=True)
     plain_shape = plan_p.launch_shape.as_dict()
 
     def step_surrogate():
@@ -275,23 +401,9 @@ def run_gpu(args):
         step_surrogate()
     torch.cuda.synchronize(dev)
 
-    # agreement of the surrogate path with the plain FP32 integrator on the same rays (no oracle)
-    step_plain()
-    torch.cuda.synchronize(dev)
-    plain_host = [hits_numpy(o.cpu()) for o in outs[:4]]
     step_surrogate()
     torch.cuda.synchronize(dev)
     st = sur.trace_stats()
-    ang = []
-    for o, hp in zip(outs[:4], plain_host):
-        hs = hits_numpy(o.cpu())
-        m = ((hs["flags"] & FLAG_SURROGATE) != 0) & (hp["status"] == 1)
-        a = hs["dir"][m].astype(np.float64)
-        b = hp["dir"][m].astype(np.float64)
-        ang.append(np.arctan2(np.linalg.norm(np.cross(a, b), axis=1), np.sum(a * b, axis=1)))
-    ang = np.concatenate(ang)
-    agreement = {"p50": float(np.percentile(ang, 50)), "p99": float(np.percentile(ang, 99)),
-                 "max": float(ang.max()), "rays": int(len(ang))}
     # phase times of one (eager) surrogate trace (dominant kernel: the surrogate pass)
     sur.trace_ptrs(views, outs, stream)
     t_pass, t_fb = sur.trace_times_ms()
@@ -407,30 +519,24 @@ def run_gpu(args):
                   "algorithm": f"{F_STEP} FLOP per executed step + {F_SETUP} per ray; "
                                f"{steps_plain / rays:.2f} steps/ray"}
 
-    cpu = None
+    cpu, accuracy = None, None
     if not args.no_cpu and world == 1:
-        v_cpu, n_cpu, thr, spr = cpu_march_sample(views, args.cpu_seconds)
-        cpu = {"value": v_cpu, "unit": UNIT, "cores": thr, "kind": "port",
-               "sample": f"{n_cpu} random pixels of the 16 poses ({args.cpu_seconds:.0f} s), FP64 CPU restatement "
-                         f"of the march, {spr:.1f} steps/ray, {cpu_model()}"}
+        cpu, accuracy = cpu_baseline_and_check(views, outs, outs_p)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic",
-        "config": {"workload": WORKLOAD if len(views) == 16 else f"first {len(views)} of: {WORKLOAD}",
-                   "views": len(views), "rays_per_step": rays,
-                   "method": "learned surrogate + plain FP32 integrator fallback",
-                   "plain_mrays_s": plain_value, "plain_ms_per_step": plain_ms,
-                   "plain_launch_shape": plain_shape, "graph_plans": True,
-                   "speedup_vs_plain": value / plain_value,
-                   "surrogate_fraction": st["surrogate"] / rays, "fallback_rays": st["fallback"],
-                   "capture_flag_disagreements": st["capture_disagree"],
-                   "agreement_vs_plain_fp32_rad": agreement,
-                   "checkpoint": "trained in this run" if trained_here else str(DEFAULT_CHECKPOINT.relative_to(ROOT)),
-                   "train_s": trained_here,
-                   "l2": "inputs are camera views; 2.1 GB of records per step and a 256 MiB L2 flush between "
-                         "timed steps", "parallelism": f"replicas x{world}"},
+        "config": step_config(views),
+        "paths": {"method": "learned surrogate + plain FP32 integrator fallback",
+                  "plain_mrays_s": plain_value, "plain_ms_per_step": plain_ms,
+                  "plain_launch_shape": plain_shape, "graph_plans": True,
+                  "speedup_vs_plain": value / plain_value,
+                  "surrogate_fraction": st["surrogate"] / rays, "fallback_rays": st["fallback"],
+                  "capture_flag_disagreements": st["capture_disagree"],
+                  "checkpoint": "trained in this run" if trained_here else str(DEFAULT_CHECKPOINT.relative_to(ROOT)),
+                  "train_s": trained_here, "parallelism": f"replicas x{world}"},
+        "accuracy": accuracy,
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": roof,

@@ -18,7 +18,11 @@
 // Host code must not pass the array's name to a kernel: on the host that name is only a
 // stand-in, not a device address. The first call on each device, with that device current,
 // resolves the address with cudaGetSymbolAddress (which may load the module, so make that
-// first call before any stream capture) and keeps it for later calls.
+// first call before any stream capture) and keeps it for later calls, together with the
+// identity of the device's context (cuCtxGetId). A cudaDeviceReset destroys the context and
+// the array with it; the next call sees a new context identity and resolves the address again,
+// so that call, too, should come before any stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -44,22 +48,44 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocS
 struct DeviceSetup {
     bool ready = false;
     NoAllocScratch* scratch = nullptr;  // device address of g_noalloc_scratch on this device
+    unsigned long long ctx_id = 0;      // the context the address belongs to
     int sms = 0;
 };
 
 std::mutex g_mu;
 DeviceSetup g_dev[kMaxDevices];
 
+// cuCtxGetId from the driver through the runtime (no link against libcuda): the unique identity
+// of the calling thread's current context.
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetId g_ctx_get_id = nullptr;
+
 int fail(int code, const std::string& msg) {
     bhr::set_last_error(msg);
     return code;
 }
 
-// Once per device, with that device current: resolve the scratch address and read the SM count.
+// Once per device (and again after a cudaDeviceReset gave it a new context), with that device
+// current: resolve the scratch address and read the SM count.
 int setup_device(int dev, DeviceSetup* out) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (dev < 0 || dev >= kMaxDevices) return fail(BHR_ERR_INVALID_ARG, "bhr_trace_noalloc: device ordinal out of range");
+    // make the device's primary context current (cudaSetDevice initialises it; no allocation)
+    cudaError_t se = cudaSetDevice(dev);
+    if (se != cudaSuccess) return fail(BHR_ERR_CUDA, std::string("bhr_trace_noalloc: cudaSetDevice: ") + cudaGetErrorString(se));
+    if (!g_ctx_get_id) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult qr{};
+        se = cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &qr);
+        if (se != cudaSuccess || qr != cudaDriverEntryPointSuccess || !fn)
+            return fail(BHR_ERR_CUDA, "bhr_trace_noalloc: the driver has no cuCtxGetId");
+        g_ctx_get_id = reinterpret_cast<CtxGetId>(fn);
+    }
+    unsigned long long ctx_id = 0;
+    if (g_ctx_get_id(nullptr, &ctx_id) != CUDA_SUCCESS)
+        return fail(BHR_ERR_CUDA, "bhr_trace_noalloc: no current context on the device");
     DeviceSetup& d = g_dev[dev];
+    if (d.ready && d.ctx_id != ctx_id) d.ready = false;  // the device was reset: the old address is gone
     if (!d.ready) {
         int major = 0, minor = 0, sms = 0;
         cudaError_t e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -74,6 +100,7 @@ int setup_device(int dev, DeviceSetup* out) {
         if (e != cudaSuccess || p == nullptr)
             return fail(BHR_ERR_CUDA, std::string("bhr_trace_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         d.scratch = static_cast<NoAllocScratch*>(p);
+        d.ctx_id = ctx_id;
         d.sms = sms;
         d.ready = true;
     }

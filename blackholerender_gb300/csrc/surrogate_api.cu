@@ -538,10 +538,18 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     }
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[2], st);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace");
-    s->last_stream = st;
-    s->last_nviews = nviews;
-    s->have_last = true;
-    s->last_from_plan = false;
+    // a trace recorded into a graph (plan creation and update) runs nothing now: its event
+    // records are capture dependencies, not timings, so the last executed trace stays the one
+    // bhr_surrogate_trace_times and bhr_surrogate_trace_stats report
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace: capture status");
+    if (cs == cudaStreamCaptureStatusNone) {
+        s->last_stream = st;
+        s->last_nviews = nviews;
+        s->have_last = true;
+        s->last_from_plan = false;
+    }
     return BHR_OK;
 }
 }  // namespace

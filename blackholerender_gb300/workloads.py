@@ -91,8 +91,9 @@ def c3_view(term_mode: int = TERM_CONFIG, width: int = 3840, height: int = 2160)
                      pose=(20.0, math.radians(88.0), 0.0))
 
 
-def c4_views(term_mode: int = TERM_CONFIG, seed: int = 1, n: int = 64, scale: float = 1.0):
-    """`scale` < 1 shrinks every view's pixel count by that factor (test sizes)."""
+def c4_specs(seed: int = 1, n: int = 64, scale: float = 1.0):
+    """Per view of C4, in draw order: (width, height, fov_deg, preset, (r, inclination, azimuth)).
+    `scale` < 1 shrinks every view's pixel count by that factor (test sizes)."""
     g = MT19937_64(seed)
     lo, hi = math.log(320 * 180), math.log(3840 * 2160)
     out = []
@@ -105,9 +106,14 @@ def c4_views(term_mode: int = TERM_CONFIG, seed: int = 1, n: int = 64, scale: fl
         inc = g.uniform(0.0, math.radians(90.0))
         az = g.uniform(0.0, 2.0 * math.pi)
         budget = (200, 300, 450, 700)[min(3, int(g.uniform(0.0, 4.0)))]
-        out.append(make_view(term_mode, width=w, height=h, fov_deg=fov, preset=PRESET_BY_BUDGET[budget],
-                             pose=(r, inc, az)))
+        out.append((w, h, fov, PRESET_BY_BUDGET[budget], (r, inc, az)))
     return out
+
+
+def c4_views(term_mode: int = TERM_CONFIG, seed: int = 1, n: int = 64, scale: float = 1.0):
+    """`scale` < 1 shrinks every view's pixel count by that factor (test sizes)."""
+    return [make_view(term_mode, width=w, height=h, fov_deg=fov, preset=preset, pose=pose)
+            for w, h, fov, preset, pose in c4_specs(seed, n, scale)]
 
 
 def body_gallery(view: View, n: int = 12, distance: float = 9.0, radius: float = 0.7) -> list[Body]:

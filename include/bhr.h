@@ -225,8 +225,10 @@ int bhr_trace_noalloc(const bhr_view* view, bhr_hit* out_dev, void* cuda_stream)
  * A small MLP (3 -> 64 -> 64 -> 64 -> 2, SiLU; BF16 tensor-core hidden layers with FP32
  * accumulation) corrects a closed-form elliptic-integral skeleton of the orbital-plane orbit
  * u(phi; r_cam, b) and predicts the capture flag; it is trained on orbits the FP64 integrator
- * generates. Rays near b = sqrt(27), captured, outgoing or outside the trained range fall back
- * to the plain integrator. No counterpart in the reference (the reference only integrates). */
+ * generates. Captured orbits are answered too (the network's capture flag, crossings from the
+ * exact one-real-root elliptic form). Rays near b = sqrt(27), outgoing at the camera, outside
+ * the trained range, or whose learned capture flag disagrees with b fall back to the plain
+ * integrator. No counterpart in the reference (the reference only integrates). */
 typedef struct bhr_surrogate bhr_surrogate;
 typedef struct bhr_surrogate_config {
     float rc_lo, rc_hi;    /* trained camera radii (6, 200) */

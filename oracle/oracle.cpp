@@ -368,6 +368,102 @@ int oracle_shade_bodies(const bhr_view* v, const bhr_hit* hits, const bhr_body_h
     return BHR_OK;
 }
 
+// A view of a benchmark configuration built without the product library, so that the CPU arm of
+// the benchmark maps the oracle alone: the uniforms a camera on the sphere of radius r at
+// inclination incl and azimuth azim (looking at the hole, roll 0) gives, with the Settings
+// defaults (src/Settings.h:19-37), a preset (Settings::applyPreset, src/Settings.cpp:12-35,
+// -1 = none), uTanHalfFov (src/Renderer.cpp:246) and the camera basis of lookRotation
+// (src/Camera.cpp:12-23: glm::quat_cast by the largest component, then glm::mat3_cast,
+// Camera.cpp:67). Float arithmetic in the reference's order, so the bytes equal the library's
+// bhr_view_init + bhr_view_apply_preset + bhr_view_set_fov + bhr_view_orbit_pose.
+int oracle_orbit_view(bhr_view* v, int term_mode, int preset, int width, int height, float fov_deg, double r,
+                      double incl, double azim) {
+    if (!v || term_mode < BHR_TERM_SHADER || term_mode > BHR_TERM_CPU || width <= 0 || height <= 0 || !(r > 0.0) ||
+        !(fov_deg > 0.0f) || !(fov_deg < 180.0f) || preset < -1 || preset > 3)
+        return -1;
+    std::memset(v, 0, sizeof *v);
+    v->width = width;
+    v->height = height;
+    v->max_steps = 450;
+    v->step_scale = 0.05f;
+    v->disk_step = 0.18f;
+    v->disk_inner = 6.0f;
+    v->disk_outer = 20.0f;
+    v->disk_thickness = 0.035f;
+    v->disk_mode = BHR_DISK_THIN;
+    v->lensing = 1;
+    v->term_mode = term_mode;
+    v->escape_r = 1000.0f;
+    v->promote_band = 1e-2f;
+    v->promote_r = 2.5f;
+    if (term_mode == BHR_TERM_CPU) {  // trace() defaults (Geodesic.h:107-108,119)
+        v->max_steps = 200000;
+        v->step_scale = 0.005f;
+        v->capture_r = 2.01f;
+        v->esc_tol = 1e-4f;
+        v->r_esc_min = 30.0f;
+        v->ds_floor = 1e-4f;
+        v->disk_mode = BHR_DISK_NONE;
+    } else {  // R_HORIZON + 0.02 (frag:144) or the configurations' 2.0001; ESC_TOL; rEscMin (frag:89)
+        v->capture_r = term_mode == BHR_TERM_SHADER ? 2.0f + 0.02f : 2.0001f;
+        v->esc_tol = 0.01f;
+        v->r_esc_min = std::max(v->disk_outer * 1.25f, 12.0f);
+        v->ds_floor = 0.02f;
+    }
+    static const int kSteps[4] = {200, 300, 450, 700};
+    static const float kScale[4] = {0.10f, 0.07f, 0.05f, 0.035f}, kDisk[4] = {0.35f, 0.30f, 0.18f, 0.10f};
+    if (preset >= 0) {
+        v->max_steps = kSteps[preset];
+        v->step_scale = kScale[preset];
+        v->disk_step = kDisk[preset];
+    }
+    v->tan_half_fov = std::tan(fov_deg * 0.01745329251994329576923690768489f * 0.5f);
+    // lookRotation(pos, 0, up = +Y)
+    const double pos[3] = {r * std::sin(incl) * std::sin(azim), r * std::cos(incl), r * std::sin(incl) * std::cos(azim)};
+    const double len = std::sqrt(pos[0] * pos[0] + pos[1] * pos[1] + pos[2] * pos[2]);
+    float f[3];  // (target - from) / |target - from|: 0.0 - pos keeps the sign of a zero component
+    for (int k = 0; k < 3; ++k) f[k] = float((0.0 - pos[k]) / len);
+    float u[3] = {0.0f, 1.0f, 0.0f};
+    if (std::fabs(f[1]) > 0.999f) {  // dot(f, normalize(up)) with up = +Y
+        u[0] = 0.0f;
+        u[1] = 0.0f;
+        u[2] = -1.0f;
+    }
+    float rt[3] = {f[1] * u[2] - u[1] * f[2], f[2] * u[0] - u[2] * f[0], f[0] * u[1] - u[0] * f[1]};
+    const float rinv = 1.0f / std::sqrt(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2]);
+    for (float& e : rt) e *= rinv;
+    const float up[3] = {rt[1] * f[2] - f[1] * rt[2], rt[2] * f[0] - f[2] * rt[0], rt[0] * f[1] - f[0] * rt[1]};
+    const float m[3][3] = {{rt[0], rt[1], rt[2]}, {up[0], up[1], up[2]}, {-f[0], -f[1], -f[2]}};  // m[col][row]
+    const float t[4] = {m[0][0] + m[1][1] + m[2][2], m[0][0] - m[1][1] - m[2][2], m[1][1] - m[0][0] - m[2][2],
+                        m[2][2] - m[0][0] - m[1][1]};
+    int big = 0;
+    for (int k = 1; k < 4; ++k)
+        if (t[k] > t[big]) big = k;
+    const float bv = std::sqrt(t[big] + 1.0f) * 0.5f, mult = 0.25f / bv;
+    float q[4];  // w, x, y, z
+    if (big == 0) {
+        q[0] = bv; q[1] = (m[1][2] - m[2][1]) * mult; q[2] = (m[2][0] - m[0][2]) * mult; q[3] = (m[0][1] - m[1][0]) * mult;
+    } else if (big == 1) {
+        q[0] = (m[1][2] - m[2][1]) * mult; q[1] = bv; q[2] = (m[0][1] + m[1][0]) * mult; q[3] = (m[2][0] + m[0][2]) * mult;
+    } else if (big == 2) {
+        q[0] = (m[2][0] - m[0][2]) * mult; q[1] = (m[0][1] + m[1][0]) * mult; q[2] = bv; q[3] = (m[1][2] + m[2][1]) * mult;
+    } else {
+        q[0] = (m[0][1] - m[1][0]) * mult; q[1] = (m[2][0] + m[0][2]) * mult; q[2] = (m[1][2] + m[2][1]) * mult; q[3] = bv;
+    }
+    const float qn = 1.0f / std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    for (float& e : q) e *= qn;
+    // glm::mat3_cast(q): columns right, up, back
+    const float qw = q[0], qx = q[1], qy = q[2], qz = q[3];
+    const float xx = qx * qx, yy = qy * qy, zz = qz * qz, xz = qx * qz, xy = qx * qy, yz = qy * qz;
+    const float wx = qw * qx, wy = qw * qy, wz = qw * qz;
+    float* B = v->cam_basis;
+    B[0] = 1.0f - 2.0f * (yy + zz); B[1] = 2.0f * (xy + wz);        B[2] = 2.0f * (xz - wy);
+    B[3] = 2.0f * (xy - wz);        B[4] = 1.0f - 2.0f * (xx + zz); B[5] = 2.0f * (yz + wx);
+    B[6] = 2.0f * (xz + wy);        B[7] = 2.0f * (yz - wx);        B[8] = 1.0f - 2.0f * (xx + yy);
+    for (int k = 0; k < 3; ++k) v->cam_pos[k] = float(pos[k]);
+    return 0;
+}
+
 int oracle_hit_size(void) { return static_cast<int>(sizeof(bhr_hit)); }
 int oracle_view_size(void) { return static_cast<int>(sizeof(bhr_view)); }
 

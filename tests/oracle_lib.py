@@ -70,6 +70,8 @@ def lib():
         L.oracle_to_half.argtypes = [ctypes.c_float]
         L.oracle_to_half.restype = ctypes.c_uint16
         L.oracle_pcg3d.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_orbit_view.argtypes = [ctypes.POINTER(View), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_float, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         assert L.oracle_hit_size() == 64 and L.oracle_view_size() == ctypes.sizeof(View)
         _lib = L
     return _lib
@@ -89,6 +91,14 @@ def ref_lib():
         L.ref_redshift_factor.restype = ctypes.c_double
         _ref = L
     return _ref
+
+
+def orbit_view(term_mode: int, preset: int, width: int, height: int, fov_deg: float, pose) -> View:
+    """The oracle's own view of a camera on a sphere looking at the hole (no product library)."""
+    v = View()
+    r, inc, az = pose
+    assert lib().oracle_orbit_view(ctypes.byref(v), term_mode, preset, width, height, fov_deg, r, inc, az) == 0
+    return v
 
 
 def nthreads() -> int:

@@ -142,6 +142,24 @@ int main() {
     assert np.array_equal(got, ref)
 
 
+def test_oracle_builds_the_same_views_as_the_library():
+    """The CPU arm of the benchmark builds its views with the oracle alone (no product library
+    mapped); those views must be the library's to the byte: C1, the 16 C2 poses under both
+    rules, the 64 C4 views, and an inclination below the lookRotation up-vector fallback."""
+    import oracle_lib as O
+
+    cases = [(_abi.TERM_CONFIG, 0, 256, 144, 60.0, (30.0, math.radians(85.0), 0.0)),
+             (_abi.TERM_SHADER, 3, 640, 360, 40.0, (20.0, math.radians(88.0), 0.0)),
+             (_abi.TERM_CPU, -1, 64, 36, 75.0, (40.0, math.radians(1.0), 0.3))]
+    for term in (_abi.TERM_CONFIG, _abi.TERM_SHADER):
+        cases += [(term, 2, 1920, 1080, 60.0, p) for p in workloads.c2_poses()]
+    cases += [(_abi.TERM_CONFIG, pre, w, h, fov, pose) for w, h, fov, pre, pose in workloads.c4_specs()]
+    for term, pre, w, h, fov, pose in cases:
+        a = O.orbit_view(term, pre, w, h, fov, pose)
+        b = make_view(term, width=w, height=h, fov_deg=fov, preset=None if pre < 0 else pre, pose=pose)
+        assert bytes(a) == bytes(b), (term, pre, w, h, fov, pose)
+
+
 def test_partition_is_balanced_and_complete():
     views = workloads.c4_views(_abi.TERM_CONFIG, scale=0.05)
     for world in (1, 2, 4, 8):

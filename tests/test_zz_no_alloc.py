@@ -1,9 +1,11 @@
 """bhr_trace_noalloc: the mixed-precision trace for callers that cannot allocate device memory
 (render loops that must not stall on cudaMalloc, hosts whose pool owns all device memory, code
 recording a CUDA graph). Its work memory is a static device array, so it is checked here
-through the C ABI against the context-based entry point (bhr_trace, BHR_PREC_MIXED), with the
-tolerances of the other GPU tests, on two calls in a row (the second call reuses the array the
-first one left behind). This file is collected last."""
+through the C ABI against the context-based entry point (bhr_trace, BHR_PREC_MIXED) on two
+calls in a row (the second call reuses the array the first one left behind). Each ray's march
+does not depend on the launch shape or on where the work memory lives, so the records must be
+the same bytes; the parity report is kept to say where they differ if they ever do. This file
+is collected last."""
 import ctypes
 
 import numpy as np
@@ -19,12 +21,11 @@ def _noalloc(view, out_tensor, stream):
 
 
 def _same(a, b):
+    if np.array_equal(a.view(np.uint8), b.view(np.uint8)):
+        return
     rep = parity.compare(a, b, max_steps=10**9, band=0.0, edge_rel=0.0)
-    assert rep.n_compared == rep.n and rep.class_mismatch == 0, rep.as_dict()
-    assert rep.steps_mismatch == 0, rep.as_dict()
-    assert rep.dir_max_scaled <= parity.DIR_MAX_RAD and rep.dir_p99_scaled <= parity.DIR_P99_RAD, rep.as_dict()
-    assert rep.cross_r_rel_p99 <= parity.CROSS_R_REL_P99, rep.as_dict()
-    assert np.array_equal(a["flags"], b["flags"]) and np.array_equal(a["b"], b["b"])
+    differ = int(np.count_nonzero(np.any(a.view(np.uint8).reshape(-1, 64) != b.view(np.uint8).reshape(-1, 64), axis=1)))
+    raise AssertionError(f"{differ} of {len(a)} records differ from bhr_trace's: {rep.as_dict()}")
 
 
 @pytest.mark.gpu
