@@ -90,6 +90,13 @@ class Tracer:
     def __exit__(self, *exc):
         self.close()
 
+    def set_surrogate(self, surrogate) -> None:
+        """Binds a Surrogate (bhr_ctx_set_surrogate; None unbinds) for method=METHOD_SURROGATE.
+        The Tracer does not own it: keep it alive while it is bound."""
+        self._surrogate = surrogate
+        _abi.check(_abi.lib().bhr_ctx_set_surrogate(self._ctx, surrogate.h if surrogate is not None else None),
+                   self._ctx)
+
     def trace_ptrs(self, views: Sequence[View], out_ptrs: Sequence[int], precision: int = PREC_FP32,
                    method: int = METHOD_PLAIN, stream: int = 0) -> None:
         """bhr_trace on raw device pointers (one per view) and a raw cudaStream_t."""

@@ -209,6 +209,7 @@ SIGNATURES = {
     "bhr_view_rays": (ctypes.c_int64, [_VP]),
     "bhr_trace": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, _P]),
     "bhr_trace_host": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int]),
+    "bhr_ctx_set_surrogate": (ctypes.c_int, [_P, _P]),
     "bhr_trace_noalloc": (ctypes.c_int, [_VP, _P, _P]),
     "bhr_trace_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
     "bhr_trace_view_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),

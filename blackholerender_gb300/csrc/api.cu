@@ -20,6 +20,7 @@
 #include "kernels.cuh"
 #include "bodies.cuh"
 #include "shade.cuh"
+#include "surrogate.cuh"
 #include "vol.cuh"
 
 // Device scratch of a trace: one work queue per launch batch, and the FP64 queues of MIXED.
@@ -66,6 +67,8 @@ struct bhr_ctx {
     // forked from and joined back to the caller's stream (made on first use)
     cudaStream_t fan[2] = {nullptr, nullptr};
     cudaEvent_t fan_fork = nullptr, fan_join[2] = {nullptr, nullptr};
+    // the learned orbit surrogate that serves BHR_METHOD_SURROGATE (bound, not owned)
+    bhr_surrogate* surr = nullptr;
     std::string err;
 };
 
@@ -532,11 +535,41 @@ int bhr_trace(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out
     if (!c) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_trace: ctx is NULL");
     if (method != BHR_METHOD_PLAIN && method != BHR_METHOD_SURROGATE)
         return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace: unknown method");
-    if (method == BHR_METHOD_SURROGATE)
-        return fail(c, BHR_ERR_NOT_READY, "bhr_trace: the surrogate runs through bhr_surrogate_trace");
     int64_t rays = 0;
     int rc = validate(c, "bhr_trace", views, nviews, out_dev, precision, &rays);
     if (rc != BHR_OK) return rc;
+    // BHR_METHOD_SURROGATE: the views the bound surrogate answers go through it (with its own
+    // fallback march for the rays it declines), the others through the plain march below
+    std::vector<bhr_view> plain_views;
+    std::vector<bhr_hit*> plain_out;
+    if (method == BHR_METHOD_SURROGATE) {
+        if (!c->surr)
+            return fail(c, BHR_ERR_NOT_READY, "bhr_trace: no surrogate is bound to the context (bhr_ctx_set_surrogate)");
+        if (precision != BHR_PREC_FP32)
+            return fail(c, BHR_ERR_UNSUPPORTED, "bhr_trace: the surrogate path runs in BHR_PREC_FP32");
+        std::vector<bhr_view> sv;
+        std::vector<bhr_hit*> so;
+        const bhr::surr::Norm nm = bhr::surr::norm_of(c->surr);
+        for (int k = 0; k < nviews; ++k) {
+            std::string why;
+            const bool s_ok = bhr::surr::supports_view(nm, views[k], &why);
+            (s_ok ? sv : plain_views).push_back(views[k]);
+            (s_ok ? so : plain_out).push_back(out_dev[k]);
+        }
+        if (!sv.empty()) {
+            const int src = bhr_surrogate_trace(c->surr, sv.data(), int(sv.size()), so.data(), cuda_stream);
+            if (src != BHR_OK) return fail(c, src, std::string("bhr_trace: ") + bhr_last_error(nullptr));
+        }
+        if (plain_views.empty()) {  // no plain march ran: bhr_trace_stats has nothing of this trace to report
+            c->have_last = false;
+            return BHR_OK;
+        }
+        views = plain_views.data();
+        out_dev = plain_out.data();
+        nviews = int(plain_views.size());
+        rays = 0;
+        for (const bhr_view& v : plain_views) rays += int64_t(v.width) * v.height;
+    }
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(c->device);
@@ -553,6 +586,14 @@ int bhr_trace(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out
     }
     cudaSetDevice(prev);
     return rc;
+}
+
+int bhr_ctx_set_surrogate(bhr_ctx* c, bhr_surrogate* s) {
+    if (!c) return fail(nullptr, BHR_ERR_INVALID_ARG, "bhr_ctx_set_surrogate: ctx is NULL");
+    if (s && bhr::surr::device_of(s) != c->device)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_ctx_set_surrogate: the surrogate lives on another device");
+    c->surr = s;
+    return BHR_OK;
 }
 
 int bhr_trace_host(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const* out_host, int precision,
@@ -627,7 +668,9 @@ int bhr_trace_host(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit* const
 int bhr_trace_stats(bhr_ctx* c, bhr_stats* s) {
     if (!c || !s) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_stats: NULL argument");
     std::memset(s, 0, sizeof *s);
-    if (!c->have_last) return fail(c, BHR_ERR_NOT_READY, "bhr_trace_stats: no trace on this context yet");
+    if (!c->have_last)
+        return fail(c, BHR_ERR_NOT_READY, "bhr_trace_stats: no plain march on this context yet (a trace answered "
+                                          "wholly by the surrogate reports through bhr_surrogate_trace_stats)");
     std::vector<bhr::WorkQueue> qs;
     const int rc = read_queues(c, c->scr, c->last_batches, c->last_stream, &qs, "bhr_trace_stats");
     if (rc != BHR_OK) return rc;

@@ -863,6 +863,7 @@ struct RayStage {  // per warp, structure of arrays over its 32 rays
     float ic[32], phi0[32], phin[32], x2[32];
     float e2x[32], e2y[32], e2z[32];
     float h2[32], baxis[32], b[32];
+    float ue[32];       // exit u of an escaping orbit (the rule's escape radius, or its tolerance escape)
     uint32_t info[32];  // bits 0-1 candidates, 2 surrogate, 3-10 plane crossings, 11+5c candidate c (k | leg << 4),
                         // 26 captured orbit
 };
@@ -981,9 +982,19 @@ __device__ __noinline__ float cap_invert(float u1, float A, float k2, float K, f
     return u;
 }
 
+// The exit radius of an escaping orbit: the CONFIG rule's fixed escape radius (1 / nm.ue), or,
+// with kTol, the tolerance escape of the SHADER and CPU rules (orbit::exit_u_tol), which depends
+// on b. The exit table and the pass evaluate it through this one function.
+template <bool kTol>
+__device__ __forceinline__ float exit_u(const SurrView& sv, float b, float u2) {
+    if (!kTol) return sv.norm.ue;
+    return orbit::exit_u_tol<float>(b, sv.rule.esc_tol, sv.u_esc_min, u2);
+}
+
 // The view's exit table: per half (0 captured, 1 escaping) and point i, x2_i = lo + i h, the
 // beta it encodes (the inverse of the x2 transform), the exit query the pass would make for that
 // beta, and the network's output through the same folded-x1 forward pass as k_surrogate.
+template <bool kTol>
 __global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ SurrView sv, const float* __restrict__ P,
                                                     float4* __restrict__ table) {
     __shared__ __align__(16) SmemNet N;
@@ -999,7 +1010,11 @@ __global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ Surr
         const float x2 = fmaf(float(i), sv.tab_h[side], sv.tab_lo[side]);
         const float mag = nm.t_eps * expm1f(fabsf(x2) / nm.t_scale);
         float sigma = 1.0f;  // the capture flag is trained at sigma = 1
-        if (side == 1) sigma = orbit::sigma_exit<float>(nm.ue, orbit::roots<float, 4>(fmaxf(mag, 1e-7f)));
+        if (side == 1) {
+            const float beta = fmaxf(mag, 1e-7f);
+            const orbit::Roots<float> Rt = orbit::roots<float, 4>(beta);
+            sigma = orbit::sigma_exit<float>(exit_u<kTol>(sv, kSqrt27f * (1.0f + beta), Rt.u2), Rt);
+        }
         qs[warp][lane] = make_float4(sv.x1, x2, sigma, 0.f);
         __syncwarp();
         mlp_eval_tiles<true>(N, qs[warp], os[warp], 2);
@@ -1064,6 +1079,7 @@ __device__ __forceinline__ float2 exit_from_table(const SurrView& sv, float x2, 
     return make_float2(fmaf(t, e.z - e.x, e.x), fmaf(t, e.w - e.y, e.y));
 }
 
+template <bool kTol>
 __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
                                                                 const float* __restrict__ P, WorkQueue* q,
                                                                 int* __restrict__ fb_list) {
@@ -1124,14 +1140,16 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             // stage slots: escaping orbit: u1 u2 u3 d32, Ic = angle camera -> turning point, phi0 = angle
             // camera -> exit; captured orbit: u1, A, k^2, K, Ic = F(camera), phi0 = angle camera -> horizon
             float s0, s1, s2, s3, Ic, phi0;
+            float ue = nm.ue;
             float Ilo = 1.f, Ihi = 0.f;  // angle range of the disk's crossings (from the turning point / camera)
             if (!cap) {
                 const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
                 sur = sur && uc < Rt.u2 * 0.9999f;
                 // closed-form baseline at the camera and at the exit
                 const float bl = orbit::base_blend<float>(beta);
+                ue = exit_u<kTol>(sv, b, Rt.u2);
                 Ic = orbit::base_sweep<float>(uc, Rt, bl);
-                phi0 = Ic + orbit::base_sweep<float>(nm.ue, Rt, bl);
+                phi0 = Ic + orbit::base_sweep<float>(ue, Rt, bl);
                 s0 = Rt.u1, s1 = Rt.u2, s2 = Rt.u3, s3 = Rt.d32;
             } else {
                 const CapStage cs = cap_stage(beta, uc, R.capture_r, R.disk_inner, R.disk_outer, sur && thin);
@@ -1188,6 +1206,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             G.h2[lane] = ri.h2;
             G.baxis[lane] = ri.b_axis;
             G.b[lane] = b;
+            G.ue[lane] = ue;
             G.info[lane] = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw |
                            (cap ? kCapBit : 0u);
         }
@@ -1285,7 +1304,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                     const float phi = G.phi0[lane] + oe.x * nm.y_scale;
                     float sp, cp;
                     sincos_rr(phi, &sp, &cp);
-                    const float ue = nm.ue;
+                    const float ue = G.ue[lane];
                     const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
                     const V3<float> e2{G.e2x[lane], G.e2y[lane], G.e2z[lane]};
                     const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
@@ -1355,15 +1374,17 @@ int train_smem_bytes() { return int(sizeof(TrainSmem)); }
 cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
                                    cudaStream_t st) {
     const int smem = int(sizeof(InferSmem));
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_surrogate, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    const bool tol = sv.rule.term_mode != BHR_TERM_CONFIG;
+    static bool attr[2] = {false, false};
+    if (!attr[tol]) {
+        auto kern = tol ? k_surrogate<true> : k_surrogate<false>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (e != cudaSuccess) return e;
-        attr = true;
+        attr[tol] = true;
     }
-    k_surrogate<<<grid, 32 * kInferWarps, smem, st>>>(sv, params, q, fb_list);
+    if (tol) k_surrogate<true><<<grid, 32 * kInferWarps, smem, st>>>(sv, params, q, fb_list);
+    else k_surrogate<false><<<grid, 32 * kInferWarps, smem, st>>>(sv, params, q, fb_list);
     return cudaGetLastError();
 }
 
@@ -1401,7 +1422,10 @@ cudaError_t launch_cross_table(const SurrView& sv, const float* params, float4* 
 }
 
 cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, cudaStream_t st) {
-    k_exit_table<<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);  // one point per thread
+    if (sv.rule.term_mode != BHR_TERM_CONFIG)  // one point per thread
+        k_exit_table<true><<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);
+    else
+        k_exit_table<false><<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);
     return cudaGetLastError();
 }
 

@@ -4,6 +4,9 @@
 
 #include <cmath>
 #include <cstdint>
+#include <string>
+
+#include "bhr.h"
 
 #include "kernels.cuh"
 #include "march.cuh"
@@ -71,6 +74,7 @@ struct SurrView {
     Norm norm;
     float x1;  // network input 1 of this view (scaled log r_cam)
     float uc;  // 1 / r_cam
+    float u_esc_min;  // 1 / rEscMin of the tolerance escape (SHADER and CPU rules)
     const float4* exit_table;  // [2][kExitTableN] (y, logit) of points i and i + 1
     float tab_lo[2], tab_h[2], tab_inv_h[2];  // x2 of a half's first point, spacing, 1 / spacing
     const float4* cross_table;  // [kCrossCells] y at the cell's corners (i, j), (i, j+1), (i+1, j), (i+1, j+1)
@@ -102,6 +106,13 @@ inline void exit_table_range(const Norm& nm, float lo[2], float h[2]) {
     }
 }
 int train_smem_bytes();
+// Whether the surrogate with normalisation nm answers view v (otherwise *why says what is missing):
+// lensed rays (no far mode), the thin disk or none, and the CONFIG rule at the trained exit
+// radius, or the SHADER or CPU rule's tolerance escape.
+bool supports_view(const Norm& nm, const bhr_view& v, std::string* why);
+// The surrogate's normalisation and device (for the context that serves BHR_METHOD_SURROGATE).
+Norm norm_of(const bhr_surrogate* s);
+int device_of(const bhr_surrogate* s);
 
 }  // namespace surr
 }  // namespace bhr

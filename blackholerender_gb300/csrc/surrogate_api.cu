@@ -418,6 +418,42 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
                          int lane);
 }
 
+}  // extern "C"
+
+namespace bhr {
+namespace surr {
+bool supports_view(const Norm& nm, const bhr_view& v, std::string* why) {
+    if (!v.lensing || v.far_mode) {
+        *why = "the surrogate answers lensed rays (lensing on, not far mode)";
+        return false;
+    }
+    if (v.disk_mode != BHR_DISK_NONE && v.disk_mode != BHR_DISK_THIN) {
+        *why = "the surrogate answers the thin disk or none";
+        return false;
+    }
+    if (v.term_mode == BHR_TERM_CONFIG) {
+        if (std::fabs(1.0f / v.escape_r - nm.ue) > 1e-9f) {
+            *why = "the CONFIG rule's escape radius differs from the trained exit radius";
+            return false;
+        }
+        return true;
+    }
+    // SHADER and CPU: the tolerance escape; exit_u_tol converges to float precision for
+    // tolerances up to the shader's ESC_TOL (0.01)
+    const float rmin = v.term_mode == BHR_TERM_SHADER ? bhr::host::shader_r_esc_min(v.disk_outer) : v.r_esc_min;
+    if (!(v.esc_tol > 0.0f && v.esc_tol <= 0.01f) || !(rmin > 3.0f) || !(1.0f / rmin > nm.ue)) {
+        *why = "the tolerance escape needs 0 < esc_tol <= 0.01 and 3 < rEscMin < the trained exit radius";
+        return false;
+    }
+    return true;
+}
+Norm norm_of(const bhr_surrogate* s) { return s->norm; }
+int device_of(const bhr_surrogate* s) { return s->device; }
+}  // namespace surr
+}  // namespace bhr
+
+extern "C" {
+
 int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev, void* stream) {
     return surrogate_trace_lane(s, views, nviews, out_dev, stream, 0);
 }
@@ -432,10 +468,9 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         std::string msg;
         const int rc = bhr::host::check_view(views[k], k, &msg);
         if (rc != BHR_OK) return fail(rc, "bhr_surrogate_trace: " + msg);
-        if (views[k].term_mode != BHR_TERM_CONFIG || !views[k].lensing || views[k].far_mode)
-            return fail(BHR_ERR_UNSUPPORTED, "bhr_surrogate_trace: the surrogate is trained for the CONFIG rule with lensing");
-        if (std::fabs(1.0f / views[k].escape_r - s->norm.ue) > 1e-9f)
-            return fail(BHR_ERR_UNSUPPORTED, "bhr_surrogate_trace: view escape radius differs from the trained one");
+        std::string why;
+        if (!bhr::surr::supports_view(s->norm, views[k], &why))
+            return fail(BHR_ERR_UNSUPPORTED, "bhr_surrogate_trace: view " + std::to_string(k) + ": " + why);
         if (!out_dev[k] || reinterpret_cast<uintptr_t>(out_dev[k]) % 16 != 0)
             return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace: output buffers must be 16-byte aligned");
         biggest = std::max<int64_t>(biggest, int64_t(views[k].width) * views[k].height);
@@ -477,6 +512,7 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         sv.x1 = float((std::log(double(sv.view.rcam)) - std::log(double(s->norm.rc_lo))) /
                           (std::log(double(s->norm.rc_hi)) - std::log(double(s->norm.rc_lo))) * 2.0 - 1.0);
         sv.uc = 1.0f / sv.view.rcam;
+        sv.u_esc_min = sv.rule.r_esc_min > 0.0f ? 1.0f / sv.rule.r_esc_min : 1.0f;
         sv.exit_table = s->etab[lane] + kTab * k;
         bhr::surr::exit_table_range(s->norm, sv.tab_lo, sv.tab_h);
         for (int h = 0; h < 2; ++h) sv.tab_inv_h[h] = 1.0f / sv.tab_h[h];

@@ -198,7 +198,11 @@ int64_t bhr_view_rays(const bhr_view* v);
 /* Traces nviews views. out_dev[k] is a caller-owned device buffer of width*height records
  * for view k. precision: BHR_PREC_*; method: BHR_METHOD_*. One view runs the plain kernel
  * with the view in constant memory; several views run one persistent launch over a
- * shared work queue. Work memory (queue counters, FP64 hand-off queue) is owned by ctx. */
+ * shared work queue. Work memory (queue counters, FP64 hand-off queue) is owned by ctx.
+ * BHR_METHOD_SURROGATE (BHR_PREC_FP32 only) needs a surrogate bound with
+ * bhr_ctx_set_surrogate (else BHR_ERR_NOT_READY): the views it answers (lensing on, not far
+ * mode, thin disk or none, every termination rule) go through bhr_surrogate_trace, rays it
+ * declines included, and the other views through the plain march, in the same call. */
 int bhr_trace(bhr_ctx* ctx, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
               int precision, int method, void* cuda_stream);
 /* Host-memory variant for callers without device buffers (the CPU mirror's trace() callers):
@@ -240,6 +244,11 @@ typedef struct bhr_surrogate_config {
     int32_t reserved[8];
 } bhr_surrogate_config;
 int bhr_surrogate_default_config(bhr_surrogate_config* cfg);
+/* Binds a surrogate to a context for bhr_trace / bhr_trace_host with BHR_METHOD_SURROGATE
+ * (NULL unbinds). The context does not own it: it must stay alive, on the context's device,
+ * while it is bound. The reference's Renderer::tracePass (src/Renderer.cpp:369-387) has one
+ * trace method; this selects the second. */
+int bhr_ctx_set_surrogate(bhr_ctx* ctx, bhr_surrogate* s);
 int bhr_surrogate_create(bhr_surrogate** s, int device, const bhr_surrogate_config* cfg, uint64_t seed);
 int bhr_surrogate_destroy(bhr_surrogate* s);
 /* Integrates n_orbits orbits (FP64 RK4 in the orbital plane) and keeps samples_per_orbit (2..8)
@@ -270,7 +279,13 @@ int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out
 int bhr_surrogate_wait_selftest(bhr_surrogate* s);
 int bhr_surrogate_save(bhr_surrogate* s, const char* path);
 int bhr_surrogate_load(bhr_surrogate* s, const char* path);
-/* Surrogate-plus-fallback trace (CONFIG rule, lensing on): stream-ordered like bhr_trace. */
+/* Surrogate-plus-fallback trace, stream-ordered like bhr_trace. Views: lensing on, not far mode,
+ * thin disk or none; the CONFIG rule at the trained exit radius (escape_r), or the SHADER / CPU
+ * rule's tolerance escape (0 < esc_tol <= 0.01), which the surrogate applies where the march's
+ * escape test first passes in the limit of small steps (beyond rEscMin, at the radius where
+ * 0.75 b'^3 / r^4 reaches esc_tol, b' the impact parameter at the current speed), then
+ * farFieldDirection there. Other views: BHR_ERR_UNSUPPORTED (bhr_trace with
+ * BHR_METHOD_SURROGATE sends them to the plain march instead). */
 int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
                         void* cuda_stream);
 /* Host-memory variant (records copied to out_host[k]; synchronous), as bhr_trace_host. */

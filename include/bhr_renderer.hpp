@@ -11,6 +11,7 @@
 //     (src/Renderer.h:58-61)
 //   Renderer::setTraceUniforms (Renderer.cpp:242-356) bhr::Renderer::makeView, makeShadeParams
 //   the frame's colour (blackhole.frag's fragColor)  bhr::Renderer::renderImage (bhr_shade)
+//   (no counterpart: the learned orbit surrogate)    Settings::surrogate, Renderer::loadSurrogate
 //
 // render() traces the frame into hit records the Renderer owns (as the reference's renderer
 // owns its targets, Renderer.cpp:125-145); renderTo() writes caller-owned device records on a
@@ -68,6 +69,9 @@ struct Settings {
     float starBrightness = 1.0f;
     float skyBrightness = 1.0f;
     bool showShadowOverlay = false;
+    // GB300 addition, no field of the reference: trace with the learned orbit surrogate
+    // (Renderer::loadSurrogate) where it answers, the plain march elsewhere.
+    bool surrogate = false;
 
     // Quality presets (Settings.cpp:12-35); PRESET_CUSTOM leaves the fields alone.
     void applyPreset(int p) {
@@ -158,7 +162,24 @@ public:
         return true;
     }
 
+    // Loads a surrogate checkpoint (bhr_surrogate_save) onto the Renderer's device and binds it
+    // to the context; frames whose Settings ask for the surrogate then trace with it.
+    bool loadSurrogate(const char* path) {
+        if (!ctx_ && !init(device_)) return false;
+        if (!surr_ && bhr_surrogate_create(&surr_, device_, nullptr, 1) != BHR_OK)
+            return logError("loadSurrogate: create", nullptr);
+        if (bhr_surrogate_load(surr_, path) != BHR_OK) return logError("loadSurrogate", nullptr);
+        if (bhr_ctx_set_surrogate(ctx_, surr_) != BHR_OK) return logError("loadSurrogate", ctx_);
+        return true;
+    }
+    bhr_surrogate* surrogate() const { return surr_; }
+
     void shutdown() {
+        if (ctx_) bhr_ctx_set_surrogate(ctx_, nullptr);
+        if (surr_) {
+            bhr_surrogate_destroy(surr_);
+            surr_ = nullptr;
+        }
         if (body_hits_) {
             cudaFree(body_hits_);
             body_hits_ = nullptr;
@@ -283,8 +304,7 @@ public:
             if (bhr_trace_volumetric(ctx_, &v, 1, outs, &p, rgbt, nullptr) != BHR_OK) return logError("render", ctx_);
             return true;
         }
-        if (bhr_trace(ctx_, &v, 1, outs, precision, BHR_METHOD_PLAIN, nullptr) != BHR_OK)
-            return logError("render", ctx_);
+        if (bhr_trace(ctx_, &v, 1, outs, precision, method(in), nullptr) != BHR_OK) return logError("render", ctx_);
         return true;
     }
 
@@ -304,8 +324,7 @@ public:
             if (bhr_trace_volumetric(ctx_, &v, 1, outs, &p, rgbt, stream) != BHR_OK) return logError("renderTo", ctx_);
             return true;
         }
-        if (bhr_trace(ctx_, &v, 1, outs, precision, BHR_METHOD_PLAIN, stream) != BHR_OK)
-            return logError("renderTo", ctx_);
+        if (bhr_trace(ctx_, &v, 1, outs, precision, method(in), stream) != BHR_OK) return logError("renderTo", ctx_);
         return true;
     }
 
@@ -322,8 +341,7 @@ public:
             return true;
         }
         bhr_hit* const outs[1] = {out.data()};
-        if (bhr_trace_host(ctx_, &v, 1, outs, precision, BHR_METHOD_PLAIN) != BHR_OK)
-            return logError("renderHost", ctx_);
+        if (bhr_trace_host(ctx_, &v, 1, outs, precision, method(in)) != BHR_OK) return logError("renderHost", ctx_);
         return true;
     }
 
@@ -355,6 +373,10 @@ public:
     bhr_ctx* context() const { return ctx_; }
 
 private:
+    static int method(const FrameInput& in) {
+        return in.settings && in.settings->surrogate ? BHR_METHOD_SURROGATE : BHR_METHOD_PLAIN;
+    }
+
     bool ensureImage(size_t n) {
         if (n <= image_capacity_) return true;
         if (image_) cudaFree(image_);
@@ -375,6 +397,7 @@ private:
     }
 
     bhr_ctx* ctx_ = nullptr;
+    bhr_surrogate* surr_ = nullptr;
     int device_ = 0;
     bhr_hit* records_ = nullptr;
     size_t capacity_ = 0;

@@ -2,7 +2,8 @@
 // tests/geodesic_tests.cpp: host-only checks always; with `--gpu <file>` also a traced frame
 // (the 256x144 view at r = 30, inclination 85 deg, 200 steps) through Renderer::render,
 // renderTo and renderHost, whose records are written to <file> for the oracle comparison the
-// Python test driver makes.
+// Python test driver makes; with `--surrogate <checkpoint>` also a 480x270 frame of the same
+// camera through the learned surrogate under the shader's rule (<file>.surrogate).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -152,7 +153,7 @@ static void testShadeParams() {
     CHECK(bhr::Renderer::makeShadeParams(faded, &p) && p.disk_opacity == 0.5f, "opacity scales with the fade");
 }
 
-static int testGpu(const char* path) {
+static int testGpu(const char* path, const char* surrogate_path) {
     std::printf("traced frame (256x144, r=30, inclination 85 deg, 200 steps)\n");
     std::string logged;
     bhr::Renderer R;
@@ -277,6 +278,37 @@ static int testGpu(const char* path) {
     bhr::FrameInput ibv = ib;
     ibv.settings = &sv;
     CHECK(!R.render(ibv) && !logged.empty(), "bodies with the volumetric disk are refused");
+    if (surrogate_path) {
+        // the learned orbit surrogate under the shader's own rule (the default termMode), thin disk
+        bhr::Settings ss;
+        ss.applyPreset(bhr::PRESET_HIGH);
+        ss.diskMode = bhr::DISK_THIN;
+        ss.surrogate = true;
+        bhr::FrameInput is = in;
+        is.settings = &ss;
+        is.windowW = 480;
+        is.windowH = 270;
+        is.termMode = BHR_TERM_SHADER;
+        logged.clear();
+        CHECK(!R.render(is) && !logged.empty(), "the surrogate before one is loaded: false and a log line");
+        CHECK(R.loadSurrogate(surrogate_path), "loadSurrogate");
+        CHECK(R.render(is), "render with the surrogate (shader rule)");
+        const size_t ns = size_t(is.windowW) * is.windowH;
+        std::vector<bhr_hit> hs(ns);
+        cudaMemcpy(hs.data(), R.hits(), ns * sizeof(bhr_hit), cudaMemcpyDeviceToHost);
+        size_t by_surr = 0;
+        for (const bhr_hit& h : hs) by_surr += (h.flags & BHR_FLAG_SURROGATE) != 0;
+        std::snprintf(msg, sizeof msg, "%zu of %zu rays answered by the surrogate", by_surr, ns);
+        CHECK(by_surr > ns * 99 / 100, msg);
+        std::vector<bhr_hit> hh2;
+        CHECK(R.renderHost(is, hh2) && hh2.size() == ns && std::memcmp(hh2.data(), hs.data(), ns * sizeof(bhr_hit)) == 0,
+              "renderHost = render with the surrogate");
+        const std::string spath = std::string(path) + ".surrogate";
+        FILE* h = std::fopen(spath.c_str(), "wb");
+        const bool wrote_s = h && std::fwrite(hs.data(), sizeof(bhr_hit), ns, h) == ns;
+        if (h) std::fclose(h);
+        CHECK(wrote_s, "surrogate records written");
+    }
     R.shutdown();
     return 0;
 }
@@ -287,7 +319,8 @@ int main(int argc, char** argv) {
     testFrameToView();
     testErrors();
     testShadeParams();
-    if (argc == 3 && std::strcmp(argv[1], "--gpu") == 0) testGpu(argv[2]);
+    if (argc >= 3 && std::strcmp(argv[1], "--gpu") == 0)
+        testGpu(argv[2], argc == 5 && std::strcmp(argv[3], "--surrogate") == 0 ? argv[4] : nullptr);
     std::printf("\n%d checks, %d failures\n", g_checks, g_failures);
     return g_failures == 0 ? 0 : 1;
 }

@@ -171,3 +171,50 @@ def check_fp32_pooled(cases, *, band: float = 1e-2, where: str = "") -> Report:
     rep.ref32_cross_r_rel_p99 = ref.cross_r_rel_p99
     assert_fp32_parity(rep, where)
     return rep
+
+
+# ----------------------------------------------------------------------------- surrogate path
+SURR_BAND = 2e-3          # |b - sqrt 27| below this the surrogate declines the ray (plain march)
+SURR_EDGE_REL = 1e-3      # surrogate crossings this close to a disk edge are ambiguous both ways
+SURR_DIR_MAX_RAD = 1e-4   # every escaped surrogate ray against the converged orbit
+
+
+def converged_view(view):
+    """The same rule in the limit of small steps, for directions (no disk, so no slab clamp):
+    CONFIG exits at its fixed radius, where step scale 0.002 is converged to 1e-6 rad; the
+    tolerance escape of the SHADER and CPU rules exits where its test first passes, which step
+    scale 1e-4 (ds floor 1e-5) locates to 3e-4 of the radius."""
+    from blackholerender_gb300 import TERM_CONFIG
+
+    fine = view.copy()
+    tol = view.term_mode != TERM_CONFIG
+    fine.step_scale = 1e-4 if tol else 0.002
+    fine.ds_floor = 1e-5 if tol else 1e-4
+    fine.max_steps = 1_000_000
+    fine.disk_mode = 0
+    return fine
+
+
+def check_surrogate(gpu: np.ndarray, view, idx: np.ndarray, where: str = "") -> dict:
+    """Surrogate-path records (surrogate rays and the plain march's fallback rays) on the pixels
+    idx: classification equal to the same-rule FP64 oracle outside the band, and every escaped
+    surrogate ray within SURR_DIR_MAX_RAD of the converged orbit of the same rule. Returns the
+    statistics, with the same-rule oracle's own distance from the converged orbit beside them."""
+    from blackholerender_gb300 import FLAG_SURROGATE
+
+    g = gpu[idx]
+    ref = O.trace_pixels(view, idx, fp64=True)
+    rep = compare(g, ref, max_steps=view.max_steps, band=SURR_BAND, edge_rel=SURR_EDGE_REL)
+    assert rep.class_mismatch == 0, f"{where}: {rep.as_dict()}"
+    conv = O.trace_pixels(converged_view(view), idx, fp64=True)
+    b = conv["b"].astype(np.float64)
+    m = ((g["flags"] & FLAG_SURROGATE) != 0) & (conv["status"] == 1) & (np.abs(b - SQRT27) > SURR_BAND)
+    assert np.all(g["status"][m] == 1), where
+    a = angle(g["dir"][m], conv["dir"][m])
+    mr = m & (ref["status"] == 1)
+    ar = angle(ref["dir"][mr], conv["dir"][mr])
+    out = {"rays": int(len(idx)), "escaped_surrogate": int(m.sum()), "class_compared": rep.n_compared,
+           "dir_p99": float(np.percentile(a, 99)) if len(a) else 0.0, "dir_max": float(a.max(initial=0.0)),
+           "same_rule_oracle_vs_converged_max": float(ar.max(initial=0.0))}
+    assert out["dir_max"] < SURR_DIR_MAX_RAD, f"{where}: {out}"
+    return out

@@ -9,7 +9,7 @@ import pytest
 
 import oracle_lib as O
 import parity
-from blackholerender_gb300 import FLAG_FALLBACK, FLAG_SURROGATE, TERM_CONFIG, Tracer, hits_numpy, workloads
+from blackholerender_gb300 import FLAG_FALLBACK, FLAG_SURROGATE, TERM_CONFIG, TERM_CPU, TERM_SHADER, Tracer, hits_numpy, workloads
 from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT, Surrogate
 
 sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "oracle"))
@@ -341,3 +341,65 @@ def test_surrogate_plan_refuses_after_work_memory_grows():
     assert np.all((hits_numpy(outs[0].cpu())["flags"] & (FLAG_SURROGATE | FLAG_FALLBACK)) != 0)
     p.close()
     s.close()
+
+
+@pytest.mark.parametrize("term", [TERM_SHADER, TERM_CPU])
+def test_drop_in_surrogate_under_the_reference_rules(surrogate, term):
+    """bhr_trace(..., BHR_METHOD_SURROGATE) through a context with the surrogate bound, under the
+    reference renderer's own rule (SHADER: capture at 2.02, tolerance escape beyond
+    max(1.25 r_out, 12)) and the CPU mirror's trace() rule (capture at 2.01, esc_tol 1e-4 beyond
+    r = 30, no disk): classification equal to the same-rule FP64 oracle outside the band, every
+    escaped surrogate ray within 1e-4 rad of the converged orbit of the same rule, and the records
+    those of bhr_surrogate_trace. Views the surrogate does not answer (far mode, lensing off) go
+    to the plain march in the same call."""
+    import torch
+
+    from blackholerender_gb300 import METHOD_SURROGATE, PREC_FP32, make_view
+
+    views = workloads.c2_views(term, width=640, height=360)[:4]
+    if term == TERM_CPU:
+        for v in views:
+            v.disk_mode = 0  # trace() has no disk
+    rng = np.random.default_rng(11)
+    with Tracer(0) as tr:
+        tr.set_surrogate(surrogate)
+        outs = tr.trace(views, method=METHOD_SURROGATE)
+        torch.cuda.synchronize()
+        got = [hits_numpy(o.cpu()) for o in outs]
+        # the same views through bhr_surrogate_trace: the same records
+        direct = surrogate.trace(views)
+        torch.cuda.synchronize()
+        for g, d in zip(got, direct):
+            assert np.array_equal(g.view(np.uint8), hits_numpy(d.cpu()).view(np.uint8))
+        # a view the surrogate does not answer (lensing off) goes to the plain march
+        flat = make_view(term, width=64, height=36, lensing=0)
+        (fo,) = tr.trace([flat], method=METHOD_SURROGATE)
+        (fp,) = tr.trace([flat], precision=PREC_FP32)
+        torch.cuda.synchronize()
+        assert np.array_equal(fo.cpu().numpy(), fp.cpu().numpy())
+    stats = []
+    for v, g in zip(views, got):
+        assert np.mean((g["flags"] & FLAG_SURROGATE) != 0) > 0.99
+        idx = rng.choice(v.rays, 1500, replace=False)
+        stats.append(parity.check_surrogate(g, v, idx, where=f"rule {term}"))
+    print(f"\nrule {term}: " + "; ".join(
+        f"max {s['dir_max']:.2e} (same-rule oracle vs converged {s['same_rule_oracle_vs_converged_max']:.2e})"
+        for s in stats))
+
+
+def test_surrogate_needs_a_bound_surrogate_and_fp32():
+    from blackholerender_gb300 import BhrError, METHOD_SURROGATE, PREC_MIXED, _abi
+
+    v = workloads.c1_view(TERM_CONFIG)
+    with Tracer(0) as tr:
+        with pytest.raises(BhrError) as e:
+            tr.trace([v], method=METHOD_SURROGATE)
+        assert e.value.code == _abi.ERR_NOT_READY
+        s = Surrogate(seed=1)
+        s.load(str(DEFAULT_CHECKPOINT))
+        tr.set_surrogate(s)
+        with pytest.raises(BhrError) as e:
+            tr.trace([v], precision=PREC_MIXED, method=METHOD_SURROGATE)
+        assert e.value.code == _abi.ERR_UNSUPPORTED
+        tr.set_surrogate(None)
+        s.close()
