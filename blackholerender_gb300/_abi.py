@@ -269,6 +269,7 @@ SIGNATURES.update({
     "bhr_surrogate_save": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "bhr_surrogate_load": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "bhr_surrogate_trace": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), _P]),
+    "bhr_surrogate_use_network": (ctypes.c_int, [_P, ctypes.c_int]),
     "bhr_surrogate_trace_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "bhr_surrogate_trace_host": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P)]),
     "bhr_surrogate_trace_times": (ctypes.c_int, [_P, _F]),

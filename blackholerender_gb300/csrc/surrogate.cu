@@ -841,39 +841,44 @@ __global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ 
 
 // ---------------------------------------------------------------------------------------
 // inference: one warp traces 32 rays at a time, in phases that hand state on through shared
-// memory, so that no lane waits on another lane's crossing loop. The network itself runs in the
-// view's two tables (k_exit_table, k_cross_table, launched before the pass); the rays
-// interpolate them:
-//   1  per ray (lane): setup and routing, orbital plane, roots, closed-form angle at the camera
-//      and at the exit, the exit query from the exit table, and the disk-plane crossings inside
-//      the disk's angle range on either leg (candidates, found without inverting the orbit)
-//   2  per candidate, spread over the warp's lanes: baseline inversion u(phi), the crossing
-//      query from the crossing table
-//   3  per candidate: corrected crossing radius and azimuth; per ray: capture-flag check,
-//      exit direction and the record
+// memory, so that no lane waits on another lane's crossing loop. Within a view, everything an
+// escaping orbit's record needs except its orientation is a function of the impact parameter
+// alone (the camera radius and the rule are the view's): the exit angle with the network's
+// residual, the escape direction in the orbital plane after farFieldDirection at the exit, the
+// angle to the turning point, the periapsis and the capture logit. The view's exit table
+// (k_exit_table, launched before the pass) holds them per point of x2, and the crossing table
+// (k_cross_table) the network's residual for crossing queries. The rays interpolate them:
+//   1  per ray (lane): setup and routing, the orbital plane, the exit table, and the disk-plane
+//      crossings inside the disk's angle range (candidates, found without inverting the orbit);
+//      captured orbits take the exact one-real-root form
+//   2  per candidate, spread over the warp's lanes: roots, inversion of the closed form u(phi),
+//      the crossing table's residual, the crossing radius and azimuth
+//   3  per ray: the escape direction in 3-D and the record
+// The surrogate variant without the network (kNet false) builds the same tables from the
+// converged closed form (orbit::Baseline<false>) and reads no crossing table.
 
 constexpr int kInferWarps = 8;
 constexpr int kMaxCand = 3;                   // crossings kept per ray (the record holds 3)
-constexpr int kMaxQ = 32 + 32 * kMaxCand;     // exit query per ray + crossing queries
 constexpr int kCapDup = 3;                    // R_F duplication steps of the captured-orbit closed form
 constexpr uint32_t kCapBit = 1u << 26;        // stage info: the ray's orbit is captured
 
 struct RayStage {  // per warp, structure of arrays over its 32 rays
-    float u1[32], u2[32], u3[32], d32[32];
-    float ic[32], phi0[32], phin[32], x2[32];
+    float s0[32], s1[32], s2[32], s3[32];  // captured orbit: u1, A, k^2, K
+    float ic[32];      // angle camera -> turning point (escaping), F(camera) (captured)
+    float psi[32];     // escaping: in-plane escape direction minus pi
+    float minr[32];    // escaping: periapsis 1 / u2
+    float phin[32], x2[32], beta[32];
     float e2x[32], e2y[32], e2z[32];
-    float h2[32], baxis[32], b[32];
-    float ue[32];       // exit u of an escaping orbit (the rule's escape radius, or its tolerance escape)
+    float baxis[32], b[32];
     uint32_t info[32];  // bits 0-1 candidates, 2 surrogate, 3-10 plane crossings, 11+5c candidate c (k | leg << 4),
                         // 26 captured orbit
 };
 
 struct InferSmem {
-    float2 o[kInferWarps][kMaxQ];  // network outputs: [0, 32) the exit queries, then the crossings
     RayStage st[kInferWarps];
     int task[kInferWarps][32 * kMaxCand];     // owner lane << 2 | candidate
-    float tu[kInferWarps][32 * kMaxCand];     // inverted u, then the corrected radius (< 0: outside the disk)
-    float tphi[kInferWarps][32 * kMaxCand];   // azimuth of the corrected crossing
+    float tu[kInferWarps][32 * kMaxCand];     // the crossing radius (< 0: outside the disk)
+    float tphi[kInferWarps][32 * kMaxCand];   // azimuth of the crossing
 };
 
 __device__ __forceinline__ unsigned long long warp_append_ull(unsigned long long* ctr) {
@@ -982,49 +987,131 @@ __device__ __noinline__ float cap_invert(float u1, float A, float k2, float K, f
     return u;
 }
 
-// The exit radius of an escaping orbit: the CONFIG rule's fixed escape radius (1 / nm.ue), or,
-// with kTol, the tolerance escape of the SHADER and CPU rules (orbit::exit_u_tol), which depends
-// on b. The exit table and the pass evaluate it through this one function.
-template <bool kTol>
-__device__ __forceinline__ float exit_u(const SurrView& sv, float b, float u2) {
-    if (!kTol) return sv.norm.ue;
-    return orbit::exit_u_tol<float>(b, sv.rule.esc_tol, sv.u_esc_min, u2);
+// Writes point i's value f into the four cubic entries (f_j .. f_{j+3}) that hold it.
+__device__ __forceinline__ void put_cubic(float* T, int i, float f) {
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        const int j = i - d;
+        if (j >= 0 && j <= kExitTableN - 4) T[4 * j + d] = f;
+    }
 }
 
-// The view's exit table: per half (0 captured, 1 escaping) and point i, x2_i = lo + i h, the
-// beta it encodes (the inverse of the x2 transform), the exit query the pass would make for that
-// beta, and the network's output through the same folded-x1 forward pass as k_surrogate.
-template <bool kTol>
+// Writes point i's values (a, c) into the pair entries i (slots 0, 2 or, with kAdj, 0, 1) and
+// i - 1 (slots 1, 3 or 2, 3): entry m holds points m and m + 1; the last entry repeats its point.
+template <bool kAdj>
+__device__ __forceinline__ void put_pair(float* T, int i, float a, float c) {
+    constexpr int s0 = 0, s1 = kAdj ? 1 : 2, t0 = kAdj ? 2 : 1, t1 = 3;
+    T[4 * i + s0] = a;
+    T[4 * i + s1] = c;
+    if (i > 0) {
+        T[4 * (i - 1) + t0] = a;
+        T[4 * (i - 1) + t1] = c;
+    }
+    if (i == kExitTableN - 1) {
+        T[4 * i + t0] = a;
+        T[4 * i + t1] = c;
+    }
+}
+
+// The view's exit table (layout in surrogate.cuh). Captured half (kNet only): the network's
+// (y, capture logit) at sigma = 1 per point. Escaping half: per point, the beta it encodes (the
+// inverse of the x2 transform) and from it the roots, the exit u of the rule, the variant's closed
+// form from the camera to the turning point, to the exit and to the disk's radii, the network's
+// residual at the exit (kNet), the exit angle, and the escape direction in the orbital plane:
+// the exit position and velocity (energy integral of x'' = -3 h^2 x / r^5 with h^2 =
+// b^2 / (1 + 2 b^2 / r_cam^3)), then farFieldDirection (geodesic.glsl:43-53) there, measured from
+// the radial direction at the exit so that the angle stays continuous in x2.
+// The in-plane escape direction (its angle from e1, e1 = the camera direction and e2 the ray's
+// tangential direction) of an escaping orbit that leaves the march at u = ue at angle phi0 from
+// the camera: the exit position and velocity (energy integral of x'' = -3 h^2 x / r^5 with
+// h^2 = b^2 / (1 + 2 b^2 / r_cam^3)), then farFieldDirection (geodesic.glsl:43-53) there,
+// measured from the radial direction at the exit, so that the angle stays continuous in b.
+__device__ __forceinline__ float escape_angle(float phi0, float ue, const orbit::Roots<float>& Rt, float b,
+                                              float two_over_r3) {
+    float sp, cp;
+    sincos_rr(phi0, &sp, &cp);
+    const float re = 1.0f / ue;
+    const V3<float> xe{re * cp, re * sp, 0.f};
+    const float sP = orbit::dudphi<float>(ue, Rt);
+    V3<float> Tv{sP * re * re * cp - re * sp, sP * re * re * sp + re * cp, 0.f};
+    const float b2 = b * b;
+    const float h2 = b2 / (1.0f + b2 * two_over_r3);
+    const float vmag = sqrtf(fmaxf(1.0f - h2 * two_over_r3 + 2.0f * h2 * ue * ue * ue, 1e-12f));
+    const float Ti = vmag * rsqrtf(dot3(Tv, Tv));
+    Tv = {Tv.x * Ti, Tv.y * Ti, 0.f};
+    const V3<float> d = far_field_dir(xe, Tv, h2);
+    return phi0 + atan2f(cp * d.y - sp * d.x, cp * d.x + sp * d.y);
+}
+
+// The view's exit table (layout in surrogate.cuh). Captured half (kNet only): the network's
+// (y, capture logit) at sigma = 1 per point. Escaping half: per point, the beta it encodes (the
+// inverse of the x2 transform) and from it the roots, the exit u of the rule (with kTol, of each
+// branch of the tolerance escape), the variant's closed form from the camera to the turning
+// point, to the exit and to the disk's radii, the network's residual at the exit (kNet), the exit
+// angle and the escape direction (escape_angle). Each point is written into every entry it
+// belongs to.
+template <bool kTol, bool kNet>
 __global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ SurrView sv, const float* __restrict__ P,
                                                     float4* __restrict__ table) {
+    constexpr int kQ = kTol ? 2 : 1;  // exit queries per point: one per branch of the rule's exit
     __shared__ __align__(16) SmemNet N;
-    __shared__ float4 qs[8][32];
-    __shared__ float2 os[8][32];
-    load_net_half<true>(N, P, sv.x1);
-    __syncthreads();
+    __shared__ float4 qs[8][32 * kQ];
+    __shared__ float2 os[8][32 * kQ];
+    if (kNet) {
+        load_net_half<true>(N, P, sv.x1);
+        __syncthreads();
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const Norm& nm = sv.norm;
+    float* T = reinterpret_cast<float*>(table);
+    constexpr float kPi = 3.14159265358979f;
     for (int base = (blockIdx.x * 8 + warp) * 32; base < 2 * kExitTableN; base += gridDim.x * 8 * 32) {
-        const int k = base + lane;  // 2 kExitTableN is a multiple of 32
+        const int k = base + lane;  // 2 kExitTableN is a multiple of 32: a warp stays on one half
         const int side = k / kExitTableN, i = k - side * kExitTableN;
+        if (!kNet && side == 0) continue;  // the converged closed form classifies captured orbits itself
         const float x2 = fmaf(float(i), sv.tab_h[side], sv.tab_lo[side]);
         const float mag = nm.t_eps * expm1f(fabsf(x2) / nm.t_scale);
-        float sigma = 1.0f;  // the capture flag is trained at sigma = 1
+        float sig[2] = {1.0f, 1.0f};  // the capture flag is trained at sigma = 1
+        float ue[2] = {0.f, 0.f};
+        float b = 0.f, beta = 0.f, Ic = 0.f, ilo = 0.f, ihi = 0.f;
+        orbit::Roots<float> Rt{};
+        using B = orbit::Baseline<kNet>;
         if (side == 1) {
-            const float beta = fmaxf(mag, 1e-7f);
-            const orbit::Roots<float> Rt = orbit::roots<float, 4>(beta);
-            sigma = orbit::sigma_exit<float>(exit_u<kTol>(sv, kSqrt27f * (1.0f + beta), Rt.u2), Rt);
+            beta = fmaxf(mag, 1e-7f);
+            b = kSqrt27f * (1.0f + beta);
+            Rt = orbit::roots<float, 4>(beta);
+            if (kTol) {
+                ue[0] = fminf(sv.u_esc_min, Rt.u2);
+                ue[1] = orbit::exit_u_tol<float>(b, sv.rule.esc_tol, 1.0f, Rt.u2);
+            } else {
+                ue[0] = nm.ue;
+            }
+            for (int r = 0; r < kQ; ++r) sig[r] = orbit::sigma_exit<float>(ue[r], Rt);
+            Ic = B::template sweep<float>(sv.uc, Rt, beta);
+            ilo = B::template sweep<float>(fminf(1.0f / (sv.rule.disk_inner * 0.97f), Rt.u2), Rt, beta);
+            ihi = B::template sweep<float>(fminf(1.0f / (sv.rule.disk_outer * 1.03f), Rt.u2), Rt, beta);
         }
-        qs[warp][lane] = make_float4(sv.x1, x2, sigma, 0.f);
-        __syncwarp();
-        mlp_eval_tiles<true>(N, qs[warp], os[warp], 2);
-        // point i is the first pair of entry i and the second of entry i - 1 (the last entry
-        // repeats its point)
-        float2* half = reinterpret_cast<float2*>(table);
-        const float2 o = os[warp][lane];
-        half[2 * k] = o;
-        if (i > 0) half[2 * k - 1] = o;
-        if (i == kExitTableN - 1) half[2 * k + 1] = o;
+        float2 o[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        if (kNet) {
+            for (int r = 0; r < kQ; ++r) qs[warp][32 * r + lane] = make_float4(sv.x1, x2, sig[r], 0.f);
+            __syncwarp();
+            mlp_eval_tiles<true>(N, qs[warp], os[warp], 2 * kQ);
+            for (int r = 0; r < kQ; ++r) o[r] = os[warp][32 * r + lane];
+        }
+        if (side == 0) {
+            put_pair<true>(T, i, o[0].x, o[0].y);
+        } else {
+            const int rule_branch = kTol && b > sv.b_kink ? 1 : 0;
+            for (int r = 0; r < kQ; ++r) {
+                const float phi0 = Ic + B::template sweep<float>(ue[r], Rt, beta) + o[r].x * nm.y_scale;
+                const float psi = escape_angle(phi0, ue[r], Rt, b, sv.view.two_over_r3);
+                put_cubic(T + 4 * (r ? kExitPsiB : kExitPsi), i, psi - kPi);
+                put_cubic(T + 4 * (r ? kExitPhi0B : kExitPhi0), i, phi0);
+            }
+            put_cubic(T + 4 * kExitIc, i, Ic);
+            put_pair<true>(T + 4 * kExitRange, i, ilo, ihi);
+            put_pair<false>(T + 4 * kExitU2, i, Rt.u2, o[rule_branch].y);
+        }
         __syncwarp();
     }
 }
@@ -1069,28 +1156,34 @@ __device__ __forceinline__ float cross_from_table(const SurrView& sv, float x2, 
     return fmaf(a, hi - lo, lo);
 }
 
-// The exit query's network output from the view's table: linear in x2 on the ray's half.
-__device__ __forceinline__ float2 exit_from_table(const SurrView& sv, float x2, bool cap) {
-    const int side = cap ? 0 : 1;
-    const float u = (x2 - sv.tab_lo[side]) * sv.tab_inv_h[side];
-    const int i = min(max(int(floorf(u)), 0), kExitTableN - 2);
-    const float t = u - float(i);
-    const float4 e = __ldg(sv.exit_table + side * kExitTableN + i);
-    return make_float2(fmaf(t, e.z - e.x, e.x), fmaf(t, e.w - e.y, e.y));
+
+// Lagrange weights of the cubic through the entry's four points (nodes 0 .. 3) at tc in [0, 3].
+__device__ __forceinline__ float4 cubic_weights(float tc) {
+    const float a = tc, b = tc - 1.0f, c = tc - 2.0f, d = tc - 3.0f;
+    const float ab = a * b, cd = c * d;
+    return make_float4(-(1.0f / 6.0f) * b * cd, 0.5f * a * cd, -0.5f * ab * d, (1.0f / 6.0f) * ab * c);
+}
+__device__ __forceinline__ float cubic(const float4 f, const float4 L) {
+    return fmaf(f.x, L.x, fmaf(f.y, L.y, fmaf(f.z, L.z, f.w * L.w)));
 }
 
-template <bool kTol>
+// The captured half's capture logit at x2 (linear between the two points of entry m).
+__device__ __forceinline__ float capture_logit(const SurrView& sv, float x2) {
+    const float u = (x2 - sv.tab_lo[0]) * sv.tab_inv_h[0];
+    const int i = min(max(int(floorf(u)), 0), kExitTableN - 2);
+    const float4 e = __ldg(sv.exit_table + i);
+    return fmaf(u - float(i), e.w - e.y, e.y);
+}
+
+template <bool kTol, bool kNet>
 __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
-                                                                const float* __restrict__ P, WorkQueue* q,
-                                                                int* __restrict__ fb_list) {
+                                                                WorkQueue* q, int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
-    (void)P;  // the network is read through the view's tables
     const DevView& w = sv.view;
     const Rule& R = sv.rule;
     const Norm& nm = sv.norm;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float2* ob = S.o[warp];
     RayStage& G = S.st[warp];
     int* task = S.task[warp];
     float* tu = S.tu[warp];
@@ -1099,7 +1192,8 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
     const float beta_band = nm.band / kSqrt27f;
     const float uc = sv.uc;
     const bool thin = R.disk_mode == BHR_DISK_THIN;
-    uint32_t n_surr = 0, n_dis = 0, n_q = 0, n_rows = 0;
+    const float4* E = sv.exit_table;
+    uint32_t n_surr = 0, n_dis = 0;
     for (;;) {
         unsigned long long chunk = 0;
         if (lane == 0) chunk = atomicAdd(&q->next_chunk, 1ull);
@@ -1137,27 +1231,42 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             e2 = {e2.x * e2i, e2.y * e2i, e2.z * e2i};
             const float tb = __logf(1.0f + fabsf(beta) * (1.0f / nm.t_eps));  // 1 + |beta|/eps >= 1.19 here
             const float x2 = (beta < 0.f ? -tb : tb) * nm.t_scale;
-            // stage slots: escaping orbit: u1 u2 u3 d32, Ic = angle camera -> turning point, phi0 = angle
-            // camera -> exit; captured orbit: u1, A, k^2, K, Ic = F(camera), phi0 = angle camera -> horizon
-            float s0, s1, s2, s3, Ic, phi0;
-            float ue = nm.ue;
+            // stage slots: escaping orbit: psi, minr, Ic = angle camera -> turning point; captured orbit:
+            // u1, A, k^2, K, Ic = F(camera); phi0 = angle camera -> exit (or -> horizon)
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, Ic = 0.f, phi0 = 0.f, psi = 0.f, minr = 0.f;
             float Ilo = 1.f, Ihi = 0.f;  // angle range of the disk's crossings (from the turning point / camera)
+            float gx = 0.f;
+            int m = 0, jc = 0;
             if (!cap) {
-                const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
-                sur = sur && uc < Rt.u2 * 0.9999f;
-                // closed-form baseline at the camera and at the exit
-                const float bl = orbit::base_blend<float>(beta);
-                ue = exit_u<kTol>(sv, b, Rt.u2);
-                Ic = orbit::base_sweep<float>(uc, Rt, bl);
-                phi0 = Ic + orbit::base_sweep<float>(ue, Rt, bl);
-                s0 = Rt.u1, s1 = Rt.u2, s2 = Rt.u3, s3 = Rt.d32;
+                sur = sur && x2 < sv.x2_lim;  // clear of the camera's tangential ray
+                // the exit table: pair entry m and cubic entry jc around the ray's x2
+                gx = (x2 - sv.tab_lo[1]) * sv.tab_inv_h[1];
+                m = min(max(int(floorf(gx)), 0), kExitTableN - 2);
+                jc = min(max(m - 1, 0), kExitTableN - 4);
+                const float4 L = cubic_weights(gx - float(jc));
+                const float4 pu = __ldg(E + kExitU2 + m);
+                const float t = gx - float(m);
+                const float u2 = fmaf(t, pu.y - pu.x, pu.x);
+                sur = sur && uc < u2 * 0.9999f;
+                if (kNet && sur && fmaf(t, pu.w - pu.z, pu.z) > 0.f) {  // the learned capture flag disagrees with
+                    sur = false;                                         // b vs sqrt(27): the integrator decides
+                    ++n_dis;
+                }
+                const bool br = kTol && b > sv.b_kink;  // the tolerance escape's branch
+                psi = cubic(__ldg(E + (br ? kExitPsiB : kExitPsi) + jc), L);
+                phi0 = cubic(__ldg(E + (br ? kExitPhi0B : kExitPhi0) + jc), L);
+                minr = 1.0f / u2;
             } else {
-                const CapStage cs = cap_stage(beta, uc, R.capture_r, R.disk_inner, R.disk_outer, sur && thin);
-                Ic = cs.Ic, phi0 = cs.phi0, Ilo = cs.Ilo, Ihi = cs.Ihi;
-                s0 = cs.u1, s1 = cs.A, s2 = cs.k2, s3 = cs.K;
+                if (kNet && sur && !(capture_logit(sv, x2) > 0.f)) {
+                    sur = false;
+                    ++n_dis;
+                }
+                if (sur) {
+                    const CapStage cs = cap_stage(beta, uc, R.capture_r, R.disk_inner, R.disk_outer, thin);
+                    Ic = cs.Ic, phi0 = cs.phi0, Ilo = cs.Ilo, Ihi = cs.Ihi;
+                    s0 = cs.u1, s1 = cs.A, s2 = cs.k2, s3 = cs.K;
+                }
             }
-            // the exit query (x1, x2, sigma at the exit; sigma = 1 for the capture flag) from the table
-            ob[lane] = sur ? exit_from_table(sv, x2, cap) : make_float2(0.f, 0.f);
             // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
             float phin = atan2f(-e1.y, e2.y);
             if (phin < 0.f) phin += kPi;
@@ -1175,11 +1284,12 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                     // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
                     // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
                     // where the orbit stays outside them)
-                    orbit::Roots<float> Rt;
-                    Rt.u1 = s0, Rt.u2 = s1, Rt.u3 = s2, Rt.d32 = s3;
-                    const float bl = orbit::base_blend<float>(beta);
-                    Ilo = orbit::base_sweep<float>(fminf(1.0f / (R.disk_inner * 0.97f), Rt.u2), Rt, bl);
-                    Ihi = orbit::base_sweep<float>(fminf(1.0f / (R.disk_outer * 1.03f), Rt.u2), Rt, bl);
+                    const float4 L = cubic_weights(gx - float(jc));
+                    Ic = cubic(__ldg(E + kExitIc + jc), L);
+                    const float4 rg = __ldg(E + kExitRange + m);
+                    const float t = gx - float(m);
+                    Ilo = fmaf(t, rg.z - rg.x, rg.x);
+                    Ihi = fmaf(t, rg.w - rg.y, rg.y);
                 }
 #pragma unroll 1
                 for (int k = 0; k < nplane && ncand < kMaxCand; ++k) {
@@ -1192,21 +1302,21 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                     }
                 }
             }
-            G.u1[lane] = s0;
-            G.u2[lane] = s1;
-            G.u3[lane] = s2;
-            G.d32[lane] = s3;
+            G.s0[lane] = s0;
+            G.s1[lane] = s1;
+            G.s2[lane] = s2;
+            G.s3[lane] = s3;
             G.ic[lane] = Ic;
-            G.phi0[lane] = phi0;
+            G.psi[lane] = psi;
+            G.minr[lane] = minr;
             G.phin[lane] = phin;
             G.x2[lane] = x2;
+            G.beta[lane] = beta;
             G.e2x[lane] = e2.x;
             G.e2y[lane] = e2.y;
             G.e2z[lane] = e2.z;
-            G.h2[lane] = ri.h2;
             G.baxis[lane] = ri.b_axis;
             G.b[lane] = b;
-            G.ue[lane] = ue;
             G.info[lane] = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw |
                            (cap ? kCapBit : 0u);
         }
@@ -1228,49 +1338,29 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             const uint32_t kl = (info >> (11 + 5 * c)) & 31u;
             const float phk = G.phin[own] + float(kl & 15u) * kPi;
             const float Ic = G.ic[own];
-            float u, sg = 0.f;
+            float us;
             if (!(info & kCapBit)) {
-                orbit::Roots<float> Rt;
-                Rt.u1 = G.u1[own];
-                Rt.u2 = G.u2[own];
-                Rt.u3 = G.u3[own];
-                Rt.d32 = G.d32[own];
+                const float beta = G.beta[own];
+                const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
                 const bool leg = (kl & 16u) != 0;
-                // the blend weight from the ray's roots: beta from u2 would cost a cubic; b is staged
-                const float bl = orbit::base_blend<float>(G.b[own] * (1.0f / kSqrt27f) - 1.0f);
-                u = orbit::invert_sweep<float, 4>(leg ? phk - Ic : Ic - phk, Rt, bl);
-                sg = leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f)) : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
+                const float u = orbit::invert_sweep_v<float, 4, kNet>(leg ? phk - Ic : Ic - phk, Rt, beta);
+                us = u;
+                if (kNet) {  // the network's residual from the view's crossing table, applied along the orbit
+                    const float sg =
+                        leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f)) : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
+                    const float dphi = cross_from_table(sv, G.x2[own], sg) * nm.y_scale;
+                    const float sPu = orbit::dudphi<float>(u, Rt);
+                    us = leg ? u + dphi * sPu : u - dphi * sPu;
+                }
             } else {
-                u = cap_invert(G.u1[own], G.u2[own], G.u3[own], G.d32[own], G.b[own], Ic, phk, uc, R.capture_r,
-                               R.disk_inner, R.disk_outer);
-            }
-            // the crossing query (x1, x2, sigma) of an escaping orbit from the view's table
-            ob[32 + t] = make_float2((info & kCapBit) ? 0.f : cross_from_table(sv, G.x2[own], sg), 0.f);
-            tu[t] = u;
-        }
-        __syncwarp();
-        // ---- phase 3: corrected crossings (per candidate), then records (per ray)
-#pragma unroll 1
-        for (int t = lane; t < total; t += 32) {
-            const int own = task[t] >> 2, c = task[t] & 3;
-            const uint32_t info = G.info[own];
-            const uint32_t kl = (info >> (11 + 5 * c)) & 31u;
-            const float u = tu[t];
-            float us = u;
-            if (!(info & kCapBit)) {  // escaping orbit: the network's correction of the baseline
-                orbit::Roots<float> Rt;
-                Rt.u1 = G.u1[own];
-                Rt.u2 = G.u2[own];
-                Rt.u3 = G.u3[own];
-                const float dphi = ob[32 + t].x * nm.y_scale;
-                const float sPu = orbit::dudphi<float>(u, Rt);
-                us = (kl & 16u) ? u + dphi * sPu : u - dphi * sPu;
+                us = cap_invert(G.s0[own], G.s1[own], G.s2[own], G.s3[own], G.b[own], Ic, phk, uc, R.capture_r,
+                                R.disk_inner, R.disk_outer);
             }
             const float rs = 1.0f / us;
             float rr = -1.f, ph = 0.f;
             if (rs >= R.disk_inner && rs <= R.disk_outer) {
                 float s2, c2;
-                sincos_rr(G.phin[own] + float(kl & 15u) * kPi, &s2, &c2);
+                sincos_rr(phk, &s2, &c2);
                 const float hx = rs * (c2 * w.rhat[0] + s2 * G.e2x[own]);
                 const float hz = rs * (c2 * w.rhat[2] + s2 * G.e2z[own]);
                 ph = atan2f(hz, hx);
@@ -1280,15 +1370,11 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
             tphi[t] = ph;
         }
         __syncwarp();
+        // ---- phase 3: records (per ray)
         {
             const uint32_t info = G.info[lane];
-            bool sur = (info & 4u) != 0;
+            const bool sur = (info & 4u) != 0;
             const bool cap = (info & kCapBit) != 0;
-            const float2 oe = ob[lane];
-            if (sur && (oe.y > 0.f) != cap) {  // the learned capture flag disagrees with b vs sqrt(27): integrator decides
-                sur = false;
-                ++n_dis;
-            }
             if (valid && !sur) fb_list[warp_append_ull(&q->fb_count)] = ray;
             if (sur) {
                 ++n_surr;
@@ -1296,40 +1382,21 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
                 V3<float> d{0.f, 0.f, 0.f};
                 float min_r = R.capture_r;
                 uint32_t status = BHR_STATUS_CAPTURED;
-                if (!cap) {
-                    orbit::Roots<float> Rt;
-                    Rt.u1 = G.u1[lane];
-                    Rt.u2 = G.u2[lane];
-                    Rt.u3 = G.u3[lane];
-                    const float phi = G.phi0[lane] + oe.x * nm.y_scale;
+                if (!cap) {  // the escape direction cos(psi) e1 + sin(psi) e2, psi = pi + the table's angle
                     float sp, cp;
-                    sincos_rr(phi, &sp, &cp);
-                    const float ue = G.ue[lane];
-                    const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
-                    const V3<float> e2{G.e2x[lane], G.e2y[lane], G.e2z[lane]};
-                    const V3<float> xr{cp * e1.x + sp * e2.x, cp * e1.y + sp * e2.y, cp * e1.z + sp * e2.z};
-                    const V3<float> xt{-sp * e1.x + cp * e2.x, -sp * e1.y + cp * e2.y, -sp * e1.z + cp * e2.z};
-                    const float re = 1.0f / ue;
-                    const V3<float> xe{xr.x * re, xr.y * re, xr.z * re};
-                    // velocity at the exit: along dx/dphi = sqrt(P)/u^2 xr + xt/u, with |v|^2 from the energy
-                    // integral of x'' = -3 h^2 x / r^5: |v|^2 = |v0|^2 - 2 h^2 / rc^3 + 2 h^2 u^3
-                    const float h2 = G.h2[lane];
-                    const float sP = orbit::dudphi<float>(ue, Rt);
-                    V3<float> T{sP * re * re * xr.x + re * xt.x, sP * re * re * xr.y + re * xt.y,
-                                sP * re * re * xr.z + re * xt.z};
-                    const float vmag = sqrtf(fmaxf(1.0f - h2 * w.two_over_r3 + 2.0f * h2 * ue * ue * ue, 1e-12f));
-                    const float Ti = vmag * rsqrtf(dot3(T, T));
-                    T = {T.x * Ti, T.y * Ti, T.z * Ti};
-                    d = far_field_dir(xe, T, h2);
-                    min_r = 1.0f / Rt.u2;
+                    sincos_rr(G.psi[lane], &sp, &cp);
+                    d = {-(cp * w.rhat[0] + sp * G.e2x[lane]), -(cp * w.rhat[1] + sp * G.e2y[lane]),
+                         -(cp * w.rhat[2] + sp * G.e2z[lane])};
+                    min_r = G.minr[lane];
                     status = BHR_STATUS_ESCAPED;
                 }
                 // crossings inside [disk_inner, disk_outer], in march order
+                const int nc = int(info & 3u);
                 float cr[3] = {0.f, 0.f, 0.f}, cph[3] = {0.f, 0.f, 0.f};
                 int nrec = 0;
 #pragma unroll
                 for (int c = 0; c < kMaxCand; ++c) {
-                    if (c < ncand) {
+                    if (c < nc) {
                         const float rr = tu[off + c];
                         if (rr > 0.f) {
                             const float pp = tphi[off + c];
@@ -1357,12 +1424,9 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
     for (int o = 16; o > 0; o >>= 1) {
         n_surr += __shfl_xor_sync(0xffffffffu, n_surr, o);
         n_dis += __shfl_xor_sync(0xffffffffu, n_dis, o);
-        n_q += __shfl_xor_sync(0xffffffffu, n_q, o);
     }
     if (lane == 0) {
         atomicAdd(&q->surr_rays, (unsigned long long)n_surr);
-        atomicAdd(&q->mlp_queries, (unsigned long long)n_q);
-        atomicAdd(&q->mlp_rows, (unsigned long long)n_rows);
         if (n_dis) atomicAdd(&q->capture_disagree, (unsigned long long)n_dis);
     }
 }
@@ -1371,20 +1435,21 @@ __global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_
 
 int train_smem_bytes() { return int(sizeof(TrainSmem)); }
 
-cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
+cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_list, int grid, bool net,
                                    cudaStream_t st) {
     const int smem = int(sizeof(InferSmem));
     const bool tol = sv.rule.term_mode != BHR_TERM_CONFIG;
-    static bool attr[2] = {false, false};
-    if (!attr[tol]) {
-        auto kern = tol ? k_surrogate<true> : k_surrogate<false>;
+    using K = void (*)(SurrView, WorkQueue*, int*);
+    const K kern = tol ? (net ? K(k_surrogate<true, true>) : K(k_surrogate<true, false>))
+                       : (net ? K(k_surrogate<false, true>) : K(k_surrogate<false, false>));
+    static bool attr[2][2] = {{false, false}, {false, false}};
+    if (!attr[tol][net]) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (e != cudaSuccess) return e;
-        attr[tol] = true;
+        attr[tol][net] = true;
     }
-    if (tol) k_surrogate<true><<<grid, 32 * kInferWarps, smem, st>>>(sv, params, q, fb_list);
-    else k_surrogate<false><<<grid, 32 * kInferWarps, smem, st>>>(sv, params, q, fb_list);
+    kern<<<grid, 32 * kInferWarps, smem, st>>>(sv, q, fb_list);
     return cudaGetLastError();
 }
 
@@ -1421,11 +1486,12 @@ cudaError_t launch_cross_table(const SurrView& sv, const float* params, float4* 
     return cudaGetLastError();
 }
 
-cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, cudaStream_t st) {
-    if (sv.rule.term_mode != BHR_TERM_CONFIG)  // one point per thread
-        k_exit_table<true><<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);
-    else
-        k_exit_table<false><<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);
+cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, bool net, cudaStream_t st) {
+    const bool tol = sv.rule.term_mode != BHR_TERM_CONFIG;
+    using K = void (*)(SurrView, const float*, float4*);
+    const K kern = tol ? (net ? K(k_exit_table<true, true>) : K(k_exit_table<true, false>))
+                       : (net ? K(k_exit_table<false, true>) : K(k_exit_table<false, false>));
+    kern<<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);  // one point per thread
     return cudaGetLastError();
 }
 

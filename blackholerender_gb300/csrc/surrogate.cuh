@@ -62,6 +62,28 @@ cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, 
 // kExitTableN points of x2 for each half (0: captured, beta < 0; 1: escaping) and read back by
 // linear interpolation. Entry i of a half holds points i and i + 1 (one 16-byte load).
 constexpr int kExitTableN = 8192;
+// A view's exit table, in float4 entries (N = kExitTableN points per half):
+//   [0, N)          captured half: entry i = (y, capture logit) of points i and i + 1
+//   escaping half, over the points x2_i = tab_lo[1] + i tab_h[1]:
+//   kExitPsi  + j   the escape direction's angle in the orbital plane (from e1 = the camera
+//                   direction towards e2) minus pi at points j .. j + 3 (cubic interpolation)
+//   kExitPhi0 + j   the angle from the camera to the exit, points j .. j + 3
+//   kExitIc   + j   the angle from the camera to the turning point, points j .. j + 3
+//   kExitRange + m  the disk's angle range from the turning point (Ilo, Ihi) of points m, m + 1
+//   kExitU2   + m   (u2_m, u2_{m+1}, logit_m, logit_{m+1}): the turning point and capture logit
+//   kExitPsiB, kExitPhi0B   the tolerance escape's second regime (below)
+// The tolerance escape of the SHADER and CPU rules exits at u_e = min(1 / rEscMin, u_tol(b)); the
+// two branches meet with a kink at b = b_kink, which cubic interpolation would smear. So psi and
+// phi0 are tabulated for each branch over the whole range (kExitPsi / kExitPhi0: the exit at
+// rEscMin, kExitPsiB / kExitPhi0B: at u_tol(b)), and a ray reads the branch its b lies on.
+constexpr int kExitPsi = kExitTableN, kExitPhi0 = 2 * kExitTableN, kExitIc = 3 * kExitTableN;
+constexpr int kExitRange = 4 * kExitTableN, kExitU2 = 5 * kExitTableN;
+constexpr int kExitPsiB = 6 * kExitTableN, kExitPhi0B = 7 * kExitTableN;
+constexpr int kExitTabEntries = 8 * kExitTableN;
+// Rays this many table spacings below the x2 of the camera's tangential ray (b = r_cam /
+// sqrt(1 - 2 / r_cam), whose turning point is the camera) go to the fallback march: the angle to
+// the turning point has a square-root end there, which the cubic interpolation does not follow.
+constexpr float kTangentMargin = 10.0f;
 // The crossing query of an escaping orbit, (x1, x2, sigma_k), is a function of (x2, sigma) per
 // view: tabulated on kCrossNx points of x2 (the escaping half's range) by kCrossNs of sigma in
 // [-1, 1], read by bilinear interpolation. Cell (i, j) holds its four corners (one 16-byte load).
@@ -75,7 +97,9 @@ struct SurrView {
     float x1;  // network input 1 of this view (scaled log r_cam)
     float uc;  // 1 / r_cam
     float u_esc_min;  // 1 / rEscMin of the tolerance escape (SHADER and CPU rules)
-    const float4* exit_table;  // [2][kExitTableN] (y, logit) of points i and i + 1
+    float b_kink;     // tolerance escape: b where the exit moves from rEscMin to u_tol(b)
+    float x2_lim;     // x2 above which rays fall back (kTangentMargin spacings below the tangential ray)
+    const float4* exit_table;  // the view's exit table (kExitTabEntries float4, layout above)
     float tab_lo[2], tab_h[2], tab_inv_h[2];  // x2 of a half's first point, spacing, 1 / spacing
     const float4* cross_table;  // [kCrossCells] y at the cell's corners (i, j), (i, j+1), (i+1, j), (i+1, j+1)
     float cx_h, cx_inv_h;       // the cross table's x2 spacing (first point tab_lo[1]) and its inverse
@@ -85,10 +109,12 @@ struct SurrView {
     double rhat_d[3];       // camera direction from the float camera position
     double b_scale_d;       // r_cam / sqrt(1 - 2 / r_cam)
 };
-cudaError_t launch_surrogate_trace(const SurrView& sv, const float* params, WorkQueue* q, int* fb_list, int grid,
+// The surrogate pass of one view (net: the learned variant, which reads the crossing table;
+// otherwise the converged closed form).
+cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_list, int grid, bool net,
                                    cudaStream_t st);
-// Fills the view's exit table (2 x kExitTableN rows through the network).
-cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, cudaStream_t st);
+// Fills the view's exit table (kExitTabEntries float4; with net, 2 x kExitTableN network rows).
+cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, bool net, cudaStream_t st);
 // Fills the view's crossing table (kCrossNx x kCrossNs rows through the network).
 cudaError_t launch_cross_table(const SurrView& sv, const float* params, float4* cells, cudaStream_t st);
 // x2 ranges of the two halves: captured beta in [-1, -band / sqrt 27], escaping in

@@ -39,7 +39,8 @@ struct bhr_surrogate {
     int last_nviews = 0;
     int* fb = nullptr;                    // fallback ray list
     int64_t fb_cap = 0;
-    float4* etab[2] = {nullptr, nullptr}; // per pipeline lane: the views' exit tables, [view][2][kExitTableN]
+    bool use_network = true;  // false: the non-learned variant (tables from the converged closed form)
+    float4* etab[2] = {nullptr, nullptr}; // per pipeline lane: the views' exit tables, [view][kExitTabEntries]
     int64_t etab_cap[2] = {0, 0};
     float4* ctab[2] = {nullptr, nullptr}; // per pipeline lane: the views' crossing tables, [view][kCrossCells]
     int64_t ctab_cap[2] = {0, 0};
@@ -61,6 +62,23 @@ struct bhr_surrogate {
 };
 
 namespace {
+
+// The b at which the tolerance escape's exit moves from rEscMin (u_esc_min) to u_tol(b): the root
+// of 0.75 b'^3 u^4 = tol at u = u_esc_min, b' = b / sqrt(1 + 2 b^2 u^3). The estimate rises with b
+// (its log-derivative is 3 / (b (1 + 2 b^2 u^3)) > 0), so bisection finds it; below sqrt(27)
+// or above 1e4 it is clamped there (one branch serves every escaping ray).
+float tolerance_kink(float tol, float u_esc_min) {
+    const double u = u_esc_min, t = tol;
+    auto est = [&](double b) { return 0.75 * std::pow(b / std::sqrt(1.0 + 2.0 * b * b * u * u * u), 3.0) * u * u * u * u; };
+    double lo = 5.196152422706632, hi = 1e4;
+    if (est(lo) >= t) return float(lo);
+    if (est(hi) < t) return float(hi);
+    for (int k = 0; k < 200; ++k) {
+        const double mid = 0.5 * (lo + hi);
+        (est(mid) < t ? lo : hi) = mid;
+    }
+    return float(0.5 * (lo + hi));
+}
 
 int fail(int code, const std::string& msg) {
     bhr::set_last_error(msg);
@@ -489,7 +507,7 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     const auto before = plan_memory();
     cudaError_t e = grow(&s->fb, &s->fb_cap, off[size_t(nviews)]);
     if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
-    constexpr int64_t kTab = 2 * bhr::surr::kExitTableN;  // table entries per view
+    constexpr int64_t kTab = bhr::surr::kExitTabEntries;  // table entries per view
     if (e == cudaSuccess) e = grow(&s->etab[lane], &s->etab_cap[lane], kTab * std::max<int64_t>(nviews, 64));
     constexpr int64_t kCells = bhr::surr::kCrossCells;
     if (e == cudaSuccess) e = grow(&s->ctab[lane], &s->ctab_cap[lane], kCells * std::max<int64_t>(nviews, 16));
@@ -513,6 +531,7 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
                           (std::log(double(s->norm.rc_hi)) - std::log(double(s->norm.rc_lo))) * 2.0 - 1.0);
         sv.uc = 1.0f / sv.view.rcam;
         sv.u_esc_min = sv.rule.r_esc_min > 0.0f ? 1.0f / sv.rule.r_esc_min : 1.0f;
+        sv.b_kink = views[k].term_mode == BHR_TERM_CONFIG ? 0.0f : tolerance_kink(sv.rule.esc_tol, sv.u_esc_min);
         sv.exit_table = s->etab[lane] + kTab * k;
         bhr::surr::exit_table_range(s->norm, sv.tab_lo, sv.tab_h);
         for (int h = 0; h < 2; ++h) sv.tab_inv_h[h] = 1.0f / sv.tab_h[h];
@@ -529,16 +548,22 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
             sv.rhat_d[1] = cy / rc;
             sv.rhat_d[2] = cz / rc;
             sv.b_scale_d = rc / std::sqrt(std::max(1.0 - 2.0 / rc, 1e-300));
+            // the camera's tangential ray has b = b_scale_d
+            const double beta_t = sv.b_scale_d / 5.196152422706632 - 1.0;
+            const double x2_t = std::log1p(beta_t / double(s->norm.t_eps)) * double(s->norm.t_scale);
+            sv.x2_lim = float(x2_t - double(bhr::surr::kTangentMargin) * double(sv.tab_h[1]));
         }
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
-        // the view's exit table, then its pass, on the same side stream
-        e = bhr::surr::launch_exit_table(sv, s->params, s->etab[lane] + kTab * k, s->side[lane][k & 1]);
-        if (e == cudaSuccess)
+        // the view's exit table (and, with the network, its crossing table), then its pass, on the
+        // same side stream
+        const bool net = s->use_network;
+        e = bhr::surr::launch_exit_table(sv, s->params, s->etab[lane] + kTab * k, net, s->side[lane][k & 1]);
+        if (e == cudaSuccess && net)
             e = bhr::surr::launch_cross_table(sv, s->params, s->ctab[lane] + kCells * k, s->side[lane][k & 1]);
         if (e == cudaSuccess)
-            e = bhr::surr::launch_surrogate_trace(sv, s->params, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3,
+            e = bhr::surr::launch_surrogate_trace(sv, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3, net,
                                                   s->side[lane][k & 1]);
     }
     for (int j = 0; e == cudaSuccess && j < 2; ++j) {
@@ -797,6 +822,12 @@ int bhr_surrogate_trace_host(bhr_surrogate* s, const bhr_view* views, int nviews
     return rc;
 }
 
+int bhr_surrogate_use_network(bhr_surrogate* s, int use_network) {
+    if (!s) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_use_network: NULL");
+    s->use_network = use_network != 0;
+    return BHR_OK;
+}
+
 int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
     if (!s || !out) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_stats: NULL");
     if (!s->have_last) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_stats: no trace yet");
@@ -816,7 +847,8 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
     }
     out[3] += q[2 * size_t(s->last_nviews)].steps;
     // the network runs in the views' tables: 2 kExitTableN + kCrossNx kCrossNs rows per view
-    const uint64_t rows = uint64_t(2 * bhr::surr::kExitTableN + bhr::surr::kCrossNx * bhr::surr::kCrossNs);
+    const uint64_t rows =
+        s->use_network ? uint64_t(2 * bhr::surr::kExitTableN + bhr::surr::kCrossNx * bhr::surr::kCrossNs) : 0;
     out[4] += rows * uint64_t(s->last_nviews);
     out[5] += rows * uint64_t(s->last_nviews);
     return BHR_OK;

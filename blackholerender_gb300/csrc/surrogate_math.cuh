@@ -178,6 +178,18 @@ __host__ __device__ __forceinline__ T base_sweep(T a, const Roots<T>& R, T blend
     return I1 + blend * (sweep_to_turn<T, kBaseDup + 1>(a, R) - I1);
 }
 
+// The closed form a surrogate variant evaluates: kNet (the learned path) the cheap baseline the
+// network corrects (base_sweep); otherwise the converged closed form, R_F with kClosedDup
+// duplication steps everywhere (error below 1e-8 rad on these orbits, no network).
+constexpr int kClosedDup = 3;
+template <bool kNet> struct Baseline {
+    template <class T>
+    static __host__ __device__ __forceinline__ T sweep(T a, const Roots<T>& R, T beta) {
+        if constexpr (kNet) return base_sweep<T>(a, R, base_blend<T>(beta));
+        else return sweep_to_turn<T, kClosedDup>(a, R);
+    }
+};
+
 // u at orbit coordinate sigma (see the file comment).
 template <class T>
 __host__ __device__ __forceinline__ T u_of_sigma(T sigma, T uc, const Roots<T>& R) {
@@ -229,6 +241,26 @@ template <class T>
 __host__ __device__ __forceinline__ T dudphi(T u, const Roots<T>& R) {
     const T p = T(2) * (u - R.u1) * (R.u2 - u) * (R.u3 - u);
     return tsqrt<T>(p > T(0) ? p : T(0));
+}
+
+// Solves I(u) = target for u in [0, u2] on a variant's closed form (Baseline<kNet>::sweep), by
+// Newton in s = sqrt(u2 - u) as invert_sweep below.
+template <class T, int kIters, bool kNet>
+__host__ __device__ __forceinline__ T invert_sweep_v(T target, const Roots<T>& R, T beta) {
+    const T X0 = (R.u2 - R.u1) * R.d32;
+    const T Z0 = R.d32 * (R.u2 - R.u1);
+    const T slope0 = T(1.4142135623730951) * rf<T, kBaseDup>(X0, X0, Z0);
+    const T smax = tsqrt<T>(R.u2);
+    T s = FM<T>::div(target, slope0);
+    s = s < T(0) ? T(0) : (s > smax ? smax : s);
+#pragma unroll 1
+    for (int k = 0; k < kIters; ++k) {
+        const T u = R.u2 - s * s;
+        const T f = Baseline<kNet>::template sweep<T>(u, R, beta) - target;
+        s -= f * T(0.5) * tsqrt<T>(T(2) * (u - R.u1) * (R.u3 - u));
+        s = s < T(0) ? T(0) : (s > smax ? smax : s);
+    }
+    return R.u2 - s * s;
 }
 
 // Solves I(u) = target for u in [0, u2] on the baseline (base_sweep), by Newton in

@@ -126,6 +126,11 @@ class Surrogate:
     def load(self, path):
         _abi.check(_abi.lib().bhr_surrogate_load(self.h, str(path).encode()))
 
+    def use_network(self, on: bool = True) -> None:
+        """bhr_surrogate_use_network: False traces with the non-learned variant (tables from the
+        converged closed form, no network)."""
+        _abi.check(_abi.lib().bhr_surrogate_use_network(self.h, int(bool(on))))
+
     def trace(self, views, outs=None, stream=None):
         """Surrogate-plus-fallback trace into device tensors (allocated if None); returns them."""
         import torch

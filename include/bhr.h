@@ -286,6 +286,12 @@ int bhr_surrogate_load(bhr_surrogate* s, const char* path);
  * 0.75 b'^3 / r^4 reaches esc_tol, b' the impact parameter at the current speed), then
  * farFieldDirection there. Other views: BHR_ERR_UNSUPPORTED (bhr_trace with
  * BHR_METHOD_SURROGATE sends them to the plain march instead). */
+/* Selects the variant bhr_surrogate_trace runs (no counterpart in the reference): use_network 1
+ * (the default) is the learned surrogate, whose network corrects a cheap closed form; 0 is the
+ * same pass with its per-view tables built from the converged closed form (Carlson R_F with three
+ * duplication steps) and no network: the non-learned orbit table the learned part is measured
+ * against. The fallback rays are the same. */
+int bhr_surrogate_use_network(bhr_surrogate* s, int use_network);
 int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
                         void* cuda_stream);
 /* Host-memory variant (records copied to out_host[k]; synchronous), as bhr_trace_host. */

@@ -32,6 +32,10 @@ def roots(beta):
     Written around the double root u = 1/3 of the critical orbit: with u = 1/3 + w,
     P = w^2 (1 + 2w) - D, D = 1/27 - 1/b^2 = beta (2 + beta) / (27 (1 + beta)^2), so the two
     roots near 1/3 are found relative to 1/3 without cancellation (Newton from +-sqrt(D)).
+    Away from it (beta >= 0.1) Newton from -sqrt(D) can step past w = -1/3, where the slope
+    vanishes, onto the wrong root; there the roots come from the trigonometric solution of the
+    cubic with a = asin(sqrt(27) / b) / 3: u2 = 2/3 sin(a) sin(2 pi/3 - a), u3 = 2/3 cos(a + pi/6)
+    cos(a - pi/6), u3 - u2 = sin(pi/3 - 2a) / sqrt(3).
     """
     beta = np.asarray(beta, dtype=np.float64)
     D = beta * (2.0 + beta) / (27.0 * (1.0 + beta) ** 2)
@@ -42,8 +46,14 @@ def roots(beta):
         wm = wm - (wm * wm * (1 + 2 * wm) - D) / (2 * wm + 6 * wm * wm)
     u2 = 1.0 / 3.0 + wm
     u3 = 1.0 / 3.0 + wp
+    d32 = wp - wm
+    a = np.arcsin(np.minimum(1.0 / (1.0 + np.maximum(beta, 1e-300)), 1.0)) / 3.0
+    far = beta >= 0.1
+    u2 = np.where(far, 2.0 / 3.0 * np.sin(a) * np.sin(2.0 * np.pi / 3.0 - a), u2)
+    u3 = np.where(far, 2.0 / 3.0 * np.cos(a + np.pi / 6.0) * np.cos(a - np.pi / 6.0), u3)
+    d32 = np.where(far, np.sin(np.pi / 3.0 - 2.0 * a) / np.sqrt(3.0), d32)
     u1 = 0.5 - u2 - u3  # roots of 2u^3 - u^2 + c sum to 1/2
-    return u1, u2, u3, wp - wm
+    return u1, u2, u3, d32
 
 
 def rf(x, y, z, ndup=None, tol=1e-16):
@@ -136,3 +146,67 @@ def cap_angle(u, uc, beta):
         return np.where(ct < 0.0, 2.0 * K - f0, f0)
 
     return (F(u) - F(uc)) / np.sqrt(2.0 * A)
+
+
+def exit_u_tol(b, tol, u_esc_min, u2):
+    """Exit u of the tolerance escape (SHADER and CPU rules) in the limit of small steps
+    (surrogate_math.cuh exit_u_tol): the outgoing leg's first u below 1 / rEscMin where
+    0.75 b'^3 u^4 < tol, b' = b / sqrt(1 + 2 b^2 u^3), and never before the turning point u2.
+    Solved here by bisection on the monotone estimate, independently of the kernel's iteration."""
+    b = np.asarray(b, dtype=np.float64)
+
+    def est(u):
+        return 0.75 * (b / np.sqrt(1.0 + 2.0 * b * b * u ** 3)) ** 3 * u ** 4
+
+    lo = np.zeros_like(b)
+    hi = np.full_like(b, 1.0)
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        below = est(mid) < tol
+        lo = np.where(below, mid, lo)
+        hi = np.where(below, hi, mid)
+    return np.minimum(np.minimum(lo, u_esc_min), u2)
+
+
+def far_field_dir(x, v, h2):
+    """farFieldDirection (shaders/geodesic.glsl:43-53, src/physics/Geodesic.h:65-75) on arrays of
+    vectors (last axis), normalised."""
+    vlen = np.linalg.norm(v, axis=-1, keepdims=True)
+    vh = v / vlen
+    r = np.linalg.norm(x, axis=-1, keepdims=True)
+    p = np.sum(x * vh, axis=-1, keepdims=True)
+    bvec = x - p * vh
+    s = np.clip(p / r, 0.0, 1.0)
+    r3 = r ** 3
+    h2 = np.asarray(h2, dtype=np.float64)[..., None]
+    dv = -(h2 / vlen) * (vh / r3 + bvec * ((2.0 + s) / (r3 * r * (1.0 + s) ** 2)))
+    o = v + dv
+    return o / np.linalg.norm(o, axis=-1, keepdims=True)
+
+
+def exit_geometry(beta, rc, ue, residual=0.0, sweep=None):
+    """The escaping orbit's answer in its orbital plane (e1 = the camera direction, e2 = the
+    tangential direction of the initial velocity), as a view's exit table holds it: (psi, phi0,
+    Ic), psi the angle of the escape direction from e1, phi0 the angle from the camera to the exit
+    at u = ue (the closed form plus the network's residual there), Ic the angle from the camera to
+    the turning point. The exit velocity follows the energy integral of x'' = -3 h^2 x / r^5,
+    |v|^2 = 1 - 2 h^2 / rc^3 + 2 h^2 u^3 with |v| = 1 at the camera and h^2 = b^2 / (1 + 2 b^2 / rc^3);
+    then farFieldDirection there."""
+    sweep = base_sweep if sweep is None else sweep
+    beta = np.asarray(beta, dtype=np.float64)
+    ue = np.broadcast_to(np.asarray(ue, dtype=np.float64), beta.shape)
+    b = SQRT27 * (1.0 + beta)
+    u1, u2, u3, _ = roots(beta)
+    Ic = sweep(1.0 / rc, beta)
+    phi0 = Ic + sweep(ue, beta) + residual
+    re = 1.0 / ue
+    c, s = np.cos(phi0), np.sin(phi0)
+    xe = np.stack([re * c, re * s, np.zeros_like(c)], -1)
+    sP = np.sqrt(np.maximum(2.0 * (ue - u1) * (u2 - ue) * (u3 - ue), 0.0))
+    T = np.stack([sP * re * re * c - re * s, sP * re * re * s + re * c, np.zeros_like(c)], -1)
+    h2 = b * b / (1.0 + 2.0 * b * b / rc ** 3)
+    vmag = np.sqrt(1.0 - 2.0 * h2 / rc ** 3 + 2.0 * h2 * ue ** 3)
+    T = T * (vmag / np.linalg.norm(T, axis=-1))[..., None]
+    d = far_field_dir(xe, T, h2)
+    gam = np.arctan2(c * d[..., 1] - s * d[..., 0], c * d[..., 0] + s * d[..., 1])
+    return phi0 + gam, phi0, Ic
