@@ -186,13 +186,15 @@ def _angle(a, b) -> np.ndarray:
     return np.arctan2(np.linalg.norm(np.cross(a, b), axis=1), np.sum(a * b, axis=1))
 
 
-def cpu_baseline_and_check(views, outs_s, outs_p, disagree_rad: float = 5e-5):
+def cpu_baseline_and_check(views, outs_s, outs_p, outs_c, disagree_rad: float = 5e-5, sample: int = 2000):
     """The cpu_baseline leg over the whole step: the FP64 CPU restatement of the march on every
     ray of the 16 views, on all host threads (timed: the CPU baseline), used afterwards as the
     checker of both GPU paths' records (the surrogate path's in outs_s, the plain FP32 path's in
     outs_p): classification of every ray, and the converged FP64 orbit (step scale 0.002, no slab
     clamp) on every ray where the two GPU paths' escape directions differ by more than
-    disagree_rad. Returns (cpu_baseline, accuracy)."""
+    disagree_rad. The non-learned comparator's records (outs_c) get the same classification check,
+    and both surrogate variants are compared with the converged orbit on `sample` random rays
+    per view. Returns (cpu_baseline, accuracy)."""
     from blackholerender_gb300 import FLAG_SURROGATE, HIT_DTYPE, hits_numpy
 
     L = _oracle()
@@ -200,9 +202,10 @@ def cpu_baseline_and_check(views, outs_s, outs_p, disagree_rad: float = 5e-5):
     t_cpu, t_conv, rays, steps = 0.0, 0.0, 0, 0
     acc = {"class_mismatch_full": 0, "class_mismatch_full_plain": 0, "rays_compared": 0, "rays_compared_plain": 0,
            "disagreeing_rays": 0, "converged_checked": 0, "surrogate_worst_vs_converged_rad": 0.0,
-           "plain_worst_vs_converged_rad": 0.0}
-    agree = []
-    for v, so, po in zip(views, outs_s, outs_p):
+           "plain_worst_vs_converged_rad": 0.0, "class_mismatch_full_closed_form": 0}
+    agree, samp_s, samp_c = [], [], []
+    rng = np.random.default_rng(0)
+    for v, so, po, co in zip(views, outs_s, outs_p, outs_c):
         ref = np.zeros(v.rays, dtype=HIT_DTYPE)
         t0 = time.perf_counter()
         rc = L.oracle_trace_view(ctypes.byref(v), ctypes.c_void_p(ref.ctypes.data), threads, 1)
@@ -218,6 +221,18 @@ def cpu_baseline_and_check(views, outs_s, outs_p, disagree_rad: float = 5e-5):
         m, n = class_mismatches(gp, ref, v, 1e-2, 1e-4)
         acc["class_mismatch_full_plain"] += m
         acc["rays_compared_plain"] += n
+        gc = hits_numpy(co.cpu())
+        acc["class_mismatch_full_closed_form"] += class_mismatches(gc, ref, v, 2e-3, 1e-3)[0]
+        fine = v.copy()
+        fine.step_scale, fine.ds_floor, fine.max_steps, fine.disk_mode = 0.002, 1e-4, 200000, 0
+        idx = np.ascontiguousarray(np.sort(rng.choice(v.rays, sample, replace=False)), dtype=np.int64)
+        conv = np.zeros(len(idx), dtype=HIT_DTYPE)
+        rc = L.oracle_trace_pixels(ctypes.byref(fine), ctypes.c_void_p(idx.ctypes.data), ctypes.c_int64(len(idx)),
+                                   ctypes.c_void_p(conv.ctypes.data), threads, 1)
+        assert rc == 0
+        ok = (conv["status"] == 1) & ((gs["flags"][idx] & FLAG_SURROGATE) != 0) & ((gc["flags"][idx] & FLAG_SURROGATE) != 0)
+        samp_s.append(_angle(gs["dir"][idx][ok], conv["dir"][ok]))
+        samp_c.append(_angle(gc["dir"][idx][ok], conv["dir"][ok]))
         both = np.nonzero(((gs["flags"] & FLAG_SURROGATE) != 0) & (gs["status"] == 1) & (gp["status"] == 1))[0]
         a = _angle(gs["dir"][both], gp["dir"][both])
         agree.append(a)
@@ -240,6 +255,13 @@ def cpu_baseline_and_check(views, outs_s, outs_p, disagree_rad: float = 5e-5):
                                                           float(es.max(initial=0.0)))
             acc["plain_worst_vs_converged_rad"] = max(acc["plain_worst_vs_converged_rad"], float(ep.max(initial=0.0)))
     agree = np.concatenate(agree)
+    samp_s, samp_c = np.concatenate(samp_s), np.concatenate(samp_c)
+    acc["sample_vs_converged_rad"] = {
+        "rays": int(len(samp_s)),
+        "learned": {"p50": float(np.percentile(samp_s, 50)), "p99": float(np.percentile(samp_s, 99)),
+                    "max": float(samp_s.max())},
+        "closed_form": {"p50": float(np.percentile(samp_c, 50)), "p99": float(np.percentile(samp_c, 99)),
+                        "max": float(samp_c.max())}}
     acc["agreement_vs_plain_fp32_rad"] = {"p50": float(np.percentile(agree, 50)), "p99": float(np.percentile(agree, 99)),
                                           "max": float(agree.max()), "rays": int(len(agree))}
     acc["converged_s"] = t_conv
@@ -441,6 +463,22 @@ def run_gpu(args):
     value = rays * world / (ms_per_step * 1e-3) / 1e6
     plain_value = rays * world / (plain_ms * 1e-3) / 1e6
 
+    # the non-learned comparator: the same pass with its views' tables built from the converged
+    # closed form (bhr_surrogate_use_network(0)), no network, the same fallback; its own records
+    outs_c = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, device=dev) for v in views]
+    sur.use_network(False)
+    plan_c = sur.plan(views, outs_c)
+    sur.use_network(True)
+    for _ in range(max(args.warmup, 0)):
+        plan_c.launch(stream)
+    per_cf, _ = timed(lambda: (plan_c.launch(stream), 0)[1], args.steps)
+    cf_ms = sum(per_cf) / args.steps
+    if dist:
+        t = torch.tensor([cf_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        cf_ms = float(t.item())
+    cf_value = rays * world / (cf_ms * 1e-3) / 1e6
+
     # ---- end to end through the host-buffer entry point (records in pinned host memory)
     host = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, pin_memory=True) for v in views]
     host_np = [h.numpy() for h in host]
@@ -521,7 +559,7 @@ def run_gpu(args):
 
     cpu, accuracy = None, None
     if not args.no_cpu and world == 1:
-        cpu, accuracy = cpu_baseline_and_check(views, outs, outs_p)
+        cpu, accuracy = cpu_baseline_and_check(views, outs, outs_p, outs_c)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -532,6 +570,9 @@ def run_gpu(args):
                   "plain_mrays_s": plain_value, "plain_ms_per_step": plain_ms,
                   "plain_launch_shape": plain_shape, "graph_plans": True,
                   "speedup_vs_plain": value / plain_value,
+                  "closed_form_mrays_s": cf_value, "closed_form_ms_per_step": cf_ms,
+                  "closed_form": "the same pass and fallback with the views' tables from the converged closed form "
+                                 "(Carlson R_F, three duplication steps), no network: the non-learned comparator",
                   "surrogate_fraction": st["surrogate"] / rays, "fallback_rays": st["fallback"],
                   "capture_flag_disagreements": st["capture_disagree"],
                   "checkpoint": "trained in this run" if trained_here else str(DEFAULT_CHECKPOINT.relative_to(ROOT)),
@@ -547,6 +588,7 @@ def run_gpu(args):
     }
     print(json.dumps(line), flush=True)
     plan_s.close()
+    plan_c.close()
     plan_p.close()
     if dist:
         dist.destroy_process_group()

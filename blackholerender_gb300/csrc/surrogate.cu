@@ -1176,7 +1176,7 @@ __device__ __forceinline__ float capture_logit(const SurrView& sv, float x2) {
 }
 
 template <bool kTol, bool kNet>
-__global__ void __launch_bounds__(32 * kInferWarps, 3) k_surrogate(const __grid_constant__ SurrView sv,
+__global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogate(const __grid_constant__ SurrView sv,
                                                                 WorkQueue* q, int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);

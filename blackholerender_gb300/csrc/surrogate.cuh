@@ -61,7 +61,7 @@ cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, 
 // captured one, depends on the view (x1) and on x2 alone: per view it is tabulated on
 // kExitTableN points of x2 for each half (0: captured, beta < 0; 1: escaping) and read back by
 // linear interpolation. Entry i of a half holds points i and i + 1 (one 16-byte load).
-constexpr int kExitTableN = 8192;
+constexpr int kExitTableN = 2048;
 // A view's exit table, in float4 entries (N = kExitTableN points per half):
 //   [0, N)          captured half: entry i = (y, capture logit) of points i and i + 1
 //   escaping half, over the points x2_i = tab_lo[1] + i tab_h[1]:
@@ -87,7 +87,7 @@ constexpr float kTangentMargin = 10.0f;
 // The crossing query of an escaping orbit, (x1, x2, sigma_k), is a function of (x2, sigma) per
 // view: tabulated on kCrossNx points of x2 (the escaping half's range) by kCrossNs of sigma in
 // [-1, 1], read by bilinear interpolation. Cell (i, j) holds its four corners (one 16-byte load).
-constexpr int kCrossNx = 512, kCrossNs = 128;
+constexpr int kCrossNx = 256, kCrossNs = 64;
 constexpr int kCrossCells = (kCrossNx - 1) * (kCrossNs - 1);
 
 struct SurrView {
@@ -109,6 +109,9 @@ struct SurrView {
     double rhat_d[3];       // camera direction from the float camera position
     double b_scale_d;       // r_cam / sqrt(1 - 2 / r_cam)
 };
+// Resident blocks per SM of the surrogate pass (its grid: SMs x this). Four fit (56 registers)
+// and measured 2% slower than three.
+constexpr int kSurrBlocksPerSM = 3;
 // The surrogate pass of one view (net: the learned variant, which reads the crossing table;
 // otherwise the converged closed form).
 cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_list, int grid, bool net,

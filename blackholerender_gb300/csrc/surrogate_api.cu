@@ -563,7 +563,8 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         if (e == cudaSuccess && net)
             e = bhr::surr::launch_cross_table(sv, s->params, s->ctab[lane] + kCells * k, s->side[lane][k & 1]);
         if (e == cudaSuccess)
-            e = bhr::surr::launch_surrogate_trace(sv, s->q + 2 * k, s->fb + off[size_t(k)], s->sms * 3, net,
+            e = bhr::surr::launch_surrogate_trace(sv, s->q + 2 * k, s->fb + off[size_t(k)],
+                                                  s->sms * bhr::surr::kSurrBlocksPerSM, net,
                                                   s->side[lane][k & 1]);
     }
     for (int j = 0; e == cudaSuccess && j < 2; ++j) {

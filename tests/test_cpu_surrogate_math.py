@@ -135,14 +135,13 @@ def _table_setup():
 
 @pytest.mark.parametrize("rcam", [15.0, 60.0])
 def test_exit_table_resolution(rcam):
-    """The surrogate pass reads each ray's exit query from a per-view table: 8,192 points of x2 per
-    half, linear interpolation. With the FP64 network (no BF16 rounding) the table stays within 1e-8
-    rad of direct evaluation on both halves, and no capture logit changes sign: the table adds
-    nothing measurable to the network's own error."""
+    """A captured ray reads its capture logit from its view's exit table: 2,048 points of x2 over
+    the captured half, linear interpolation. With the FP64 network (no BF16 rounding) no capture
+    logit changes sign against direct evaluation."""
     nm, P, x1_of, beta_of, esc, cap = _table_setup()
     x1 = x1_of(rcam)
     rng = np.random.default_rng(3)
-    for side, (lo, hi) in (("captured", cap), ("escaping", esc)):
+    for side, (lo, hi) in (("captured", cap),):
         def f(x2):
             beta = beta_of(x2)
             sig = np.ones_like(beta)
@@ -150,7 +149,7 @@ def test_exit_table_resolution(rcam):
                 u1, u2, u3, d32 = om.roots(beta)
                 sig = np.sqrt(np.maximum((u2 - nm["ue"]) / u2, 0.0))
             return mlp_ref.forward(P, np.stack([np.full_like(x2, x1), x2, sig], 1), quantize=False)[0]
-        n = 8192
+        n = 2048
         g = np.linspace(lo, hi, n)
         T = f(g)
         xs = rng.uniform(lo, hi, 4000)
@@ -159,20 +158,18 @@ def test_exit_table_resolution(rcam):
         i = np.clip(np.floor(u).astype(int), 0, n - 2)
         t = (u - i)[:, None]
         I = T[i] + t * (T[i + 1] - T[i])
-        err = np.abs(I[:, 0] - D[:, 0]) * nm["y_scale"]
-        assert err.max() < 1e-8, (side, err.max())
         assert np.all(np.sign(I[:, 1]) == np.sign(D[:, 1]))
 
 
 @pytest.mark.parametrize("rcam", [15.0, 60.0])
 def test_crossing_table_resolution(rcam):
-    """The crossing queries of escaping orbits come from a per-view 512 x 128 table over (x2,
-    sigma), bilinear: with the FP64 network within 1e-6 rad of direct evaluation at the 99th
-    percentile and 5e-6 at most, against the 1e-4 rad tolerance and the network's own ~5e-6 BF16
-    noise."""
+    """The crossing queries of escaping orbits come from a per-view 256 x 64 table over (x2,
+    sigma), bilinear: with the FP64 network within 2e-6 rad of direct evaluation at the 99th
+    percentile and 5e-6 at most (measured 1.1e-6 and 2.6e-6), against the 1e-4 rad tolerance and the
+    network's own ~3e-6 BF16 noise."""
     nm, P, x1_of, beta_of, esc, cap = _table_setup()
     x1 = x1_of(rcam)
-    nx, ns = 512, 128
+    nx, ns = 256, 64
     gx, gs = np.linspace(esc[0], esc[1], nx), np.linspace(-1.0, 1.0, ns)
     X, S = np.meshgrid(gx, gs, indexing="ij")
     T = mlp_ref.forward(P, np.stack([np.full(X.size, x1), X.ravel(), S.ravel()], 1), quantize=False)[0][:, 0]
@@ -187,7 +184,7 @@ def test_crossing_table_resolution(rcam):
     I = ((1 - a) * (1 - b) * T[i, j] + a * (1 - b) * T[i + 1, j] + (1 - a) * b * T[i, j + 1]
          + a * b * T[i + 1, j + 1])
     err = np.abs(I - D) * nm["y_scale"]
-    assert np.percentile(err, 99) < 1e-6 and err.max() < 5e-6, (np.percentile(err, 99), err.max())
+    assert np.percentile(err, 99) < 2e-6 and err.max() < 5e-6, (np.percentile(err, 99), err.max())
 
 
 def _cubic_table_lookup(T, lo, h, xs):
@@ -206,11 +203,11 @@ def _cubic_table_lookup(T, lo, h, xs):
 @pytest.mark.parametrize("rcam,rule", [(15.0, "config"), (60.0, "config"), (15.0, "shader"), (45.0, "cpu")])
 def test_escape_table_resolution(rcam, rule):
     """The surrogate pass reads an escaping ray's escape direction (psi), exit angle (phi0) and
-    angle to the turning point (Ic) from its view's exit table: 8,192 points of x2 over the
+    angle to the turning point (Ic) from its view's exit table: 2,048 points of x2 over the
     escaping half, cubic interpolation, the tolerance escape's two branches (exit at rEscMin, or
     where the estimate reaches esc_tol) tabulated apart, rays within ten spacings of the camera's
     tangential ray left to the plain march. With the FP64 network the table stays within 1e-6 rad
-    of direct evaluation (1e-9 at the 99th percentile), under the CONFIG rule's fixed exit and the
+    of direct evaluation (1e-7 at the 99th percentile; measured 6e-7 and 3e-8), under the CONFIG rule's fixed exit and the
     SHADER and CPU rules' tolerance escape: far below the 1e-4 rad bar and the network's own noise."""
     nm, P, x1_of, beta_of, esc, cap = _table_setup()
     x1 = x1_of(rcam)
@@ -231,7 +228,7 @@ def test_escape_table_resolution(rcam, rule):
         y = mlp_ref.forward(P, np.stack([np.full_like(x2, x1), x2, sig], 1), quantize=False)[0][:, 0]
         return om.exit_geometry(beta, rcam, ue, y * nm["y_scale"])
 
-    n = 8192
+    n = 2048
     lo, hi = esc
     h = (hi - lo) / (n - 1)
     g = lo + h * np.arange(n)
@@ -250,5 +247,5 @@ def test_escape_table_resolution(rcam, rule):
     for q, name in enumerate(("psi", "phi0", "Ic")):
         got = np.where(br == 1, _cubic_table_lookup(tabs[1][q], lo, h, xs), _cubic_table_lookup(tabs[0][q], lo, h, xs))
         err = np.abs(got - direct[q])
-        # worst next to the tangential ray's square-root end (3e-7 at ten spacings), 1e-10 elsewhere
-        assert err.max() < 1e-6 and np.percentile(err, 99) < 1e-9, (name, err.max(), np.percentile(err, 99))
+        # worst next to the tangential ray's square-root end (6e-7 at ten spacings)
+        assert err.max() < 1e-6 and np.percentile(err, 99) < 1e-7, (name, err.max(), np.percentile(err, 99))

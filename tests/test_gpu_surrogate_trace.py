@@ -189,7 +189,10 @@ def test_surrogate_near_the_photon_ring(surrogate):
     assert np.all(e_rule < DIR_MAX_RAD + e_rule_conv), (e_rule - e_rule_conv).max()
 
 
-def test_network_gain_over_closed_form_baseline(surrogate):
+def test_network_corrects_its_cheap_baseline(surrogate):
+    """What the network learns: on held-out integrator orbits, the exit angle of the one-step
+    closed form it corrects, with and without its residual (about 100x closer with it). The
+    comparison with the best method without a network is test_learned_vs_non_learned_comparator."""
     # held-out orbits from the integrator: polar-angle error at the exit with and without the network
     s = Surrogate(seed=4)
     s.generate(50_000, per_orbit=4, seed=987654)
@@ -403,3 +406,41 @@ def test_surrogate_needs_a_bound_surrogate_and_fp32():
         assert e.value.code == _abi.ERR_UNSUPPORTED
         tr.set_surrogate(None)
         s.close()
+
+
+def test_learned_vs_non_learned_comparator(surrogate):
+    """The learned surrogate against the best method without a network: the same pass with its
+    views' tables built from the converged closed form (bhr_surrogate_use_network(0), Carlson R_F
+    with three duplication steps), on 8 of the 1080p poses. Both must meet the 1e-4 rad bar against
+    the converged orbit with classification equal to the FP64 oracle; their speeds and errors are
+    printed side by side. The converged closed form is the more accurate of the two and costs no
+    network evaluations: on Schwarzschild orbits, which have exact elliptic-integral solutions, the
+    network adds no accuracy and no speed over it."""
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG)[:8]
+    outs = {}
+    times = {}
+    for net in (True, False):
+        surrogate.use_network(net)
+        o = surrogate.trace(views)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            surrogate.trace(views, o)
+        e1.record()
+        torch.cuda.synchronize()
+        times[net] = e0.elapsed_time(e1) / 3
+        outs[net] = [hits_numpy(x.cpu()) for x in o]
+    surrogate.use_network(True)
+    rng = np.random.default_rng(21)
+    err = {True: [], False: []}
+    for k, v in enumerate(views[:4]):
+        idx = rng.choice(v.rays, 1500, replace=False)
+        for net in (True, False):
+            st = parity.check_surrogate(outs[net][k], v, idx, where=f"network {net}, pose {k}")
+            err[net].append(st["dir_max"])
+    print(f"\n8 poses: learned {times[True]:.3f} ms (max {max(err[True]):.2e} rad vs converged), "
+          f"non-learned closed form {times[False]:.3f} ms (max {max(err[False]):.2e} rad)")
+    assert max(err[False]) < 1e-4 and max(err[True]) < 1e-4
