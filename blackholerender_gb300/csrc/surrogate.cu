@@ -1,14 +1,16 @@
 // Learned orbit surrogate for sm_103a: training data from the FP64 integrator, a fused BF16
-// tensor-core MLP (mma.sync m16n8k16, FP32 accumulation) for training and for the per-view tables
-// the trace reads, Adam, and the surrogate trace with its fallback list.
+// tensor-core training step (mma.sync m16n8k16, FP32 accumulation), Adam, the views' tables built
+// on the fifth-generation tensor cores (tcgen05, tc_mlp.cuh), and the surrogate trace with its
+// fallback list.
 //
 // Network (3 -> 64 -> 64 -> 64 -> 2, SiLU): inputs x1 = scaled log r_cam, x2 = scaled
 // sign(beta) ln(1 + |beta|/eps) with beta = b / sqrt(27) - 1, x3 = orbit coordinate sigma
 // (surrogate_math.cuh); outputs y = (polar angle of the integrated orbit - closed-form baseline)
-// / y_scale at sigma, and a capture logit. The first and last layers run in FP32 on the CUDA
-// cores, the two 64x64 layers in BF16 on the tensor cores, every activation rounded to BF16, exactly
-// as in training. SiLU uses the SFU tanh: silu(z) = h + h tanh(h) with h = z/2. In inference the
-// output layer runs on the tensor cores too, with W4 split into three BF16 parts (FP32 accuracy).
+// / y_scale at sigma, and a capture logit. The first layer runs in FP32 on the CUDA cores, the
+// two 64x64 layers in BF16 on the tensor cores, every activation rounded to BF16, identically in
+// training and inference. SiLU uses the SFU tanh: silu(z) = h + h tanh(h) with h = z/2. The output
+// layer is FP32 in training; in inference it runs on the tensor cores with W4 split into three
+// BF16 parts (FP32 accuracy).
 //
 // Fragment layout (PTX ISA, mma.m16n8k16 .bf16): with g = lane / 4, t = lane % 4, a thread holds
 // A rows g and g+8, columns 2t, 2t+1, 2t+8, 2t+9; B column g, rows 2t, 2t+1, 2t+8, 2t+9; C rows
@@ -16,6 +18,8 @@
 // A tiles (k = 16i..16i+15) from tiles 2i and 2i+1 without leaving registers.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "surrogate.cuh"
 #include "surrogate_math.cuh"
@@ -208,152 +212,6 @@ __device__ __forceinline__ void out_layer(const SmemNet& N, const float (&Z)[8][
     o[0][1] = pa1 + N.b4[1];
     o[1][0] = pb0 + N.b4[0];
     o[1][1] = pb1 + N.b4[1];
-}
-
-// ---------------------------------------------------------------------------------------
-// inference forward pass on half-scaled weights
-//
-// With W1, b1, W2, b2, W3, b3 multiplied by 1/2 when they are staged (exact in FP32 and BF16),
-// every hidden pre-activation comes out as h = z / 2 exactly (the FP32 accumulation of halved
-// products is the halved accumulation), so silu_pair_h takes the accumulators as they stand: the same
-// bits as the training kernel's activations, one multiply fewer per activation.
-
-// kFoldX1: every query of the launch has the same first input x1 (one view: x1 = scaled log r_cam),
-// so its term is folded into the first-layer bias and w1[f] holds {w_x2, w_sigma, w_x1 x1 + b, 0}/2.
-template <bool kFoldX1>
-__device__ void load_net_half(SmemNet& N, const float* __restrict__ P, float x1 = 0.f) {
-    for (int k = threadIdx.x; k < kH * kH; k += blockDim.x) {
-        const int o = k / kH, i = k % kH;
-        N.w2[o * kLd + i] = __float2bfloat16_rn(0.5f * P[kW2 + k]);
-        N.w3[o * kLd + i] = __float2bfloat16_rn(0.5f * P[kW3 + k]);
-    }
-    for (int f = threadIdx.x; f < kH; f += blockDim.x) {
-        if (kFoldX1)
-            N.w1[f] = make_float4(0.5f * P[kW1 + 3 * f + 1], 0.5f * P[kW1 + 3 * f + 2],
-                                  0.5f * fmaf(P[kW1 + 3 * f], x1, P[kB1 + f]), 0.f);
-        else
-            N.w1[f] = make_float4(0.5f * P[kW1 + 3 * f], 0.5f * P[kW1 + 3 * f + 1], 0.5f * P[kW1 + 3 * f + 2],
-                                  0.5f * P[kB1 + f]);
-        N.b2[f] = 0.5f * P[kB2 + f];
-        N.b3[f] = 0.5f * P[kB3 + f];
-        N.w4[f] = P[kW4 + f];
-        N.w4[kH + f] = P[kW4 + kH + f];
-    }
-    // W4 = hi + mid + lo, each part BF16 (the differences are exact in FP32)
-    for (int k = threadIdx.x; k < 8 * kH; k += blockDim.x) {
-        const int n = k / kH, i = k % kH;
-        __nv_bfloat16 v = __float2bfloat16_rn(0.f);
-        if (n < 6) {
-            const float w = P[kW4 + (n & 1) * kH + i];
-            const __nv_bfloat16 hi = __float2bfloat16_rn(w);
-            const float r1 = w - __bfloat162float(hi);
-            const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
-            v = n < 2 ? hi : n < 4 ? mid : __float2bfloat16_rn(r1 - __bfloat162float(mid));
-        }
-        N.w4s[n * kLd + i] = v;
-    }
-    if (threadIdx.x < kOut) N.b4[threadIdx.x] = P[kB4 + threadIdx.x];
-}
-
-__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
-    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(a));
-}
-
-// C = A W^T + bias for a 64x64 BF16 layer; the B fragments of four k-steps of an n-tile come from
-// two ldmatrix.x4 (lane L addresses row 8j + L%8, columns 8 (L/8) + 16 i0 of W[n][k]).
-__device__ __forceinline__ void mma_layer_ldsm(const __nv_bfloat16* W, const float* bias, const uint32_t (&A)[4][4],
-                                               float (&C)[8][4], int lane, int t) {
-    const __nv_bfloat16* wl = W + (lane & 7) * kLd + 8 * (lane >> 3);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const float c0 = bias[8 * j + 2 * t], c1 = bias[8 * j + 2 * t + 1];
-        C[j][0] = c0;
-        C[j][1] = c1;
-        C[j][2] = c0;
-        C[j][3] = c1;
-        uint32_t b[8];
-        ldsm_x4(b[0], b[1], b[2], b[3], wl + 8 * j * kLd);
-        ldsm_x4(b[4], b[5], b[6], b[7], wl + 8 * j * kLd + 32);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) mma_bf16(C[j], A[i], b[2 * i], b[2 * i + 1]);
-    }
-}
-
-// Forward pass of the queries q[0 .. 16 ntiles) in shared memory (q[r] = {x1, x2, sigma, -}),
-// one 16-row tile at a time; all 32 lanes. Rows past the caller's count compute garbage that
-// nobody reads.
-template <bool kFoldX1>
-__device__ void mlp_eval_tiles(const SmemNet& N, const float4* q, float2* out, int ntiles) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll 1
-    for (int mt = 0; mt < ntiles; ++mt) {
-        const int ra = 16 * mt + g, rb = ra + 8;
-        const float4 xa = q[ra], xb = q[rb];
-        uint32_t A[4][4];
-        float C[8][4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            float ha[4], hb[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int f = 16 * i + 2 * t + (k & 1) + ((k & 2) ? 8 : 0);
-                const float4 w = N.w1[f];
-                if (kFoldX1) {
-                    ha[k] = fmaf(w.x, xa.y, fmaf(w.y, xa.z, w.z));
-                    hb[k] = fmaf(w.x, xb.y, fmaf(w.y, xb.z, w.z));
-                } else {
-                    ha[k] = fmaf(w.x, xa.x, fmaf(w.y, xa.y, fmaf(w.z, xa.z, w.w)));
-                    hb[k] = fmaf(w.x, xb.x, fmaf(w.y, xb.y, fmaf(w.z, xb.z, w.w)));
-                }
-            }
-            A[i][0] = silu_pair_h(ha[0], ha[1]);
-            A[i][1] = silu_pair_h(hb[0], hb[1]);
-            A[i][2] = silu_pair_h(ha[2], ha[3]);
-            A[i][3] = silu_pair_h(hb[2], hb[3]);
-        }
-        mma_layer_ldsm(N.w2, N.b2, A, C, lane, t);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            A[i][0] = silu_pair_h(C[2 * i][0], C[2 * i][1]);
-            A[i][1] = silu_pair_h(C[2 * i][2], C[2 * i][3]);
-            A[i][2] = silu_pair_h(C[2 * i + 1][0], C[2 * i + 1][1]);
-            A[i][3] = silu_pair_h(C[2 * i + 1][2], C[2 * i + 1][3]);
-        }
-        mma_layer_ldsm(N.w3, N.b3, A, C, lane, t);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            A[i][0] = silu_pair_h(C[2 * i][0], C[2 * i][1]);
-            A[i][1] = silu_pair_h(C[2 * i][2], C[2 * i][3]);
-            A[i][2] = silu_pair_h(C[2 * i + 1][0], C[2 * i + 1][1]);
-            A[i][3] = silu_pair_h(C[2 * i + 1][2], C[2 * i + 1][3]);
-        }
-        // output layer on the tensor core: column 2p + o of the n = 8 tile is part p of output o;
-        // the quad's lanes t hold parts t, so the outputs are the sums over t (b4 enters at t = 0)
-        float O[4];
-        O[0] = O[2] = t == 0 ? N.b4[0] : 0.f;
-        O[1] = O[3] = t == 0 ? N.b4[1] : 0.f;
-        {
-            const __nv_bfloat16* wl = N.w4s + (lane & 7) * kLd + 8 * (lane >> 3);
-            uint32_t b[8];
-            ldsm_x4(b[0], b[1], b[2], b[3], wl);
-            ldsm_x4(b[4], b[5], b[6], b[7], wl + 32);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) mma_bf16(O, A[i], b[2 * i], b[2 * i + 1]);
-        }
-#pragma unroll
-        for (int m = 1; m <= 2; m <<= 1) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) O[c] += __shfl_xor_sync(0xffffffffu, O[c], m);
-        }
-        if (t == 0) {
-            out[ra] = make_float2(O[0], O[1]);
-            out[rb] = make_float2(O[2], O[3]);
-        }
-    }
-    __syncwarp();
 }
 
 // ---------------------------------------------------------------------------------------
@@ -805,10 +663,12 @@ __global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ 
                                                       const tc::TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     tc::Net& N = *reinterpret_cast<tc::Net*>(smem_raw);
-    tc::Tile& T = *reinterpret_cast<tc::Tile*>(smem_raw + sizeof(tc::Net));
+    tc::L1& l1 = *reinterpret_cast<tc::L1*>(smem_raw + sizeof(tc::Net));
+    tc::Tile& T = *reinterpret_cast<tc::Tile*>(smem_raw + sizeof(tc::Net) + sizeof(tc::L1));
     __shared__ uint32_t tmem_slot;
     __shared__ int fail;
     tc::load_net(N, P, false, 0.f);
+    tc::load_l1(l1, P);
     if (threadIdx.x == 0) {
         tc::mbar_init(tc::smem_u32(&T.mbar), 1);
         fail = 0;
@@ -824,7 +684,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ 
         const int row = t0 + int(threadIdx.x);
         const float4 x = row < n ? q[row] : make_float4(0.f, 0.f, 0.f, 0.f);
         float2 o;
-        const bool ok = tc::mlp_tile(N, T, tmem, int(threadIdx.x), 1, phase, x, o, ctl);
+        const bool ok = tc::mlp_tile_l1f(N, l1, T, tmem, int(threadIdx.x), 1, phase, x, o, ctl);
         if (!ok) fail = 1;
         if (row < n) out[row] = ok ? o : make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
         __syncthreads();
@@ -1013,14 +873,6 @@ __device__ __forceinline__ void put_pair(float* T, int i, float a, float c) {
     }
 }
 
-// The view's exit table (layout in surrogate.cuh). Captured half (kNet only): the network's
-// (y, capture logit) at sigma = 1 per point. Escaping half: per point, the beta it encodes (the
-// inverse of the x2 transform) and from it the roots, the exit u of the rule, the variant's closed
-// form from the camera to the turning point, to the exit and to the disk's radii, the network's
-// residual at the exit (kNet), the exit angle, and the escape direction in the orbital plane:
-// the exit position and velocity (energy integral of x'' = -3 h^2 x / r^5 with h^2 =
-// b^2 / (1 + 2 b^2 / r_cam^3)), then farFieldDirection (geodesic.glsl:43-53) there, measured from
-// the radial direction at the exit so that the angle stays continuous in x2.
 // The in-plane escape direction (its angle from e1, e1 = the camera direction and e2 the ray's
 // tangential direction) of an escaping orbit that leaves the march at u = ue at angle phi0 from
 // the camera: the exit position and velocity (energy integral of x'' = -3 h^2 x / r^5 with
@@ -1043,104 +895,153 @@ __device__ __forceinline__ float escape_angle(float phi0, float ue, const orbit:
     return phi0 + atan2f(cp * d.y - sp * d.x, cp * d.x + sp * d.y);
 }
 
-// The view's exit table (layout in surrogate.cuh). Captured half (kNet only): the network's
-// (y, capture logit) at sigma = 1 per point. Escaping half: per point, the beta it encodes (the
-// inverse of the x2 transform) and from it the roots, the exit u of the rule (with kTol, of each
-// branch of the tolerance escape), the variant's closed form from the camera to the turning
-// point, to the exit and to the disk's radii, the network's residual at the exit (kNet), the exit
-// angle and the escape direction (escape_angle). Each point is written into every entry it
-// belongs to.
-template <bool kTol, bool kNet>
-__global__ void __launch_bounds__(256) k_exit_table(const __grid_constant__ SurrView sv, const float* __restrict__ P,
-                                                    float4* __restrict__ table) {
-    constexpr int kQ = kTol ? 2 : 1;  // exit queries per point: one per branch of the rule's exit
-    __shared__ __align__(16) SmemNet N;
-    __shared__ float4 qs[8][32 * kQ];
-    __shared__ float2 os[8][32 * kQ];
-    if (kNet) {
-        load_net_half<true>(N, P, sv.x1);
-        __syncthreads();
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// The exit table (layout in surrogate.cuh) of the non-learned variant: per point of the escaping
+// half, the beta it encodes (the inverse of the x2 transform) and from it the roots, the exit u of
+// the rule (with kTol, of each branch of the tolerance escape), the converged closed form from the
+// camera to the turning point, to the exit and to the disk's radii, the exit angle and the escape
+// direction (escape_angle). Each point is written into every entry it belongs to. (The learned
+// variant's tables, with the network, come from k_tables.)
+template <bool kTol>
+__global__ void __launch_bounds__(256) k_exit_table_cf(const __grid_constant__ SurrView sv, float4* __restrict__ table) {
+    constexpr int kQ = kTol ? 2 : 1;  // exits per point: one per branch of the rule's exit
     const Norm& nm = sv.norm;
     float* T = reinterpret_cast<float*>(table);
     constexpr float kPi = 3.14159265358979f;
-    for (int base = (blockIdx.x * 8 + warp) * 32; base < 2 * kExitTableN; base += gridDim.x * 8 * 32) {
-        const int k = base + lane;  // 2 kExitTableN is a multiple of 32: a warp stays on one half
-        const int side = k / kExitTableN, i = k - side * kExitTableN;
-        if (!kNet && side == 0) continue;  // the converged closed form classifies captured orbits itself
-        const float x2 = fmaf(float(i), sv.tab_h[side], sv.tab_lo[side]);
-        const float mag = nm.t_eps * expm1f(fabsf(x2) / nm.t_scale);
-        float sig[2] = {1.0f, 1.0f};  // the capture flag is trained at sigma = 1
-        float ue[2] = {0.f, 0.f};
-        float b = 0.f, beta = 0.f, Ic = 0.f, ilo = 0.f, ihi = 0.f;
-        orbit::Roots<float> Rt{};
-        using B = orbit::Baseline<kNet>;
-        if (side == 1) {
-            beta = fmaxf(mag, 1e-7f);
-            b = kSqrt27f * (1.0f + beta);
-            Rt = orbit::roots<float, 4>(beta);
-            if (kTol) {
-                ue[0] = fminf(sv.u_esc_min, Rt.u2);
-                ue[1] = orbit::exit_u_tol<float>(b, sv.rule.esc_tol, 1.0f, Rt.u2);
-            } else {
-                ue[0] = nm.ue;
-            }
-            for (int r = 0; r < kQ; ++r) sig[r] = orbit::sigma_exit<float>(ue[r], Rt);
-            Ic = B::template sweep<float>(sv.uc, Rt, beta);
-            ilo = B::template sweep<float>(fminf(1.0f / (sv.rule.disk_inner * 0.97f), Rt.u2), Rt, beta);
-            ihi = B::template sweep<float>(fminf(1.0f / (sv.rule.disk_outer * 1.03f), Rt.u2), Rt, beta);
-        }
-        float2 o[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        if (kNet) {
-            for (int r = 0; r < kQ; ++r) qs[warp][32 * r + lane] = make_float4(sv.x1, x2, sig[r], 0.f);
-            __syncwarp();
-            mlp_eval_tiles<true>(N, qs[warp], os[warp], 2 * kQ);
-            for (int r = 0; r < kQ; ++r) o[r] = os[warp][32 * r + lane];
-        }
-        if (side == 0) {
-            put_pair<true>(T, i, o[0].x, o[0].y);
+    using B = orbit::Baseline<false>;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kExitTableN; i += gridDim.x * blockDim.x) {
+        const float x2 = fmaf(float(i), sv.tab_h[1], sv.tab_lo[1]);
+        const float beta = fmaxf(nm.t_eps * expm1f(x2 / nm.t_scale), 1e-7f);
+        const float b = kSqrt27f * (1.0f + beta);
+        const orbit::Roots<float> Rt = orbit::roots<float, 4>(beta);
+        float ue[2];
+        if (kTol) {
+            ue[0] = fminf(sv.u_esc_min, Rt.u2);
+            ue[1] = orbit::exit_u_tol<float>(b, sv.rule.esc_tol, 1.0f, Rt.u2);
         } else {
-            const int rule_branch = kTol && b > sv.b_kink ? 1 : 0;
-            for (int r = 0; r < kQ; ++r) {
-                const float phi0 = Ic + B::template sweep<float>(ue[r], Rt, beta) + o[r].x * nm.y_scale;
-                const float psi = escape_angle(phi0, ue[r], Rt, b, sv.view.two_over_r3);
-                put_cubic(T + 4 * (r ? kExitPsiB : kExitPsi), i, psi - kPi);
-                put_cubic(T + 4 * (r ? kExitPhi0B : kExitPhi0), i, phi0);
-            }
-            put_cubic(T + 4 * kExitIc, i, Ic);
-            put_pair<true>(T + 4 * kExitRange, i, ilo, ihi);
-            put_pair<false>(T + 4 * kExitU2, i, Rt.u2, o[rule_branch].y);
+            ue[0] = nm.ue;
         }
-        __syncwarp();
+        const float Ic = B::template sweep<float>(sv.uc, Rt, beta);
+        for (int r = 0; r < kQ; ++r) {
+            const float phi0 = Ic + B::template sweep<float>(ue[r], Rt, beta);
+            const float psi = escape_angle(phi0, ue[r], Rt, b, sv.view.two_over_r3);
+            put_cubic(T + 4 * (r ? kExitPsiB : kExitPsi), i, psi - kPi);
+            put_cubic(T + 4 * (r ? kExitPhi0B : kExitPhi0), i, phi0);
+        }
+        put_cubic(T + 4 * kExitIc, i, Ic);
+        put_pair<true>(T + 4 * kExitRange, i, B::template sweep<float>(fminf(1.0f / (sv.rule.disk_inner * 0.97f), Rt.u2), Rt, beta),
+                       B::template sweep<float>(fminf(1.0f / (sv.rule.disk_outer * 1.03f), Rt.u2), Rt, beta));
+        put_pair<false>(T + 4 * kExitU2, i, Rt.u2, 0.f);
     }
 }
 
-// The view's crossing table: the network's y at (x2_i, sigma_j) = (lo + i hx, -1 + j hs), each point
-// written into the (up to four) cells it is a corner of.
-__global__ void __launch_bounds__(256) k_cross_table(const __grid_constant__ SurrView sv, const float* __restrict__ P,
-                                                     float4* __restrict__ cells) {
-    __shared__ __align__(16) SmemNet N;
-    __shared__ float4 qs[8][32];
-    __shared__ float2 os[8][32];
-    load_net_half<true>(N, P, sv.x1);
+// The learned surrogate's tables of a batch of views in one launch on the tensor cores: every
+// view's exit table (the escaping half per branch of the rule's exit, the captured half) and
+// crossing table, as 128-row tiles of network queries. A block is one warpgroup with its own TMEM
+// accumulator; it stages the network once (tc::load_net, tc::load_l1) and then takes tiles until
+// the batch is done. Each thread forms its row's query (for an escaping exit point the closed form
+// of the point, as k_exit_table), the tile runs through tc::mlp_tile_l1f, and each thread writes
+// its row's results into the entries of the table that hold them (as k_exit_table and
+// k_cross_table do). A completion wait that runs out makes the block write NaN for its tile, set
+// *status and stop.
+__global__ void __launch_bounds__(128, 4) k_tables(const __grid_constant__ TabBatch B, const float* __restrict__ P,
+                                                   int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tc::Net& N = *reinterpret_cast<tc::Net*>(smem_raw);
+    tc::L1& l1 = *reinterpret_cast<tc::L1*>(smem_raw + sizeof(tc::Net));
+    tc::Tile& T = *reinterpret_cast<tc::Tile*>(smem_raw + sizeof(tc::Net) + sizeof(tc::L1));
+    __shared__ uint32_t tmem_slot;
+    __shared__ int fail;
+    tc::load_net(N, P, false, 0.f);
+    tc::load_l1(l1, P);
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_u32(&T.mbar), 1);
+        fail = 0;
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(tc::smem_u32(&tmem_slot), tc::kTmemCols);
+    tc::fence_smem_async();
+    tc::fence_before();
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int W = kCrossNs - 1;  // cells per row
+    tc::fence_after();
+    const uint32_t tmem = tmem_slot;
+    uint32_t phase = 0;
+    const Norm& nm = B.norm;
+    const int row = int(threadIdx.x);
+    constexpr float kPi = 3.14159265358979f;
     const float hs = 2.0f / float(kCrossNs - 1);
-    float* c = reinterpret_cast<float*>(cells);
-    for (int base = (blockIdx.x * 8 + warp) * 32; base < kCrossNx * kCrossNs; base += gridDim.x * 8 * 32) {
-        const int k = base + lane;  // kCrossNx kCrossNs is a multiple of 32
-        const int i = k / kCrossNs, j = k - i * kCrossNs;
-        qs[warp][lane] = make_float4(sv.x1, fmaf(float(i), sv.cx_h, sv.tab_lo[1]), fmaf(float(j), hs, -1.0f), 0.f);
-        __syncwarp();
-        mlp_eval_tiles<true>(N, qs[warp], os[warp], 2);
-        const float y = os[warp][lane].x;
-        if (i < kCrossNx - 1 && j < W) c[4 * (i * W + j) + 0] = y;
-        if (i < kCrossNx - 1 && j > 0) c[4 * (i * W + j - 1) + 1] = y;
-        if (i > 0 && j < W) c[4 * ((i - 1) * W + j) + 2] = y;
-        if (i > 0 && j > 0) c[4 * ((i - 1) * W + j - 1) + 3] = y;
-        __syncwarp();
+    for (int tile = blockIdx.x; tile < B.ntiles; tile += gridDim.x) {
+        int v = 0;
+        while (v + 1 < B.nviews && B.v[v + 1].tile0 <= tile) ++v;
+        const TabView& V = B.v[v];
+        const int t = tile - V.tile0;
+        const int nesc = kTabTilesExit * (V.tol ? 2 : 1);
+        // kind 0: an escaping exit point (branch r); 1: a captured exit point; 2: a crossing cell corner
+        const int kind = t < nesc ? 0 : (t < nesc + kTabTilesExit ? 1 : 2);
+        const int r = kind == 0 ? t / kTabTilesExit : 0;
+        int i = 0, jj = 0;
+        float x2, sigma = 1.0f;  // the capture flag is trained at sigma = 1
+        float b = 0.f, beta = 0.f, Ic = 0.f, Ie = 0.f, ue = 0.f;
+        orbit::Roots<float> Rt{};
+        if (kind == 0) {
+            i = (t - r * kTabTilesExit) * 128 + row;
+            x2 = fmaf(float(i), B.tab_h[1], B.tab_lo[1]);
+            beta = fmaxf(nm.t_eps * expm1f(x2 / nm.t_scale), 1e-7f);
+            b = kSqrt27f * (1.0f + beta);
+            Rt = orbit::roots<float, 4>(beta);
+            ue = !V.tol ? nm.ue : (r == 0 ? fminf(V.u_esc_min, Rt.u2) : orbit::exit_u_tol<float>(b, V.esc_tol, 1.0f, Rt.u2));
+            sigma = orbit::sigma_exit<float>(ue, Rt);
+            using Bl = orbit::Baseline<true>;
+            Ic = Bl::template sweep<float>(V.uc, Rt, beta);
+            Ie = Bl::template sweep<float>(ue, Rt, beta);
+        } else if (kind == 1) {
+            i = (t - nesc) * 128 + row;
+            x2 = fmaf(float(i), B.tab_h[0], B.tab_lo[0]);
+        } else {
+            const int c = (t - nesc - kTabTilesExit) * 128 + row;
+            i = c / kCrossNs;
+            jj = c - i * kCrossNs;
+            x2 = fmaf(float(i), B.cx_h, B.tab_lo[1]);
+            sigma = fmaf(float(jj), hs, -1.0f);
+        }
+        float2 o;
+        const bool ok = tc::mlp_tile_l1f(N, l1, T, tmem, row, 1, phase, make_float4(V.x1, x2, sigma, 0.f), o);
+        if (!ok) {
+            fail = 1;
+            o = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+        }
+        if (kind == 0) {
+            float* E = reinterpret_cast<float*>(V.exit_table);
+            const float phi0 = Ic + Ie + o.x * nm.y_scale;
+            const float psi = escape_angle(phi0, ue, Rt, b, V.two_over_r3);
+            put_cubic(E + 4 * (r ? kExitPsiB : kExitPsi), i, psi - kPi);
+            put_cubic(E + 4 * (r ? kExitPhi0B : kExitPhi0), i, phi0);
+            if (r == 0) {
+                using Bl = orbit::Baseline<true>;
+                put_cubic(E + 4 * kExitIc, i, Ic);
+                put_pair<true>(E + 4 * kExitRange, i,
+                               Bl::template sweep<float>(fminf(1.0f / (V.disk_inner * 0.97f), Rt.u2), Rt, beta),
+                               Bl::template sweep<float>(fminf(1.0f / (V.disk_outer * 1.03f), Rt.u2), Rt, beta));
+            }
+            if (r == (V.tol && b > V.b_kink ? 1 : 0)) put_pair<false>(E + 4 * kExitU2, i, Rt.u2, o.y);
+        } else if (kind == 1) {
+            put_pair<true>(reinterpret_cast<float*>(V.exit_table), i, o.x, o.y);
+        } else {
+            constexpr int W = kCrossNs - 1;  // cells per row
+            float* c = reinterpret_cast<float*>(V.cross_table);
+            const float y = o.x;
+            if (i < kCrossNx - 1 && jj < W) c[4 * (i * W + jj) + 0] = y;
+            if (i < kCrossNx - 1 && jj > 0) c[4 * (i * W + jj - 1) + 1] = y;
+            if (i > 0 && jj < W) c[4 * ((i - 1) * W + jj) + 2] = y;
+            if (i > 0 && jj > 0) c[4 * ((i - 1) * W + jj - 1) + 3] = y;
+        }
+        __syncthreads();
+        if (fail) break;
+    }
+    if (fail && threadIdx.x == 0) atomicExch(status, 1);
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, tc::kTmemCols);
     }
 }
 
@@ -1481,17 +1382,22 @@ cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_cross_table(const SurrView& sv, const float* params, float4* cells, cudaStream_t st) {
-    k_cross_table<<<kCrossNx * kCrossNs / 256, 256, 0, st>>>(sv, params, cells);  // one point per thread
+cudaError_t launch_exit_table_cf(const SurrView& sv, float4* table, cudaStream_t st) {
+    const int grid = (kExitTableN + 255) / 256;  // one point per thread
+    if (sv.rule.term_mode != BHR_TERM_CONFIG) k_exit_table_cf<true><<<grid, 256, 0, st>>>(sv, table);
+    else k_exit_table_cf<false><<<grid, 256, 0, st>>>(sv, table);
     return cudaGetLastError();
 }
 
-cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, bool net, cudaStream_t st) {
-    const bool tol = sv.rule.term_mode != BHR_TERM_CONFIG;
-    using K = void (*)(SurrView, const float*, float4*);
-    const K kern = tol ? (net ? K(k_exit_table<true, true>) : K(k_exit_table<true, false>))
-                       : (net ? K(k_exit_table<false, true>) : K(k_exit_table<false, false>));
-    kern<<<2 * kExitTableN / 256, 256, 0, st>>>(sv, params, table);  // one point per thread
+cudaError_t launch_tables(const TabBatch& b, const float* params, int* status, int grid, cudaStream_t st) {
+    const int smem = int(sizeof(tc::Net) + sizeof(tc::L1) + sizeof(tc::Tile));
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_tables<<<std::max(1, std::min(grid, b.ntiles)), 128, smem, st>>>(b, params, status);
     return cudaGetLastError();
 }
 
@@ -1500,7 +1406,7 @@ cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, 
     tc::TileCtl ctl;
     if (wait_cycles > 0) ctl.wait_cycles = wait_cycles;
     ctl.withhold = withhold;
-    k_mlp_infer<<<grid, 128, sizeof(tc::Net) + sizeof(tc::Tile), st>>>(params, q, out, n, status, ctl);
+    k_mlp_infer<<<grid, 128, sizeof(tc::Net) + sizeof(tc::L1) + sizeof(tc::Tile), st>>>(params, q, out, n, status, ctl);
     return cudaGetLastError();
 }
 

@@ -109,6 +109,30 @@ struct SurrView {
     double rhat_d[3];       // camera direction from the float camera position
     double b_scale_d;       // r_cam / sqrt(1 - 2 / r_cam)
 };
+// The learned surrogate's tables of up to kTabMaxViews views, built by one launch on the tensor
+// cores (surrogate.cu k_tables): per view its exit table (escaping half: one tile of 128 points
+// per branch of the rule's exit; captured half) and crossing table, 128-row tiles of network
+// queries, each tile through the tcgen05 network (tc_mlp.cuh mlp_tile_l1f).
+constexpr int kTabMaxViews = 64;
+struct TabView {
+    float x1, uc, u_esc_min, esc_tol, b_kink, two_over_r3, disk_inner, disk_outer;
+    int32_t tol;    // the tolerance escape (SHADER and CPU rules): two exit branches
+    int32_t tile0;  // the view's first tile in the launch
+    float4* exit_table;
+    float4* cross_table;
+};
+struct TabBatch {
+    int32_t nviews, ntiles;
+    Norm norm;
+    float tab_lo[2], tab_h[2], cx_h;
+    TabView v[kTabMaxViews];
+};
+// tiles of one view: kExitTableN / 128 per exit branch, kExitTableN / 128 captured, the crossing cells' rows
+constexpr int kTabTilesExit = kExitTableN / 128, kTabTilesCross = kCrossNx * kCrossNs / 128;
+inline int tab_tiles(bool tol) { return kTabTilesExit * (tol ? 3 : 2) + kTabTilesCross; }
+// Builds the batch's tables; *status becomes 1 if a tensor-core completion wait ran out (the
+// tables are then NaN where it did).
+cudaError_t launch_tables(const TabBatch& b, const float* params, int* status, int grid, cudaStream_t st);
 // Resident blocks per SM of the surrogate pass (its grid: SMs x this). Four fit (56 registers)
 // and measured 2% slower than three.
 constexpr int kSurrBlocksPerSM = 3;
@@ -116,10 +140,8 @@ constexpr int kSurrBlocksPerSM = 3;
 // otherwise the converged closed form).
 cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_list, int grid, bool net,
                                    cudaStream_t st);
-// Fills the view's exit table (kExitTabEntries float4; with net, 2 x kExitTableN network rows).
-cudaError_t launch_exit_table(const SurrView& sv, const float* params, float4* table, bool net, cudaStream_t st);
-// Fills the view's crossing table (kCrossNx x kCrossNs rows through the network).
-cudaError_t launch_cross_table(const SurrView& sv, const float* params, float4* cells, cudaStream_t st);
+// Fills the view's exit table for the non-learned variant (the converged closed form, no network).
+cudaError_t launch_exit_table_cf(const SurrView& sv, float4* table, cudaStream_t st);
 // x2 ranges of the two halves: captured beta in [-1, -band / sqrt 27], escaping in
 // [band / sqrt 27, b_max / sqrt 27 - 1].
 inline void exit_table_range(const Norm& nm, float lo[2], float h[2]) {

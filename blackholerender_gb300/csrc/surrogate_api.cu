@@ -32,6 +32,7 @@ struct bhr_surrogate {
     int8_t* lab = nullptr;
     int64_t n_samples = 0;
     unsigned long long* stats = nullptr;  // data generation counters (device, 4)
+    int* tab_status = nullptr;            // set on the device when a table build's tensor-core wait ran out
     float* loss = nullptr;                // per-step loss sums (device, 3 * loss_cap)
     int loss_cap = 0;
     bhr::WorkQueue* q = nullptr;          // per view of a trace: [2v] surrogate pass, [2v+1] fallback march
@@ -175,6 +176,8 @@ int bhr_surrogate_create(bhr_surrogate** out, int device, const bhr_surrogate_co
     if (e == cudaSuccess) e = cudaMalloc(&s->adam_m, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMalloc(&s->adam_v, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMalloc(&s->stats, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&s->tab_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(s->tab_status, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(s->params, P.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(s->adam_m, 0, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMemset(s->adam_v, 0, sizeof(float) * kNParams);
@@ -196,7 +199,8 @@ int bhr_surrogate_destroy(bhr_surrogate* s) {
     if (!s) return BHR_OK;
     DevGuard dg(s->device);
     for (void* p : {(void*)s->params, (void*)s->grads, (void*)s->adam_m, (void*)s->adam_v, (void*)s->X,
-                    (void*)s->lab, (void*)s->stats, (void*)s->loss, (void*)s->q, (void*)s->fb, (void*)s->staging,
+                    (void*)s->lab, (void*)s->stats, (void*)s->tab_status, (void*)s->loss, (void*)s->q, (void*)s->fb,
+                    (void*)s->staging,
                     (void*)s->etab[0], (void*)s->etab[1], (void*)s->ctab[0], (void*)s->ctab[1]})
         if (p) cudaFree(p);
     for (cudaEvent_t& e : s->ev)
@@ -514,15 +518,15 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     if (plan_memory() != before) ++s->work_gen;
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
     e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->tab_status, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
-    if (e == cudaSuccess) e = cudaEventRecord(s->fork[lane], st);
-    for (int j = 0; e == cudaSuccess && j < 2; ++j) e = cudaStreamWaitEvent(s->side[lane][j], s->fork[lane], 0);
-    // 1) the surrogate pass of every view, alternating between the two side streams
+    // the views' constants
+    std::vector<bhr::surr::SurrView> svs(static_cast<size_t>(nviews));
     std::vector<bhr::DevView> dvs(static_cast<size_t>(nviews));
     std::vector<bhr::Rule> rules(static_cast<size_t>(nviews));
     bool one_rule = true;
-    for (int k = 0; e == cudaSuccess && k < nviews; ++k) {
-        bhr::surr::SurrView sv{};
+    for (int k = 0; k < nviews; ++k) {
+        bhr::surr::SurrView& sv = svs[size_t(k)];
         sv.view = bhr::host::make_dev_view(views[k], out_dev[k]);
         sv.view.list_off = off[size_t(k)];
         sv.rule = bhr::host::make_rule(views[k]);
@@ -556,23 +560,60 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
-        // the view's exit table (and, with the network, its crossing table), then its pass, on the
-        // same side stream
-        const bool net = s->use_network;
-        e = bhr::surr::launch_exit_table(sv, s->params, s->etab[lane] + kTab * k, net, s->side[lane][k & 1]);
-        if (e == cudaSuccess && net)
-            e = bhr::surr::launch_cross_table(sv, s->params, s->ctab[lane] + kCells * k, s->side[lane][k & 1]);
+    }
+    // 1) the learned surrogate's tables of every view: one launch on the tensor cores per 64 views
+    const bool net = s->use_network;
+    if (net) {
+        static thread_local bhr::surr::TabBatch tb;
+        for (int k0 = 0; e == cudaSuccess && k0 < nviews; k0 += bhr::surr::kTabMaxViews) {
+            const int k1 = std::min(nviews, k0 + bhr::surr::kTabMaxViews);
+            tb.nviews = k1 - k0;
+            tb.norm = s->norm;
+            for (int h = 0; h < 2; ++h) {
+                tb.tab_lo[h] = svs[0].tab_lo[h];
+                tb.tab_h[h] = svs[0].tab_h[h];
+            }
+            tb.cx_h = svs[0].cx_h;
+            int tiles = 0;
+            for (int k = k0; k < k1; ++k) {
+                const bhr::surr::SurrView& sv = svs[size_t(k)];
+                bhr::surr::TabView& tv = tb.v[k - k0];
+                tv.x1 = sv.x1;
+                tv.uc = sv.uc;
+                tv.u_esc_min = sv.u_esc_min;
+                tv.esc_tol = sv.rule.esc_tol;
+                tv.b_kink = sv.b_kink;
+                tv.two_over_r3 = sv.view.two_over_r3;
+                tv.disk_inner = sv.rule.disk_inner;
+                tv.disk_outer = sv.rule.disk_outer;
+                tv.tol = views[k].term_mode != BHR_TERM_CONFIG;
+                tv.tile0 = tiles;
+                tv.exit_table = s->etab[lane] + kTab * k;
+                tv.cross_table = s->ctab[lane] + kCells * k;
+                tiles += bhr::surr::tab_tiles(tv.tol != 0);
+            }
+            tb.ntiles = tiles;
+            e = bhr::surr::launch_tables(tb, s->params, s->tab_status, s->sms * 4, st);
+        }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(s->fork[lane], st);
+    for (int j = 0; e == cudaSuccess && j < 2; ++j) e = cudaStreamWaitEvent(s->side[lane][j], s->fork[lane], 0);
+    // 2) the surrogate pass of every view (the non-learned variant builds its exit table first),
+    // alternating between the two side streams
+    for (int k = 0; e == cudaSuccess && k < nviews; ++k) {
+        const bhr::surr::SurrView& sv = svs[size_t(k)];
+        cudaStream_t vs = s->side[lane][k & 1];
+        if (!net) e = bhr::surr::launch_exit_table_cf(sv, s->etab[lane] + kTab * k, vs);
         if (e == cudaSuccess)
             e = bhr::surr::launch_surrogate_trace(sv, s->q + 2 * k, s->fb + off[size_t(k)],
-                                                  s->sms * bhr::surr::kSurrBlocksPerSM, net,
-                                                  s->side[lane][k & 1]);
+                                                  s->sms * bhr::surr::kSurrBlocksPerSM, net, vs);
     }
     for (int j = 0; e == cudaSuccess && j < 2; ++j) {
         e = cudaEventRecord(s->join[lane][j], s->side[lane][j]);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, s->join[lane][j], 0);
     }
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
-    // 2) the integrator on the fallback rays: one launch for all views when they share a rule
+    // 3) the integrator on the fallback rays: one launch for all views when they share a rule
     // the fallback rays are few and the near-critical ones long: claims of 32 spread them over
     // as many warps as possible, so the launch ends with its slowest ray, not a warp's queue
     bhr::LaunchCfg cfg{};
@@ -834,9 +875,14 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
     if (!s->have_last) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_stats: no trace yet");
     DevGuard dg(s->device);
     std::vector<bhr::WorkQueue> q(2 * size_t(s->last_nviews) + 1);
+    int tab_status = 0;
     cudaError_t e = cudaStreamSynchronize(s->last_stream);
     if (e == cudaSuccess) e = cudaMemcpy(q.data(), s->q, sizeof(bhr::WorkQueue) * q.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&tab_status, s->tab_status, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace_stats");
+    if (tab_status)
+        return fail(BHR_ERR_TIMEOUT, "bhr_surrogate_trace_stats: a tensor-core completion wait of the table build ran out "
+                                     "(the affected table entries are NaN)");
     for (int k = 0; k < 6; ++k) out[k] = 0;
     for (int v = 0; v < s->last_nviews; ++v) {
         out[0] += q[2 * v].surr_rays;

@@ -7,8 +7,9 @@
 // tcgen05.commit; the threads then read their row back with tcgen05.ld, apply SiLU in FP32, and
 // write the BF16 activations as the next layer's A operand.
 //
-// Precision: the network computes the same function as the mma.sync path and training, with the
-// pieces that were FP32 on the CUDA cores moved into the MMAs as split BF16 products:
+// The production form (mlp_tile_l1f) keeps layer 1 in FP32 on the CUDA cores, as training does,
+// and runs layers 2, 3 and the output layer on the tensor cores. The all-tensor-core form
+// (mlp_tile) moves the pieces that are FP32 on the CUDA cores into the MMAs as split BF16 products:
 //   - layer 1: each input x = xh + xl and weight w = wh + wl (BF16 parts); the products
 //     xh wh + xl wh + xh wl take 9 of the 16 K slots, the bias three more (below). The dropped
 //     xl wl term is below 2^-18 of the product;
@@ -250,6 +251,90 @@ __device__ __forceinline__ void act_to_a(uint32_t taddr, unsigned char* a, int r
 
 constexpr uint32_t kI64 = idesc_bf16(128, 64);
 constexpr uint32_t kI16 = idesc_bf16(128, 16);
+
+// Layer 1 in FP32 on the CUDA cores, as the training kernel and the mma.sync path compute it:
+// per feature f, {w_x1, w_x2, w_sigma, b1} / 2 (halved, so that the pre-activation comes out as
+// h = z / 2 and silu(z) = fma(h, tanh h, h)).
+struct L1 {
+    float4 w[kH];
+};
+__device__ inline void load_l1(L1& L, const float* __restrict__ P) {
+    for (int f = threadIdx.x; f < kH; f += blockDim.x)
+        L.w[f] = make_float4(0.5f * P[kW1 + 3 * f], 0.5f * P[kW1 + 3 * f + 1], 0.5f * P[kW1 + 3 * f + 2],
+                             0.5f * P[kB1 + f]);
+}
+
+// The output layer and layers 2 and 3 on the tensor cores, from the A rows already in T.a;
+// shared by both tile forms below. Returns false if a completion wait ran out.
+__device__ inline bool mlp_tile_upper(const Net& N, Tile& T, uint32_t tmem, int row, int bar_id, uint32_t& phase,
+                                      float2& out, const TileCtl& ctl) {
+    unsigned char* a = reinterpret_cast<unsigned char*>(T.a);
+    const uint32_t a_s = smem_u32(T.a), mbar = smem_u32(&T.mbar);
+    const uint32_t taddr = tmem + (uint32_t((row >> 5) * 32) << 16);
+    const bool issuer = row == 0 && !ctl.withhold;
+    bool ok = true;
+    const uint16_t* W[2] = {N.w2, N.w3};
+    const uint16_t* B[2] = {N.b2, N.b3};
+#pragma unroll 1
+    for (int l = 0; l < 2; ++l) {  // layers 2 and 3
+        fence_smem_async();
+        fence_before();
+        wg_sync(bar_id);
+        if (issuer) {
+            fence_after();
+            const uint32_t w_s = smem_u32(W[l]);
+#pragma unroll
+            for (int s = 0; s < 4; ++s) mma(tmem, sdesc(a_s + 256u * s, 128, 1024), sdesc(w_s + 256u * s, 128, 1024), kI64, s);
+            mma(tmem, sdesc(smem_u32(N.ones), 128, 256), sdesc(smem_u32(B[l]), 128, 256), kI64, 1u);
+            commit(mbar);
+        }
+        ok &= mbar_wait(mbar, phase, ctl.wait_cycles);
+        phase ^= 1u;
+        fence_after();
+        act_to_a(taddr, a, row);
+    }
+    // output layer: columns 2p + o hold part p of output o
+    fence_smem_async();
+    fence_before();
+    wg_sync(bar_id);
+    if (issuer) {
+        fence_after();
+        const uint32_t w_s = smem_u32(N.w4);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) mma(tmem, sdesc(a_s + 256u * s, 128, 1024), sdesc(w_s + 256u * s, 128, 1024), kI16, s);
+        mma(tmem, sdesc(smem_u32(N.ones), 128, 256), sdesc(smem_u32(N.b4), 128, 256), kI16, 1u);
+        commit(mbar);
+    }
+    ok &= mbar_wait(mbar, phase, ctl.wait_cycles);
+    phase ^= 1u;
+    fence_after();
+    float c[8];
+    tmem_ld8(taddr, c);
+    out = make_float2(c[0] + c[2] + c[4], c[1] + c[3] + c[5]);
+    fence_before();
+    return ok;
+}
+
+// One 128-row tile with layer 1 in FP32 on the CUDA cores (the same arithmetic, the same BF16
+// activations as training and the mma.sync path) and layers 2, 3 and the output layer on the
+// tensor cores. Called by all 128 threads of a warpgroup with their own row's query; the other
+// arguments as mlp_tile's. The production form: the surrogate's tables and bhr_surrogate_eval.
+__device__ inline bool mlp_tile_l1f(const Net& N, const L1& l1, Tile& T, uint32_t tmem, int row, int bar_id,
+                                    uint32_t& phase, float4 x, float2& out, const TileCtl& ctl = TileCtl{}) {
+    unsigned char* a = reinterpret_cast<unsigned char*>(T.a);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {  // features 8c .. 8c + 7: one 16-byte chunk of the row
+        float h[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float4 w = l1.w[8 * c + k];
+            h[k] = fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, w.w)));
+        }
+        *reinterpret_cast<uint4*>(a + kmaj(row, 8 * c, 8)) =
+            make_uint4(silu_pack(h[0], h[1]), silu_pack(h[2], h[3]), silu_pack(h[4], h[5]), silu_pack(h[6], h[7]));
+    }
+    return mlp_tile_upper(N, T, tmem, row, bar_id, phase, out, ctl);
+}
 
 // One 128-row tile through the network, called by all 128 threads of a warpgroup with their own
 // row's query x = {x1, x2, sigma}; the warpgroup's named barrier is bar_id, its accumulator the

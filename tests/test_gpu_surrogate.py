@@ -30,10 +30,15 @@ def test_gradients_match_fp64_reference():
     loss_c, g_cpu = mlp_ref.loss_and_grad(p, samples, labels, 0.05, quantize=True)
     assert abs(loss_g[2] - loss_c[2]) < 0.5
     assert abs(loss_g[0] - loss_c[0]) < 1e-2 * loss_c[0] + 1e-6
+    rels = {}
     for name, (o, sz) in mlp_ref.OFF.items():
         a, b = g_gpu[o:o + sz].astype(np.float64), g_cpu[o:o + sz]
         cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30)
-        assert _rel(a, b) < 3e-2 and cos > 0.999, (name, _rel(a, b), cos)
+        rels[name] = _rel(a, b)
+        # the reference mirrors the kernel's BF16 roundings; what differs is the order of the FP32
+        # sums and the SFU tanh: measured at most 2.9e-3 (b1), 1.5e-5 to 2e-3 elsewhere
+        assert _rel(a, b) < 1e-2 and cos > 0.9999, (name, _rel(a, b), cos)
+    print("\ngradient relative L2 error per tensor: " + ", ".join(f"{k} {v:.1e}" for k, v in rels.items()))
     # forward pass of the inference kernel against the same reference
     q = samples[:64, :3]
     out = s.eval(q)
@@ -78,9 +83,10 @@ def test_short_training_reduces_loss():
 
 
 def test_tensor_core_forward_pass_matches_reference():
-    """The evaluation kernel runs the network on tcgen05 (128-row tiles, TMEM accumulators, the
-    first layer and the biases as split BF16 products): against the FP64 network with the GPU's
-    BF16 roundings, on 8192 queries of the trained range."""
+    """The evaluation kernel runs the network exactly as the production table build (k_tables)
+    does: 128-row tiles through tc::mlp_tile_l1f, layer 1 in FP32 on the CUDA cores, layers 2 and 3
+    and the output layer on tcgen05 with TMEM accumulators, biases and W4 as split BF16 parts.
+    Against the FP64 network with the GPU's BF16 roundings, on 8192 queries of the trained range."""
     from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT
     s = Surrogate(seed=1)
     s.load(str(DEFAULT_CHECKPOINT))

@@ -444,3 +444,26 @@ def test_learned_vs_non_learned_comparator(surrogate):
     print(f"\n8 poses: learned {times[True]:.3f} ms (max {max(err[True]):.2e} rad vs converged), "
           f"non-learned closed form {times[False]:.3f} ms (max {max(err[False]):.2e} rad)")
     assert max(err[False]) < 1e-4 and max(err[True]) < 1e-4
+
+
+def test_every_record_written_exactly_once(surrogate):
+    """Every ray of the 16 poses gets one record, from the surrogate or from the plain march of its
+    fallback rays (the band pre-pass lists the photon-sphere band, the pass the rays it declines):
+    the outputs start as stale bytes, and afterwards every record carries exactly one of the two
+    flags, a valid status, and the fallback flags count the statistics' fallback rays."""
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG)
+    outs = [torch.full((v.rays * 64,), 0xAB, dtype=torch.uint8, device="cuda") for v in views]
+    surrogate.trace(views, outs)
+    torch.cuda.synchronize()
+    st = surrogate.trace_stats()
+    n_fb = 0
+    for o in outs:
+        g = hits_numpy(o.cpu())
+        s_ = (g["flags"] & FLAG_SURROGATE) != 0
+        f_ = (g["flags"] & FLAG_FALLBACK) != 0
+        assert np.all(s_ ^ f_)
+        assert np.all(np.isin(g["status"], (1, 2, 3)))
+        n_fb += int(f_.sum())
+    assert n_fb == st["fallback"] and st["surrogate"] + st["fallback"] == sum(v.rays for v in views), (n_fb, st)
