@@ -412,7 +412,9 @@ def run_gpu(args):
 
     def step_surrogate():
         plan_s.launch(stream)
-        return 3 * len(views) + 1  # per view its exit and crossing tables and its pass, + one fallback march
+        # one table launch per 64 views (every view's exit and crossing tables), one pass per
+        # view, one fallback march for all views
+        return (len(views) + 63) // 64 + len(views) + 1
 
     def step_plain():
         plan_p.launch(stream)
@@ -537,15 +539,16 @@ def run_gpu(args):
                             "are 64 B x 2.07 M rays = 133 MB per view, part of the dirty lines still in L2 when "
                             "the kernel ends",
             "peak_source": hbm_src,
-            "kernel": "k_surrogate with its k_exit_table and k_cross_table (one of each per view; ms below is the "
-                      "16-view pass)",
+            "kernel": "k_surrogate (one launch per view) with k_tables (every view's exit and crossing tables in "
+                      "one launch); pass_ms is the 16 views' passes with their table launch",
             "algorithm": f"{HIT_BYTES} B written per ray (the hit record), {rays} rays per step",
             "pass_ms": t_pass, "fallback_ms": t_fb,
             "tensor": {"achieved": tensor_achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                        "frac": tensor_achieved / bf16_peak, "peak_source": bf16_src,
                        "algorithm": f"{F_MLP} BF16 FLOP per network row; {st['mlp_queries']} rows "
                                     f"({st['mlp_queries'] / max(st['surrogate'], 1):.3f} per surrogate ray: the views' "
-                                    f"exit and crossing tables, 81920 rows per view, which the rays interpolate)"},
+                                    f"exit and crossing tables, {st['mlp_queries'] // max(len(views), 1)} rows per "
+                                    f"view, which the rays interpolate)"},
             "note": "the pass is latency-bound on the CUDA cores (ray setup, closed-form orbit, the tables' loads, "
                     "the records); neither HBM nor the tensor pipe is its limit"}
     plan_p.launch(stream)

@@ -1169,18 +1169,15 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
                 }
             }
             // disk-plane crossings: y(phi) = 0 at phi_k = phi_n + k pi
-            float phin = atan2f(-e1.y, e2.y);
+            float phin = orbit::atan_ratio(-e1.y, e2.y);  // the nodal line's angle, taken in [0, pi)
             if (phin < 0.f) phin += kPi;
             if (phin >= kPi) phin -= kPi;
             sur = sur && (fabsf(e1.y) + fabsf(e2.y)) > 1e-6f;
             int nplane = 0;
             uint32_t cw = 0;
             if (sur) {
-#pragma unroll 1
-                for (int k = 0; k < 16; ++k) {
-                    if (phin + float(k) * kPi >= phi0) break;
-                    ++nplane;
-                }
+                // crossings k = 0, 1, ... with phin + k pi < phi0 (at most 16)
+                if (phi0 > phin) nplane = min(int(ceilf((phi0 - phin) * (1.0f / kPi))), 16);
                 if (!cap && thin && nplane > 0) {
                     // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
                     // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
@@ -1264,7 +1261,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
                 sincos_rr(phk, &s2, &c2);
                 const float hx = rs * (c2 * w.rhat[0] + s2 * G.e2x[own]);
                 const float hz = rs * (c2 * w.rhat[2] + s2 * G.e2z[own]);
-                ph = atan2f(hz, hx);
+                ph = orbit::atan2_fast(hz, hx);
                 rr = rs;
             }
             tu[t] = rr;

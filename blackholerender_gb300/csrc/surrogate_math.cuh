@@ -326,6 +326,40 @@ __host__ __device__ __forceinline__ T cap_F(T u, const CapOrbit<T>& o) {
     return cth < T(0) ? T(2) * o.K - f0 : f0;
 }
 
+// Arctangent in float for the surrogate's per-ray angles: range reduction to a = min / max of
+// |y|, |x| in [0, 1] (atan(1/a) = pi/2 - atan(a)), then atan(a) = a + a s Q(s), s = a^2, with Q of
+// degree 7 fitted to (atan(a) - a) / (a s) by least squares weighted by a s on 4000 Chebyshev
+// nodes of [0, 1] (a near-minimax fit; its float evaluation stays within 7e-8 rad of atan,
+// checked against numpy's arctan by tests/test_cpu_surrogate_math.py, which reads these constants).
+// atan(a) for a in [0, 1]
+__host__ __device__ __forceinline__ float atan_unit(float a) {
+    const float s = a * a;
+    // Q(s) = c0 + c1 s + ... + c7 s^7, Horner from c7
+    float q = 0.002599463565275073f;
+    q = q * s + -0.015040560625493526f;
+    q = q * s + 0.04097096249461174f;
+    q = q * s + -0.07353820651769638f;
+    q = q * s + 0.1056785061955452f;
+    q = q * s + -0.1418442726135254f;
+    q = q * s + 0.19990207254886627f;
+    q = q * s + -0.33332979679107666f;
+    return a + a * s * q;
+}
+// atan(y / x) in [-pi/2, pi/2]
+__host__ __device__ __forceinline__ float atan_ratio(float y, float x) {
+    const float ax = x < 0.f ? -x : x, ay = y < 0.f ? -y : y;
+    const float mx = ax > ay ? ax : ay, mn = ax > ay ? ay : ax;
+    float r = mx > 0.f ? atan_unit(FM<float>::div(mn, mx)) : 0.f;
+    if (ay > ax) r = 1.57079632679489662f - r;
+    return (x < 0.f) != (y < 0.f) ? -r : r;
+}
+// atan2(y, x) in (-pi, pi]
+__host__ __device__ __forceinline__ float atan2_fast(float y, float x) {
+    const float r = atan_ratio(y, x);
+    if (x >= 0.f) return r;
+    return y >= 0.f ? r + 3.14159265358979f : r - 3.14159265358979f;
+}
+
 // Monotone transform of b / sqrt(27): t = sign(beta) ln(1 + |beta| / eps).
 template <class T>
 __host__ __device__ __forceinline__ T b_transform(T beta, T eps) {

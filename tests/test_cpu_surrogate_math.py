@@ -249,3 +249,33 @@ def test_escape_table_resolution(rcam, rule):
         err = np.abs(got - direct[q])
         # worst next to the tangential ray's square-root end (6e-7 at ten spacings)
         assert err.max() < 1e-6 and np.percentile(err, 99) < 1e-7, (name, err.max(), np.percentile(err, 99))
+
+
+def test_own_arctangent_within_its_bound():
+    """The surrogate's per-ray angles use an own arctangent (surrogate_math.cuh atan_unit, a
+    degree-7 polynomial in a^2 fitted to atan on [0, 1]): its coefficients are read from the header
+    and its float32 evaluation, Horner as the kernel does, stays within 1e-7 rad of numpy's arctan
+    over [0, 1], and refitting by the documented method gives the same coefficients."""
+    import re
+    from pathlib import Path
+
+    text = (Path(__file__).resolve().parent.parent / "blackholerender_gb300" / "csrc" / "surrogate_math.cuh").read_text()
+    body = text[text.index("float atan_unit(float a)"):]
+    body = body[:body.index("return")]
+    c = [float(v) for v in re.findall(r"(-?\d+\.\d+(?:e-?\d+)?)f", body)][::-1]  # Horner runs c7 .. c0
+    assert len(c) == 8
+    x = np.linspace(0, 1, 400001).astype(np.float32)
+    s = (x * x).astype(np.float32)
+    q = np.float32(c[7])
+    for k in range(6, -1, -1):
+        q = (q * s + np.float32(c[k])).astype(np.float32)
+    r = (x + (x * s).astype(np.float32) * q).astype(np.float32)
+    assert np.abs(r.astype(np.float64) - np.arctan(x.astype(np.float64))).max() < 1e-7
+    # the fit: weighted least squares on 4000 Chebyshev nodes of [0, 1]
+    n = 4000
+    a = 0.5 * (1 - np.cos(np.pi * (np.arange(n) + 0.5) / n))
+    ss = a * a
+    w = a * ss
+    A = np.vander(ss, 8, increasing=True)
+    fit, *_ = np.linalg.lstsq(A * w[:, None], (np.arctan(a) - a) / (a * ss) * w, rcond=None)
+    assert np.allclose(fit, c, rtol=1e-5, atol=1e-7)
