@@ -18,6 +18,8 @@
 
 #include <map>
 #include <mutex>
+#include <set>
+#include <utility>
 
 #include "kernels.cuh"
 #include "march.cuh"
@@ -392,23 +394,26 @@ __global__ void __launch_bounds__(512) k_march_list(const __grid_constant__ DevV
     __shared__ float s_pool[512 / 32][kPoolFields * kPool];
     const int wid = threadIdx.x >> 5;
     const int64_t n = (int64_t)*list_len;
+    if (n == 0) return;
     const int64_t total_chunks = (n + chunk - 1) / chunk;
     march_warp<false, kTerm, kDisk, false, true>(&view, 1, total_chunks, rule, sc, chunk, refill_min,
                                                  Pool{s_pool[wid], nullptr}, list, n);
 }
 
 // The surrogate's fallback rays of several views in one launch: view v's list is
-// list[list_off_v .. list_off_v + qv[2v].fb_count) (counts written on the device).
-template <int kTerm, int kDisk>
-__global__ void __launch_bounds__(512) k_march_multi_list(const __grid_constant__ ViewBatch batch, const Scratch sc,
-                                                          const int* list, const WorkQueue* qv, int chunk,
-                                                          int refill_min) {
-    __shared__ float s_pool[512 / 32][kPoolFields * kPool];
-    __shared__ uint8_t s_pool_view[512 / 32][kPool];
+// list[list_off_v .. list_off_v + qv[2v].fb_count) (counts written on the device). 512-thread
+// blocks after the surrogate pass; 64-thread blocks for the band march beside it, which holds
+// few warps and must leave the SMs' registers to the pass.
+template <int BS, int kTerm, int kDisk>
+__global__ void __launch_bounds__(BS) k_march_multi_list(const __grid_constant__ ViewBatch batch, const Scratch sc,
+                                                         const int* list, const WorkQueue* qv, int chunk,
+                                                         int refill_min) {
+    __shared__ float s_pool[BS / 32][kPoolFields * kPool];
+    __shared__ uint8_t s_pool_view[BS / 32][kPool];
     __shared__ DevView s_views[kMaxViews];
     __shared__ int64_t s_total;
     const int nwords = batch.nviews * (int)(sizeof(DevView) / 4);
-    for (int k = threadIdx.x; k < nwords; k += 512)
+    for (int k = threadIdx.x; k < nwords; k += BS)
         reinterpret_cast<uint32_t*>(s_views)[k] = reinterpret_cast<const uint32_t*>(batch.views)[k];
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -422,6 +427,7 @@ __global__ void __launch_bounds__(512) k_march_multi_list(const __grid_constant_
         s_total = acc;
     }
     __syncthreads();
+    if (s_total == 0) return;  // an empty list (the usual case after the band march): no claims on the counter
     const int wid = threadIdx.x >> 5;
     march_warp<true, kTerm, kDisk, false, true>(s_views, batch.nviews, s_total, batch.rule, sc, chunk, refill_min,
                                                 Pool{s_pool[wid], s_pool_view[wid]}, list, 0);
@@ -537,18 +543,44 @@ cudaError_t launch_march_list(const DevView& v, const Rule& r, const Scratch& s,
     return cudaLaunchKernel(fn, dim3(grid), dim3(512), args, 0, st);
 }
 
+namespace {
+template <int BS>
+const void* multi_list_kernel(int variant) {
+    switch (variant) {
+        case kVariantConfigThin: return (const void*)k_march_multi_list<BS, BHR_TERM_CONFIG, BHR_DISK_THIN>;
+        case kVariantShaderThin: return (const void*)k_march_multi_list<BS, BHR_TERM_SHADER, BHR_DISK_THIN>;
+        case kVariantCpuNone: return (const void*)k_march_multi_list<BS, BHR_TERM_CPU, BHR_DISK_NONE>;
+        default: return (const void*)k_march_multi_list<BS, -1, -1>;
+    }
+}
+}  // namespace
+
 cudaError_t launch_march_multi_list(const ViewBatch& b, const Scratch& s, const int* list, const WorkQueue* qv,
                                     const LaunchCfg& c, cudaStream_t st) {
     int chunk = c.chunk, refill = c.refill;
-    const void* fn;
-    switch (c.variant) {
-        case kVariantConfigThin: fn = (const void*)k_march_multi_list<BHR_TERM_CONFIG, BHR_DISK_THIN>; break;
-        case kVariantShaderThin: fn = (const void*)k_march_multi_list<BHR_TERM_SHADER, BHR_DISK_THIN>; break;
-        case kVariantCpuNone: fn = (const void*)k_march_multi_list<BHR_TERM_CPU, BHR_DISK_NONE>; break;
-        default: fn = (const void*)k_march_multi_list<-1, -1>; break;
+    if (c.block != 64 && c.block != 512) return cudaErrorInvalidValue;
+    const void* fn = c.block == 64 ? multi_list_kernel<64>(c.variant) : multi_list_kernel<512>(c.variant);
+    if (c.block == 64) {  // the band march, beside the surrogate pass
+        const cudaError_t e = prefer_max_smem(fn, 0, true);
+        if (e != cudaSuccess) return e;
     }
     void* args[] = {(void*)&b, (void*)&s, (void*)&list, (void*)&qv, &chunk, &refill};
-    return cudaLaunchKernel(fn, dim3(c.grid > 0 ? c.grid : 1), dim3(512), args, 0, st);
+    return cudaLaunchKernel(fn, dim3(c.grid > 0 ? c.grid : 1), dim3(c.block), args, 0, st);
+}
+
+cudaError_t prefer_max_smem(const void* fn, int dyn_smem, bool max_carveout) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void*>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({dev, fn})) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem);
+    if (e == cudaSuccess && max_carveout)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e == cudaSuccess) done.insert({dev, fn});
+    return e;
 }
 
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed) {

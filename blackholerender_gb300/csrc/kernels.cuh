@@ -77,7 +77,7 @@ cudaError_t launch_march_fp64_multi(const ViewBatch& b, const Scratch& s, int gr
 cudaError_t launch_march_list(const DevView& v, const Rule& r, const Scratch& s, const int* list,
                               const unsigned long long* list_len, const LaunchCfg& c, cudaStream_t st);
 // The FP32 march over per-view pixel lists of several views sharing one rule; view v's list
-// starts at list + views[v].list_off and its length is qv[2v].fb_count.
+// starts at list + views[v].list_off and its length is qv[2v].fb_count. c.block: 64 or 512.
 cudaError_t launch_march_multi_list(const ViewBatch& b, const Scratch& s, const int* list, const WorkQueue* qv,
                                     const LaunchCfg& c, cudaStream_t st);
 // Lens table of a camera at cam_r (lens.cu): the reference's RK4 construction, or (closed_form)
@@ -87,5 +87,11 @@ double lens_alpha_crit(double r);
 float lens_alpha_host(float u, float ac);
 // Max resident blocks per SM of an FP32 march kernel (occupancy API).
 int march_blocks_per_sm(int block, int variant, bool multi, bool mixed);
+// Sets a kernel's dynamic shared-memory limit (dyn_smem bytes) and, with max_carveout, its
+// preference for the largest shared-memory carveout, once per kernel and device (the runtime
+// keeps function attributes per device context). A kernel that runs beside the surrogate pass
+// must prefer the same carveout: an SM changes its L1 / shared split only when idle, so a
+// co-resident block configured for less shared memory keeps the pass's blocks off that SM.
+cudaError_t prefer_max_smem(const void* fn, int dyn_smem, bool max_carveout);
 
 }  // namespace bhr

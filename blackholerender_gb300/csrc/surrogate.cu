@@ -773,20 +773,101 @@ __device__ __forceinline__ void sincos_rr(float x, float* sn, float* cs) {
 // ray and the radial direction, from the unnormalised pixel direction (blackhole.frag:68-72)
 // in double. The view constants arrive in double. Out of line: rare, and its FP64 code would
 // otherwise crowd the instruction cache.
-__device__ __noinline__ double impact_parameter_fp64(const SurrView& sv, int i, int j) {
-    const DevView& w = sv.view;
+__device__ __noinline__ double impact_parameter_fp64(const DevView& w, const Fp64Cam& fc, int i, int j) {
     const double pxx = double(i) + 0.5 + double(w.jitter[0]);
     const double pxy = double(j) + 0.5 + double(w.jitter[1]);
     const double th = double(w.tan_half);
-    const double cx = (pxx * sv.inv_w2 - 1.0) * th * sv.aspect_d;
-    const double cy = (pxy * sv.inv_h2 - 1.0) * th;
+    const double cx = (pxx * fc.inv_w2 - 1.0) * th * fc.aspect_d;
+    const double cy = (pxy * fc.inv_h2 - 1.0) * th;
     const double dx = double(w.basis[0]) * cx + double(w.basis[3]) * cy - double(w.basis[6]);
     const double dy = double(w.basis[1]) * cx + double(w.basis[4]) * cy - double(w.basis[7]);
     const double dz = double(w.basis[2]) * cx + double(w.basis[5]) * cy - double(w.basis[8]);
-    const double* rh = sv.rhat_d;
+    const double* rh = fc.rhat_d;
     const double px = rh[1] * dz - rh[2] * dy, py = rh[2] * dx - rh[0] * dz, pz = rh[0] * dy - rh[1] * dx;
     const double s2 = (px * px + py * py + pz * pz) / (dx * dx + dy * dy + dz * dz);
-    return sv.b_scale_d * ::sqrt(s2);
+    return fc.b_scale_d * ::sqrt(s2);
+}
+
+// The band rays of every view, before the surrogate pass (one warp per searched pixel row).
+// Along row j the pixel direction is d(cx) = cx R + (cy U - B) (the camera basis' columns), and
+// cos^2 of its angle from the hole, (rhat . d)^2 / |d|^2, is at least c exactly where the
+// quadratic (rhat . d)^2 - c |d|^2 is non-negative: between its two roots, since the hole lies
+// well inside the field of view (bhr::surr::band_rows). The band's pixels lie between the
+// roots for c_out (the larger angle) and outside those for c_in; two pixels of margin on each
+// end, and a b range twice the band's, leave every band ray inside the searched pixels, which
+// the warp's lanes take 32 at a time. Everything runs in FP32 (FP64 runs at a small fraction
+// of the FP32 rate here): the roots, and the band test on the FP32 impact parameter, which is
+// within 2e-6 of the FP64 one in beta near the photon sphere. Only rays within kBandEdge of the
+// band's edge take the pass's own FP64 test. A band ray joins its view's list and sets its bit
+// in the view's mask (the pass skips those rays). A ray the search missed would still be found
+// by the pass and go to the fallback list: the mask, not the test, decides who answers a ray.
+constexpr float kBandEdge = 1e-5f;
+__global__ void __launch_bounds__(128) k_band_list(const __grid_constant__ BandBatch bb) {
+    const int t = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (t >= bb.total_rows) return;
+    int vi = 0;
+    while (vi + 1 < bb.nviews && t >= bb.v[vi + 1].row0) ++vi;
+    const BandView& bv = bb.v[vi];
+    const int j = t - bv.row0;
+    if (j >= bv.rows) return;
+    const DevView& w = bv.view;
+    const BandRows& Q = bv.q;
+    // the row's quadratic in cx: (a cx + a0)^2 - c (RR cx^2 + 2 rd cx + dd)
+    const float th = w.tan_half;
+    const float cy = ((float(j) + 0.5f + w.jitter[1]) * (2.0f / float(w.height)) - 1.0f) * th;
+    const float a = Q.a, a0 = cy * Q.rhU - Q.rhB;
+    const float rd = cy * Q.RU - Q.RB, dd = cy * cy * Q.UU - 2.0f * cy * Q.UB + Q.BB;
+    const float sx = th * w.aspect;  // cx = ((i + 0.5 + jitter) 2 / W - 1) sx
+    auto roots = [&](float c, float* lo, float* hi) {
+        const float A2 = a * a - c * Q.RR, A1 = 2.0f * (a * a0 - c * rd), A0 = a0 * a0 - c * dd;
+        float disc = A1 * A1 - 4.0f * A2 * A0;
+        if (disc < 0.0f && disc > -1e-5f) disc = 0.0f;  // a tangent row: the margin covers the rounding
+        if (!(A2 < 0.0f) || !(disc >= 0.0f)) return false;
+        const float q = sqrtf(disc);
+        const float x1 = (-A1 + q) / (2.0f * A2), x2 = (-A1 - q) / (2.0f * A2);
+        auto col = [&](float cx) { return (cx / sx + 1.0f) * (0.5f * float(w.width)) - 0.5f - w.jitter[0]; };
+        *lo = col(fminf(x1, x2));
+        *hi = col(fmaxf(x1, x2));
+        return true;
+    };
+    float p1, p2, q1 = 0.0f, q2 = -1.0f;
+    if (!roots(Q.c_out, &p1, &p2)) return;
+    const bool inner = roots(Q.c_in, &q1, &q2);
+    constexpr float kMargin = 2.0f;
+    auto clampc = [&](float x) { return int(fminf(fmaxf(x, -1.0f), float(w.width))); };
+    int seg[2][2] = {{0, -1}, {0, -1}};
+    if (inner && q2 - q1 > 2.0f * kMargin) {
+        seg[0][0] = clampc(floorf(p1 - kMargin));
+        seg[0][1] = clampc(ceilf(q1 + kMargin));
+        seg[1][0] = clampc(floorf(q2 - kMargin));
+        seg[1][1] = clampc(ceilf(p2 + kMargin));
+    } else {
+        seg[0][0] = clampc(floorf(p1 - kMargin));
+        seg[0][1] = clampc(ceilf(p2 + kMargin));
+    }
+    const float beta_band = bb.band / kSqrt27f;
+    unsigned long long* cnt = &bb.qb[2 * vi].fb_count;
+    for (int sgi = 0; sgi < 2; ++sgi) {
+        const int i0 = max(seg[sgi][0], 0), i1 = min(seg[sgi][1], w.width - 1);
+        for (int i = i0 + lane; i <= i1; i += 32) {
+            const RayInit<float> ri = setup_ray<float>(w, bb.rule, i, j);
+            const float ab = fabsf(ri.b * (1.0f / kSqrt27f) - 1.0f);
+            bool in = ab < beta_band - kBandEdge;
+            if (!in && ab < beta_band + kBandEdge) {  // at the edge: the pass's FP64 test
+                const double bd = impact_parameter_fp64(w, bv.fc, i, j);
+                in = fabsf(float(bd * (1.0 / kSqrt27d) - 1.0)) < beta_band;
+            }
+            if (!in) continue;
+            const int ray = j * w.width + i;
+            const unsigned long long k = atomicAdd(cnt, 1ull);
+            if (k < (unsigned long long)kBandCap) {
+                bv.list[k] = ray;
+                atomicOr(bv.mask + (ray >> 5), 1u << (ray & 31));
+            } else {
+                atomicAdd(cnt, ~0ull);  // minus one: the count settles at kBandCap; this ray takes the fallback list
+            }
+        }
+    }
 }
 
 // Phase-1 work of a captured orbit, out of line: it runs for the rays of the shadow only, and
@@ -1103,17 +1184,19 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
         if (base >= w.nrays) break;
         const int ray = int(base + lane);
         const bool valid = ray < w.nrays;
+        // rays of the band march (k_band_list) are neither answered nor sent to the fallback list
+        const bool pre = sv.band_mask != nullptr && ((__ldg(sv.band_mask + chunk) >> lane) & 1u) != 0u;
         // ---- phase 1: per ray
         int ncand = 0;
         {
-            bool sur = valid;
+            bool sur = valid && !pre;
             const int j = valid ? ray / w.width : 0, i = valid ? ray - j * w.width : 0;
             const RayInit<float> ri = setup_ray<float>(w, R, i, j);
             const V3<float> cam{w.cam[0], w.cam[1], w.cam[2]};
             float b = ri.b;
             float beta = b * (1.0f / kSqrt27f) - 1.0f;
             if (sur && fabsf(beta) < 0.02f) {  // near the photon sphere: impact parameter in FP64
-                const double bd = impact_parameter_fp64(sv, i, j);
+                const double bd = impact_parameter_fp64(w, sv.fc, i, j);
                 beta = float(bd * (1.0 / kSqrt27d) - 1.0);
                 b = float(bd);
             }
@@ -1273,7 +1356,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
             const uint32_t info = G.info[lane];
             const bool sur = (info & 4u) != 0;
             const bool cap = (info & kCapBit) != 0;
-            if (valid && !sur) fb_list[warp_append_ull(&q->fb_count)] = ray;
+            if (valid && !sur && !pre) fb_list[warp_append_ull(&q->fb_count)] = ray;
             if (sur) {
                 ++n_surr;
                 // captured: no direction (as TraceResult::dir), closest approach = the capture radius
@@ -1333,6 +1416,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
 
 int train_smem_bytes() { return int(sizeof(TrainSmem)); }
 
+
 cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_list, int grid, bool net,
                                    cudaStream_t st) {
     const int smem = int(sizeof(InferSmem));
@@ -1340,13 +1424,8 @@ cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_lis
     using K = void (*)(SurrView, WorkQueue*, int*);
     const K kern = tol ? (net ? K(k_surrogate<true, true>) : K(k_surrogate<true, false>))
                        : (net ? K(k_surrogate<false, true>) : K(k_surrogate<false, false>));
-    static bool attr[2][2] = {{false, false}, {false, false}};
-    if (!attr[tol][net]) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        if (e != cudaSuccess) return e;
-        attr[tol][net] = true;
-    }
+    const cudaError_t e = prefer_max_smem((const void*)kern, smem, true);
+    if (e != cudaSuccess) return e;
     kern<<<grid, 32 * kInferWarps, smem, st>>>(sv, q, fb_list);
     return cudaGetLastError();
 }
@@ -1362,12 +1441,8 @@ cudaError_t launch_train_step(const float* params, const TrainSample* X, const i
                               const int64_t* idx, int batch, uint64_t seed, float w_u, float w_c, float* grads,
                               float* loss, int grid, cudaStream_t st) {
     const int smem = train_smem_bytes();
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_train_step, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    const cudaError_t e = prefer_max_smem((const void*)k_train_step, smem, false);
+    if (e != cudaSuccess) return e;
     k_train_step<<<grid, 32 * kTrainWarps, smem, st>>>(params, X, lab, n_samples, idx, batch, seed, w_u, w_c, grads,
                                                         loss);
     return cudaGetLastError();
@@ -1381,19 +1456,55 @@ cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, i
 
 cudaError_t launch_exit_table_cf(const SurrView& sv, float4* table, cudaStream_t st) {
     const int grid = (kExitTableN + 255) / 256;  // one point per thread
-    if (sv.rule.term_mode != BHR_TERM_CONFIG) k_exit_table_cf<true><<<grid, 256, 0, st>>>(sv, table);
+    const bool tol = sv.rule.term_mode != BHR_TERM_CONFIG;
+    const cudaError_t e =
+        prefer_max_smem(tol ? (const void*)k_exit_table_cf<true> : (const void*)k_exit_table_cf<false>, 0, true);
+    if (e != cudaSuccess) return e;
+    if (tol) k_exit_table_cf<true><<<grid, 256, 0, st>>>(sv, table);
     else k_exit_table_cf<false><<<grid, 256, 0, st>>>(sv, table);
     return cudaGetLastError();
 }
 
+cudaError_t launch_band_list(const BandBatch& b, cudaStream_t st) {
+    if (b.total_rows <= 0) return cudaSuccess;
+    const cudaError_t e = prefer_max_smem((const void*)k_band_list, 0, true);
+    if (e != cudaSuccess) return e;
+    k_band_list<<<(b.total_rows + 3) / 4, 128, 0, st>>>(b);
+    return cudaGetLastError();
+}
+
+bool band_rows(const bhr_view& v, const Fp64Cam& fc, double b_lo, double b_hi, BandRows* q) {
+    // sin of the angle from the hole for impact parameter b: b / b_scale
+    const double s_hi = b_hi / fc.b_scale_d, s_lo = std::max(b_lo, 0.0) / fc.b_scale_d;
+    if (!(s_hi < 1.0) || !(s_lo < s_hi)) return false;
+    const double R[3] = {v.cam_basis[0], v.cam_basis[1], v.cam_basis[2]};
+    const double U[3] = {v.cam_basis[3], v.cam_basis[4], v.cam_basis[5]};
+    const double B[3] = {v.cam_basis[6], v.cam_basis[7], v.cam_basis[8]};
+    const double* rh = fc.rhat_d;
+    auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+    const double bn = std::sqrt(dot(B, B));
+    if (!(bn > 0.0)) return false;
+    // the view axis is -B; the hole is at -rhat
+    const double theta = std::acos(std::min(1.0, std::max(-1.0, dot(B, rh) / bn)));
+    if (!(theta + std::asin(s_hi) < 85.0 * 3.14159265358979323846 / 180.0)) return false;
+    q->c_out = float(1.0 - s_hi * s_hi);
+    q->c_in = float(1.0 - s_lo * s_lo);
+    q->a = float(dot(rh, R));
+    q->rhU = float(dot(rh, U));
+    q->rhB = float(dot(rh, B));
+    q->RR = float(dot(R, R));
+    q->RU = float(dot(R, U));
+    q->RB = float(dot(R, B));
+    q->UU = float(dot(U, U));
+    q->UB = float(dot(U, B));
+    q->BB = float(dot(B, B));
+    return true;
+}
+
 cudaError_t launch_tables(const TabBatch& b, const float* params, int* status, int grid, cudaStream_t st) {
     const int smem = int(sizeof(tc::Net) + sizeof(tc::L1) + sizeof(tc::Tile));
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    const cudaError_t e = prefer_max_smem((const void*)k_tables, smem, true);
+    if (e != cudaSuccess) return e;
     k_tables<<<std::max(1, std::min(grid, b.ntiles)), 128, smem, st>>>(b, params, status);
     return cudaGetLastError();
 }

@@ -90,6 +90,14 @@ constexpr float kTangentMargin = 10.0f;
 constexpr int kCrossNx = 256, kCrossNs = 64;
 constexpr int kCrossCells = (kCrossNx - 1) * (kCrossNs - 1);
 
+// View constants in double for the impact parameter near the photon sphere (the direction of a
+// pixel and its angle from the hole, as the FP32 setup computes them, in FP64)
+struct Fp64Cam {
+    double inv_w2, inv_h2;  // 2 / width, 2 / height
+    double aspect_d;        // width / height
+    double rhat_d[3];       // camera direction from the float camera position
+    double b_scale_d;       // r_cam / sqrt(1 - 2 / r_cam)
+};
 struct SurrView {
     DevView view;
     Rule rule;
@@ -103,11 +111,38 @@ struct SurrView {
     float tab_lo[2], tab_h[2], tab_inv_h[2];  // x2 of a half's first point, spacing, 1 / spacing
     const float4* cross_table;  // [kCrossCells] y at the cell's corners (i, j), (i, j+1), (i+1, j), (i+1, j+1)
     float cx_h, cx_inv_h;       // the cross table's x2 spacing (first point tab_lo[1]) and its inverse
-    // double constants of the view for the FP64 impact parameter near the photon sphere
-    double inv_w2, inv_h2;  // 2 / width, 2 / height
-    double aspect_d;        // width / height
-    double rhat_d[3];       // camera direction from the float camera position
-    double b_scale_d;       // r_cam / sqrt(1 - 2 / r_cam)
+    Fp64Cam fc;             // the FP64 impact parameter near the photon sphere
+    // the rays of the view's photon-sphere band that the band march takes (bit ray % 32 of word
+    // ray / 32; they are skipped here), or nullptr when no band march runs
+    const uint32_t* band_mask;
+};
+// The band march: the rays of the fallback band (|b - sqrt 27| < band) found before the pass by
+// k_band_list and marched by the integrator beside it. Per view a list of at most kBandCap rays;
+// rays beyond it go the fallback list's way.
+constexpr int kBandCap = 1 << 15;
+// The row search's constants of a view (rhat the camera direction; R, U, B the camera basis'
+// columns), in float: the rows' quadratics lose nothing that two pixels of margin do not cover.
+struct BandRows {
+    float c_out, c_in;      // cos^2 of the angles from the hole at b_hi and b_lo (b range with margin)
+    float a, rhU, rhB;      // rhat . R, rhat . U, rhat . B
+    float RR, RU, RB;       // R . R, R . U, R . B
+    float UU, UB, BB;       // U . U, U . B, B . B
+};
+struct BandView {
+    DevView view;
+    Fp64Cam fc;
+    BandRows q;
+    uint32_t* mask;   // the view's band mask (ceil(rays / 32) words, zeroed before the launch)
+    int* list;        // the view's band list (kBandCap rays)
+    int32_t row0;     // first row of this view in the launch's row numbering
+    int32_t rows;     // rows searched (0: the view's band is not searched, see bhr::surr::band_rows)
+};
+struct BandBatch {
+    int32_t nviews, total_rows;
+    Rule rule;
+    float band;       // the fallback band |b - sqrt 27| < band
+    WorkQueue* qb;    // qb[2 v].fb_count: rays in view v's band list
+    BandView v[kMaxViews];
 };
 // The learned surrogate's tables of up to kTabMaxViews views, built by one launch on the tensor
 // cores (surrogate.cu k_tables): per view its exit table (escaping half: one tile of 128 points
@@ -140,6 +175,14 @@ constexpr int kSurrBlocksPerSM = 3;
 // otherwise the converged closed form).
 cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_list, int grid, bool net,
                                    cudaStream_t st);
+// Finds every view's band rays (search rows from bhr::surr::band_rows) into their band lists and
+// masks: one warp per searched row.
+cudaError_t launch_band_list(const BandBatch& b, cudaStream_t st);
+// The row search of a view's band: the b range [b_lo, b_hi] as cos^2 of the angle from the hole
+// (c_out at b_hi, c_in at b_lo) and the rows' quadratic coefficients, and whether the view's
+// pixel rows cut that cone in bounded intervals (the hole within 85 degrees of the view axis less
+// the cone's angle). Views that fail it have no band march: their band rays take the fallback list.
+bool band_rows(const bhr_view& v, const Fp64Cam& fc, double b_lo, double b_hi, BandRows* q);
 // Fills the view's exit table for the non-learned variant (the converged closed form, no network).
 cudaError_t launch_exit_table_cf(const SurrView& sv, float4* table, cudaStream_t st);
 // x2 ranges of the two halves: captured beta in [-1, -band / sqrt 27], escaping in

@@ -19,6 +19,34 @@
 
 using bhr::surr::kNParams;
 
+// One trace pipeline: its work memory, streams and events. Lane 0 serves bhr_surrogate_trace and
+// plans; bhr_surrogate_trace_host alternates lanes 0 and 1, whose traces overlap on the GPU, so
+// nothing a trace writes is shared between lanes.
+struct SurrLane {
+    // work queues of a trace of n views: [2v] view v's pass, [2v+1] its own fallback march,
+    // [2n] the fallback march of all views; then the band march's: [2n+1+2v] view v's band list
+    // count, [4n+1] the band march itself
+    bhr::WorkQueue* q = nullptr;
+    int64_t nq = 0;
+    int* fb = nullptr;  // fallback ray lists, one per view, one after the other
+    int64_t fb_cap = 0;
+    uint32_t* mask = nullptr;  // band masks, one bit per ray, per view ceil(rays / 32) words
+    int64_t mask_cap = 0;
+    int* band = nullptr;  // band lists, kBandCap rays per view
+    int64_t band_cap = 0;
+    float4* etab = nullptr;  // the views' exit tables, [view][kExitTabEntries]
+    int64_t etab_cap = 0;
+    float4* ctab = nullptr;  // the views' crossing tables, [view][kCrossCells]
+    int64_t ctab_cap = 0;
+    // the views' passes alternate between side[0] and side[1] (fork / join on the caller's
+    // stream), so each launch's last wave overlaps the next view's first; side[2] finds and
+    // marches the band rays beside them
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t start = nullptr, fork = nullptr, band_ready = nullptr;
+    cudaEvent_t join[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // timing: start, passes done, fallback done
+};
+
 struct bhr_surrogate {
     int device = 0;
     int sms = 0;
@@ -32,30 +60,20 @@ struct bhr_surrogate {
     int8_t* lab = nullptr;
     int64_t n_samples = 0;
     unsigned long long* stats = nullptr;  // data generation counters (device, 4)
-    int* tab_status = nullptr;            // set on the device when a table build's tensor-core wait ran out
+    int* tab_status = nullptr;  // per lane, set on the device when a table build's tensor-core wait ran out
     float* loss = nullptr;                // per-step loss sums (device, 3 * loss_cap)
     int loss_cap = 0;
-    bhr::WorkQueue* q = nullptr;          // per view of a trace: [2v] surrogate pass, [2v+1] fallback march
-    int64_t nq = 0;
-    int last_nviews = 0;
-    int* fb = nullptr;                    // fallback ray list
-    int64_t fb_cap = 0;
     bool use_network = true;  // false: the non-learned variant (tables from the converged closed form)
-    float4* etab[2] = {nullptr, nullptr}; // per pipeline lane: the views' exit tables, [view][kExitTabEntries]
-    int64_t etab_cap[2] = {0, 0};
-    float4* ctab[2] = {nullptr, nullptr}; // per pipeline lane: the views' crossing tables, [view][kCrossCells]
-    int64_t ctab_cap[2] = {0, 0};
-    uint64_t work_gen = 0;  // bumped whenever a trace reallocates its work memory (plans hold pointers into it)
+    SurrLane lane[2];
+    uint64_t work_gen = 0;  // bumped whenever a trace reallocates lane 0's work memory (plans hold pointers into it)
     unsigned long long last[4] = {0, 0, 0, 0};
+    // the last trace: its stream, lane, views and network rows
     cudaStream_t last_stream = nullptr;
+    int last_lane = 0;
+    int last_nviews = 0;
+    uint64_t last_rows = 0;
     bool have_last = false;
     bool last_from_plan = false;  // the last trace was a graph replay (its events do not time)
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // start, surrogate pass done, fallback done
-    // the views' surrogate launches alternate between two side streams (fork / join on the
-    // caller's stream), so each launch's last wave overlaps the next view's first; one pair per
-    // pipeline lane (lane 0: bhr_surrogate_trace and plans; lanes 0 and 1: the host-buffer path)
-    cudaStream_t side[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    cudaEvent_t fork[2] = {nullptr, nullptr}, join[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     // bhr_surrogate_trace_host: device staging and two streams
     bhr_hit* staging = nullptr;
     int64_t staging_rays = 0;
@@ -176,16 +194,16 @@ int bhr_surrogate_create(bhr_surrogate** out, int device, const bhr_surrogate_co
     if (e == cudaSuccess) e = cudaMalloc(&s->adam_m, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMalloc(&s->adam_v, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMalloc(&s->stats, sizeof(unsigned long long) * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&s->tab_status, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(s->tab_status, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->tab_status, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(s->tab_status, 0, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(s->params, P.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(s->adam_m, 0, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMemset(s->adam_v, 0, sizeof(float) * kNParams);
-    for (int k = 0; e == cudaSuccess && k < 3; ++k) e = cudaEventCreate(&s->ev[k]);
-    for (int l = 0; e == cudaSuccess && l < 2; ++l) {
-        for (int k = 0; e == cudaSuccess && k < 2; ++k) e = cudaStreamCreateWithFlags(&s->side[l][k], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork[l], cudaEventDisableTiming);
-        for (int k = 0; e == cudaSuccess && k < 2; ++k) e = cudaEventCreateWithFlags(&s->join[l][k], cudaEventDisableTiming);
+    for (SurrLane& L : s->lane) {
+        for (int k = 0; e == cudaSuccess && k < 3; ++k) e = cudaEventCreate(&L.ev[k]);
+        for (int k = 0; e == cudaSuccess && k < 3; ++k) e = cudaStreamCreateWithFlags(&L.side[k], cudaStreamNonBlocking);
+        for (cudaEvent_t* ev : {&L.start, &L.fork, &L.band_ready, &L.join[0], &L.join[1], &L.join[2]})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     }
     if (e != cudaSuccess) {
         bhr_surrogate_destroy(s);
@@ -199,17 +217,14 @@ int bhr_surrogate_destroy(bhr_surrogate* s) {
     if (!s) return BHR_OK;
     DevGuard dg(s->device);
     for (void* p : {(void*)s->params, (void*)s->grads, (void*)s->adam_m, (void*)s->adam_v, (void*)s->X,
-                    (void*)s->lab, (void*)s->stats, (void*)s->tab_status, (void*)s->loss, (void*)s->q, (void*)s->fb,
-                    (void*)s->staging,
-                    (void*)s->etab[0], (void*)s->etab[1], (void*)s->ctab[0], (void*)s->ctab[1]})
+                    (void*)s->lab, (void*)s->stats, (void*)s->tab_status, (void*)s->loss, (void*)s->staging})
         if (p) cudaFree(p);
-    for (cudaEvent_t& e : s->ev)
-        if (e) cudaEventDestroy(e);
-    for (int l = 0; l < 2; ++l) {
-        for (cudaEvent_t& e : s->join[l])
+    for (SurrLane& L : s->lane) {
+        for (void* p : {(void*)L.q, (void*)L.fb, (void*)L.mask, (void*)L.band, (void*)L.etab, (void*)L.ctab})
+            if (p) cudaFree(p);
+        for (cudaEvent_t e : {L.ev[0], L.ev[1], L.ev[2], L.start, L.fork, L.band_ready, L.join[0], L.join[1], L.join[2]})
             if (e) cudaEventDestroy(e);
-        if (s->fork[l]) cudaEventDestroy(s->fork[l]);
-        for (cudaStream_t& st : s->side[l])
+        for (cudaStream_t st : L.side)
             if (st) cudaStreamDestroy(st);
     }
     for (cudaStream_t& st : s->hs)
@@ -502,24 +517,30 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     // per-view fallback lists, one after the other
     std::vector<int64_t> off(size_t(nviews) + 1, 0);
     for (int k = 0; k < nviews; ++k) off[size_t(k) + 1] = off[size_t(k)] + int64_t(views[k].width) * views[k].height;
-    // what plans point into: the fallback list, the work queues and lane 0's tables (plans run on lane 0)
+    SurrLane& L = s->lane[lane];
+    // what plans point into: lane 0's work memory (plans run on lane 0)
     auto plan_memory = [&] {
-        return std::array<uintptr_t, 8>{uintptr_t(s->fb),      uintptr_t(s->fb_cap),      uintptr_t(s->q),
-                                        uintptr_t(s->nq),      uintptr_t(s->etab[0]),     uintptr_t(s->etab_cap[0]),
-                                        uintptr_t(s->ctab[0]), uintptr_t(s->ctab_cap[0])};
+        return std::array<uintptr_t, 12>{uintptr_t(L.fb),   uintptr_t(L.fb_cap),   uintptr_t(L.q),
+                                         uintptr_t(L.nq),   uintptr_t(L.etab),     uintptr_t(L.etab_cap),
+                                         uintptr_t(L.ctab), uintptr_t(L.ctab_cap), uintptr_t(L.mask),
+                                         uintptr_t(L.mask_cap), uintptr_t(L.band), uintptr_t(L.band_cap)};
     };
     const auto before = plan_memory();
-    cudaError_t e = grow(&s->fb, &s->fb_cap, off[size_t(nviews)]);
-    if (e == cudaSuccess) e = grow(&s->q, &s->nq, 2 * int64_t(nviews) + 1);
+    // per-view band masks, one after the other (ceil(rays / 32) words each)
+    std::vector<int64_t> moff(size_t(nviews) + 1, 0);
+    for (int k = 0; k < nviews; ++k) moff[size_t(k) + 1] = moff[size_t(k)] + (int64_t(views[k].width) * views[k].height + 31) / 32;
+    const int64_t nq = 4 * int64_t(nviews) + 2;
+    cudaError_t e = grow(&L.fb, &L.fb_cap, off[size_t(nviews)]);
+    if (e == cudaSuccess) e = grow(&L.q, &L.nq, nq);
+    if (e == cudaSuccess) e = grow(&L.mask, &L.mask_cap, moff[size_t(nviews)]);
+    if (e == cudaSuccess) e = grow(&L.band, &L.band_cap, int64_t(bhr::surr::kBandCap) * nviews);
     constexpr int64_t kTab = bhr::surr::kExitTabEntries;  // table entries per view
-    if (e == cudaSuccess) e = grow(&s->etab[lane], &s->etab_cap[lane], kTab * std::max<int64_t>(nviews, 64));
+    if (e == cudaSuccess) e = grow(&L.etab, &L.etab_cap, kTab * std::max<int64_t>(nviews, 64));
     constexpr int64_t kCells = bhr::surr::kCrossCells;
-    if (e == cudaSuccess) e = grow(&s->ctab[lane], &s->ctab_cap[lane], kCells * std::max<int64_t>(nviews, 16));
-    if (plan_memory() != before) ++s->work_gen;
+    if (e == cudaSuccess) e = grow(&L.ctab, &L.ctab_cap, kCells * std::max<int64_t>(nviews, 16));
+    if (lane == 0 && plan_memory() != before) ++s->work_gen;
     if (e != cudaSuccess) return fail(BHR_ERR_OOM, "bhr_surrogate_trace: work memory");
-    e = cudaMemsetAsync(s->q, 0, sizeof(bhr::WorkQueue) * size_t(2 * nviews + 1), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->tab_status, 0, sizeof(int), st);
-    if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
+    bhr::WorkQueue* const qb = L.q + 2 * nviews + 1;  // the band march's queues
     // the views' constants
     std::vector<bhr::surr::SurrView> svs(static_cast<size_t>(nviews));
     std::vector<bhr::DevView> dvs(static_cast<size_t>(nviews));
@@ -536,33 +557,90 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         sv.uc = 1.0f / sv.view.rcam;
         sv.u_esc_min = sv.rule.r_esc_min > 0.0f ? 1.0f / sv.rule.r_esc_min : 1.0f;
         sv.b_kink = views[k].term_mode == BHR_TERM_CONFIG ? 0.0f : tolerance_kink(sv.rule.esc_tol, sv.u_esc_min);
-        sv.exit_table = s->etab[lane] + kTab * k;
+        sv.exit_table = L.etab + kTab * k;
         bhr::surr::exit_table_range(s->norm, sv.tab_lo, sv.tab_h);
         for (int h = 0; h < 2; ++h) sv.tab_inv_h[h] = 1.0f / sv.tab_h[h];
-        sv.cross_table = s->ctab[lane] + kCells * k;
+        sv.cross_table = L.ctab + kCells * k;
         sv.cx_h = sv.tab_h[1] * float(bhr::surr::kExitTableN - 1) / float(bhr::surr::kCrossNx - 1);
         sv.cx_inv_h = 1.0f / sv.cx_h;
         {
             const double cx = views[k].cam_pos[0], cy = views[k].cam_pos[1], cz = views[k].cam_pos[2];
             const double rc = std::sqrt(cx * cx + cy * cy + cz * cz);
-            sv.inv_w2 = 2.0 / double(views[k].width);
-            sv.inv_h2 = 2.0 / double(views[k].height);
-            sv.aspect_d = double(views[k].width) / double(views[k].height);
-            sv.rhat_d[0] = cx / rc;
-            sv.rhat_d[1] = cy / rc;
-            sv.rhat_d[2] = cz / rc;
-            sv.b_scale_d = rc / std::sqrt(std::max(1.0 - 2.0 / rc, 1e-300));
+            bhr::surr::Fp64Cam& fc = sv.fc;
+            fc.inv_w2 = 2.0 / double(views[k].width);
+            fc.inv_h2 = 2.0 / double(views[k].height);
+            fc.aspect_d = double(views[k].width) / double(views[k].height);
+            fc.rhat_d[0] = cx / rc;
+            fc.rhat_d[1] = cy / rc;
+            fc.rhat_d[2] = cz / rc;
+            fc.b_scale_d = rc / std::sqrt(std::max(1.0 - 2.0 / rc, 1e-300));
             // the camera's tangential ray has b = b_scale_d
-            const double beta_t = sv.b_scale_d / 5.196152422706632 - 1.0;
+            const double beta_t = fc.b_scale_d / 5.196152422706632 - 1.0;
             const double x2_t = std::log1p(beta_t / double(s->norm.t_eps)) * double(s->norm.t_scale);
             sv.x2_lim = float(x2_t - double(bhr::surr::kTangentMargin) * double(sv.tab_h[1]));
         }
+        sv.band_mask = nullptr;
         dvs[size_t(k)] = sv.view;
         rules[size_t(k)] = sv.rule;
         one_rule = one_rule && std::memcmp(&rules[0], &sv.rule, sizeof sv.rule) == 0;
     }
-    // 1) the learned surrogate's tables of every view: one launch on the tensor cores per 64 views
+    // the band march: the views' band rays found before the pass and marched beside it (views that
+    // share one rule, as the fallback march's multi-view launch needs; views whose rows the search
+    // cannot bound keep their band rays on the fallback list)
+    const bool band = one_rule && nviews <= bhr::kMaxViews;
+    static thread_local bhr::surr::BandBatch bb;
+    if (band) {
+        bb.nviews = nviews;
+        bb.rule = rules[0];
+        bb.band = s->norm.band;
+        bb.qb = qb;
+        int rows = 0;
+        const double s27 = 5.196152422706632, margin = 2.0 * double(s->norm.band);
+        for (int k = 0; k < nviews; ++k) {
+            bhr::surr::BandView& bv = bb.v[k];
+            bhr::surr::SurrView& sv = svs[size_t(k)];
+            bv.view = sv.view;
+            bv.fc = sv.fc;
+            bv.mask = L.mask + moff[size_t(k)];
+            bv.list = L.band + int64_t(bhr::surr::kBandCap) * k;
+            bv.row0 = rows;
+            bv.rows = bhr::surr::band_rows(views[k], sv.fc, s27 - margin, s27 + margin, &bv.q) ? views[k].height : 0;
+            rows += bv.rows;
+            sv.band_mask = bv.mask;
+            dvs[size_t(k)].list_off = int64_t(bhr::surr::kBandCap) * k;
+        }
+        bb.total_rows = rows;
+    }
+    e = cudaMemsetAsync(L.q, 0, sizeof(bhr::WorkQueue) * size_t(nq), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->tab_status + lane, 0, sizeof(int), st);
+    if (e == cudaSuccess && band) e = cudaMemsetAsync(L.mask, 0, sizeof(uint32_t) * size_t(moff[size_t(nviews)]), st);
+    if (e == cudaSuccess) e = cudaEventRecord(L.ev[0], st);
+    // 1) on side[2]: the band rays of every view (lists and masks), then their march, which runs
+    // beside the tables and the passes (64-thread blocks: they leave the SMs' registers to the pass)
+    if (e == cudaSuccess && band) {
+        e = cudaEventRecord(L.start, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(L.side[2], L.start, 0);
+        if (e == cudaSuccess) e = bhr::surr::launch_band_list(bb, L.side[2]);
+        if (e == cudaSuccess) e = cudaEventRecord(L.band_ready, L.side[2]);
+        static thread_local bhr::ViewBatch vb;
+        vb.nviews = nviews;
+        vb.rule = rules[0];
+        vb.total_chunks = 0;
+        for (int k = 0; k < nviews; ++k) vb.views[k] = dvs[size_t(k)];
+        bhr::LaunchCfg cfg{};
+        cfg.block = 64;
+        cfg.chunk = 32;
+        cfg.refill = 8;
+        cfg.variant = bhr::rule_variant(vb.rule);
+        cfg.grid = s->sms;
+        const bhr::Scratch sc{qb + 2 * nviews, nullptr, nullptr};
+        if (e == cudaSuccess) e = bhr::launch_march_multi_list(vb, sc, L.band, qb, cfg, L.side[2]);
+        if (e == cudaSuccess) e = cudaEventRecord(L.join[2], L.side[2]);
+        for (int k = 0; k < nviews; ++k) dvs[size_t(k)].list_off = off[size_t(k)];
+    }
+    // 2) the learned surrogate's tables of every view: one launch on the tensor cores per 64 views
     const bool net = s->use_network;
+    uint64_t net_rows = 0;
     if (net) {
         static thread_local bhr::surr::TabBatch tb;
         for (int k0 = 0; e == cudaSuccess && k0 < nviews; k0 += bhr::surr::kTabMaxViews) {
@@ -588,34 +666,38 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
                 tv.disk_outer = sv.rule.disk_outer;
                 tv.tol = views[k].term_mode != BHR_TERM_CONFIG;
                 tv.tile0 = tiles;
-                tv.exit_table = s->etab[lane] + kTab * k;
-                tv.cross_table = s->ctab[lane] + kCells * k;
+                tv.exit_table = L.etab + kTab * k;
+                tv.cross_table = L.ctab + kCells * k;
                 tiles += bhr::surr::tab_tiles(tv.tol != 0);
             }
             tb.ntiles = tiles;
-            e = bhr::surr::launch_tables(tb, s->params, s->tab_status, s->sms * 4, st);
+            net_rows += uint64_t(tiles) * 128u;
+            e = bhr::surr::launch_tables(tb, s->params, s->tab_status + lane, s->sms * 4, st);
         }
     }
-    if (e == cudaSuccess) e = cudaEventRecord(s->fork[lane], st);
-    for (int j = 0; e == cudaSuccess && j < 2; ++j) e = cudaStreamWaitEvent(s->side[lane][j], s->fork[lane], 0);
-    // 2) the surrogate pass of every view (the non-learned variant builds its exit table first),
-    // alternating between the two side streams
+    if (e == cudaSuccess) e = cudaEventRecord(L.fork, st);
+    for (int j = 0; e == cudaSuccess && j < 2; ++j) {
+        e = cudaStreamWaitEvent(L.side[j], L.fork, 0);
+        if (e == cudaSuccess && band) e = cudaStreamWaitEvent(L.side[j], L.band_ready, 0);
+    }
+    // 3) the surrogate pass of every view (the non-learned variant builds its exit table first),
+    // alternating between side[0] and side[1]
     for (int k = 0; e == cudaSuccess && k < nviews; ++k) {
         const bhr::surr::SurrView& sv = svs[size_t(k)];
-        cudaStream_t vs = s->side[lane][k & 1];
-        if (!net) e = bhr::surr::launch_exit_table_cf(sv, s->etab[lane] + kTab * k, vs);
+        cudaStream_t vs = L.side[k & 1];
+        if (!net) e = bhr::surr::launch_exit_table_cf(sv, L.etab + kTab * k, vs);
         if (e == cudaSuccess)
-            e = bhr::surr::launch_surrogate_trace(sv, s->q + 2 * k, s->fb + off[size_t(k)],
+            e = bhr::surr::launch_surrogate_trace(sv, L.q + 2 * k, L.fb + off[size_t(k)],
                                                   s->sms * bhr::surr::kSurrBlocksPerSM, net, vs);
     }
     for (int j = 0; e == cudaSuccess && j < 2; ++j) {
-        e = cudaEventRecord(s->join[lane][j], s->side[lane][j]);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, s->join[lane][j], 0);
+        e = cudaEventRecord(L.join[j], L.side[j]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, L.join[j], 0);
     }
-    if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
-    // 3) the integrator on the fallback rays: one launch for all views when they share a rule
-    // the fallback rays are few and the near-critical ones long: claims of 32 spread them over
-    // as many warps as possible, so the launch ends with its slowest ray, not a warp's queue
+    if (e == cudaSuccess) e = cudaEventRecord(L.ev[1], st);
+    // 4) the integrator on the rays the pass sent to the fallback list: one launch for all views
+    // when they share a rule. The rays are few and the near-critical ones long: claims of 32
+    // spread them over as many warps as possible, so the launch ends with its slowest ray
     bhr::LaunchCfg cfg{};
     cfg.block = 512;
     cfg.chunk = 32;
@@ -628,18 +710,20 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         for (int k = 0; k < nviews; ++k) b.views[k] = dvs[size_t(k)];
         cfg.variant = bhr::rule_variant(b.rule);
         cfg.grid = s->sms * std::max(1, bhr::march_blocks_per_sm(512, cfg.variant, true, false));
-        const bhr::Scratch sc{s->q + 2 * nviews, nullptr, nullptr};
-        e = bhr::launch_march_multi_list(b, sc, s->fb, s->q, cfg, st);
+        const bhr::Scratch sc{L.q + 2 * nviews, nullptr, nullptr};
+        e = bhr::launch_march_multi_list(b, sc, L.fb, L.q, cfg, st);
     } else {
         for (int k = 0; e == cudaSuccess && k < nviews; ++k) {
             cfg.variant = bhr::rule_variant(rules[size_t(k)]);
             cfg.grid = s->sms * std::max(1, bhr::march_blocks_per_sm(512, cfg.variant, false, false));
-            const bhr::Scratch sc{s->q + 2 * k + 1, nullptr, nullptr};
-            e = bhr::launch_march_list(dvs[size_t(k)], rules[size_t(k)], sc, s->fb + off[size_t(k)],
-                                       &s->q[2 * k].fb_count, cfg, st);
+            const bhr::Scratch sc{L.q + 2 * k + 1, nullptr, nullptr};
+            e = bhr::launch_march_list(dvs[size_t(k)], rules[size_t(k)], sc, L.fb + off[size_t(k)],
+                                       &L.q[2 * k].fb_count, cfg, st);
         }
     }
-    if (e == cudaSuccess) e = cudaEventRecord(s->ev[2], st);
+    // the trace ends with the band march too
+    if (e == cudaSuccess && band) e = cudaStreamWaitEvent(st, L.join[2], 0);
+    if (e == cudaSuccess) e = cudaEventRecord(L.ev[2], st);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace");
     // a trace recorded into a graph (plan creation and update) runs nothing now: its event
     // records are capture dependencies, not timings, so the last executed trace stays the one
@@ -649,7 +733,9 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace: capture status");
     if (cs == cudaStreamCaptureStatusNone) {
         s->last_stream = st;
+        s->last_lane = lane;
         s->last_nviews = nviews;
+        s->last_rows = net_rows;
         s->have_last = true;
         s->last_from_plan = false;
     }
@@ -665,6 +751,7 @@ struct bhr_surrogate_plan {
     cudaGraphExec_t exec = nullptr;
     int nviews = 0;
     uint64_t work_gen = 0;  // the surrogate's work memory generation the graph was captured with
+    uint64_t rows = 0;      // network rows of a replay (the views' tables)
     std::vector<bhr_view> views;  // the views and outputs of the captured trace
     std::vector<bhr_hit*> outs;
 };
@@ -702,6 +789,7 @@ int bhr_surrogate_plan_create(bhr_surrogate* s, const bhr_view* views, int nview
     if (rc == BHR_OK) {
         e = cudaStreamSynchronize(p->cap);
         if (e != cudaSuccess) rc = cfail(e, "bhr_surrogate_plan_create: first trace");
+        p->rows = s->last_rows;
     }
     if (rc == BHR_OK) {
         e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
@@ -786,7 +874,9 @@ int bhr_surrogate_plan_launch(bhr_surrogate_plan* p, void* stream) {
     const cudaError_t e = cudaGraphLaunch(p->exec, st);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_plan_launch");
     p->s->last_stream = st;
+    p->s->last_lane = 0;
     p->s->last_nviews = p->nviews;
+    p->s->last_rows = p->rows;
     p->s->have_last = true;
     p->s->last_from_plan = true;
     return BHR_OK;
@@ -798,9 +888,10 @@ int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2) {
     if (s->last_from_plan)
         return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_times: phase times come from bhr_surrogate_trace, not from plan replays");
     DevGuard dg(s->device);
-    cudaError_t e = cudaEventSynchronize(s->ev[2]);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms2[0], s->ev[0], s->ev[1]);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms2[1], s->ev[1], s->ev[2]);
+    const SurrLane& L = s->lane[s->last_lane];
+    cudaError_t e = cudaEventSynchronize(L.ev[2]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms2[0], L.ev[0], L.ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms2[1], L.ev[1], L.ev[2]);
     return e == cudaSuccess ? BHR_OK : cfail(e, "bhr_surrogate_trace_times");
 }
 
@@ -874,30 +965,32 @@ int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out) {
     if (!s || !out) return fail(BHR_ERR_INVALID_ARG, "bhr_surrogate_trace_stats: NULL");
     if (!s->have_last) return fail(BHR_ERR_NOT_READY, "bhr_surrogate_trace_stats: no trace yet");
     DevGuard dg(s->device);
-    std::vector<bhr::WorkQueue> q(2 * size_t(s->last_nviews) + 1);
+    const size_t n = size_t(s->last_nviews);
+    const SurrLane& L = s->lane[s->last_lane];
+    std::vector<bhr::WorkQueue> q(4 * n + 2);
     int tab_status = 0;
     cudaError_t e = cudaStreamSynchronize(s->last_stream);
-    if (e == cudaSuccess) e = cudaMemcpy(q.data(), s->q, sizeof(bhr::WorkQueue) * q.size(), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(&tab_status, s->tab_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(q.data(), L.q, sizeof(bhr::WorkQueue) * q.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&tab_status, s->tab_status + s->last_lane, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cfail(e, "bhr_surrogate_trace_stats");
     if (tab_status)
         return fail(BHR_ERR_TIMEOUT, "bhr_surrogate_trace_stats: a tensor-core completion wait of the table build ran out "
                                      "(the affected table entries are NaN)");
     for (int k = 0; k < 6; ++k) out[k] = 0;
-    for (int v = 0; v < s->last_nviews; ++v) {
+    const bhr::WorkQueue* qb = q.data() + 2 * n + 1;  // the band march's queues
+    for (size_t v = 0; v < n; ++v) {
         out[0] += q[2 * v].surr_rays;
-        out[1] += q[2 * v].fb_count;
+        out[1] += q[2 * v].fb_count + qb[2 * v].fb_count;
         out[2] += q[2 * v].capture_disagree;
         out[3] += q[2 * v + 1].steps;
         out[4] += q[2 * v].mlp_queries;
         out[5] += q[2 * v].mlp_rows;
     }
-    out[3] += q[2 * size_t(s->last_nviews)].steps;
-    // the network runs in the views' tables: 2 kExitTableN + kCrossNx kCrossNs rows per view
-    const uint64_t rows =
-        s->use_network ? uint64_t(2 * bhr::surr::kExitTableN + bhr::surr::kCrossNx * bhr::surr::kCrossNs) : 0;
-    out[4] += rows * uint64_t(s->last_nviews);
-    out[5] += rows * uint64_t(s->last_nviews);
+    out[3] += q[2 * n].steps + qb[2 * n].steps;
+    // the network runs in the views' tables (whole 128-row tiles)
+    out[4] += s->last_rows;
+    out[5] += s->last_rows;
     return BHR_OK;
 }
 

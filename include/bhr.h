@@ -279,25 +279,31 @@ int bhr_surrogate_eval(bhr_surrogate* s, const float* queries, int n, float* out
 int bhr_surrogate_wait_selftest(bhr_surrogate* s);
 int bhr_surrogate_save(bhr_surrogate* s, const char* path);
 int bhr_surrogate_load(bhr_surrogate* s, const char* path);
-/* Surrogate-plus-fallback trace, stream-ordered like bhr_trace. Views: lensing on, not far mode,
- * thin disk or none; the CONFIG rule at the trained exit radius (escape_r), or the SHADER / CPU
- * rule's tolerance escape (0 < esc_tol <= 0.01), which the surrogate applies where the march's
- * escape test first passes in the limit of small steps (beyond rEscMin, at the radius where
- * 0.75 b'^3 / r^4 reaches esc_tol, b' the impact parameter at the current speed), then
- * farFieldDirection there. Other views: BHR_ERR_UNSUPPORTED (bhr_trace with
- * BHR_METHOD_SURROGATE sends them to the plain march instead). */
 /* Selects the variant bhr_surrogate_trace runs (no counterpart in the reference): use_network 1
  * (the default) is the learned surrogate, whose network corrects a cheap closed form; 0 is the
  * same pass with its per-view tables built from the converged closed form (Carlson R_F with three
  * duplication steps) and no network: the non-learned orbit table the learned part is measured
  * against. The fallback rays are the same. */
 int bhr_surrogate_use_network(bhr_surrogate* s, int use_network);
+/* Surrogate-plus-fallback trace, stream-ordered like bhr_trace. Views: lensing on, not far mode,
+ * thin disk or none; the CONFIG rule at the trained exit radius (escape_r), or the SHADER / CPU
+ * rule's tolerance escape (0 < esc_tol <= 0.01), which the surrogate applies where the march's
+ * escape test first passes in the limit of small steps (beyond rEscMin, at the radius where
+ * 0.75 b'^3 / r^4 reaches esc_tol, b' the impact parameter at the current speed), then
+ * farFieldDirection there. Other views: BHR_ERR_UNSUPPORTED (bhr_trace with
+ * BHR_METHOD_SURROGATE sends them to the plain march instead).
+ * The rays of the photon-sphere band (|b - sqrt 27| < band) are found before the surrogate pass
+ * and marched by the plain integrator beside it (views sharing one rule, up to 64); the rays the
+ * pass itself sends back are marched after it. Either way a ray's record is the plain march's. */
 int bhr_surrogate_trace(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_dev,
                         void* cuda_stream);
-/* Host-memory variant (records copied to out_host[k]; synchronous), as bhr_trace_host. */
+/* Host-memory variant (records copied to out_host[k]; synchronous), as bhr_trace_host. Groups of
+ * views are traced on two pipelines in turn, each with its own work memory, so that one group's
+ * copy to the host overlaps the next group's trace. */
 int bhr_surrogate_trace_host(bhr_surrogate* s, const bhr_view* views, int nviews, bhr_hit* const* out_host);
-/* The same trace of a fixed batch of views captured once into a CUDA graph and replayed: the 2 x
- * nviews + 1 launches of a trace become one graph launch. The plan uses the surrogate's work
+/* The same trace of a fixed batch of views captured once into a CUDA graph and replayed: the
+ * launches of a trace (the band search and march, the tables, one pass per view, the fallback
+ * march) become one graph launch. The plan uses the surrogate's work
  * memory and outputs: replays and traces on the same surrogate must not overlap on the GPU, and a
  * later trace that needs more work memory (more rays or views) reallocates it, after which
  * bhr_surrogate_plan_launch returns BHR_ERR_NOT_READY (recreate the plan).
@@ -311,12 +317,17 @@ int bhr_surrogate_plan_launch(bhr_surrogate_plan* plan, void* cuda_stream);
  * trace is re-captured with the same outputs and the instantiated graph updated in place. */
 int bhr_surrogate_plan_update(bhr_surrogate_plan* plan, const bhr_view* views, int nviews);
 int bhr_surrogate_plan_destroy(bhr_surrogate_plan* plan);
-/* Device time of the last bhr_surrogate_trace: ms2[0] surrogate pass, ms2[1] fallback march. */
+/* Device time of the last bhr_surrogate_trace: ms2[0] from its start to the end of the views'
+ * passes (the tables and passes; the band march runs beside them), ms2[1] from there to its end
+ * (the fallback march of the rays the passes sent back, and the rest of the band march if that
+ * was still running). */
 int bhr_surrogate_trace_times(bhr_surrogate* s, float* ms2);
-/* Of the last bhr_surrogate_trace: rays answered by the surrogate, rays sent to the integrator,
- * capture-flag disagreements (also sent to the integrator), integrator steps of the fallback,
- * network rows (the views' exit and crossing tables: 2 x 8192 + 512 x 128 rows per view; the rays
- * read them by interpolation), network rows evaluated (the same, in full 16-row tiles). */
+/* Of the last bhr_surrogate_trace: rays answered by the surrogate, rays marched by the
+ * integrator (band march and fallback), capture-flag disagreements (also sent to the
+ * integrator), integrator steps of those rays, network rows (the views' exit and crossing
+ * tables: 2 x 2048 exit points, 2048 more for the tolerance escape's second branch, and
+ * 256 x 64 crossing points per view; the rays read them by interpolation), network rows
+ * evaluated (the same: whole 128-row tiles). */
 int bhr_surrogate_trace_stats(bhr_surrogate* s, uint64_t* out6);
 
 /* Statistics of the last bhr_trace on ctx (synchronises that call's stream). */

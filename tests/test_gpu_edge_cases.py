@@ -134,21 +134,35 @@ def test_argument_errors_are_reported(tracer):
     assert len(g) == 64
 
 
-def test_surrogate_refuses_rules_it_was_not_trained_for():
-    """The network is trained on CONFIG-rule orbits with lensing; other rules are the plain
-    integrator's (bhr_trace): the surrogate says so with BHR_ERR_UNSUPPORTED and stays usable."""
+def test_surrogate_refuses_views_it_does_not_answer():
+    """The surrogate answers lensed rays under the CONFIG rule at its trained exit radius and
+    under the SHADER / CPU tolerance escape; lensing off, far mode, the volumetric disk and a
+    CONFIG escape radius other than the trained one are the plain integrator's (bhr_trace): the
+    surrogate says so with BHR_ERR_UNSUPPORTED and stays usable."""
     import torch
 
     from blackholerender_gb300.surrogate import DEFAULT_CHECKPOINT, Surrogate
 
     s = Surrogate(seed=2)
     s.load(DEFAULT_CHECKPOINT)
-    for v in (make_view(TERM_SHADER, width=64, height=36, preset=2, pose=(30.0, 1.45, 0.0)),
-              make_view(TERM_CONFIG, width=64, height=36, preset=2, pose=(30.0, 1.45, 0.0), lensing=0)):
+    pose = (30.0, 1.45, 0.0)
+    far = make_view(TERM_CONFIG, width=64, height=36, preset=2, pose=pose)
+    far.far_mode = 1
+    vol = make_view(TERM_CONFIG, width=64, height=36, preset=2, pose=pose)
+    vol.disk_mode = DISK_VOLUMETRIC
+    esc = make_view(TERM_CONFIG, width=64, height=36, preset=2, pose=pose)
+    esc.escape_r = 500.0
+    cases = [(make_view(TERM_CONFIG, width=64, height=36, preset=2, pose=pose, lensing=0), "lensing"),
+             (far, "far mode"), (vol, "volumetric"), (esc, "escape radius")]
+    for v, why in cases:
         with pytest.raises(BhrError) as e:
             s.trace([v])
-        assert e.value.code == -5 and "CONFIG" in str(e.value)
-    (o,) = s.trace([make_view(TERM_CONFIG, width=64, height=36, preset=2, pose=(30.0, 1.45, 0.0))])
+        assert e.value.code == -5 and why in str(e.value), str(e.value)
+    (o,) = s.trace([make_view(TERM_SHADER, width=64, height=36, preset=2, pose=pose)])
+    torch.cuda.synchronize()
+    g = hits_numpy(o.cpu())
+    assert np.all((g["flags"] & (FLAG_SURROGATE | FLAG_FALLBACK)) != 0)
+    (o,) = s.trace([make_view(TERM_CONFIG, width=64, height=36, preset=2, pose=pose)])
     torch.cuda.synchronize()
     g = hits_numpy(o.cpu())
     s.close()

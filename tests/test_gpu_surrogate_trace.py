@@ -317,6 +317,25 @@ def test_surrogate_host_buffers_and_uneven_views(surrogate):
     assert len(a) > 5000 and np.percentile(a, 99) < DIR_MAX_RAD, np.percentile(a, 99)
 
 
+def test_surrogate_host_buffers_overlapping_pipelines(surrogate):
+    """Six 1080p poses through bhr_surrogate_trace_host: three groups of two views (the staging
+    half holds 4.2 M rays), traced on the two pipelines in turn while the previous group's records
+    copy out, so two traces overlap on the GPU. Each pipeline has its own work queues, fallback
+    and band lists: the records equal the device-buffer trace's byte for byte."""
+    import torch
+
+    from blackholerender_gb300 import HIT_DTYPE
+
+    views = workloads.c2_views(TERM_CONFIG)[:6]
+    dev = surrogate.trace(views)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        host = [np.zeros(v.rays, dtype=HIT_DTYPE) for v in views]
+        surrogate.trace_host(views, host)
+        for k, (a, h) in enumerate(zip(dev, host)):
+            assert np.array_equal(a.cpu().numpy().view(np.uint8), h.view(np.uint8)), k
+
+
 def test_surrogate_plan_refuses_after_work_memory_grows():
     """A plan holds pointers into the surrogate's work memory: after a larger trace reallocates it
     (here 20 views, past the crossing tables' 16-view allocation), the plan's launch is refused
