@@ -1237,9 +1237,19 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
                     ++n_dis;
                 }
                 const bool br = kTol && b > sv.b_kink;  // the tolerance escape's branch
+                // the turning point's angle and the disk's range are loaded with the others, so
+                // that the five loads' latencies overlap (they are used only when the ray has
+                // plane crossings)
+                const float4 ei = __ldg(E + kExitIc + jc);
+                const float4 rg = __ldg(E + kExitRange + m);
                 psi = cubic(__ldg(E + (br ? kExitPsiB : kExitPsi) + jc), L);
                 phi0 = cubic(__ldg(E + (br ? kExitPhi0B : kExitPhi0) + jc), L);
                 minr = 1.0f / u2;
+                Ic = cubic(ei, L);
+                if (thin) {
+                    Ilo = fmaf(t, rg.z - rg.x, rg.x);
+                    Ihi = fmaf(t, rg.w - rg.y, rg.y);
+                }
             } else {
                 if (kNet && sur && !(capture_logit(sv, x2) > 0.f)) {
                     sur = false;
@@ -1261,17 +1271,9 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
             if (sur) {
                 // crossings k = 0, 1, ... with phin + k pi < phi0 (at most 16)
                 if (phi0 > phin) nplane = min(int(ceilf((phi0 - phin) * (1.0f / kPi))), 16);
-                if (!cap && thin && nplane > 0) {
-                    // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
-                    // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
-                    // where the orbit stays outside them)
-                    const float4 L = cubic_weights(gx - float(jc));
-                    Ic = cubic(__ldg(E + kExitIc + jc), L);
-                    const float4 rg = __ldg(E + kExitRange + m);
-                    const float t = gx - float(m);
-                    Ilo = fmaf(t, rg.z - rg.x, rg.x);
-                    Ihi = fmaf(t, rg.w - rg.y, rg.y);
-                }
+                // crossing k lies in [0.97 r_in, 1.03 r_out] iff its angle from the turning point,
+                // |phi_k - Ic|, lies between the sweeps to those radii (or to the turning point,
+                // where the orbit stays outside them): [Ilo, Ihi] from the exit table
 #pragma unroll 1
                 for (int k = 0; k < nplane && ncand < kMaxCand; ++k) {
                     const float phk = phin + float(k) * kPi;
@@ -1324,7 +1326,9 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
                 const float beta = G.beta[own];
                 const orbit::Roots<float> Rt = orbit::roots<float, 4>(fmaxf(beta, 1e-7f));
                 const bool leg = (kl & 16u) != 0;
-                const float u = orbit::invert_sweep_v<float, 4, kNet>(leg ? phk - Ic : Ic - phk, Rt, beta);
+                // three Newton steps: within 2e-6 of the crossing's u (relative) for every crossing
+                // of the disk's radii (the fourth step measured 1% of the step for nothing visible)
+                const float u = orbit::invert_sweep_v<float, 3, kNet>(leg ? phk - Ic : Ic - phk, Rt, beta);
                 us = u;
                 if (kNet) {  // the network's residual from the view's crossing table, applied along the orbit
                     const float sg =
