@@ -50,6 +50,13 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 __device__ __forceinline__ uint32_t lds32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+// one 32-byte store (p 32-byte aligned)
+__device__ __forceinline__ void st_global_v8(const void* p, uint32_t a, uint32_t b, uint32_t c, uint32_t d, uint32_t e,
+                                             uint32_t f, uint32_t g, uint32_t h) {
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(a), "r"(b), "r"(c), "r"(d),
+                 "r"(e), "r"(f), "r"(g), "r"(h)
+                 : "memory");
+}
 __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
     return uint32_t(__bfloat16_as_ushort(lo)) | (uint32_t(__bfloat16_as_ushort(hi)) << 16);
 }
@@ -1173,6 +1180,9 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
     constexpr float kPi = 3.14159265358979f;
     const float beta_band = nm.band / kSqrt27f;
     const float uc = sv.uc;
+    // records go out as two 32-byte stores when the view's buffer allows it (records are 64 B,
+    // so every record is then 32-byte aligned); the interface guarantees 16 bytes
+    const bool out32 = (reinterpret_cast<uintptr_t>(w.out) & 31u) == 0;
     const bool thin = R.disk_mode == BHR_DISK_THIN;
     const float4* E = sv.exit_table;
     uint32_t n_surr = 0, n_dis = 0;
@@ -1397,11 +1407,20 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
                 }
                 const uint32_t nplane = (info >> 3) & 0xffu;
                 const uint32_t w0 = status | (uint32_t(nrec) << 8) | (uint32_t(BHR_FLAG_SURROGATE) << 16) | (nplane << 24);
-                float4* p = reinterpret_cast<float4*>(w.out + ray);
-                p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
-                p[1] = make_float4(d.z, min_r, 0.f, 0.f);
-                p[2] = make_float4(G.baxis[lane], G.b[lane], cr[0], cr[1]);
-                p[3] = make_float4(cr[2], cph[0], cph[1], cph[2]);
+                if (out32) {  // two 32-byte stores: each covers whole sectors
+                    st_global_v8(w.out + ray, w0, 0u, __float_as_uint(d.x), __float_as_uint(d.y),
+                                 __float_as_uint(d.z), __float_as_uint(min_r), 0u, 0u);
+                    st_global_v8(reinterpret_cast<const char*>(w.out + ray) + 32, __float_as_uint(G.baxis[lane]),
+                                 __float_as_uint(G.b[lane]), __float_as_uint(cr[0]), __float_as_uint(cr[1]),
+                                 __float_as_uint(cr[2]), __float_as_uint(cph[0]), __float_as_uint(cph[1]),
+                                 __float_as_uint(cph[2]));
+                } else {
+                    float4* p = reinterpret_cast<float4*>(w.out + ray);
+                    p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
+                    p[1] = make_float4(d.z, min_r, 0.f, 0.f);
+                    p[2] = make_float4(G.baxis[lane], G.b[lane], cr[0], cr[1]);
+                    p[3] = make_float4(cr[2], cph[0], cph[1], cph[2]);
+                }
             }
         }
         __syncwarp();

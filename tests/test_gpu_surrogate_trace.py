@@ -336,6 +336,23 @@ def test_surrogate_host_buffers_overlapping_pipelines(surrogate):
             assert np.array_equal(a.cpu().numpy().view(np.uint8), h.view(np.uint8)), k
 
 
+def test_records_equal_for_16_and_32_byte_aligned_outputs(surrogate):
+    """The pass writes a record as two 32-byte stores when the view's output is 32-byte aligned
+    and as four 16-byte stores when it is only 16-byte aligned (all the interface asks): both
+    give the same bytes."""
+    import torch
+
+    views = workloads.c2_views(TERM_CONFIG, width=640, height=360)[:2]
+    a = surrogate.trace(views)
+    big = [torch.empty(v.rays * 64 + 32, dtype=torch.uint8, device="cuda") for v in views]
+    outs = [b[16:16 + v.rays * 64] for b, v in zip(big, views)]
+    assert all(o.data_ptr() % 32 == 16 for o in outs)
+    surrogate.trace(views, outs)
+    torch.cuda.synchronize()
+    for x, y in zip(a, outs):
+        assert torch.equal(x, y)
+
+
 def test_surrogate_plan_refuses_after_work_memory_grows():
     """A plan holds pointers into the surrogate's work memory: after a larger trace reallocates it
     (here 20 views, past the crossing tables' 16-view allocation), the plan's launch is refused
