@@ -732,11 +732,9 @@ constexpr uint32_t kCapBit = 1u << 26;        // stage info: the ray's orbit is 
 struct RayStage {  // per warp, structure of arrays over its 32 rays
     float s0[32], s1[32], s2[32], s3[32];  // captured orbit: u1, A, k^2, K
     float ic[32];      // angle camera -> turning point (escaping), F(camera) (captured)
-    float psi[32];     // escaping: in-plane escape direction minus pi
-    float minr[32];    // escaping: periapsis 1 / u2
     float phin[32], x2[32], beta[32];
-    float e2x[32], e2y[32], e2z[32];
-    float baxis[32], b[32];
+    float e2x[32], e2z[32];
+    float b[32];
     uint32_t info[32];  // bits 0-1 candidates, 2 surrogate, 3-10 plane crossings, 11+5c candidate c (k | leg << 4),
                         // 26 captured orbit
 };
@@ -1198,6 +1196,10 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
         const bool pre = sv.band_mask != nullptr && ((__ldg(sv.band_mask + chunk) >> lane) & 1u) != 0u;
         // ---- phase 1: per ray
         int ncand = 0;
+        // what only this lane's record needs stays in registers through phase 2
+        float o_psi = 0.f, o_minr = 0.f, o_baxis = 0.f, o_b = 0.f;
+        V3<float> o_e2{0.f, 0.f, 0.f};
+        uint32_t o_info = 0;
         {
             bool sur = valid && !pre;
             const int j = valid ? ray / w.width : 0, i = valid ? ray - j * w.width : 0;
@@ -1300,18 +1302,19 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
             G.s2[lane] = s2;
             G.s3[lane] = s3;
             G.ic[lane] = Ic;
-            G.psi[lane] = psi;
-            G.minr[lane] = minr;
             G.phin[lane] = phin;
             G.x2[lane] = x2;
             G.beta[lane] = beta;
             G.e2x[lane] = e2.x;
-            G.e2y[lane] = e2.y;
             G.e2z[lane] = e2.z;
-            G.baxis[lane] = ri.b_axis;
             G.b[lane] = b;
-            G.info[lane] = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw |
-                           (cap ? kCapBit : 0u);
+            o_info = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw | (cap ? kCapBit : 0u);
+            G.info[lane] = o_info;
+            o_psi = psi;
+            o_minr = minr;
+            o_baxis = ri.b_axis;
+            o_b = b;
+            o_e2 = e2;
         }
         // ---- phase 2: crossing candidates, compacted over the lanes
         int off = ncand;
@@ -1367,7 +1370,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
         __syncwarp();
         // ---- phase 3: records (per ray)
         {
-            const uint32_t info = G.info[lane];
+            const uint32_t info = o_info;
             const bool sur = (info & 4u) != 0;
             const bool cap = (info & kCapBit) != 0;
             if (valid && !sur && !pre) fb_list[warp_append_ull(&q->fb_count)] = ray;
@@ -1379,10 +1382,10 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
                 uint32_t status = BHR_STATUS_CAPTURED;
                 if (!cap) {  // the escape direction cos(psi) e1 + sin(psi) e2, psi = pi + the table's angle
                     float sp, cp;
-                    sincos_rr(G.psi[lane], &sp, &cp);
-                    d = {-(cp * w.rhat[0] + sp * G.e2x[lane]), -(cp * w.rhat[1] + sp * G.e2y[lane]),
-                         -(cp * w.rhat[2] + sp * G.e2z[lane])};
-                    min_r = G.minr[lane];
+                    sincos_rr(o_psi, &sp, &cp);
+                    d = {-(cp * w.rhat[0] + sp * o_e2.x), -(cp * w.rhat[1] + sp * o_e2.y),
+                         -(cp * w.rhat[2] + sp * o_e2.z)};
+                    min_r = o_minr;
                     status = BHR_STATUS_ESCAPED;
                 }
                 // crossings inside [disk_inner, disk_outer], in march order
@@ -1410,15 +1413,15 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
                 if (out32) {  // two 32-byte stores: each covers whole sectors
                     st_global_v8(w.out + ray, w0, 0u, __float_as_uint(d.x), __float_as_uint(d.y),
                                  __float_as_uint(d.z), __float_as_uint(min_r), 0u, 0u);
-                    st_global_v8(reinterpret_cast<const char*>(w.out + ray) + 32, __float_as_uint(G.baxis[lane]),
-                                 __float_as_uint(G.b[lane]), __float_as_uint(cr[0]), __float_as_uint(cr[1]),
+                    st_global_v8(reinterpret_cast<const char*>(w.out + ray) + 32, __float_as_uint(o_baxis),
+                                 __float_as_uint(o_b), __float_as_uint(cr[0]), __float_as_uint(cr[1]),
                                  __float_as_uint(cr[2]), __float_as_uint(cph[0]), __float_as_uint(cph[1]),
                                  __float_as_uint(cph[2]));
                 } else {
                     float4* p = reinterpret_cast<float4*>(w.out + ray);
                     p[0] = make_float4(__uint_as_float(w0), __uint_as_float(0u), d.x, d.y);
                     p[1] = make_float4(d.z, min_r, 0.f, 0.f);
-                    p[2] = make_float4(G.baxis[lane], G.b[lane], cr[0], cr[1]);
+                    p[2] = make_float4(o_baxis, o_b, cr[0], cr[1]);
                     p[3] = make_float4(cr[2], cph[0], cph[1], cph[2]);
                 }
             }
