@@ -713,8 +713,8 @@ __global__ void __launch_bounds__(128, 4) k_mlp_infer(const float* __restrict__ 
 // alone (the camera radius and the rule are the view's): the exit angle with the network's
 // residual, the escape direction in the orbital plane after farFieldDirection at the exit, the
 // angle to the turning point, the periapsis and the capture logit. The view's exit table
-// (k_exit_table, launched before the pass) holds them per point of x2, and the crossing table
-// (k_cross_table) the network's residual for crossing queries. The rays interpolate them:
+// (built by k_tables before the pass) holds them per point of x2, and its crossing table the
+// network's residual for crossing queries. The rays interpolate them:
 //   1  per ray (lane): setup and routing, the orbital plane, the exit table, and the disk-plane
 //      crossings inside the disk's angle range (candidates, found without inverting the orbit);
 //      captured orbits take the exact one-real-root form
@@ -1024,10 +1024,10 @@ __global__ void __launch_bounds__(256) k_exit_table_cf(const __grid_constant__ S
 // view's exit table (the escaping half per branch of the rule's exit, the captured half) and
 // crossing table, as 128-row tiles of network queries. A block is one warpgroup with its own TMEM
 // accumulator; it stages the network once (tc::load_net, tc::load_l1) and then takes tiles until
-// the batch is done. Each thread forms its row's query (for an escaping exit point the closed form
-// of the point, as k_exit_table), the tile runs through tc::mlp_tile_l1f, and each thread writes
-// its row's results into the entries of the table that hold them (as k_exit_table and
-// k_cross_table do). A completion wait that runs out makes the block write NaN for its tile, set
+// the batch is done. Each thread forms its row's query (for an escaping exit point, from the closed
+// form at the point), the tile runs through tc::mlp_tile_l1f, and each thread writes its row's
+// results into the table entries that hold them (a point enters four cubic windows and two
+// linear pairs). A completion wait that runs out makes the block write NaN for its tile, set
 // *status and stop.
 __global__ void __launch_bounds__(128, 4) k_tables(const __grid_constant__ TabBatch B, const float* __restrict__ P,
                                                    int* __restrict__ status) {

@@ -252,7 +252,7 @@ __device__ __forceinline__ void act_to_a(uint32_t taddr, unsigned char* a, int r
 constexpr uint32_t kI64 = idesc_bf16(128, 64);
 constexpr uint32_t kI16 = idesc_bf16(128, 16);
 
-// Layer 1 in FP32 on the CUDA cores, as the training kernel and the mma.sync path compute it:
+// Layer 1 in FP32 on the CUDA cores, as the training kernel computes it:
 // per feature f, {w_x1, w_x2, w_sigma, b1} / 2 (halved, so that the pre-activation comes out as
 // h = z / 2 and silu(z) = fma(h, tanh h, h)).
 struct L1 {
@@ -316,7 +316,7 @@ __device__ inline bool mlp_tile_upper(const Net& N, Tile& T, uint32_t tmem, int 
 }
 
 // One 128-row tile with layer 1 in FP32 on the CUDA cores (the same arithmetic, the same BF16
-// activations as training and the mma.sync path) and layers 2, 3 and the output layer on the
+// activations as training) and layers 2, 3 and the output layer on the
 // tensor cores. Called by all 128 threads of a warpgroup with their own row's query; the other
 // arguments as mlp_tile's. The production form: the surrogate's tables and bhr_surrogate_eval.
 __device__ inline bool mlp_tile_l1f(const Net& N, const L1& l1, Tile& T, uint32_t tmem, int row, int bar_id,
