@@ -1163,7 +1163,7 @@ __device__ __forceinline__ float capture_logit(const SurrView& sv, float x2) {
 }
 
 template <bool kTol, bool kNet>
-__global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogate(const __grid_constant__ SurrView sv,
+__global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_surrogate(const __grid_constant__ SurrView sv,
                                                                 WorkQueue* q, int* __restrict__ fb_list) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
@@ -1184,17 +1184,19 @@ __global__ void __launch_bounds__(32 * kInferWarps, kSurrBlocksPerSM) k_surrogat
     const bool thin = R.disk_mode == BHR_DISK_THIN;
     const float4* E = sv.exit_table;
     uint32_t n_surr = 0, n_dis = 0;
-    // a warp claims two 32-ray chunks per atomic on the view's counter: one claim per chunk made
-    // the counter's atomics a serial point (65,000 a view; two per claim measured 6% faster)
+    // a warp claims four 32-ray chunks per atomic on the view's counter: one claim per chunk made
+    // the counter's atomics a serial point (65,000 a view; two per claim measured 6% faster, four
+    // another 0.5-2%, with the grid's four blocks per SM)
+    constexpr int kClaim = 4;
     unsigned long long claim = 0;
     int left = 0;
     for (;;) {
         if (left == 0) {
-            if (lane == 0) claim = atomicAdd(&q->next_chunk, 2ull);
+            if (lane == 0) claim = atomicAdd(&q->next_chunk, (unsigned long long)kClaim);
             claim = __shfl_sync(0xffffffffu, claim, 0);
-            left = 2;
+            left = kClaim;
         }
-        const unsigned long long chunk = claim + (unsigned long long)(2 - left);
+        const unsigned long long chunk = claim + (unsigned long long)(kClaim - left);
         --left;
         const int64_t base = (int64_t)chunk * 32;
         if (base >= w.nrays) break;

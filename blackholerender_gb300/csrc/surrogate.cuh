@@ -168,9 +168,9 @@ inline int tab_tiles(bool tol) { return kTabTilesExit * (tol ? 3 : 2) + kTabTile
 // Builds the batch's tables; *status becomes 1 if a tensor-core completion wait ran out (the
 // tables are then NaN where it did).
 cudaError_t launch_tables(const TabBatch& b, const float* params, int* status, int grid, cudaStream_t st);
-// Resident blocks per SM of the surrogate pass (its grid: SMs x this). Four fit (56 registers)
-// and measured 2% slower than three.
-constexpr int kSurrBlocksPerSM = 3;
+// Resident blocks per SM of the surrogate pass (its grid: SMs x this), per variant as measured:
+// the learned pass 2% faster with four than with three, the closed-form pass 5% slower.
+constexpr int surr_blocks_per_sm(bool net) { return net ? 4 : 3; }
 // The surrogate pass of one view (net: the learned variant, which reads the crossing table;
 // otherwise the converged closed form).
 cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_list, int grid, bool net,

@@ -688,7 +688,7 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         if (!net) e = bhr::surr::launch_exit_table_cf(sv, L.etab + kTab * k, vs);
         if (e == cudaSuccess)
             e = bhr::surr::launch_surrogate_trace(sv, L.q + 2 * k, L.fb + off[size_t(k)],
-                                                  s->sms * bhr::surr::kSurrBlocksPerSM, net, vs);
+                                                  s->sms * bhr::surr::surr_blocks_per_sm(net), net, vs);
     }
     for (int j = 0; e == cudaSuccess && j < 2; ++j) {
         e = cudaEventRecord(L.join[j], L.side[j]);
