@@ -93,9 +93,9 @@ template <class T> struct RayInit {
     T b;         // impact parameter h / |v_inf|
 };
 
-// blackhole.frag:68-93 for pixel (i, j) of view w, in arithmetic type T.
+// The unit direction of pixel (i, j) of view w (blackhole.frag:68-72), in arithmetic type T.
 template <class T>
-__device__ __forceinline__ RayInit<T> setup_ray(const DevView& w, const Rule& R, int i, int j) {
+__device__ __forceinline__ V3<T> pixel_dir(const DevView& w, int i, int j) {
     const T pxx = T(i) + T(0.5) + T(w.jitter[0]);
     const T pxy = T(j) + T(0.5) + T(w.jitter[1]);
     const T ndcx = pxx / T(w.width) * T(2) - T(1);
@@ -111,7 +111,13 @@ __device__ __forceinline__ RayInit<T> setup_ray(const DevView& w, const Rule& R,
             T(w.basis[1]) * dc.x + T(w.basis[4]) * dc.y + T(w.basis[7]) * dc.z,
             T(w.basis[2]) * dc.x + T(w.basis[5]) * dc.y + T(w.basis[8]) * dc.z};
     inv = M<T>::rsqrt(dot3(d, d));
-    d = {d.x * inv, d.y * inv, d.z * inv};
+    return {d.x * inv, d.y * inv, d.z * inv};
+}
+
+// blackhole.frag:68-93 for pixel (i, j) of view w, in arithmetic type T.
+template <class T>
+__device__ __forceinline__ RayInit<T> setup_ray(const DevView& w, const Rule& R, int i, int j) {
+    const V3<T> d = pixel_dir<T>(w, i, j);
     V3<T> cam;
     T baxis_scale, lapse;
     V3<T> rh;
@@ -135,7 +141,7 @@ __device__ __forceinline__ RayInit<T> setup_ray(const DevView& w, const Rule& R,
         const T nr = dot3(d, rh);
         const T nrf = nr * lapse - nr;
         V3<T> v{d.x + nrf * rh.x, d.y + nrf * rh.y, d.z + nrf * rh.z};
-        inv = M<T>::rsqrt(dot3(v, v));
+        const T inv = M<T>::rsqrt(dot3(v, v));
         v = {v.x * inv, v.y * inv, v.z * inv};
         const V3<T> hv{cam.y * v.z - v.y * cam.z, cam.z * v.x - v.z * cam.x, cam.x * v.y - v.x * cam.y};
         o.v = v;

@@ -1213,9 +1213,14 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
         {
             bool sur = valid && !pre;
             const int j = valid ? ray / w.width : 0, i = valid ? ray - j * w.width : 0;
-            const RayInit<float> ri = setup_ray<float>(w, R, i, j);
-            const V3<float> cam{w.cam[0], w.cam[1], w.cam[2]};
-            float b = ri.b;
+            // the pixel's direction (as the plain march's setup), its angle from the radial
+            // direction e1 and b = r sin(angle) / sqrt(1 - 2 / r): the reference's h / |v_inf| for
+            // the initial velocity of geodesic.glsl:27-34 (whose radial part the lapse scales),
+            // without forming that velocity; its tangential part, and so the orbital plane, is d's
+            const V3<float> d = pixel_dir<float>(w, i, j);
+            const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
+            const V3<float> cx{e1.y * d.z - e1.z * d.y, e1.z * d.x - e1.x * d.z, e1.x * d.y - e1.y * d.x};
+            float b = sv.b_scale * sqrtf(dot3(cx, cx));
             float beta = b * (1.0f / kSqrt27f) - 1.0f;
             if (sur && fabsf(beta) < 0.02f) {  // near the photon sphere: impact parameter in FP64
                 const double bd = impact_parameter_fp64(w, sv.fc, i, j);
@@ -1225,12 +1230,11 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
             // captured orbits (b < sqrt(27)) are answered too: the network gives their capture flag,
             // the closed form their crossings (no turning point, no learned residual)
             const bool cap = beta < 0.f;
-            sur = sur && dot3(cam, ri.v) < 0.f && w.rcam >= nm.rc_lo && w.rcam <= nm.rc_hi && b <= nm.b_max &&
+            const float ve = dot3(d, e1);  // ingoing at the camera: ve < 0
+            sur = sur && ve < 0.f && w.rcam >= nm.rc_lo && w.rcam <= nm.rc_hi && b <= nm.b_max &&
                   fabsf(beta) >= beta_band;
-            // orbital plane: e1 along the camera, e2 along the tangential part of the velocity
-            const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
-            const float ve = dot3(ri.v, e1);
-            V3<float> e2{ri.v.x - ve * e1.x, ri.v.y - ve * e1.y, ri.v.z - ve * e1.z};
+            // orbital plane: e1 along the camera, e2 along the tangential part of the direction
+            V3<float> e2{d.x - ve * e1.x, d.y - ve * e1.y, d.z - ve * e1.z};
             const float e2n = dot3(e2, e2);
             sur = sur && e2n > 1e-12f;
             const float e2i = rsqrtf(fmaxf(e2n, 1e-30f));
@@ -1307,22 +1311,26 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
                     }
                 }
             }
-            G.s0[lane] = s0;
-            G.s1[lane] = s1;
-            G.s2[lane] = s2;
-            G.s3[lane] = s3;
-            G.ic[lane] = Ic;
-            G.phin[lane] = phin;
-            G.x2[lane] = x2;
-            G.beta[lane] = beta;
-            G.e2x[lane] = e2.x;
-            G.e2z[lane] = e2.z;
-            G.b[lane] = b;
+            // phase 2 reads the stage of rays with candidates only
+            if (__any_sync(0xffffffffu, ncand > 0)) {
+                G.s0[lane] = s0;
+                G.s1[lane] = s1;
+                G.s2[lane] = s2;
+                G.s3[lane] = s3;
+                G.ic[lane] = Ic;
+                G.phin[lane] = phin;
+                G.x2[lane] = x2;
+                G.beta[lane] = beta;
+                G.e2x[lane] = e2.x;
+                G.e2z[lane] = e2.z;
+                G.b[lane] = b;
+            }
             o_info = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw | (cap ? kCapBit : 0u);
             G.info[lane] = o_info;
             o_psi = psi;
             o_minr = minr;
-            o_baxis = ri.b_axis;
+            // impactParameterAboutAxis: -dot(cross(cam, dir), +Y) / sqrt(max(1 - 2/r, 1e-6))
+            o_baxis = -(w.cam[2] * d.x - d.z * w.cam[0]) * w.baxis_scale;
             o_b = b;
             o_e2 = e2;
         }

@@ -111,6 +111,7 @@ struct SurrView {
     float tab_lo[2], tab_h[2], tab_inv_h[2];  // x2 of a half's first point, spacing, 1 / spacing
     const float4* cross_table;  // [kCrossCells] y at the cell's corners (i, j), (i, j+1), (i+1, j), (i+1, j+1)
     float cx_h, cx_inv_h;       // the cross table's x2 spacing (first point tab_lo[1]) and its inverse
+    float b_scale;          // r_cam / sqrt(1 - 2 / r_cam): b = b_scale sin(angle from the radial direction)
     Fp64Cam fc;             // the FP64 impact parameter near the photon sphere
     // the rays of the view's photon-sphere band that the band march takes (bit ray % 32 of word
     // ray / 32; they are skipped here), or nullptr when no band march runs

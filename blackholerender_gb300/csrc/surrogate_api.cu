@@ -574,6 +574,7 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
             fc.rhat_d[1] = cy / rc;
             fc.rhat_d[2] = cz / rc;
             fc.b_scale_d = rc / std::sqrt(std::max(1.0 - 2.0 / rc, 1e-300));
+            sv.b_scale = float(fc.b_scale_d);
             // the camera's tangential ray has b = b_scale_d
             const double beta_t = fc.b_scale_d / 5.196152422706632 - 1.0;
             const double x2_t = std::log1p(beta_t / double(s->norm.t_eps)) * double(s->norm.t_scale);
