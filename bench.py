@@ -317,7 +317,9 @@ def run_reference(args):
     if rank != 0:
         return
     views = oracle_c2_views(TERM_CONFIG)[:args.views]
-    per_step_s = 4.0
+    # a bounded sample per step: 4 s of CPU march, less when many steps are asked for, so that the
+    # whole run stays within about three minutes
+    per_step_s = max(0.25, min(4.0, 180.0 / max(args.steps, 1)))
     for _ in range(args.warmup):
         cpu_march_sample(views, 0.5, seed=99)
     vals = []
@@ -329,7 +331,7 @@ def run_reference(args):
         rays_total += rays
     wall = time.perf_counter() - t0
     value = rays_total / wall / 1e6
-    sample = (f"random pixels of the 16 poses, {per_step_s:.0f} s of CPU march per step "
+    sample = (f"random pixels of the 16 poses, {per_step_s:.2f} s of CPU march per step "
               f"({rays_total / max(args.steps, 1):.0f} rays/step), FP64 restatement of the shader march")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,

@@ -412,6 +412,15 @@ __global__ void __launch_bounds__(BS) k_march_multi_list(const __grid_constant__
     __shared__ uint8_t s_pool_view[BS / 32][kPool];
     __shared__ DevView s_views[kMaxViews];
     __shared__ int64_t s_total;
+    // the lists' lengths first: an empty set of lists (the usual case after the band march) ends
+    // the block before it copies the views or claims work
+    if (threadIdx.x == 0) {
+        int64_t n = 0;
+        for (int v = 0; v < batch.nviews; ++v) n += (int64_t)qv[2 * v].fb_count;
+        s_total = n;
+    }
+    __syncthreads();
+    if (s_total == 0) return;
     const int nwords = batch.nviews * (int)(sizeof(DevView) / 4);
     for (int k = threadIdx.x; k < nwords; k += BS)
         reinterpret_cast<uint32_t*>(s_views)[k] = reinterpret_cast<const uint32_t*>(batch.views)[k];
@@ -427,7 +436,6 @@ __global__ void __launch_bounds__(BS) k_march_multi_list(const __grid_constant__
         s_total = acc;
     }
     __syncthreads();
-    if (s_total == 0) return;  // an empty list (the usual case after the band march): no claims on the counter
     const int wid = threadIdx.x >> 5;
     march_warp<true, kTerm, kDisk, false, true>(s_views, batch.nviews, s_total, batch.rule, sc, chunk, refill_min,
                                                 Pool{s_pool[wid], s_pool_view[wid]}, list, 0);

@@ -710,7 +710,9 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
         b.total_chunks = 0;
         for (int k = 0; k < nviews; ++k) b.views[k] = dvs[size_t(k)];
         cfg.variant = bhr::rule_variant(b.rule);
-        cfg.grid = s->sms * std::max(1, bhr::march_blocks_per_sm(512, cfg.variant, true, false));
+        // one block per SM: the list is usually empty (the band march took the band rays), and
+        // 16 warps per SM still spread a few thousand rays in claims of 32
+        cfg.grid = s->sms;
         const bhr::Scratch sc{L.q + 2 * nviews, nullptr, nullptr};
         e = bhr::launch_march_multi_list(b, sc, L.fb, L.q, cfg, st);
     } else {
