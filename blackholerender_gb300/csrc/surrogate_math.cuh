@@ -243,20 +243,60 @@ __host__ __device__ __forceinline__ T dudphi(T u, const Roots<T>& R) {
     return tsqrt<T>(p > T(0) ? p : T(0));
 }
 
+// One duplication step of R_F(x, y, z), with sqrt(y) given.
+template <class T>
+__host__ __device__ __forceinline__ void rf_dup(T& x, T& y, T& z, T sy) {
+    const T sx = tsqrt<T>(x), sz = tsqrt<T>(z);
+    const T lam = sx * sy + sy * sz + sz * sx;
+    x = T(0.25) * (x + lam);
+    y = T(0.25) * (y + lam);
+    z = T(0.25) * (z + lam);
+}
+// R_F after its duplication steps: the fifth-order series at the mean of (x, y, z), as rf.
+template <class T>
+__host__ __device__ __forceinline__ T rf_tail(T x, T y, T z) {
+    const T A = (x + y + z) * T(1.0 / 3.0);
+    const T iA = FM<T>::rcp(A);
+    const T X = T(1) - x * iA, Y = T(1) - y * iA, Z = -(X + Y);
+    const T E2 = X * Y - Z * Z, E3 = X * Y * Z;
+    const T s = T(1) - E2 * T(0.1) + E3 * T(1.0 / 14.0) + E2 * E2 * T(1.0 / 24.0) - T(3.0 / 44.0) * E2 * E3;
+    return FM<T>::div_sqrt(s, A);
+}
+
 // Solves I(u) = target for u in [0, u2] on a variant's closed form (Baseline<kNet>::sweep), by
-// Newton in s = sqrt(u2 - u) as invert_sweep below.
+// Newton in s = sqrt(u2 - u) as invert_sweep below, with the sweep written for it: in
+// I = sqrt(2) s R_F((u - u1) d32, (u2 - u1) d32, (u3 - u)(u2 - u1)) the factor sqrt(u2 - u) is s,
+// the middle argument and its square root are the same at every u, the first guess is the slope
+// at the turning point, sqrt(2) R_F(y, y, y) = sqrt(2 / y), and the learned variant's second
+// duplication step (its blend near the photon sphere) continues from the first.
 template <class T, int kIters, bool kNet>
 __host__ __device__ __forceinline__ T invert_sweep_v(T target, const Roots<T>& R, T beta) {
-    const T X0 = (R.u2 - R.u1) * R.d32;
-    const T Z0 = R.d32 * (R.u2 - R.u1);
-    const T slope0 = T(1.4142135623730951) * rf<T, kBaseDup>(X0, X0, Z0);
+    const T d21 = R.u2 - R.u1;
+    const T Y = d21 * R.d32;
+    const T sY = tsqrt<T>(Y);
     const T smax = tsqrt<T>(R.u2);
-    T s = FM<T>::div(target, slope0);
+    T s = target * sY * T(0.70710678118654752);
     s = s < T(0) ? T(0) : (s > smax ? smax : s);
+    const T blend = kNet ? base_blend<T>(beta) : T(0);
 #pragma unroll 1
     for (int k = 0; k < kIters; ++k) {
         const T u = R.u2 - s * s;
-        const T f = Baseline<kNet>::template sweep<T>(u, R, beta) - target;
+        T x = (u - R.u1) * R.d32, y = Y, z = (R.u3 - u) * d21;
+        rf_dup<T>(x, y, z, sY);
+        T rfv;
+        if constexpr (kNet) {
+            static_assert(kBaseDup == 1, "the learned baseline takes one duplication step, two in its blend");
+            rfv = rf_tail<T>(x, y, z);
+            if (blend > T(0)) {
+                rf_dup<T>(x, y, z, tsqrt<T>(y));
+                rfv += blend * (rf_tail<T>(x, y, z) - rfv);
+            }
+        } else {
+#pragma unroll
+            for (int d = 1; d < kClosedDup; ++d) rf_dup<T>(x, y, z, tsqrt<T>(y));
+            rfv = rf_tail<T>(x, y, z);
+        }
+        const T f = T(1.4142135623730951) * s * rfv - target;
         s -= f * T(0.5) * tsqrt<T>(T(2) * (u - R.u1) * (R.u3 - u));
         s = s < T(0) ? T(0) : (s > smax ? smax : s);
     }
