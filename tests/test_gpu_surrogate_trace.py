@@ -336,6 +336,44 @@ def test_surrogate_host_buffers_overlapping_pipelines(surrogate):
             assert np.array_equal(a.cpu().numpy().view(np.uint8), h.view(np.uint8)), k
 
 
+def test_band_march_and_fallback_agree_and_cover_every_ray(surrogate):
+    """The photon-sphere band's rays are marched beside the passes when the views share one rule
+    (k_band_list finds them), else after the passes from the fallback list. Views that stress the
+    band search, each traced alone (band march) and next to a SHADER-rule view (two rules: no
+    band march): a camera turned so that the image edge cuts the photon ring, a wide-angle camera
+    turned so far that the search gate refuses the view, and a 1080p pose. Both ways give the same
+    records byte for byte; every record is written once (one of the two flags, a valid status);
+    classification equals the FP64 oracle on sampled pixels and on every marched pixel."""
+    import torch
+
+    from blackholerender_gb300 import make_view
+
+    cut = make_view(TERM_CONFIG, width=480, height=270, preset=2, look_at=((0.0, 3.0, 30.0), (25.0, 0.0, 0.0)))
+    wide = make_view(TERM_CONFIG, width=480, height=270, preset=2, fov_deg=120.0,
+                     look_at=((0.0, 3.0, 30.0), (150.0, 0.0, 0.0)))
+    pose = workloads.c2_views(TERM_CONFIG)[0]
+    other = make_view(TERM_SHADER, width=64, height=36, preset=2, pose=(30.0, 1.45, 0.0))
+    rng = np.random.default_rng(29)
+    for name, v in (("edge-cut ring", cut), ("wide, gate refused", wide), ("1080p pose 0", pose)):
+        (alone,) = surrogate.trace([v])
+        torch.cuda.synchronize()
+        st = surrogate.trace_stats()
+        mixed = surrogate.trace([v, other])
+        torch.cuda.synchronize()
+        assert torch.equal(alone, mixed[0]), name
+        g = hits_numpy(alone.cpu())
+        s_ = (g["flags"] & FLAG_SURROGATE) != 0
+        f_ = (g["flags"] & FLAG_FALLBACK) != 0
+        assert np.all(s_ ^ f_) and np.all(np.isin(g["status"], (1, 2, 3))), name
+        assert int(f_.sum()) == st["fallback"] and int(s_.sum()) == st["surrogate"], (name, int(f_.sum()), st)
+        marched = np.nonzero(f_)[0]
+        idx = np.unique(np.concatenate([rng.choice(v.rays, 3000, replace=False), marched[:4000]]))
+        ref = O.trace_pixels(v, idx, fp64=True)
+        rep = parity.compare(g[idx], ref, max_steps=v.max_steps, band=2e-3, edge_rel=EDGE_REL)
+        assert rep.class_mismatch == 0, (name, rep.as_dict())
+        print(f"\n{name}: {int(f_.sum())} rays marched by the integrator, {int(s_.sum())} answered by the surrogate")
+
+
 def test_records_equal_for_16_and_32_byte_aligned_outputs(surrogate):
     """The pass writes a record as two 32-byte stores when the view's output is 32-byte aligned
     and as four 16-byte stores when it is only 16-byte aligned (all the interface asks): both
