@@ -245,9 +245,37 @@ class Tracer:
                                                ctypes.c_void_p(stream.cuda_stream)), self._ctx)
         return hits, body_hits
 
+    def trace_bodies_volumetric(self, view: View, bodies: Sequence[Body], params: ShadeParams | None = None,
+                                hits=None, body_hits=None, rgbt=None, stream=None):
+        """bhr_trace_bodies_volumetric: one view marched with bodies and the volumetric disk.
+        Returns (hits, body_hits, rgbt): the records, the body records and a (height, width, 4)
+        float32 tensor of the gathered rgb and transmittance, which shade_bodies(..., out=rgbt)
+        completes in place."""
+        import torch
+
+        dev = torch.device("cuda", self.device)
+        if params is None:
+            params = shade_params()
+        if hits is None:
+            hits = torch.empty(view.rays * HIT_BYTES, dtype=torch.uint8, device=dev)
+        if body_hits is None:
+            body_hits = torch.empty(view.rays * 64, dtype=torch.uint8, device=dev)
+        if rgbt is None:
+            rgbt = torch.empty((view.height, view.width, 4), dtype=torch.float32, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        n = len(bodies)
+        arr = (Body * max(n, 1))(*bodies)
+        _abi.check(_abi.lib().bhr_trace_bodies_volumetric(
+            self._ctx, ctypes.byref(view), arr, n, ctypes.byref(params), ctypes.c_void_p(hits.data_ptr()),
+            ctypes.c_void_p(body_hits.data_ptr()), ctypes.c_void_p(rgbt.data_ptr()),
+            ctypes.c_void_p(stream.cuda_stream)), self._ctx)
+        return hits, body_hits, rgbt
+
     def shade_bodies(self, view: View, hits, body_hits, bodies: Sequence[Body], params: ShadeParams | None = None,
                      out=None, stream=None):
-        """bhr_shade_bodies: shades a view marched by trace_bodies; (height, width, 4) float32."""
+        """bhr_shade_bodies: shades a view marched by trace_bodies; (height, width, 4) float32. A
+        volumetric view is shaded in place: pass the rgbt of trace_bodies_volumetric as `out`."""
         import torch
 
         dev = torch.device("cuda", self.device)

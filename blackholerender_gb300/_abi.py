@@ -222,6 +222,8 @@ SIGNATURES = {
     "bhr_trace_volumetric": (ctypes.c_int, [_P, _VP, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(ShadeParams),
                                             ctypes.POINTER(_P), _P]),
     "bhr_trace_bodies": (ctypes.c_int, [_P, _VP, ctypes.POINTER(Body), ctypes.c_int, _P, _P, _P]),
+    "bhr_trace_bodies_volumetric": (ctypes.c_int, [_P, _VP, ctypes.POINTER(Body), ctypes.c_int,
+                                                   ctypes.POINTER(ShadeParams), _P, _P, _P, _P]),
     "bhr_shade_bodies": (ctypes.c_int, [_P, _VP, _P, _P, ctypes.POINTER(Body), ctypes.c_int, ctypes.POINTER(ShadeParams),
                                         _P, _P]),
     "bhr_noise_bake": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P]),

@@ -744,34 +744,56 @@ int bhr_blackbody_lut(float* out) {
     return BHR_OK;
 }
 
-int bhr_trace_bodies(bhr_ctx* c, const bhr_view* view, const bhr_body* bodies, int nbodies, bhr_hit* hits,
-                     bhr_body_hit* body_out, void* cuda_stream) {
+namespace {
+
+// The arguments both body marches check; `volumetric` selects which disk modes are accepted.
+int check_body_march(bhr_ctx* c, const char* at, const bhr_view* view, const bhr_body* bodies, int nbodies,
+                     const bhr_hit* hits, const bhr_body_hit* body_out, bool volumetric) {
+    const std::string who(at);
     if (!c || !view || !hits || !body_out || nbodies < 0 || (nbodies > 0 && !bodies))
-        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: NULL argument");
+        return fail(c, BHR_ERR_INVALID_ARG, who + ": NULL argument");
     if (nbodies > BHR_MAX_BODIES)
-        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: at most BHR_MAX_BODIES (32) bodies per view");
+        return fail(c, BHR_ERR_INVALID_ARG, who + ": at most BHR_MAX_BODIES (32) bodies per view");
     const bhr_view& v = *view;
     if (v.width <= 0 || v.height <= 0 || v.max_steps < 0)
-        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: width and height must be positive, max_steps >= 0");
-    if (v.disk_mode != BHR_DISK_NONE && v.disk_mode != BHR_DISK_THIN)
-        return fail(c, BHR_ERR_UNSUPPORTED, "bhr_trace_bodies: bodies are marched with a thin disk or none");
+        return fail(c, BHR_ERR_INVALID_ARG, who + ": width and height must be positive, max_steps >= 0");
+    if (volumetric && v.disk_mode != BHR_DISK_VOLUMETRIC)
+        return fail(c, BHR_ERR_INVALID_ARG, who + ": disk_mode must be BHR_DISK_VOLUMETRIC (bhr_trace_bodies marches the others)");
+    if (!volumetric && v.disk_mode != BHR_DISK_NONE && v.disk_mode != BHR_DISK_THIN)
+        return fail(c, BHR_ERR_UNSUPPORTED, who + ": the volumetric disk is marched with bodies by bhr_trace_bodies_volumetric");
+    if (volumetric && (!(v.disk_step > 0.0f) || !(v.disk_thickness > 0.0f)))
+        return fail(c, BHR_ERR_INVALID_ARG, who + ": disk_step and disk_thickness must be positive");
     if (v.term_mode != BHR_TERM_SHADER && v.term_mode != BHR_TERM_CONFIG)
-        return fail(c, BHR_ERR_UNSUPPORTED, "bhr_trace_bodies: bodies are marched under the SHADER or CONFIG rule");
+        return fail(c, BHR_ERR_UNSUPPORTED, who + ": bodies are marched under the SHADER or CONFIG rule");
     if (reinterpret_cast<uintptr_t>(hits) % 16 != 0 || reinterpret_cast<uintptr_t>(body_out) % 16 != 0)
-        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: buffers must be 16-byte aligned");
+        return fail(c, BHR_ERR_INVALID_ARG, who + ": buffers must be 16-byte aligned");
     for (int k = 0; k < nbodies; ++k)
         if (!(bodies[k].pos_radius[3] > 0.0f))
-            return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies: body " + std::to_string(k) + " has no positive radius");
-    int prev = 0;
-    cudaGetDevice(&prev);
-    cudaSetDevice(c->device);
+            return fail(c, BHR_ERR_INVALID_ARG, who + ": body " + std::to_string(k) + " has no positive radius");
+    return BHR_OK;
+}
+
+bhr::BodyArgs body_args(const bhr_view& v, const bhr_body* bodies, int nbodies, bhr_hit* hits, bhr_body_hit* body_out) {
     bhr::BodyArgs a{};
     a.view = bhr::host::make_dev_view(v, hits);
     a.rule = bhr::host::make_rule(v);
     a.nbodies = nbodies;
     a.body_out = body_out;
     for (int k = 0; k < nbodies; ++k) a.bodies[k] = bodies[k];
-    const cudaError_t e = bhr::launch_march_bodies(a, static_cast<cudaStream_t>(cuda_stream));
+    return a;
+}
+
+}  // namespace
+
+int bhr_trace_bodies(bhr_ctx* c, const bhr_view* view, const bhr_body* bodies, int nbodies, bhr_hit* hits,
+                     bhr_body_hit* body_out, void* cuda_stream) {
+    const int rc = check_body_march(c, "bhr_trace_bodies", view, bodies, nbodies, hits, body_out, false);
+    if (rc != BHR_OK) return rc;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const bhr::BodyArgs a = body_args(*view, bodies, nbodies, hits, body_out);
+    const cudaError_t e = bhr::launch_march_bodies(a, false, static_cast<cudaStream_t>(cuda_stream));
     cudaSetDevice(prev);
     return e == cudaSuccess ? BHR_OK : cuda_fail(c, e, "bhr_trace_bodies");
 }
@@ -864,6 +886,19 @@ int ensure_shade_resources(bhr_ctx* c, uint32_t seed, cudaStream_t st) {
     return BHR_OK;
 }
 
+// The volumetric disk's look for a march: the shading parameters, the view's thickness and the
+// context's textures (ensure_shade_resources first).
+bhr::DiskLook disk_look(const bhr_ctx* c, const bhr_shade_params& p, const bhr_view& v) {
+    bhr::DiskLook L{};
+    L.p = p;
+    L.ln_1000 = std::log(1000.0f);
+    L.ln_40000 = std::log(40000.0f);
+    L.thick = v.disk_thickness;
+    L.noise8 = c->noise8;
+    L.lut = c->lut;
+    return L;
+}
+
 }  // namespace
 
 int bhr_shade(bhr_ctx* c, const bhr_view* views, int nviews, const bhr_hit* const* hits, const bhr_shade_params* p,
@@ -932,8 +967,6 @@ int bhr_shade_bodies(bhr_ctx* c, const bhr_view* view, const bhr_hit* hits, cons
         return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade_bodies: at most BHR_MAX_BODIES (32) bodies per view");
     const bhr_view& v = *view;
     if (v.width <= 0 || v.height <= 0) return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade_bodies: width and height must be positive");
-    if (v.disk_mode == BHR_DISK_VOLUMETRIC)
-        return fail(c, BHR_ERR_UNSUPPORTED, "bhr_shade_bodies: bodies are shaded with a thin disk or none");
     if (reinterpret_cast<uintptr_t>(hits) % 16 != 0 || reinterpret_cast<uintptr_t>(body) % 16 != 0 ||
         reinterpret_cast<uintptr_t>(rgba) % 16 != 0)
         return fail(c, BHR_ERR_INVALID_ARG, "bhr_shade_bodies: buffers must be 16-byte aligned");
@@ -954,7 +987,7 @@ int bhr_shade_bodies(bhr_ctx* c, const bhr_view* view, const bhr_hit* hits, cons
         a.disk_inner = v.disk_inner;
         a.disk_outer = v.disk_outer;
         a.disk_thin = v.disk_mode == BHR_DISK_THIN;
-        a.volumetric = 0;
+        a.volumetric = v.disk_mode == BHR_DISK_VOLUMETRIC;
         a.far_mode = v.far_mode;
         a.lensing = (v.lensing != 0 && v.far_mode == 0) ? 1 : 0;
         a.p = *p;
@@ -1010,12 +1043,7 @@ int bhr_trace_volumetric(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit*
         bhr::VolArgs a{};
         a.view = bhr::host::make_dev_view(views[k], hits[k]);
         a.rule = bhr::host::make_rule(views[k]);
-        a.p = *p;
-        a.ln_1000 = std::log(1000.0f);
-        a.ln_40000 = std::log(40000.0f);
-        a.thick = views[k].disk_thickness;
-        a.noise8 = c->noise8;
-        a.lut = c->lut;
+        a.look = disk_look(c, *p, views[k]);
         a.rgbt = reinterpret_cast<float4*>(rgbt[k]);
         const cudaError_t e = bhr::launch_march_vol(a, fan.lane(k));
         if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace_volumetric: kernel launch");
@@ -1023,6 +1051,30 @@ int bhr_trace_volumetric(bhr_ctx* c, const bhr_view* views, int nviews, bhr_hit*
     {
         const cudaError_t e = fan.close();
         if (e != cudaSuccess && rc == BHR_OK) rc = cuda_fail(c, e, "bhr_trace_volumetric: side streams");
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int bhr_trace_bodies_volumetric(bhr_ctx* c, const bhr_view* view, const bhr_body* bodies, int nbodies,
+                                const bhr_shade_params* p, bhr_hit* hits, bhr_body_hit* body_out, float* rgbt,
+                                void* cuda_stream) {
+    int rc = check_body_march(c, "bhr_trace_bodies_volumetric", view, bodies, nbodies, hits, body_out, true);
+    if (rc != BHR_OK) return rc;
+    if (!p || !rgbt) return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies_volumetric: NULL argument");
+    if (reinterpret_cast<uintptr_t>(rgbt) % 16 != 0)
+        return fail(c, BHR_ERR_INVALID_ARG, "bhr_trace_bodies_volumetric: buffers must be 16-byte aligned");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    rc = ensure_shade_resources(c, p->noise_seed, st);
+    if (rc == BHR_OK) {
+        bhr::BodyArgs a = body_args(*view, bodies, nbodies, hits, body_out);
+        a.look = disk_look(c, *p, *view);
+        a.rgbt = reinterpret_cast<float4*>(rgbt);
+        const cudaError_t e = bhr::launch_march_bodies(a, true, st);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "bhr_trace_bodies_volumetric");
     }
     cudaSetDevice(prev);
     return rc;

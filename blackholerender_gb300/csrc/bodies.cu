@@ -1,5 +1,5 @@
-// The body-aware march (blackhole.frag's BHS_BODIES 1 variant with a thin or no disk): the
-// plain march plus spheres it can hit.
+// The body-aware march (blackhole.frag's BHS_BODIES 1 variant): the plain march, or the
+// volumetric disk's march (vol.cu), plus spheres it can hit.
 //   setup   (:101-121)  near-field bodies: a straight camera-relative ray along the geodesic's
 //                       initial direction is exact while the geodesic has not bent away, for
 //                       t < sqrt(0.02 R / |x''|); bodies wholly inside that stretch are settled
@@ -8,6 +8,9 @@
 //   step size (:184-190) land on the near-field hit; short steps near the other bodies
 //   after the step (:236-250) the step's straight chord against the other bodies
 // Shading the hit is the consumer's (bhr_shade_bodies); the march records where it happened.
+// With the volumetric disk (kVol) the steps in the slab are clamped to 6 diskStep and sampled
+// (:173-175,217-233) before the ray can turn opaque (:234) and before the step's chord is tested
+// against the bodies, so a body behind the disk keeps the light gathered in front of it.
 // One ray per thread, warps of 8 x 4 pixels; the bodies are kernel parameters (constant bank,
 // read warp-uniformly). FP32, like the shader.
 //
@@ -45,8 +48,14 @@ __device__ __forceinline__ float ray_sphere(V3<float> ro, V3<float> rd, V3<float
     return (t > t_min && t < t_max) ? t : -1.f;
 }
 
+template <bool kVol>
 __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ BodyArgs A) {
+    __shared__ float4 s_lut[kVol ? BHR_BLACKBODY_LUT : 1];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if constexpr (kVol) {
+        for (int k = tid; k < BHR_BLACKBODY_LUT; k += 256) s_lut[k] = A.look.lut[k];
+        __syncthreads();
+    }
     const DevView& w = A.view;
     const int i = blockIdx.x * 32 + (warp & 3) * 8 + (lane & 7);
     const int j = blockIdx.y * 8 + (warp >> 2) * 4 + (lane >> 3);
@@ -92,7 +101,11 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
     int hit = -1;
     V3<float> hit_ro{0.f, 0.f, 0.f}, hit_rd{0.f, 0.f, 0.f};
     float hit_t = 0.f;
-    const bool thin = R.disk_mode == BHR_DISK_THIN;
+    const bool thin = !kVol && R.disk_mode == BHR_DISK_THIN;
+    const shading::Tex tx{A.look.noise8, s_lut, A.look.ln_1000, A.look.ln_40000};
+    const shading::DiskConsts C = shading::disk_consts(A.look.p, rcam);
+    shading::F3 col{0.f, 0.f, 0.f};
+    float trans = 1.0f;
     float clear = -1.f;  // lower bound of |x - c| - R over the bodies the loops test; < 0: unknown
     if (R.far_mode) {
         status = BHR_STATUS_ESCAPED;
@@ -133,11 +146,17 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
                 }
             }
             float ds = fmaxf(ri.ssf * r, R.ds_floor);
-            if (thin) {
+            bool near_disk = false;
+            if (kVol || thin) {
                 const float rc2 = x.x * x.x + x.z * x.z;
                 if (rc2 > R.rcyl_lo2 && rc2 < R.rcyl_hi2) {
                     const float outside = fabsf(x.y) - R.slab * (rc2 * rsqrtf(rc2));
-                    if (outside > 0.f) ds = fminf(ds, fmaxf(w.disk_step, __fdividef(outside, fabsf(v.y) * vi + R.slab)));
+                    if (outside > 0.f) {
+                        ds = fminf(ds, fmaxf(w.disk_step, __fdividef(outside, fabsf(v.y) * vi + R.slab)));
+                    } else if (kVol) {  // inside the slab: sub-sampled after the step
+                        near_disk = true;
+                        ds = fminf(ds, 6.0f * w.disk_step);
+                    }
                 }
             }
             // land on the near-field hit; short steps near the other bodies (:184-190)
@@ -158,7 +177,7 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
                 }
             }
             const float dt = ds * vi;
-            const V3<float> x0 = x;
+            const V3<float> x0 = x, v0 = v;
             if (lensing) {
                 rk4_update(x, v, h2, dt, rinv);
             } else {
@@ -180,6 +199,13 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
                         cp[ncross] = atan2f(hz, hx);
                         ++ncross;
                     }
+                }
+            }
+            if (kVol && near_disk) {
+                vol_segment(tx, A.look, C, R, w.disk_step, ri.b_axis, x0, v0, x, v, dt, seg, col, trans);
+                if (trans < 0.004f) {  // blackhole.frag:234, before the chord test
+                    status = BHR_STATUS_OPAQUE;
+                    break;
                 }
             }
             // the step's chord against the bodies not settled by the near-field test (:236-250);
@@ -233,13 +259,17 @@ __global__ void __launch_bounds__(256) k_march_bodies(const __grid_constant__ Bo
     q[1] = make_float4(hit_ro.z, hit_rd.x, hit_rd.y, hit_rd.z);
     q[2] = make_float4(x.x, x.y, x.z, __uint_as_float(near_mask));
     q[3] = make_float4(__int_as_float(near_idx), near_t, travelled, 0.f);
+    if constexpr (kVol) A.rgbt[k] = make_float4(col.x, col.y, col.z, trans);
 }
 
 }  // namespace
 
-cudaError_t launch_march_bodies(const BodyArgs& a, cudaStream_t st) {
+cudaError_t launch_march_bodies(const BodyArgs& a, bool volumetric, cudaStream_t st) {
     const dim3 grid((a.view.width + 31) / 32, (a.view.height + 7) / 8);
-    k_march_bodies<<<grid, 256, 0, st>>>(a);
+    if (volumetric)
+        k_march_bodies<true><<<grid, 256, 0, st>>>(a);
+    else
+        k_march_bodies<false><<<grid, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 
 #include "bhr.h"
 #include "march.cuh"
+#include "vol.cuh"
 
 namespace bhr {
 
@@ -15,9 +16,12 @@ struct BodyArgs {
     int32_t nbodies;
     int32_t pad;
     bhr_body_hit* body_out;           // per pixel
+    DiskLook look;                    // the volumetric disk's look (volumetric views only)
+    float4* rgbt;                     // volumetric views: per pixel gathered rgb, transmittance
     bhr_body bodies[BHR_MAX_BODIES];  // the reference's BodyGpu array
 };
 
-cudaError_t launch_march_bodies(const BodyArgs& a, cudaStream_t st);
+// Thin or no disk: k_march_bodies<false>; the volumetric disk (view.disk_mode): <true>.
+cudaError_t launch_march_bodies(const BodyArgs& a, bool volumetric, cudaStream_t st);
 
 }  // namespace bhr

@@ -23,19 +23,17 @@ namespace {
 
 using shading::F3;
 
-constexpr int kMaxSubSamples = 64;  // inside the slab ds <= 6 diskStep: a finite segment needs <= 7
-
 __global__ void __launch_bounds__(256) k_march_vol(const __grid_constant__ VolArgs A) {
     __shared__ float4 s_lut[BHR_BLACKBODY_LUT];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int k = tid; k < BHR_BLACKBODY_LUT; k += 256) s_lut[k] = A.lut[k];
+    for (int k = tid; k < BHR_BLACKBODY_LUT; k += 256) s_lut[k] = A.look.lut[k];
     __syncthreads();
     const DevView& w = A.view;
     const int i = blockIdx.x * 32 + (warp & 3) * 8 + (lane & 7);
     const int j = blockIdx.y * 8 + (warp >> 2) * 4 + (lane >> 3);
     if (i >= w.width || j >= w.height) return;
     const Rule& R = A.rule;
-    const shading::Tex tx{A.noise8, s_lut, A.ln_1000, A.ln_40000};
+    const shading::Tex tx{A.look.noise8, s_lut, A.look.ln_1000, A.look.ln_40000};
     const RayInit<float> ri = setup_ray<float>(w, R, i, j);
     const int64_t k = int64_t(j) * w.width + i;
     bhr_hit* rec = w.out + k;
@@ -48,7 +46,7 @@ __global__ void __launch_bounds__(256) k_march_vol(const __grid_constant__ VolAr
     float trans = 1.0f;
     const bool lensing = R.lensing != 0;
     const float b_axis = ri.b_axis;
-    const shading::DiskConsts C = shading::disk_consts(A.p, w.rcam);
+    const shading::DiskConsts C = shading::disk_consts(A.look.p, w.rcam);
     if (R.far_mode) {
         status = BHR_STATUS_ESCAPED;
     } else {
@@ -105,27 +103,8 @@ __global__ void __launch_bounds__(256) k_march_vol(const __grid_constant__ VolAr
             steps += 1;
             if ((x.y > 0.f) != (x0.y > 0.f) && nplane < 255u) ++nplane;
             if (near_disk) {
-                // blackhole.frag:217-233: n samples along the cubic Hermite interpolant of the segment
                 const V3<float> dx{x.x - x0.x, x.y - x0.y, x.z - x0.z};
-                const float seg = sqrtf(dot3(dx, dx));
-                const float nf = ceilf(seg / w.disk_step);
-                const int n = isfinite(nf) ? min(max(1, int(fminf(nf, float(kMaxSubSamples)))), kMaxSubSamples) : 1;
-                const float sub = seg / float(n);
-                const V3<float> m0{dt * v0.x, dt * v0.y, dt * v0.z}, m1{dt * v.x, dt * v.y, dt * v.z};
-                for (int s = 0; s < n; ++s) {
-                    const float t = (float(s) + 0.5f) / float(n);
-                    const float t2 = t * t, t3 = t2 * t;
-                    const float h00 = 2.0f * t3 - 3.0f * t2 + 1.0f, h10 = t3 - 2.0f * t2 + t;
-                    const float h01 = -2.0f * t3 + 3.0f * t2, h11 = t3 - t2;
-                    const F3 p{h00 * x0.x + h10 * m0.x + h01 * x.x + h11 * m1.x,
-                               h00 * x0.y + h10 * m0.y + h01 * x.y + h11 * m1.y,
-                               h00 * x0.z + h10 * m0.z + h01 * x.z + h11 * m1.z};
-                    const float rm = sqrtf(p.x * p.x + p.z * p.z);
-                    if (rm > R.disk_inner - 0.5f && rm < R.disk_outer && fabsf(p.y) < R.slab * rm)
-                        shading::vol_disk_step(tx, A.p, C, R.disk_inner, R.disk_outer, A.thick, p, rm, sub, b_axis, col,
-                                               trans);
-                    if (trans < 0.004f) break;
-                }
+                vol_segment(tx, A.look, C, R, w.disk_step, b_axis, x0, v0, x, v, dt, sqrtf(dot3(dx, dx)), col, trans);
                 if (trans < 0.004f) {  // blackhole.frag:234
                     status = BHR_STATUS_OPAQUE;
                     break;

@@ -450,11 +450,22 @@ typedef struct bhr_body_hit {
  * body_dev width x height bhr_body_hit. Stream-ordered. */
 int bhr_trace_bodies(bhr_ctx* ctx, const bhr_view* view, const bhr_body* bodies, int nbodies, bhr_hit* hits_dev,
                      bhr_body_hit* body_dev, void* cuda_stream);
+/* The same with the volumetric disk (the reference's default disk with BHS_BODIES 1,
+ * blackhole.frag:101-121,146-150,169-190,217-250): the march of bhr_trace_volumetric with the body
+ * tests of bhr_trace_bodies, the disk sampled on each step before the ray can turn opaque
+ * (BHR_STATUS_OPAQUE) and before the step's chord meets a body, so a ray stopped by a body keeps
+ * the disk's light gathered in front of it. rgbt_dev gets width x height float4 (gathered rgb,
+ * transmittance); pass it to bhr_shade_bodies as rgba_dev, which shades it in place. The view
+ * must have disk_mode BHR_DISK_VOLUMETRIC; params is the disk's look. FP32. Stream-ordered. */
+int bhr_trace_bodies_volumetric(bhr_ctx* ctx, const bhr_view* view, const bhr_body* bodies, int nbodies,
+                                const bhr_shade_params* params, bhr_hit* hits_dev, bhr_body_hit* body_dev,
+                                float* rgbt_dev, void* cuda_stream);
 /* Shades one view marched by bhr_trace_bodies (bhr_shade plus blackhole.frag:255-296): the hit
  * body's surface (shadeBodySurface, bodies.glsl:224-292: nine planet looks, stars, an exploding
  * photosphere), a body turning transparent letting the ray on, the bodies along the straight
  * stretches before and after the march (with their rings), and the halos of the bodies the ray
- * just missed; then the sky. params->time is uTime. rgba_dev as bhr_shade's. */
+ * just missed; then the sky. params->time is uTime. rgba_dev as bhr_shade's: a volumetric view
+ * (marched by bhr_trace_bodies_volumetric) is shaded in place, rgba_dev holding its rgbt. */
 int bhr_shade_bodies(bhr_ctx* ctx, const bhr_view* view, const bhr_hit* hits_dev, const bhr_body_hit* body_dev,
                      const bhr_body* bodies, int nbodies, const bhr_shade_params* params, float* rgba_dev,
                      void* cuda_stream);

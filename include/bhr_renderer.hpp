@@ -284,7 +284,6 @@ public:
         bhr_hit* const outs[1] = {records_};
         const int nb = in.bodies ? int(in.bodies->size()) : 0;
         if (nb > 0) {  // the BHS_BODIES variant (Renderer.cpp:359-366)
-            if (v.disk_mode == BHR_DISK_VOLUMETRIC) return logError("render: bodies are marched with a thin disk or none", nullptr);
             if (n > body_capacity_) {
                 if (body_hits_) cudaFree(body_hits_);
                 body_hits_ = nullptr;
@@ -292,6 +291,14 @@ public:
                 if (cudaMalloc(&body_hits_, n * sizeof(bhr_body_hit)) != cudaSuccess)
                     return logError("render: cannot allocate the body records", nullptr);
                 body_capacity_ = n;
+            }
+            if (v.disk_mode == BHR_DISK_VOLUMETRIC) {  // the disk's light gathered into image()
+                bhr_shade_params p{};
+                if (!makeShadeParams(in, &p) || !ensureImage(n)) return logError("render: volumetric disk", nullptr);
+                if (bhr_trace_bodies_volumetric(ctx_, &v, in.bodies->data(), nb, &p, records_, body_hits_, image_,
+                                                nullptr) != BHR_OK)
+                    return logError("render", ctx_);
+                return true;
             }
             if (bhr_trace_bodies(ctx_, &v, in.bodies->data(), nb, records_, body_hits_, nullptr) != BHR_OK)
                 return logError("render", ctx_);

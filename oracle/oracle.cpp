@@ -55,6 +55,56 @@ struct VolumeSampler {
     }
 };
 
+// The body-aware march of the listed pixels (idx = j * width + i; every pixel when idx is NULL)
+// with the disk sampler `vol` (NoVolume, or VolumeSampler for the volumetric disk, which also
+// fills rgbt[4k..4k+3] with the gathered colour and transmittance).
+template <class Vol>
+int trace_bodies_impl(const bhr_view* v, const bhr_body* bodies, int nb, const int64_t* idx, int64_t n, bhr_hit* out,
+                      bhr_body_hit* bout, const Vol& vol, float* rgbt, int nthreads, int fp64) {
+    const int64_t npix = static_cast<int64_t>(v->width) * v->height;
+    if (idx) {
+        for (int64_t k = 0; k < n; ++k)
+            if (idx[k] < 0 || idx[k] >= npix) return BHR_ERR_INVALID_ARG;
+    } else if (n != npix) {
+        return BHR_ERR_INVALID_ARG;
+    }
+    auto one = [&](auto R, int64_t k) {
+        using T = decltype(R.step_scale);
+        const int64_t px = idx ? idx[k] : k;
+        const int i = static_cast<int>(px % v->width), j = static_cast<int>(px / v->width);
+        const V3<T> cam{T(v->cam_pos[0]), T(v->cam_pos[1]), T(v->cam_pos[2])};
+        BodyMarch<T> bm;
+        bm.b = bodies;
+        bm.n = nb;
+        const Result<T> r = march(R, cam, primaryRay<T>(*v, i, j), vol, bm);
+        toHit(r, out + k);
+        bhr_body_hit& o = bout[k];
+        o = bhr_body_hit{};
+        // the loop-head near-field hit records only the body (blackhole.frag:147-149)
+        o.body = r.status == BHR_STATUS_BODY ? (bm.hit >= 0 ? bm.hit : bm.near_idx) : -1;
+        o.t = float(bm.hit_t);
+        o.ro[0] = float(bm.hit_ro.x), o.ro[1] = float(bm.hit_ro.y), o.ro[2] = float(bm.hit_ro.z);
+        o.rd[0] = float(bm.hit_rd.x), o.rd[1] = float(bm.hit_rd.y), o.rd[2] = float(bm.hit_rd.z);
+        o.x[0] = float(r.x.x), o.x[1] = float(r.x.y), o.x[2] = float(r.x.z);
+        o.near_mask = bm.near_mask;
+        o.near_idx = bm.near_idx;
+        o.near_t = float(bm.near_t);
+        o.travelled = float(bm.travelled);
+        if (rgbt) {
+            for (int c = 0; c < 3; ++c) rgbt[4 * k + c] = r.col[c];
+            rgbt[4 * k + 3] = r.trans;
+        }
+    };
+    if (fp64) {
+        const Rule<double> R = Rule<double>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
+    } else {
+        const Rule<float> R = Rule<float>::from_view(*v);
+        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
+    }
+    return BHR_OK;
+}
+
 template <class T>
 void trace_one(const bhr_view& w, const Rule<T>& R, int64_t idx, bhr_hit* out) {
     const int i = static_cast<int>(idx % w.width);
@@ -306,44 +356,7 @@ int oracle_trace_bodies_pixels(const bhr_view* v, const bhr_body* bodies, int nb
                                bhr_hit* out, bhr_body_hit* bout, int nthreads, int fp64) {
     if (!view_ok(v) || nb < 0 || nb > BHR_MAX_BODIES || (nb > 0 && !bodies) || !out || !bout || n < 0)
         return BHR_ERR_INVALID_ARG;
-    const int64_t npix = static_cast<int64_t>(v->width) * v->height;
-    if (idx) {
-        for (int64_t k = 0; k < n; ++k)
-            if (idx[k] < 0 || idx[k] >= npix) return BHR_ERR_INVALID_ARG;
-    } else if (n != npix) {
-        return BHR_ERR_INVALID_ARG;
-    }
-    auto one = [&](auto R, int64_t k) {
-        using T = decltype(R.step_scale);
-        const int64_t px = idx ? idx[k] : k;
-        const int i = static_cast<int>(px % v->width), j = static_cast<int>(px / v->width);
-        const V3<T> cam{T(v->cam_pos[0]), T(v->cam_pos[1]), T(v->cam_pos[2])};
-        BodyMarch<T> bm;
-        bm.b = bodies;
-        bm.n = nb;
-        const Result<T> r = march(R, cam, primaryRay<T>(*v, i, j), NoVolume{}, bm);
-        toHit(r, out + k);
-        bhr_body_hit& o = bout[k];
-        o = bhr_body_hit{};
-        // the loop-head near-field hit records only the body (blackhole.frag:147-149)
-        o.body = r.status == BHR_STATUS_BODY ? (bm.hit >= 0 ? bm.hit : bm.near_idx) : -1;
-        o.t = float(bm.hit_t);
-        o.ro[0] = float(bm.hit_ro.x), o.ro[1] = float(bm.hit_ro.y), o.ro[2] = float(bm.hit_ro.z);
-        o.rd[0] = float(bm.hit_rd.x), o.rd[1] = float(bm.hit_rd.y), o.rd[2] = float(bm.hit_rd.z);
-        o.x[0] = float(r.x.x), o.x[1] = float(r.x.y), o.x[2] = float(r.x.z);
-        o.near_mask = bm.near_mask;
-        o.near_idx = bm.near_idx;
-        o.near_t = float(bm.near_t);
-        o.travelled = float(bm.travelled);
-    };
-    if (fp64) {
-        const Rule<double> R = Rule<double>::from_view(*v);
-        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
-    } else {
-        const Rule<float> R = Rule<float>::from_view(*v);
-        parallel_for(n, nthreads, 64, [&](int64_t k) { one(R, k); });
-    }
-    return BHR_OK;
+    return trace_bodies_impl(v, bodies, nb, idx, n, out, bout, NoVolume{}, nullptr, nthreads, fp64);
 }
 
 int oracle_trace_bodies(const bhr_view* v, const bhr_body* bodies, int nb, bhr_hit* out, bhr_body_hit* bout,
@@ -351,6 +364,47 @@ int oracle_trace_bodies(const bhr_view* v, const bhr_body* bodies, int nb, bhr_h
     if (!view_ok(v)) return BHR_ERR_INVALID_ARG;
     return oracle_trace_bodies_pixels(v, bodies, nb, nullptr, static_cast<int64_t>(v->width) * v->height, out, bout,
                                       nthreads, fp64);
+}
+
+// The body-aware march with the volumetric disk (BHS_BODIES 1, DISK_VOLUMETRIC) of the listed
+// pixels (every pixel when idx is NULL): records, body records, and rgbt[4k..4k+3] = the colour
+// the march gathered and the transmittance left.
+int oracle_trace_bodies_volumetric_pixels(const bhr_view* v, const bhr_body* bodies, int nb, const bhr_shade_params* p,
+                                          const uint16_t* noise, const float* lut, const int64_t* idx, int64_t n,
+                                          bhr_hit* out, bhr_body_hit* bout, float* rgbt, int nthreads, int fp64) {
+    if (!v || v->width <= 0 || v->height <= 0 || v->max_steps < 0 || v->disk_mode != BHR_DISK_VOLUMETRIC || nb < 0 ||
+        nb > BHR_MAX_BODIES || (nb > 0 && !bodies) || !p || !noise || !lut || !out || !bout || !rgbt || n < 0)
+        return BHR_ERR_INVALID_ARG;
+    const oracle::shade::Tex tx{noise, lut};
+    const float cx = v->cam_pos[0], cy = v->cam_pos[1], cz = v->cam_pos[2];
+    const VolumeSampler vs{&tx, p, v->disk_inner, v->disk_outer, v->disk_thickness, std::sqrt(cx * cx + cy * cy + cz * cz)};
+    return trace_bodies_impl(v, bodies, nb, idx, n, out, bout, vs, rgbt, nthreads, fp64);
+}
+
+int oracle_trace_bodies_volumetric(const bhr_view* v, const bhr_body* bodies, int nb, const bhr_shade_params* p,
+                                   const uint16_t* noise, const float* lut, bhr_hit* out, bhr_body_hit* bout,
+                                   float* rgbt, int nthreads, int fp64) {
+    if (!v || v->width <= 0 || v->height <= 0) return BHR_ERR_INVALID_ARG;
+    return oracle_trace_bodies_volumetric_pixels(v, bodies, nb, p, noise, lut, nullptr,
+                                                 static_cast<int64_t>(v->width) * v->height, out, bout, rgbt, nthreads,
+                                                 fp64);
+}
+
+// Shades a view marched with bodies and the volumetric disk: records, body records, the bodies
+// and the march's rgbt.
+int oracle_shade_bodies_volumetric(const bhr_view* v, const bhr_hit* hits, const bhr_body_hit* bh, const bhr_body* bodies,
+                                   int nb, const float* rgbt, const bhr_shade_params* p, const uint16_t* noise,
+                                   const float* lut, float* rgba, int nthreads) {
+    if (!v || !hits || !bh || (nb > 0 && !bodies) || nb < 0 || nb > BHR_MAX_BODIES || !rgbt || !p || !noise || !lut ||
+        !rgba || v->width <= 0 || v->height <= 0 || v->disk_mode != BHR_DISK_VOLUMETRIC)
+        return BHR_ERR_INVALID_ARG;
+    const oracle::shade::Tex tx{noise, lut};
+    const float cx = v->cam_pos[0], cy = v->cam_pos[1], cz = v->cam_pos[2];
+    const oracle::body::BodyPost post{&tx, bodies, nb, bh, v, std::sqrt(cx * cx + cy * cy + cz * cz),
+                                      2.0f * v->tan_half_fov / float(v->height), p->time};
+    parallel_for(v->height, nthreads, 1,
+                 [&](int64_t j) { oracle::shade::shade_view(tx, *p, *v, hits, rgba, j, j + 1, rgbt, post); });
+    return BHR_OK;
 }
 
 // Shades a view marched with bodies: its records, body records and the bodies.

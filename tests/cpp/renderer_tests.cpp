@@ -275,9 +275,23 @@ static int testGpu(const char* path, const char* surrogate_path) {
     const size_t mid = (in.windowH / 2) * size_t(in.windowW) + in.windowW / 2;
     std::snprintf(msg, sizeof msg, "%d pixels on the planet, the centre among them", onb);
     CHECK(onb > 50 && hb[mid].status == BHR_STATUS_BODY, msg);
+    // the same planet with the volumetric disk (the default disk): marched through the disk's
+    // volume, then shaded in place over the light the march gathered
     bhr::FrameInput ibv = ib;
     ibv.settings = &sv;
-    CHECK(!R.render(ibv) && !logged.empty(), "bodies with the volumetric disk are refused");
+    CHECK(R.renderImage(ibv), "renderImage with a body and the volumetric disk");
+    cudaMemcpy(hb.data(), R.hits(), n * sizeof(bhr_hit), cudaMemcpyDeviceToHost);
+    cudaMemcpy(bb.data(), R.bodyHits(), n * sizeof(bhr_body_hit), cudaMemcpyDeviceToHost);
+    std::vector<float> imb(n * 4);
+    cudaMemcpy(imb.data(), R.image(), imb.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    int onv = 0, litv = 0;
+    for (size_t k = 0; k < n; ++k) {
+        const bool on = hb[k].status == BHR_STATUS_BODY && bb[k].body == 0;
+        onv += on;
+        litv += on && imb[4 * k] + imb[4 * k + 1] + imb[4 * k + 2] > 0.0f && imb[4 * k + 3] == 0.0f;
+    }
+    std::snprintf(msg, sizeof msg, "volumetric disk: %d pixels on the planet, %d of them lit without sky", onv, litv);
+    CHECK(onv > 50 && hb[mid].status == BHR_STATUS_BODY && litv > onv / 2, msg);
     if (surrogate_path) {
         // the learned orbit surrogate under the shader's own rule (the default termMode), thin disk
         bhr::Settings ss;

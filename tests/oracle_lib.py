@@ -64,6 +64,16 @@ def lib():
         L.oracle_shade_bodies.argtypes = [VP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.POINTER(ShadeParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_int]
+        L.oracle_trace_bodies_volumetric.argtypes = [VP, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ShadeParams),
+                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.oracle_trace_bodies_volumetric_pixels.argtypes = [VP, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ShadeParams),
+                                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                            ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                                            ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.oracle_shade_bodies_volumetric.argtypes = [VP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                     ctypes.c_void_p, ctypes.POINTER(ShadeParams), ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.oracle_redshift_factor.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.oracle_redshift_factor.restype = ctypes.c_float
         L.oracle_blackbody_xyz.argtypes = [ctypes.c_double, D]
@@ -282,6 +292,52 @@ def trace_bodies_pixels(view: View, bodies, idx: np.ndarray, fp64: bool = True, 
                                           len(idx), hits.ctypes.data, bh.ctypes.data, threads or nthreads(), int(fp64))
     assert rc == 0
     return hits, bh
+
+
+def trace_bodies_volumetric(view: View, bodies, params: ShadeParams, noise: np.ndarray, lut: np.ndarray,
+                            fp64: bool = True, idx: np.ndarray | None = None, threads: int | None = None):
+    """The body-aware march with the volumetric disk, of every pixel or of the listed ones
+    (j * width + i): (records, body records, rgbt (n, 4))."""
+    n = len(bodies)
+    arr = (Body * max(n, 1))(*bodies)
+    m = view.width * view.height if idx is None else len(idx)
+    hits = np.zeros(m, dtype=HIT_DTYPE)
+    bh = np.zeros(m, dtype=BODY_HIT_DTYPE)
+    rgbt = np.zeros((m, 4), dtype=np.float32)
+    noise = np.ascontiguousarray(noise, dtype=np.uint16)
+    lut = np.ascontiguousarray(lut, dtype=np.float32)
+    if idx is None:
+        rc = lib().oracle_trace_bodies_volumetric(ctypes.byref(view), ctypes.cast(arr, ctypes.c_void_p), n,
+                                                  ctypes.byref(params), noise.ctypes.data, lut.ctypes.data,
+                                                  hits.ctypes.data, bh.ctypes.data, rgbt.ctypes.data,
+                                                  threads or nthreads(), int(fp64))
+    else:
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        rc = lib().oracle_trace_bodies_volumetric_pixels(ctypes.byref(view), ctypes.cast(arr, ctypes.c_void_p), n,
+                                                         ctypes.byref(params), noise.ctypes.data, lut.ctypes.data,
+                                                         idx.ctypes.data, len(idx), hits.ctypes.data, bh.ctypes.data,
+                                                         rgbt.ctypes.data, threads or nthreads(), int(fp64))
+    assert rc == 0
+    return hits, bh, rgbt
+
+
+def shade_bodies_volumetric(view: View, hits: np.ndarray, body_hits: np.ndarray, bodies, rgbt: np.ndarray,
+                            params: ShadeParams, noise: np.ndarray, lut: np.ndarray,
+                            threads: int | None = None) -> np.ndarray:
+    """Shades a view marched with bodies and the volumetric disk; (height, width, 4) float32."""
+    n = len(bodies)
+    arr = (Body * max(n, 1))(*bodies)
+    hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    body_hits = np.ascontiguousarray(body_hits, dtype=BODY_HIT_DTYPE)
+    rgbt = np.ascontiguousarray(rgbt, dtype=np.float32)
+    out = np.zeros((view.height, view.width, 4), dtype=np.float32)
+    rc = lib().oracle_shade_bodies_volumetric(ctypes.byref(view), hits.ctypes.data, body_hits.ctypes.data,
+                                              ctypes.cast(arr, ctypes.c_void_p), n, rgbt.ctypes.data,
+                                              ctypes.byref(params), np.ascontiguousarray(noise, dtype=np.uint16).ctypes.data,
+                                              np.ascontiguousarray(lut, dtype=np.float32).ctypes.data, out.ctypes.data,
+                                              threads or nthreads())
+    assert rc == 0
+    return out
 
 
 def shade_bodies(view: View, hits: np.ndarray, body_hits: np.ndarray, bodies, params: ShadeParams, noise: np.ndarray,

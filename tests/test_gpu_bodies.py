@@ -126,3 +126,104 @@ def test_body_shading_matches_the_oracle(tracer):
     assert np.all(np.isfinite(img))
     assert bad.mean() <= 2e-3 and bad[on].mean() <= 2e-3
     assert d.max() <= 1e-3 * max(1.0, float(np.abs(ref).max()))
+
+
+def _vol_scene():
+    """The volumetric disk with the planet below the disk plane (tests/test_cpu_bodies_volumetric)
+    and the near-field, far-side and side bodies of the thin-disk cases."""
+    from test_cpu_bodies_volumetric import scene
+
+    v, below = scene(192, 108)
+    return v, below + _scene(v)
+
+
+@pytest.mark.parametrize("density", [1.0, 6.0])
+def test_volumetric_body_march_matches_the_oracle(tracer, density):
+    import torch
+
+    from blackholerender_gb300 import STATUS_OPAQUE, shade_params
+
+    v, bodies = _vol_scene()
+    p = shade_params(disk_density=density)
+    h, bhd, rgbt = tracer.trace_bodies_volumetric(v, bodies, p)
+    noise = tracer.noise_bake(7)
+    torch.cuda.synchronize()
+    g = hits_numpy(h.cpu())
+    gb = bhd.cpu().numpy().view(np.uint8).reshape(-1).view(BODY_HIT_DTYPE)
+    gc = rgbt.cpu().numpy().reshape(-1, 4)
+    tex = (noise.cpu().numpy().view(np.uint16), O.blackbody_lut())
+    r64, b64, c64 = O.trace_bodies_volumetric(v, bodies, p, *tex, fp64=True)
+    r32, b32, c32 = O.trace_bodies_volumetric(v, bodies, p, *tex, fp64=False)
+    T = c64[:, 3]
+    # ill-conditioned: the photon-sphere band, a budget decided on the last steps, a transmittance
+    # within a factor 2 of the opacity threshold
+    amb = ((np.abs(r64["b"] - SQRT27) < 1e-2) | (np.abs(r64["steps"].astype(int) - v.max_steps) <= 2)
+           | ((T > 0.002) & (T < 0.008)))
+    mism = ((g["status"] != r64["status"]) | (gb["body"] != b64["body"])) & ~amb
+    mism32 = ((r32["status"] != r64["status"]) | (b32["body"] != b64["body"])) & ~amb
+    same = (g["status"] == r64["status"]) & (gb["body"] == b64["body"]) & ~amb
+    e = (np.abs(gc - c64) / (np.abs(c64) + 1e-3))[same]
+    same32 = same & (r32["status"] == r64["status"]) & (b32["body"] == b64["body"])
+    e32 = (np.abs(c32 - c64) / (np.abs(c64) + 1e-3))[same32]
+    hit = same & (g["status"] == STATUS_BODY)
+    print(f"\nvolumetric + bodies, density {density}: body hits {int(hit.sum())} (through the slab "
+          f"{int((hit & (T < 0.99)).sum())}), opaque {int((r64['status'] == STATUS_OPAQUE).sum())}, status/body "
+          f"mismatches {int(mism.sum())} (FP32 restatement {int(mism32.sum())}); |d rgbt|/(|ref|+1e-3) p99 "
+          f"{np.percentile(e, 99):.1e} (FP32 restatement {np.percentile(e32, 99):.1e})")
+    assert hit.sum() > 100 and (hit & (T < 0.99)).sum() > 50
+    assert mism.sum() <= max(3, 3 * mism32.sum())
+    assert np.percentile(e, 99) <= max(2e-3, 3 * np.percentile(e32, 99))
+    assert np.all(gb["near_mask"] == b64["near_mask"])
+    esc = same & (g["status"] == 1) & (r32["status"] == 1)
+    ang = O.angle(g["dir"][esc], r64["dir"][esc])
+    ang32 = O.angle(r32["dir"][esc], r64["dir"][esc])
+    assert np.percentile(ang, 99) <= max(2e-5, 3 * np.percentile(ang32, 99))
+
+
+def test_volumetric_body_shading_in_place(tracer):
+    import torch
+
+    from blackholerender_gb300 import shade_params
+
+    v, bodies = _vol_scene()
+    p = shade_params(time=21.0, doppler_strength=0.5)
+    h, bhd, rgbt = tracer.trace_bodies_volumetric(v, bodies, p)
+    noise = tracer.noise_bake(7)
+    torch.cuda.synchronize()
+    g = hits_numpy(h.cpu()).copy()
+    gb = bhd.cpu().numpy().view(np.uint8).reshape(-1).view(BODY_HIT_DTYPE).copy()
+    march = rgbt.cpu().numpy().copy()
+    img = tracer.shade_bodies(v, h, bhd, bodies, p, out=rgbt)  # in place
+    torch.cuda.synchronize()
+    img = img.cpu().numpy()
+    ref = O.shade_bodies_volumetric(v, g, gb, bodies, march.reshape(-1, 4), p, noise.cpu().numpy().view(np.uint16),
+                                    O.blackbody_lut())
+    on = g["status"] == STATUS_BODY
+    d = np.abs(img - ref)
+    bad = np.any(d > 1e-4 * np.abs(ref) + 1e-6, axis=-1).reshape(-1)
+    print(f"\nvolumetric body shading 192x108: body pixels {int(on.sum())}; outside 1e-4: {int(bad.sum())} "
+          f"({int(bad[on].sum())} on bodies), max |d| {d.max():.2e}")
+    assert on.sum() > 100 and np.all(np.isfinite(img))
+    assert bad.mean() <= 2e-3 and bad[on].mean() <= 2e-3
+    assert d.max() <= 1e-3 * max(1.0, float(np.abs(ref).max()))
+    # the disk's light in front of a body is kept
+    assert np.all(img.reshape(-1, 4)[on, :3] >= march.reshape(-1, 4)[on, :3] - 1e-6)
+
+
+def test_volumetric_body_march_argument_errors(tracer):
+    from blackholerender_gb300 import shade_params
+
+    v, bodies = _vol_scene()
+    thin = v.copy()
+    thin.disk_mode = DISK_THIN
+    with pytest.raises(BhrError) as e:
+        tracer.trace_bodies_volumetric(thin, bodies, shade_params())
+    assert e.value.code == -1
+    with pytest.raises(BhrError) as e:  # the thin-disk entry point points to this one
+        tracer.trace_bodies(v, bodies)
+    assert e.value.code == -5 and "bhr_trace_bodies_volumetric" in str(e.value)
+    flat = v.copy()
+    flat.disk_thickness = 0.0
+    with pytest.raises(BhrError) as e:
+        tracer.trace_bodies_volumetric(flat, bodies, shade_params())
+    assert e.value.code == -1
