@@ -1220,14 +1220,26 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
             j += ((j + 1) * w.width <= ray) ? 1 : 0;
             j = valid ? j : 0;
             const int i = valid ? ray - j * w.width : 0;
-            // the pixel's direction (as the plain march's setup), its angle from the radial
-            // direction e1 and b = r sin(angle) / sqrt(1 - 2 / r): the reference's h / |v_inf| for
-            // the initial velocity of geodesic.glsl:27-34 (whose radial part the lapse scales),
-            // without forming that velocity; its tangential part, and so the orbital plane, is d's
-            const V3<float> d = pixel_dir<float>(w, i, j);
+            // the pixel's direction, its angle from the radial direction e1 and b = r sin(angle) /
+            // sqrt(1 - 2 / r): the reference's h / |v_inf| for the initial velocity of
+            // geodesic.glsl:27-34 (whose radial part the lapse scales), without forming that
+            // velocity; its tangential part, and so the orbital plane, is d's. The direction of
+            // blackhole.frag:68-72 is the camera basis times (cx, cy, -1), normalised, with cx and
+            // cy affine in the pixel: one normalisation of an affine map of (i, j) about the
+            // image's centre (within 1.3e-7 rad of the FP64 direction at 1080p; the shader's two
+            // divisions and two normalisations were 5% of the step)
+            V3<float> d;
+            {
+                const float fi = float(i - sv.i_mid), fj = float(j - sv.j_mid);
+                d = {fmaf(fi, sv.dir_i[0], fmaf(fj, sv.dir_j[0], sv.dir_0[0])),
+                     fmaf(fi, sv.dir_i[1], fmaf(fj, sv.dir_j[1], sv.dir_0[1])),
+                     fmaf(fi, sv.dir_i[2], fmaf(fj, sv.dir_j[2], sv.dir_0[2]))};
+                const float dn = rsqrtf(dot3(d, d));
+                d = {d.x * dn, d.y * dn, d.z * dn};
+            }
             const V3<float> e1{w.rhat[0], w.rhat[1], w.rhat[2]};
             const V3<float> cx{e1.y * d.z - e1.z * d.y, e1.z * d.x - e1.x * d.z, e1.x * d.y - e1.y * d.x};
-            float b = sv.b_scale * sqrtf(dot3(cx, cx));
+            float b = sv.b_scale * orbit::FM<float>::sqrt(dot3(cx, cx));
             float beta = b * (1.0f / kSqrt27f) - 1.0f;
             if (sur && fabsf(beta) < 0.02f) {  // near the photon sphere: impact parameter in FP64
                 const double bd = impact_parameter_fp64(w, sv.fc, i, j);
@@ -1277,7 +1289,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
                 const float4 rg = __ldg(E + kExitRange + m);
                 psi = cubic(__ldg(E + (br ? kExitPsiB : kExitPsi) + jc), L);
                 phi0 = cubic(__ldg(E + (br ? kExitPhi0B : kExitPhi0) + jc), L);
-                minr = 1.0f / u2;
+                minr = orbit::FM<float>::rcp(u2);
                 Ic = cubic(ei, L);
                 if (thin) {
                     Ilo = fmaf(t, rg.z - rg.x, rg.x);
@@ -1370,7 +1382,8 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
                 us = u;
                 if (kNet) {  // the network's residual from the view's crossing table, applied along the orbit
                     const float sg =
-                        leg ? sqrtf(fmaxf((Rt.u2 - u) / Rt.u2, 0.f)) : -sqrtf(fmaxf((Rt.u2 - u) / (Rt.u2 - uc), 0.f));
+                        leg ? orbit::FM<float>::sqrt(fmaxf((Rt.u2 - u) * orbit::FM<float>::rcp(Rt.u2), 0.f))
+                            : -orbit::FM<float>::sqrt(fmaxf((Rt.u2 - u) * orbit::FM<float>::rcp(Rt.u2 - uc), 0.f));
                     const float dphi = cross_from_table(sv, G.x2[own], sg) * nm.y_scale;
                     const float sPu = orbit::dudphi<float>(u, Rt);
                     us = leg ? u + dphi * sPu : u - dphi * sPu;
@@ -1379,7 +1392,7 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
                 us = cap_invert(G.s0[own], G.s1[own], G.s2[own], G.s3[own], G.b[own], Ic, phk, uc, R.capture_r,
                                 R.disk_inner, R.disk_outer);
             }
-            const float rs = 1.0f / us;
+            const float rs = orbit::FM<float>::rcp(us);
             float rr = -1.f, ph = 0.f;
             if (rs >= R.disk_inner && rs <= R.disk_outer) {
                 float s2, c2;

@@ -112,6 +112,11 @@ struct SurrView {
     const float4* cross_table;  // [kCrossCells] y at the cell's corners (i, j), (i, j+1), (i+1, j), (i+1, j+1)
     float cx_h, cx_inv_h;       // the cross table's x2 spacing (first point tab_lo[1]) and its inverse
     float b_scale;          // r_cam / sqrt(1 - 2 / r_cam): b = b_scale sin(angle from the radial direction)
+    // the pixel direction of blackhole.frag:68-72 before its normalisation, an affine function
+    // of the pixel: (i - i_mid) dir_i + (j - j_mid) dir_j + dir_0 (from the image's centre, so
+    // that the terms stay near unit size)
+    float dir_i[3], dir_j[3], dir_0[3];
+    int32_t i_mid, j_mid;
     Fp64Cam fc;             // the FP64 impact parameter near the photon sphere
     // the rays of the view's photon-sphere band that the band march takes (bit ray % 32 of word
     // ray / 32; they are skipped here), or nullptr when no band march runs

@@ -575,6 +575,20 @@ int surrogate_trace_lane(bhr_surrogate* s, const bhr_view* views, int nviews, bh
             fc.rhat_d[2] = cz / rc;
             fc.b_scale_d = rc / std::sqrt(std::max(1.0 - 2.0 / rc, 1e-300));
             sv.b_scale = float(fc.b_scale_d);
+            // the pixel direction before normalisation, B (cx, cy, -1) with cx, cy affine in the
+            // pixel (blackhole.frag:68-72), about the image's centre
+            const bhr::DevView& dv = sv.view;
+            const double th = double(dv.tan_half), asp = double(dv.aspect);
+            sv.i_mid = views[k].width / 2;
+            sv.j_mid = views[k].height / 2;
+            const double sx = fc.inv_w2 * th * asp, sy = fc.inv_h2 * th;
+            const double cx0 = ((double(sv.i_mid) + 0.5 + double(dv.jitter[0])) * fc.inv_w2 - 1.0) * th * asp;
+            const double cy0 = ((double(sv.j_mid) + 0.5 + double(dv.jitter[1])) * fc.inv_h2 - 1.0) * th;
+            for (int c = 0; c < 3; ++c) {
+                sv.dir_i[c] = float(double(dv.basis[c]) * sx);
+                sv.dir_j[c] = float(double(dv.basis[3 + c]) * sy);
+                sv.dir_0[c] = float(double(dv.basis[c]) * cx0 + double(dv.basis[3 + c]) * cy0 - double(dv.basis[6 + c]));
+            }
             // the camera's tangential ray has b = b_scale_d
             const double beta_t = fc.b_scale_d / 5.196152422706632 - 1.0;
             const double x2_t = std::log1p(beta_t / double(s->norm.t_eps)) * double(s->norm.t_scale);
