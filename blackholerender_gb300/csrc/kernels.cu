@@ -568,8 +568,8 @@ cudaError_t launch_march_multi_list(const ViewBatch& b, const Scratch& s, const 
     int chunk = c.chunk, refill = c.refill;
     if (c.block != 64 && c.block != 512) return cudaErrorInvalidValue;
     const void* fn = c.block == 64 ? multi_list_kernel<64>(c.variant) : multi_list_kernel<512>(c.variant);
-    if (c.block == 64) {  // the band march, beside the surrogate pass
-        const cudaError_t e = prefer_max_smem(fn, 0, true);
+    if (c.block == 64) {  // the band march, beside the surrogate pass (the driver's carveout, as the pass's)
+        const cudaError_t e = prefer_max_smem(fn, 0, false);
         if (e != cudaSuccess) return e;
     }
     void* args[] = {(void*)&b, (void*)&s, (void*)&list, (void*)&qv, &chunk, &refill};

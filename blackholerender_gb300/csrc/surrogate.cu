@@ -1488,7 +1488,10 @@ cudaError_t launch_surrogate_trace(const SurrView& sv, WorkQueue* q, int* fb_lis
     using K = void (*)(SurrView, WorkQueue*, int*);
     const K kern = tol ? (net ? K(k_surrogate<true, true>) : K(k_surrogate<true, false>))
                        : (net ? K(k_surrogate<false, true>) : K(k_surrogate<false, false>));
-    const cudaError_t e = prefer_max_smem((const void*)kern, smem, true);
+    // the driver's own split of the SM's memory: the blocks need at most 90 KB of shared memory, and
+    // the rest serves as L1 for the views' tables (the largest carveout left 28 KB of L1, a 20%
+    // hit rate on the table loads, and was 2% slower)
+    const cudaError_t e = prefer_max_smem((const void*)kern, smem, false);
     if (e != cudaSuccess) return e;
     kern<<<grid, 32 * kInferWarps, smem, st>>>(sv, q, fb_list);
     return cudaGetLastError();
