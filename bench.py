@@ -486,7 +486,8 @@ def run_gpu(args):
     # ---- end to end through the host-buffer entry point (records in pinned host memory)
     host = [torch.empty(v.rays * HIT_BYTES, dtype=torch.uint8, pin_memory=True) for v in views]
     host_np = [h.numpy() for h in host]
-    sur.trace_host(views, host_np)
+    for _ in range(max(args.warmup, 3)):  # warm-up steps, as for the device-timed paths
+        sur.trace_host(views, host_np)
     e2e_steps = max(3, min(args.steps, 10))
     if dist:
         dist.barrier()
