@@ -29,6 +29,10 @@ constexpr int kB3 = kW3 + kH * kH;   // [64]
 constexpr int kW4 = kB3 + kH;        // [2][64]
 constexpr int kB4 = kW4 + kOut * kH; // [2]
 constexpr int kNParams = kB4 + kOut; // 8706
+// training gradients: each warp adds its tile's gradients into copy (warp % kGradCopies) of the
+// buffer, which spreads the global atomics over as many addresses; Adam sums the copies and
+// zeroes them for the next step
+constexpr int kGradCopies = 32;
 
 // Input normalisation and the trained range (stored with the weights).
 struct Norm {
@@ -51,7 +55,7 @@ cudaError_t launch_orbit_data(uint64_t seed, int64_t n_orbits, int k_per_orbit, 
 cudaError_t launch_train_step(const float* params, const TrainSample* X, const int8_t* lab, int64_t n_samples,
                               const int64_t* idx, int batch, uint64_t seed, float w_u, float w_c, float* grads,
                               float* loss, int grid, cudaStream_t st);
-cudaError_t launch_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
+cudaError_t launch_adam(float* params, float* grads, float* m, float* v, int step, float lr, float beta1,
                         float beta2, float eps, cudaStream_t st);
 // wait_cycles <= 0: the default completion-wait limit; withhold: the timeout self-test
 cudaError_t launch_mlp_infer(const float* params, const float4* q, float2* out, int n, int* status, int grid,

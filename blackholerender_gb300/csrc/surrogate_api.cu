@@ -190,7 +190,7 @@ int bhr_surrogate_create(bhr_surrogate** out, int device, const bhr_surrogate_co
     std::vector<float> P;
     init_params(P, seed);
     cudaError_t e = cudaMalloc(&s->params, sizeof(float) * kNParams);
-    if (e == cudaSuccess) e = cudaMalloc(&s->grads, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMalloc(&s->grads, sizeof(float) * kNParams * bhr::surr::kGradCopies);
     if (e == cudaSuccess) e = cudaMalloc(&s->adam_m, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMalloc(&s->adam_v, sizeof(float) * kNParams);
     if (e == cudaSuccess) e = cudaMalloc(&s->stats, sizeof(unsigned long long) * 4);
@@ -284,7 +284,8 @@ int bhr_surrogate_train(bhr_surrogate* s, int steps, int batch, float lr_max, fl
     for (int k = 0; e == cudaSuccess && k < steps; ++k) {
         const double frac = steps > 1 ? double(k) / double(steps - 1) : 1.0;
         const float lr = float(lr_min + 0.5 * (lr_max - lr_min) * (1.0 + std::cos(3.141592653589793 * frac)));
-        e = cudaMemsetAsync(s->grads, 0, sizeof(float) * kNParams, st);
+        // the gradient copies are zeroed here once; each Adam step zeroes them after reading
+        if (k == 0) e = cudaMemsetAsync(s->grads, 0, sizeof(float) * kNParams * bhr::surr::kGradCopies, st);
         if (e == cudaSuccess)
             e = bhr::surr::launch_train_step(s->params, s->X, s->lab, s->n_samples, nullptr, batch,
                                              seed + 0x632BE59BD9B4E019ull * uint64_t(s->adam_step + 1), 1.0f,
@@ -347,16 +348,23 @@ int bhr_surrogate_gradients(bhr_surrogate* s, const float* samples, const int8_t
     cudaError_t e = cudaMalloc(&X, sizeof(bhr::surr::TrainSample) * size_t(n));
     if (e == cudaSuccess) e = cudaMalloc(&L, size_t(n));
     if (e == cudaSuccess) e = cudaMalloc(&idx, sizeof(int64_t) * size_t(n));
-    if (e == cudaSuccess) e = cudaMalloc(&G, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMalloc(&G, sizeof(float) * kNParams * bhr::surr::kGradCopies);
     if (e == cudaSuccess) e = cudaMalloc(&loss, sizeof(float) * 3);
     if (e == cudaSuccess) e = cudaMemcpy(X, samples, sizeof(bhr::surr::TrainSample) * size_t(n), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(L, labels, size_t(n), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(idx, hidx.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(G, 0, sizeof(float) * kNParams);
+    if (e == cudaSuccess) e = cudaMemset(G, 0, sizeof(float) * kNParams * bhr::surr::kGradCopies);
     if (e == cudaSuccess) e = cudaMemset(loss, 0, sizeof(float) * 3);
     if (e == cudaSuccess)
         e = bhr::surr::launch_train_step(s->params, X, L, n, idx, n, 0, 1.0f, w_capture, G, loss, s->sms, nullptr);
-    if (e == cudaSuccess) e = cudaMemcpy(grad_out, G, sizeof(float) * kNParams, cudaMemcpyDeviceToHost);
+    std::vector<float> hg(size_t(kNParams) * bhr::surr::kGradCopies);
+    if (e == cudaSuccess) e = cudaMemcpy(hg.data(), G, sizeof(float) * hg.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        for (int k = 0; k < kNParams; ++k) {
+            float acc = 0.f;
+            for (int r = 0; r < bhr::surr::kGradCopies; ++r) acc += hg[size_t(r) * kNParams + k];
+            grad_out[k] = acc;
+        }
     float hl[3] = {0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpy(hl, loss, sizeof hl, cudaMemcpyDeviceToHost);
     for (void* p : {(void*)X, (void*)L, (void*)idx, (void*)G, (void*)loss})
