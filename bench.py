@@ -815,17 +815,23 @@ def run_vol_workload(args):
 
 
 def run_bodies_workload(args):
-    """--workload bodies: the BHS_BODIES variant on the 16 poses at 1920x1080, 450 steps, thin disk,
-    twelve bodies in front of every camera (workloads.body_gallery). Each step marches the 16
-    views with their bodies (bhr_trace_bodies) and shades them (bhr_shade_bodies). One JSON line,
-    not the headline."""
+    """--workload bodies: the BHS_BODIES variant on the 16 poses at 1920x1080, 450 steps, twelve
+    bodies in front of every camera (workloads.body_gallery), thin disk (--disk volumetric: the
+    reference's default disk). Each step marches the 16 views with their bodies
+    (bhr_trace_bodies, or bhr_trace_bodies_volumetric into the image's rgbt) and shades them
+    (bhr_shade_bodies). One JSON line, not the headline."""
     import torch
 
-    from blackholerender_gb300 import HIT_BYTES, STATUS_BODY, TERM_CONFIG, Tracer, hits_numpy, shade_params, workloads
+    from blackholerender_gb300 import (DISK_VOLUMETRIC, HIT_BYTES, STATUS_BODY, TERM_CONFIG, Tracer, hits_numpy,
+                                       shade_params, workloads)
 
     dev = torch.device("cuda", 0)
     tr = Tracer(0)
     views = workloads.c2_views(TERM_CONFIG)[: args.views]
+    vol = args.disk == "volumetric"
+    if vol:
+        for v in views:
+            v.disk_mode = DISK_VOLUMETRIC
     scenes = [workloads.body_gallery(v) for v in views]
     rays = sum(v.rays for v in views)
     p = shade_params(time=10.0)
@@ -835,8 +841,11 @@ def run_bodies_workload(args):
     st = torch.cuda.current_stream(dev)
 
     def step():
-        for v, b, h, q in zip(views, scenes, hits, bh):
-            tr.trace_bodies(v, b, h, q, st)
+        for v, b, h, q, o in zip(views, scenes, hits, bh, img):
+            if vol:  # the march gathers the disk's light into the image, which the shading completes
+                tr.trace_bodies_volumetric(v, b, p, h, q, o, st)
+            else:
+                tr.trace_bodies(v, b, h, q, st)
         mid = torch.cuda.Event(enable_timing=True)
         mid.record(st)
         for v, b, h, q, o in zip(views, scenes, hits, bh, img):
@@ -864,7 +873,7 @@ def run_bodies_workload(args):
     line = {"metric": "Mrays/s (bodies: march + shading)", "value": rays / (ms * 1e-3) / 1e6, "unit": "Mrays/s",
             "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{len(views)} poses (seed 0) x 1920x1080, FOV 60, 450 steps, thin disk, 12 bodies "
+            "config": {"workload": f"{len(views)} poses (seed 0) x 1920x1080, FOV 60, 450 steps, {args.disk} disk, 12 bodies "
                                    "per view (nine planet looks, a star, an exploding photosphere, a ringed translucent "
                                    "planet), time 10", "rays_per_step": rays, "body_pixel_fraction": on / rays,
                        "march_ms": ms_trace, "shade_ms": ms - ms_trace, "l2": "flushed (256 MiB write) between steps"},
@@ -886,6 +895,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--views", type=int, default=16, help="first N of the 16 poses (small profiling cases)")
+    ap.add_argument("--disk", default="thin", choices=["thin", "volumetric"], help="the bodies workload's disk")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "shade", "vol", "bodies"],
                     help="c2: the headline (16 poses at 1080p); c3 / c4: the other configurations; "
                          "shade: the records' shading consumer; vol: the volumetric disk march; "

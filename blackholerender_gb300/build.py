@@ -17,7 +17,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libbhr.so"
-SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu", "surrogate_api.cu", "lens.cu", "shade.cu", "vol.cu", "bodies.cu"]
+SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "surrogate.cu", "surrogate_api.cu", "lens.cu", "shade.cu", "vol.cu",
+           "bodies.cu", "bodies_vol.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -34,7 +35,7 @@ DEVICE_FLAGS = {"kernels.cu": ["-ftz=true"], "surrogate.cu": ["-ftz=true"], "len
                 # shading: IEEE +, -, *, / and sqrt without contraction, so that the noise volume
                 # and every non-transcendental step round as the CPU restatement does
                 "shade.cu": ["-fmad=false"], "vol.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
-                "bodies.cu": ["-ftz=true"]}
+                "bodies.cu": ["-ftz=true"], "bodies_vol.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]}
 
 
 def _flags() -> list[str]:

@@ -21,7 +21,8 @@ struct BodyArgs {
     bhr_body bodies[BHR_MAX_BODIES];  // the reference's BodyGpu array
 };
 
-// Thin or no disk: k_march_bodies<false>; the volumetric disk (view.disk_mode): <true>.
+// Thin or no disk: k_march_bodies<false> (bodies.cu); the volumetric disk: <true> (bodies_vol.cu).
 cudaError_t launch_march_bodies(const BodyArgs& a, bool volumetric, cudaStream_t st);
+cudaError_t launch_march_bodies_vol(const BodyArgs& a, cudaStream_t st);
 
 }  // namespace bhr
