@@ -739,7 +739,8 @@ struct RayStage {  // per warp, structure of arrays over its 32 rays
     float s0[32], s1[32], s2[32], s3[32];  // captured orbit: u1, A, k^2, K
     float ic[32];      // angle camera -> turning point (escaping), F(camera) (captured)
     float phin[32], x2[32], beta[32];
-    float e2x[32], e2z[32];
+    float nx[32], nz[32];  // the nodal line's direction in the disk plane (x, z; unnormalised): crossing k lies
+                           // at its end (-1)^k
     float b[32];
     uint32_t info[32];  // bits 0-1 candidates, 2 surrogate, 3-10 plane crossings, 11+5c candidate c (k | leg << 4),
                         // 26 captured orbit
@@ -1346,8 +1347,12 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
                 G.phin[lane] = phin;
                 G.x2[lane] = x2;
                 G.beta[lane] = beta;
-                G.e2x[lane] = e2.x;
-                G.e2z[lane] = e2.z;
+                // the crossings' direction from the hole: phi_k = phin + k pi gives cos(phi_k) e1 +
+                // sin(phi_k) e2 = (-1)^k n, n along (e2.y e1 - e1.y e2) with the sign that makes
+                // sin(phin) >= 0 (phin in [0, pi)); no trigonometry per crossing
+                const float sn = e1.y < 0.f ? 1.f : (e1.y > 0.f ? -1.f : (e2.y >= 0.f ? 1.f : -1.f));
+                G.nx[lane] = sn * (e2.y * e1.x - e1.y * e2.x);
+                G.nz[lane] = sn * (e2.y * e1.z - e1.y * e2.z);
                 G.b[lane] = b;
             }
             o_info = uint32_t(ncand) | (sur ? 4u : 0u) | (uint32_t(min(nplane, 255)) << 3) | cw | (cap ? kCapBit : 0u);
@@ -1401,11 +1406,8 @@ __global__ void __launch_bounds__(32 * kInferWarps, surr_blocks_per_sm(kNet)) k_
             const float rs = orbit::FM<float>::rcp(us);
             float rr = -1.f, ph = 0.f;
             if (rs >= R.disk_inner && rs <= R.disk_outer) {
-                float s2, c2;
-                sincos_rr(phk, &s2, &c2);
-                const float hx = rs * (c2 * w.rhat[0] + s2 * G.e2x[own]);
-                const float hz = rs * (c2 * w.rhat[2] + s2 * G.e2z[own]);
-                ph = orbit::atan2_fast(hz, hx);
+                const float sk = (kl & 1u) ? -1.f : 1.f;  // the nodal line's far end for odd k
+                ph = orbit::atan2_fast(sk * G.nz[own], sk * G.nx[own]);
                 rr = rs;
             }
             tu[t] = rr;
