@@ -20,10 +20,10 @@ def tex():
     return O.noise_bake(7), O.blackbody_lut()
 
 
-def scene(width=128, height=72):
+def scene(width=128, height=72, term=TERM_CONFIG):
     """A camera 30 M out, 30 degrees above the disk, and a planet of radius 2 below the disk
     plane at radius 8 on the camera's side: every ray to it crosses the disk's slab first."""
-    v = make_view(TERM_CONFIG, width=width, height=height, preset=0, pose=(30.0, math.radians(60.0), 0.4),
+    v = make_view(term, width=width, height=height, preset=0, pose=(30.0, math.radians(60.0), 0.4),
                   disk_mode=DISK_VOLUMETRIC)
     cam = np.array(v.cam_pos, dtype=np.float64)
     hor = np.array([cam[0], 0.0, cam[2]])

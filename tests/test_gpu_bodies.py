@@ -128,22 +128,23 @@ def test_body_shading_matches_the_oracle(tracer):
     assert d.max() <= 1e-3 * max(1.0, float(np.abs(ref).max()))
 
 
-def _vol_scene():
+def _vol_scene(term=TERM_CONFIG):
     """The volumetric disk with the planet below the disk plane (tests/test_cpu_bodies_volumetric)
     and the near-field, far-side and side bodies of the thin-disk cases."""
     from test_cpu_bodies_volumetric import scene
 
-    v, below = scene(192, 108)
+    v, below = scene(192, 108, term)
     return v, below + _scene(v)
 
 
-@pytest.mark.parametrize("density", [1.0, 6.0])
-def test_volumetric_body_march_matches_the_oracle(tracer, density):
+@pytest.mark.parametrize("density,term", [(1.0, TERM_CONFIG), (6.0, TERM_CONFIG), (2.0, TERM_SHADER)],
+                         ids=["density 1, CONFIG", "density 6, CONFIG", "density 2, shader rule"])
+def test_volumetric_body_march_matches_the_oracle(tracer, density, term):
     import torch
 
     from blackholerender_gb300 import STATUS_OPAQUE, shade_params
 
-    v, bodies = _vol_scene()
+    v, bodies = _vol_scene(term)
     p = shade_params(disk_density=density)
     h, bhd, rgbt = tracer.trace_bodies_volumetric(v, bodies, p)
     noise = tracer.noise_bake(7)
@@ -166,7 +167,7 @@ def test_volumetric_body_march_matches_the_oracle(tracer, density):
     same32 = same & (r32["status"] == r64["status"]) & (b32["body"] == b64["body"])
     e32 = (np.abs(c32 - c64) / (np.abs(c64) + 1e-3))[same32]
     hit = same & (g["status"] == STATUS_BODY)
-    print(f"\nvolumetric + bodies, density {density}: body hits {int(hit.sum())} (through the slab "
+    print(f"\nvolumetric + bodies, density {density}, rule {term}: body hits {int(hit.sum())} (through the slab "
           f"{int((hit & (T < 0.99)).sum())}), opaque {int((r64['status'] == STATUS_OPAQUE).sum())}, status/body "
           f"mismatches {int(mism.sum())} (FP32 restatement {int(mism32.sum())}); |d rgbt|/(|ref|+1e-3) p99 "
           f"{np.percentile(e, 99):.1e} (FP32 restatement {np.percentile(e32, 99):.1e})")
