@@ -415,8 +415,9 @@ def run_gpu(args):
     def step_surrogate():
         plan_s.launch(stream)
         # one table launch per 64 views (every view's exit and crossing tables), one pass per
-        # view, one fallback march for all views
-        return (len(views) + 63) // 64 + len(views) + 1
+        # view, one fallback march for all views, and the band search and band march (one launch
+        # each for up to 64 views that share one rule, as these do)
+        return (len(views) + 63) // 64 + len(views) + 1 + (2 if len(views) <= 64 else 0)
 
     def step_plain():
         plan_p.launch(stream)
