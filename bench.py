@@ -497,7 +497,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         sur.trace_host(views, host_np)
         e2e_each.append(time.perf_counter() - t0)
-    # the median step: single steps on the box have been seen stalled for tens of ms on the host
+    # the median step: single steps on a GB300 host have been seen stalled for tens of ms
     # (8 of 10 steps at 11.3 ms, one at 96 ms); the mean and every step are reported beside it
     e2e_s = statistics.median(e2e_each)
     e2e_mean = sum(e2e_each) / e2e_steps

@@ -1,6 +1,6 @@
 """Closed-form orbit pieces of the surrogate, restated in numpy FP64 -- TEST INFRASTRUCTURE ONLY.
 
-These are the checker's versions of blackholerender_gb300/csrc/surrogate_math.cuh. For a photon
+These are the oracle's versions of blackholerender_gb300/csrc/surrogate_math.cuh. For a photon
 in Schwarzschild (G = c = M = 1) with impact parameter b, u = 1/r obeys the first integral of
 the Binet equation u'' + u = 3u^2 (the orbit shape of x'' = -3 h^2 x / r^5,
 shaders/geodesic.glsl:3-5 and src/physics/Geodesic.h:4-6):
